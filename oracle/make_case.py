@@ -1,0 +1,160 @@
+"""Write a rising-bubble case directory in the reference's input formats.
+
+Test infrastructure: the case directories feed the reference-built oracle
+harness (oracle/_ref/euler_oracle) that generates the golden fixtures, and
+the product's own host driver reads the same files.  Formats follow the
+reference's examples: controls file with brace blocks (src/util/util.cpp:32-79),
+block-mesh description read by the mesh app (apps/mesh/meshApp.cpp), and
+field files with an `internal` initialiser plus per-boundary conditions
+(src/field/field.h:1409-1519).
+"""
+import argparse
+import os
+
+CONTROLS = """general
+{{
+    solver                       euler
+    mesh                         grid
+    P0                           100000
+    T0                           300
+    cp                           1004.5
+    cv                           717.5
+    state                        TRANSIENT
+    start_step                   0
+    end_step                     {end_step}
+    write_interval               {end_step}
+    dt                           {dt}
+    n_deferred                   0
+    convection_scheme            RUSANOV
+    time_scheme                  BDF1
+    print_time                   0
+    gravity   0 0 -9.81
+    npx       {npx}
+    npy       {npy}
+    npz       {npz}
+}}
+
+euler
+{{
+    diffusion                    NO
+    buoyancy                     YES
+}}
+"""
+
+GRID_2D = """8
+{{
+0 0 0
+{lx} 0 0
+{lx} 0 {lz}
+0 0 {lz}
+0 {ly} 0
+{lx} {ly} 0
+{lx} {ly} {lz}
+0 {ly} {lz}
+}}
+
+8{{0 1 5 4 3 2 6 7}} wall 3{{{nx} 1 {nz}}} 3{{1 1 1}}
+
+top     4{{3 2 6 7}}
+bottom  4{{0 1 5 4}}
+delete  4{{0 1 2 3}} 4{{4 5 6 7}}
+sides   4{{1 5 6 2}} 4{{0 4 7 3}}
+"""
+
+GRID_3D = """8
+{{
+0 0 0
+{lx} 0 0
+{lx} {ly} 0
+0 {ly} 0
+0 0 {lz}
+{lx} 0 {lz}
+{lx} {ly} {lz}
+0 {ly} {lz}
+}}
+
+8{{0 1 2 3 4 5 6 7}} wall 3{{{nx} {ny} {nz}}} 3{{1 1 1}}
+
+top     4{{4 5 6 7}}
+bottom  4{{0 1 2 3}}
+sides   4{{0 1 5 4}} 4{{3 2 6 7}} 4{{0 3 7 4}} 4{{1 2 6 5}}
+"""
+
+FIELD = """size {size}
+internal 1
+{{
+    {init}
+}}
+boundary 3
+{{
+    top {{
+        type {bc}
+    }}
+    bottom {{
+        type {bc}
+    }}
+    sides {{
+        type {bc}
+    }}
+}}
+"""
+
+
+def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius):
+    os.makedirs(out, exist_ok=True)
+    lx, ly, lz = length
+    nx, ny, nz = n
+    npy = 0 if dim == 2 else order
+    with open(os.path.join(out, "controls"), "w") as f:
+        f.write(CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order))
+    grid = GRID_2D if dim == 2 else GRID_3D
+    with open(os.path.join(out, "grid"), "w") as f:
+        f.write(grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz))
+    cx, cy, cz = center
+    rx, ry, rz = radius
+    cos_init = f"cosine 0 {amp}    {cx} {cy} {cz}   {rx} {ry} {rz}"
+    files = {
+        "T0.txt": (1, cos_init, "NEUMANN"),
+        "U0.txt": (3, "uniform 0 0 0", "SYMMETRY"),
+        "p0.txt": (1, "uniform 0", "NEUMANN"),
+        "rho0.txt": (1, "uniform 0", "NEUMANN"),
+    }
+    for name, (size, init, bc) in files.items():
+        with open(os.path.join(out, name), "w") as f:
+            f.write(FIELD.format(size=size, init=init, bc=bc))
+
+
+# Rising-bubble workloads (2D: one element thick in y, y faces deleted).
+CASES = {
+    # 1000 x 1000 m, 10x10 elements, N=4, theta' = 0.25(1+cos(pi r/250))
+    "c1_2d": dict(dim=2, n=(10, 1, 10), order=4, length=(1000, 100, 1000),
+                  amp=0.5, center=(500, 50, 350), radius=(250, 1000, 250)),
+    # 2000^3 m box, amplitude 0.5 K, radius 400 m, centre (1000,1000,600)
+    "c2_32": dict(dim=3, n=(32, 32, 32), order=4, length=(2000, 2000, 2000),
+                  amp=0.5, center=(1000, 1000, 600), radius=(400, 400, 400)),
+    "c3_16n7": dict(dim=3, n=(16, 16, 16), order=7, length=(2000, 2000, 2000),
+                    amp=0.5, center=(1000, 1000, 600), radius=(400, 400, 400)),
+    "c4_16": dict(dim=3, n=(16, 16, 16), order=4, length=(2000, 2000, 2000),
+                  amp=0.5, center=(1000, 1000, 600), radius=(400, 400, 400)),
+    # small 3D cases for golden fixtures (same bubble, coarser meshes)
+    "g3_2": dict(dim=3, n=(2, 2, 2), order=4, length=(2000, 2000, 2000),
+                 amp=0.5, center=(1000, 1000, 600), radius=(400, 400, 400)),
+    "g3_4n3": dict(dim=3, n=(4, 3, 2), order=3, length=(2000, 1500, 1000),
+                   amp=0.5, center=(1000, 750, 300), radius=(400, 400, 400)),
+    "g3_2n7": dict(dim=3, n=(2, 2, 2), order=7, length=(2000, 2000, 2000),
+                   amp=0.5, center=(1000, 1000, 600), radius=(400, 400, 400)),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=sorted(CASES))
+    ap.add_argument("out")
+    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--steps", type=int, default=10)
+    a = ap.parse_args()
+    write_case(a.out, dt=a.dt, steps=a.steps, **CASES[a.case])
+
+
+if __name__ == "__main__":
+    main()

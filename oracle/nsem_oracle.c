@@ -1,0 +1,396 @@
+/*
+ * CPU restatement of the reference's explicit dGSEM Euler right-hand side and
+ * of the coupled SSP-RK3 driver used as the parity oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY (see nsem_oracle.h).  Every operation is written
+ * in the order the reference evaluates it, so that with -ffp-contract=off the
+ * result is bit-identical to the reference library's on the same inputs:
+ *
+ *   tensor helpers       src/tensor/tensor.h:116-118 (right-nested Vector dot),
+ *                        src/tensor/tensor.cpp:15-27 (outer product), 72-78
+ *                        (Tensor.Vector), tensor.h:486-494 (sym)
+ *   boundary ghosts      src/field/field.h:2670-2685 (NEUMANN, SYMMETRY)
+ *   equation of state    apps/euler/euler.cpp:211-213
+ *   wave speed           apps/euler/euler.cpp:186, cds field.h:2881-2893
+ *   Rusanov flux         src/field/field.h:2928-2943
+ *   surface lift         src/field/field.h:3086-3117 (weak form)
+ *   volume term          src/field/field.h:3440-3464 with DPSI dg.h:67-75
+ *   gravity source       apps/euler/euler.cpp:224-234, src field.h:3712-3723
+ *   tendency             L = -Su/cV (forward-Euler update of solve.cpp:563-564
+ *                        written per unit time)
+ */
+#include "nsem_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
+
+static int g_pow_mode = 0;
+
+void nsem_oracle_set_pow(int which) { g_pow_mode = which; }
+
+int nsem_oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+static inline double eos_pow(double x, double y) {
+    return g_pow_mode ? nsem_oracle_pow_dd(x, y) : pow(x, y);
+}
+
+/* Vector dot, nested from the right as the reference's unrolled loop. */
+static inline double vdot(const double* a, const double* b) {
+    return a[0] * b[0] + (a[1] * b[1] + (a[2] * b[2] + 0.0));
+}
+static inline double vmag(const double* a) { return sqrt(vdot(a, a)); }
+
+/* Tensor . Vector, row by row, summed left to right. */
+static inline void tdot(const double* q, const double* p, double* r) {
+    r[0] = q[XX] * p[0] + q[XY] * p[1] + q[XZ] * p[2];
+    r[1] = q[YX] * p[0] + q[YY] * p[1] + q[YZ] * p[2];
+    r[2] = q[ZX] * p[0] + q[ZY] * p[1] + q[ZZ] * p[2];
+}
+
+/* Outer product p (x) q in XX,YY,ZZ,XY,YZ,XZ,YX,ZY,ZX order. */
+static inline void outer(const double* p, const double* q, double* r) {
+    r[XX] = p[0] * q[0];
+    r[YY] = p[1] * q[1];
+    r[ZZ] = p[2] * q[2];
+    r[XY] = p[0] * q[1];
+    r[YZ] = p[1] * q[2];
+    r[XZ] = p[0] * q[2];
+    r[YX] = p[1] * q[0];
+    r[ZY] = p[2] * q[1];
+    r[ZX] = p[2] * q[0];
+}
+
+/* Symmetry ghost velocity: tangential projection rescaled to |p|. */
+static inline void sym_vec(const double* p, const double* n, double* out) {
+    double mg = vmag(n);
+    double en[3] = {n[0] / mg, n[1] / mg, n[2] / mg};
+    /* A = I - en en^T (symmetric storage XX,YY,ZZ,XY,YZ,XZ) */
+    double A[6];
+    A[0] = 1.0 - en[0] * en[0];
+    A[1] = 1.0 - en[1] * en[1];
+    A[2] = 1.0 - en[2] * en[2];
+    A[3] = 0.0 - en[0] * en[1];
+    A[4] = 0.0 - en[1] * en[2];
+    A[5] = 0.0 - en[0] * en[2];
+    double r[3];
+    r[0] = A[0] * p[0] + A[3] * p[1] + A[5] * p[2];
+    r[1] = A[3] * p[0] + A[1] * p[1] + A[4] * p[2];
+    r[2] = A[5] * p[0] + A[4] * p[1] + A[2] * p[2];
+    double magR = vmag(r);
+    if (fabs(magR - 0.0) <= 1e-7) {
+        out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+        return;
+    }
+    double s = vmag(p) / magR;
+    out[0] = r[0] * s; out[1] = r[1] * s; out[2] = r[2] * s;
+}
+
+typedef struct {
+    double *rho, *U, *T, *p;    /* primitive fields on n_all (+pad) nodes */
+    double *d_rho, *d_mom, *d_th; /* per-slot lifted fluxes                */
+    double *r_rho, *r_mom, *r_th; /* residuals on n_all nodes              */
+} work_t;
+
+static void work_alloc(const nsem_oracle_mesh* m, work_t* w) {
+    size_t na = (size_t)m->n_all + (size_t)m->np;
+    size_t ns = (size_t)m->n_face * (size_t)m->npf;
+    w->rho = calloc(na, sizeof(double));
+    w->U = calloc(na * 3, sizeof(double));
+    w->T = calloc(na, sizeof(double));
+    w->p = calloc(na, sizeof(double));
+    w->d_rho = calloc(ns, sizeof(double));
+    w->d_mom = calloc(ns * 3, sizeof(double));
+    w->d_th = calloc(ns, sizeof(double));
+    w->r_rho = calloc(na, sizeof(double));
+    w->r_mom = calloc(na * 3, sizeof(double));
+    w->r_th = calloc(na, sizeof(double));
+}
+
+static void work_free(work_t* w) {
+    free(w->rho); free(w->U); free(w->T); free(w->p);
+    free(w->d_rho); free(w->d_mom); free(w->d_th);
+    free(w->r_rho); free(w->r_mom); free(w->r_th);
+}
+
+/* NEUMANN (value 0) ghost: interior value + 0*|dv| (field.h:2674-2676). */
+static inline double neumann(const nsem_oracle_mesh* m, const double* f, uint32_t c1,
+                             uint32_t c2) {
+    const double* a = m->cC + 3 * (size_t)c1;
+    const double* b = m->cC + 3 * (size_t)c2;
+    double dv[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    return f[c1] + 0.0 * vmag(dv);
+}
+
+static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t* w,
+                     double* p_out) {
+    const int32_t NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
+    const int64_t n_int = m->n_int, n_all = m->n_all;
+    const int64_t n_slot = (int64_t)m->n_face * NPF;
+    const double P0 = m->P0, R = m->R, gam = m->gamma;
+
+    /* primitive variables on interior nodes */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n_int; i++) {
+        double r = u[0][i];
+        w->rho[i] = r;
+        w->U[3 * i + 0] = u[1][i] / r;
+        w->U[3 * i + 1] = u[2][i] / r;
+        w->U[3 * i + 2] = u[3][i] / r;
+        w->T[i] = u[4][i] / r;
+    }
+    /* ghost values: rho, T Neumann; U symmetry */
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n_slot; k++) {
+        if (!m->bcU[k]) continue;
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c2 >= (uint32_t)n_all) continue;
+        w->rho[c2] = neumann(m, w->rho, c1, c2);
+        w->T[c2] = neumann(m, w->T, c1, c2);
+        if (m->bcU[k] == 2) {
+            sym_vec(w->U + 3 * (size_t)c1, m->fN + 3 * k, w->U + 3 * (size_t)c2);
+        } else {
+            for (int c = 0; c < 3; c++) {
+                const double* a = m->cC + 3 * (size_t)c1;
+                const double* b = m->cC + 3 * (size_t)c2;
+                double dv[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+                w->U[3 * (size_t)c2 + c] = w->U[3 * (size_t)c1 + c] + 0.0 * vmag(dv);
+            }
+        }
+    }
+    /* equation of state on every node, then Neumann ghosts, then p' */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n_all; i++)
+        w->p[i] = P0 * eos_pow(((w->rho[i] * w->T[i]) * R) / P0, gam);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n_slot; k++) {
+        if (!m->bcU[k]) continue;
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c2 >= (uint32_t)n_all) continue;
+        w->p[c2] = neumann(m, w->p, c1, c2);
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n_all; i++) w->p[i] -= m->p_ref[i];
+    if (p_out) memcpy(p_out, w->p, (size_t)n_all * sizeof(double));
+
+    const double gR = gam * R;
+    /* face slots: Rusanov fluxes of the three equations dotted with fN */
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n_slot; k++) {
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+        const double fi = m->fI[k], fo = 1 - fi;
+        const double* n = m->fN + 3 * k;
+        const double mgn = vmag(n);
+        const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+        const double *U1 = w->U + 3 * (size_t)c1, *U2 = w->U + 3 * (size_t)c2;
+        const double r1 = w->rho[c1], r2 = w->rho[c2];
+        const double T1 = w->T[c1], T2 = w->T[c2];
+        const double p1 = w->p[c1], p2 = w->p[c2];
+        double lam = ((vmag(U1) * fi + vmag(U2) * fo) +
+                      (sqrt(gR * T1) * fi + sqrt(gR * T2) * fo)) / 2;
+        /* rho: flux U*rho, state rho */
+        {
+            double F[3], jump = lam * (r2 - r1);
+            for (int c = 0; c < 3; c++) {
+                double a = U1[c] * r1, b = U2[c] * r2;
+                F[c] = (a * fi + b * fo) - en[c] * jump;
+            }
+            w->d_rho[k] = vdot(F, n);
+        }
+        /* momentum: flux (rho U) (x) U + p' I, state rho U */
+        {
+            double Fc1[3] = {U1[0] * r1, U1[1] * r1, U1[2] * r1};
+            double Fc2[3] = {U2[0] * r2, U2[1] * r2, U2[2] * r2};
+            double T1t[9], T2t[9], F[9], O[9];
+            outer(Fc1, U1, T1t);
+            outer(Fc2, U2, T2t);
+            for (int c = 0; c < 9; c++) {
+                double i1 = (c < 3) ? 1.0 : 0.0;
+                T1t[c] = T1t[c] + i1 * p1;
+                T2t[c] = T2t[c] + i1 * p2;
+            }
+            double dq[3];
+            for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
+            outer(en, dq, O);
+            for (int c = 0; c < 9; c++) F[c] = (T1t[c] * fi + T2t[c] * fo) - O[c];
+            tdot(F, n, w->d_mom + 3 * k);
+        }
+        /* rho theta: flux (rho U) theta, state rho theta */
+        {
+            double F[3], jump = lam * (r2 * T2 - r1 * T1);
+            for (int c = 0; c < 3; c++) {
+                double a = (U1[c] * r1) * T1, b = (U2[c] * r2) * T2;
+                F[c] = (a * fi + b * fo) - en[c] * jump;
+            }
+            w->d_th[k] = vdot(F, n);
+        }
+    }
+
+    /* surface lift (div_flux, weak form) then volume term, per element */
+    const int64_t n_elem = m->n_elem;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < n_elem; e++) {
+        const int64_t base = e * NP;
+        for (int32_t a = 0; a < NP; a++) {
+            w->r_rho[base + a] = 0.0;
+            w->r_th[base + a] = 0.0;
+            w->r_mom[3 * (base + a) + 0] = 0.0;
+            w->r_mom[3 * (base + a) + 1] = 0.0;
+            w->r_mom[3 * (base + a) + 2] = 0.0;
+        }
+        for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
+            for (int32_t nn = 0; nn < NPF; nn++) {
+                int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
+                uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                if (c1 >= base && c1 < base + NP) {
+                    w->r_rho[c1] += w->d_rho[k];
+                    for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c1 + c] += w->d_mom[3 * k + c];
+                    w->r_th[c1] += w->d_th[k];
+                } else if (c2 < (uint32_t)n_all) {
+                    w->r_rho[c2] -= w->d_rho[k];
+                    for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c2 + c] -= w->d_mom[3 * k + c];
+                    w->r_th[c2] -= w->d_th[k];
+                }
+            }
+        }
+        /* volume term, scattered from node b to the nodes of its 3 lines */
+        for (int32_t ii = 0; ii < NPX; ii++)
+        for (int32_t jj = 0; jj < NPY; jj++)
+        for (int32_t kk = 0; kk < NPZ; kk++) {
+            const int64_t b = base + (int64_t)ii * NPY * NPZ + jj * NPZ + kk;
+            double Jin[9];
+            for (int c = 0; c < 9; c++) Jin[c] = m->Jinv[9 * b + c] * m->cV[b];
+            const double rb = w->rho[b], Tb = w->T[b], pb = w->p[b];
+            const double* Ub = w->U + 3 * b;
+            double fr[3] = {Ub[0] * rb, Ub[1] * rb, Ub[2] * rb};    /* U*rho */
+            double Fc[3] = {Ub[0] * rb, Ub[1] * rb, Ub[2] * rb};    /* rho*U */
+            double fm[9];
+            outer(Fc, Ub, fm);
+            for (int c = 0; c < 9; c++) fm[c] = fm[c] + ((c < 3) ? 1.0 : 0.0) * pb;
+            double ft[3] = {Fc[0] * Tb, Fc[1] * Tb, Fc[2] * Tb};
+            for (int pass = 0; pass < 3; pass++) {
+                const int32_t lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
+                for (int32_t q = 0; q < lim; q++) {
+                    int32_t im = ii, jm = jj, km = kk;
+                    if (pass == 0) im = q;
+                    else if (pass == 1) { if (q == jj) continue; jm = q; }
+                    else { if (q == kk) continue; km = q; }
+                    const int64_t a = base + (int64_t)im * NPY * NPZ + jm * NPZ + km;
+                    double dv[3], dj[3], t[3];
+                    dv[0] = m->dpsi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[1] = m->psi[0][ii * NPX + im] * m->dpsi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[2] = m->psi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->dpsi[2][kk * NPZ + km];
+                    tdot(Jin, dv, dj);
+                    w->r_rho[a] -= vdot(fr, dj);
+                    tdot(fm, dj, t);
+                    w->r_mom[3 * a + 0] -= t[0];
+                    w->r_mom[3 * a + 1] -= t[1];
+                    w->r_mom[3 * a + 2] -= t[2];
+                    w->r_th[a] -= vdot(ft, dj);
+                }
+            }
+        }
+    }
+    /* momentum source: Su -= ((rho - rho_ref) g) cV */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n_int; i++) {
+        double s = w->rho[i] - m->rho_ref[i];
+        for (int c = 0; c < 3; c++) {
+            double sc = 0.0 + m->gravity[c] * s;
+            w->r_mom[3 * i + c] = w->r_mom[3 * i + c] - sc * m->cV[i];
+        }
+    }
+}
+
+static void tendency_w(const nsem_oracle_mesh* m, const double* const u[5],
+                       double* const L[5], work_t* w, double* p_out) {
+    residual(m, u, w, p_out);
+    const int64_t n_int = m->n_int;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n_int; i++) {
+        double cv = m->cV[i];
+        L[0][i] = -(w->r_rho[i] / cv);
+        L[1][i] = -(w->r_mom[3 * i + 0] / cv);
+        L[2][i] = -(w->r_mom[3 * i + 1] / cv);
+        L[3][i] = -(w->r_mom[3 * i + 2] / cv);
+        L[4][i] = -(w->r_th[i] / cv);
+    }
+}
+
+void nsem_oracle_tendency(const nsem_oracle_mesh* m, const double* const u[5],
+                          double* const L[5], double* p_out) {
+    work_t w;
+    work_alloc(m, &w);
+    tendency_w(m, u, L, &w, p_out);
+    work_free(&w);
+}
+
+void nsem_oracle_ssprk3(const nsem_oracle_mesh* m, double* const u[5], double dt,
+                        int nsteps) {
+    const int64_t n = m->n_int;
+    work_t w;
+    work_alloc(m, &w);
+    double *L[5], *s[5];
+    for (int c = 0; c < 5; c++) {
+        L[c] = malloc((size_t)n * sizeof(double));
+        s[c] = malloc((size_t)n * sizeof(double));
+    }
+    const double a2 = 0.75, b2 = 0.25, a3 = 1.0 / 3.0, b3 = 2.0 / 3.0;
+    for (int step = 0; step < nsteps; step++) {
+        tendency_w(m, (const double* const*)u, L, &w, NULL);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) s[c][i] = u[c][i] + dt * L[c][i];
+        }
+        tendency_w(m, (const double* const*)s, L, &w, NULL);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) {
+                double t = s[c][i] + dt * L[c][i];
+                s[c][i] = a2 * u[c][i] + b2 * t;
+            }
+        }
+        tendency_w(m, (const double* const*)s, L, &w, NULL);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) {
+                double t = s[c][i] + dt * L[c][i];
+                u[c][i] = a3 * u[c][i] + b3 * t;
+            }
+        }
+    }
+    for (int c = 0; c < 5; c++) { free(L[c]); free(s[c]); }
+    work_free(&w);
+}
+
+void nsem_oracle_diagnostics(const nsem_oracle_mesh* m, const double* const u[5],
+                             const double* gh, double cv_heat, double out[3]) {
+    const double P0 = m->P0, R = m->R, cp = m->R + cv_heat;
+    double mass = 0, energy = 0, vol = 0;
+    work_t w;
+    work_alloc(m, &w);
+    residual(m, u, &w, NULL);
+    for (int64_t i = 0; i < m->n_int; i++) {
+        double rho = w.rho[i], cvn = m->cV[i];
+        const double* U = w.U + 3 * i;
+        mass += rho * cvn;
+        double sf = gh[i] + 0.5 * vdot(U, U) +
+                    pow((w.p[i] + m->p_ref[i]) / P0, R / cp) * w.T[i] * cv_heat;
+        energy += rho * cvn * sf;
+        vol += cvn;
+    }
+    work_free(&w);
+    out[0] = mass; out[1] = energy; out[2] = vol;
+}

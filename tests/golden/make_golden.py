@@ -1,0 +1,107 @@
+"""Generate the golden fixtures from the reference library itself.
+
+Builds the reference NebulaSEM sources (read-only checkout given by --ref)
+with oracle/Makefile.ref into oracle/_ref, writes rising-bubble case
+directories (oracle/make_case.py), runs the reference mesh app and the oracle
+harness (oracle/ref_harness.cpp, which calls the reference's own divf /
+rusanov / applyExplicitBCs), and stores per case one compressed .npz:
+
+  geometry  meta, cC, cV, Jinv, FO, FN, fN, fI, allFaces, faceIdx0/1,
+            xgl/wgl/psi/dpsi per direction, bcU, p_ref, rho_ref, gh
+  states    u0_* (initial, at rest), L0_* (its tendency), up_* (smooth
+            velocity perturbation), Lp_*, p0prime/ppprime (p - p_ref),
+            traj_<step>_* (coupled SSP-RK3 states after <step> steps)
+
+Run in the build container (the reference is not present on GPU machines):
+  python tests/golden/make_golden.py --ref /root/reference
+"""
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import load_dump  # noqa: E402
+from oracle.make_case import CASES, write_case  # noqa: E402
+
+VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
+
+# case -> (dt, start state, [dump steps], total steps)
+PLAN = {
+    "c1_2d": (0.0175, "rest", [50, 500], 500),
+    "g3_2": (0.01, "pert", [20], 20),
+    "g3_4n3": (0.01, "pert", [10, 30], 30),
+    "g3_2n7": (0.005, "pert", [10], 10),
+}
+
+KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
+            "xgl0", "xgl1", "xgl2", "wgl0", "wgl1", "wgl2",
+            "psi0", "psi1", "psi2", "dpsi0", "dpsi1", "dpsi2"]
+KEEP_U32 = ["meta", "FO", "FN", "allFaces", "faceIdx0", "faceIdx1", "bcU"]
+
+
+def run(cmd, cwd, threads=8):
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    subprocess.run(cmd, cwd=cwd, check=True, env=env, stdout=subprocess.DEVNULL)
+
+
+def make_case(name, ref_bin, tmp):
+    dt, start, dumps, nsteps = PLAN[name]
+    case = os.path.join(tmp, name)
+    write_case(case, dt=dt, steps=nsteps, **CASES[name])
+    run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    os.makedirs(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
+    d = load_dump(os.path.join(case, "out"))
+    os.makedirs(os.path.join(case, "rk"))
+    every = dumps[0] if len(dumps) == 1 else int(np.gcd.reduce(dumps))
+    args = [os.path.join(ref_bin, "euler_oracle"), "./controls", "rk3", "rk",
+            str(nsteps), str(every)]
+    if start == "pert":
+        args.append("pert")
+    run(args, case)
+    r = load_dump(os.path.join(case, "rk"))
+    n_int = int(d["meta"][7])
+    out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    for tag in ("u0", "L0", "up", "Lp"):
+        for v in VARS:
+            out[f"{tag}_{v}"] = d[f"{tag}_{v}"]
+    out["p0prime"] = d["p0prime"][:n_int]
+    out["ppprime"] = d["ppprime"][:n_int]
+    for s in dumps:
+        for v in VARS:
+            out[f"traj_{s}_{v}"] = r[f"s{s:05d}_{v}"]
+    out["dt"] = np.float64(dt)
+    out["start"] = np.array(start)
+    out["steps"] = np.array(dumps, dtype=np.int64)
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {n_int} interior nodes -> {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", required=True, help="reference NebulaSEM source tree")
+    ap.add_argument("--cases", nargs="*", default=sorted(PLAN))
+    ap.add_argument("-j", type=int, default=8)
+    a = ap.parse_args()
+    subprocess.run(["make", "-f", "oracle/Makefile.ref", f"REF={a.ref}", f"-j{a.j}"],
+                   cwd=ROOT, check=True)
+    ref_bin = os.path.join(ROOT, "oracle", "_ref")
+    tmp = tempfile.mkdtemp(prefix="nsem_golden_")
+    try:
+        for name in a.cases:
+            make_case(name, ref_bin, tmp)
+    finally:
+        shutil.rmtree(tmp)
+
+
+if __name__ == "__main__":
+    main()
