@@ -1,0 +1,156 @@
+/*
+ * libnsem_gpu -- GB300 (sm_103a) explicit dGSEM Euler right-hand side and
+ * SSP-RK stage update behind a C ABI.
+ *
+ * This library replaces the hot path of NebulaSEM's euler solver: the three
+ * operator chains of apps/euler/euler.cpp:181-258 -- divf with Rusanov face
+ * flux (src/field/field.h:3417-3478, 2928-2943), the weak surface lift
+ * (field.h:3086-3117), the hydrostatic-perturbation gravity source
+ * (euler.cpp:218-225, src field.h:3712-3723), the equation of state
+ * (euler.cpp:211-213), the ghost-node boundary conditions
+ * (applyExplicitBCs, field.h:2586-2727) -- and the explicit time update that
+ * addTemporal/ddt/SolveTexplicit perform (field.h:3741-3920,
+ * src/solvers/solve.cpp:563-564), here as a coupled Shu-Osher SSP-RK3.
+ *
+ * The reference has no plugin or FFI layer: its operator API is the set of
+ * header templates in src/field/field.h over MeshField arrays and the Mesh::
+ * and DG:: globals.  A C++ caller of the reference binds this ABI by passing
+ * those globals and arrays directly.
+ *
+ * Conventions
+ *  - node index n = e*NP + i*NPY*NPZ + j*NPZ + k (src/field/dg.h:43-44);
+ *    interior nodes [0, n_int) come first, ghost ("boundary cell") nodes
+ *    [n_int, n_all) after them, n_all is the unused-slot sentinel
+ *    (Mesh::gBCSfield / Mesh::gALLfield);
+ *  - tensors in XX,YY,ZZ,XY,YZ,XZ,YX,ZY,ZX order (src/tensor/tensor.h:450);
+ *  - state = conserved (rho, rho*u, rho*theta) on interior nodes, theta the
+ *    full potential temperature (the euler app's T + T0);
+ *  - every call returns nsem_status; nsem_last_error() describes the last
+ *    failure on a context.  Nothing exits, traps or prints.
+ *  - One context per host thread.  All device memory belongs to the context;
+ *    host pointers are never kept after a call returns.
+ */
+#ifndef NSEM_H
+#define NSEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSEM_ABI_VERSION 1
+
+typedef enum {
+    NSEM_OK = 0,
+    NSEM_BAD_ARG = 1,     /* invalid argument or mesh description          */
+    NSEM_CUDA_ERROR = 2,  /* CUDA runtime error (message in last_error)    */
+    NSEM_NONFINITE = 3,   /* a NaN/Inf appeared in the state               */
+    NSEM_TIMEOUT = 4,     /* a bounded device wait ran out                 */
+    NSEM_UNSUPPORTED = 5, /* configuration not implemented                 */
+    NSEM_NO_MEMORY = 6    /* device or host allocation failed              */
+} nsem_status;
+
+typedef enum {
+    NSEM_FP64 = 0,  /* plain form: FP64 throughout, reference operation order */
+    NSEM_MIXED = 1  /* precision form: FP32 bulk, FP64 background/RK/sums      */
+} nsem_precision;
+
+typedef enum {
+    NSEM_SSPRK3 = 0  /* coupled Shu-Osher SSP-RK3 */
+} nsem_scheme;
+
+/* Mesh in the reference's own layout (Mesh:: and DG:: globals after
+ * Mesh::LoadMesh / DG::init_geom, src/field/field.cpp:95-384,
+ * src/field/dg.cpp:167-477).  All arrays are host memory; they are copied. */
+typedef struct nsem_mesh_desc {
+    int32_t npx, npy, npz;      /* DG::NPX, NPY, NPZ (LGL nodes per direction) */
+    int32_t npf;                /* DG::NPF (slots per facet)                    */
+    int32_t n_elem;             /* Mesh::gBCS   interior cells                  */
+    int32_t n_cells;            /* Mesh::gNCells interior + boundary cells      */
+    int32_t n_face;             /* Mesh::gNFacets                               */
+    const double* cC;           /* [n_all*3] Mesh::cC node coordinates          */
+    const double* cV;           /* [n_all]   Mesh::cV node mass weights         */
+    const double* Jinv;         /* [n_all*9] DG::Jinv (inverse-transposed J)    */
+    const uint32_t* FO;         /* [n_face*npf] Mesh::FO owner node per slot    */
+    const uint32_t* FN;         /* [n_face*npf] Mesh::FN neighbour node         */
+    const double* fN;           /* [n_face*npf*3] Mesh::fN weighted normal      */
+    const double* fI;           /* [n_face*npf] Mesh::fI owner weight           */
+    const uint32_t* all_faces;  /* Mesh::allFaces (cell face lists)             */
+    const uint32_t* face_idx0;  /* [n_cells] Mesh::faceIndices[0]              */
+    const uint32_t* face_idx1;  /* [n_cells] Mesh::faceIndices[1]              */
+    const double* psi[3];       /* DG::psi[d]  [npd*npd]                         */
+    const double* dpsi[3];      /* DG::dpsi[d] [npd*npd]                         */
+    const uint32_t* bc_U;       /* [n_face*npf] velocity BC per slot:
+                                   0 none, 1 NEUMANN, 2 SYMMETRY; scalars
+                                   (rho, T, p) are NEUMANN wherever bc_U != 0 */
+} nsem_mesh_desc;
+
+typedef struct nsem_params {
+    double P0, T0, cp, cv;      /* Fluid:: properties (R = cp - cv, gamma = cp/cv) */
+    double gravity[3];          /* Controls::gravity                               */
+    double dt;                  /* Controls::dt                                    */
+    const double* p_ref;        /* [n_all] hydrostatic p (euler.cpp:122), or NULL  */
+    const double* rho_ref;      /* [n_all] hydrostatic rho (euler.cpp:123), or NULL*/
+    int32_t device;             /* CUDA device ordinal                             */
+} nsem_params;
+
+typedef struct nsem_ctx nsem_ctx;
+
+/* Replaces the setup of euler.cpp:104-131 plus the mesh upload.  If p_ref or
+ * rho_ref is NULL they are computed on the host from gh = g . cC exactly as
+ * euler.cpp:114-123 does (C library pow). */
+nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params,
+                        nsem_ctx** out);
+void nsem_destroy(nsem_ctx* ctx);
+const char* nsem_last_error(const nsem_ctx* ctx);
+int nsem_abi_version(void);
+
+/* Interior node count (Mesh::gBCSfield) and the context's CUDA stream. */
+int64_t nsem_num_nodes(const nsem_ctx* ctx);
+void* nsem_stream(const nsem_ctx* ctx);
+
+/* Conserved state on interior nodes: rho[n], rhoU[3n] (AoS, as a
+ * VectorCellField), rhoTheta[n].  Host buffers. */
+nsem_status nsem_set_state(nsem_ctx* ctx, const double* rho, const double* rhoU,
+                           const double* rhoTheta);
+nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rhoTheta);
+
+/* Same in the solver's own field layout (euler.cpp:58-61): rho, U (AoS
+ * velocity), T (theta' = theta - T0).  Conversion as euler.cpp:181,
+ * 200, 233, 251 (rho*U, rho*(T+T0)). */
+nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U,
+                            const double* T);
+nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T);
+
+/* Tendencies L = -Su/cV of (rho, rho u, rho v, rho w, rho theta) for the
+ * current state, the divf + src chains of euler.cpp:193-258 evaluated on one
+ * state.  L is five host arrays of n_int doubles; p_prime (optional, may be
+ * NULL) receives p - p_ref on interior nodes. */
+nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5],
+                          double* p_prime);
+
+/* Advance the state by nsteps SSP-RK3 steps of size params.dt.  Launches are
+ * captured once per (precision, nsteps) into a CUDA graph and replayed. */
+nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec);
+
+/* Mass, energy and volume sums over interior nodes (euler.cpp:165-176,
+ * 263-274) with compensated summation; gh = g . cC. */
+nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double* volume);
+
+/* Measurement helper: run nsteps SSP-RK3 steps launch by launch (no graph)
+ * with CUDA events on the context's stream around every kernel, and report
+ * per kernel class the summed device time in ms, the launch count and the
+ * class name (names: 8 slots of 32 chars).  Advances the state like
+ * nsem_step.  No reference counterpart (the reference has no GPU path). */
+nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double ms[8],
+                         int launches[8], char names[8 * 32]);
+
+/* Wait for all work on the context's stream. */
+nsem_status nsem_sync(nsem_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,551 @@
+/*
+ * Host side of libnsem_gpu: the C ABI of include/nsem.h.
+ *
+ * Converts the reference's mesh layout (Mesh:: / DG:: globals) into the
+ * device layout of nsem_internal.h, owns all device memory of a context,
+ * captures the RK step launches into CUDA graphs and reports errors as
+ * nsem_status codes.  Compiled with -ffp-contract=off: the host-side products
+ * it precomputes (Jinv*cV, unit normals, hydrostatic background) must round
+ * exactly like the reference's.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "nsem.h"
+#include "nsem_internal.h"
+#include "nsem_mixed.h"
+
+struct nsem_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    NsemDev dev{};
+    NsemTables tab{};
+    NsemBuf buf{};
+    NsemMixedBuf mbuf{};
+    bool mixed_ready = false;
+    double dt = 0, T0 = 0;
+    int64_t n_all = 0;
+    std::vector<void*> allocations;
+    double* scratch_aos = nullptr;   /* [3*n_int] AoS staging for rhoU */
+    double* red = nullptr;           /* reduction partials */
+    double* h_red = nullptr;         /* pinned host copy of the reduction result */
+    uint32_t* h_status = nullptr;    /* pinned host copy of the status word */
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    std::string err;
+};
+
+namespace {
+
+enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
+
+nsem_status fail(nsem_ctx* c, nsem_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+nsem_status cuda_fail(nsem_ctx* c, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(c, NSEM_CUDA_ERROR, m);
+}
+
+#define NSEM_CUDA(call)                                               \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);      \
+    } while (0)
+
+template <typename T>
+nsem_status dalloc(nsem_ctx* ctx, T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(ctx, NSEM_NO_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    ctx->allocations.push_back((void*)*p);
+    return NSEM_OK;
+}
+
+template <typename T>
+nsem_status upload(nsem_ctx* ctx, T** p, const std::vector<T>& h) {
+    nsem_status s = dalloc(ctx, p, h.size());
+    if (s != NSEM_OK) return s;
+    NSEM_CUDA(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return NSEM_OK;
+}
+
+inline double vdot3(const double* a, const double* b) {
+    return a[0] * b[0] + (a[1] * b[1] + (a[2] * b[2] + 0.0));
+}
+
+nsem_status check_desc(nsem_ctx* ctx, const nsem_mesh_desc* m) {
+    if (!m) return fail(ctx, NSEM_BAD_ARG, "mesh description is NULL");
+    const int npd[3] = {m->npx, m->npy, m->npz};
+    for (int d = 0; d < 3; d++) {
+        if (npd[d] < 1 || npd[d] > NSEM_MAX_NPD)
+            return fail(ctx, NSEM_UNSUPPORTED, "nodes per direction must be 1..10");
+        if (!m->psi[d] || !m->dpsi[d]) return fail(ctx, NSEM_BAD_ARG, "psi/dpsi table is NULL");
+    }
+    if (m->n_elem <= 0 || m->n_cells < m->n_elem || m->n_face < 0 || m->npf <= 0)
+        return fail(ctx, NSEM_BAD_ARG, "inconsistent element/cell/face counts");
+    if (!m->cC || !m->cV || !m->Jinv || !m->FO || !m->FN || !m->fN || !m->fI ||
+        !m->all_faces || !m->face_idx0 || !m->face_idx1 || !m->bc_U)
+        return fail(ctx, NSEM_BAD_ARG, "a mesh array is NULL");
+    const int64_t np = (int64_t)m->npx * m->npy * m->npz;
+    if ((int64_t)m->n_cells * np >= (int64_t)0x7fffffff)
+        return fail(ctx, NSEM_UNSUPPORTED, "more than 2^31 nodes");
+    /* the volume gather assumes nodal (Kronecker) basis values at LGL points */
+    for (int d = 0; d < 3; d++)
+        for (int s = 0; s < npd[d]; s++)
+            for (int i = 0; i < npd[d]; i++)
+                if (m->psi[d][s * npd[d] + i] != (s == i ? 1.0 : 0.0))
+                    return fail(ctx, NSEM_UNSUPPORTED, "psi is not the identity at LGL nodes");
+    return NSEM_OK;
+}
+
+nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem_params* p) {
+    NsemDev& D = ctx->dev;
+    D.npx = m->npx; D.npy = m->npy; D.npz = m->npz;
+    D.np = m->npx * m->npy * m->npz;
+    const int64_t NP = D.np;
+    D.n_elem = m->n_elem;
+    D.n_int = (int64_t)m->n_elem * NP;
+    const int64_t n_int = D.n_int;
+    const int64_t n_all = (int64_t)m->n_cells * NP;
+    ctx->n_all = n_all;
+    const int64_t n_slot_all = (int64_t)m->n_face * m->npf;
+
+    D.R = p->cp - p->cv;
+    D.gamma = p->cp / p->cv;
+    D.gR = D.gamma * D.R;
+    D.P0 = p->P0;
+    D.cp = p->cp;
+    D.cv_heat = p->cv;
+    for (int c = 0; c < 3; c++) D.g[c] = p->gravity[c];
+    ctx->dt = p->dt;
+    ctx->T0 = p->T0;
+
+    /* tables: dpsi[d][s*npd + i] */
+    const int npd[3] = {m->npx, m->npy, m->npz};
+    std::memset(&ctx->tab, 0, sizeof(ctx->tab));
+    for (int d = 0; d < 3; d++)
+        for (int q = 0; q < npd[d] * npd[d]; q++) ctx->tab.dpsi[d][q] = m->dpsi[d][q];
+
+    /* used slots in reference order */
+    std::vector<int64_t> compact(n_slot_all, -1);
+    std::vector<int32_t> c1, c2;
+    std::vector<uint8_t> bc;
+    std::vector<double> fi, fn[3], en[3];
+    for (int64_t k = 0; k < n_slot_all; k++) {
+        const uint32_t o = m->FO[k], n = m->FN[k];
+        if (o >= (uint64_t)n_all || n >= (uint64_t)n_all) continue;
+        if (o >= (uint64_t)n_int)
+            return fail(ctx, NSEM_BAD_ARG, "face slot owner is not an interior node");
+        compact[k] = (int64_t)c1.size();
+        c1.push_back((int32_t)o);
+        const bool ghost = n >= (uint64_t)n_int;
+        c2.push_back(ghost ? -1 : (int32_t)n);
+        if (ghost && m->bc_U[k] == 0)
+            return fail(ctx, NSEM_BAD_ARG, "boundary slot without a boundary condition");
+        if (m->bc_U[k] > 2) return fail(ctx, NSEM_UNSUPPORTED, "velocity BC other than NEUMANN/SYMMETRY");
+        bc.push_back(ghost ? (uint8_t)m->bc_U[k] : 0);
+        fi.push_back(m->fI[k]);
+        const double* v = m->fN + 3 * k;
+        const double mg = std::sqrt(vdot3(v, v));
+        for (int c = 0; c < 3; c++) {
+            fn[c].push_back(v[c]);
+            en[c].push_back(v[c] / mg);
+        }
+    }
+    D.n_slot = (int64_t)c1.size();
+
+    /* per-node lift lists in div_flux order (field.h:3097-3113) */
+    std::vector<int32_t> lift(3 * n_int, -1);
+    std::vector<int> cnt(n_int, 0);
+    for (int64_t e = 0; e < m->n_elem; e++) {
+        const int64_t lo = e * NP, hi = lo + NP;
+        for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
+            for (int q = 0; q < m->npf; q++) {
+                const int64_t k = (int64_t)m->all_faces[f] * m->npf + q;
+                if (k >= n_slot_all) return fail(ctx, NSEM_BAD_ARG, "face id out of range");
+                const uint32_t o = m->FO[k], n = m->FN[k];
+                int64_t node;
+                int neg;
+                if (o >= lo && o < hi) { node = o; neg = 0; }
+                else if (n < (uint64_t)n_all) { node = n; neg = 1; }
+                else continue;
+                if (node < lo || node >= hi)
+                    return fail(ctx, NSEM_BAD_ARG, "face slot does not belong to its cell");
+                if (compact[k] < 0) return fail(ctx, NSEM_BAD_ARG, "lift from an unused slot");
+                if (cnt[node] >= 3) return fail(ctx, NSEM_BAD_ARG, "node on more than 3 faces");
+                lift[(int64_t)cnt[node] * n_int + node] = (int32_t)((compact[k] << 1) | neg);
+                cnt[node]++;
+            }
+        }
+    }
+
+    /* node arrays: Jinv*cV (field.h:3445), cV, background */
+    std::vector<double> jin(9 * n_int), cv(n_int), pref(n_int), rref(n_int), gh(n_int);
+    for (int64_t i = 0; i < n_int; i++) {
+        cv[i] = m->cV[i];
+        for (int c = 0; c < 9; c++) jin[(int64_t)c * n_int + i] = m->Jinv[9 * i + c] * m->cV[i];
+        /* gh = g . cC (euler.cpp:114), right-nested like the reference's Vector dot */
+        gh[i] = vdot3(p->gravity, m->cC + 3 * i);
+    }
+    const double R = D.R, gam = D.gamma, P0 = p->P0, cp = p->cp, T0 = p->T0;
+    for (int64_t i = 0; i < n_int; i++) {
+        /* euler.cpp:122-123 */
+        pref[i] = p->p_ref ? p->p_ref[i] : P0 * std::pow(1.0 + gh[i] / (cp * T0), cp / R);
+        rref[i] = p->rho_ref ? p->rho_ref[i] : (P0 / (R * T0)) * std::pow(pref[i] / P0, 1 / gam);
+    }
+
+    nsem_status s;
+#define UP(ptr, vec) if ((s = upload(ctx, &(ptr), vec)) != NSEM_OK) return s
+    UP(D.jin, jin);
+    UP(D.cv, cv);
+    UP(D.p_ref, pref);
+    UP(D.rho_ref, rref);
+    UP(D.gh, gh);
+    UP(D.lift, lift);
+    UP(D.c1, c1);
+    UP(D.c2, c2);
+    UP(D.bc, bc);
+    UP(D.fi, fi);
+    std::vector<double> fn3, en3;
+    for (int c = 0; c < 3; c++) {
+        fn3.insert(fn3.end(), fn[c].begin(), fn[c].end());
+        en3.insert(en3.end(), en[c].begin(), en[c].end());
+    }
+    UP(D.fn, fn3);
+    UP(D.en, en3);
+#undef UP
+    if ((s = dalloc(ctx, &D.status, 1)) != NSEM_OK) return s;
+    NSEM_CUDA(cudaMemset(D.status, 0, sizeof(uint32_t)));
+
+    /* state buffers */
+    NsemBuf& b = ctx->buf;
+    for (int c = 0; c < 5; c++) {
+        if ((s = dalloc(ctx, &b.u[c], n_int)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &b.s[c], n_int)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &b.d[c], D.n_slot)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &b.L[c], n_int)) != NSEM_OK) return s;
+    }
+    for (int c = 0; c < NSEM_NPRIM; c++)
+        if ((s = dalloc(ctx, &b.prim[c], n_int)) != NSEM_OK) return s;
+    if ((s = dalloc(ctx, &ctx->scratch_aos, 3 * n_int)) != NSEM_OK) return s;
+    if ((s = dalloc(ctx, &ctx->red, NSEM_RED_PARTIALS * 6 + 8)) != NSEM_OK) return s;
+    NSEM_CUDA(cudaMallocHost((void**)&ctx->h_red, 8 * sizeof(double)));
+    NSEM_CUDA(cudaMallocHost((void**)&ctx->h_status, sizeof(uint32_t)));
+    *ctx->h_status = 0;
+
+    /* mixed form: per-element affine data, FP32 */
+    if ((s = nsem_mixed_setup(ctx->dev, m, &ctx->mbuf, &ctx->allocations, ctx->err)) != NSEM_OK) {
+        ctx->mixed_ready = false;
+        if (s != NSEM_UNSUPPORTED) return s;
+    } else {
+        ctx->mixed_ready = true;
+    }
+    return NSEM_OK;
+}
+
+nsem_status check_status(nsem_ctx* ctx) {
+    NSEM_CUDA(cudaStreamSynchronize(ctx->stream));
+    uint32_t st = *ctx->h_status;
+    if (st & NSEM_STATUS_NONFINITE) {
+        *ctx->h_status = 0;
+        NSEM_CUDA(cudaMemset(ctx->dev.status, 0, sizeof(uint32_t)));
+        return fail(ctx, NSEM_NONFINITE, "non-finite value in the state");
+    }
+    return NSEM_OK;
+}
+
+/* launches of one nsem_step call (captured into a graph) */
+nsem_status enqueue_steps(nsem_ctx* ctx, int nsteps, nsem_precision prec) {
+    NsemDev* D = &ctx->dev;
+    NsemBuf* b = &ctx->buf;
+    void* st = (void*)ctx->stream;
+    int e;
+    if (prec == NSEM_FP64) {
+        if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
+        for (int n = 0; n < nsteps; n++) {
+            for (int stage = 1; stage <= 3; stage++) {
+                if ((e = nsem_fp64_face(D, b, stage == 1, st)))
+                    return cuda_fail(ctx, (cudaError_t)e, "face");
+                if ((e = nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st)))
+                    return cuda_fail(ctx, (cudaError_t)e, "volume");
+            }
+        }
+    } else {
+        if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+        if ((e = nsem_mixed_steps(D, &ctx->mbuf, b, &ctx->tab, nsteps, ctx->dt, st)))
+            return cuda_fail(ctx, (cudaError_t)e, "mixed step");
+    }
+    return NSEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsem_abi_version(void) { return NSEM_ABI_VERSION; }
+
+const char* nsem_last_error(const nsem_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : "context is NULL";
+}
+
+int64_t nsem_num_nodes(const nsem_ctx* ctx) { return ctx ? ctx->dev.n_int : 0; }
+
+void* nsem_stream(const nsem_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params, nsem_ctx** out) {
+    if (!out) return NSEM_BAD_ARG;
+    *out = nullptr;
+    nsem_ctx* ctx = new (std::nothrow) nsem_ctx();
+    if (!ctx) return NSEM_NO_MEMORY;
+    *out = ctx;
+    if (!params) return fail(ctx, NSEM_BAD_ARG, "params is NULL");
+    if (!(params->cp > params->cv) || !(params->cv > 0) || !(params->P0 > 0) || !(params->T0 > 0))
+        return fail(ctx, NSEM_BAD_ARG, "invalid fluid properties");
+    nsem_status s = check_desc(ctx, mesh);
+    if (s != NSEM_OK) return s;
+    ctx->device = params->device;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    NSEM_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    s = build_device_mesh(ctx, mesh, params);
+    if (s != NSEM_OK) return s;
+    int e = nsem_fp64_check_smem(&ctx->dev);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "volume kernel shared memory");
+    return NSEM_OK;
+}
+
+void nsem_destroy(nsem_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    for (void* p : ctx->allocations) cudaFree(p);
+    if (ctx->h_red) cudaFreeHost(ctx->h_red);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+nsem_status nsem_set_state(nsem_ctx* ctx, const double* rho, const double* rhoU,
+                           const double* rhoTheta) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!rho || !rhoU || !rhoTheta) return fail(ctx, NSEM_BAD_ARG, "state pointer is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ctx->dev.n_int;
+    NSEM_CUDA(cudaMemcpyAsync(ctx->buf.u[0], rho, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->buf.u[4], rhoTheta, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->scratch_aos, rhoU, 3 * n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    int e = nsem_aos_to_soa(ctx->scratch_aos, ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3],
+                            ctx->dev.n_int, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
+    return NSEM_OK;
+}
+
+nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rhoTheta) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!rho || !rhoU || !rhoTheta) return fail(ctx, NSEM_BAD_ARG, "state pointer is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ctx->dev.n_int;
+    int e = nsem_soa_to_aos(ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3], ctx->scratch_aos,
+                            ctx->dev.n_int, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "soa_to_aos");
+    NSEM_CUDA(cudaMemcpyAsync(rho, ctx->buf.u[0], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(rhoTheta, ctx->buf.u[4], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(rhoU, ctx->scratch_aos, 3 * n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U, const double* T) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!rho || !U || !T) return fail(ctx, NSEM_BAD_ARG, "field pointer is NULL");
+    const int64_t n = ctx->dev.n_int;
+    std::vector<double> ru(3 * n), rt(n);
+    for (int64_t i = 0; i < n; i++) {
+        const double r = rho[i];
+        for (int c = 0; c < 3; c++) ru[3 * i + c] = r * U[3 * i + c];
+        rt[i] = r * (T[i] + ctx->T0);
+    }
+    nsem_status s = nsem_set_state(ctx, rho, ru.data(), rt.data());
+    if (s != NSEM_OK) return s;
+    NSEM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NSEM_OK;
+}
+
+nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!rho || !U || !T) return fail(ctx, NSEM_BAD_ARG, "field pointer is NULL");
+    const int64_t n = ctx->dev.n_int;
+    std::vector<double> ru(3 * n), rt(n);
+    nsem_status s = nsem_get_state(ctx, rho, ru.data(), rt.data());
+    if (s != NSEM_OK) return s;
+    for (int64_t i = 0; i < n; i++) {
+        const double r = rho[i];
+        for (int c = 0; c < 3; c++) U[3 * i + c] = ru[3 * i + c] / r;
+        T[i] = rt[i] / r - ctx->T0;
+    }
+    return NSEM_OK;
+}
+
+nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5],
+                          double* p_prime) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!L) return fail(ctx, NSEM_BAD_ARG, "L is NULL");
+    for (int c = 0; c < 5; c++) if (!L[c]) return fail(ctx, NSEM_BAD_ARG, "L[c] is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    NsemDev* D = &ctx->dev;
+    NsemBuf* b = &ctx->buf;
+    void* st = (void*)ctx->stream;
+    int e;
+    if (prec == NSEM_FP64) {
+        if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
+        if ((e = nsem_fp64_face(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "face");
+        if ((e = nsem_fp64_volume(D, &ctx->tab, b, 0, ctx->dt, st)))
+            return cuda_fail(ctx, (cudaError_t)e, "volume");
+    } else if (prec == NSEM_MIXED) {
+        if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+        if ((e = nsem_mixed_tendency(D, &ctx->mbuf, b, &ctx->tab, st)))
+            return cuda_fail(ctx, (cudaError_t)e, "mixed tendency");
+    } else {
+        return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    }
+    const size_t n = (size_t)D->n_int;
+    for (int c = 0; c < 5; c++)
+        NSEM_CUDA(cudaMemcpyAsync(L[c], b->L[c], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (p_prime)
+        NSEM_CUDA(cudaMemcpyAsync(p_prime, b->prim[4], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
+    if (scheme != NSEM_SSPRK3) return fail(ctx, NSEM_UNSUPPORTED, "only SSPRK3 is implemented");
+    if (prec != NSEM_FP64 && prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    if (nsteps == 0) return NSEM_OK;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    auto key = std::make_pair((int)prec, nsteps);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+        cudaGraph_t g;
+        NSEM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        nsem_status s = enqueue_steps(ctx, nsteps, prec);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (s != NSEM_OK) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return s;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaGraphExec_t ex;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+        it = ctx->graphs.emplace(key, ex).first;
+    }
+    NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    return NSEM_OK;
+}
+
+nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double ms[8],
+                         int launches[8], char names[8 * 32]) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!ms || !launches || !names) return fail(ctx, NSEM_BAD_ARG, "output pointer is NULL");
+    if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps < 1");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    for (int i = 0; i < 8; i++) { ms[i] = 0; launches[i] = 0; }
+    std::memset(names, 0, 8 * 32);
+    NsemDev* D = &ctx->dev;
+    NsemBuf* b = &ctx->buf;
+    void* st = (void*)ctx->stream;
+    /* one event pair per launch, timed after the whole run */
+    struct Rec { int cls; cudaEvent_t a, z; };
+    std::vector<Rec> recs;
+    auto timed = [&](int cls, auto&& launch) -> nsem_status {
+        Rec r;
+        r.cls = cls;
+        NSEM_CUDA(cudaEventCreate(&r.a));
+        NSEM_CUDA(cudaEventCreate(&r.z));
+        NSEM_CUDA(cudaEventRecord(r.a, ctx->stream));
+        int e = launch();
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "profiled launch");
+        NSEM_CUDA(cudaEventRecord(r.z, ctx->stream));
+        recs.push_back(r);
+        return NSEM_OK;
+    };
+    nsem_status s = NSEM_OK;
+    if (prec == NSEM_FP64) {
+        std::strncpy(names + 0 * 32, "fp64_prim", 31);
+        std::strncpy(names + 1 * 32, "fp64_face", 31);
+        std::strncpy(names + 2 * 32, "fp64_volume", 31);
+        s = timed(0, [&] { return nsem_fp64_prim(D, b, 1, st); });
+        for (int n = 0; n < nsteps && s == NSEM_OK; n++)
+            for (int stage = 1; stage <= 3 && s == NSEM_OK; stage++) {
+                s = timed(1, [&] { return nsem_fp64_face(D, b, stage == 1, st); });
+                if (s == NSEM_OK)
+                    s = timed(2, [&] { return nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st); });
+            }
+    } else if (prec == NSEM_MIXED) {
+        if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+        const char* const* nm = nsem_mixed_kernel_names();
+        for (int i = 0; i < 8 && nm[i]; i++) std::strncpy(names + i * 32, nm[i], 31);
+        for (int n = 0; n < nsteps && s == NSEM_OK; n++) {
+            for (int k = 0; k < nsem_mixed_launches_per_step() && s == NSEM_OK; k++) {
+                int cls = nsem_mixed_launch_class(k);
+                s = timed(cls, [&] {
+                    return nsem_mixed_launch(D, &ctx->mbuf, b, &ctx->tab, k, n == 0, ctx->dt, st);
+                });
+            }
+        }
+    } else {
+        return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    }
+    cudaError_t ce = cudaStreamSynchronize(ctx->stream);
+    for (Rec& r : recs) {
+        float t = 0;
+        if (ce == cudaSuccess && s == NSEM_OK) {
+            cudaEventElapsedTime(&t, r.a, r.z);
+            ms[r.cls] += t;
+            launches[r.cls] += 1;
+        }
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.z);
+    }
+    if (s != NSEM_OK) return s;
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "profile sync");
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+nsem_status nsem_sync(nsem_ctx* ctx) {
+    if (!ctx) return NSEM_BAD_ARG;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    return check_status(ctx);
+}
+
+nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double* volume) {
+    if (!ctx) return NSEM_BAD_ARG;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    int e = nsem_reduce_diagnostics(&ctx->dev, &ctx->buf, ctx->red, ctx->h_red, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "diagnostics");
+    nsem_status s = check_status(ctx);
+    if (s != NSEM_OK) return s;
+    if (mass) *mass = ctx->h_red[0];
+    if (energy) *energy = ctx->h_red[1];
+    if (volume) *volume = ctx->h_red[2];
+    return NSEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+/*
+ * Internal device data layout shared by the host side (nsem_api.cpp) and the
+ * kernels (nsem_fp64.cu, nsem_mixed.cu).
+ *
+ * HBM layout, all structure-of-arrays so that consecutive threads touch
+ * consecutive addresses:
+ *   node arrays   [n_int]       state u[5], stage s[5], primitives prim[7]
+ *                               (U0,U1,U2,theta,p',|U|,c), Jinv*cV jin[9],
+ *                               cV, rho_ref, p_ref, gh, lift[3]
+ *   slot arrays   [n_slot]      used face slots in the reference's slot order:
+ *                               owner c1, neighbour c2 (-1: boundary ghost),
+ *                               bc, fI, weighted normal fN[3], unit normal en[3],
+ *                               lifted fluxes d[5]
+ * lift[j][a] lists, in the order the reference's div_flux visits them
+ * (field.h:3097-3113), the slots touching interior node a: value
+ * (slot << 1) | (a is the neighbour side), or -1.
+ */
+#ifndef NSEM_INTERNAL_H
+#define NSEM_INTERNAL_H
+
+#include <stdint.h>
+
+#define NSEM_MAX_NPD 10          /* up to order 9 per direction */
+#define NSEM_NPRIM 7
+#define NSEM_STATUS_NONFINITE 1u
+
+struct NsemTables {
+    double dpsi[3][NSEM_MAX_NPD * NSEM_MAX_NPD]; /* dpsi[d][s*npd + i] = l_i'(x_s) */
+};
+
+struct NsemDev {
+    int32_t npx, npy, npz, np;
+    int64_t n_elem, n_int, n_slot;
+    /* physical constants */
+    double P0, R, gamma, gR, cv_heat, cp;
+    double g[3];
+    /* node arrays */
+    double* jin;       /* [9][n_int] */
+    double* cv;
+    double* rho_ref;
+    double* p_ref;
+    double* gh;
+    int32_t* lift;     /* [3][n_int] */
+    /* slot arrays */
+    int32_t* c1;
+    int32_t* c2;
+    uint8_t* bc;
+    double* fi;
+    double* fn;        /* [3][n_slot] */
+    double* en;        /* [3][n_slot] */
+    /* element -> geometry for the mixed form (affine per element) */
+    float* ejin;       /* [9][n_elem] Jinv*cV/w at element level (mixed form) */
+    /* status word (bit flags) */
+    uint32_t* status;
+};
+
+/* Buffers of one solver state. */
+struct NsemBuf {
+    double* u[5];      /* state u^n                    */
+    double* s[5];      /* stage state                  */
+    double* prim[NSEM_NPRIM];
+    double* d[5];      /* face fluxes per used slot    */
+    double* L[5];      /* tendency output (nsem_tendency) */
+};
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* FP64 (plain) form launchers, nsem_fp64.cu.  stage: 0 = tendency only
+ * (writes L), 1..3 = Shu-Osher stage. */
+int nsem_fp64_prim(const NsemDev* m, NsemBuf* b, int from_state, void* stream);
+int nsem_fp64_face(const NsemDev* m, NsemBuf* b, int from_state, void* stream);
+int nsem_fp64_volume(const NsemDev* m, const NsemTables* t, NsemBuf* b, int stage,
+                     double dt, void* stream);
+int nsem_fp64_check_smem(const NsemDev* m);
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,48 @@
+/*
+ * Precision form (FP32 bulk arithmetic, FP64 state, background subtraction,
+ * RK accumulation and conservation sums) and auxiliary kernels.
+ */
+#ifndef NSEM_MIXED_H
+#define NSEM_MIXED_H
+
+#include <string>
+#include <vector>
+
+#include "nsem.h"
+#include "nsem_internal.h"
+
+#define NSEM_RED_PARTIALS 1024
+
+struct NsemMixedBuf {
+    bool ready = false;
+    int64_t n_elem = 0;
+    /* per-element affine geometry and per-face data live here */
+    float* egeo = nullptr;       /* [n_elem*4] Jinv diagonal * cV-scale, see nsem_mixed.cu */
+    int32_t* nbr = nullptr;      /* [6][n_elem] neighbour element or -1 (wall) */
+    float* dmat = nullptr;       /* [3][npd*npd] D matrices, FP32 */
+    double* du[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  /* FP32-precision increments kept in FP64 buffers */
+    float* dl[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   /* FP32 stage increments */
+};
+
+nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMixedBuf* mb,
+                             std::vector<void*>* allocs, std::string& err);
+int nsem_mixed_steps(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, const NsemTables* t,
+                     int nsteps, double dt, void* stream);
+int nsem_mixed_tendency(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, const NsemTables* t,
+                        void* stream);
+
+/* launch-by-launch interface for measurement (nsem_profile) */
+const char* const* nsem_mixed_kernel_names();
+int nsem_mixed_launches_per_step();
+int nsem_mixed_launch_class(int k);
+int nsem_mixed_launch(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, const NsemTables* t, int k,
+                      int first_step, double dt, void* stream);
+
+/* auxiliary kernels (nsem_aux.cu) */
+int nsem_aos_to_soa(const double* aos, double* x, double* y, double* z, int64_t n, void* stream);
+int nsem_soa_to_aos(const double* x, const double* y, const double* z, double* aos, int64_t n,
+                    void* stream);
+int nsem_reduce_diagnostics(const NsemDev* dev, const NsemBuf* b, double* partials,
+                            double* h_out, void* stream);
+
+#endif
