@@ -49,7 +49,8 @@ typedef enum {
     NSEM_NONFINITE = 3,   /* a NaN/Inf appeared in the state               */
     NSEM_TIMEOUT = 4,     /* a bounded device wait ran out                 */
     NSEM_UNSUPPORTED = 5, /* configuration not implemented                 */
-    NSEM_NO_MEMORY = 6    /* device or host allocation failed              */
+    NSEM_NO_MEMORY = 6,   /* device or host allocation failed              */
+    NSEM_TOO_LARGE = 7    /* request exceeds a fixed-size working array    */
 } nsem_status;
 
 typedef enum {
@@ -149,6 +150,34 @@ nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double 
 
 /* Wait for all work on the context's stream. */
 nsem_status nsem_sync(nsem_ctx* ctx);
+
+/* Allocation-free mass / energy / volume sums (no counterpart in the
+ * reference; it is the nsem_diagnostics computation for callers that may not
+ * allocate).  For host codes that own every byte of device memory -- a solver
+ * embedded in an application with its own pre-reserved pool, or a time loop
+ * that must not call cudaMalloc once running (cudaMalloc can synchronise the
+ * device and escapes the caller's memory accounting).
+ *
+ * All pointers are DEVICE memory of the current device, n_nodes entries each
+ * (state SoA: rho, rho u, rho v, rho w, rho theta; node weights cV; gh = g.x;
+ * hydrostatic p_ref); out3 receives mass, energy, volume in device memory,
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream).
+ * Nothing is allocated: the working memory is one fixed file-scope device
+ * array of 3 MiB, resident on every GPU that loads the library until the
+ * process exits.  n_nodes above NSEM_NOALLOC_MAX_NODES returns
+ * NSEM_TOO_LARGE; NULL pointers or bad constants return NSEM_BAD_ARG.
+ * The first call on a device resolves the array's device address for that
+ * device (set-up once per device); make that first call before any stream
+ * capture.  Every call shares the one array and fully rewrites the part it
+ * uses, so calls that overlap on the GPU (different streams or host threads
+ * without ordering) race with each other. */
+#define NSEM_NOALLOC_MAX_NODES ((int64_t)4096 * 65536)
+nsem_status nsem_conservation_sums_noalloc(const double* rho, const double* rhou,
+                                           const double* rhov, const double* rhow,
+                                           const double* rhoTheta, const double* cV,
+                                           const double* gh, const double* p_ref,
+                                           int64_t n_nodes, double P0, double cp, double cv,
+                                           double* out3, void* stream);
 
 #ifdef __cplusplus
 }
