@@ -30,6 +30,7 @@ struct nsem_ctx {
     NsemBuf buf{};
     NsemMixedBuf mbuf{};
     bool mixed_ready = false;
+    int rep = 0;                     /* 0: state in buf.u; 1: perturbation in mbuf.U[cur] */
     double dt = 0, T0 = 0;
     int64_t n_all = 0;
     std::vector<void*> allocations;
@@ -37,7 +38,7 @@ struct nsem_ctx {
     double* red = nullptr;           /* reduction partials */
     double* h_red = nullptr;         /* pinned host copy of the reduction result */
     uint32_t* h_status = nullptr;    /* pinned host copy of the status word */
-    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  /* key: (prec*2 + cur, nsteps) */
     std::string err;
 };
 
@@ -127,6 +128,7 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
     D.gR = D.gamma * D.R;
     D.P0 = p->P0;
     D.cp = p->cp;
+    D.T0 = p->T0;
     D.cv_heat = p->cv;
     for (int c = 0; c < 3; c++) D.g[c] = p->gravity[c];
     ctx->dt = p->dt;
@@ -266,6 +268,15 @@ nsem_status check_status(nsem_ctx* ctx) {
     return NSEM_OK;
 }
 
+/* move the current state to the representation a form needs */
+nsem_status ensure_rep(nsem_ctx* ctx, int want) {
+    if (ctx->rep == want) return NSEM_OK;
+    int e = nsem_mixed_convert(&ctx->dev, &ctx->mbuf, &ctx->buf, want == 1, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+    ctx->rep = want;
+    return NSEM_OK;
+}
+
 /* launches of one nsem_step call (captured into a graph) */
 nsem_status enqueue_steps(nsem_ctx* ctx, int nsteps, nsem_precision prec) {
     NsemDev* D = &ctx->dev;
@@ -349,6 +360,7 @@ nsem_status nsem_set_state(nsem_ctx* ctx, const double* rho, const double* rhoU,
     int e = nsem_aos_to_soa(ctx->scratch_aos, ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3],
                             ctx->dev.n_int, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
+    ctx->rep = 0;
     return NSEM_OK;
 }
 
@@ -357,6 +369,8 @@ nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rho
     if (!rho || !rhoU || !rhoTheta) return fail(ctx, NSEM_BAD_ARG, "state pointer is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     const size_t n = (size_t)ctx->dev.n_int;
+    nsem_status rs = ensure_rep(ctx, 0);
+    if (rs != NSEM_OK) return rs;
     int e = nsem_soa_to_aos(ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3], ctx->scratch_aos,
                             ctx->dev.n_int, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "soa_to_aos");
@@ -407,6 +421,9 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
     NsemBuf* b = &ctx->buf;
     void* st = (void*)ctx->stream;
     int e;
+    if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+    nsem_status rs = ensure_rep(ctx, prec == NSEM_MIXED ? 1 : 0);
+    if (rs != NSEM_OK) return rs;
     if (prec == NSEM_FP64) {
         if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
         if ((e = nsem_fp64_face(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "face");
@@ -422,7 +439,7 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
     const size_t n = (size_t)D->n_int;
     for (int c = 0; c < 5; c++)
         NSEM_CUDA(cudaMemcpyAsync(L[c], b->L[c], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    if (p_prime)
+    if (p_prime && prec == NSEM_FP64)
         NSEM_CUDA(cudaMemcpyAsync(p_prime, b->prim[4], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     return check_status(ctx);
 }
@@ -434,7 +451,11 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
     if (prec != NSEM_FP64 && prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
     if (nsteps == 0) return NSEM_OK;
     NSEM_CUDA(cudaSetDevice(ctx->device));
-    auto key = std::make_pair((int)prec, nsteps);
+    if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+    nsem_status rs = ensure_rep(ctx, prec == NSEM_MIXED ? 1 : 0);
+    if (rs != NSEM_OK) return rs;
+    const int cur = (prec == NSEM_MIXED) ? ctx->mbuf.cur : 0;
+    auto key = std::make_pair((int)prec * 2 + cur, nsteps);
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
         cudaGraph_t g;
@@ -453,6 +474,7 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
         it = ctx->graphs.emplace(key, ex).first;
     }
     NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
+    if (prec == NSEM_MIXED) ctx->mbuf.cur ^= (nsteps & 1);
     NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, ctx->stream));
     return NSEM_OK;
@@ -464,6 +486,11 @@ nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double 
     if (!ms || !launches || !names) return fail(ctx, NSEM_BAD_ARG, "output pointer is NULL");
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps < 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
+    if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+    {
+        nsem_status rs = ensure_rep(ctx, prec == NSEM_MIXED ? 1 : 0);
+        if (rs != NSEM_OK) return rs;
+    }
     for (int i = 0; i < 8; i++) { ms[i] = 0; launches[i] = 0; }
     std::memset(names, 0, 8 * 32);
     NsemDev* D = &ctx->dev;
@@ -538,6 +565,8 @@ nsem_status nsem_sync(nsem_ctx* ctx) {
 nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double* volume) {
     if (!ctx) return NSEM_BAD_ARG;
     NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status rs = ensure_rep(ctx, 0);
+    if (rs != NSEM_OK) return rs;
     int e = nsem_reduce_diagnostics(&ctx->dev, &ctx->buf, ctx->red, ctx->h_red, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "diagnostics");
     nsem_status s = check_status(ctx);

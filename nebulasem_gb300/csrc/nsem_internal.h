@@ -32,7 +32,7 @@ struct NsemDev {
     int32_t npx, npy, npz, np;
     int64_t n_elem, n_int, n_slot;
     /* physical constants */
-    double P0, R, gamma, gR, cv_heat, cp;
+    double P0, R, gamma, gR, cv_heat, cp, T0;
     double g[3];
     /* node arrays */
     double* jin;       /* [9][n_int] */

@@ -16,13 +16,22 @@
 struct NsemMixedBuf {
     bool ready = false;
     int64_t n_elem = 0;
-    /* per-element affine geometry and per-face data live here */
-    float* egeo = nullptr;       /* [n_elem*4] Jinv diagonal * cV-scale, see nsem_mixed.cu */
-    int32_t* nbr = nullptr;      /* [6][n_elem] neighbour element or -1 (wall) */
-    float* dmat = nullptr;       /* [3][npd*npd] D matrices, FP32 */
-    double* du[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  /* FP32-precision increments kept in FP64 buffers */
-    float* dl[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   /* FP32 stage increments */
+    int npd[3] = {0, 0, 0};
+    int n_layers = 0;
+    int cur = 0;                  /* which of U[0], U[1] holds u'^n      */
+    double* U[2][5] = {};         /* FP64 perturbation state, ping-pong   */
+    float* D[2][5] = {};          /* FP32 stage increments                */
+    int32_t* nbr = nullptr;       /* [6][n_elem] neighbour element, -1 wall */
+    float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h       */
+    int32_t* layer = nullptr;     /* [n_elem] background layer             */
+    float* bg = nullptr;          /* [layers][3][NP] rho_ref, rho_ref T0, p_ref */
+    void* tabs = nullptr;         /* host copy of the kernel tables        */
+    size_t tabs_size = 0;
 };
+
+/* u' <-> u conversion of the current state (to_pert: buf.u -> U[cur]) */
+int nsem_mixed_convert(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int to_pert,
+                       void* stream);
 
 nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMixedBuf* mb,
                              std::vector<void*>* allocs, std::string& err);
