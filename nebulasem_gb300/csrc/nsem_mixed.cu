@@ -47,17 +47,20 @@ struct MixedTabs {
 };
 
 struct StageArgs {
-    const double* U[5];        /* u'^n (FP64)                        */
-    const float* Din[5];       /* previous stage increment (or null) */
-    float* Dout[5];            /* stage increment out (stages 1, 2)  */
-    double* Unew[5];           /* u'^{n+1} (stage 3)                 */
-    double* L[5];              /* tendency out (stage 0)             */
-    const int32_t* nbr;        /* [6][n_elem]                        */
-    const float* J;            /* [3][n_elem]                        */
-    const int32_t* layer;      /* [n_elem]                           */
+    const double* U[5];        /* u'^n (FP64)                             */
+    const float* U32[5];       /* FP32 shadow of u'^n                     */
+    const float* Din[5];       /* previous stage increment (or null)      */
+    float* Dout[5];            /* stage increment out (stages 1, 2)       */
+    double* Unew[5];           /* u'^{n+1} (stage 3)                      */
+    float* U32new[5];          /* its FP32 shadow (stage 3)               */
+    double* L[5];              /* tendency out (stage 0)                  */
+    const int32_t* nbr;        /* [6][n_elem]                             */
+    const float* J;            /* [3][n_elem]                             */
+    const int32_t* layer;      /* [n_elem]                                */
     const float* bg;           /* [layers][3][NP]: rho_ref, Theta_ref, p_ref */
     int64_t n_elem;
     float dt, gamma, gR, g[3];
+    float eos[6];              /* binomial coefficients C(gamma, k), k = 1..6 */
     int stage;
     uint32_t* status;
 };
@@ -72,13 +75,58 @@ struct Geo {
     static constexpr int OFF_Z = 2 * NFX + (HAS_Y ? 2 * NFY : 0);
     static constexpr int NFS = OFF_Z + 2 * NFZ;
     static constexpr int BLOCK = ((NP > NFS ? NP : NFS) + 31) / 32 * 32;
-    /* dynamic shared memory: F[3][5][NP], P[13][NP], FF[5][NFS], Q[3][MAXN^2], meta[4] */
-    static constexpr size_t SMEM =
-        sizeof(float) * (15 * NP + 13 * NP + 5 * NFS + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD + 4);
+    /* dynamic shared memory (floats): flux F4[3][NP] (x4) + F1[3][NP],
+     * primitives P[4][NP] (x4), face fluxes FF4[NFS] (x4) + FF1[NFS],
+     * Q[3][MAXN^2], meta[4] */
+    /* every float4 region starts on a 16-byte boundary (offsets in floats
+     * rounded up to a multiple of 4) */
+    static constexpr int OFF_F1 = 12 * NP;
+    static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
+    static constexpr int OFF_FF4 = OFF_P + 16 * NP;
+    static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
+    static constexpr int OFF_Q = OFF_FF1 + NFS;
+    static constexpr int OFF_META = OFF_Q + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    static_assert(OFF_P % 4 == 0 && OFF_FF4 % 4 == 0, "float4 regions must be 16-byte aligned");
+    static constexpr size_t SMEM = sizeof(float) * (OFF_META + 4);
 };
 
-/* (1 + d)^gamma - 1, accurate relative to d */
-__device__ __forceinline__ float pow1m(float d, float gamma) {
+/* Exact-rounding conversions on the integer pipes.  GB300 executes F2F
+ * conversions on its (narrow) FP64 pipe; these use the ALU instead. */
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long sgn = b & 0x8000000000000000ull;
+    const unsigned long long m = b ^ sgn;
+    const unsigned long long r = m + 0x0fffffffull + ((m >> 29) & 1ull);  /* round to nearest even */
+    unsigned int f = (unsigned int)(r >> 29) - (896u << 23);               /* rebias exponent */
+    f = (m < 0x3810000000000000ull) ? 0u : f;                              /* below FLT_MIN: 0 */
+    f = (m >= 0x47effffff0000000ull) ? 0x7f800000u : f;                    /* overflow: inf   */
+    return __uint_as_float(f | (unsigned int)(sgn >> 32));
+}
+
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned int u = __float_as_uint(f);
+    const unsigned int sgn = u & 0x80000000u;
+    const unsigned int a = u ^ sgn;
+    unsigned int hi = (a >> 3) + (896u << 20);
+    unsigned int lo = a << 29;
+    hi = (a < 0x00800000u) ? 0u : hi;                                      /* zero, subnormal */
+    lo = (a < 0x00800000u) ? 0u : lo;
+    hi = (a >= 0x7f800000u) ? (0x7ff00000u | ((a >> 3) & 0xfffffu)) : hi;   /* inf, nan */
+    return __hiloint2double((int)(hi | sgn), (int)lo);
+}
+
+/* (1 + d)^gamma - 1, accurate relative to d: binomial series for |d| < 1/32
+ * (truncation < 1e-9 relative), log1p/expm1 otherwise */
+__device__ __forceinline__ float pow1m(float d, const float* c, float gamma) {
+    if (fabsf(d) < 0.03125f) {
+        float p = c[5];
+        p = fmaf(p, d, c[4]);
+        p = fmaf(p, d, c[3]);
+        p = fmaf(p, d, c[2]);
+        p = fmaf(p, d, c[1]);
+        p = fmaf(p, d, c[0]);
+        return p * d;
+    }
     return expm1f(gamma * log1pf(d));
 }
 
@@ -87,19 +135,49 @@ struct Prim {
     float rho, u0, u1, u2, th, pp, c, umag;
 };
 
-__device__ __forceinline__ Prim make_prim(float rp, float m0, float m1, float m2, float tp,
-                                          float rref, float tref, float pref, float gamma,
-                                          float gR) {
+__device__ __forceinline__ float safe_sqrt(float s) { return s > 0.0f ? s * rsqrtf(s) : 0.0f; }
+
+__device__ __forceinline__ Prim make_prim(const float* s, float rref, float tref, float pref,
+                                          const StageArgs& a) {
     Prim p;
-    p.rp = rp; p.m0 = m0; p.m1 = m1; p.m2 = m2; p.tp = tp;
-    p.rho = rref + rp;
-    const float inv = 1.0f / p.rho;
-    p.u0 = m0 * inv; p.u1 = m1 * inv; p.u2 = m2 * inv;
-    p.th = (tref + tp) * inv;
-    p.pp = pref * pow1m(tp / tref, gamma);
-    p.c = sqrtf(gR * p.th);
-    p.umag = sqrtf(p.u0 * p.u0 + p.u1 * p.u1 + p.u2 * p.u2);
+    p.rp = s[0]; p.m0 = s[1]; p.m1 = s[2]; p.m2 = s[3]; p.tp = s[4];
+    p.rho = rref + p.rp;
+    const float inv = __frcp_rn(p.rho);
+    p.u0 = p.m0 * inv; p.u1 = p.m1 * inv; p.u2 = p.m2 * inv;
+    p.th = (tref + p.tp) * inv;
+    p.pp = pref * pow1m(p.tp * __frcp_rn(tref), a.eos, a.gamma);
+    p.c = safe_sqrt(a.gR * p.th);
+    p.umag = safe_sqrt(p.u0 * p.u0 + p.u1 * p.u1 + p.u2 * p.u2);
     return p;
+}
+
+template <int NX, int NY, int NZ>
+struct FaceSlot {
+    int dir, side, la, lo, face;
+};
+
+template <int NX, int NY, int NZ>
+__device__ __forceinline__ FaceSlot<NX, NY, NZ> face_slot(int t) {
+    using G = Geo<NX, NY, NZ>;
+    int dir, side, s0, s1;
+    if (t < G::OFF_Y) {
+        dir = 0; side = t / G::NFX; const int r = t % G::NFX; s0 = r / NZ; s1 = r % NZ;
+    } else if (t < G::OFF_Z) {
+        dir = 1; const int q = t - G::OFF_Y; side = q / G::NFY; const int r = q % G::NFY;
+        s0 = r / NZ; s1 = r % NZ;
+    } else {
+        dir = 2; const int q = t - G::OFF_Z; side = q / G::NFZ; const int r = q % G::NFZ;
+        s0 = r / NY; s1 = r % NY;
+    }
+    int i, j, k, io, jo, ko;
+    if (dir == 0) { i = side ? NX - 1 : 0; j = s0; k = s1; io = side ? 0 : NX - 1; jo = j; ko = k; }
+    else if (dir == 1) { i = s0; j = side ? NY - 1 : 0; k = s1; io = i; jo = side ? 0 : NY - 1; ko = k; }
+    else { i = s0; j = s1; k = side ? NZ - 1 : 0; io = i; jo = j; ko = side ? 0 : NZ - 1; }
+    FaceSlot<NX, NY, NZ> f;
+    f.dir = dir; f.side = side; f.face = 2 * dir + side;
+    f.la = (i * NY + j) * NZ + k;
+    f.lo = (io * NY + jo) * NZ + ko;
+    return f;
 }
 
 template <int NX, int NY, int NZ>
@@ -108,176 +186,198 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
     using G = Geo<NX, NY, NZ>;
     constexpr int NP = G::NP;
     constexpr int NFS = G::NFS;
-    /* shared: volume fluxes F[dir][var][node], primitives for the faces,
-     * face fluxes, tables */
-    extern __shared__ float smem[];
-    float(*sF)[5][NP] = reinterpret_cast<float(*)[5][NP]>(smem);
-    float(*sP)[NP] = reinterpret_cast<float(*)[NP]>(smem + 15 * NP);
-    float(*sFF)[NFS] = reinterpret_cast<float(*)[NFS]>(smem + 28 * NP);
-    float(*sQ)[MAXN * MAXN] = reinterpret_cast<float(*)[MAXN * MAXN]>(smem + 28 * NP + 5 * NFS);
-    float* sMeta = smem + 28 * NP + 5 * NFS + 3 * MAXN * MAXN;
+    extern __shared__ float4 smem4[];
+    float* smem = reinterpret_cast<float*>(smem4);
+    float4* sF4 = smem4;                                   /* [3][NP] */
+    float* sF1 = smem + G::OFF_F1;                         /* [3][NP] */
+    float4* sP = reinterpret_cast<float4*>(smem + G::OFF_P);     /* [4][NP] */
+    float4* sFF4 = reinterpret_cast<float4*>(smem + G::OFF_FF4); /* [NFS] */
+    float* sFF1 = smem + G::OFF_FF1;                       /* [NFS] */
+    float* sQ = smem + G::OFF_Q;
+    float* sMeta = smem + G::OFF_META;
 
     const int t = threadIdx.x;
     const int64_t e = blockIdx.x;
-    for (int q = t; q < 3 * MAXN * MAXN; q += blockDim.x) (&sQ[0][0])[q] = (&tab.Q[0][0])[q];
-    if (t < 3) sMeta[t] = a.J[(int64_t)t * a.n_elem + e];
+    const bool has_din = a.Din[0] != nullptr;
 
-    const int lay = a.layer[e];
-    const float* bg = a.bg + (int64_t)lay * 3 * NP;
-
-    /* phase 1: own node */
+    /* issue every global load first: own node, face neighbour, stage-3 FP64 */
+    float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[3] = {0, 0, 0};
+    double u64[5];
     if (t < NP) {
         const int64_t n = e * NP + t;
-        float s[5];
-        for (int v = 0; v < 5; v++) {
-            float x = (float)a.U[v][n];
-            if (a.Din[0]) x += a.Din[v][n];
-            s[v] = x;
+#pragma unroll
+        for (int v = 0; v < 5; v++) own[v] = __ldg(a.U32[v] + n);
+        if (has_din) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) {
+                din[v] = __ldg(a.Din[v] + n);
+                own[v] += din[v];
+            }
         }
-        const Prim p = make_prim(s[0], s[1], s[2], s[3], s[4], bg[t], bg[NP + t], bg[2 * NP + t],
-                                 a.gamma, a.gR);
-        sP[0][t] = p.rp; sP[1][t] = p.m0; sP[2][t] = p.m1; sP[3][t] = p.m2; sP[4][t] = p.tp;
-        sP[5][t] = p.rho; sP[6][t] = p.u0; sP[7][t] = p.u1; sP[8][t] = p.u2;
-        sP[9][t] = p.th; sP[10][t] = p.pp; sP[11][t] = p.c; sP[12][t] = p.umag;
+        const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 3 * NP;
+        bgs[0] = __ldg(bg + t); bgs[1] = __ldg(bg + NP + t); bgs[2] = __ldg(bg + 2 * NP + t);
+        if (a.stage == 3) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) u64[v] = __ldg(a.U[v] + n);
+        }
+    }
+    FaceSlot<NX, NY, NZ> fs;
+    int32_t nb = -1;
+    float oth[5], bgo[3];
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if (nb >= 0) {
+            const int64_t n = (int64_t)nb * NP + fs.lo;
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(a.U32[v] + n);
+            if (has_din) {
+#pragma unroll
+                for (int v = 0; v < 5; v++) oth[v] += __ldg(a.Din[v] + n);
+            }
+            const float* bg = a.bg + (int64_t)__ldg(a.layer + nb) * 3 * NP;
+            bgo[0] = __ldg(bg + fs.lo); bgo[1] = __ldg(bg + NP + fs.lo); bgo[2] = __ldg(bg + 2 * NP + fs.lo);
+        }
+    }
+    for (int q = t; q < 3 * MAXN * MAXN; q += blockDim.x) sQ[q] = (&tab.Q[0][0])[q];
+    if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
+
+    /* phase 1: own node primitives and volume fluxes */
+    if (t < NP) {
+        const Prim p = make_prim(own, bgs[0], bgs[1], bgs[2], a);
+        sP[t] = make_float4(p.rp, p.m0, p.m1, p.m2);
+        sP[NP + t] = make_float4(p.tp, p.rho, p.u0, p.u1);
+        sP[2 * NP + t] = make_float4(p.u2, p.th, p.pp, p.c);
+        sP[3 * NP + t] = make_float4(p.umag, 0.0f, 0.0f, 0.0f);
         const float u[3] = {p.u0, p.u1, p.u2};
         const float m[3] = {p.m0, p.m1, p.m2};
+#pragma unroll
         for (int d = 0; d < 3; d++) {
-            sF[d][0][t] = m[d];
-            sF[d][1][t] = m[0] * u[d] + (d == 0 ? p.pp : 0.0f);
-            sF[d][2][t] = m[1] * u[d] + (d == 1 ? p.pp : 0.0f);
-            sF[d][3][t] = m[2] * u[d] + (d == 2 ? p.pp : 0.0f);
-            sF[d][4][t] = m[d] * p.th;
+            sF4[d * NP + t] = make_float4(m[d], fmaf(m[0], u[d], d == 0 ? p.pp : 0.0f),
+                                          fmaf(m[1], u[d], d == 1 ? p.pp : 0.0f),
+                                          fmaf(m[2], u[d], d == 2 ? p.pp : 0.0f));
+            sF1[d * NP + t] = m[d] * p.th;
         }
     }
     __syncthreads();
 
-    /* phase 2: face nodes */
+    /* phase 2: Rusanov flux on every face node */
     if (t < NFS) {
-        int dir, side, s0, s1;  /* side: 0 low face, 1 high face; (s0,s1) in-face coords */
-        if (t < G::OFF_Y) {
-            dir = 0; side = t / G::NFX; const int r = t % G::NFX; s0 = r / NZ; s1 = r % NZ;
-        } else if (t < G::OFF_Z) {
-            dir = 1; const int q = t - G::OFF_Y; side = q / G::NFY; const int r = q % G::NFY;
-            s0 = r / NZ; s1 = r % NZ;
-        } else {
-            dir = 2; const int q = t - G::OFF_Z; side = q / G::NFZ; const int r = q % G::NFZ;
-            s0 = r / NY; s1 = r % NY;
-        }
-        int i, j, k, io, jo, ko;
-        if (dir == 0) { i = side ? NX - 1 : 0; j = s0; k = s1; io = side ? 0 : NX - 1; jo = j; ko = k; }
-        else if (dir == 1) { i = s0; j = side ? NY - 1 : 0; k = s1; io = i; jo = side ? 0 : NY - 1; ko = k; }
-        else { i = s0; j = s1; k = side ? NZ - 1 : 0; io = i; jo = j; ko = side ? 0 : NZ - 1; }
-        const int la = (i * NY + j) * NZ + k;
-        const int face = 2 * dir + side;
-        const int32_t nb = a.nbr[(int64_t)face * a.n_elem + e];
-        const float sg = side ? 1.0f : -1.0f;   /* outward normal = sg e_dir */
+        const int dir = fs.dir;
+        const float sg = fs.side ? 1.0f : -1.0f;   /* outward normal = sg e_dir */
+        const float4 P0 = sP[fs.la], P1 = sP[NP + fs.la], P2 = sP[2 * NP + fs.la], P3 = sP[3 * NP + fs.la];
         Prim S;
-        S.rp = sP[0][la]; S.m0 = sP[1][la]; S.m1 = sP[2][la]; S.m2 = sP[3][la]; S.tp = sP[4][la];
-        S.rho = sP[5][la]; S.u0 = sP[6][la]; S.u1 = sP[7][la]; S.u2 = sP[8][la];
-        S.th = sP[9][la]; S.pp = sP[10][la]; S.c = sP[11][la]; S.umag = sP[12][la];
+        S.rp = P0.x; S.m0 = P0.y; S.m1 = P0.z; S.m2 = P0.w;
+        S.tp = P1.x; S.rho = P1.y; S.u0 = P1.z; S.u1 = P1.w;
+        S.u2 = P2.x; S.th = P2.y; S.pp = P2.z; S.c = P2.w; S.umag = P3.x;
         Prim O;
         if (nb >= 0) {
-            const int lo = (io * NY + jo) * NZ + ko;
-            const int64_t n = (int64_t)nb * NP + lo;
-            float s[5];
-            for (int v = 0; v < 5; v++) {
-                float x = (float)a.U[v][n];
-                if (a.Din[0]) x += a.Din[v][n];
-                s[v] = x;
-            }
-            const float* bgo = a.bg + (int64_t)a.layer[nb] * 3 * NP;
-            O = make_prim(s[0], s[1], s[2], s[3], s[4], bgo[lo], bgo[NP + lo], bgo[2 * NP + lo],
-                          a.gamma, a.gR);
+            O = make_prim(oth, bgo[0], bgo[1], bgo[2], a);
         } else {
             /* wall ghost: NEUMANN for rho, theta, p; SYMMETRY velocity
              * (tangential projection rescaled to |U|, tensor.h:486-494) */
             O = S;
-            float r[3] = {S.u0, S.u1, S.u2};
-            r[dir] = 0.0f;
-            const float mr = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            float r0 = dir == 0 ? 0.0f : S.u0;
+            float r1 = dir == 1 ? 0.0f : S.u1;
+            float r2 = dir == 2 ? 0.0f : S.u2;
+            const float mr = safe_sqrt(r0 * r0 + r1 * r1 + r2 * r2);
             if (mr > 1e-7f) {
                 const float sc = S.umag / mr;
-                r[0] *= sc; r[1] *= sc; r[2] *= sc;
+                r0 *= sc; r1 *= sc; r2 *= sc;
             }
-            O.u0 = r[0]; O.u1 = r[1]; O.u2 = r[2];
-            O.m0 = O.rho * r[0]; O.m1 = O.rho * r[1]; O.m2 = O.rho * r[2];
-            O.umag = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            O.u0 = r0; O.u1 = r1; O.u2 = r2;
+            O.m0 = O.rho * r0; O.m1 = O.rho * r1; O.m2 = O.rho * r2;
+            O.umag = safe_sqrt(r0 * r0 + r1 * r1 + r2 * r2);
         }
-        const float us[3] = {S.u0, S.u1, S.u2}, uo[3] = {O.u0, O.u1, O.u2};
-        const float ms[3] = {S.m0, S.m1, S.m2}, mo[3] = {O.m0, O.m1, O.m2};
-        const float uns = sg * us[dir], uno = sg * uo[dir];
+        /* Canonical orientation: L is the element below the face along +e_dir,
+         * R the one above (the ghost on a wall).  Both elements of an interior
+         * face evaluate the same expression on the same (L, R) data, so their
+         * fluxes are bit-identical and the face conserves exactly. */
+        const bool self_low = fs.side == 1;
+        const Prim& Lp = self_low ? S : O;
+        const Prim& Rp = self_low ? O : S;
         /* face average with the reference's weights (field.h:2888-2890, fI of
          * field.cpp:257-266): 1/2 inside, the ghost value alone on a wall */
-        const float ws = (nb >= 0) ? 0.5f : 0.0f, wo = (nb >= 0) ? 0.5f : 1.0f;
-        /* sums of two products are rounded explicitly (no contraction), so the
-         * two elements of a face get exactly opposite fluxes */
-        const float lam = 0.5f * __fadd_rn(__fadd_rn(__fmul_rn(ws, S.umag), __fmul_rn(wo, O.umag)),
-                                           __fadd_rn(__fmul_rn(ws, S.c), __fmul_rn(wo, O.c)));
-        /* F* . n_out = avg(F) . n_out - lam (q_other - q_self) (normal part only
-         * for momentum), field.h:2928-2943 */
-        const float fr = __fadd_rn(__fmul_rn(ws, S.rho * uns), __fmul_rn(wo, O.rho * uno)) -
-                         lam * (O.rp - S.rp);
+        float wL = 0.5f, wR = 0.5f;
+        if (nb < 0) { wL = self_low ? 0.0f : 1.0f; wR = 1.0f - wL; }
+        const float uL = dir == 0 ? Lp.u0 : dir == 1 ? Lp.u1 : Lp.u2;
+        const float uR = dir == 0 ? Rp.u0 : dir == 1 ? Rp.u1 : Rp.u2;
+        const float lam = 0.5f * ((wL * Lp.umag + wR * Rp.umag) + (wL * Lp.c + wR * Rp.c));
+        /* F* . e_dir = avg(F) . e_dir - lam (q_R - q_L) (normal component only for
+         * momentum), field.h:2928-2943; the self element takes sg * F* */
+        const float fr = (wL * (Lp.rho * uL) + wR * (Rp.rho * uR)) - lam * (Rp.rp - Lp.rp);
+        const float mL[3] = {Lp.m0, Lp.m1, Lp.m2}, mR[3] = {Rp.m0, Rp.m1, Rp.m2};
         float fm[3];
+#pragma unroll
         for (int c = 0; c < 3; c++) {
-            const float pn = (c == dir) ? sg : 0.0f;
-            const float fs = __fadd_rn(__fmul_rn(ms[c], uns), __fmul_rn(S.pp, pn));
-            const float fo = __fadd_rn(__fmul_rn(mo[c], uno), __fmul_rn(O.pp, pn));
-            fm[c] = __fadd_rn(__fmul_rn(ws, fs), __fmul_rn(wo, fo));
+            const float pL = (c == dir) ? Lp.pp : 0.0f, pR = (c == dir) ? Rp.pp : 0.0f;
+            fm[c] = wL * fmaf(mL[c], uL, pL) + wR * fmaf(mR[c], uR, pR);
+            if (c == dir) fm[c] -= lam * (mR[c] - mL[c]);
         }
-        fm[dir] -= lam * (mo[dir] - ms[dir]);
-        const float ft = __fadd_rn(__fmul_rn(ws, S.rho * uns * S.th), __fmul_rn(wo, O.rho * uno * O.th)) -
-                         lam * (O.tp - S.tp);
-        sFF[0][t] = fr; sFF[1][t] = fm[0]; sFF[2][t] = fm[1]; sFF[3][t] = fm[2]; sFF[4][t] = ft;
+        const float ft = (wL * (Lp.rho * uL * Lp.th) + wR * (Rp.rho * uR * Rp.th)) - lam * (Rp.tp - Lp.tp);
+        const float fr_o = sg * fr, ft_o = sg * ft;
+        fm[0] *= sg; fm[1] *= sg; fm[2] *= sg;
+        sFF4[t] = make_float4(fr_o, fm[0], fm[1], fm[2]);
+        sFF1[t] = ft_o;
     }
     __syncthreads();
 
-    /* phase 3: own node residual and update */
+    /* phase 3: weak volume term (line sums with Q), lift, buoyancy, update */
     if (t >= NP) return;
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
-    float Lv[5] = {0, 0, 0, 0, 0};
+    float L0, L1, L2, L3, L4;
     {
-        float acc[5] = {0, 0, 0, 0, 0};
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
 #pragma unroll
         for (int m = 0; m < NX; m++) {
-            const float q = sQ[0][i * MAXN + m];
+            const float q = sQ[i * MAXN + m];
             const int b = (m * NY + j) * NZ + k;
-#pragma unroll
-            for (int v = 0; v < 5; v++) acc[v] = fmaf(q, sF[0][v][b], acc[v]);
+            const float4 f = sF4[b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sF1[b], acc1);
         }
         const float Jx = sMeta[0];
-#pragma unroll
-        for (int v = 0; v < 5; v++) Lv[v] = Jx * acc[v];
+        L0 = Jx * acc.x; L1 = Jx * acc.y; L2 = Jx * acc.z; L3 = Jx * acc.w; L4 = Jx * acc1;
     }
     if (NY > 1) {
-        float acc[5] = {0, 0, 0, 0, 0};
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
 #pragma unroll
         for (int m = 0; m < NY; m++) {
-            const float q = sQ[1][j * MAXN + m];
+            const float q = sQ[MAXN * MAXN + j * MAXN + m];
             const int b = (i * NY + m) * NZ + k;
-#pragma unroll
-            for (int v = 0; v < 5; v++) acc[v] = fmaf(q, sF[1][v][b], acc[v]);
+            const float4 f = sF4[NP + b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sF1[NP + b], acc1);
         }
         const float Jy = sMeta[1];
-#pragma unroll
-        for (int v = 0; v < 5; v++) Lv[v] = fmaf(Jy, acc[v], Lv[v]);
+        L0 = fmaf(Jy, acc.x, L0); L1 = fmaf(Jy, acc.y, L1); L2 = fmaf(Jy, acc.z, L2);
+        L3 = fmaf(Jy, acc.w, L3); L4 = fmaf(Jy, acc1, L4);
     }
     {
-        float acc[5] = {0, 0, 0, 0, 0};
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
 #pragma unroll
         for (int m = 0; m < NZ; m++) {
-            const float q = sQ[2][k * MAXN + m];
+            const float q = sQ[2 * MAXN * MAXN + k * MAXN + m];
             const int b = (i * NY + j) * NZ + m;
-#pragma unroll
-            for (int v = 0; v < 5; v++) acc[v] = fmaf(q, sF[2][v][b], acc[v]);
+            const float4 f = sF4[2 * NP + b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sF1[2 * NP + b], acc1);
         }
         const float Jz = sMeta[2];
-#pragma unroll
-        for (int v = 0; v < 5; v++) Lv[v] = fmaf(Jz, acc[v], Lv[v]);
+        L0 = fmaf(Jz, acc.x, L0); L1 = fmaf(Jz, acc.y, L1); L2 = fmaf(Jz, acc.z, L2);
+        L3 = fmaf(Jz, acc.w, L3); L4 = fmaf(Jz, acc1, L4);
     }
     /* surface lift: -(J_d / w_end) F*.n_out for each face through the node */
     auto lift = [&](int slot, float coef) {
-#pragma unroll
-        for (int v = 0; v < 5; v++) Lv[v] = fmaf(-coef, sFF[v][slot], Lv[v]);
+        const float4 f = sFF4[slot];
+        L0 = fmaf(-coef, f.x, L0); L1 = fmaf(-coef, f.y, L1); L2 = fmaf(-coef, f.z, L2);
+        L3 = fmaf(-coef, f.w, L3); L4 = fmaf(-coef, sFF1[slot], L4);
     };
     const float cx = sMeta[0] * tab.lift[0], cy = sMeta[1] * tab.lift[1], cz = sMeta[2] * tab.lift[2];
     if (i == 0) lift(G::OFF_X + j * NZ + k, cx);
@@ -289,15 +389,16 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
     if (k == 0) lift(G::OFF_Z + i * NY + j, cz);
     if (k == NZ - 1) lift(G::OFF_Z + G::NFZ + i * NY + j, cz);
     /* buoyancy (rho - rho_ref) g */
-    const float rp = sP[0][t];
-    Lv[1] = fmaf(rp, a.g[0], Lv[1]);
-    Lv[2] = fmaf(rp, a.g[1], Lv[2]);
-    Lv[3] = fmaf(rp, a.g[2], Lv[3]);
+    const float rp = own[0];
+    L1 = fmaf(rp, a.g[0], L1);
+    L2 = fmaf(rp, a.g[1], L2);
+    L3 = fmaf(rp, a.g[2], L3);
+    const float Lv[5] = {L0, L1, L2, L3, L4};
 
     const int64_t n = e * NP + t;
     if (a.stage == 0) {
 #pragma unroll
-        for (int v = 0; v < 5; v++) a.L[v][n] = (double)Lv[v];
+        for (int v = 0; v < 5; v++) a.L[v][n] = f2d(Lv[v]);
         return;
     }
     const float dt = a.dt;
@@ -306,15 +407,17 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
         for (int v = 0; v < 5; v++) a.Dout[v][n] = dt * Lv[v];
     } else if (a.stage == 2) {
 #pragma unroll
-        for (int v = 0; v < 5; v++) a.Dout[v][n] = 0.25f * fmaf(dt, Lv[v], a.Din[v][n]);
+        for (int v = 0; v < 5; v++) a.Dout[v][n] = 0.25f * fmaf(dt, Lv[v], din[v]);
     } else {
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], a.Din[v][n]);
-            const double un = a.U[v][n] + (double)D;
+            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], din[v]);
+            const double un = u64[v] + f2d(D);
             a.Unew[v][n] = un;
-            finite = finite && isfinite(un);
+            a.U32new[v][n] = d2f_rn(un);
+            /* exponent field all ones = inf or nan (integer test, no FP64 op) */
+            finite = finite && ((__double2hiint(un) & 0x7ff00000) != 0x7ff00000);
         }
         if (!finite) atomicOr(a.status, NSEM_STATUS_NONFINITE);
     }
@@ -325,8 +428,12 @@ struct Ptr5 {
     double* p[5];
 };
 
-__global__ void k_convert(Ptr5 src, Ptr5 dst, const double* rho_ref, double T0, int64_t n,
-                          int to_pert) {
+struct FPtr5 {
+    float* p[5];
+};
+
+__global__ void k_convert(Ptr5 src, Ptr5 dst, FPtr5 shadow, const double* rho_ref, double T0,
+                          int64_t n, int to_pert) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         /* explicitly rounded: rho_ref T0 must round as on the host (no FMA) */
@@ -342,6 +449,8 @@ __global__ void k_convert(Ptr5 src, Ptr5 dst, const double* rho_ref, double T0, 
         dst.p[1][i] = src.p[1][i];
         dst.p[2][i] = src.p[2][i];
         dst.p[3][i] = src.p[3][i];
+        if (to_pert)
+            for (int v = 0; v < 5; v++) shadow.p[v][i] = d2f_rn(dst.p[v][i]);
     }
 }
 
@@ -553,11 +662,13 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
     for (int s = 0; s < 2; s++)
         for (int v = 0; v < 5; v++) {
             if (cudaMalloc((void**)&mb->U[s][v], n_int * sizeof(double)) != cudaSuccess ||
+                cudaMalloc((void**)&mb->U32[s][v], n_int * sizeof(float)) != cudaSuccess ||
                 cudaMalloc((void**)&mb->D[s][v], n_int * sizeof(float)) != cudaSuccess) {
                 err = "precision form: device allocation failed";
                 return NSEM_NO_MEMORY;
             }
             allocs->push_back(mb->U[s][v]);
+            allocs->push_back(mb->U32[s][v]);
             allocs->push_back(mb->D[s][v]);
         }
     if (prepare(NX, NY, NZ) != 0) {
@@ -580,6 +691,8 @@ StageArgs stage_args(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage
     StageArgs a{};
     for (int v = 0; v < 5; v++) {
         a.U[v] = mb->U[cur][v];
+        a.U32[v] = mb->U32[cur][v];
+        a.U32new[v] = mb->U32[cur ^ 1][v];
         a.Din[v] = (stage == 2) ? mb->D[0][v] : (stage == 3) ? mb->D[1][v] : nullptr;
         a.Dout[v] = (stage == 1) ? mb->D[0][v] : (stage == 2) ? mb->D[1][v] : nullptr;
         a.Unew[v] = mb->U[cur ^ 1][v];
@@ -594,6 +707,12 @@ StageArgs stage_args(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage
     a.gamma = (float)dev->gamma;
     a.gR = (float)dev->gR;
     for (int c = 0; c < 3; c++) a.g[c] = (float)dev->g[c];
+    /* binomial coefficients C(gamma, k) of (1 + d)^gamma - 1 */
+    double ck = 1.0;
+    for (int k = 1; k <= 6; k++) {
+        ck *= (dev->gamma - (k - 1)) / k;
+        a.eos[k - 1] = (float)ck;
+    }
     a.stage = stage;
     a.status = dev->status;
     return a;
@@ -616,16 +735,18 @@ int grid_for(int64_t n) {
 int nsem_mixed_convert(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int to_pert,
                        void* stream) {
     Ptr5 full, pert;
+    FPtr5 shadow;
     for (int v = 0; v < 5; v++) {
         full.p[v] = b->u[v];
         pert.p[v] = mb->U[mb->cur][v];
+        shadow.p[v] = mb->U32[mb->cur][v];
     }
     if (to_pert)
-        k_convert<<<grid_for(dev->n_int), 256, 0, (cudaStream_t)stream>>>(full, pert, dev->rho_ref,
-                                                                          dev->T0, dev->n_int, 1);
+        k_convert<<<grid_for(dev->n_int), 256, 0, (cudaStream_t)stream>>>(
+            full, pert, shadow, dev->rho_ref, dev->T0, dev->n_int, 1);
     else
-        k_convert<<<grid_for(dev->n_int), 256, 0, (cudaStream_t)stream>>>(pert, full, dev->rho_ref,
-                                                                          dev->T0, dev->n_int, 0);
+        k_convert<<<grid_for(dev->n_int), 256, 0, (cudaStream_t)stream>>>(
+            pert, full, shadow, dev->rho_ref, dev->T0, dev->n_int, 0);
     return (int)cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@ struct NsemMixedBuf {
     int n_layers = 0;
     int cur = 0;                  /* which of U[0], U[1] holds u'^n      */
     double* U[2][5] = {};         /* FP64 perturbation state, ping-pong   */
+    float* U32[2][5] = {};        /* FP32 shadow of U (read by the stages) */
     float* D[2][5] = {};          /* FP32 stage increments                */
     int32_t* nbr = nullptr;       /* [6][n_elem] neighbour element, -1 wall */
     float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h       */
