@@ -140,6 +140,25 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
  * 263-274) with compensated summation; gh = g . cC. */
 nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double* volume);
 
+/* Discrete adjoint of the plain (FP64) form.  No reference counterpart: the
+ * reference has no adjoint or tangent-linear model.
+ *
+ * nsem_vjp: g = J_L(u)^T w for the current state u (w, g: five host arrays
+ * of n_int doubles, SoA rho, rho u, rho v, rho w, rho theta).
+ *
+ * nsem_forward_checkpointed: advance the state by nsteps SSP-RK3 steps (FP64)
+ * keeping device checkpoints of the state every ckpt_every steps.
+ * nsem_adjoint: given lam_final = dJ/du at the final state of the last
+ * nsem_forward_checkpointed call, return lam0 = dJ/du at its initial state
+ * (reverse Shu-Osher sweep, each segment recomputed from its checkpoint with
+ * its stage states kept).  The context's state is left at the final state.
+ * ms_fwd / ms_adj (optional) receive the device time of the forward pass and
+ * of the reverse sweep. */
+nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]);
+nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every, double* ms_fwd);
+nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double* const lam0[5],
+                         double* ms_adj);
+
 /* Measurement helper: run nsteps SSP-RK3 steps launch by launch (no graph)
  * with CUDA events on the context's stream around every kernel, and report
  * per kernel class the summed device time in ms, the launch count and the

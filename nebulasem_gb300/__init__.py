@@ -82,6 +82,9 @@ def load(build_if_missing=True):
         "nsem_diagnostics": ([P, P, P, P], ctypes.c_int),
         "nsem_sync": ([P], ctypes.c_int),
         "nsem_profile": ([P, ctypes.c_int, ctypes.c_int, P, P, P], ctypes.c_int),
+        "nsem_vjp": ([P, vp, vp], ctypes.c_int),
+        "nsem_forward_checkpointed": ([P, ctypes.c_int, ctypes.c_int, P], ctypes.c_int),
+        "nsem_adjoint": ([P, vp, vp, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -214,6 +217,35 @@ class Solver:
             if nm:
                 out[nm] = (ms[i], cnt[i])
         return out
+
+    def vjp(self, w):
+        """g = J_L(u)^T w at the current state (plain form)."""
+        n = self.n_int
+        ws = [_f64(a) for a in w]
+        g = [np.empty(n) for _ in range(5)]
+        wa = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in ws])
+        ga = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in g])
+        self._check(self._lib.nsem_vjp(self._ctx, wa, ga))
+        return g
+
+    def forward_checkpointed(self, nsteps, ckpt_every):
+        """Advance nsteps FP64 steps keeping checkpoints; returns device ms."""
+        ms = ctypes.c_double()
+        self._check(self._lib.nsem_forward_checkpointed(self._ctx, int(nsteps), int(ckpt_every),
+                                                        ctypes.byref(ms)))
+        return ms.value
+
+    def adjoint(self, lam_final):
+        """dJ/du0 from dJ/du_final for the last checkpointed forward run.
+        Returns (lam0, device ms of the reverse sweep)."""
+        n = self.n_int
+        ls = [_f64(a) for a in lam_final]
+        out = [np.empty(n) for _ in range(5)]
+        la = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in ls])
+        oa = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in out])
+        ms = ctypes.c_double()
+        self._check(self._lib.nsem_adjoint(self._ctx, la, oa, ctypes.byref(ms)))
+        return out, ms.value
 
     def get_state(self):
         n = self.n_int

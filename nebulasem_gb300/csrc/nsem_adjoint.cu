@@ -1,0 +1,385 @@
+/*
+ * Discrete adjoint of the FP64 dGSEM Euler tendency and of the SSP-RK3 step.
+ *
+ * Vector-Jacobian product g = J_L(v)^T w of the operator chain of the plain
+ * form (nsem_fp64.cu; reference: euler.cpp:181-258, field.h:2881-2943,
+ * 3086-3117, 3417-3478), hand-derived in reverse mode:
+ *   r = -cV L                     ->  rbar = -w / cV
+ *   source  r_m -= g (rho - rho_ref) cV
+ *   volume  r[a] -= F_b . (Jin_b dpsi(b->a))  -> Fbar_b = -sum_a rbar[a] (x) dj(b->a)
+ *           (the transposed line contraction, gathered per source node b)
+ *   lift    r[c1] += d_k, r[c2] -= d_k         -> dbar_k = rbar[c1] - rbar[c2]
+ *   Rusanov d = (cds F - n^ (x) lambda dq) . fN, lambda = (cds|U| + cds c) / 2
+ *   ghosts  NEUMANN copies, SYMMETRY velocity (tangential projection
+ *           rescaled to |U|, tensor.h:486-494), adjoint folded into the owner
+ *   EOS     p = P0 (rho theta R / P0)^gamma -> dp/drho = gamma p / rho,
+ *                                              dp/dtheta = gamma p / theta
+ * Non-smooth points take the one-sided choice of the value's branch
+ * (d|U| = U/|U|, 0 at U = 0; the SYMMETRY threshold |r| <= 1e-7 as forward).
+ *
+ * Kernels: k_adj_face (per used slot: adjoint of the face flux for both
+ * sides, in primitive variables), k_adj_volume (per element, thread per node:
+ * transposed volume gather, source, face contributions gathered through the
+ * lift lists, primitive -> conserved chain rule).  FP64 throughout; this file
+ * may use FMA contraction (the adjoint is checked to 1e-6, not bitwise).
+ */
+#include <cuda_runtime.h>
+
+#include "nsem_adjoint.h"
+
+namespace {
+
+enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
+constexpr int NPA = 6;   /* primitive adjoints per side: rho, U0, U1, U2, theta, p' */
+
+__device__ __forceinline__ double vdot3(const double* a, const double* b) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+struct NodePrim {
+    double r, U[3], T, p, pp, mu, c;   /* p: full pressure, pp = p - p_ref */
+};
+
+__device__ __forceinline__ NodePrim node_prim(const NsemDev& m, const double* const* S, int64_t i) {
+    NodePrim q;
+    q.r = S[0][i];
+    q.U[0] = S[1][i] / q.r;
+    q.U[1] = S[2][i] / q.r;
+    q.U[2] = S[3][i] / q.r;
+    q.T = S[4][i] / q.r;
+    q.p = m.P0 * pow(((q.r * q.T) * m.R) / m.P0, m.gamma);
+    q.pp = q.p - m.p_ref[i];
+    q.mu = sqrt(vdot3(q.U, q.U));
+    q.c = sqrt(m.gR * q.T);
+    return q;
+}
+
+/* ghost velocity of the SYMMETRY condition and the transpose of its
+ * Jacobian applied to gbar (adds into ubar) */
+__device__ __forceinline__ void sym_fwd(const double* p, const double* en, double* out, double* r,
+                                        double& magR, double& magP, bool& scaled) {
+    const double dn = vdot3(p, en);
+    r[0] = p[0] - en[0] * dn;
+    r[1] = p[1] - en[1] * dn;
+    r[2] = p[2] - en[2] * dn;
+    magR = sqrt(vdot3(r, r));
+    magP = sqrt(vdot3(p, p));
+    scaled = !(fabs(magR) <= 1e-7);
+    const double s = scaled ? magP / magR : 1.0;
+    out[0] = r[0] * s; out[1] = r[1] * s; out[2] = r[2] * s;
+}
+
+__device__ __forceinline__ void sym_vjp(const double* p, const double* en, const double* r,
+                                        double magR, double magP, bool scaled, const double* gbar,
+                                        double* ubar) {
+    /* out = A p s, A = I - en en^T (symmetric), s = |p| / |A p| */
+    double Ag[3];
+    const double gn = vdot3(gbar, en);
+    Ag[0] = gbar[0] - en[0] * gn;
+    Ag[1] = gbar[1] - en[1] * gn;
+    Ag[2] = gbar[2] - en[2] * gn;
+    if (!scaled) {
+        ubar[0] += Ag[0]; ubar[1] += Ag[1]; ubar[2] += Ag[2];
+        return;
+    }
+    const double s = magP / magR;
+    const double rg = vdot3(r, gbar);        /* d out = A dp s + r ds */
+    /* ds = (p . dp) / (|p| |r|) - |p| (r . A dp) / |r|^3 ; A r = r */
+    const double c1 = (magP > 0) ? rg / (magP * magR) : 0.0;
+    const double c2 = rg * magP / (magR * magR * magR);
+    for (int k = 0; k < 3; k++) ubar[k] += s * Ag[k] + c1 * p[k] - c2 * r[k];
+}
+
+struct FaceAdjArgs {
+    const double* S[5];      /* state v */
+    const double* W[5];      /* w = adjoint of L */
+    double* adjO[NPA];       /* per slot, owner side primitive adjoints */
+    double* adjN[NPA];       /* per slot, neighbour side (0 for ghosts) */
+};
+
+__global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double nmag = sqrt(vdot3(n, n));
+    const double fi = m.fi[k], fo = 1 - fi;
+
+    const NodePrim P1 = node_prim(m, a.S, c1);
+    NodePrim P2;
+    double rsym[3] = {0, 0, 0}, magR = 0, magP = 0;
+    bool scaled = false;
+    if (c2 >= 0) {
+        P2 = node_prim(m, a.S, c2);
+    } else {
+        P2 = P1;
+        if (m.bc[k] == 2) sym_fwd(P1.U, en, P2.U, rsym, magR, magP, scaled);
+        P2.mu = sqrt(vdot3(P2.U, P2.U));
+    }
+    /* dbar from rbar = -w / cV */
+    double db[5];
+    for (int v = 0; v < 5; v++) {
+        double x = -a.W[v][c1] / m.cv[c1];
+        if (c2 >= 0) x -= -a.W[v][c2] / m.cv[c2];
+        db[v] = x;
+    }
+    const double lam = ((P1.mu * fi + P2.mu * fo) + (P1.c * fi + P2.c * fo)) / 2;
+    /* primitive adjoints of both sides */
+    double rb1 = 0, rb2 = 0, Ub1[3] = {0, 0, 0}, Ub2[3] = {0, 0, 0}, Tb1 = 0, Tb2 = 0, pb1 = 0,
+           pb2 = 0, lamb = 0;
+    /* continuity */
+    {
+        const double A0 = db[0] * nmag;     /* sum_c Fbar_c en_c */
+        for (int c = 0; c < 3; c++) {
+            const double Fb = db[0] * n[c];
+            Ub1[c] += Fb * P1.r * fi; rb1 += Fb * P1.U[c] * fi;
+            Ub2[c] += Fb * P2.r * fo; rb2 += Fb * P2.U[c] * fo;
+        }
+        lamb += -A0 * (P2.r - P1.r);
+        rb2 += -A0 * lam;
+        rb1 += A0 * lam;
+    }
+    /* momentum */
+    {
+        const double Fc1[3] = {P1.U[0] * P1.r, P1.U[1] * P1.r, P1.U[2] * P1.r};
+        const double Fc2[3] = {P2.U[0] * P2.r, P2.U[1] * P2.r, P2.U[2] * P2.r};
+        double Fcb1[3] = {0, 0, 0}, Fcb2[3] = {0, 0, 0};
+        const double dmen = db[1] * en[0] + db[2] * en[1] + db[3] * en[2];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                const double Fb = db[1 + r] * n[c];      /* Fbar[r][c] */
+                const double Ab = fi * Fb, Bb = fo * Fb;
+                Fcb1[r] += Ab * P1.U[c]; Ub1[c] += Ab * Fc1[r];
+                Fcb2[r] += Bb * P2.U[c]; Ub2[c] += Bb * Fc2[r];
+                if (r == c) { pb1 += Ab; pb2 += Bb; }
+            }
+        for (int c = 0; c < 3; c++) {
+            const double dqb = -dmen * n[c];
+            Fcb2[c] += dqb * lam;
+            Fcb1[c] -= dqb * lam;
+            lamb += dqb * (Fc2[c] - Fc1[c]);
+        }
+        for (int c = 0; c < 3; c++) {
+            Ub1[c] += Fcb1[c] * P1.r; rb1 += Fcb1[c] * P1.U[c];
+            Ub2[c] += Fcb2[c] * P2.r; rb2 += Fcb2[c] * P2.U[c];
+        }
+    }
+    /* potential temperature */
+    {
+        const double B4 = db[4] * nmag;
+        for (int c = 0; c < 3; c++) {
+            const double Fb = db[4] * n[c];
+            Ub1[c] += Fb * P1.r * P1.T * fi; rb1 += Fb * P1.U[c] * P1.T * fi; Tb1 += Fb * P1.U[c] * P1.r * fi;
+            Ub2[c] += Fb * P2.r * P2.T * fo; rb2 += Fb * P2.U[c] * P2.T * fo; Tb2 += Fb * P2.U[c] * P2.r * fo;
+        }
+        lamb += -B4 * (P2.r * P2.T - P1.r * P1.T);
+        rb2 += -B4 * lam * P2.T; Tb2 += -B4 * lam * P2.r;
+        rb1 += B4 * lam * P1.T;  Tb1 += B4 * lam * P1.r;
+    }
+    /* lambda -> |U|, c */
+    {
+        const double mub1 = lamb * fi / 2, mub2 = lamb * fo / 2;
+        const double cb1 = lamb * fi / 2, cb2 = lamb * fo / 2;
+        if (P1.mu > 0) for (int c = 0; c < 3; c++) Ub1[c] += mub1 * P1.U[c] / P1.mu;
+        if (P2.mu > 0) for (int c = 0; c < 3; c++) Ub2[c] += mub2 * P2.U[c] / P2.mu;
+        if (P1.c > 0) Tb1 += cb1 * m.gR / (2 * P1.c);
+        if (P2.c > 0) Tb2 += cb2 * m.gR / (2 * P2.c);
+    }
+    if (c2 < 0) {
+        /* ghost: fold into the owner */
+        rb1 += rb2; Tb1 += Tb2; pb1 += pb2;
+        if (m.bc[k] == 2) sym_vjp(P1.U, en, rsym, magR, magP, scaled, Ub2, Ub1);
+        else for (int c = 0; c < 3; c++) Ub1[c] += Ub2[c];
+        rb2 = 0; Tb2 = 0; pb2 = 0; Ub2[0] = Ub2[1] = Ub2[2] = 0;
+    }
+    a.adjO[0][k] = rb1; a.adjO[1][k] = Ub1[0]; a.adjO[2][k] = Ub1[1]; a.adjO[3][k] = Ub1[2];
+    a.adjO[4][k] = Tb1; a.adjO[5][k] = pb1;
+    a.adjN[0][k] = rb2; a.adjN[1][k] = Ub2[0]; a.adjN[2][k] = Ub2[1]; a.adjN[3][k] = Ub2[2];
+    a.adjN[4][k] = Tb2; a.adjN[5][k] = pb2;
+}
+
+struct VolAdjArgs {
+    const double* S[5];
+    const double* W[5];
+    const double* adjO[NPA];
+    const double* adjN[NPA];
+    double* G[5];            /* output: J_L(v)^T w */
+};
+
+__global__ void k_adj_volume(const NsemDev m, const NsemTables tab, VolAdjArgs a) {
+    extern __shared__ double sm[];
+    const int NPX = m.npx, NPY = m.npy, NPZ = m.npz, NP = m.np;
+    double* rb = sm;                                 /* [5][NP] rbar of the element */
+    double* dps = sm + 5 * NP;                       /* dpsi tables */
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const int64_t node = e * NP + t;
+    const bool active = t < NP;
+    if (active) {
+        const double cv = m.cv[node];
+        for (int v = 0; v < 5; v++) rb[v * NP + t] = -a.W[v][node] / cv;
+    }
+    __syncthreads();
+    if (!active) return;
+    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
+    const NodePrim P = node_prim(m, a.S, node);
+    double Jin[9];
+    for (int c = 0; c < 9; c++) Jin[c] = m.jin[(int64_t)c * m.n_int + node];
+
+    /* transposed volume gather: G_c, H_rc, K_c over the targets a of node b */
+    double Gv[3] = {0, 0, 0}, H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, K[3] = {0, 0, 0};
+    const double* Dx = dps;
+    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    auto acc = [&](int la, const double* dj) {
+        const double r0 = rb[la], r4 = rb[4 * NP + la];
+        const double rm[3] = {rb[NP + la], rb[2 * NP + la], rb[3 * NP + la]};
+        for (int c = 0; c < 3; c++) {
+            Gv[c] += r0 * dj[c];
+            K[c] += r4 * dj[c];
+            for (int r = 0; r < 3; r++) H[r][c] += rm[r] * dj[c];
+        }
+    };
+    /* targets on the x line (including self), then y and z lines */
+    for (int im = 0; im < NPX; im++) {
+        double dv[3];
+        dv[0] = Dx[ia * NPX + im];
+        dv[1] = (im == ia) ? Dy[ja * NPY + ja] : 0.0;
+        dv[2] = (im == ia) ? Dz[ka * NPZ + ka] : 0.0;
+        double dj[3];
+        dj[0] = Jin[XX] * dv[0] + Jin[XY] * dv[1] + Jin[XZ] * dv[2];
+        dj[1] = Jin[YX] * dv[0] + Jin[YY] * dv[1] + Jin[YZ] * dv[2];
+        dj[2] = Jin[ZX] * dv[0] + Jin[ZY] * dv[1] + Jin[ZZ] * dv[2];
+        acc(t + (im - ia) * NPY * NPZ, dj);
+    }
+    for (int jm = 0; jm < NPY; jm++) {
+        if (jm == ja) continue;
+        const double D = Dy[ja * NPY + jm];
+        const double dj[3] = {Jin[XY] * D, Jin[YY] * D, Jin[ZY] * D};
+        acc(t + (jm - ja) * NPZ, dj);
+    }
+    for (int km = 0; km < NPZ; km++) {
+        if (km == ka) continue;
+        const double D = Dz[ka * NPZ + km];
+        const double dj[3] = {Jin[XZ] * D, Jin[YZ] * D, Jin[ZZ] * D};
+        acc(t + (km - ka), dj);
+    }
+    /* flux adjoints -> primitive adjoints (fr = U rho, fm = (rho U) (x) U + p' I,
+     * ft = (rho U) theta; Fbar = -(G, H, K)) */
+    double rbar = 0, Ub[3] = {0, 0, 0}, Tb = 0, pb = 0;
+    const double Fc[3] = {P.U[0] * P.r, P.U[1] * P.r, P.U[2] * P.r};
+    double Fcb[3] = {0, 0, 0};
+    for (int c = 0; c < 3; c++) {
+        const double frb = -Gv[c];
+        Ub[c] += frb * P.r;
+        rbar += frb * P.U[c];
+        const double ftb = -K[c];
+        Fcb[c] += ftb * P.T;
+        Tb += ftb * Fc[c];
+    }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            const double fmb = -H[r][c];
+            Fcb[r] += fmb * P.U[c];
+            Ub[c] += fmb * Fc[r];
+            if (r == c) pb += fmb;
+        }
+    for (int c = 0; c < 3; c++) {
+        Ub[c] += Fcb[c] * P.r;
+        rbar += Fcb[c] * P.U[c];
+    }
+    /* gravity source: r_m -= g (rho - rho_ref) cV */
+    const double cv = m.cv[node];
+    rbar += -(rb[NP + t] * m.g[0] + rb[2 * NP + t] * m.g[1] + rb[3 * NP + t] * m.g[2]) * cv;
+    /* face contributions gathered through the lift lists */
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        const double* const* src = (code & 1) ? a.adjN : a.adjO;
+        rbar += src[0][k]; Ub[0] += src[1][k]; Ub[1] += src[2][k]; Ub[2] += src[3][k];
+        Tb += src[4][k]; pb += src[5][k];
+    }
+    /* EOS: p = P0 (rho theta R / P0)^gamma */
+    rbar += pb * m.gamma * P.p / P.r;
+    Tb += pb * m.gamma * P.p / P.T;
+    /* U = m / rho, theta = E / rho */
+    const double inv = 1.0 / P.r;
+    double g0 = rbar - inv * vdot3(Ub, P.U) - inv * Tb * P.T;
+    a.G[0][node] = g0;
+    a.G[1][node] = Ub[0] * inv;
+    a.G[2][node] = Ub[1] * inv;
+    a.G[3][node] = Ub[2] * inv;
+    a.G[4][node] = Tb * inv;
+}
+
+/* lam = c0 * lam + c1 * x + c2 * y (elementwise over 5 arrays) */
+struct Lin3Args {
+    double* out[5];
+    const double* x[5];
+    const double* y[5];
+    const double* z[5];
+    double cx, cy, cz;
+    int64_t n;
+};
+
+__global__ void k_lin3(Lin3Args a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        for (int v = 0; v < 5; v++) {
+            double s = a.cx * a.x[v][i];
+            if (a.y[0]) s += a.cy * a.y[v][i];
+            if (a.z[0]) s += a.cz * a.z[v][i];
+            a.out[v][i] = s;
+        }
+}
+
+int grid_for(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
+                 const double* const* W, double* const* G, NsemAdjBuf* ab, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    FaceAdjArgs fa;
+    for (int v = 0; v < 5; v++) { fa.S[v] = S[v]; fa.W[v] = W[v]; }
+    for (int v = 0; v < NPA; v++) { fa.adjO[v] = ab->adjO[v]; fa.adjN[v] = ab->adjN[v]; }
+    const int64_t fb = (m->n_slot + 127) / 128;
+    k_adj_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
+    VolAdjArgs va;
+    for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.W[v] = W[v]; va.G[v] = G[v]; }
+    for (int v = 0; v < NPA; v++) { va.adjO[v] = ab->adjO[v]; va.adjN[v] = ab->adjN[v]; }
+    const int threads = ((m->np + 31) / 32) * 32;
+    const size_t smem = (5 * (size_t)m->np + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+    k_adj_volume<<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
+    return (int)cudaGetLastError();
+}
+
+int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const double* const* y,
+                  double cy, const double* const* z, double cz, int64_t n, void* stream) {
+    Lin3Args a;
+    for (int v = 0; v < 5; v++) {
+        a.out[v] = out[v];
+        a.x[v] = x[v];
+        a.y[v] = y ? y[v] : nullptr;
+        a.z[v] = z ? z[v] : nullptr;
+    }
+    a.cx = cx; a.cy = cy; a.cz = cz; a.n = n;
+    k_lin3<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(a);
+    return (int)cudaGetLastError();
+}
+
+int nsem_adj_prepare(const NsemDev* m) {
+    const size_t smem = (5 * (size_t)m->np + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+    if (smem > 48 * 1024)
+        return (int)cudaFuncSetAttribute(k_adj_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    return 0;
+}

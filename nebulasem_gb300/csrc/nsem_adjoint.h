@@ -1,0 +1,34 @@
+/*
+ * Discrete adjoint of the plain form (nsem_adjoint.cu).
+ */
+#ifndef NSEM_ADJOINT_H
+#define NSEM_ADJOINT_H
+
+#include <stdint.h>
+
+#include "nsem_internal.h"
+
+struct NsemAdjBuf {
+    double* adjO[6] = {};   /* per slot: owner-side primitive adjoints   */
+    double* adjN[6] = {};   /* per slot: neighbour-side primitive adjoints */
+    double* lam[5] = {};    /* adjoint of the current step state          */
+    double* a3[5] = {};
+    double* lu2[5] = {};
+    double* lu1[5] = {};
+    double* g[5] = {};      /* VJP output                                 */
+    double* fin[5] = {};    /* final forward state (restored afterwards)  */
+    double* ckpt = nullptr; /* [n_ckpt][5][n_int] states every k steps     */
+    double* seg = nullptr;  /* [k][3][5][n_int] u^n, u1, u2 of a segment   */
+    int nsteps = 0, every = 0, n_ckpt = 0;
+    bool ready = false;
+};
+
+/* g = J_L(S)^T W (all device pointers, 5 SoA arrays each) */
+int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
+                 const double* const* W, double* const* G, NsemAdjBuf* ab, void* stream);
+/* out = cx x + cy y + cz z (y, z may be null) */
+int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const double* const* y,
+                  double cy, const double* const* z, double cz, int64_t n, void* stream);
+int nsem_adj_prepare(const NsemDev* m);
+
+#endif

@@ -20,6 +20,7 @@
 
 #include "nsem.h"
 #include "nsem_internal.h"
+#include "nsem_adjoint.h"
 #include "nsem_mixed.h"
 
 struct nsem_ctx {
@@ -29,6 +30,7 @@ struct nsem_ctx {
     NsemTables tab{};
     NsemBuf buf{};
     NsemMixedBuf mbuf{};
+    NsemAdjBuf abuf{};
     bool mixed_ready = false;
     int rep = 0;                     /* 0: state in buf.u; 1: perturbation in mbuf.U[cur] */
     double dt = 0, T0 = 0;
@@ -342,6 +344,8 @@ void nsem_destroy(nsem_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : ctx->allocations) cudaFree(p);
+    if (ctx->abuf.ckpt) cudaFree(ctx->abuf.ckpt);
+    if (ctx->abuf.seg) cudaFree(ctx->abuf.seg);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -477,6 +481,200 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
     if (prec == NSEM_MIXED) ctx->mbuf.cur ^= (nsteps & 1);
     NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, ctx->stream));
+    return NSEM_OK;
+}
+
+/* ---------------------------------------------------------------- adjoint */
+
+static nsem_status adj_alloc(nsem_ctx* ctx) {
+    NsemAdjBuf& A = ctx->abuf;
+    if (A.ready) return NSEM_OK;
+    nsem_status s;
+    for (int v = 0; v < 6; v++) {
+        if ((s = dalloc(ctx, &A.adjO[v], ctx->dev.n_slot)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.adjN[v], ctx->dev.n_slot)) != NSEM_OK) return s;
+    }
+    for (int v = 0; v < 5; v++) {
+        const size_t n = (size_t)ctx->dev.n_int;
+        if ((s = dalloc(ctx, &A.lam[v], n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.a3[v], n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.lu2[v], n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.lu1[v], n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.g[v], n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &A.fin[v], n)) != NSEM_OK) return s;
+    }
+    int e = nsem_adj_prepare(&ctx->dev);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "adjoint shared memory");
+    A.ready = true;
+    return NSEM_OK;
+}
+
+static nsem_status copy_state(nsem_ctx* ctx, double* const* dst, const double* const* src) {
+    const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(dst[v], src[v], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return NSEM_OK;
+}
+
+/* pointer set of state slot j of a [count][5][n_int] block */
+static void slots(double* block, int64_t j, int64_t n, double* out[5]) {
+    for (int v = 0; v < 5; v++) out[v] = block + (j * 5 + v) * n;
+}
+
+/* one FP64 step; optionally keeps the two stage states */
+static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const* keep2) {
+    NsemDev* D = &ctx->dev;
+    NsemBuf* b = &ctx->buf;
+    void* st = (void*)ctx->stream;
+    int e;
+    if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
+    for (int stage = 1; stage <= 3; stage++) {
+        if ((e = nsem_fp64_face(D, b, stage == 1, st))) return cuda_fail(ctx, (cudaError_t)e, "face");
+        if ((e = nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st)))
+            return cuda_fail(ctx, (cudaError_t)e, "volume");
+        nsem_status s = NSEM_OK;
+        if (stage == 1 && keep1) s = copy_state(ctx, keep1, b->s);
+        if (stage == 2 && keep2) s = copy_state(ctx, keep2, b->s);
+        if (s != NSEM_OK) return s;
+    }
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
+    for (int v = 0; v < 5; v++)
+        if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status s = ensure_rep(ctx, 0);
+    if (s != NSEM_OK) return s;
+    if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
+    NsemAdjBuf& A = ctx->abuf;
+    const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(A.lam[v], w[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    int e = nsem_adj_vjp(&ctx->dev, &ctx->tab, ctx->buf.u, A.lam, A.g, &A, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "vjp");
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(g[v], A.g[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
+                                                 double* ms_fwd) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status s = ensure_rep(ctx, 0);
+    if (s != NSEM_OK) return s;
+    if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
+    NsemAdjBuf& A = ctx->abuf;
+    const int64_t n = ctx->dev.n_int;
+    const int n_ckpt = (nsteps + ckpt_every - 1) / ckpt_every;
+    if (A.ckpt) { cudaFree(A.ckpt); A.ckpt = nullptr; }
+    if (A.seg) { cudaFree(A.seg); A.seg = nullptr; }
+    cudaError_t ce = cudaMalloc((void**)&A.ckpt, (size_t)n_ckpt * 5 * n * sizeof(double));
+    if (ce != cudaSuccess) return fail(ctx, NSEM_NO_MEMORY, "checkpoint allocation failed");
+    ce = cudaMalloc((void**)&A.seg, (size_t)ckpt_every * 3 * 5 * n * sizeof(double));
+    if (ce != cudaSuccess) return fail(ctx, NSEM_NO_MEMORY, "segment allocation failed");
+    cudaEvent_t e0, e1;
+    NSEM_CUDA(cudaEventCreate(&e0));
+    NSEM_CUDA(cudaEventCreate(&e1));
+    NSEM_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int st = 0; st < nsteps; st++) {
+        if (st % ckpt_every == 0) {
+            double* c[5];
+            slots(A.ckpt, st / ckpt_every, n, c);
+            if ((s = copy_state(ctx, c, ctx->buf.u)) != NSEM_OK) return s;
+        }
+        if ((s = fp64_step(ctx, nullptr, nullptr)) != NSEM_OK) return s;
+    }
+    NSEM_CUDA(cudaEventRecord(e1, ctx->stream));
+    if ((s = copy_state(ctx, A.fin, ctx->buf.u)) != NSEM_OK) return s;
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    s = check_status(ctx);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != NSEM_OK) return s;
+    if (ms_fwd) *ms_fwd = ms;
+    A.nsteps = nsteps;
+    A.every = ckpt_every;
+    A.n_ckpt = n_ckpt;
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
+                                    double* const lam0[5], double* ms_adj) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
+    NsemAdjBuf& A = ctx->abuf;
+    if (!A.ready || !A.ckpt || A.nsteps < 1)
+        return fail(ctx, NSEM_BAD_ARG, "no checkpointed forward run to differentiate");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const int64_t n = ctx->dev.n_int;
+    const size_t bytes = (size_t)n * sizeof(double);
+    for (int v = 0; v < 5; v++) {
+        if (!lam_final[v] || !lam0[v]) return fail(ctx, NSEM_BAD_ARG, "lam array is NULL");
+        NSEM_CUDA(cudaMemcpyAsync(A.lam[v], lam_final[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    const double dt = ctx->dt;
+    void* st = (void*)ctx->stream;
+    cudaEvent_t e0, e1;
+    NSEM_CUDA(cudaEventCreate(&e0));
+    NSEM_CUDA(cudaEventCreate(&e1));
+    NSEM_CUDA(cudaEventRecord(e0, ctx->stream));
+    nsem_status s = NSEM_OK;
+    int e = 0;
+    for (int sg = A.n_ckpt - 1; sg >= 0 && s == NSEM_OK; sg--) {
+        const int start = sg * A.every;
+        const int cnt = (A.nsteps - start < A.every) ? A.nsteps - start : A.every;
+        double* c[5];
+        slots(A.ckpt, sg, n, c);
+        if ((s = copy_state(ctx, ctx->buf.u, c)) != NSEM_OK) break;
+        for (int j = 0; j < cnt && s == NSEM_OK; j++) {
+            double *u0[5], *u1[5], *u2[5];
+            slots(A.seg, 3 * j, n, u0);
+            slots(A.seg, 3 * j + 1, n, u1);
+            slots(A.seg, 3 * j + 2, n, u2);
+            if ((s = copy_state(ctx, u0, ctx->buf.u)) != NSEM_OK) break;
+            s = fp64_step(ctx, u1, u2);
+        }
+        if (s != NSEM_OK) break;
+        for (int j = cnt - 1; j >= 0; j--) {
+            double *u0[5], *u1[5], *u2[5];
+            slots(A.seg, 3 * j, n, u0);
+            slots(A.seg, 3 * j + 1, n, u1);
+            slots(A.seg, 3 * j + 2, n, u2);
+            /* u3 = u/3 + 2/3 (u2 + dt L(u2)) */
+            if ((s = copy_state(ctx, A.a3, A.lam)) != NSEM_OK) break;
+            if ((e = nsem_adj_vjp(&ctx->dev, &ctx->tab, u2, A.a3, A.g, &A, st))) break;
+            if ((e = nsem_adj_lin3(A.lu2, A.a3, 2.0 / 3.0, A.g, 2.0 / 3.0 * dt, nullptr, 0, n, st))) break;
+            /* u2 = 3/4 u + 1/4 (u1 + dt L(u1)) */
+            if ((e = nsem_adj_vjp(&ctx->dev, &ctx->tab, u1, A.lu2, A.g, &A, st))) break;
+            if ((e = nsem_adj_lin3(A.lu1, A.lu2, 0.25, A.g, 0.25 * dt, nullptr, 0, n, st))) break;
+            /* u1 = u + dt L(u) */
+            if ((e = nsem_adj_vjp(&ctx->dev, &ctx->tab, u0, A.lu1, A.g, &A, st))) break;
+            if ((e = nsem_adj_lin3(A.lam, A.a3, 1.0 / 3.0, A.lu2, 0.75, A.lu1, 1.0, n, st))) break;
+            if ((e = nsem_adj_lin3(A.lam, A.lam, 1.0, A.g, dt, nullptr, 0, n, st))) break;
+        }
+    }
+    if (e) s = cuda_fail(ctx, (cudaError_t)e, "adjoint sweep");
+    if (s != NSEM_OK) return s;
+    NSEM_CUDA(cudaEventRecord(e1, ctx->stream));
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(lam0[v], A.lam[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((s = copy_state(ctx, ctx->buf.u, A.fin)) != NSEM_OK) return s;
+    ctx->rep = 0;
+    s = check_status(ctx);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != NSEM_OK) return s;
+    if (ms_adj) *ms_adj = ms;
     return NSEM_OK;
 }
 

@@ -58,6 +58,9 @@ def lib():
         _lib.nsem_oracle_pow_dd.restype = ctypes.c_double
         _lib.nsem_oracle_set_pow.argtypes = [ctypes.c_int]
         _lib.nsem_oracle_threads.restype = ctypes.c_int
+        _lib.nsem_oracle_jvp.argtypes = [ctypes.POINTER(_Mesh), P, P, P, P]
+        _lib.nsem_oracle_tlm_ssprk3.argtypes = [ctypes.POINTER(_Mesh), P, P, ctypes.c_double,
+                                                ctypes.c_int]
     return _lib
 
 
@@ -141,6 +144,24 @@ class OracleMesh:
         arrs, up = self._vec([np.array(a, dtype=np.float64, copy=True) for a in u])
         lib().nsem_oracle_ssprk3(ctypes.byref(self.struct), up, float(dt), int(nsteps))
         return arrs
+
+    def jvp(self, u, du):
+        """Tendency L(u) and its directional derivative J_L(u) du (dual numbers)."""
+        _, up = self._vec(u)
+        _, dp = self._vec(du)
+        L = [np.empty(self.n_int) for _ in range(5)]
+        Ld = [np.empty(self.n_int) for _ in range(5)]
+        _, lp = self._vec(L)
+        _, ldp = self._vec(Ld)
+        lib().nsem_oracle_jvp(ctypes.byref(self.struct), up, dp, lp, ldp)
+        return L, Ld
+
+    def tlm_ssprk3(self, u, du, dt, nsteps):
+        """Tangent-linear SSP-RK3: returns (u_n, du_n) after nsteps."""
+        ua, up = self._vec([np.array(a, dtype=np.float64, copy=True) for a in u])
+        da, dp = self._vec([np.array(a, dtype=np.float64, copy=True) for a in du])
+        lib().nsem_oracle_tlm_ssprk3(ctypes.byref(self.struct), up, dp, float(dt), int(nsteps))
+        return ua, da
 
     def diagnostics(self, u):
         _, up = self._vec(u)

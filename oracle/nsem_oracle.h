@@ -73,6 +73,13 @@ void nsem_oracle_diagnostics(const nsem_oracle_mesh* m, const double* const u[5]
 
 double nsem_oracle_pow_dd(double x, double y);
 
+/* Tangent-linear model (nsem_tlm.cpp, dual numbers): Ld = J_L(u) du; and
+ * (u, du) advanced through nsteps SSP-RK3 steps. */
+void nsem_oracle_jvp(const nsem_oracle_mesh* m, const double* const u[5], const double* const du[5],
+                     double* const L[5], double* const Ld[5]);
+void nsem_oracle_tlm_ssprk3(const nsem_oracle_mesh* m, double* const u[5], double* const du[5],
+                            double dt, int nsteps);
+
 int nsem_oracle_threads(void);
 
 #ifdef __cplusplus
