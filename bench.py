@@ -41,7 +41,6 @@ WORKLOAD = "bubble3d_32_n4"
 DT = 0.0075           # largest stable step of this mesh (dt = 0.01 diverges)
 METRIC = "DG DOF-stages/s: mixed-precision vs FP64 at stated L2 error; adjoint/forward"
 UNIT = "DOF-stages/s"
-BYTES_PER_DOF_STAGE_FP64 = 64.0 / 3.0   # u^n read+write, stage read/write (21.33 B)
 
 
 def peaks():
@@ -263,18 +262,27 @@ def run_ours(args):
     top_name, (top_ms, top_n) = top
     per_launch_s = top_ms / top_n * 1e-3
     hbm, src = peaks()
-    if prec_name == "mixed":
-        alg_bytes = nsem_mixed_alg_bytes(n)
+    # algorithmic bytes of the dominant kernel's launches: FP64 state traffic of
+    # the stage it runs (precision form: one kernel class per stage), or the
+    # stage average for the plain form's per-stage kernels
+    stage_of = {"mixed_stage1": 1, "mixed_stage2": 2, "mixed_stage3": 3}
+    if top_name in stage_of:
+        alg_bytes = ng.ALG_BYTES_PER_DOF_STAGE[stage_of[top_name]] * dofs
     else:
-        alg_bytes = BYTES_PER_DOF_STAGE_FP64 * dofs
+        alg_bytes = ng.ALG_BYTES_PER_DOF_STAGE_AVG * dofs
     achieved = alg_bytes / per_launch_s / 1e9
     launches_per_step = sum(c for _, c in prof.values()) / max(1, min(args.steps, 5))
+    step_gbs = ng.ALG_BYTES_PER_DOF_STAGE_AVG * value / 1e9
     roof = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
             "alg_bytes_per_launch": alg_bytes,
             "kernel_ms_per_launch": top_ms / top_n,
+            "step_achieved": step_gbs, "step_frac": step_gbs / hbm,
             "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items()}}
+    if prec_name == "mixed":
+        own = ng.mixed_own_bytes_per_node_stage()
+        roof["own_layout_bytes_per_dof_stage"] = sum(own.values()) / 15.0
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -303,14 +311,6 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
-
-
-def nsem_mixed_alg_bytes(n):
-    """Compulsory HBM bytes of one precision-form stage launch (set by the
-    precision-form kernels' state layout); see nebulasem_gb300.mixed_bytes."""
-    from nebulasem_gb300 import mixed_bytes_per_stage
-
-    return mixed_bytes_per_stage(n)
 
 
 def main():

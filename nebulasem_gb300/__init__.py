@@ -20,7 +20,7 @@ MIXED = 1
 SSPRK3 = 0
 
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA_ERROR", 3: "NONFINITE", 4: "TIMEOUT",
-          5: "UNSUPPORTED", 6: "NO_MEMORY"}
+          5: "UNSUPPORTED", 6: "NO_MEMORY", 7: "TOO_LARGE"}
 VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
 
 _lib = None
@@ -276,13 +276,19 @@ class Solver:
         return np.array([m.value, e.value, v.value])
 
 
-def mixed_bytes_per_stage(n_int):
-    """Compulsory HBM bytes of one precision-form stage over n_int nodes.
+# Algorithmic HBM bytes per DOF of one SSP-RK3 stage: the compulsory FP64
+# state traffic of the Shu-Osher stages (stage 1 reads u^n, writes u1; stage 2
+# reads u1 and u^n, writes u2; stage 3 reads u2 and u^n, writes u^{n+1}), the
+# same figure for both forms because both keep the RK state in FP64.
+ALG_BYTES_PER_DOF_STAGE = {1: 16.0, 2: 24.0, 3: 24.0}
+ALG_BYTES_PER_DOF_STAGE_AVG = 64.0 / 3.0
 
-    State u^n in FP64 (5 x 8 B), read every stage; the stage increment in FP32
-    (5 x 4 B) written by stages 1-2 and read by stages 2-3; u^{n+1} written by
-    stage 3 (5 x 8 B).  Per node and step: 40*3 (read u^n) + 20 (write d1)
-    + 20+20 (read d1, write d2) + 20 + 40 (read d2, write u^{n+1}) = 240 B,
-    i.e. 80 B per node-stage (16 B per DOF-stage).
-    """
-    return 80.0 * n_int
+
+def mixed_own_bytes_per_node_stage():
+    """HBM bytes per node that the precision form's own layout must move, by
+    stage: stage 1 reads the FP32 shadow of u'^n and writes the FP32 increment
+    (20 + 20 B); stage 2 reads the shadow and the first increment and writes the
+    second (60 B); stage 3 reads u'^n (FP64), its shadow and the second
+    increment and writes u'^{n+1} and its shadow (40 + 20 + 20 + 40 + 20 B).
+    240 B per node and step, 16 B per DOF-stage."""
+    return {1: 40.0, 2: 60.0, 3: 140.0}

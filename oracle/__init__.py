@@ -61,6 +61,9 @@ def lib():
         _lib.nsem_oracle_jvp.argtypes = [ctypes.POINTER(_Mesh), P, P, P, P]
         _lib.nsem_oracle_tlm_ssprk3.argtypes = [ctypes.POINTER(_Mesh), P, P, ctypes.c_double,
                                                 ctypes.c_int]
+        _lib.nsem_oracle_tlm_ssprk3_multi.argtypes = [ctypes.POINTER(_Mesh), P, P, ctypes.c_int,
+                                                      ctypes.c_double, ctypes.c_int]
+        _lib.nsem_oracle_tlm_ssprk3_multi.restype = ctypes.c_int
     return _lib
 
 
@@ -162,6 +165,21 @@ class OracleMesh:
         da, dp = self._vec([np.array(a, dtype=np.float64, copy=True) for a in du])
         lib().nsem_oracle_tlm_ssprk3(ctypes.byref(self.struct), up, dp, float(dt), int(nsteps))
         return ua, da
+
+    def tlm_ssprk3_multi(self, u, dus, dt, nsteps):
+        """Tangent-linear SSP-RK3 along len(dus) <= 8 directions in one pass:
+        returns (u_n, [du_n per direction])."""
+        nd = len(dus)
+        ua, up = self._vec([np.array(a, dtype=np.float64, copy=True) for a in u])
+        da = [np.array(a, dtype=np.float64, copy=True) for d in dus for a in d]
+        for a in da:
+            assert a.shape == (self.n_int,)
+        dp = (ctypes.c_void_p * (5 * nd))(*[a.ctypes.data for a in da])
+        rc = lib().nsem_oracle_tlm_ssprk3_multi(ctypes.byref(self.struct), up, dp, nd,
+                                                float(dt), int(nsteps))
+        if rc != 0:
+            raise ValueError("tlm_ssprk3_multi: 1 <= directions <= 8")
+        return ua, [da[5 * d:5 * d + 5] for d in range(nd)]
 
     def diagnostics(self, u):
         _, up = self._vec(u)

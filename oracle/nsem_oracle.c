@@ -33,6 +33,7 @@ enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
 static int g_pow_mode = 0;
 
 void nsem_oracle_set_pow(int which) { g_pow_mode = which; }
+int nsem_oracle_get_pow(void) { return g_pow_mode; }
 
 int nsem_oracle_threads(void) {
 #ifdef _OPENMP

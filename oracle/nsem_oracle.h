@@ -54,6 +54,7 @@ typedef struct {
 /* pow used for the equation of state: 0 = C library pow (as the reference),
  * 1 = double-double correctly rounded restatement (see oracle_pow_dd). */
 void nsem_oracle_set_pow(int which);
+int nsem_oracle_get_pow(void);
 
 /* Tendencies L = -Su/cV of (rho, rho u, rho v, rho w, rho theta) on interior
  * nodes for the conserved state u (SoA, 5 arrays of n_int).  p_out, if not
@@ -79,6 +80,10 @@ void nsem_oracle_jvp(const nsem_oracle_mesh* m, const double* const u[5], const 
                      double* const L[5], double* const Ld[5]);
 void nsem_oracle_tlm_ssprk3(const nsem_oracle_mesh* m, double* const u[5], double* const du[5],
                             double dt, int nsteps);
+/* nd <= 8 tangent directions in one pass: du[5*d + c] is direction d,
+ * variable c.  Returns 0, or -1 if nd is out of range. */
+int nsem_oracle_tlm_ssprk3_multi(const nsem_oracle_mesh* m, double* const u[5], double* const* du,
+                                 int nd, double dt, int nsteps);
 
 int nsem_oracle_threads(void);
 

@@ -19,34 +19,101 @@
 
 namespace {
 
-struct Dual {
-    double v, d;
-    Dual() : v(0), d(0) {}
-    Dual(double x) : v(x), d(0) {}
-    Dual(double x, double y) : v(x), d(y) {}
+/* the equation-of-state pow follows the oracle's switch (C library or the
+ * correctly rounded restatement), so values match nsem_oracle_tendency */
+inline double eos_pow(double a, double e) {
+    return nsem_oracle_get_pow() ? nsem_oracle_pow_dd(a, e) : std::pow(a, e);
+}
+
+/* value plus K directional derivatives (K directions share one pass) */
+template <int K>
+struct DualN {
+    double v, d[K];
+    DualN() : v(0) { for (int i = 0; i < K; i++) d[i] = 0; }
+    DualN(double x) : v(x) { for (int i = 0; i < K; i++) d[i] = 0; }
 };
-inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
-inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
-inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
-inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-inline Dual operator/(Dual a, Dual b) {
+template <int K>
+inline DualN<K> operator+(const DualN<K>& a, const DualN<K>& b) {
+    DualN<K> r(a.v + b.v);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator-(const DualN<K>& a, const DualN<K>& b) {
+    DualN<K> r(a.v - b.v);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator-(const DualN<K>& a) {
+    DualN<K> r(-a.v);
+    for (int i = 0; i < K; i++) r.d[i] = -a.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator*(const DualN<K>& a, const DualN<K>& b) {
+    DualN<K> r(a.v * b.v);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator*(const DualN<K>& a, double b) {
+    DualN<K> r(a.v * b);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i] * b;
+    return r;
+}
+template <int K>
+inline DualN<K> operator*(double a, const DualN<K>& b) {
+    DualN<K> r(a * b.v);
+    for (int i = 0; i < K; i++) r.d[i] = a * b.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator+(const DualN<K>& a, double b) {
+    DualN<K> r(a.v + b);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator-(const DualN<K>& a, double b) {
+    DualN<K> r(a.v - b);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i];
+    return r;
+}
+template <int K>
+inline DualN<K> operator/(const DualN<K>& a, const DualN<K>& b) {
     const double q = a.v / b.v;
-    return {q, (a.d - q * b.d) / b.v};
+    DualN<K> r(q);
+    for (int i = 0; i < K; i++) r.d[i] = (a.d[i] - q * b.d[i]) / b.v;
+    return r;
 }
-inline Dual sqrt(Dual a) {
+template <int K>
+inline DualN<K> operator/(const DualN<K>& a, double b) {
+    DualN<K> r(a.v / b);
+    for (int i = 0; i < K; i++) r.d[i] = a.d[i] / b;
+    return r;
+}
+template <int K>
+inline DualN<K> sqrt_(const DualN<K>& a) {
     const double s = std::sqrt(a.v);
-    return {s, s > 0 ? a.d / (2 * s) : 0.0};
+    DualN<K> r(s);
+    for (int i = 0; i < K; i++) r.d[i] = s > 0 ? a.d[i] / (2 * s) : 0.0;
+    return r;
 }
-inline Dual pow(Dual a, double e) {
-    const double p = std::pow(a.v, e);
-    return {p, a.v != 0 ? e * p / a.v * a.d : 0.0};
+template <int K>
+inline DualN<K> pow_(const DualN<K>& a, double e) {
+    const double p = eos_pow(a.v, e);
+    DualN<K> r(p);
+    const double f = a.v != 0 ? e * p / a.v : 0.0;
+    for (int i = 0; i < K; i++) r.d[i] = f * a.d[i];
+    return r;
 }
-inline double val(Dual a) { return a.v; }
+template <int K>
+inline double val(const DualN<K>& a) { return a.v; }
+using Dual = DualN<1>;
 inline double val(double a) { return a; }
 inline double sqrt_(double a) { return std::sqrt(a); }
-inline Dual sqrt_(Dual a) { return sqrt(a); }
-inline double pow_(double a, double e) { return std::pow(a, e); }
-inline Dual pow_(Dual a, double e) { return pow(a, e); }
+inline double pow_(double a, double e) { return eos_pow(a, e); }
 
 enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
 
@@ -97,6 +164,7 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
     const int64_t n_slot = (int64_t)m->n_face * NPF;
     const double P0 = m->P0, R = m->R, gam = m->gamma, gR = gam * R;
     std::vector<T> rho(n_all), U(3 * n_all), Th(n_all), p(n_all);
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n_int; i++) {
         const T r = u[0][i];
         rho[i] = r;
@@ -114,9 +182,11 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
         if (m->bcU[k] == 2) sym_vec(&U[3 * (size_t)c1], m->fN + 3 * k, &U[3 * (size_t)c2]);
         else for (int c = 0; c < 3; c++) U[3 * (size_t)c2 + c] = U[3 * (size_t)c1 + c];
     }
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n_all; i++) p[i] = P0 * pow_(((rho[i] * Th[i]) * R) / P0, gam) - m->p_ref[i];
 
     std::vector<T> dr(n_slot), dm(3 * n_slot), dt_(n_slot);
+#pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < n_slot; k++) {
         const uint32_t c1 = m->FO[k], c2 = m->FN[k];
         if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
@@ -162,6 +232,7 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
     }
 
     std::vector<T> rr(n_int), rm(3 * n_int), rt(n_int);
+#pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m->n_elem; e++) {
         const int64_t base = e * NP;
         for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++)
@@ -214,6 +285,7 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
             }
         }
     }
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n_int; i++) {
         const T s = rho[i] - m->rho_ref[i];
         for (int c = 0; c < 3; c++) rm[3 * i + c] = rm[3 * i + c] - s * m->gravity[c] * m->cV[i];
@@ -224,6 +296,45 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
         L[3][i] = -(rm[3 * i + 2] / cv);
         L[4][i] = -(rt[i] / cv);
     }
+}
+
+/* Tangent-linear SSP-RK3 on K directions at once: u (values) and du[d][c]
+ * advanced in place by nsteps steps; nd <= K directions are used. */
+template <int K>
+void tlm_ssprk3(const nsem_oracle_mesh* m, double* const u[5], double* const* du, int nd,
+                double dt, int nsteps) {
+    const int64_t n = m->n_int;
+    std::vector<DualN<K>> u0[5], s[5], L[5];
+    for (int c = 0; c < 5; c++) {
+        u0[c].resize(n); s[c].resize(n); L[c].resize(n);
+        for (int64_t i = 0; i < n; i++) {
+            u0[c][i] = DualN<K>(u[c][i]);
+            for (int d = 0; d < nd; d++) u0[c][i].d[d] = du[5 * d + c][i];
+        }
+    }
+    const double a2 = 0.75, b2 = 0.25, a3 = 1.0 / 3.0, b3 = 2.0 / 3.0;
+    for (int st = 0; st < nsteps; st++) {
+        tendency<DualN<K>>(m, u0, L);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) s[c][i] = u0[c][i] + L[c][i] * dt;
+        }
+        tendency<DualN<K>>(m, s, L);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) s[c][i] = u0[c][i] * a2 + (s[c][i] + L[c][i] * dt) * b2;
+        }
+        tendency<DualN<K>>(m, s, L);
+        for (int c = 0; c < 5; c++) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; i++) u0[c][i] = u0[c][i] * a3 + (s[c][i] + L[c][i] * dt) * b3;
+        }
+    }
+    for (int c = 0; c < 5; c++)
+        for (int64_t i = 0; i < n; i++) {
+            u[c][i] = u0[c][i].v;
+            for (int d = 0; d < nd; d++) du[5 * d + c][i] = u0[c][i].d[d];
+        }
 }
 
 }  // namespace
@@ -238,42 +349,34 @@ void nsem_oracle_jvp(const nsem_oracle_mesh* m, const double* const u[5], const 
     for (int c = 0; c < 5; c++) {
         uu[c].resize(n);
         LL[c].resize(n);
-        for (int64_t i = 0; i < n; i++) uu[c][i] = Dual(u[c][i], du[c][i]);
+        for (int64_t i = 0; i < n; i++) {
+            uu[c][i] = Dual(u[c][i]);
+            uu[c][i].d[0] = du[c][i];
+        }
     }
     tendency<Dual>(m, uu, LL);
     for (int c = 0; c < 5; c++)
         for (int64_t i = 0; i < n; i++) {
             if (L) L[c][i] = LL[c][i].v;
-            Ld[c][i] = LL[c][i].d;
+            Ld[c][i] = LL[c][i].d[0];
         }
 }
 
 /* Tangent-linear SSP-RK3: advances (u, du) in place by nsteps steps. */
 void nsem_oracle_tlm_ssprk3(const nsem_oracle_mesh* m, double* const u[5], double* const du[5],
                             double dt, int nsteps) {
-    const int64_t n = m->n_int;
-    std::vector<Dual> u0[5], s[5], L[5];
-    for (int c = 0; c < 5; c++) {
-        u0[c].resize(n); s[c].resize(n); L[c].resize(n);
-        for (int64_t i = 0; i < n; i++) u0[c][i] = Dual(u[c][i], du[c][i]);
-    }
-    const double a2 = 0.75, b2 = 0.25, a3 = 1.0 / 3.0, b3 = 2.0 / 3.0;
-    for (int st = 0; st < nsteps; st++) {
-        tendency<Dual>(m, u0, L);
-        for (int c = 0; c < 5; c++)
-            for (int64_t i = 0; i < n; i++) s[c][i] = u0[c][i] + L[c][i] * dt;
-        tendency<Dual>(m, s, L);
-        for (int c = 0; c < 5; c++)
-            for (int64_t i = 0; i < n; i++) s[c][i] = u0[c][i] * a2 + (s[c][i] + L[c][i] * dt) * b2;
-        tendency<Dual>(m, s, L);
-        for (int c = 0; c < 5; c++)
-            for (int64_t i = 0; i < n; i++) u0[c][i] = u0[c][i] * a3 + (s[c][i] + L[c][i] * dt) * b3;
-    }
-    for (int c = 0; c < 5; c++)
-        for (int64_t i = 0; i < n; i++) {
-            u[c][i] = u0[c][i].v;
-            du[c][i] = u0[c][i].d;
-        }
+    tlm_ssprk3<1>(m, u, du, 1, dt, nsteps);
+}
+
+/* Same for nd <= 8 directions in one pass; du holds 5*nd arrays, direction
+ * d's variable c at du[5*d + c].  Returns 0, or -1 if nd is out of range. */
+int nsem_oracle_tlm_ssprk3_multi(const nsem_oracle_mesh* m, double* const u[5], double* const* du,
+                                 int nd, double dt, int nsteps) {
+    if (nd < 1 || nd > 8) return -1;
+    if (nd == 1) tlm_ssprk3<1>(m, u, du, 1, dt, nsteps);
+    else if (nd <= 4) tlm_ssprk3<4>(m, u, du, nd, dt, nsteps);
+    else tlm_ssprk3<8>(m, u, du, nd, dt, nsteps);
+    return 0;
 }
 
 }  // extern "C"
