@@ -155,6 +155,15 @@ nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double
  * ms_fwd / ms_adj (optional) receive the device time of the forward pass and
  * of the reverse sweep. */
 nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]);
+/* Tangent-linear counterparts (no reference counterpart either).
+ * nsem_jvp: Ld = J_L(u) dv for the current state u (dv, Ld: five host arrays
+ * of n_int doubles, SoA).
+ * nsem_tlm: advance the state by nsteps FP64 SSP-RK3 steps and propagate the
+ * perturbation du0 through the linearised steps; du_final receives it at the
+ * final state.  ms_tlm (optional) receives the device time. */
+nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]);
+nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5], double* const du_final[5],
+                     double* ms_tlm);
 nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every, double* ms_fwd);
 nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double* const lam0[5],
                          double* ms_adj);

@@ -85,6 +85,8 @@ def load(build_if_missing=True):
         "nsem_vjp": ([P, vp, vp], ctypes.c_int),
         "nsem_forward_checkpointed": ([P, ctypes.c_int, ctypes.c_int, P], ctypes.c_int),
         "nsem_adjoint": ([P, vp, vp, P], ctypes.c_int),
+        "nsem_jvp": ([P, vp, vp], ctypes.c_int),
+        "nsem_tlm": ([P, ctypes.c_int, vp, vp, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -227,6 +229,28 @@ class Solver:
         ga = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in g])
         self._check(self._lib.nsem_vjp(self._ctx, wa, ga))
         return g
+
+    def jvp(self, dv):
+        """Ld = J_L(u) dv at the current state (plain form)."""
+        n = self.n_int
+        ds = [_f64(a) for a in dv]
+        out = [np.empty(n) for _ in range(5)]
+        da = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in ds])
+        oa = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in out])
+        self._check(self._lib.nsem_jvp(self._ctx, da, oa))
+        return out
+
+    def tlm(self, nsteps, du0):
+        """Advance nsteps FP64 steps carrying the perturbation du0 through the
+        linearised steps.  Returns (du_final, device ms)."""
+        n = self.n_int
+        ds = [_f64(a) for a in du0]
+        out = [np.empty(n) for _ in range(5)]
+        da = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in ds])
+        oa = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in out])
+        ms = ctypes.c_double()
+        self._check(self._lib.nsem_tlm(self._ctx, int(nsteps), da, oa, ctypes.byref(ms)))
+        return out, ms.value
 
     def forward_checkpointed(self, nsteps, ckpt_every):
         """Advance nsteps FP64 steps keeping checkpoints; returns device ms."""

@@ -20,7 +20,9 @@
  * Kernels: k_adj_face (per used slot: adjoint of the face flux for both
  * sides, in primitive variables), k_adj_volume (per element, thread per node:
  * transposed volume gather, source, face contributions gathered through the
- * lift lists, primitive -> conserved chain rule).  FP64 throughout; this file
+ * lift lists, primitive -> conserved chain rule).  The tangent-linear product
+ * (k_tan_face, k_tan_volume) linearises the same chain in forward mode.
+ * FP64 throughout; this file
  * may use FMA contraction (the adjoint is checked to 1e-6, not bitwise).
  */
 #include <cuda_runtime.h>
@@ -316,6 +318,218 @@ __global__ void k_adj_volume(const NsemDev m, const NsemTables tab, VolAdjArgs a
     a.G[4][node] = Tb * inv;
 }
 
+/* ------------------------------------------------------------------------
+ * Tangent-linear (forward-mode) product Ld = J_L(v) dv of the same operator
+ * chain: the linearisation of every step of the forward kernels, taken at v
+ * along dv, with the same one-sided choices at non-smooth points.
+ * ------------------------------------------------------------------------ */
+struct NodeTan {
+    double r, U[3], T, p, mu, c;
+};
+
+__device__ __forceinline__ NodeTan node_tan(const NsemDev& m, const NodePrim& P,
+                                            const double* const* dS, int64_t i) {
+    NodeTan d;
+    d.r = dS[0][i];
+    const double inv = 1.0 / P.r;
+    for (int c = 0; c < 3; c++) d.U[c] = (dS[1 + c][i] - P.U[c] * d.r) * inv;
+    d.T = (dS[4][i] - P.T * d.r) * inv;
+    /* p = P0 (rho theta R / P0)^gamma: dp / p = gamma (drho / rho + dtheta / theta) */
+    d.p = m.gamma * P.p * (d.r / P.r + d.T / P.T);
+    d.mu = P.mu > 0 ? vdot3(P.U, d.U) / P.mu : 0.0;
+    d.c = P.c > 0 ? m.gR * d.T / (2 * P.c) : 0.0;
+    return d;
+}
+
+/* tangent of the SYMMETRY ghost velocity out = A p s (A = I - en en^T,
+ * s = |p| / |A p| when scaled) along dp */
+__device__ __forceinline__ void sym_jvp(const double* p, const double* en, const double* r,
+                                        double magR, double magP, bool scaled, const double* dp,
+                                        double* dout) {
+    const double dn = vdot3(dp, en);
+    const double Ad[3] = {dp[0] - en[0] * dn, dp[1] - en[1] * dn, dp[2] - en[2] * dn};
+    if (!scaled) {
+        dout[0] = Ad[0]; dout[1] = Ad[1]; dout[2] = Ad[2];
+        return;
+    }
+    const double s = magP / magR;
+    const double ds = (magP > 0 ? vdot3(p, dp) / (magP * magR) : 0.0) -
+                      magP * vdot3(r, dp) / (magR * magR * magR);
+    for (int k = 0; k < 3; k++) dout[k] = Ad[k] * s + r[k] * ds;
+}
+
+struct FaceTanArgs {
+    const double* S[5];
+    const double* dS[5];
+    double* dd[5];           /* per slot: tangent of the lifted face flux */
+};
+
+__global__ void __launch_bounds__(128) k_tan_face(const NsemDev m, FaceTanArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+
+    const NodePrim P1 = node_prim(m, a.S, c1);
+    const NodeTan d1 = node_tan(m, P1, a.dS, c1);
+    NodePrim P2;
+    NodeTan d2;
+    if (c2 >= 0) {
+        P2 = node_prim(m, a.S, c2);
+        d2 = node_tan(m, P2, a.dS, c2);
+    } else {
+        /* ghost: NEUMANN copies rho, theta, p; the velocity is copied or
+         * takes the SYMMETRY projection */
+        P2 = P1;
+        d2 = d1;
+        if (m.bc[k] == 2) {
+            double rsym[3], magR, magP;
+            bool scaled;
+            sym_fwd(P1.U, en, P2.U, rsym, magR, magP, scaled);
+            sym_jvp(P1.U, en, rsym, magR, magP, scaled, d1.U, d2.U);
+        }
+        P2.mu = sqrt(vdot3(P2.U, P2.U));
+        d2.mu = P2.mu > 0 ? vdot3(P2.U, d2.U) / P2.mu : 0.0;
+    }
+    const double lam = ((P1.mu * fi + P2.mu * fo) + (P1.c * fi + P2.c * fo)) / 2;
+    const double dlam = ((d1.mu * fi + d2.mu * fo) + (d1.c * fi + d2.c * fo)) / 2;
+    const double Fc1[3] = {P1.U[0] * P1.r, P1.U[1] * P1.r, P1.U[2] * P1.r};
+    const double Fc2[3] = {P2.U[0] * P2.r, P2.U[1] * P2.r, P2.U[2] * P2.r};
+    double dFc1[3], dFc2[3];
+    for (int c = 0; c < 3; c++) {
+        dFc1[c] = d1.U[c] * P1.r + P1.U[c] * d1.r;
+        dFc2[c] = d2.U[c] * P2.r + P2.U[c] * d2.r;
+    }
+    /* continuity: F = (U rho)_avg - lam (rho_N - rho_O) en */
+    double dd0 = 0;
+    {
+        const double jump = P2.r - P1.r, djump = d2.r - d1.r;
+        for (int c = 0; c < 3; c++)
+            dd0 += (dFc1[c] * fi + dFc2[c] * fo - (dlam * jump + lam * djump) * en[c]) * n[c];
+    }
+    /* momentum: F[r][c] = (Fc U + p' I)_avg[r][c] - lam (Fc_N - Fc_O)[c] en[r] */
+    double ddm[3];
+    for (int r = 0; r < 3; r++) {
+        double acc = 0;
+        for (int c = 0; c < 3; c++) {
+            const double dA = dFc1[r] * P1.U[c] + Fc1[r] * d1.U[c] + (r == c ? d1.p : 0.0);
+            const double dB = dFc2[r] * P2.U[c] + Fc2[r] * d2.U[c] + (r == c ? d2.p : 0.0);
+            const double ddq = (dFc2[c] - dFc1[c]) * lam + (Fc2[c] - Fc1[c]) * dlam;
+            acc += (dA * fi + dB * fo - ddq * en[r]) * n[c];
+        }
+        ddm[r] = acc;
+    }
+    /* potential temperature: F = (U rho theta)_avg - lam (rho theta_N - rho theta_O) en */
+    double dd4 = 0;
+    {
+        const double e1 = P1.r * P1.T, e2 = P2.r * P2.T;
+        const double de1 = d1.r * P1.T + P1.r * d1.T, de2 = d2.r * P2.T + P2.r * d2.T;
+        for (int c = 0; c < 3; c++) {
+            const double f1 = dFc1[c] * P1.T + Fc1[c] * d1.T;
+            const double f2 = dFc2[c] * P2.T + Fc2[c] * d2.T;
+            dd4 += (f1 * fi + f2 * fo - (dlam * (e2 - e1) + lam * (de2 - de1)) * en[c]) * n[c];
+        }
+    }
+    a.dd[0][k] = dd0; a.dd[1][k] = ddm[0]; a.dd[2][k] = ddm[1]; a.dd[3][k] = ddm[2];
+    a.dd[4][k] = dd4;
+}
+
+struct VolTanArgs {
+    const double* S[5];
+    const double* dS[5];
+    const double* dd[5];
+    double* out[5];          /* J_L(v) dv */
+};
+
+/* shared layout per node: dfr[3] dfm[9] dft[3] jin[9] */
+constexpr int TAN_W = 24;
+
+__global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a) {
+    extern __shared__ double sm[];
+    const int NPX = m.npx, NPY = m.npy, NPZ = m.npz, NP = m.np;
+    double* dps = sm + (size_t)NP * TAN_W;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    double drho = 0;
+    if (active) {
+        const NodePrim P = node_prim(m, a.S, node);
+        const NodeTan d = node_tan(m, P, a.dS, node);
+        drho = d.r;
+        double* my = sm + (size_t)t * TAN_W;
+        const double Fc[3] = {P.U[0] * P.r, P.U[1] * P.r, P.U[2] * P.r};
+        double dFc[3];
+        for (int c = 0; c < 3; c++) dFc[c] = d.U[c] * P.r + P.U[c] * d.r;
+        for (int c = 0; c < 3; c++) my[c] = dFc[c];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                const int idx = (r == c) ? r : (r == 0 && c == 1) ? XY : (r == 1 && c == 2) ? YZ
+                              : (r == 0 && c == 2) ? XZ : (r == 1 && c == 0) ? YX
+                              : (r == 2 && c == 1) ? ZY : ZX;
+                my[3 + idx] = dFc[r] * P.U[c] + Fc[r] * d.U[c] + (r == c ? d.p : 0.0);
+            }
+        for (int c = 0; c < 3; c++) my[12 + c] = dFc[c] * P.T + Fc[c] * d.T;
+        for (int c = 0; c < 9; c++) my[15 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
+    double r[5] = {0, 0, 0, 0, 0};
+    /* surface lift */
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        const double sg = (code & 1) ? -1.0 : 1.0;
+        for (int v = 0; v < 5; v++) r[v] += sg * a.dd[v][k];
+    }
+    /* volume term: r[a] -= dF_b . (Jin_b dpsi(b -> a)) over the lines through a */
+    const double* Dx = dps;
+    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    auto apply = [&](int lb, const double* dj) {
+        const double* sb = sm + (size_t)lb * TAN_W;
+        r[0] -= vdot3(sb, dj);
+        const double* F = sb + 3;
+        r[1] -= F[XX] * dj[0] + F[XY] * dj[1] + F[XZ] * dj[2];
+        r[2] -= F[YX] * dj[0] + F[YY] * dj[1] + F[YZ] * dj[2];
+        r[3] -= F[ZX] * dj[0] + F[ZY] * dj[1] + F[ZZ] * dj[2];
+        r[4] -= vdot3(sb + 12, dj);
+    };
+    auto line = [&](int dir, int lb, double D) {
+        const double* J = sm + (size_t)lb * TAN_W + 15;
+        double dj[3];
+        if (dir == 0) { dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D; }
+        else if (dir == 1) { dj[0] = J[XY] * D; dj[1] = J[YY] * D; dj[2] = J[ZY] * D; }
+        else { dj[0] = J[XZ] * D; dj[1] = J[YZ] * D; dj[2] = J[ZZ] * D; }
+        apply(lb, dj);
+    };
+    const int sx = NPY * NPZ, sy = NPZ;
+    for (int ii = 0; ii < NPX; ii++)
+        if (ii != ia) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
+    for (int jj = 0; jj < NPY; jj++)
+        if (jj != ja) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
+    for (int kk = 0; kk < NPZ; kk++)
+        if (kk != ka) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
+    {
+        const double* J = sm + (size_t)t * TAN_W + 15;
+        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
+        const double dj[3] = {J[XX] * dv[0] + J[XY] * dv[1] + J[XZ] * dv[2],
+                              J[YX] * dv[0] + J[YY] * dv[1] + J[YZ] * dv[2],
+                              J[ZX] * dv[0] + J[ZY] * dv[1] + J[ZZ] * dv[2]};
+        apply(t, dj);
+    }
+    /* gravity source: r_m -= g (rho - rho_ref) cV */
+    const double cv = m.cv[node];
+    for (int c = 0; c < 3; c++) r[1 + c] -= m.g[c] * drho * cv;
+    for (int v = 0; v < 5; v++) a.out[v][node] = -(r[v] / cv);
+}
+
 /* lam = c0 * lam + c1 * x + c2 * y (elementwise over 5 arrays) */
 struct Lin3Args {
     double* out[5];
@@ -362,6 +576,21 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
     return (int)cudaGetLastError();
 }
 
+int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
+                 const double* const* dS, double* const* out, NsemAdjBuf* ab, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    FaceTanArgs fa;
+    for (int v = 0; v < 5; v++) { fa.S[v] = S[v]; fa.dS[v] = dS[v]; fa.dd[v] = ab->adjO[v]; }
+    const int64_t fb = (m->n_slot + 127) / 128;
+    k_tan_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
+    VolTanArgs va;
+    for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.dS[v] = dS[v]; va.dd[v] = ab->adjO[v]; va.out[v] = out[v]; }
+    const int threads = ((m->np + 31) / 32) * 32;
+    const size_t smem = ((size_t)m->np * TAN_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+    k_tan_volume<<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
+    return (int)cudaGetLastError();
+}
+
 int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const double* const* y,
                   double cy, const double* const* z, double cz, int64_t n, void* stream) {
     Lin3Args a;
@@ -378,8 +607,14 @@ int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const d
 
 int nsem_adj_prepare(const NsemDev* m) {
     const size_t smem = (5 * (size_t)m->np + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
-    if (smem > 48 * 1024)
-        return (int)cudaFuncSetAttribute(k_adj_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    if (smem > 48 * 1024) {
+        const int e = (int)cudaFuncSetAttribute(k_adj_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem);
+        if (e) return e;
+    }
+    const size_t tsm = ((size_t)m->np * TAN_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+    if (tsm > 48 * 1024)
+        return (int)cudaFuncSetAttribute(k_tan_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tsm);
     return 0;
 }

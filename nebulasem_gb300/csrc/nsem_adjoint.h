@@ -19,6 +19,7 @@ struct NsemAdjBuf {
     double* fin[5] = {};    /* final forward state (restored afterwards)  */
     double* ckpt = nullptr; /* [n_ckpt][5][n_int] states every k steps     */
     double* seg = nullptr;  /* [k][3][5][n_int] u^n, u1, u2 of a segment   */
+    int64_t seg_slots = 0;  /* state slots allocated in seg                 */
     int nsteps = 0, every = 0, n_ckpt = 0;
     bool ready = false;
 };
@@ -26,6 +27,9 @@ struct NsemAdjBuf {
 /* g = J_L(S)^T W (all device pointers, 5 SoA arrays each) */
 int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
                  const double* const* W, double* const* G, NsemAdjBuf* ab, void* stream);
+/* out = J_L(S) dS (tangent-linear product; uses ab->adjO[0..4] as slot scratch) */
+int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
+                 const double* const* dS, double* const* out, NsemAdjBuf* ab, void* stream);
 /* out = cx x + cy y + cz z (y, z may be null) */
 int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const double* const* y,
                   double cy, const double* const* z, double cz, int64_t n, void* stream);

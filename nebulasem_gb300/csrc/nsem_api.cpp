@@ -560,6 +560,93 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
     return check_status(ctx);
 }
 
+extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
+    for (int v = 0; v < 5; v++)
+        if (!dv[v] || !Ld[v]) return fail(ctx, NSEM_BAD_ARG, "dv[v] or Ld[v] is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status s = ensure_rep(ctx, 0);
+    if (s != NSEM_OK) return s;
+    if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
+    NsemAdjBuf& A = ctx->abuf;
+    const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(A.lam[v], dv[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    int e = nsem_adj_jvp(&ctx->dev, &ctx->tab, ctx->buf.u, A.lam, A.g, &A, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "jvp");
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(Ld[v], A.g[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
+                                double* const du_final[5], double* ms_tlm) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
+    if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
+    for (int v = 0; v < 5; v++)
+        if (!du0[v] || !du_final[v]) return fail(ctx, NSEM_BAD_ARG, "du array is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status s = ensure_rep(ctx, 0);
+    if (s != NSEM_OK) return s;
+    if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
+    NsemAdjBuf& A = ctx->abuf;
+    const int64_t n = ctx->dev.n_int;
+    const size_t bytes = (size_t)n * sizeof(double);
+    /* stage states of one step: u^n, u1, u2 */
+    if (!A.seg || A.seg_slots < 3) {
+        if (A.seg) { cudaFree(A.seg); A.seg = nullptr; }
+        if (cudaMalloc((void**)&A.seg, (size_t)3 * 5 * n * sizeof(double)) != cudaSuccess)
+            return fail(ctx, NSEM_NO_MEMORY, "stage-state allocation failed");
+        A.seg_slots = 3;
+    }
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(A.lam[v], du0[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    const double dt = ctx->dt;
+    void* st = (void*)ctx->stream;
+    cudaEvent_t e0, e1;
+    NSEM_CUDA(cudaEventCreate(&e0));
+    NSEM_CUDA(cudaEventCreate(&e1));
+    NSEM_CUDA(cudaEventRecord(e0, ctx->stream));
+    int e = 0;
+    double *u0[5], *u1[5], *u2[5];
+    slots(A.seg, 0, n, u0);
+    slots(A.seg, 1, n, u1);
+    slots(A.seg, 2, n, u2);
+    for (int step = 0; step < nsteps && s == NSEM_OK && !e; step++) {
+        if ((s = copy_state(ctx, u0, ctx->buf.u)) != NSEM_OK) break;
+        if ((s = fp64_step(ctx, u1, u2)) != NSEM_OK) break;
+        /* du1 = du + dt J(u^n) du */
+        if ((e = nsem_adj_jvp(&ctx->dev, &ctx->tab, u0, A.lam, A.g, &A, st))) break;
+        if ((e = nsem_adj_lin3(A.lu1, A.lam, 1.0, A.g, dt, nullptr, 0, n, st))) break;
+        /* du2 = 3/4 du + 1/4 (du1 + dt J(u1) du1) */
+        if ((e = nsem_adj_jvp(&ctx->dev, &ctx->tab, u1, A.lu1, A.g, &A, st))) break;
+        if ((e = nsem_adj_lin3(A.lu2, A.lam, 0.75, A.lu1, 0.25, A.g, 0.25 * dt, n, st))) break;
+        /* du^{n+1} = 1/3 du + 2/3 (du2 + dt J(u2) du2) */
+        if ((e = nsem_adj_jvp(&ctx->dev, &ctx->tab, u2, A.lu2, A.g, &A, st))) break;
+        if ((e = nsem_adj_lin3(A.lam, A.lam, 1.0 / 3.0, A.lu2, 2.0 / 3.0, A.g, 2.0 / 3.0 * dt, n, st))) break;
+    }
+    if (e) s = cuda_fail(ctx, (cudaError_t)e, "tangent-linear sweep");
+    if (s != NSEM_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return s;
+    }
+    NSEM_CUDA(cudaEventRecord(e1, ctx->stream));
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(du_final[v], A.lam[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->rep = 0;
+    s = check_status(ctx);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != NSEM_OK) return s;
+    if (ms_tlm) *ms_tlm = ms;
+    return NSEM_OK;
+}
+
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
     if (!ctx) return NSEM_BAD_ARG;
@@ -577,6 +664,7 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
     if (ce != cudaSuccess) return fail(ctx, NSEM_NO_MEMORY, "checkpoint allocation failed");
     ce = cudaMalloc((void**)&A.seg, (size_t)ckpt_every * 3 * 5 * n * sizeof(double));
     if (ce != cudaSuccess) return fail(ctx, NSEM_NO_MEMORY, "segment allocation failed");
+    A.seg_slots = 3 * (int64_t)ckpt_every;
     cudaEvent_t e0, e1;
     NSEM_CUDA(cudaEventCreate(&e0));
     NSEM_CUDA(cudaEventCreate(&e1));
