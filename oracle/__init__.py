@@ -41,6 +41,7 @@ class _Mesh(ctypes.Structure):
         ("bcU", ctypes.c_void_p), ("p_ref", ctypes.c_void_p), ("rho_ref", ctypes.c_void_p),
         ("gravity", ctypes.c_double * 3),
         ("P0", ctypes.c_double), ("R", ctypes.c_double), ("gamma", ctypes.c_double),
+        ("T0", ctypes.c_double),
     ]
 
 
@@ -64,6 +65,9 @@ def lib():
         _lib.nsem_oracle_tlm_ssprk3_multi.argtypes = [ctypes.POINTER(_Mesh), P, P, ctypes.c_int,
                                                       ctypes.c_double, ctypes.c_int]
         _lib.nsem_oracle_tlm_ssprk3_multi.restype = ctypes.c_int
+        _lib.nsem_oracle_segregated.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_double, ctypes.c_int]
     return _lib
 
 
@@ -124,6 +128,7 @@ class OracleMesh:
         cp, cv = float(g.get("cp", 1004.5)), float(g.get("cv", 717.5))
         s.R = float(g.get("R", cp - cv))
         s.gamma = float(g.get("gamma", cp / cv))
+        s.T0 = float(g.get("T0", 300.0))
         self.cv_heat = cv
         self.struct = s
         self.gh = f64("gh") if "gh" in g else None
@@ -180,6 +185,17 @@ class OracleMesh:
         if rc != 0:
             raise ValueError("tlm_ssprk3_multi: 1 <= directions <= 8")
         return ua, [da[5 * d:5 * d + 5] for d in range(nd)]
+
+    def segregated(self, rho, U, T, dt, nsteps):
+        """The reference's segregated forward-Euler steps on the primitive
+        fields rho, U (n_int x 3), T = theta'; returns the advanced copies."""
+        r = np.array(rho, dtype=np.float64, copy=True)
+        u = np.ascontiguousarray(np.array(U, dtype=np.float64, copy=True).reshape(-1, 3))
+        t = np.array(T, dtype=np.float64, copy=True)
+        assert r.shape == (self.n_int,) and u.shape == (self.n_int, 3) and t.shape == (self.n_int,)
+        lib().nsem_oracle_segregated(ctypes.byref(self.struct), _ptr(r), _ptr(u), _ptr(t),
+                                     float(dt), int(nsteps))
+        return r, u, t
 
     def diagnostics(self, u):
         _, up = self._vec(u)

@@ -395,3 +395,231 @@ void nsem_oracle_diagnostics(const nsem_oracle_mesh* m, const double* const u[5]
     work_free(&w);
     out[0] = mass; out[1] = energy; out[2] = vol;
 }
+
+/* ------------------------------------------------------------------------
+ * The reference's own time update (apps/euler/euler.cpp:179-287 with
+ * time_scheme BDF1, diffusion NO): segregated forward Euler over the
+ * primitive fields.  Per step, on every node including the ghosts:
+ *   T += T0; lambda from U^n, T^n; rho-eq with flux U rho^n, state rho^n;
+ *   rho^{n+1} = Su/ap (ddt, field.h:3741-3841 BDF1: ap = (-1/dt) cV,
+ *   Su += rho^n ap; SolveTexplicit, solve.cpp:563-564) and Neumann ghosts;
+ *   p' from rho^{n+1}, T^n; U-eq with flux (rho^n U^n) (x) U^n + p' I, state
+ *   rho^{n+1} U^n, source (rho^{n+1} - rho_ref) g; U^{n+1} = Su/ap with
+ *   ap = (-1/dt) cV rho^{n+1}, Su += (U^n rho^n)(-1/dt) cV; symmetry ghosts;
+ *   T-eq with flux (rho^n U^n) T^n, state rho^{n+1} T^n, the same update;
+ *   T -= T0.
+ * ------------------------------------------------------------------------ */
+
+/* ghosts of a scalar (Neumann) and of the velocity (per slot BC) */
+static void ghosts_scalar(const nsem_oracle_mesh* m, double* f) {
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    for (int64_t k = 0; k < n_slot; k++) {
+        if (!m->bcU[k]) continue;
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c2 >= (uint32_t)m->n_all) continue;
+        f[c2] = neumann(m, f, c1, c2);
+    }
+}
+
+static void ghosts_velocity(const nsem_oracle_mesh* m, double* U) {
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    for (int64_t k = 0; k < n_slot; k++) {
+        if (!m->bcU[k]) continue;
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c2 >= (uint32_t)m->n_all) continue;
+        if (m->bcU[k] == 2) {
+            sym_vec(U + 3 * (size_t)c1, m->fN + 3 * k, U + 3 * (size_t)c2);
+        } else {
+            const double* a = m->cC + 3 * (size_t)c1;
+            const double* b = m->cC + 3 * (size_t)c2;
+            double dv[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+            for (int c = 0; c < 3; c++)
+                U[3 * (size_t)c2 + c] = U[3 * (size_t)c1 + c] + 0.0 * vmag(dv);
+        }
+    }
+}
+
+/* weak divergence Su of one equation (field.h:3417-3478): lift of the per-slot
+ * fluxes d (ncomp per slot) in the cell's face order, then the volume term of
+ * the nodal flux F (ncomp x 3 per node: Vector flux for ncomp 1, Tensor for 3) */
+static void seg_divf(const nsem_oracle_mesh* m, int ncomp, const double* F, const double* d,
+                     double* r) {
+    const int32_t NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
+    const int64_t n_all = m->n_all;
+    const int w = ncomp == 1 ? 3 : 9;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m->n_elem; e++) {
+        const int64_t base = e * NP;
+        for (int32_t a = 0; a < NP; a++)
+            for (int c = 0; c < ncomp; c++) r[ncomp * (base + a) + c] = 0.0;
+        for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
+            for (int32_t nn = 0; nn < NPF; nn++) {
+                int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
+                uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                if (c1 >= base && c1 < base + NP) {
+                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c1 + c] += d[ncomp * k + c];
+                } else if (c2 < (uint32_t)n_all) {
+                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c2 + c] -= d[ncomp * k + c];
+                }
+            }
+        }
+        for (int32_t ii = 0; ii < NPX; ii++)
+        for (int32_t jj = 0; jj < NPY; jj++)
+        for (int32_t kk = 0; kk < NPZ; kk++) {
+            const int64_t b = base + (int64_t)ii * NPY * NPZ + jj * NPZ + kk;
+            double Jin[9];
+            for (int c = 0; c < 9; c++) Jin[c] = m->Jinv[9 * b + c] * m->cV[b];
+            const double* Fb = F + (size_t)w * b;
+            for (int pass = 0; pass < 3; pass++) {
+                const int32_t lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
+                for (int32_t q = 0; q < lim; q++) {
+                    int32_t im = ii, jm = jj, km = kk;
+                    if (pass == 0) im = q;
+                    else if (pass == 1) { if (q == jj) continue; jm = q; }
+                    else { if (q == kk) continue; km = q; }
+                    const int64_t a = base + (int64_t)im * NPY * NPZ + jm * NPZ + km;
+                    double dv[3], dj[3];
+                    dv[0] = m->dpsi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[1] = m->psi[0][ii * NPX + im] * m->dpsi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[2] = m->psi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->dpsi[2][kk * NPZ + km];
+                    tdot(Jin, dv, dj);
+                    if (ncomp == 1) {
+                        r[a] -= vdot(Fb, dj);
+                    } else {
+                        double t[3];
+                        tdot(Fb, dj, t);
+                        r[3 * a + 0] -= t[0];
+                        r[3 * a + 1] -= t[1];
+                        r[3 * a + 2] -= t[2];
+                    }
+                }
+            }
+        }
+    }
+}
+
+void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U_in, double* T_in,
+                            double dt, int nsteps) {
+    const int64_t n_int = m->n_int, n_all = m->n_all;
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    const size_t na = (size_t)n_all + (size_t)m->np;
+    const double P0 = m->P0, R = m->R, gam = m->gamma, T0 = m->T0;
+    double* rho = calloc(na, sizeof(double));
+    double* rhof = calloc(na, sizeof(double));
+    double* U = calloc(3 * na, sizeof(double));
+    double* T = calloc(na, sizeof(double));
+    double* p = calloc(na, sizeof(double));
+    double* lam = calloc((size_t)n_slot, sizeof(double));
+    double* Fv = calloc(9 * na, sizeof(double));
+    double* q = calloc(3 * na, sizeof(double));
+    double* d = calloc(3 * (size_t)n_slot, sizeof(double));
+    double* r = calloc(3 * na, sizeof(double));
+    double* Fc = calloc(3 * na, sizeof(double));
+    memcpy(rho, rho_in, (size_t)n_int * sizeof(double));
+    memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
+    memcpy(T, T_in, (size_t)n_int * sizeof(double));
+    ghosts_scalar(m, rho);
+    ghosts_velocity(m, U);
+    ghosts_scalar(m, T);
+    const double c_dt = -1.0 / dt;
+    for (int step = 0; step < nsteps; step++) {
+        for (int64_t i = 0; i < n_all; i++) T[i] += T0;
+        memcpy(rhof, rho, (size_t)n_all * sizeof(double));
+        /* Fc = flxc(rho U), lambda = (cds|U| + cds sqrt(gamma R T)) / 2 */
+        for (int64_t i = 0; i < n_all; i++)
+            for (int c = 0; c < 3; c++) Fc[3 * i + c] = rho[i] * U[3 * i + c];
+        const double gR = gam * R;
+        for (int64_t k = 0; k < n_slot; k++) {
+            uint32_t c1 = m->FO[k], c2 = m->FN[k];
+            if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+            const double fi = m->fI[k], fo = 1 - fi;
+            lam[k] = ((vmag(U + 3 * (size_t)c1) * fi + vmag(U + 3 * (size_t)c2) * fo) +
+                      (sqrt(gR * T[c1]) * fi + sqrt(gR * T[c2]) * fo)) / 2;
+        }
+        /* rho equation: flux U rho, state rho */
+        for (int64_t i = 0; i < n_all; i++)
+            for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * rho[i];
+        for (int64_t k = 0; k < n_slot; k++) {
+            uint32_t c1 = m->FO[k], c2 = m->FN[k];
+            if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+            const double fi = m->fI[k], fo = 1 - fi;
+            const double* n = m->fN + 3 * k;
+            const double mgn = vmag(n);
+            const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+            double F[3], jump = lam[k] * (rho[c2] - rho[c1]);
+            for (int c = 0; c < 3; c++)
+                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            d[k] = vdot(F, n);
+        }
+        seg_divf(m, 1, Fv, d, r);
+        for (int64_t i = 0; i < n_int; i++) {
+            const double ap = c_dt * m->cV[i];
+            rho[i] = (r[i] + rho[i] * ap) / (0.0 + ap);
+        }
+        ghosts_scalar(m, rho);
+        /* p' from the new rho and the old theta */
+        for (int64_t i = 0; i < n_all; i++) p[i] = P0 * eos_pow(((rho[i] * T[i]) * R) / P0, gam);
+        ghosts_scalar(m, p);
+        for (int64_t i = 0; i < n_all; i++) p[i] -= m->p_ref[i];
+        /* U equation: flux Fc (x) U + p' I, state rho U */
+        for (int64_t i = 0; i < n_all; i++) {
+            double* Ft = Fv + 9 * i;
+            outer(Fc + 3 * i, U + 3 * i, Ft);
+            for (int c = 0; c < 9; c++) Ft[c] = Ft[c] + ((c < 3) ? 1.0 : 0.0) * p[i];
+            for (int c = 0; c < 3; c++) q[3 * i + c] = rho[i] * U[3 * i + c];
+        }
+        for (int64_t k = 0; k < n_slot; k++) {
+            uint32_t c1 = m->FO[k], c2 = m->FN[k];
+            if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+            const double fi = m->fI[k], fo = 1 - fi;
+            const double* n = m->fN + 3 * k;
+            const double mgn = vmag(n);
+            const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+            double dq[3], O[9], F[9];
+            for (int c = 0; c < 3; c++) dq[c] = (q[3 * (size_t)c2 + c] - q[3 * (size_t)c1 + c]) * lam[k];
+            outer(en, dq, O);
+            for (int c = 0; c < 9; c++) F[c] = (Fv[9 * (size_t)c1 + c] * fi + Fv[9 * (size_t)c2 + c] * fo) - O[c];
+            tdot(F, n, d + 3 * k);
+        }
+        seg_divf(m, 3, Fv, d, r);
+        for (int64_t i = 0; i < n_int; i++) {
+            const double s = rho[i] - m->rho_ref[i];
+            const double ap0 = c_dt * m->cV[i];
+            const double ap = ap0 * rho[i];
+            for (int c = 0; c < 3; c++) {
+                const double sc = 0.0 + m->gravity[c] * s;
+                const double su = r[3 * i + c] - sc * m->cV[i];
+                U[3 * i + c] = (su + (U[3 * i + c] * rhof[i]) * ap0) / (0.0 + ap);
+            }
+        }
+        ghosts_velocity(m, U);
+        /* T equation: flux Fc T, state rho T (U no longer enters) */
+        for (int64_t i = 0; i < n_all; i++)
+            for (int c = 0; c < 3; c++) Fv[3 * i + c] = Fc[3 * i + c] * T[i];
+        for (int64_t k = 0; k < n_slot; k++) {
+            uint32_t c1 = m->FO[k], c2 = m->FN[k];
+            if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+            const double fi = m->fI[k], fo = 1 - fi;
+            const double* n = m->fN + 3 * k;
+            const double mgn = vmag(n);
+            const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+            double F[3], jump = lam[k] * (rho[c2] * T[c2] - rho[c1] * T[c1]);
+            for (int c = 0; c < 3; c++)
+                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            d[k] = vdot(F, n);
+        }
+        seg_divf(m, 1, Fv, d, r);
+        for (int64_t i = 0; i < n_int; i++) {
+            const double ap0 = c_dt * m->cV[i];
+            const double ap = ap0 * rho[i];
+            T[i] = (r[i] + (T[i] * rhof[i]) * ap0) / (0.0 + ap);
+        }
+        ghosts_scalar(m, T);
+        for (int64_t i = 0; i < n_all; i++) T[i] -= T0;
+    }
+    memcpy(rho_in, rho, (size_t)n_int * sizeof(double));
+    memcpy(U_in, U, 3 * (size_t)n_int * sizeof(double));
+    memcpy(T_in, T, (size_t)n_int * sizeof(double));
+    free(rho); free(rhof); free(U); free(T); free(p); free(lam); free(Fv); free(q); free(d);
+    free(r); free(Fc);
+}

@@ -49,6 +49,7 @@ typedef struct {
     const double* rho_ref;  /* [n_all] hydrostatic density            */
     double gravity[3];
     double P0, R, gamma;
+    double T0;              /* background potential temperature (segregated scheme) */
 } nsem_oracle_mesh;
 
 /* pow used for the equation of state: 0 = C library pow (as the reference),
@@ -84,6 +85,12 @@ void nsem_oracle_tlm_ssprk3(const nsem_oracle_mesh* m, double* const u[5], doubl
  * variable c.  Returns 0, or -1 if nd is out of range. */
 int nsem_oracle_tlm_ssprk3_multi(const nsem_oracle_mesh* m, double* const u[5], double* const* du,
                                  int nd, double dt, int nsteps);
+
+/* The reference's own segregated forward-Euler update (euler.cpp:179-287,
+ * BDF1, no diffusion) on the primitive fields: rho[n_int], U[n_int*3] (AoS),
+ * T[n_int] = theta' (perturbation), advanced in place by nsteps steps. */
+void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho, double* U, double* T,
+                            double dt, int nsteps);
 
 int nsem_oracle_threads(void);
 

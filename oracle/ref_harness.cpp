@@ -9,7 +9,7 @@
  * geometry, initial state, right-hand sides and SSP-RK3 trajectories as raw
  * little-endian float64 / uint32 files for the golden fixtures.
  *
- *   euler_oracle <controls> setup <outdir>
+ *   euler_oracle <controls> setup <outdir>   (also fld_rho/U/T: the step-0 fields)
  *   euler_oracle <controls> rk3 <outdir> <nsteps> <dump_every> [pert]
  *   euler_oracle <controls> rk3time <nsteps>
  *
@@ -323,6 +323,14 @@ int main(int argc, char* argv[]) {
 
     m.rho = &rho; m.U = &U; m.T = &T; m.p = &p; m.g = &g;
     m.p_ref = &p_ref; m.rho_ref = &rho_ref; m.gh = &gh;
+
+    /* the solver's own fields at step 0 (rho, U, T = theta'), as the euler
+     * app holds them when its time loop starts */
+    if (mode == "setup") {
+        dump_raw("fld_rho.f64", &rho[0], Mesh::gBCSfield);
+        dump_raw("fld_U.f64", &U[0][0], 3 * (size_t)Mesh::gBCSfield);
+        dump_raw("fld_T.f64", &T[0], Mesh::gBCSfield);
+    }
 
     /* T holds theta' in the reference's files; stages use full theta */
     T += T0;

@@ -12,6 +12,12 @@ rusanov / applyExplicitBCs), and stores per case one compressed .npz:
             velocity perturbation), Lp_*, p0prime/ppprime (p - p_ref),
             traj_<step>_* (coupled SSP-RK3 states after <step> steps)
 
+Segregated-scheme fixtures (seg_<case>.npz): the unmodified reference `euler`
+binary (its own time loop, euler.cpp:179-287, BDF1) runs the case for N steps
+and writes its fields; stored are the geometry, the step-0 fields as the solver
+holds them (rho, U, T = theta', from the harness) and the binary's step-N
+fields read back from its binary field files.
+
 Run in the build container (the reference is not present on GPU machines):
   python tests/golden/make_golden.py --ref /root/reference
 """
@@ -39,6 +45,12 @@ PLAN = {
     "g3_2": (0.01, "pert", [20], 20),
     "g3_4n3": (0.01, "pert", [10, 30], 30),
     "g3_2n7": (0.005, "pert", [10], 10),
+}
+
+# case -> (dt, steps) for the segregated scheme, at steps the scheme keeps stable
+SEG_PLAN = {
+    "c1_2d": (0.005, 100),
+    "g3_2": (0.005, 30),
 }
 
 KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
@@ -86,10 +98,38 @@ def make_case(name, ref_bin, tmp):
     print(f"{name}: {n_int} interior nodes -> {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
 
 
+def make_seg_case(name, ref_bin, tmp):
+    from nebulasem_gb300.fields import read_field
+    dt, nsteps = SEG_PLAN[name]
+    case = os.path.join(tmp, "seg_" + name)
+    write_case(case, dt=dt, steps=nsteps, **CASES[name])
+    run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    os.makedirs(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
+    d = load_dump(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler"), "./controls"], case)
+    n_int = int(d["meta"][7])
+    out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    out["fld0_rho"] = d["fld_rho"][:n_int]
+    out["fld0_U"] = d["fld_U"][:3 * n_int]
+    out["fld0_T"] = d["fld_T"][:n_int]
+    for f in ("rho", "U", "T"):
+        v = read_field(os.path.join(case, f"{f}1.bin")).values
+        assert v.shape[0] == n_int
+        out[f"fldN_{f}"] = v.reshape(-1)
+    out["dt"] = np.float64(dt)
+    out["nsteps"] = np.int64(nsteps)
+    path = os.path.join(HERE, f"seg_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"seg_{name}: {n_int} interior nodes, {nsteps} steps -> {path} "
+          f"({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", required=True, help="reference NebulaSEM source tree")
     ap.add_argument("--cases", nargs="*", default=sorted(PLAN))
+    ap.add_argument("--seg-cases", nargs="*", default=sorted(SEG_PLAN))
     ap.add_argument("-j", type=int, default=8)
     a = ap.parse_args()
     subprocess.run(["make", "-f", "oracle/Makefile.ref", f"REF={a.ref}", f"-j{a.j}"],
@@ -99,6 +139,8 @@ def main():
     try:
         for name in a.cases:
             make_case(name, ref_bin, tmp)
+        for name in a.seg_cases:
+            make_seg_case(name, ref_bin, tmp)
     finally:
         shutil.rmtree(tmp)
 
