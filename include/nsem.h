@@ -59,7 +59,10 @@ typedef enum {
 } nsem_precision;
 
 typedef enum {
-    NSEM_SSPRK3 = 0  /* coupled Shu-Osher SSP-RK3 */
+    NSEM_SSPRK3 = 0,         /* coupled Shu-Osher SSP-RK3                              */
+    NSEM_REF_SEGREGATED = 1  /* the reference's own update: segregated forward Euler
+                              * (rho, then U, then T; euler.cpp:179-287, BDF1) on the
+                              * primitive fields, FP64 only */
 } nsem_scheme;
 
 /* Mesh in the reference's own layout (Mesh:: and DG:: globals after

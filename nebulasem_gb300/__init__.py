@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libnsem_gpu.so")
 FP64 = 0
 MIXED = 1
 SSPRK3 = 0
+REF_SEGREGATED = 1
 
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "CUDA_ERROR", 3: "NONFINITE", 4: "TIMEOUT",
           5: "UNSUPPORTED", 6: "NO_MEMORY", 7: "TOO_LARGE"}
@@ -271,6 +272,19 @@ class Solver:
         self._check(self._lib.nsem_adjoint(self._ctx, la, oa, ctypes.byref(ms)))
         return out, ms.value
 
+    def set_fields(self, rho, U, T):
+        """The euler app's fields: rho, U (n_int x 3), T = theta' (kept as given)."""
+        r = _f64(rho)
+        u = np.ascontiguousarray(np.asarray(U, dtype=np.float64).reshape(-1, 3))
+        t = _f64(T)
+        self._check(self._lib.nsem_set_fields(self._ctx, _p(r), _p(u), _p(t)))
+
+    def get_fields(self):
+        n = self.n_int
+        r, u, t = np.empty(n), np.empty((n, 3)), np.empty(n)
+        self._check(self._lib.nsem_get_fields(self._ctx, _p(r), _p(u), _p(t)))
+        return r, u, t
+
     def get_state(self):
         n = self.n_int
         rho, mom, rt = np.empty(n), np.empty((n, 3)), np.empty(n)
@@ -285,8 +299,8 @@ class Solver:
         self._check(self._lib.nsem_tendency(self._ctx, prec, arr, _p(p)))
         return (L, p) if return_p else L
 
-    def step(self, nsteps, prec=FP64, sync=True):
-        self._check(self._lib.nsem_step(self._ctx, int(nsteps), SSPRK3, prec))
+    def step(self, nsteps, prec=FP64, sync=True, scheme=SSPRK3):
+        self._check(self._lib.nsem_step(self._ctx, int(nsteps), scheme, prec))
         if sync:
             self._check(self._lib.nsem_sync(self._ctx))
 

@@ -29,6 +29,7 @@ UNITS = [
     ("nsem_aux.cu", EXACT),
     ("nsem_mixed.cu", []),
     ("nsem_noalloc.cu", EXACT),
+    ("nsem_seg.cu", EXACT),
     ("nsem_adjoint.cu", []),
 ]
 

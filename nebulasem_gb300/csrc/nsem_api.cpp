@@ -22,6 +22,7 @@
 #include "nsem_internal.h"
 #include "nsem_adjoint.h"
 #include "nsem_mixed.h"
+#include "nsem_seg.h"
 
 struct nsem_ctx {
     int device = 0;
@@ -31,8 +32,11 @@ struct nsem_ctx {
     NsemBuf buf{};
     NsemMixedBuf mbuf{};
     NsemAdjBuf abuf{};
+    NsemSegBuf sbuf{};
     bool mixed_ready = false;
-    int rep = 0;                     /* 0: state in buf.u; 1: perturbation in mbuf.U[cur] */
+    /* where the state lives: 0 conserved in buf.u; 1 perturbation in
+     * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme) */
+    int rep = 0;
     double dt = 0, T0 = 0;
     int64_t n_all = 0;
     std::vector<void*> allocations;
@@ -40,7 +44,7 @@ struct nsem_ctx {
     double* red = nullptr;           /* reduction partials */
     double* h_red = nullptr;         /* pinned host copy of the reduction result */
     uint32_t* h_status = nullptr;    /* pinned host copy of the status word */
-    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  /* key: (prec*2 + cur, nsteps) */
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  /* key: (form*2 + cur, nsteps) */
     std::string err;
 };
 
@@ -271,12 +275,60 @@ nsem_status check_status(nsem_ctx* ctx) {
 }
 
 /* move the current state to the representation a form needs */
+nsem_status seg_alloc(nsem_ctx* ctx) {
+    NsemSegBuf& S = ctx->sbuf;
+    if (S.ready) return NSEM_OK;
+    const size_t n = (size_t)ctx->dev.n_int, ns = (size_t)ctx->dev.n_slot;
+    nsem_status s;
+    double** node_arrays[] = {&S.rho[0], &S.rho[1], &S.U[0], &S.U[1], &S.U[2], &S.Tp, &S.Tf,
+                              &S.Fc[0], &S.Fc[1], &S.Fc[2], &S.mu, &S.cs, &S.pp};
+    for (double** a : node_arrays)
+        if ((s = dalloc(ctx, a, n)) != NSEM_OK) return s;
+    if ((s = dalloc(ctx, &S.lam, ns)) != NSEM_OK) return s;
+    for (int v = 0; v < 5; v++)
+        if ((s = dalloc(ctx, &S.d[v], ns)) != NSEM_OK) return s;
+    const int e = nsem_seg_prepare(&ctx->dev);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "segregated-scheme shared memory");
+    S.cur = 0;
+    S.ready = true;
+    return NSEM_OK;
+}
+
 nsem_status ensure_rep(nsem_ctx* ctx, int want) {
     if (ctx->rep == want) return NSEM_OK;
-    int e = nsem_mixed_convert(&ctx->dev, &ctx->mbuf, &ctx->buf, want == 1, ctx->stream);
+    int e = 0;
+    if (ctx->rep == 2) {
+        /* primitive fields -> conserved state */
+        if ((e = nsem_seg_to_cons(&ctx->dev, &ctx->sbuf, ctx->buf.u, ctx->stream)))
+            return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+        ctx->rep = 0;
+        if (want == 0) return NSEM_OK;
+    }
+    if (want == 2) {
+        if (ctx->rep == 1 &&
+            (e = nsem_mixed_convert(&ctx->dev, &ctx->mbuf, &ctx->buf, 0, ctx->stream)))
+            return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+        nsem_status s = seg_alloc(ctx);
+        if (s != NSEM_OK) return s;
+        if ((e = nsem_cons_to_seg(&ctx->dev, &ctx->sbuf, ctx->buf.u, ctx->stream)))
+            return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+        ctx->rep = 2;
+        return NSEM_OK;
+    }
+    e = nsem_mixed_convert(&ctx->dev, &ctx->mbuf, &ctx->buf, want == 1, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "state conversion");
     ctx->rep = want;
     return NSEM_OK;
+}
+
+/* the conserved state in buf.u for reading, without moving the state out of
+ * the primitive fields (a segregated run stays bit-exact across reads) */
+nsem_status materialise_conserved(nsem_ctx* ctx) {
+    if (ctx->rep == 2) {
+        const int e = nsem_seg_to_cons(&ctx->dev, &ctx->sbuf, ctx->buf.u, ctx->stream);
+        return e ? cuda_fail(ctx, (cudaError_t)e, "state conversion") : NSEM_OK;
+    }
+    return ensure_rep(ctx, 0);
 }
 
 /* launches of one nsem_step call (captured into a graph) */
@@ -373,7 +425,7 @@ nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rho
     if (!rho || !rhoU || !rhoTheta) return fail(ctx, NSEM_BAD_ARG, "state pointer is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     const size_t n = (size_t)ctx->dev.n_int;
-    nsem_status rs = ensure_rep(ctx, 0);
+    nsem_status rs = materialise_conserved(ctx);
     if (rs != NSEM_OK) return rs;
     int e = nsem_soa_to_aos(ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3], ctx->scratch_aos,
                             ctx->dev.n_int, ctx->stream);
@@ -387,15 +439,19 @@ nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rho
 nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U, const double* T) {
     if (!ctx) return NSEM_BAD_ARG;
     if (!rho || !U || !T) return fail(ctx, NSEM_BAD_ARG, "field pointer is NULL");
-    const int64_t n = ctx->dev.n_int;
-    std::vector<double> ru(3 * n), rt(n);
-    for (int64_t i = 0; i < n; i++) {
-        const double r = rho[i];
-        for (int c = 0; c < 3; c++) ru[3 * i + c] = r * U[3 * i + c];
-        rt[i] = r * (T[i] + ctx->T0);
-    }
-    nsem_status s = nsem_set_state(ctx, rho, ru.data(), rt.data());
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    /* the fields are kept as given (the segregated scheme steps them
+     * directly); other forms convert them on the device when they step */
+    nsem_status s = seg_alloc(ctx);
     if (s != NSEM_OK) return s;
+    NsemSegBuf& S = ctx->sbuf;
+    const size_t n = (size_t)ctx->dev.n_int;
+    NSEM_CUDA(cudaMemcpyAsync(S.rho[S.cur], rho, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(S.Tp, T, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->scratch_aos, U, 3 * n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    int e = nsem_aos_to_soa(ctx->scratch_aos, S.U[0], S.U[1], S.U[2], ctx->dev.n_int, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
+    ctx->rep = 2;
     NSEM_CUDA(cudaStreamSynchronize(ctx->stream));
     return NSEM_OK;
 }
@@ -403,7 +459,17 @@ nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U, c
 nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
     if (!ctx) return NSEM_BAD_ARG;
     if (!rho || !U || !T) return fail(ctx, NSEM_BAD_ARG, "field pointer is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
     const int64_t n = ctx->dev.n_int;
+    if (ctx->rep == 2) {
+        NsemSegBuf& S = ctx->sbuf;
+        int e = nsem_soa_to_aos(S.U[0], S.U[1], S.U[2], ctx->scratch_aos, n, ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "soa_to_aos");
+        NSEM_CUDA(cudaMemcpyAsync(rho, S.rho[S.cur], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        NSEM_CUDA(cudaMemcpyAsync(T, S.Tp, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        NSEM_CUDA(cudaMemcpyAsync(U, ctx->scratch_aos, 3 * n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        return check_status(ctx);
+    }
     std::vector<double> ru(3 * n), rt(n);
     nsem_status s = nsem_get_state(ctx, rho, ru.data(), rt.data());
     if (s != NSEM_OK) return s;
@@ -426,7 +492,7 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
     void* st = (void*)ctx->stream;
     int e;
     if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    nsem_status rs = ensure_rep(ctx, prec == NSEM_MIXED ? 1 : 0);
+    nsem_status rs = (prec == NSEM_MIXED) ? ensure_rep(ctx, 1) : materialise_conserved(ctx);
     if (rs != NSEM_OK) return rs;
     if (prec == NSEM_FP64) {
         if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
@@ -451,20 +517,30 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
 nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec) {
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
-    if (scheme != NSEM_SSPRK3) return fail(ctx, NSEM_UNSUPPORTED, "only SSPRK3 is implemented");
+    if (scheme != NSEM_SSPRK3 && scheme != NSEM_REF_SEGREGATED)
+        return fail(ctx, NSEM_BAD_ARG, "unknown scheme");
     if (prec != NSEM_FP64 && prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    if (scheme == NSEM_REF_SEGREGATED && prec != NSEM_FP64)
+        return fail(ctx, NSEM_UNSUPPORTED, "the segregated scheme runs in FP64 only");
     if (nsteps == 0) return NSEM_OK;
     NSEM_CUDA(cudaSetDevice(ctx->device));
     if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    nsem_status rs = ensure_rep(ctx, prec == NSEM_MIXED ? 1 : 0);
+    const int form = (scheme == NSEM_REF_SEGREGATED) ? 2 : (prec == NSEM_MIXED ? 1 : 0);
+    nsem_status rs = ensure_rep(ctx, form);
     if (rs != NSEM_OK) return rs;
-    const int cur = (prec == NSEM_MIXED) ? ctx->mbuf.cur : 0;
-    auto key = std::make_pair((int)prec * 2 + cur, nsteps);
+    const int cur = form == 1 ? ctx->mbuf.cur : form == 2 ? ctx->sbuf.cur : 0;
+    auto key = std::make_pair(form * 2 + cur, nsteps);
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
         cudaGraph_t g;
         NSEM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        nsem_status s = enqueue_steps(ctx, nsteps, prec);
+        nsem_status s;
+        if (form == 2) {
+            const int e = nsem_seg_steps(&ctx->dev, &ctx->tab, &ctx->sbuf, nsteps, ctx->dt, ctx->stream);
+            s = e ? cuda_fail(ctx, (cudaError_t)e, "segregated step") : NSEM_OK;
+        } else {
+            s = enqueue_steps(ctx, nsteps, prec);
+        }
         cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
         if (s != NSEM_OK) {
             if (ce == cudaSuccess) cudaGraphDestroy(g);
@@ -478,7 +554,8 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
         it = ctx->graphs.emplace(key, ex).first;
     }
     NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
-    if (prec == NSEM_MIXED) ctx->mbuf.cur ^= (nsteps & 1);
+    if (form == 1) ctx->mbuf.cur ^= (nsteps & 1);
+    if (form == 2) ctx->sbuf.cur ^= (nsteps & 1);
     NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, ctx->stream));
     return NSEM_OK;
@@ -546,7 +623,7 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
-    nsem_status s = ensure_rep(ctx, 0);
+    nsem_status s = materialise_conserved(ctx);
     if (s != NSEM_OK) return s;
     if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
     NsemAdjBuf& A = ctx->abuf;
@@ -566,7 +643,7 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
     for (int v = 0; v < 5; v++)
         if (!dv[v] || !Ld[v]) return fail(ctx, NSEM_BAD_ARG, "dv[v] or Ld[v] is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
-    nsem_status s = ensure_rep(ctx, 0);
+    nsem_status s = materialise_conserved(ctx);
     if (s != NSEM_OK) return s;
     if ((s = adj_alloc(ctx)) != NSEM_OK) return s;
     NsemAdjBuf& A = ctx->abuf;
@@ -851,7 +928,7 @@ nsem_status nsem_sync(nsem_ctx* ctx) {
 nsem_status nsem_diagnostics(nsem_ctx* ctx, double* mass, double* energy, double* volume) {
     if (!ctx) return NSEM_BAD_ARG;
     NSEM_CUDA(cudaSetDevice(ctx->device));
-    nsem_status rs = ensure_rep(ctx, 0);
+    nsem_status rs = materialise_conserved(ctx);
     if (rs != NSEM_OK) return rs;
     int e = nsem_reduce_diagnostics(&ctx->dev, &ctx->buf, ctx->red, ctx->h_red, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "diagnostics");

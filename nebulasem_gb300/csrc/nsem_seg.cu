@@ -1,0 +1,452 @@
+/*
+ * The reference's own time update on the GPU: segregated forward Euler over
+ * the primitive fields (apps/euler/euler.cpp:179-287 with time_scheme BDF1,
+ * diffusion NO), the drop-in counterpart of the shipped euler solver.
+ *
+ * Compiled with --fmad=false; every operation in the order the reference
+ * evaluates it (the same restatement as the oracle's nsem_oracle_segregated),
+ * so the result is bit-identical to the reference wherever its C library pow
+ * is correctly rounded (the equation of state uses nsem_ddpow.h).
+ *
+ * One step, five kernels:
+ *   prep      per node: theta = theta' + T0 (T += T0, euler.cpp:181),
+ *             Fc = rho U (flxc, field.h:3392-3395), |U|, sqrt(gamma R theta);
+ *   face_rho  per used slot: lambda = (cds|U| + cds c)/2 (euler.cpp:186),
+ *             Rusanov flux of the rho equation (flux U rho, state rho);
+ *   vol_rho   per element: lift + weak volume term of the rho equation, then
+ *             rho^{n+1} = Su/ap with ap = (-1/dt) cV, Su += rho^n ap
+ *             (addTemporal<1> / ddt BDF1, field.h:3741-3841, 3875-3920;
+ *             SolveTexplicit, solve.cpp:563-564), and p' = P0 (rho^{n+1}
+ *             theta R / P0)^gamma - p_ref (euler.cpp:211-213);
+ *   face_ut   per used slot: Rusanov fluxes of the U equation (flux
+ *             Fc (x) U + p' I, state rho^{n+1} U) and the T equation (flux
+ *             Fc theta, state rho^{n+1} theta), lambda of the step;
+ *   vol_ut    per element: lift + volume terms, gravity source (rho^{n+1} -
+ *             rho_ref) g, U^{n+1} = Su/ap with ap = (-1/dt) cV rho^{n+1} and
+ *             Su += (U^n rho^n)(-1/dt) cV, likewise theta, then T -= T0.
+ * Ghost values follow applyExplicitBCs (field.h:2586-2727) on the fly:
+ * NEUMANN owner + 0, SYMMETRY velocity the rescaled tangential projection.
+ */
+#include <cuda_runtime.h>
+
+#include "nsem_ddpow.h"
+#include "nsem_seg.h"
+
+namespace {
+
+enum { XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX };
+
+__device__ __forceinline__ double vdot3(const double* a, const double* b) {
+    return a[0] * b[0] + (a[1] * b[1] + (a[2] * b[2] + 0.0));
+}
+
+__device__ __forceinline__ void tdot(const double* q, const double* p, double* r) {
+    r[0] = q[XX] * p[0] + q[XY] * p[1] + q[XZ] * p[2];
+    r[1] = q[YX] * p[0] + q[YY] * p[1] + q[YZ] * p[2];
+    r[2] = q[ZX] * p[0] + q[ZY] * p[1] + q[ZZ] * p[2];
+}
+
+__device__ __forceinline__ void outer(const double* p, const double* q, double* r) {
+    r[XX] = p[0] * q[0];
+    r[YY] = p[1] * q[1];
+    r[ZZ] = p[2] * q[2];
+    r[XY] = p[0] * q[1];
+    r[YZ] = p[1] * q[2];
+    r[XZ] = p[0] * q[2];
+    r[YX] = p[1] * q[0];
+    r[ZY] = p[2] * q[1];
+    r[ZX] = p[2] * q[0];
+}
+
+/* SYMMETRY ghost velocity (src/tensor/tensor.h:486-494) */
+__device__ __forceinline__ void sym_vec(const double* p, const double* n, double* out) {
+    const double mg = sqrt(vdot3(n, n));
+    const double en[3] = {n[0] / mg, n[1] / mg, n[2] / mg};
+    const double A0 = 1.0 - en[0] * en[0];
+    const double A1 = 1.0 - en[1] * en[1];
+    const double A2 = 1.0 - en[2] * en[2];
+    const double A3 = 0.0 - en[0] * en[1];
+    const double A4 = 0.0 - en[1] * en[2];
+    const double A5 = 0.0 - en[0] * en[2];
+    double r[3];
+    r[0] = A0 * p[0] + A3 * p[1] + A5 * p[2];
+    r[1] = A3 * p[0] + A1 * p[1] + A4 * p[2];
+    r[2] = A5 * p[0] + A4 * p[1] + A2 * p[2];
+    const double magR = sqrt(vdot3(r, r));
+    if (fabs(magR - 0.0) <= 1e-7) {
+        out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+        return;
+    }
+    const double s = sqrt(vdot3(p, p)) / magR;
+    out[0] = r[0] * s; out[1] = r[1] * s; out[2] = r[2] * s;
+}
+
+/* ghost velocity of slot k from the owner's */
+__device__ __forceinline__ void ghost_U(const NsemDev& m, int64_t k, const double* n,
+                                        const double* U1, double* U2) {
+    if (m.bc[k] == 2) {
+        sym_vec(U1, n, U2);
+    } else {
+        U2[0] = U1[0] + 0.0; U2[1] = U1[1] + 0.0; U2[2] = U1[2] + 0.0;
+    }
+}
+
+struct SegArgs {
+    const double* rho_o;     /* rho^n            */
+    double* rho_n;           /* rho^{n+1}        */
+    double* U[3];            /* U^n -> U^{n+1}   */
+    double* Tp;              /* theta' in/out    */
+    double* Tf;              /* theta = theta' + T0 of the step */
+    double* Fc[3];
+    double* mu;
+    double* cs;
+    double* pp;
+    double* lam;             /* per slot */
+    double* d[5];            /* per slot */
+    double c_dt;             /* -1 / dt */
+};
+
+__global__ void __launch_bounds__(256) k_seg_prep(const NsemDev m, SegArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_int) return;
+    const double r = a.rho_o[i];
+    const double U[3] = {a.U[0][i], a.U[1][i], a.U[2][i]};
+    const double Tf = a.Tp[i] + m.T0;
+    a.Tf[i] = Tf;
+    for (int c = 0; c < 3; c++) a.Fc[c][i] = r * U[c];
+    a.mu[i] = sqrt(vdot3(U, U));
+    a.cs[i] = sqrt(m.gR * Tf);
+}
+
+__global__ void __launch_bounds__(256) k_seg_face_rho(const NsemDev m, SegArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double r1 = a.rho_o[c1];
+    const double U1[3] = {a.U[0][c1], a.U[1][c1], a.U[2][c1]};
+    const double mu1 = a.mu[c1], cs1 = a.cs[c1];
+    double r2, U2[3], mu2, cs2;
+    if (c2 >= 0) {
+        r2 = a.rho_o[c2];
+        U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
+        mu2 = a.mu[c2]; cs2 = a.cs[c2];
+    } else {
+        r2 = r1 + 0.0;
+        ghost_U(m, k, n, U1, U2);
+        mu2 = sqrt(vdot3(U2, U2));
+        cs2 = sqrt(m.gR * (a.Tf[c1] + 0.0));
+    }
+    const double lam = ((mu1 * fi + mu2 * fo) + (cs1 * fi + cs2 * fo)) / 2;
+    a.lam[k] = lam;
+    double F[3];
+    const double jump = lam * (r2 - r1);
+    for (int c = 0; c < 3; c++) {
+        const double x = U1[c] * r1, y = U2[c] * r2;
+        F[c] = (x * fi + y * fo) - en[c] * jump;
+    }
+    a.d[0][k] = vdot3(F, n);
+}
+
+/* weak volume term gathered in the order of the reference's scatter loop
+ * (field.h:3440-3464): X-line below, Y-line below, Z-line below, self,
+ * Z above, Y above, X above; sm holds W doubles per node with the metric
+ * Jinv cV at offset JOFF */
+template <int W, int JOFF, typename Apply>
+__device__ __forceinline__ void volume_gather(const NsemDev& m, const double* sm, const double* dps,
+                                              int t, Apply apply) {
+    const int NPX = m.npx, NPY = m.npy, NPZ = m.npz;
+    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
+    const double* Dx = dps;
+    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    auto line = [&](int dir, int lb, double D) {
+        const double* J = sm + (size_t)lb * W + JOFF;
+        double dj[3];
+        if (dir == 0) { dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D; }
+        else if (dir == 1) { dj[0] = J[XY] * D; dj[1] = J[YY] * D; dj[2] = J[ZY] * D; }
+        else { dj[0] = J[XZ] * D; dj[1] = J[YZ] * D; dj[2] = J[ZZ] * D; }
+        apply(lb, dj);
+    };
+    const int sx = NPY * NPZ, sy = NPZ;
+    for (int ii = 0; ii < ia; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
+    for (int jj = 0; jj < ja; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
+    for (int kk = 0; kk < ka; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
+    {
+        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
+        double dj[3];
+        tdot(sm + (size_t)t * W + JOFF, dv, dj);
+        apply(t, dj);
+    }
+    for (int kk = ka + 1; kk < NPZ; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
+    for (int jj = ja + 1; jj < NPY; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
+    for (int ii = ia + 1; ii < NPX; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
+}
+
+constexpr int W_RHO = 12;   /* fr[3] jin[9] */
+constexpr int W_UT = 21;    /* fm[9] ft[3] jin[9] */
+
+__global__ void k_seg_vol_rho(const NsemDev m, const NsemTables tab, SegArgs a) {
+    extern __shared__ double sm[];
+    const int NP = m.np;
+    double* dps = sm + (size_t)NP * W_RHO;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    double rho = 0;
+    if (active) {
+        rho = a.rho_o[node];
+        double* my = sm + (size_t)t * W_RHO;
+        for (int c = 0; c < 3; c++) my[c] = a.U[c][node] * rho;     /* U * rho */
+        for (int c = 0; c < 9; c++) my[3 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    double r = 0.0;
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        if (code & 1) r -= a.d[0][k];
+        else r += a.d[0][k];
+    }
+    volume_gather<W_RHO, 3>(m, sm, dps, t, [&](int lb, const double* dj) {
+        r -= vdot3(sm + (size_t)lb * W_RHO, dj);
+    });
+    const double cv = m.cv[node];
+    const double ap = a.c_dt * cv;
+    const double rn = (r + rho * ap) / (0.0 + ap);
+    a.rho_n[node] = rn;
+    const double p = m.P0 * nsem_pow(((rn * a.Tf[node]) * m.R) / m.P0, m.gamma);
+    a.pp[node] = p - m.p_ref[node];
+}
+
+__global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double lam = a.lam[k];
+    const double r1 = a.rho_n[c1];
+    const double U1[3] = {a.U[0][c1], a.U[1][c1], a.U[2][c1]};
+    const double Fc1[3] = {a.Fc[0][c1], a.Fc[1][c1], a.Fc[2][c1]};
+    const double T1 = a.Tf[c1], p1 = a.pp[c1];
+    double r2, U2[3], Fc2[3], T2, p2;
+    if (c2 >= 0) {
+        r2 = a.rho_n[c2];
+        for (int c = 0; c < 3; c++) { U2[c] = a.U[c][c2]; Fc2[c] = a.Fc[c][c2]; }
+        T2 = a.Tf[c2];
+        p2 = a.pp[c2];
+    } else {
+        r2 = r1 + 0.0;
+        ghost_U(m, k, n, U1, U2);
+        const double ro2 = a.rho_o[c1] + 0.0;
+        for (int c = 0; c < 3; c++) Fc2[c] = ro2 * U2[c];
+        T2 = T1 + 0.0;
+        p2 = p1;
+    }
+    /* U equation: flux Fc (x) U + p' I, state rho U */
+    {
+        double A[9], B[9], O[9], F[9], dq[3], out[3];
+        outer(Fc1, U1, A);
+        outer(Fc2, U2, B);
+        for (int c = 0; c < 9; c++) {
+            const double i1 = (c < 3) ? 1.0 : 0.0;
+            A[c] = A[c] + i1 * p1;
+            B[c] = B[c] + i1 * p2;
+        }
+        for (int c = 0; c < 3; c++) dq[c] = (r2 * U2[c] - r1 * U1[c]) * lam;
+        outer(en, dq, O);
+        for (int c = 0; c < 9; c++) F[c] = (A[c] * fi + B[c] * fo) - O[c];
+        tdot(F, n, out);
+        a.d[1][k] = out[0];
+        a.d[2][k] = out[1];
+        a.d[3][k] = out[2];
+    }
+    /* T equation: flux Fc theta, state rho theta */
+    {
+        double F[3];
+        const double jump = lam * (r2 * T2 - r1 * T1);
+        for (int c = 0; c < 3; c++) {
+            const double x = Fc1[c] * T1, y = Fc2[c] * T2;
+            F[c] = (x * fi + y * fo) - en[c] * jump;
+        }
+        a.d[4][k] = vdot3(F, n);
+    }
+}
+
+__global__ void k_seg_vol_ut(const NsemDev m, const NsemTables tab, SegArgs a) {
+    extern __shared__ double sm[];
+    const int NP = m.np;
+    double* dps = sm + (size_t)NP * W_UT;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    double U[3] = {0, 0, 0}, Tf = 0;
+    if (active) {
+        double* my = sm + (size_t)t * W_UT;
+        double Fc[3];
+        for (int c = 0; c < 3; c++) { U[c] = a.U[c][node]; Fc[c] = a.Fc[c][node]; }
+        Tf = a.Tf[node];
+        const double p = a.pp[node];
+        outer(Fc, U, my);
+        for (int c = 0; c < 9; c++) my[c] = my[c] + ((c < 3) ? 1.0 : 0.0) * p;
+        for (int c = 0; c < 3; c++) my[9 + c] = Fc[c] * Tf;
+        for (int c = 0; c < 9; c++) my[12 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    double r1 = 0.0, r2 = 0.0, r3 = 0.0, r4 = 0.0;
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        if (code & 1) {
+            r1 -= a.d[1][k]; r2 -= a.d[2][k]; r3 -= a.d[3][k]; r4 -= a.d[4][k];
+        } else {
+            r1 += a.d[1][k]; r2 += a.d[2][k]; r3 += a.d[3][k]; r4 += a.d[4][k];
+        }
+    }
+    volume_gather<W_UT, 12>(m, sm, dps, t, [&](int lb, const double* dj) {
+        const double* sb = sm + (size_t)lb * W_UT;
+        double tv[3];
+        tdot(sb, dj, tv);
+        r1 -= tv[0]; r2 -= tv[1]; r3 -= tv[2];
+        r4 -= vdot3(sb + 9, dj);
+    });
+    const double cv = m.cv[node];
+    const double rn = a.rho_n[node];
+    const double ro = a.rho_o[node];
+    const double s = rn - m.rho_ref[node];
+    const double ap0 = a.c_dt * cv;
+    const double ap = ap0 * rn;
+    const double r[3] = {r1, r2, r3};
+    bool finite = isfinite(rn);
+    for (int c = 0; c < 3; c++) {
+        const double sc = 0.0 + m.g[c] * s;
+        const double su = r[c] - sc * cv;
+        const double un = (su + (U[c] * ro) * ap0) / (0.0 + ap);
+        a.U[c][node] = un;
+        finite = finite && isfinite(un);
+    }
+    const double Tn = (r4 + (Tf * ro) * ap0) / (0.0 + ap);
+    a.Tp[node] = Tn - m.T0;
+    finite = finite && isfinite(Tn);
+    if (!finite) atomicOr(m.status, NSEM_STATUS_NONFINITE);
+}
+
+/* conversions between the primitive fields and the conserved state */
+struct ConvArgs {
+    const double* rho;
+    double* rho_w;
+    double* U[3];
+    double* Tp;
+    double* u[5];
+};
+
+__global__ void __launch_bounds__(256) k_seg_to_cons(const NsemDev m, ConvArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_int) return;
+    const double r = a.rho[i];
+    a.u[0][i] = r;
+    for (int c = 0; c < 3; c++) a.u[1 + c][i] = r * a.U[c][i];
+    a.u[4][i] = r * (a.Tp[i] + m.T0);
+}
+
+__global__ void __launch_bounds__(256) k_cons_to_seg(const NsemDev m, ConvArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_int) return;
+    const double r = a.u[0][i];
+    a.rho_w[i] = r;
+    for (int c = 0; c < 3; c++) a.U[c][i] = a.u[1 + c][i] / r;
+    a.Tp[i] = a.u[4][i] / r - m.T0;
+}
+
+SegArgs seg_args(const NsemDev* m, NsemSegBuf* b, int cur, double dt) {
+    SegArgs a;
+    a.rho_o = b->rho[cur];
+    a.rho_n = b->rho[cur ^ 1];
+    for (int c = 0; c < 3; c++) { a.U[c] = b->U[c]; a.Fc[c] = b->Fc[c]; }
+    a.Tp = b->Tp;
+    a.Tf = b->Tf;
+    a.mu = b->mu;
+    a.cs = b->cs;
+    a.pp = b->pp;
+    a.lam = b->lam;
+    for (int c = 0; c < 5; c++) a.d[c] = b->d[c];
+    a.c_dt = -1.0 / dt;
+    (void)m;
+    return a;
+}
+
+size_t smem_rho(const NsemDev* m) {
+    return ((size_t)m->np * W_RHO + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+}
+size_t smem_ut(const NsemDev* m) {
+    return ((size_t)m->np * W_UT + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+}
+
+}  // namespace
+
+int nsem_seg_prepare(const NsemDev* m) {
+    if (smem_rho(m) > 48 * 1024) {
+        const int e = (int)cudaFuncSetAttribute(k_seg_vol_rho, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_rho(m));
+        if (e) return e;
+    }
+    if (smem_ut(m) > 48 * 1024)
+        return (int)cudaFuncSetAttribute(k_seg_vol_ut, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_ut(m));
+    return 0;
+}
+
+int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nsteps, double dt,
+                   void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned nb = (unsigned)((m->n_int + 255) / 256);
+    const unsigned sb = (unsigned)((m->n_slot + 255) / 256);
+    const int threads = ((m->np + 31) / 32) * 32;
+    int cur = b->cur;
+    for (int s = 0; s < nsteps; s++) {
+        const SegArgs a = seg_args(m, b, cur, dt);
+        k_seg_prep<<<nb, 256, 0, st>>>(*m, a);
+        k_seg_face_rho<<<sb, 256, 0, st>>>(*m, a);
+        k_seg_vol_rho<<<(unsigned)m->n_elem, threads, smem_rho(m), st>>>(*m, *t, a);
+        k_seg_face_ut<<<sb, 256, 0, st>>>(*m, a);
+        k_seg_vol_ut<<<(unsigned)m->n_elem, threads, smem_ut(m), st>>>(*m, *t, a);
+        const int e = (int)cudaGetLastError();
+        if (e) return e;
+        cur ^= 1;
+    }
+    return 0;
+}
+
+int nsem_seg_to_cons(const NsemDev* m, const NsemSegBuf* b, double* const* u, void* stream) {
+    ConvArgs a{};
+    a.rho = b->rho[b->cur];
+    for (int c = 0; c < 3; c++) a.U[c] = b->U[c];
+    a.Tp = b->Tp;
+    for (int v = 0; v < 5; v++) a.u[v] = u[v];
+    k_seg_to_cons<<<(unsigned)((m->n_int + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);
+    return (int)cudaGetLastError();
+}
+
+int nsem_cons_to_seg(const NsemDev* m, NsemSegBuf* b, double* const* u, void* stream) {
+    ConvArgs a{};
+    a.rho_w = b->rho[b->cur];
+    for (int c = 0; c < 3; c++) a.U[c] = b->U[c];
+    a.Tp = b->Tp;
+    for (int v = 0; v < 5; v++) a.u[v] = u[v];
+    k_cons_to_seg<<<(unsigned)((m->n_int + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);
+    return (int)cudaGetLastError();
+}

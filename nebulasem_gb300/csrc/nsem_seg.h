@@ -1,0 +1,33 @@
+/*
+ * The reference's segregated forward-Euler update (nsem_seg.cu): device
+ * buffers of the primitive fields and launchers.
+ */
+#ifndef NSEM_SEG_H
+#define NSEM_SEG_H
+
+#include "nsem_internal.h"
+
+struct NsemSegBuf {
+    bool ready = false;
+    int cur = 0;                  /* rho[cur] holds rho^n                   */
+    double* rho[2] = {};          /* density, ping-pong                     */
+    double* U[3] = {};            /* velocity (SoA)                         */
+    double* Tp = nullptr;         /* theta' (the euler app's T field)       */
+    double* Tf = nullptr;         /* theta of the step                      */
+    double* Fc[3] = {};           /* rho^n U^n                              */
+    double* mu = nullptr;         /* |U^n|                                  */
+    double* cs = nullptr;         /* sqrt(gamma R theta^n)                  */
+    double* pp = nullptr;         /* p' from rho^{n+1}, theta^n             */
+    double* lam = nullptr;        /* per slot: Rusanov speed of the step    */
+    double* d[5] = {};            /* per slot: lifted fluxes                */
+};
+
+int nsem_seg_prepare(const NsemDev* m);
+int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nsteps, double dt,
+                   void* stream);
+/* u = conserved state of the primitive fields rho[cur], U, T' */
+int nsem_seg_to_cons(const NsemDev* m, const NsemSegBuf* b, double* const* u, void* stream);
+/* primitive fields from the conserved state u */
+int nsem_cons_to_seg(const NsemDev* m, NsemSegBuf* b, double* const* u, void* stream);
+
+#endif

@@ -1,0 +1,68 @@
+"""The reference's own update (REF_SEGREGATED: segregated forward Euler,
+BDF1) on the GPU against the oracle's restatement, which is itself pinned bit
+for bit to the unmodified reference `euler` binary (tests/test_segregated_oracle.py).
+
+With the correctly rounded pow in the oracle the GPU result is bit-identical;
+against the reference binary itself (C library pow) the difference is the pow
+floor of the plain form."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2"])
+def test_segregated_gpu_bitwise_vs_oracle(case):
+    import nebulasem_gb300 as ng
+    g = load_golden(case)
+    n = int(g["meta"][7])
+    dt, steps = float(g["dt"]), int(g["nsteps"])
+    rho0, U0, T0 = g["fld0_rho"], g["fld0_U"].reshape(n, 3), g["fld0_T"]
+    m = oracle.OracleMesh(g)
+    oracle.set_pow(1)
+    r_o, u_o, t_o = m.segregated(rho0, U0, T0, dt, steps)
+    oracle.set_pow(0)
+    s = ng.Solver(g, dt=dt)
+    s.set_fields(rho0, U0, T0)
+    r1, u1, t1 = s.get_fields()
+    assert np.array_equal(r1, rho0) and np.array_equal(u1, U0) and np.array_equal(t1, T0)
+    # in two calls (graph keys and the ping-pong state) with a read in between
+    s.step(steps // 2, scheme=ng.REF_SEGREGATED)
+    s.diagnostics()
+    s.step(steps - steps // 2, scheme=ng.REF_SEGREGATED)
+    r, u, t = s.get_fields()
+    assert np.array_equal(r, r_o)
+    assert np.array_equal(u, u_o)
+    assert np.array_equal(t, t_o)
+    # against the reference binary: within the oracle's own CR-vs-C-library pow
+    # floor (measured: rho 1e-15, theta' 4e-12, U 6e-10 after 100 steps of 2D)
+    assert rel(r, g["fldN_rho"]) <= 1e-14
+    assert rel(t, g["fldN_T"]) <= 1e-11
+    U_ref = g["fldN_U"].reshape(n, 3)
+    floor = np.linalg.norm(u_o - U_ref)
+    assert np.linalg.norm(u - U_ref) <= 1.01 * floor + 1e-300
+    s.close()
+
+
+def test_segregated_then_coupled_forms_switch():
+    """State moves between the primitive fields and the other forms."""
+    import nebulasem_gb300 as ng
+    g = load_golden("seg_g3_2")
+    n = int(g["meta"][7])
+    s = ng.Solver(g, dt=float(g["dt"]))
+    s.set_fields(g["fld0_rho"], g["fld0_U"].reshape(n, 3), g["fld0_T"])
+    s.step(3, scheme=ng.REF_SEGREGATED)
+    u_cons = s.get_state()
+    s.step(2)                      # coupled SSP-RK3 from the converted state
+    s.step(2, scheme=ng.REF_SEGREGATED)
+    r, u, t = s.get_fields()
+    assert all(np.isfinite(x).all() for x in (r, u, t))
+    assert np.allclose(u_cons[0], g["fld0_rho"], rtol=1e-3)
+    s.close()
