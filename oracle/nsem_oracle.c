@@ -523,12 +523,15 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
     ghosts_scalar(m, T);
     const double c_dt = -1.0 / dt;
     for (int step = 0; step < nsteps; step++) {
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) T[i] += T0;
         memcpy(rhof, rho, (size_t)n_all * sizeof(double));
         /* Fc = flxc(rho U), lambda = (cds|U| + cds sqrt(gamma R T)) / 2 */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fc[3 * i + c] = rho[i] * U[3 * i + c];
         const double gR = gam * R;
+#pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
             if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
@@ -537,8 +540,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
                       (sqrt(gR * T[c1]) * fi + sqrt(gR * T[c2]) * fo)) / 2;
         }
         /* rho equation: flux U rho, state rho */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * rho[i];
+#pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
             if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
@@ -552,22 +557,27 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             d[k] = vdot(F, n);
         }
         seg_divf(m, 1, Fv, d, r);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap = c_dt * m->cV[i];
             rho[i] = (r[i] + rho[i] * ap) / (0.0 + ap);
         }
         ghosts_scalar(m, rho);
         /* p' from the new rho and the old theta */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) p[i] = P0 * eos_pow(((rho[i] * T[i]) * R) / P0, gam);
         ghosts_scalar(m, p);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) p[i] -= m->p_ref[i];
         /* U equation: flux Fc (x) U + p' I, state rho U */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) {
             double* Ft = Fv + 9 * i;
             outer(Fc + 3 * i, U + 3 * i, Ft);
             for (int c = 0; c < 9; c++) Ft[c] = Ft[c] + ((c < 3) ? 1.0 : 0.0) * p[i];
             for (int c = 0; c < 3; c++) q[3 * i + c] = rho[i] * U[3 * i + c];
         }
+#pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
             if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
@@ -582,6 +592,7 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             tdot(F, n, d + 3 * k);
         }
         seg_divf(m, 3, Fv, d, r);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double s = rho[i] - m->rho_ref[i];
             const double ap0 = c_dt * m->cV[i];
@@ -594,8 +605,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
         }
         ghosts_velocity(m, U);
         /* T equation: flux Fc T, state rho T (U no longer enters) */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fv[3 * i + c] = Fc[3 * i + c] * T[i];
+#pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
             if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
@@ -609,12 +622,14 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             d[k] = vdot(F, n);
         }
         seg_divf(m, 1, Fv, d, r);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap0 = c_dt * m->cV[i];
             const double ap = ap0 * rho[i];
             T[i] = (r[i] + (T[i] * rhof[i]) * ap0) / (0.0 + ap);
         }
         ghosts_scalar(m, T);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) T[i] -= T0;
     }
     memcpy(rho_in, rho, (size_t)n_int * sizeof(double));

@@ -128,6 +128,44 @@ def run_gpu(name, dt, steps, adjoint_ckpt=0, with_oracle=False):
     return out
 
 
+def run_segregated(name, dt, steps, with_oracle=False):
+    """The reference's own update (segregated forward Euler) on the GPU from the
+    workload's fields; throughput and, with the oracle, bitwise comparison."""
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300.mesh import workload
+    m, u0 = workload(name)
+    n = int(m["meta"][7])
+    rho = u0[0]
+    U = np.stack([u0[1] / rho, u0[2] / rho, u0[3] / rho], axis=1)
+    T = u0[4] / rho - 300.0
+    s = ng.Solver(m, dt=dt)
+    out = dict(workload=name, scheme="REF_SEGREGATED", dt=dt, steps=steps, nodes=n, dof=5 * n)
+    for rep in range(2):
+        s.set_fields(rho, U, T)
+        s.sync()
+        t = time.perf_counter()
+        s.step(steps, scheme=ng.REF_SEGREGATED)
+        s.sync()
+        wall = time.perf_counter() - t
+    r, u, th = s.get_fields()
+    s.close()
+    out["seconds"] = wall
+    out["dof_steps_per_s"] = 5 * n * steps / wall   # one stage per step
+    out["finite"] = bool(np.isfinite(r).all() and np.isfinite(u).all() and np.isfinite(th).all())
+    out["sha256"] = digest([r, u.reshape(-1), th])
+    if with_oracle:
+        import oracle
+        om = oracle.OracleMesh(m)
+        oracle.set_pow(1)
+        t = time.time()
+        ro, uo, to = om.segregated(rho, U, T, dt, steps)
+        out["oracle_seconds"] = time.time() - t
+        out["oracle_threads"] = oracle.lib().nsem_oracle_threads()
+        out["oracle_sha256"] = digest([ro, uo.reshape(-1), to])
+        out["equals_oracle_bitwise"] = out["oracle_sha256"] == out["sha256"]
+    return out
+
+
 def run_oracle(name, dt, steps):
     import oracle
     from nebulasem_gb300.mesh import workload
@@ -149,12 +187,16 @@ def main():
     ap.add_argument("--dt", type=float, required=True)
     ap.add_argument("--steps", type=int, required=True)
     ap.add_argument("--oracle", action="store_true")
+    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg"],
+                    help="seg: the reference's own segregated update (FP64)")
     ap.add_argument("--with-oracle", action="store_true",
                     help="also run the oracle on this host and compare bit for bit")
     ap.add_argument("--adjoint-ckpt", type=int, default=0,
                     help="also time the FP64 adjoint with checkpoints every k steps")
     a = ap.parse_args()
-    if a.oracle:
+    if a.scheme == "seg":
+        r = run_segregated(a.workload, a.dt, a.steps, a.with_oracle)
+    elif a.oracle:
         r = run_oracle(a.workload, a.dt, a.steps)
     else:
         r = run_gpu(a.workload, a.dt, a.steps, a.adjoint_ckpt, a.with_oracle)
