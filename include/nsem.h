@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define NSEM_ABI_VERSION 1
+#define NSEM_ABI_VERSION 2
 
 typedef enum {
     NSEM_OK = 0,
@@ -98,6 +98,10 @@ typedef struct nsem_params {
     const double* p_ref;        /* [n_all] hydrostatic p (euler.cpp:122), or NULL  */
     const double* rho_ref;      /* [n_all] hydrostatic rho (euler.cpp:123), or NULL*/
     int32_t device;             /* CUDA device ordinal                             */
+    double viscosity;           /* Fluid::viscosity when the euler app runs with
+                                   diffusion YES (mu = rho viscosity), else 0;
+                                   used by NSEM_REF_SEGREGATED                     */
+    double Pr;                  /* Fluid::Pr (> 0 when viscosity > 0)              */
 } nsem_params;
 
 typedef struct nsem_ctx nsem_ctx;

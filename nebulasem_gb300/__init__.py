@@ -52,6 +52,7 @@ class Params(ctypes.Structure):
         ("P0", ctypes.c_double), ("T0", ctypes.c_double), ("cp", ctypes.c_double),
         ("cv", ctypes.c_double), ("gravity", ctypes.c_double * 3), ("dt", ctypes.c_double),
         ("p_ref", ctypes.c_void_p), ("rho_ref", ctypes.c_void_p), ("device", ctypes.c_int32),
+        ("viscosity", ctypes.c_double), ("Pr", ctypes.c_double),
     ]
 
 
@@ -118,7 +119,8 @@ class Solver:
     """
 
     def __init__(self, mesh, dt, P0=1e5, T0=300.0, cp=1004.5, cv=717.5,
-                 gravity=(0.0, 0.0, -9.81), device=0, use_ref_background=True):
+                 gravity=(0.0, 0.0, -9.81), device=0, use_ref_background=True,
+                 viscosity=None, Pr=None):
         lib = load()
         meta = np.asarray(mesh["meta"], dtype=np.int64)
         npx, npy, npz, np_, npf = (int(v) for v in meta[:5])
@@ -157,6 +159,9 @@ class Solver:
             pr.p_ref = _p(keep["p_ref"])
             pr.rho_ref = _p(keep["rho_ref"])
         pr.device = device
+        # artificial viscosity of the segregated scheme (diffusion YES)
+        pr.viscosity = float(mesh.get("viscosity", 0.0) if viscosity is None else viscosity)
+        pr.Pr = float(mesh.get("Pr", 0.9) if Pr is None else Pr)
         ctx = ctypes.c_void_p()
         st = lib.nsem_create(ctypes.byref(md), ctypes.byref(pr), ctypes.byref(ctx))
         self._ctx = ctx

@@ -135,6 +135,8 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
     D.P0 = p->P0;
     D.cp = p->cp;
     D.T0 = p->T0;
+    D.nu = p->viscosity;
+    D.iPr = p->viscosity != 0.0 ? 1 / p->Pr : 0.0;
     D.cv_heat = p->cv;
     for (int c = 0; c < 3; c++) D.g[c] = p->gravity[c];
     ctx->dt = p->dt;
@@ -287,6 +289,12 @@ nsem_status seg_alloc(nsem_ctx* ctx) {
     if ((s = dalloc(ctx, &S.lam, ns)) != NSEM_OK) return s;
     for (int v = 0; v < 5; v++)
         if ((s = dalloc(ctx, &S.d[v], ns)) != NSEM_OK) return s;
+    if (ctx->dev.nu != 0.0) {
+        for (int c = 0; c < 12; c++)
+            if ((s = dalloc(ctx, &S.G[c], n)) != NSEM_OK) return s;
+        for (int c = 0; c < 4; c++)
+            if ((s = dalloc(ctx, &S.fF[c], ns)) != NSEM_OK) return s;
+    }
     const int e = nsem_seg_prepare(&ctx->dev);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "segregated-scheme shared memory");
     S.cur = 0;
@@ -376,6 +384,8 @@ nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params, n
     if (!ctx) return NSEM_NO_MEMORY;
     *out = ctx;
     if (!params) return fail(ctx, NSEM_BAD_ARG, "params is NULL");
+    if (params->viscosity != 0.0 && !(params->viscosity > 0 && params->Pr > 0))
+        return fail(ctx, NSEM_BAD_ARG, "viscosity must be >= 0, with Pr > 0 when it is not 0");
     if (!(params->cp > params->cv) || !(params->cv > 0) || !(params->P0 > 0) || !(params->T0 > 0))
         return fail(ctx, NSEM_BAD_ARG, "invalid fluid properties");
     nsem_status s = check_desc(ctx, mesh);

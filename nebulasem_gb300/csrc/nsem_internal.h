@@ -33,6 +33,7 @@ struct NsemDev {
     int64_t n_elem, n_int, n_slot;
     /* physical constants */
     double P0, R, gamma, gR, cv_heat, cp, T0;
+    double nu, iPr;    /* artificial viscosity (segregated scheme), 1 / Pr */
     double g[3];
     /* node arrays */
     double* jin;       /* [9][n_int] */

@@ -1,7 +1,8 @@
 /*
  * The reference's own time update on the GPU: segregated forward Euler over
  * the primitive fields (apps/euler/euler.cpp:179-287 with time_scheme BDF1,
- * diffusion NO), the drop-in counterpart of the shipped euler solver.
+ * with or without diffusion), the drop-in counterpart of the shipped euler
+ * solver.
  *
  * Compiled with --fmad=false; every operation in the order the reference
  * evaluates it (the same restatement as the oracle's nsem_oracle_segregated),
@@ -26,6 +27,12 @@
  *             Su += (U^n rho^n)(-1/dt) cV, likewise theta, then T -= T0.
  * Ghost values follow applyExplicitBCs (field.h:2586-2727) on the fly:
  * NEUMANN owner + 0, SYMMETRY velocity the rescaled tangential projection.
+ * With diffusion YES (viscosity nu > 0) two more kernels per step form the
+ * strong-form DG gradients of U^n and theta^n (gradf<true>, field.h:3327-3360:
+ * face terms fN (x) (cds(p) - p) in the cell's face order, then the volume
+ * derivative along the three lines, divided by cV; zero on the wall ghosts,
+ * fillBCs field.h:2731-2769), and the fluxes carry - mu grad U and
+ * - (mu / Pr) grad theta with mu = rho^n nu (euler.cpp:189-190, 232, 250).
  */
 #include <cuda_runtime.h>
 
@@ -103,7 +110,10 @@ struct SegArgs {
     double* pp;
     double* lam;             /* per slot */
     double* d[5];            /* per slot */
+    double* G[12];           /* per node: grad U, grad theta (viscous runs) */
+    double* fF[4];           /* per slot: cds(U), cds(theta) (viscous runs) */
     double c_dt;             /* -1 / dt */
+    int visc;
 };
 
 __global__ void __launch_bounds__(256) k_seg_prep(const NsemDev m, SegArgs a) {
@@ -185,6 +195,112 @@ __device__ __forceinline__ void volume_gather(const NsemDev& m, const double* sm
     for (int ii = ia + 1; ii < NPX; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
 }
 
+/* cds(U^n), cds(theta^n) per slot for the gradients */
+__global__ void __launch_bounds__(256) k_seg_grad_face(const NsemDev m, SegArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double U1[3] = {a.U[0][c1], a.U[1][c1], a.U[2][c1]};
+    const double T1 = a.Tf[c1];
+    double U2[3], T2;
+    if (c2 >= 0) {
+        U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
+        T2 = a.Tf[c2];
+    } else {
+        ghost_U(m, k, n, U1, U2);
+        T2 = T1 + 0.0;
+    }
+    for (int c = 0; c < 3; c++) a.fF[c][k] = (U1[c] * fi) + (U2[c] * fo);
+    a.fF[3][k] = (T1 * fi) + (T2 * fo);
+}
+
+constexpr int W_GRAD = 13;   /* U[3] theta jin[9] */
+
+__global__ void k_seg_grad_vol(const NsemDev m, const NsemTables tab, SegArgs a) {
+    extern __shared__ double sm[];
+    const int NP = m.np, NPX = m.npx, NPY = m.npy, NPZ = m.npz;
+    double* dps = sm + (size_t)NP * W_GRAD;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    if (active) {
+        double* my = sm + (size_t)t * W_GRAD;
+        for (int c = 0; c < 3; c++) my[c] = a.U[c][node];
+        my[3] = a.Tf[node];
+        for (int c = 0; c < 9; c++) my[4 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    const double* me = sm + (size_t)t * W_GRAD;
+    double gU[9], gT[3];
+    for (int c = 0; c < 9; c++) gU[c] = 0.0;
+    for (int c = 0; c < 3; c++) gT[c] = 0.0;
+    /* face terms, in the cell's face order */
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+        const double dU[3] = {a.fF[0][k] - me[0], a.fF[1][k] - me[1], a.fF[2][k] - me[2]};
+        const double dT = a.fF[3][k] - me[3];
+        double tU[9];
+        outer(n, dU, tU);
+        if (code & 1) {
+            for (int c = 0; c < 9; c++) gU[c] -= tU[c];
+            for (int c = 0; c < 3; c++) gT[c] -= n[c] * dT;
+        } else {
+            for (int c = 0; c < 9; c++) gU[c] += tU[c];
+            for (int c = 0; c < 3; c++) gT[c] += n[c] * dT;
+        }
+    }
+    /* volume derivative at the node: sources on the x line (self included),
+     * then the y and z lines (field.h:3338-3356) */
+    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
+    const double* J = me + 4;
+    const double* Dx = dps;
+    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    auto add = [&](int lb, const double* dj) {
+        const double* sb = sm + (size_t)lb * W_GRAD;
+        double tU[9];
+        outer(dj, sb, tU);
+        for (int c = 0; c < 9; c++) gU[c] += tU[c];
+        for (int c = 0; c < 3; c++) gT[c] += dj[c] * sb[3];
+    };
+    const int sx = NPY * NPZ, sy = NPZ;
+    for (int ii = 0; ii < NPX; ii++) {
+        double dj[3];
+        if (ii == ia) {
+            const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
+            tdot(J, dv, dj);
+        } else {
+            const double D = Dx[ia * NPX + ii];
+            dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D;
+        }
+        add(t + (ii - ia) * sx, dj);
+    }
+    for (int jj = 0; jj < NPY; jj++) {
+        if (jj == ja) continue;
+        const double D = Dy[ja * NPY + jj];
+        const double dj[3] = {J[XY] * D, J[YY] * D, J[ZY] * D};
+        add(t + (jj - ja) * sy, dj);
+    }
+    for (int kk = 0; kk < NPZ; kk++) {
+        if (kk == ka) continue;
+        const double D = Dz[ka * NPZ + kk];
+        const double dj[3] = {J[XZ] * D, J[YZ] * D, J[ZZ] * D};
+        add(t + (kk - ka), dj);
+    }
+    const double cv = m.cv[node];
+    for (int c = 0; c < 9; c++) a.G[c][node] = gU[c] / cv;
+    for (int c = 0; c < 3; c++) a.G[9 + c][node] = gT[c] / cv;
+}
+
 constexpr int W_RHO = 12;   /* fr[3] jin[9] */
 constexpr int W_UT = 21;    /* fm[9] ft[3] jin[9] */
 
@@ -252,7 +368,10 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
         T2 = T1 + 0.0;
         p2 = p1;
     }
-    /* U equation: flux Fc (x) U + p' I, state rho U */
+    /* artificial viscosity mu = rho^n nu; the wall ghosts' gradient is zero */
+    const double mu1 = a.visc ? a.rho_o[c1] * m.nu : 0.0;
+    const double mu2 = a.visc ? (c2 >= 0 ? a.rho_o[c2] : a.rho_o[c1] + 0.0) * m.nu : 0.0;
+    /* U equation: flux Fc (x) U + p' I - mu grad U, state rho U */
     {
         double A[9], B[9], O[9], F[9], dq[3], out[3];
         outer(Fc1, U1, A);
@@ -262,6 +381,11 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
             A[c] = A[c] + i1 * p1;
             B[c] = B[c] + i1 * p2;
         }
+        if (a.visc)
+            for (int c = 0; c < 9; c++) {
+                A[c] = A[c] - mu1 * a.G[c][c1];
+                B[c] = B[c] - mu2 * (c2 >= 0 ? a.G[c][c2] : 0.0);
+            }
         for (int c = 0; c < 3; c++) dq[c] = (r2 * U2[c] - r1 * U1[c]) * lam;
         outer(en, dq, O);
         for (int c = 0; c < 9; c++) F[c] = (A[c] * fi + B[c] * fo) - O[c];
@@ -270,12 +394,16 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
         a.d[2][k] = out[1];
         a.d[3][k] = out[2];
     }
-    /* T equation: flux Fc theta, state rho theta */
+    /* T equation: flux Fc theta - (mu / Pr) grad theta, state rho theta */
     {
         double F[3];
         const double jump = lam * (r2 * T2 - r1 * T1);
         for (int c = 0; c < 3; c++) {
-            const double x = Fc1[c] * T1, y = Fc2[c] * T2;
+            double x = Fc1[c] * T1, y = Fc2[c] * T2;
+            if (a.visc) {
+                x = x - (mu1 * m.iPr) * a.G[9 + c][c1];
+                y = y - (mu2 * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
+            }
             F[c] = (x * fi + y * fo) - en[c] * jump;
         }
         a.d[4][k] = vdot3(F, n);
@@ -302,6 +430,11 @@ __global__ void k_seg_vol_ut(const NsemDev m, const NsemTables tab, SegArgs a) {
         outer(Fc, U, my);
         for (int c = 0; c < 9; c++) my[c] = my[c] + ((c < 3) ? 1.0 : 0.0) * p;
         for (int c = 0; c < 3; c++) my[9 + c] = Fc[c] * Tf;
+        if (a.visc) {
+            const double mu = a.rho_o[node] * m.nu;
+            for (int c = 0; c < 9; c++) my[c] = my[c] - mu * a.G[c][node];
+            for (int c = 0; c < 3; c++) my[9 + c] = my[9 + c] - (mu * m.iPr) * a.G[9 + c][node];
+        }
         for (int c = 0; c < 9; c++) my[12 + c] = m.jin[(int64_t)c * m.n_int + node];
     }
     __syncthreads();
@@ -384,13 +517,18 @@ SegArgs seg_args(const NsemDev* m, NsemSegBuf* b, int cur, double dt) {
     a.pp = b->pp;
     a.lam = b->lam;
     for (int c = 0; c < 5; c++) a.d[c] = b->d[c];
+    for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
+    for (int c = 0; c < 4; c++) a.fF[c] = b->fF[c];
     a.c_dt = -1.0 / dt;
-    (void)m;
+    a.visc = m->nu != 0.0;
     return a;
 }
 
 size_t smem_rho(const NsemDev* m) {
     return ((size_t)m->np * W_RHO + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+}
+size_t smem_grad(const NsemDev* m) {
+    return ((size_t)m->np * W_GRAD + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
 }
 size_t smem_ut(const NsemDev* m) {
     return ((size_t)m->np * W_UT + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
@@ -402,6 +540,11 @@ int nsem_seg_prepare(const NsemDev* m) {
     if (smem_rho(m) > 48 * 1024) {
         const int e = (int)cudaFuncSetAttribute(k_seg_vol_rho, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem_rho(m));
+        if (e) return e;
+    }
+    if (smem_grad(m) > 48 * 1024) {
+        const int e = (int)cudaFuncSetAttribute(k_seg_grad_vol, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_grad(m));
         if (e) return e;
     }
     if (smem_ut(m) > 48 * 1024)
@@ -420,6 +563,10 @@ int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nst
     for (int s = 0; s < nsteps; s++) {
         const SegArgs a = seg_args(m, b, cur, dt);
         k_seg_prep<<<nb, 256, 0, st>>>(*m, a);
+        if (a.visc) {
+            k_seg_grad_face<<<sb, 256, 0, st>>>(*m, a);
+            k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, a);
+        }
         k_seg_face_rho<<<sb, 256, 0, st>>>(*m, a);
         k_seg_vol_rho<<<(unsigned)m->n_elem, threads, smem_rho(m), st>>>(*m, *t, a);
         k_seg_face_ut<<<sb, 256, 0, st>>>(*m, a);

@@ -20,6 +20,9 @@ struct NsemSegBuf {
     double* pp = nullptr;         /* p' from rho^{n+1}, theta^n             */
     double* lam = nullptr;        /* per slot: Rusanov speed of the step    */
     double* d[5] = {};            /* per slot: lifted fluxes                */
+    /* artificial viscosity (diffusion YES) */
+    double* G[12] = {};           /* per node: grad U (XX..ZX), grad theta  */
+    double* fF[4] = {};           /* per slot: cds(U), cds(theta)           */
 };
 
 int nsem_seg_prepare(const NsemDev* m);

@@ -41,7 +41,7 @@ class _Mesh(ctypes.Structure):
         ("bcU", ctypes.c_void_p), ("p_ref", ctypes.c_void_p), ("rho_ref", ctypes.c_void_p),
         ("gravity", ctypes.c_double * 3),
         ("P0", ctypes.c_double), ("R", ctypes.c_double), ("gamma", ctypes.c_double),
-        ("T0", ctypes.c_double),
+        ("T0", ctypes.c_double), ("nu", ctypes.c_double), ("Pr", ctypes.c_double),
     ]
 
 
@@ -129,6 +129,8 @@ class OracleMesh:
         s.R = float(g.get("R", cp - cv))
         s.gamma = float(g.get("gamma", cp / cv))
         s.T0 = float(g.get("T0", 300.0))
+        s.nu = float(g.get("viscosity", 0.0))
+        s.Pr = float(g.get("Pr", 0.9))
         self.cv_heat = cv
         self.struct = s
         self.gh = f64("gh") if "gh" in g else None

@@ -28,6 +28,8 @@ CONTROLS = """general
     convection_scheme            RUSANOV
     time_scheme                  BDF1
     print_time                   0
+    viscosity                    {viscosity}
+    Pr                           {Pr}
     gravity   0 0 -9.81
     npx       {npx}
     npy       {npy}
@@ -36,7 +38,7 @@ CONTROLS = """general
 
 euler
 {{
-    diffusion                    NO
+    diffusion                    {diffusion}
     buoyancy                     YES
 }}
 """
@@ -100,13 +102,16 @@ boundary 3
 """
 
 
-def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius):
+def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
+               Pr=0.9):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
     npy = 0 if dim == 2 else order
     with open(os.path.join(out, "controls"), "w") as f:
-        f.write(CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order))
+        f.write(CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order,
+                                viscosity=viscosity, Pr=Pr,
+                                diffusion="YES" if viscosity else "NO"))
     grid = GRID_2D if dim == 2 else GRID_3D
     with open(os.path.join(out, "grid"), "w") as f:
         f.write(grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz))

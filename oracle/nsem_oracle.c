@@ -408,6 +408,9 @@ void nsem_oracle_diagnostics(const nsem_oracle_mesh* m, const double* const u[5]
  *   ap = (-1/dt) cV rho^{n+1}, Su += (U^n rho^n)(-1/dt) cV; symmetry ghosts;
  *   T-eq with flux (rho^n U^n) T^n, state rho^{n+1} T^n, the same update;
  *   T -= T0.
+ * With diffusion YES the fluxes also carry the artificial viscosity
+ * mu = rho^n nu: - mu grad U^n in the U equation and - (mu / Pr) grad theta^n in
+ * the T equation, strong-form DG gradients (euler.cpp:189-190, 232, 250).
  * ------------------------------------------------------------------------ */
 
 /* ghosts of a scalar (Neumann) and of the velocity (per slot BC) */
@@ -498,6 +501,80 @@ static void seg_divf(const nsem_oracle_mesh* m, int ncomp, const double* F, cons
     }
 }
 
+/* strong-form DG gradient per unit volume (gradf<true>, field.h:3327-3360 with
+ * grad_flux<true>, field.h:3050-3083): face terms fN (x) (cds(p) - p) in the
+ * cell's face order, then the volume derivative at the node from its three
+ * lines, divided by cV; ncomp 1 (Scalar -> Vector) or 3 (Vector -> Tensor in
+ * XX..ZX order, G[r][c] = d_r p_c).  Interior nodes only: the ghosts' gradient
+ * is set to zero on every wall (fillBCs, field.h:2731-2769). */
+static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G) {
+    const int32_t NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
+    const int64_t n_all = m->n_all;
+    const int w = ncomp == 1 ? 3 : 9;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m->n_elem; e++) {
+        const int64_t base = e * NP;
+        for (int32_t a = 0; a < NP; a++)
+            for (int c = 0; c < w; c++) G[(size_t)w * (base + a) + c] = 0.0;
+        for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
+            for (int32_t nn = 0; nn < NPF; nn++) {
+                const int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
+                const uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+                const double fi = m->fI[k], fo = 1 - fi;
+                const double* n = m->fN + 3 * k;
+                double fF[3];
+                for (int c = 0; c < ncomp; c++)
+                    fF[c] = (p[(size_t)ncomp * c1 + c] * fi) + (p[(size_t)ncomp * c2 + c] * fo);
+                uint32_t own;
+                double sg;
+                if (c1 >= base && c1 < base + NP) { own = c1; sg = 1.0; }
+                else { own = c2; sg = -1.0; }
+                double d[3], t[9];
+                for (int c = 0; c < ncomp; c++) d[c] = fF[c] - p[(size_t)ncomp * own + c];
+                if (ncomp == 1) {
+                    for (int r = 0; r < 3; r++) t[r] = n[r] * d[0];
+                } else {
+                    outer(n, d, t);
+                }
+                double* g = G + (size_t)w * own;
+                if (sg > 0) for (int c = 0; c < w; c++) g[c] += t[c];
+                else for (int c = 0; c < w; c++) g[c] -= t[c];
+            }
+        }
+        for (int32_t ii = 0; ii < NPX; ii++)
+        for (int32_t jj = 0; jj < NPY; jj++)
+        for (int32_t kk = 0; kk < NPZ; kk++) {
+            const int64_t a = base + (int64_t)ii * NPY * NPZ + jj * NPZ + kk;
+            double Jin[9];
+            for (int c = 0; c < 9; c++) Jin[c] = m->Jinv[9 * a + c] * m->cV[a];
+            double* g = G + (size_t)w * a;
+            for (int pass = 0; pass < 3; pass++) {
+                const int32_t lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
+                for (int32_t q = 0; q < lim; q++) {
+                    int32_t im = ii, jm = jj, km = kk;
+                    if (pass == 0) im = q;
+                    else if (pass == 1) { if (q == jj) continue; jm = q; }
+                    else { if (q == kk) continue; km = q; }
+                    const int64_t b = base + (int64_t)im * NPY * NPZ + jm * NPZ + km;
+                    double dv[3], dj[3], t[9];
+                    dv[0] = m->dpsi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[1] = m->psi[0][ii * NPX + im] * m->dpsi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[2] = m->psi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->dpsi[2][kk * NPZ + km];
+                    tdot(Jin, dv, dj);
+                    if (ncomp == 1) {
+                        for (int r = 0; r < 3; r++) t[r] = dj[r] * p[b];
+                    } else {
+                        outer(dj, p + 3 * (size_t)b, t);
+                    }
+                    for (int c = 0; c < w; c++) g[c] += t[c];
+                }
+            }
+            for (int c = 0; c < w; c++) g[c] = g[c] / m->cV[a];
+        }
+    }
+}
+
 void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U_in, double* T_in,
                             double dt, int nsteps) {
     const int64_t n_int = m->n_int, n_all = m->n_all;
@@ -515,6 +592,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
     double* d = calloc(3 * (size_t)n_slot, sizeof(double));
     double* r = calloc(3 * na, sizeof(double));
     double* Fc = calloc(3 * na, sizeof(double));
+    const int visc = m->nu != 0.0;
+    double* mu = visc ? calloc(na, sizeof(double)) : NULL;
+    double* G = visc ? calloc(9 * na, sizeof(double)) : NULL;
+    const double iPr = visc ? 1 / m->Pr : 0.0;
     memcpy(rho, rho_in, (size_t)n_int * sizeof(double));
     memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
     memcpy(T, T_in, (size_t)n_int * sizeof(double));
@@ -526,6 +607,9 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) T[i] += T0;
         memcpy(rhof, rho, (size_t)n_all * sizeof(double));
+        /* artificial viscosity mu = rho nu (euler.cpp:189-190) */
+        if (visc)
+            for (int64_t i = 0; i < n_all; i++) mu[i] = rho[i] * m->nu;
         /* Fc = flxc(rho U), lambda = (cds|U| + cds sqrt(gamma R T)) / 2 */
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
@@ -569,12 +653,18 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
         ghosts_scalar(m, p);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) p[i] -= m->p_ref[i];
-        /* U equation: flux Fc (x) U + p' I, state rho U */
+        /* U equation: flux Fc (x) U + p' I - mu grad U, state rho U */
+        if (visc) grad_strong(m, 3, U, G);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) {
             double* Ft = Fv + 9 * i;
             outer(Fc + 3 * i, U + 3 * i, Ft);
             for (int c = 0; c < 9; c++) Ft[c] = Ft[c] + ((c < 3) ? 1.0 : 0.0) * p[i];
+            if (visc) {
+                /* the ghosts' gradient is zero on the walls */
+                const double* g = G + 9 * i;
+                for (int c = 0; c < 9; c++) Ft[c] = Ft[c] - mu[i] * (i < n_int ? g[c] : 0.0);
+            }
             for (int c = 0; c < 3; c++) q[3 * i + c] = rho[i] * U[3 * i + c];
         }
 #pragma omp parallel for schedule(static)
@@ -604,10 +694,15 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             }
         }
         ghosts_velocity(m, U);
-        /* T equation: flux Fc T, state rho T (U no longer enters) */
+        /* T equation: flux Fc T - (mu / Pr) grad T, state rho T (U no longer enters) */
+        if (visc) grad_strong(m, 1, T, G);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
-            for (int c = 0; c < 3; c++) Fv[3 * i + c] = Fc[3 * i + c] * T[i];
+            for (int c = 0; c < 3; c++) {
+                Fv[3 * i + c] = Fc[3 * i + c] * T[i];
+                if (visc)
+                    Fv[3 * i + c] = Fv[3 * i + c] - (mu[i] * iPr) * (i < n_int ? G[3 * i + c] : 0.0);
+            }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
@@ -637,4 +732,5 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
     memcpy(T_in, T, (size_t)n_int * sizeof(double));
     free(rho); free(rhof); free(U); free(T); free(p); free(lam); free(Fv); free(q); free(d);
     free(r); free(Fc);
+    free(mu); free(G);
 }

@@ -50,6 +50,8 @@ typedef struct {
     double gravity[3];
     double P0, R, gamma;
     double T0;              /* background potential temperature (segregated scheme) */
+    double nu, Pr;          /* artificial viscosity (mu = rho nu) and Prandtl number;
+                             * nu = 0: diffusion NO (segregated scheme) */
 } nsem_oracle_mesh;
 
 /* pow used for the equation of state: 0 = C library pow (as the reference),

@@ -47,10 +47,13 @@ PLAN = {
     "g3_2n7": (0.005, "pert", [10], 10),
 }
 
-# case -> (dt, steps) for the segregated scheme, at steps the scheme keeps stable
+# fixture -> (case, dt, steps, artificial viscosity) for the segregated scheme,
+# at steps the scheme keeps stable; viscosity 1.5 as the reference's srtb example
 SEG_PLAN = {
-    "c1_2d": (0.005, 100),
-    "g3_2": (0.005, 30),
+    "c1_2d": ("c1_2d", 0.005, 100, 0.0),
+    "g3_2": ("g3_2", 0.005, 30, 0.0),
+    "c1_2d_visc": ("c1_2d", 0.005, 30, 1.5),
+    "g3_2_visc": ("g3_2", 0.005, 10, 1.5),
 }
 
 KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
@@ -100,9 +103,9 @@ def make_case(name, ref_bin, tmp):
 
 def make_seg_case(name, ref_bin, tmp):
     from nebulasem_gb300.fields import read_field
-    dt, nsteps = SEG_PLAN[name]
+    base, dt, nsteps, visc = SEG_PLAN[name]
     case = os.path.join(tmp, "seg_" + name)
-    write_case(case, dt=dt, steps=nsteps, **CASES[name])
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, **CASES[base])
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
@@ -119,6 +122,8 @@ def make_seg_case(name, ref_bin, tmp):
         out[f"fldN_{f}"] = v.reshape(-1)
     out["dt"] = np.float64(dt)
     out["nsteps"] = np.int64(nsteps)
+    out["viscosity"] = np.float64(visc)
+    out["Pr"] = np.float64(0.9)
     path = os.path.join(HERE, f"seg_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"seg_{name}: {n_int} interior nodes, {nsteps} steps -> {path} "

@@ -32,7 +32,9 @@ def test_library_exports_every_declared_symbol():
     lib = nebulasem_gb300.load()
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, f"not exported: {missing}"
-    assert lib.nsem_abi_version() == 1
+    with open(os.path.join(ROOT, "include", "nsem.h")) as f:
+        version = int(re.search(r"#define NSEM_ABI_VERSION (\d+)", f.read()).group(1))
+    assert lib.nsem_abi_version() == version
 
 
 def test_create_rejects_null_mesh():

@@ -1,5 +1,6 @@
 """The reference's own update (REF_SEGREGATED: segregated forward Euler,
-BDF1) on the GPU against the oracle's restatement, which is itself pinned bit
+BDF1, with and without the artificial viscosity of diffusion YES) on the GPU
+against the oracle's restatement, which is itself pinned bit
 for bit to the unmodified reference `euler` binary (tests/test_segregated_oracle.py).
 
 With the correctly rounded pow in the oracle the GPU result is bit-identical;
@@ -18,7 +19,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2"])
+@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc"])
 def test_segregated_gpu_bitwise_vs_oracle(case):
     import nebulasem_gb300 as ng
     g = load_golden(case)

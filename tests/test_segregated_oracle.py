@@ -1,5 +1,6 @@
 """The oracle's restatement of the reference's own time update (segregated
-forward Euler, euler.cpp:179-287 with BDF1) reproduces the unmodified reference
+forward Euler, euler.cpp:179-287 with BDF1; with and without the artificial
+viscosity of diffusion YES) reproduces the unmodified reference
 `euler` binary bit for bit (fixtures tests/golden/seg_*.npz, made by
 tests/golden/make_golden.py from the binary's field files)."""
 import numpy as np
@@ -9,7 +10,7 @@ import oracle
 from conftest import load_golden
 
 
-@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2"])
+@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc"])
 def test_segregated_oracle_matches_reference_binary(case):
     g = load_golden(case)
     m = oracle.OracleMesh(g)
