@@ -180,8 +180,11 @@ __device__ __forceinline__ FaceSlot<NX, NY, NZ> face_slot(int t) {
     return f;
 }
 
-template <int NX, int NY, int NZ>
-__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK)
+/* one kernel per stage (0: tendency only): the stage's own loads and update
+ * only; registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the
+ * stage that also carries the FP64 state (measured best on GB300) */
+template <int NX, int NY, int NZ, int STAGE>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (STAGE == 1 || STAGE == 2) ? 8 : 7)
 k_mixed_stage(StageArgs a, MixedTabs tab) {
     using G = Geo<NX, NY, NZ>;
     constexpr int NP = G::NP;
@@ -198,7 +201,7 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
 
     const int t = threadIdx.x;
     const int64_t e = blockIdx.x;
-    const bool has_din = a.Din[0] != nullptr;
+    constexpr bool has_din = STAGE >= 2;
 
     /* issue every global load first: own node, face neighbour, stage-3 FP64 */
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[3] = {0, 0, 0};
@@ -216,7 +219,7 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
         }
         const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 3 * NP;
         bgs[0] = __ldg(bg + t); bgs[1] = __ldg(bg + NP + t); bgs[2] = __ldg(bg + 2 * NP + t);
-        if (a.stage == 3) {
+        if constexpr (STAGE == 3) {
 #pragma unroll
             for (int v = 0; v < 5; v++) u64[v] = __ldg(a.U[v] + n);
         }
@@ -396,16 +399,16 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
     const float Lv[5] = {L0, L1, L2, L3, L4};
 
     const int64_t n = e * NP + t;
-    if (a.stage == 0) {
+    if constexpr (STAGE == 0) {
 #pragma unroll
         for (int v = 0; v < 5; v++) a.L[v][n] = f2d(Lv[v]);
         return;
     }
     const float dt = a.dt;
-    if (a.stage == 1) {
+    if constexpr (STAGE == 1) {
 #pragma unroll
         for (int v = 0; v < 5; v++) a.Dout[v][n] = dt * Lv[v];
-    } else if (a.stage == 2) {
+    } else if constexpr (STAGE == 2) {
 #pragma unroll
         for (int v = 0; v < 5; v++) a.Dout[v][n] = 0.25f * fmaf(dt, Lv[v], din[v]);
     } else {
@@ -457,7 +460,12 @@ __global__ void k_convert(Ptr5 src, Ptr5 dst, FPtr5 shadow, const double* rho_re
 template <int NX, int NY, int NZ>
 int launch_stage(const StageArgs& a, const MixedTabs& t, cudaStream_t st) {
     using G = Geo<NX, NY, NZ>;
-    k_mixed_stage<NX, NY, NZ><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t);
+    switch (a.stage) {
+        case 0: k_mixed_stage<NX, NY, NZ, 0><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        case 1: k_mixed_stage<NX, NY, NZ, 1><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        case 2: k_mixed_stage<NX, NY, NZ, 2><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        default: k_mixed_stage<NX, NY, NZ, 3><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
+    }
     return (int)cudaGetLastError();
 }
 
@@ -465,8 +473,12 @@ template <int NX, int NY, int NZ>
 int prepare_stage() {
     using G = Geo<NX, NY, NZ>;
     if (G::SMEM <= 48 * 1024) return 0;
-    return (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    int e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0>, at, (int)G::SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1>, at, (int)G::SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2>, at, (int)G::SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3>, at, (int)G::SMEM);
+    return e;
 }
 
 int prepare(int nx, int ny, int nz) {
