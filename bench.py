@@ -105,6 +105,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def ncu_traffic(kernel):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+    a kernel class from the committed ncu summary of this workload, or None."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        d = json.load(f)
+    k = d.get("kernels", {}).get(kernel)
+    if not k or d.get("workload") != WORKLOAD:
+        return None, None
+    return float(k["dram_bytes_per_launch"]), d.get("source")
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -282,8 +296,10 @@ def run_ours(args):
     achieved = alg_bytes / per_launch_s / 1e9
     launches_per_step = sum(c for _, c in prof.values()) / max(1, min(args.steps, 5))
     step_gbs = ng.ALG_BYTES_PER_DOF_STAGE_AVG * value / 1e9
+    traffic, traffic_src = ncu_traffic(top_name)
     roof = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm,
-            "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+            "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+            "traffic_source": traffic_src,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
             "alg_bytes_per_launch": alg_bytes,
             "kernel_ms_per_launch": top_ms / top_n,

@@ -57,6 +57,7 @@ struct StageArgs {
     const int32_t* nbr;        /* [6][n_elem]                             */
     const float* J;            /* [3][n_elem]                             */
     const int32_t* layer;      /* [n_elem]                                */
+    const float* Qg;           /* device copy of MixedTabs::Q (coalesced loads) */
     const float* bg;           /* [layers][3][NP]: rho_ref, Theta_ref, p_ref */
     int64_t n_elem;
     float dt, gamma, gR, g[3];
@@ -137,15 +138,23 @@ struct Prim {
 
 __device__ __forceinline__ float safe_sqrt(float s) { return s > 0.0f ? s * rsqrtf(s) : 0.0f; }
 
+/* reciprocal: hardware approximation refined by one Newton step (within an
+ * ulp; both elements of a face evaluate it on the same bits) */
+__device__ __forceinline__ float rcp_nr(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return __fmaf_rn(__fmaf_rn(-x, r, 1.0f), r, r);
+}
+
 __device__ __forceinline__ Prim make_prim(const float* s, float rref, float tref, float pref,
                                           const StageArgs& a) {
     Prim p;
     p.rp = s[0]; p.m0 = s[1]; p.m1 = s[2]; p.m2 = s[3]; p.tp = s[4];
     p.rho = rref + p.rp;
-    const float inv = __frcp_rn(p.rho);
+    const float inv = rcp_nr(p.rho);
     p.u0 = p.m0 * inv; p.u1 = p.m1 * inv; p.u2 = p.m2 * inv;
     p.th = (tref + p.tp) * inv;
-    p.pp = pref * pow1m(p.tp * __frcp_rn(tref), a.eos, a.gamma);
+    p.pp = pref * pow1m(p.tp * rcp_nr(tref), a.eos, a.gamma);
     p.c = safe_sqrt(a.gR * p.th);
     p.umag = safe_sqrt(p.u0 * p.u0 + p.u1 * p.u1 + p.u2 * p.u2);
     return p;
@@ -242,7 +251,7 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
             bgo[0] = __ldg(bg + fs.lo); bgo[1] = __ldg(bg + NP + fs.lo); bgo[2] = __ldg(bg + 2 * NP + fs.lo);
         }
     }
-    for (int q = t; q < 3 * MAXN * MAXN; q += blockDim.x) sQ[q] = (&tab.Q[0][0])[q];
+    for (int q = t; q < 3 * MAXN * MAXN; q += blockDim.x) sQ[q] = __ldg(a.Qg + q);
     if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
 
     /* phase 1: own node primitives and volume fluxes */
@@ -667,7 +676,9 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         allocs->push_back((void*)*ptr);
         return cudaMemcpy(*ptr, vec.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
     };
-    if (!up(&mb->nbr, nbr) || !up(&mb->J, J) || !up(&mb->layer, layer) || !up(&mb->bg, bg)) {
+    const std::vector<float> qtab(&tabs->Q[0][0], &tabs->Q[0][0] + 3 * MAXN * MAXN);
+    if (!up(&mb->nbr, nbr) || !up(&mb->J, J) || !up(&mb->layer, layer) || !up(&mb->bg, bg) ||
+        !up(&mb->Qg, qtab)) {
         err = "precision form: device allocation failed";
         return NSEM_NO_MEMORY;
     }
@@ -713,6 +724,7 @@ StageArgs stage_args(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage
     a.nbr = mb->nbr;
     a.J = mb->J;
     a.layer = mb->layer;
+    a.Qg = mb->Qg;
     a.bg = mb->bg;
     a.n_elem = mb->n_elem;
     a.dt = (float)dt;

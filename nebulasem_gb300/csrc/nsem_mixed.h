@@ -26,6 +26,7 @@ struct NsemMixedBuf {
     float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h       */
     int32_t* layer = nullptr;     /* [n_elem] background layer             */
     float* bg = nullptr;          /* [layers][3][NP] rho_ref, rho_ref T0, p_ref */
+    float* Qg = nullptr;          /* device copy of the line-sum weights   */
     void* tabs = nullptr;         /* host copy of the kernel tables        */
     size_t tabs_size = 0;
 };
