@@ -175,6 +175,17 @@ nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
 nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double* const lam0[5],
                          double* ms_adj);
 
+/* Scalar DG convection: the reference's convection app (apps/convection/
+ * convection.cpp with problem_init NONE and time_scheme BDF1), a scalar T
+ * carried by a fixed wind U with the same weak divergence, Rusanov speed
+ * cds(|U|)/2 and explicit update; FP64, bit-identical to the reference where
+ * no pow is involved (none is).  U: [n_int*3] AoS, T: [n_int], host arrays;
+ * the wind's ghost values follow bc_U, T is NEUMANN on every wall.  Runs on
+ * the context's mesh and dt, independent of the Euler state. */
+nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const double* T);
+nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps);
+nsem_status nsem_convection_get(nsem_ctx* ctx, double* T);
+
 /* Measurement helper: run nsteps SSP-RK3 steps launch by launch (no graph)
  * with CUDA events on the context's stream around every kernel, and report
  * per kernel class the summed device time in ms, the launch count and the

@@ -88,6 +88,9 @@ def load(build_if_missing=True):
         "nsem_forward_checkpointed": ([P, ctypes.c_int, ctypes.c_int, P], ctypes.c_int),
         "nsem_adjoint": ([P, vp, vp, P], ctypes.c_int),
         "nsem_jvp": ([P, vp, vp], ctypes.c_int),
+        "nsem_convection_set": ([P, P, P], ctypes.c_int),
+        "nsem_convection_step": ([P, ctypes.c_int], ctypes.c_int),
+        "nsem_convection_get": ([P, P], ctypes.c_int),
         "nsem_tlm": ([P, ctypes.c_int, vp, vp, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
@@ -289,6 +292,20 @@ class Solver:
         r, u, t = np.empty(n), np.empty((n, 3)), np.empty(n)
         self._check(self._lib.nsem_get_fields(self._ctx, _p(r), _p(u), _p(t)))
         return r, u, t
+
+    def convection_set(self, U, T):
+        """Scalar DG convection: the fixed wind U (n_int x 3) and the scalar T."""
+        u = np.ascontiguousarray(np.asarray(U, dtype=np.float64).reshape(-1, 3))
+        t = _f64(T)
+        self._check(self._lib.nsem_convection_set(self._ctx, _p(u), _p(t)))
+
+    def convection_step(self, nsteps):
+        self._check(self._lib.nsem_convection_step(self._ctx, int(nsteps)))
+
+    def convection_get(self):
+        t = np.empty(self.n_int)
+        self._check(self._lib.nsem_convection_get(self._ctx, _p(t)))
+        return t
 
     def get_state(self):
         n = self.n_int

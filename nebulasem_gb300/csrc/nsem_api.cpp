@@ -33,6 +33,7 @@ struct nsem_ctx {
     NsemMixedBuf mbuf{};
     NsemAdjBuf abuf{};
     NsemSegBuf sbuf{};
+    NsemConvBuf cbuf{};
     bool mixed_ready = false;
     /* where the state lives: 0 conserved in buf.u; 1 perturbation in
      * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme) */
@@ -851,6 +852,78 @@ extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final
     if (s != NSEM_OK) return s;
     if (ms_adj) *ms_adj = ms;
     return NSEM_OK;
+}
+
+/* --------------------------------------------------- scalar convection */
+
+extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const double* T) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!U || !T) return fail(ctx, NSEM_BAD_ARG, "U or T is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    NsemConvBuf& C = ctx->cbuf;
+    const size_t n = (size_t)ctx->dev.n_int, ns = (size_t)ctx->dev.n_slot;
+    nsem_status s;
+    if (!C.ready) {
+        double** arrays[] = {&C.T[0], &C.T[1], &C.U[0], &C.U[1], &C.U[2]};
+        for (double** a : arrays)
+            if ((s = dalloc(ctx, a, n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &C.lam, ns)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &C.d, ns)) != NSEM_OK) return s;
+        if ((s = seg_alloc(ctx)) != NSEM_OK) return s;   /* shared-memory attributes */
+        C.ready = true;
+    }
+    C.cur = 0;
+    NSEM_CUDA(cudaMemcpyAsync(C.T[0], T, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->scratch_aos, U, 3 * n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    int e = nsem_aos_to_soa(ctx->scratch_aos, C.U[0], C.U[1], C.U[2], (int64_t)n, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
+    if ((e = nsem_conv_lambda(&ctx->dev, &C, ctx->stream)))
+        return cuda_fail(ctx, (cudaError_t)e, "convection speed");
+    NSEM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
+    NsemConvBuf& C = ctx->cbuf;
+    if (!C.ready) return fail(ctx, NSEM_BAD_ARG, "nsem_convection_set was not called");
+    if (nsteps == 0) return NSEM_OK;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    auto key = std::make_pair(3 * 2 + C.cur, nsteps);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+        cudaGraph_t g;
+        NSEM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int e = nsem_conv_steps(&ctx->dev, &ctx->tab, &C, nsteps, ctx->dt, ctx->stream);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (e) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return cuda_fail(ctx, (cudaError_t)e, "convection step");
+        }
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaGraphExec_t ex;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+        it = ctx->graphs.emplace(key, ex).first;
+    }
+    NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
+    C.cur ^= (nsteps & 1);
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_convection_get(nsem_ctx* ctx, double* T) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!T) return fail(ctx, NSEM_BAD_ARG, "T is NULL");
+    NsemConvBuf& C = ctx->cbuf;
+    if (!C.ready) return fail(ctx, NSEM_BAD_ARG, "nsem_convection_set was not called");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    NSEM_CUDA(cudaMemcpyAsync(T, C.T[C.cur], (size_t)ctx->dev.n_int * 8, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    return check_status(ctx);
 }
 
 nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double ms[8],

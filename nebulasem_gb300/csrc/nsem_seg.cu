@@ -33,6 +33,10 @@
  * derivative along the three lines, divided by cV; zero on the wall ghosts,
  * fillBCs field.h:2731-2769), and the fluxes carry - mu grad U and
  * - (mu / Pr) grad theta with mu = rho^n nu (euler.cpp:189-190, 232, 250).
+ *
+ * Also here: the reference's scalar DG convection (apps/convection/
+ * convection.cpp, problem_init NONE, BDF1) -- a scalar T in a fixed wind U,
+ * Fc = U, lambda = cds(|U|)/2, the same weak divergence and BDF1 update.
  */
 #include <cuda_runtime.h>
 
@@ -534,9 +538,144 @@ size_t smem_ut(const NsemDev* m) {
     return ((size_t)m->np * W_UT + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
 }
 
+
+/* ------------------------------------------------------------ convection */
+
+struct AdvArgs {
+    const double* T_o;
+    double* T_n;
+    const double* U[3];
+    double* lam;
+    double* d;
+    double c_dt;
+};
+
+__global__ void __launch_bounds__(256) k_conv_lambda(const NsemDev m, AdvArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double U1[3] = {a.U[0][c1], a.U[1][c1], a.U[2][c1]};
+    double U2[3];
+    if (c2 >= 0) {
+        U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
+    } else {
+        ghost_U(m, k, n, U1, U2);
+    }
+    a.lam[k] = (sqrt(vdot3(U1, U1)) * fi + sqrt(vdot3(U2, U2)) * fo) / 2;
+}
+
+__global__ void __launch_bounds__(256) k_conv_face(const NsemDev m, AdvArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double U1[3] = {a.U[0][c1], a.U[1][c1], a.U[2][c1]};
+    const double T1 = a.T_o[c1];
+    double U2[3], T2;
+    if (c2 >= 0) {
+        U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
+        T2 = a.T_o[c2];
+    } else {
+        ghost_U(m, k, n, U1, U2);
+        T2 = T1 + 0.0;
+    }
+    double F[3];
+    const double jump = a.lam[k] * (T2 - T1);
+    for (int c = 0; c < 3; c++) {
+        const double x = U1[c] * T1, y = U2[c] * T2;
+        F[c] = (x * fi + y * fo) - en[c] * jump;
+    }
+    a.d[k] = vdot3(F, n);
+}
+
+constexpr int W_CONV = 12;   /* fv[3] jin[9] */
+
+__global__ void k_conv_vol(const NsemDev m, const NsemTables tab, AdvArgs a) {
+    extern __shared__ double sm[];
+    const int NP = m.np;
+    double* dps = sm + (size_t)NP * W_CONV;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    double T = 0;
+    if (active) {
+        T = a.T_o[node];
+        double* my = sm + (size_t)t * W_CONV;
+        for (int c = 0; c < 3; c++) my[c] = a.U[c][node] * T;
+        for (int c = 0; c < 9; c++) my[3 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    double r = 0.0;
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        if (code & 1) r -= a.d[k];
+        else r += a.d[k];
+    }
+    volume_gather<W_CONV, 3>(m, sm, dps, t, [&](int lb, const double* dj) {
+        r -= vdot3(sm + (size_t)lb * W_CONV, dj);
+    });
+    const double ap = a.c_dt * m.cv[node];
+    const double Tn = (r + T * ap) / (0.0 + ap);
+    a.T_n[node] = Tn;
+    if (!isfinite(Tn)) atomicOr(m.status, NSEM_STATUS_NONFINITE);
+}
+
+size_t smem_conv(const NsemDev* m) {
+    return ((size_t)m->np * W_CONV + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+}
+
+AdvArgs adv_args(NsemConvBuf* b, int cur, double dt) {
+    AdvArgs a;
+    a.T_o = b->T[cur];
+    a.T_n = b->T[cur ^ 1];
+    for (int c = 0; c < 3; c++) a.U[c] = b->U[c];
+    a.lam = b->lam;
+    a.d = b->d;
+    a.c_dt = -1.0 / dt;
+    return a;
+}
+
 }  // namespace
 
+int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream) {
+    const AdvArgs a = adv_args(b, b->cur, 1.0);
+    k_conv_lambda<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);
+    return (int)cudaGetLastError();
+}
+
+int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps, double dt,
+                    void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned sb = (unsigned)((m->n_slot + 255) / 256);
+    const int threads = ((m->np + 31) / 32) * 32;
+    int cur = b->cur;
+    for (int s = 0; s < nsteps; s++) {
+        const AdvArgs a = adv_args(b, cur, dt);
+        k_conv_face<<<sb, 256, 0, st>>>(*m, a);
+        k_conv_vol<<<(unsigned)m->n_elem, threads, smem_conv(m), st>>>(*m, *t, a);
+        const int e = (int)cudaGetLastError();
+        if (e) return e;
+        cur ^= 1;
+    }
+    return 0;
+}
+
 int nsem_seg_prepare(const NsemDev* m) {
+    if (smem_conv(m) > 48 * 1024) {
+        const int e = (int)cudaFuncSetAttribute(k_conv_vol, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_conv(m));
+        if (e) return e;
+    }
     if (smem_rho(m) > 48 * 1024) {
         const int e = (int)cudaFuncSetAttribute(k_seg_vol_rho, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem_rho(m));

@@ -25,7 +25,21 @@ struct NsemSegBuf {
     double* fF[4] = {};           /* per slot: cds(U), cds(theta)           */
 };
 
+/* scalar DG convection (the reference's convection app): T in a fixed wind */
+struct NsemConvBuf {
+    bool ready = false;
+    int cur = 0;                  /* T[cur] holds T^n                       */
+    double* T[2] = {};
+    double* U[3] = {};
+    double* lam = nullptr;        /* per slot: cds(|U|) / 2                 */
+    double* d = nullptr;          /* per slot: lifted flux                  */
+};
+
 int nsem_seg_prepare(const NsemDev* m);
+/* lambda of the fixed wind (once, after U is set) */
+int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream);
+int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps, double dt,
+                    void* stream);
 int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nsteps, double dt,
                    void* stream);
 /* u = conserved state of the primitive fields rho[cur], U, T' */

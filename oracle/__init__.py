@@ -68,6 +68,8 @@ def lib():
         _lib.nsem_oracle_segregated.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_double, ctypes.c_int]
+        _lib.nsem_oracle_convection.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
     return _lib
 
 
@@ -198,6 +200,15 @@ class OracleMesh:
         lib().nsem_oracle_segregated(ctypes.byref(self.struct), _ptr(r), _ptr(u), _ptr(t),
                                      float(dt), int(nsteps))
         return r, u, t
+
+    def convection(self, U, T, dt, nsteps):
+        """The reference's scalar convection of T in the fixed wind U (n_int x 3)."""
+        u = np.ascontiguousarray(np.asarray(U, dtype=np.float64).reshape(-1, 3))
+        t = np.array(T, dtype=np.float64, copy=True)
+        assert u.shape == (self.n_int, 3) and t.shape == (self.n_int,)
+        lib().nsem_oracle_convection(ctypes.byref(self.struct), _ptr(u), _ptr(t), float(dt),
+                                     int(nsteps))
+        return t
 
     def diagnostics(self, u):
         _, up = self._vec(u)

@@ -103,24 +103,32 @@ boundary 3
 
 
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
-               Pr=0.9):
+               Pr=0.9, solver="euler", wind=None):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
     npy = 0 if dim == 2 else order
     with open(os.path.join(out, "controls"), "w") as f:
-        f.write(CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order,
-                                viscosity=viscosity, Pr=Pr,
-                                diffusion="YES" if viscosity else "NO"))
+        ctl = CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order,
+                              viscosity=viscosity, Pr=Pr,
+                              diffusion="YES" if viscosity else "NO")
+        if solver != "euler":
+            ctl = ctl.replace("solver                       euler",
+                              f"solver                       {solver}")
+            ctl += "\n" + solver + "\n{\n    problem_init NONE\n}\n"
+        f.write(ctl)
     grid = GRID_2D if dim == 2 else GRID_3D
     with open(os.path.join(out, "grid"), "w") as f:
         f.write(grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz))
     cx, cy, cz = center
     rx, ry, rz = radius
     cos_init = f"cosine 0 {amp}    {cx} {cy} {cz}   {rx} {ry} {rz}"
+    # the scalar convection case carries a uniform wind with zero-gradient walls
+    U_init = "uniform 0 0 0" if wind is None else "uniform {} {} {}".format(*wind)
+    U_bc = "SYMMETRY" if wind is None else "NEUMANN"
     files = {
         "T0.txt": (1, cos_init, "NEUMANN"),
-        "U0.txt": (3, "uniform 0 0 0", "SYMMETRY"),
+        "U0.txt": (3, U_init, U_bc),
         "p0.txt": (1, "uniform 0", "NEUMANN"),
         "rho0.txt": (1, "uniform 0", "NEUMANN"),
     }
@@ -129,7 +137,8 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
             f.write(FIELD.format(size=size, init=init, bc=bc))
 
 
-# Rising-bubble workloads (2D: one element thick in y, y faces deleted).
+# Rising-bubble workloads (2D: one element thick in y, y faces deleted); the
+# scalar convection cases reuse the meshes and the cosine bump as the scalar.
 CASES = {
     # 1000 x 1000 m, 10x10 elements, N=4, theta' = 0.25(1+cos(pi r/250))
     "c1_2d": dict(dim=2, n=(10, 1, 10), order=4, length=(1000, 100, 1000),

@@ -734,3 +734,60 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
     free(r); free(Fc);
     free(mu); free(G);
 }
+
+/* The reference's scalar DG convection (apps/convection/convection.cpp with
+ * problem_init NONE and BDF1): a fixed wind U, Fc = flxc(U) = U,
+ * lambda = cds(|U|)/2 (convection.cpp:106-108); per step the flux Fc T with the
+ * Rusanov state T, T^{n+1} = Su/ap with ap = (-1/dt) cV and Su += T^n ap
+ * (addTemporal<1> without density), Neumann ghosts of T. */
+void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, double* T_in, double dt,
+                            int nsteps) {
+    const int64_t n_int = m->n_int, n_all = m->n_all;
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    const size_t na = (size_t)n_all + (size_t)m->np;
+    double* U = calloc(3 * na, sizeof(double));
+    double* T = calloc(na, sizeof(double));
+    double* Fv = calloc(3 * na, sizeof(double));
+    double* lam = calloc((size_t)n_slot, sizeof(double));
+    double* d = calloc((size_t)n_slot, sizeof(double));
+    double* r = calloc(na, sizeof(double));
+    memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
+    memcpy(T, T_in, (size_t)n_int * sizeof(double));
+    ghosts_velocity(m, U);
+    ghosts_scalar(m, T);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n_slot; k++) {
+        uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+        const double fi = m->fI[k], fo = 1 - fi;
+        lam[k] = (vmag(U + 3 * (size_t)c1) * fi + vmag(U + 3 * (size_t)c2) * fo) / 2;
+    }
+    const double c_dt = -1.0 / dt;
+    for (int step = 0; step < nsteps; step++) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n_all; i++)
+            for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * T[i];
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < n_slot; k++) {
+            uint32_t c1 = m->FO[k], c2 = m->FN[k];
+            if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+            const double fi = m->fI[k], fo = 1 - fi;
+            const double* n = m->fN + 3 * k;
+            const double mgn = vmag(n);
+            const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+            double F[3], jump = lam[k] * (T[c2] - T[c1]);
+            for (int c = 0; c < 3; c++)
+                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            d[k] = vdot(F, n);
+        }
+        seg_divf(m, 1, Fv, d, r);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n_int; i++) {
+            const double ap = c_dt * m->cV[i];
+            T[i] = (r[i] + T[i] * ap) / (0.0 + ap);
+        }
+        ghosts_scalar(m, T);
+    }
+    memcpy(T_in, T, (size_t)n_int * sizeof(double));
+    free(U); free(T); free(Fv); free(lam); free(d); free(r);
+}

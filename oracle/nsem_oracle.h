@@ -94,6 +94,12 @@ int nsem_oracle_tlm_ssprk3_multi(const nsem_oracle_mesh* m, double* const u[5], 
 void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho, double* U, double* T,
                             double dt, int nsteps);
 
+/* The reference's scalar DG convection (apps/convection/convection.cpp,
+ * problem_init NONE, BDF1): T[n_int] advected by the fixed wind U[n_int*3]
+ * (AoS) for nsteps steps, in place. */
+void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U, double* T, double dt,
+                            int nsteps);
+
 int nsem_oracle_threads(void);
 
 #ifdef __cplusplus

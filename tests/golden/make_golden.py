@@ -18,6 +18,9 @@ and writes its fields; stored are the geometry, the step-0 fields as the solver
 holds them (rho, U, T = theta', from the harness) and the binary's step-N
 fields read back from its binary field files.
 
+Scalar convection fixtures (conv_<case>.npz): the unmodified reference
+`convection` app on a uniform wind; geometry, step-0 fields and its step-N T.
+
 Run in the build container (the reference is not present on GPU machines):
   python tests/golden/make_golden.py --ref /root/reference
 """
@@ -54,6 +57,12 @@ SEG_PLAN = {
     "g3_2": ("g3_2", 0.005, 30, 0.0),
     "c1_2d_visc": ("c1_2d", 0.005, 30, 1.5),
     "g3_2_visc": ("g3_2", 0.005, 10, 1.5),
+}
+
+# fixture -> (case, dt, steps, wind) for the reference's scalar convection app
+CONV_PLAN = {
+    "c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0)),
+    "g3_2": ("g3_2", 1.0, 30, (6.0, -4.0, 5.0)),
 }
 
 KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
@@ -130,11 +139,46 @@ def make_seg_case(name, ref_bin, tmp):
           f"({os.path.getsize(path) / 1e6:.2f} MB)")
 
 
+def make_conv_case(name, ref_bin, tmp):
+    """Scalar convection fixture: the unmodified reference `convection` app
+    (convection.cpp, problem_init NONE, BDF1) on a uniform wind; geometry and
+    the step-0 fields from the harness (run on a copy of the controls naming
+    the euler solver, which the harness binary requires)."""
+    from nebulasem_gb300.fields import read_field
+    base, dt, nsteps, wind = CONV_PLAN[name]
+    case = os.path.join(tmp, "conv_" + name)
+    write_case(case, dt=dt, steps=nsteps, solver="convection", wind=wind, **CASES[base])
+    with open(os.path.join(case, "controls")) as f:
+        ctl = f.read()
+    with open(os.path.join(case, "controls_setup"), "w") as f:
+        f.write(ctl.replace("solver                       convection",
+                            "solver                       euler"))
+    run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    os.makedirs(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls_setup", "setup", "out"], case)
+    d = load_dump(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "convection"), "./controls"], case)
+    n_int = int(d["meta"][7])
+    out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    out["fld0_U"] = d["fld_U"][:3 * n_int]
+    out["fld0_T"] = d["fld_T"][:n_int]
+    v = read_field(os.path.join(case, "T1.bin")).values
+    assert v.shape[0] == n_int
+    out["fldN_T"] = v.reshape(-1)
+    out["dt"] = np.float64(dt)
+    out["nsteps"] = np.int64(nsteps)
+    path = os.path.join(HERE, f"conv_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"conv_{name}: {n_int} interior nodes, {nsteps} steps -> {path} "
+          f"({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", required=True, help="reference NebulaSEM source tree")
     ap.add_argument("--cases", nargs="*", default=sorted(PLAN))
     ap.add_argument("--seg-cases", nargs="*", default=sorted(SEG_PLAN))
+    ap.add_argument("--conv-cases", nargs="*", default=sorted(CONV_PLAN))
     ap.add_argument("-j", type=int, default=8)
     a = ap.parse_args()
     subprocess.run(["make", "-f", "oracle/Makefile.ref", f"REF={a.ref}", f"-j{a.j}"],
@@ -146,6 +190,8 @@ def main():
             make_case(name, ref_bin, tmp)
         for name in a.seg_cases:
             make_seg_case(name, ref_bin, tmp)
+        for name in a.conv_cases:
+            make_conv_case(name, ref_bin, tmp)
     finally:
         shutil.rmtree(tmp)
 
