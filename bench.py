@@ -119,6 +119,24 @@ def ncu_traffic(kernel):
     return float(k["dram_bytes_per_launch"]), d.get("source")
 
 
+def max_over_ranks(ms, world):
+    """The slowest rank's time (replicas: every rank runs the whole workload)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(dofs, steps, ms, world):
+    """Whole-job DOF-stages/s of `world` replicas of the workload in `ms`."""
+    return world * dofs * 3 * steps / (ms * 1e-3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -232,20 +250,13 @@ def run_ours(args):
         e1.record(stream)
         solver.sync()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1), world)
 
     clocks = ClockSampler(local)
     clocks.start()
     ms = timed(prec, args.steps, args.warmup)
     clk = clocks.stop()
-    value = world * dofs * 3 * args.steps / (ms * 1e-3)
+    value = whole_job_value(dofs, args.steps, ms, world)
 
     # the other form, for the mixed/FP64 speed-up
     other = None
