@@ -103,7 +103,7 @@ boundary 3
 
 
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
-               Pr=0.9, solver="euler", wind=None):
+               Pr=0.9, solver="euler", wind=None, time_scheme="BDF1"):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
@@ -112,6 +112,8 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
         ctl = CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order,
                               viscosity=viscosity, Pr=Pr,
                               diffusion="YES" if viscosity else "NO")
+        ctl = ctl.replace("time_scheme                  BDF1",
+                          f"time_scheme                  {time_scheme}")
         if solver != "euler":
             ctl = ctl.replace("solver                       euler",
                               f"solver                       {solver}")

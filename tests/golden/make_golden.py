@@ -50,13 +50,15 @@ PLAN = {
     "g3_2n7": (0.005, "pert", [10], 10),
 }
 
-# fixture -> (case, dt, steps, artificial viscosity) for the segregated scheme,
-# at steps the scheme keeps stable; viscosity 1.5 as the reference's srtb example
+# fixture -> (case, dt, steps, artificial viscosity, time scheme) for the
+# segregated scheme, at steps the scheme keeps stable; viscosity 1.5 as the
+# reference's srtb example; AB1 as its srtb-3d example (same arithmetic as BDF1)
 SEG_PLAN = {
-    "c1_2d": ("c1_2d", 0.005, 100, 0.0),
-    "g3_2": ("g3_2", 0.005, 30, 0.0),
-    "c1_2d_visc": ("c1_2d", 0.005, 30, 1.5),
-    "g3_2_visc": ("g3_2", 0.005, 10, 1.5),
+    "c1_2d": ("c1_2d", 0.005, 100, 0.0, "BDF1"),
+    "g3_2": ("g3_2", 0.005, 30, 0.0, "BDF1"),
+    "c1_2d_visc": ("c1_2d", 0.005, 30, 1.5, "BDF1"),
+    "g3_2_visc": ("g3_2", 0.005, 10, 1.5, "BDF1"),
+    "g3_2_visc_ab1": ("g3_2", 0.005, 10, 1.5, "AB1"),
 }
 
 # fixture -> (case, dt, steps, wind) for the reference's scalar convection app
@@ -112,9 +114,9 @@ def make_case(name, ref_bin, tmp):
 
 def make_seg_case(name, ref_bin, tmp):
     from nebulasem_gb300.fields import read_field
-    base, dt, nsteps, visc = SEG_PLAN[name]
+    base, dt, nsteps, visc, scheme = SEG_PLAN[name]
     case = os.path.join(tmp, "seg_" + name)
-    write_case(case, dt=dt, steps=nsteps, viscosity=visc, **CASES[base])
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, time_scheme=scheme, **CASES[base])
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)

@@ -19,7 +19,8 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc"])
+@pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc",
+                                  "seg_g3_2_visc_ab1"])
 def test_segregated_gpu_bitwise_vs_oracle(case):
     import nebulasem_gb300 as ng
     g = load_golden(case)
