@@ -340,6 +340,18 @@ nsem_status materialise_conserved(nsem_ctx* ctx) {
     return ensure_rep(ctx, 0);
 }
 
+/* the FP64 face kernel of a stage, after the gradients of its state when the
+ * run is viscous */
+int fp64_face(nsem_ctx* ctx, int from_state) {
+    NsemBuf* b = &ctx->buf;
+    if (b->G[0]) {
+        const double* U[3] = {b->prim[0], b->prim[1], b->prim[2]};
+        const int e = nsem_grad_ut(&ctx->dev, &ctx->tab, U, b->prim[3], b->G, b->fF, ctx->stream);
+        if (e) return e;
+    }
+    return nsem_fp64_face(&ctx->dev, b, from_state, ctx->stream);
+}
+
 /* launches of one nsem_step call (captured into a graph) */
 nsem_status enqueue_steps(nsem_ctx* ctx, int nsteps, nsem_precision prec) {
     NsemDev* D = &ctx->dev;
@@ -350,7 +362,7 @@ nsem_status enqueue_steps(nsem_ctx* ctx, int nsteps, nsem_precision prec) {
         if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
         for (int n = 0; n < nsteps; n++) {
             for (int stage = 1; stage <= 3; stage++) {
-                if ((e = nsem_fp64_face(D, b, stage == 1, st)))
+                if ((e = fp64_face(ctx, stage == 1)))
                     return cuda_fail(ctx, (cudaError_t)e, "face");
                 if ((e = nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st)))
                     return cuda_fail(ctx, (cudaError_t)e, "volume");
@@ -398,6 +410,15 @@ nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params, n
     if (s != NSEM_OK) return s;
     int e = nsem_fp64_check_smem(&ctx->dev);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "volume kernel shared memory");
+    if (ctx->dev.nu != 0.0) {
+        /* viscous runs: gradient buffers shared by the coupled and the
+         * segregated schemes; the precision form has no viscous terms */
+        if ((s = seg_alloc(ctx)) != NSEM_OK) return s;
+        for (int c = 0; c < 12; c++) ctx->buf.G[c] = ctx->sbuf.G[c];
+        for (int c = 0; c < 4; c++) ctx->buf.fF[c] = ctx->sbuf.fF[c];
+        ctx->mixed_ready = false;
+        ctx->err = "the precision form has no artificial viscosity (diffusion YES)";
+    }
     return NSEM_OK;
 }
 
@@ -507,7 +528,7 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
     if (rs != NSEM_OK) return rs;
     if (prec == NSEM_FP64) {
         if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
-        if ((e = nsem_fp64_face(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "face");
+        if ((e = fp64_face(ctx, 1))) return cuda_fail(ctx, (cudaError_t)e, "face");
         if ((e = nsem_fp64_volume(D, &ctx->tab, b, 0, ctx->dt, st)))
             return cuda_fail(ctx, (cudaError_t)e, "volume");
     } else if (prec == NSEM_MIXED) {
@@ -617,7 +638,7 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
     int e;
     if ((e = nsem_fp64_prim(D, b, 1, st))) return cuda_fail(ctx, (cudaError_t)e, "prim");
     for (int stage = 1; stage <= 3; stage++) {
-        if ((e = nsem_fp64_face(D, b, stage == 1, st))) return cuda_fail(ctx, (cudaError_t)e, "face");
+        if ((e = fp64_face(ctx, stage == 1))) return cuda_fail(ctx, (cudaError_t)e, "face");
         if ((e = nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st)))
             return cuda_fail(ctx, (cudaError_t)e, "volume");
         nsem_status s = NSEM_OK;
@@ -630,6 +651,8 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
 
 extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
     if (!ctx) return NSEM_BAD_ARG;
+    if (ctx->dev.nu != 0.0)
+        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
@@ -650,6 +673,8 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
 
 extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
     if (!ctx) return NSEM_BAD_ARG;
+    if (ctx->dev.nu != 0.0)
+        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
     for (int v = 0; v < 5; v++)
         if (!dv[v] || !Ld[v]) return fail(ctx, NSEM_BAD_ARG, "dv[v] or Ld[v] is NULL");
@@ -671,6 +696,8 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
 extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
                                 double* const du_final[5], double* ms_tlm) {
     if (!ctx) return NSEM_BAD_ARG;
+    if (ctx->dev.nu != 0.0)
+        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
     if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
     for (int v = 0; v < 5; v++)
@@ -738,6 +765,8 @@ extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const d
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
     if (!ctx) return NSEM_BAD_ARG;
+    if (ctx->dev.nu != 0.0)
+        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     nsem_status s = ensure_rep(ctx, 0);
@@ -785,6 +814,8 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
 extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                     double* const lam0[5], double* ms_adj) {
     if (!ctx) return NSEM_BAD_ARG;
+    if (ctx->dev.nu != 0.0)
+        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
     NsemAdjBuf& A = ctx->abuf;
     if (!A.ready || !A.ckpt || A.nsteps < 1)
@@ -965,7 +996,7 @@ nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double 
         s = timed(0, [&] { return nsem_fp64_prim(D, b, 1, st); });
         for (int n = 0; n < nsteps && s == NSEM_OK; n++)
             for (int stage = 1; stage <= 3 && s == NSEM_OK; stage++) {
-                s = timed(1, [&] { return nsem_fp64_face(D, b, stage == 1, st); });
+                s = timed(1, [&] { return fp64_face(ctx, stage == 1); });
                 if (s == NSEM_OK)
                     s = timed(2, [&] { return nsem_fp64_volume(D, &ctx->tab, b, stage, ctx->dt, st); });
             }

@@ -108,6 +108,7 @@ struct FaceArgs {
     const double* S0;            /* rho of the stage state */
     const double* prim[NSEM_NPRIM];
     double* d[5];
+    const double* G[12];         /* viscous runs: grad U, grad theta (else null) */
 };
 
 __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
@@ -165,6 +166,15 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
             A[c] = A[c] + i1 * p1;
             B[c] = B[c] + i1 * p2;
         }
+        if (a.G[0]) {
+            /* artificial viscosity: - mu grad U, mu = rho nu; zero gradient
+             * on the wall ghosts (euler.cpp:189-190, 232) */
+            const double mu1 = r1 * m.nu, mu2 = r2 * m.nu;
+            for (int c = 0; c < 9; c++) {
+                A[c] = A[c] - mu1 * a.G[c][c1];
+                B[c] = B[c] - mu2 * (c2 >= 0 ? a.G[c][c2] : 0.0);
+            }
+        }
         for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
         outer(en, dq, O);
         for (int c = 0; c < 9; c++) F[c] = (A[c] * fi + B[c] * fo) - O[c];
@@ -178,7 +188,12 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
         double F[3];
         const double jump = lam * (r2 * T2 - r1 * T1);
         for (int c = 0; c < 3; c++) {
-            const double x = (U1[c] * r1) * T1, y = (U2[c] * r2) * T2;
+            double x = (U1[c] * r1) * T1, y = (U2[c] * r2) * T2;
+            if (a.G[0]) {
+                /* - (mu / Pr) grad theta (euler.cpp:250) */
+                x = x - ((r1 * m.nu) * m.iPr) * a.G[9 + c][c1];
+                y = y - ((r2 * m.nu) * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
+            }
             F[c] = (x * fi + y * fo) - en[c] * jump;
         }
         a.d[4][k] = vdot3(F, n);
@@ -193,6 +208,7 @@ struct VolArgs {
     const double* d[5];
     int stage;
     double dt;
+    const double* G[12];    /* viscous runs: grad U, grad theta (else null) */
 };
 
 /* shared layout per node: fr[3] fm[9] ft[3] jin[9] = 24 doubles */
@@ -222,8 +238,14 @@ __global__ void k_volume(const NsemDev m, const NsemTables tab, VolArgs a) {
         double fm[9];
         outer(Fc, U, fm);
         for (int c = 0; c < 9; c++) fm[c] = fm[c] + ((c < 3) ? 1.0 : 0.0) * pp;
+        double ft[3] = {Fc[0] * T, Fc[1] * T, Fc[2] * T};
+        if (a.G[0]) {
+            const double mu = rho * m.nu;
+            for (int c = 0; c < 9; c++) fm[c] = fm[c] - mu * a.G[c][node];
+            for (int c = 0; c < 3; c++) ft[c] = ft[c] - (mu * m.iPr) * a.G[9 + c][node];
+        }
         for (int c = 0; c < 9; c++) my[3 + c] = fm[c];
-        my[12] = Fc[0] * T; my[13] = Fc[1] * T; my[14] = Fc[2] * T;
+        my[12] = ft[0]; my[13] = ft[1]; my[14] = ft[2];
         for (int c = 0; c < 9; c++) my[15 + c] = m.jin[(int64_t)c * m.n_int + node];
     }
     __syncthreads();
@@ -338,6 +360,7 @@ extern "C" int nsem_fp64_face(const NsemDev* m, NsemBuf* b, int from_state, void
     a.S0 = from_state ? b->u[0] : b->s[0];
     for (int c = 0; c < NSEM_NPRIM; c++) a.prim[c] = b->prim[c];
     for (int c = 0; c < 5; c++) a.d[c] = b->d[c];
+    for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
     const int64_t blocks = (m->n_slot + 255) / 256;
     k_face<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(*m, a);
     return launch_err();
@@ -371,6 +394,7 @@ extern "C" int nsem_fp64_volume(const NsemDev* m, const NsemTables* t, NsemBuf* 
         else { a.S[c] = b->s[c]; a.out[c] = b->u[c]; }
     }
     for (int c = 0; c < NSEM_NPRIM; c++) a.prim[c] = b->prim[c];
+    for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
     const int threads = ((m->np + 31) / 32) * 32;
     k_volume<<<(unsigned)m->n_elem, threads, vol_smem(m), (cudaStream_t)stream>>>(*m, *t, a);
     return launch_err();

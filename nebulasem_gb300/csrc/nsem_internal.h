@@ -62,6 +62,8 @@ struct NsemBuf {
     double* prim[NSEM_NPRIM];
     double* d[5];      /* face fluxes per used slot    */
     double* L[5];      /* tendency output (nsem_tendency) */
+    double* G[12];     /* viscous runs: grad U, grad theta of the stage state */
+    double* fF[4];     /* viscous runs: per-slot scratch of the gradients   */
 };
 
 #ifdef __cplusplus

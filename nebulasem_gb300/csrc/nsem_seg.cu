@@ -199,8 +199,16 @@ __device__ __forceinline__ void volume_gather(const NsemDev& m, const double* sm
     for (int ii = ia + 1; ii < NPX; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
 }
 
-/* cds(U^n), cds(theta^n) per slot for the gradients */
-__global__ void __launch_bounds__(256) k_seg_grad_face(const NsemDev m, SegArgs a) {
+/* inputs and outputs of the strong-form gradients of U and theta */
+struct GradArgs {
+    const double* U[3];
+    const double* Tf;        /* full potential temperature */
+    double* G[12];           /* per node: grad U (XX..ZX), grad theta */
+    double* fF[4];           /* per slot: cds(U), cds(theta) */
+};
+
+/* cds(U), cds(theta) per slot for the gradients */
+__global__ void __launch_bounds__(256) k_seg_grad_face(const NsemDev m, GradArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.n_slot) return;
     const int32_t c1 = m.c1[k], c2 = m.c2[k];
@@ -222,7 +230,7 @@ __global__ void __launch_bounds__(256) k_seg_grad_face(const NsemDev m, SegArgs 
 
 constexpr int W_GRAD = 13;   /* U[3] theta jin[9] */
 
-__global__ void k_seg_grad_vol(const NsemDev m, const NsemTables tab, SegArgs a) {
+__global__ void k_seg_grad_vol(const NsemDev m, const NsemTables tab, GradArgs a) {
     extern __shared__ double sm[];
     const int NP = m.np, NPX = m.npx, NPY = m.npy, NPZ = m.npz;
     double* dps = sm + (size_t)NP * W_GRAD;
@@ -647,6 +655,20 @@ AdvArgs adv_args(NsemConvBuf* b, int cur, double dt) {
 
 }  // namespace
 
+int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
+                 double* const* G, double* const* fF, void* stream) {
+    GradArgs ga;
+    for (int c = 0; c < 3; c++) ga.U[c] = U[c];
+    ga.Tf = T;
+    for (int c = 0; c < 12; c++) ga.G[c] = G[c];
+    for (int c = 0; c < 4; c++) ga.fF[c] = fF[c];
+    cudaStream_t st = (cudaStream_t)stream;
+    const int threads = ((m->np + 31) / 32) * 32;
+    k_seg_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
+    k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, ga);
+    return (int)cudaGetLastError();
+}
+
 int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream) {
     const AdvArgs a = adv_args(b, b->cur, 1.0);
     k_conv_lambda<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);
@@ -703,8 +725,13 @@ int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nst
         const SegArgs a = seg_args(m, b, cur, dt);
         k_seg_prep<<<nb, 256, 0, st>>>(*m, a);
         if (a.visc) {
-            k_seg_grad_face<<<sb, 256, 0, st>>>(*m, a);
-            k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, a);
+            GradArgs ga;
+            for (int c = 0; c < 3; c++) ga.U[c] = a.U[c];
+            ga.Tf = a.Tf;
+            for (int c = 0; c < 12; c++) ga.G[c] = a.G[c];
+            for (int c = 0; c < 4; c++) ga.fF[c] = a.fF[c];
+            k_seg_grad_face<<<sb, 256, 0, st>>>(*m, ga);
+            k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, ga);
         }
         k_seg_face_rho<<<sb, 256, 0, st>>>(*m, a);
         k_seg_vol_rho<<<(unsigned)m->n_elem, threads, smem_rho(m), st>>>(*m, *t, a);

@@ -36,6 +36,10 @@ struct NsemConvBuf {
 };
 
 int nsem_seg_prepare(const NsemDev* m);
+/* strong-form gradients of U (3 arrays) and the full theta T into G (12 per
+ * node) with the per-slot scratch fF (4), for the viscous fluxes */
+int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
+                 double* const* G, double* const* fF, void* stream);
 /* lambda of the fixed wind (once, after U is set) */
 int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream);
 int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps, double dt,

@@ -102,6 +102,7 @@ typedef struct {
     double *rho, *U, *T, *p;    /* primitive fields on n_all (+pad) nodes */
     double *d_rho, *d_mom, *d_th; /* per-slot lifted fluxes                */
     double *r_rho, *r_mom, *r_th; /* residuals on n_all nodes              */
+    double *mu, *GU, *GT;         /* artificial viscosity: rho nu, grad U, grad theta */
 } work_t;
 
 static void work_alloc(const nsem_oracle_mesh* m, work_t* w) {
@@ -117,12 +118,19 @@ static void work_alloc(const nsem_oracle_mesh* m, work_t* w) {
     w->r_rho = calloc(na, sizeof(double));
     w->r_mom = calloc(na * 3, sizeof(double));
     w->r_th = calloc(na, sizeof(double));
+    w->mu = w->GU = w->GT = NULL;
+    if (m->nu != 0.0) {
+        w->mu = calloc(na, sizeof(double));
+        w->GU = calloc(na * 9, sizeof(double));
+        w->GT = calloc(na * 3, sizeof(double));
+    }
 }
 
 static void work_free(work_t* w) {
     free(w->rho); free(w->U); free(w->T); free(w->p);
     free(w->d_rho); free(w->d_mom); free(w->d_th);
     free(w->r_rho); free(w->r_mom); free(w->r_th);
+    free(w->mu); free(w->GU); free(w->GT);
 }
 
 /* NEUMANN (value 0) ghost: interior value + 0*|dv| (field.h:2674-2676). */
@@ -133,6 +141,8 @@ static inline double neumann(const nsem_oracle_mesh* m, const double* f, uint32_
     double dv[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
     return f[c1] + 0.0 * vmag(dv);
 }
+
+static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G);
 
 static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t* w,
                      double* p_out) {
@@ -185,6 +195,16 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
     for (int64_t i = 0; i < n_all; i++) w->p[i] -= m->p_ref[i];
     if (p_out) memcpy(p_out, w->p, (size_t)n_all * sizeof(double));
 
+    /* artificial viscosity (diffusion YES, euler.cpp:189-190, 232, 250):
+     * mu = rho nu; strong-form gradients of U and theta, zero on wall ghosts */
+    const int visc = m->nu != 0.0;
+    const double iPr = visc ? 1 / m->Pr : 0.0;
+    if (visc) {
+        for (int64_t i = 0; i < n_all; i++) w->mu[i] = w->rho[i] * m->nu;
+        grad_strong(m, 3, w->U, w->GU);
+        grad_strong(m, 1, w->T, w->GT);
+    }
+
     const double gR = gam * R;
     /* face slots: Rusanov fluxes of the three equations dotted with fN */
 #pragma omp parallel for schedule(static)
@@ -222,6 +242,13 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
                 T1t[c] = T1t[c] + i1 * p1;
                 T2t[c] = T2t[c] + i1 * p2;
             }
+            if (visc) {
+                const int g1 = c1 < (uint32_t)n_int, g2 = c2 < (uint32_t)n_int;
+                for (int c = 0; c < 9; c++) {
+                    T1t[c] = T1t[c] - w->mu[c1] * (g1 ? w->GU[9 * (size_t)c1 + c] : 0.0);
+                    T2t[c] = T2t[c] - w->mu[c2] * (g2 ? w->GU[9 * (size_t)c2 + c] : 0.0);
+                }
+            }
             double dq[3];
             for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
             outer(en, dq, O);
@@ -233,6 +260,10 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
             double F[3], jump = lam * (r2 * T2 - r1 * T1);
             for (int c = 0; c < 3; c++) {
                 double a = (U1[c] * r1) * T1, b = (U2[c] * r2) * T2;
+                if (visc) {
+                    a = a - (w->mu[c1] * iPr) * (c1 < (uint32_t)n_int ? w->GT[3 * (size_t)c1 + c] : 0.0);
+                    b = b - (w->mu[c2] * iPr) * (c2 < (uint32_t)n_int ? w->GT[3 * (size_t)c2 + c] : 0.0);
+                }
                 F[c] = (a * fi + b * fo) - en[c] * jump;
             }
             w->d_th[k] = vdot(F, n);
@@ -281,6 +312,10 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
             outer(Fc, Ub, fm);
             for (int c = 0; c < 9; c++) fm[c] = fm[c] + ((c < 3) ? 1.0 : 0.0) * pb;
             double ft[3] = {Fc[0] * Tb, Fc[1] * Tb, Fc[2] * Tb};
+            if (visc) {
+                for (int c = 0; c < 9; c++) fm[c] = fm[c] - w->mu[b] * w->GU[9 * b + c];
+                for (int c = 0; c < 3; c++) ft[c] = ft[c] - (w->mu[b] * iPr) * w->GT[3 * b + c];
+            }
             for (int pass = 0; pass < 3; pass++) {
                 const int32_t lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
                 for (int32_t q = 0; q < lim; q++) {

@@ -56,6 +56,7 @@ struct Model {
     ScalarCellField* rho_ref;
     ScalarCellField* gh;
     Scalar P0, R, cp, cv, gamma, T0;
+    Scalar nu;              /* artificial viscosity (diffusion YES), else 0 */
 };
 
 /* Residuals Su of the three equations of the euler app (euler.cpp:181-258)
@@ -81,7 +82,9 @@ void residual(Model& m, ScalarCellField& r_rho, VectorCellField& r_U,
     /* euler.cpp:184-186 */
     VectorCellField Fc = flxc(rho * U);
     ScalarFacetField lambdaMax = (cds(mag(U)) + cds(sqrt(p_gamma * R * T))) / 2;
+    /* euler.cpp:189-190: mu = rho viscosity with diffusion YES */
     ScalarCellField mu = Scalar(0);
+    if (m.nu != 0) mu = rho * m.nu;
 
     /* rho equation, euler.cpp:199-203 */
     {
@@ -298,6 +301,7 @@ int main(int argc, char* argv[]) {
     m.P0 = P0; m.cp = cp; m.cv = cv; m.T0 = T0;
     m.R = cp - cv;
     m.gamma = cp / cv;
+    m.nu = diffusion ? Fluid::viscosity : 0;
     const Scalar R = m.R, p_gamma = m.gamma;
 
     /* hydrostatic reference state, euler.cpp:106-123 */

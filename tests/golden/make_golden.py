@@ -42,12 +42,15 @@ from oracle.make_case import CASES, write_case  # noqa: E402
 
 VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
 
-# case -> (dt, start state, [dump steps], total steps)
+# fixture -> (dt, start state, [dump steps], total steps[, case, viscosity])
 PLAN = {
     "c1_2d": (0.0175, "rest", [50, 500], 500),
     "g3_2": (0.01, "pert", [20], 20),
     "g3_4n3": (0.01, "pert", [10, 30], 30),
     "g3_2n7": (0.005, "pert", [10], 10),
+    # coupled SSP-RK3 with the artificial viscosity of diffusion YES
+    "g3_2_visc": (0.01, "pert", [10], 10, "g3_2", 1.5),
+    "c1_2d_visc": (0.005, "rest", [40], 40, "c1_2d", 1.5),
 }
 
 # fixture -> (case, dt, steps, artificial viscosity, time scheme) for the
@@ -79,9 +82,11 @@ def run(cmd, cwd, threads=8):
 
 
 def make_case(name, ref_bin, tmp):
-    dt, start, dumps, nsteps = PLAN[name]
+    dt, start, dumps, nsteps = PLAN[name][:4]
+    base = PLAN[name][4] if len(PLAN[name]) > 4 else name
+    visc = PLAN[name][5] if len(PLAN[name]) > 5 else 0.0
     case = os.path.join(tmp, name)
-    write_case(case, dt=dt, steps=nsteps, **CASES[name])
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, **CASES[base])
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
@@ -105,6 +110,8 @@ def make_case(name, ref_bin, tmp):
         for v in VARS:
             out[f"traj_{s}_{v}"] = r[f"s{s:05d}_{v}"]
     out["dt"] = np.float64(dt)
+    out["viscosity"] = np.float64(visc)
+    out["Pr"] = np.float64(0.9)
     out["start"] = np.array(start)
     out["steps"] = np.array(dumps, dtype=np.int64)
     path = os.path.join(HERE, f"{name}.npz")
