@@ -166,6 +166,41 @@ def run_segregated(name, dt, steps, with_oracle=False):
     return out
 
 
+def run_convection(name, dt, steps, with_oracle=False):
+    """The reference's scalar convection of the workload's theta' in a uniform
+    wind (6, -4, 5) m/s on the GPU; throughput and, with the oracle, bitwise
+    comparison."""
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300.mesh import workload
+    m, u0 = workload(name)
+    n = int(m["meta"][7])
+    T = u0[4] / u0[0] - 300.0
+    U = np.tile(np.array([6.0, -4.0, 5.0]), (n, 1))
+    s = ng.Solver(m, dt=dt)
+    out = dict(workload=name, scheme="convection", dt=dt, steps=steps, nodes=n, dof=n)
+    for rep in range(2):
+        s.convection_set(U, T)
+        s.sync()
+        t = time.perf_counter()
+        s.convection_step(steps)
+        s.sync()
+        wall = time.perf_counter() - t
+    got = s.convection_get()
+    s.close()
+    out["seconds"] = wall
+    out["dof_steps_per_s"] = n * steps / wall
+    out["sha256"] = digest([got])
+    if with_oracle:
+        import oracle
+        om = oracle.OracleMesh(m)
+        t = time.time()
+        want = om.convection(U, T, dt, steps)
+        out["oracle_seconds"] = time.time() - t
+        out["oracle_threads"] = oracle.lib().nsem_oracle_threads()
+        out["equals_oracle_bitwise"] = bool(np.array_equal(got, want))
+    return out
+
+
 def run_oracle(name, dt, steps):
     import oracle
     from nebulasem_gb300.mesh import workload
@@ -187,7 +222,7 @@ def main():
     ap.add_argument("--dt", type=float, required=True)
     ap.add_argument("--steps", type=int, required=True)
     ap.add_argument("--oracle", action="store_true")
-    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg"],
+    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg", "conv"],
                     help="seg: the reference's own segregated update (FP64)")
     ap.add_argument("--with-oracle", action="store_true",
                     help="also run the oracle on this host and compare bit for bit")
@@ -196,6 +231,8 @@ def main():
     a = ap.parse_args()
     if a.scheme == "seg":
         r = run_segregated(a.workload, a.dt, a.steps, a.with_oracle)
+    elif a.scheme == "conv":
+        r = run_convection(a.workload, a.dt, a.steps, a.with_oracle)
     elif a.oracle:
         r = run_oracle(a.workload, a.dt, a.steps)
     else:
