@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "nsem_adjoint.h"
+#include "nsem_gather.cuh"
 
 namespace {
 
@@ -257,14 +258,16 @@ __global__ void k_adj_volume(const NsemDev m, const NsemTables tab, VolAdjArgs a
         dj[2] = Jin[ZX] * dv[0] + Jin[ZY] * dv[1] + Jin[ZZ] * dv[2];
         acc(t + (im - ia) * NPY * NPZ, dj);
     }
-    for (int jm = 0; jm < NPY; jm++) {
-        if (jm == ja) continue;
+    /* the y and z lines without the node itself: the same trip count on
+     * every thread, the node's own index skipped by the mapping */
+    for (int q = 0; q + 1 < NPY; q++) {
+        const int jm = q < ja ? q : q + 1;
         const double D = Dy[ja * NPY + jm];
         const double dj[3] = {Jin[XY] * D, Jin[YY] * D, Jin[ZY] * D};
         acc(t + (jm - ja) * NPZ, dj);
     }
-    for (int km = 0; km < NPZ; km++) {
-        if (km == ka) continue;
+    for (int q = 0; q + 1 < NPZ; q++) {
+        const int km = q < ka ? q : q + 1;
         const double D = Dz[ka * NPZ + km];
         const double dj[3] = {Jin[XZ] * D, Jin[YZ] * D, Jin[ZZ] * D};
         acc(t + (km - ka), dj);
@@ -478,7 +481,6 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
     }
     __syncthreads();
     if (!active) return;
-    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
     double r[5] = {0, 0, 0, 0, 0};
     /* surface lift */
     for (int j = 0; j < 3; j++) {
@@ -489,10 +491,7 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
         for (int v = 0; v < 5; v++) r[v] += sg * a.dd[v][k];
     }
     /* volume term: r[a] -= dF_b . (Jin_b dpsi(b -> a)) over the lines through a */
-    const double* Dx = dps;
-    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
-    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    auto apply = [&](int lb, const double* dj) {
+    nsem_volume_gather<TAN_W, 15>(NPX, NPY, NPZ, sm, dps, t, [&](int lb, const double* dj) {
         const double* sb = sm + (size_t)lb * TAN_W;
         r[0] -= vdot3(sb, dj);
         const double* F = sb + 3;
@@ -500,30 +499,7 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
         r[2] -= F[YX] * dj[0] + F[YY] * dj[1] + F[YZ] * dj[2];
         r[3] -= F[ZX] * dj[0] + F[ZY] * dj[1] + F[ZZ] * dj[2];
         r[4] -= vdot3(sb + 12, dj);
-    };
-    auto line = [&](int dir, int lb, double D) {
-        const double* J = sm + (size_t)lb * TAN_W + 15;
-        double dj[3];
-        if (dir == 0) { dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D; }
-        else if (dir == 1) { dj[0] = J[XY] * D; dj[1] = J[YY] * D; dj[2] = J[ZY] * D; }
-        else { dj[0] = J[XZ] * D; dj[1] = J[YZ] * D; dj[2] = J[ZZ] * D; }
-        apply(lb, dj);
-    };
-    const int sx = NPY * NPZ, sy = NPZ;
-    for (int ii = 0; ii < NPX; ii++)
-        if (ii != ia) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
-    for (int jj = 0; jj < NPY; jj++)
-        if (jj != ja) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
-    for (int kk = 0; kk < NPZ; kk++)
-        if (kk != ka) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
-    {
-        const double* J = sm + (size_t)t * TAN_W + 15;
-        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
-        const double dj[3] = {J[XX] * dv[0] + J[XY] * dv[1] + J[XZ] * dv[2],
-                              J[YX] * dv[0] + J[YY] * dv[1] + J[YZ] * dv[2],
-                              J[ZX] * dv[0] + J[ZY] * dv[1] + J[ZZ] * dv[2]};
-        apply(t, dj);
-    }
+    });
     /* gravity source: r_m -= g (rho - rho_ref) cV */
     const double cv = m.cv[node];
     for (int c = 0; c < 3; c++) r[1 + c] -= m.g[c] * drho * cv;

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "nsem_ddpow.h"
+#include "nsem_gather.cuh"
 #include "nsem_internal.h"
 
 namespace {
@@ -225,7 +226,6 @@ __global__ void k_volume(const NsemDev m, const NsemTables tab, VolArgs a) {
     const int64_t e = blockIdx.x;
     const bool active = t < NP;
     const int64_t node = e * NP + t;
-    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
     double rho = 0, U[3] = {0, 0, 0}, T = 0, pp = 0;
     if (active) {
         rho = a.S[0][node];
@@ -267,38 +267,14 @@ __global__ void k_volume(const NsemDev m, const NsemTables tab, VolArgs a) {
     /* weak volume term.  Source b adds -F_b . (Jin_b . dpsi(b->a)); sources
      * arrive in lexicographic order of b: X-line below, Y-line below, Z-line
      * below, self, Z above, Y above, X above. */
-    const double* Dx = dps;
-    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
-    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    auto apply = [&](int lb, const double* dj) {
+    nsem_volume_gather<SM_W, 15>(NPX, NPY, NPZ, sm, dps, t, [&](int lb, const double* dj) {
         const double* sb = sm + (size_t)lb * SM_W;
         double tv[3];
         r0 -= vdot3(sb, dj);
         tdot(sb + 3, dj, tv);
         r1 -= tv[0]; r2 -= tv[1]; r3 -= tv[2];
         r4 -= vdot3(sb + 12, dj);
-    };
-    auto line = [&](int dir, int lb, double D) {
-        const double* J = sm + (size_t)lb * SM_W + 15;
-        double dj[3];
-        if (dir == 0) { dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D; }
-        else if (dir == 1) { dj[0] = J[XY] * D; dj[1] = J[YY] * D; dj[2] = J[ZY] * D; }
-        else { dj[0] = J[XZ] * D; dj[1] = J[YZ] * D; dj[2] = J[ZZ] * D; }
-        apply(lb, dj);
-    };
-    const int sx = NPY * NPZ, sy = NPZ;
-    for (int ii = 0; ii < ia; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
-    for (int jj = 0; jj < ja; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
-    for (int kk = 0; kk < ka; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
-    {
-        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
-        double dj[3];
-        tdot(sm + (size_t)t * SM_W + 15, dv, dj);
-        apply(t, dj);
-    }
-    for (int kk = ka + 1; kk < NPZ; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
-    for (int jj = ja + 1; jj < NPY; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
-    for (int ii = ia + 1; ii < NPX; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
+    });
 
     /* gravity source: Su -= ((rho - rho_ref) g) cV */
     const double cv = m.cv[node];

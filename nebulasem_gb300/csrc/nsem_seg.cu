@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include "nsem_ddpow.h"
+#include "nsem_gather.cuh"
 #include "nsem_seg.h"
 
 namespace {
@@ -164,39 +165,11 @@ __global__ void __launch_bounds__(256) k_seg_face_rho(const NsemDev m, SegArgs a
     a.d[0][k] = vdot3(F, n);
 }
 
-/* weak volume term gathered in the order of the reference's scatter loop
- * (field.h:3440-3464): X-line below, Y-line below, Z-line below, self,
- * Z above, Y above, X above; sm holds W doubles per node with the metric
- * Jinv cV at offset JOFF */
+/* weak volume term of one node, sources in the reference's scatter order */
 template <int W, int JOFF, typename Apply>
 __device__ __forceinline__ void volume_gather(const NsemDev& m, const double* sm, const double* dps,
                                               int t, Apply apply) {
-    const int NPX = m.npx, NPY = m.npy, NPZ = m.npz;
-    const int ia = t / (NPY * NPZ), ja = (t / NPZ) % NPY, ka = t % NPZ;
-    const double* Dx = dps;
-    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
-    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    auto line = [&](int dir, int lb, double D) {
-        const double* J = sm + (size_t)lb * W + JOFF;
-        double dj[3];
-        if (dir == 0) { dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D; }
-        else if (dir == 1) { dj[0] = J[XY] * D; dj[1] = J[YY] * D; dj[2] = J[ZY] * D; }
-        else { dj[0] = J[XZ] * D; dj[1] = J[YZ] * D; dj[2] = J[ZZ] * D; }
-        apply(lb, dj);
-    };
-    const int sx = NPY * NPZ, sy = NPZ;
-    for (int ii = 0; ii < ia; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
-    for (int jj = 0; jj < ja; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
-    for (int kk = 0; kk < ka; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
-    {
-        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
-        double dj[3];
-        tdot(sm + (size_t)t * W + JOFF, dv, dj);
-        apply(t, dj);
-    }
-    for (int kk = ka + 1; kk < NPZ; kk++) line(2, t + (kk - ka), Dz[kk * NPZ + ka]);
-    for (int jj = ja + 1; jj < NPY; jj++) line(1, t + (jj - ja) * sy, Dy[jj * NPY + ja]);
-    for (int ii = ia + 1; ii < NPX; ii++) line(0, t + (ii - ia) * sx, Dx[ii * NPX + ia]);
+    nsem_volume_gather<W, JOFF>(m.npx, m.npy, m.npz, sm, dps, t, apply);
 }
 
 /* inputs and outputs of the strong-form gradients of U and theta */
@@ -285,25 +258,28 @@ __global__ void k_seg_grad_vol(const NsemDev m, const NsemTables tab, GradArgs a
         for (int c = 0; c < 3; c++) gT[c] += dj[c] * sb[3];
     };
     const int sx = NPY * NPZ, sy = NPZ;
+    /* every thread runs the same trip counts: the node's own term is selected
+     * on the x line, and the y and z loops map past the node's index */
+    double dj_self[3];
+    {
+        const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
+        tdot(J, dv, dj_self);
+    }
     for (int ii = 0; ii < NPX; ii++) {
-        double dj[3];
-        if (ii == ia) {
-            const double dv[3] = {Dx[ia * NPX + ia], Dy[ja * NPY + ja], Dz[ka * NPZ + ka]};
-            tdot(J, dv, dj);
-        } else {
-            const double D = Dx[ia * NPX + ii];
-            dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D;
-        }
+        const double D = Dx[ia * NPX + ii];
+        const bool self = ii == ia;
+        const double dj[3] = {self ? dj_self[0] : J[XX] * D, self ? dj_self[1] : J[YX] * D,
+                              self ? dj_self[2] : J[ZX] * D};
         add(t + (ii - ia) * sx, dj);
     }
-    for (int jj = 0; jj < NPY; jj++) {
-        if (jj == ja) continue;
+    for (int q = 0; q + 1 < NPY; q++) {
+        const int jj = q < ja ? q : q + 1;
         const double D = Dy[ja * NPY + jj];
         const double dj[3] = {J[XY] * D, J[YY] * D, J[ZY] * D};
         add(t + (jj - ja) * sy, dj);
     }
-    for (int kk = 0; kk < NPZ; kk++) {
-        if (kk == ka) continue;
+    for (int q = 0; q + 1 < NPZ; q++) {
+        const int kk = q < ka ? q : q + 1;
         const double D = Dz[ka * NPZ + kk];
         const double dj[3] = {J[XZ] * D, J[YZ] * D, J[ZZ] * D};
         add(t + (kk - ka), dj);
