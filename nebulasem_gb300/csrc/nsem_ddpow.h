@@ -17,6 +17,14 @@
  *     y log x = n ln2/64 + r, exp = 2^(n/64) (1 + expm1 r).
  * Tables come from nsem_pow_tables.h (gen_pow_tables.py, 200-bit mpmath).
  *
+ * Evaluation order (Ziv's strategy, A. Ziv, ACM TOMS 17(3), 1991): a fast
+ * phase evaluates y log x and exp with a few double-double steps and Taylor
+ * polynomials to about 2^-70 relative, then tests whether every value within
+ * the phase's error bound rounds to the same double; only when it does not
+ * (about one call in 2^14) does the accurate double-double phase above run.
+ * Both phases return the correctly rounded x^y, so the result does not
+ * depend on which one ran.
+ *
  * Every operation is an explicit fma or a plain IEEE op; compile without FP
  * contraction (nvcc --fmad=false / gcc -ffp-contract=off) so host and device
  * agree bit for bit.
@@ -219,6 +227,118 @@ NSEM_HD double nsem_exp_dd(nsem_dd y) {
     return (res.h * half) * nsem_u2d((uint64_t)((k - k / 2) + 1023) << 52);
 }
 
+/* Fast phase of x^y for normal x > 0 and finite y: x^y = 2^k (hi + lo) with
+ * |x^y / 2^k - (hi + lo)| <= *err.  Returns 0 (and nothing else) when x is
+ * subnormal or the result leaves the normal range, which the accurate phase
+ * handles.
+ *
+ *   log x = e ln2 - log r_i + log1p z,  z = m r_i - 1 exact, |z| < 2^-7,
+ *   log1p z = z - z^2/2 + z^3 (1/3 - z/4 + ... - z^7/10)   (tail < 2^-80),
+ *   t = y log x = n ln2/64 + r,  |r| <= ln2/128,
+ *   exp t = 2^(n/64) (1 + expm1 r),
+ *   expm1 r = r + r^2/2 + r^3 (1/6 + r/24 + ... + r^5/8!)  (tail < 2^-86).
+ * z^2 and r^2 are kept exact as products of two doubles (two_prod), the
+ * higher terms are plain doubles; the error bound holds the worst-case sum
+ * of the truncation and rounding terms with a factor of 4 to spare. */
+NSEM_HD int nsem_pow_fast_core(double x, double y, double* hi, double* lo, double* err, int* kk) {
+    const uint64_t u = nsem_d2u(x);
+    const int ex = (int)((u >> 52) & 0x7ff);
+    if (ex == 0) return 0;
+    int e = ex - 1023;
+    double m = nsem_u2d((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
+    if (m > 1.4142135623730951) { m = m * 0.5; e += 1; }
+    int i = (int)((m - 0.703125) * 128.0);
+    if (i < 0) i = 0;
+    if (i > NSEM_LOG_NBIN - 1) i = NSEM_LOG_NBIN - 1;
+    /* z = m r_i - 1: the product is exact as a pair, the subtraction exact
+     * (Sterbenz), and |p.h - 1| >= |p.l| unless it is zero */
+    const nsem_dd p = nsem_two_prod(m, NSEM_LOG_R[i]);
+    const nsem_dd z = nsem_fast_two_sum(p.h - 1.0, p.l);
+    const nsem_dd z2 = nsem_two_prod(z.h, z.h);
+    double q = -1.0 / 10;
+    q = fma(q, z.h, 1.0 / 9);
+    q = fma(q, z.h, -1.0 / 8);
+    q = fma(q, z.h, 1.0 / 7);
+    q = fma(q, z.h, -1.0 / 6);
+    q = fma(q, z.h, 1.0 / 5);
+    q = fma(q, z.h, -1.0 / 4);
+    q = fma(q, z.h, 1.0 / 3);
+    const double z3q = (z2.h * z.h) * q;
+    const nsem_dd a = nsem_fast_two_sum(z.h, -0.5 * z2.h);
+    const double l1p_lo = ((a.l + z.l) - (0.5 * z2.l + z.h * z.l)) + z3q;
+    /* e ln2 - log r_i + log1p z; e LN2_HI is exact (LN2_HI has 32 bits) */
+    const double de = (double)e;
+    const nsem_dd em = nsem_two_prod(de, NSEM_LN2_MID);
+    const nsem_dd h1 = nsem_two_sum(de * NSEM_LN2_HI, NSEM_LOG_NLR[i][0]);
+    const nsem_dd h2 = nsem_two_sum(h1.h, a.h);
+    const double llo = ((((h1.l + h2.l) + NSEM_LOG_NLR[i][1]) + l1p_lo) + em.h) + (em.l + de * NSEM_LN2_LO);
+    const nsem_dd L = nsem_fast_two_sum(h2.h, llo);
+    /* t = y log x */
+    nsem_dd t = nsem_two_prod(L.h, y);
+    t.l += L.l * y;
+    if (!(fabs(t.h) < 700.0)) return 0;
+    /* r = t - n ln2/64 */
+    const double nd = rint(t.h * NSEM_INV_LN2_64);
+    const long long n = (long long)nd;
+    const double rhi = fma(-nd, NSEM_LN2_HI / 64, t.h);
+    const nsem_dd c2 = nsem_two_prod(nd, NSEM_LN2_MID / 64);
+    const double rlo = (t.l - c2.h) - (c2.l + nd * (NSEM_LN2_LO / 64));
+    const nsem_dd r = nsem_two_sum(rhi, rlo);
+    /* expm1 r */
+    const nsem_dd r2 = nsem_two_prod(r.h, r.h);
+    double c = 1.0 / 40320;
+    c = fma(c, r.h, 1.0 / 5040);
+    c = fma(c, r.h, 1.0 / 720);
+    c = fma(c, r.h, 1.0 / 120);
+    c = fma(c, r.h, 1.0 / 24);
+    c = fma(c, r.h, 1.0 / 6);
+    const double r3c = (r2.h * r.h) * c;
+    const nsem_dd b = nsem_fast_two_sum(r.h, 0.5 * r2.h);
+    const double elo = ((b.l + r.l) + (0.5 * r2.l + r.h * r.l)) + r3c;
+    /* 2^(j/64) (1 + expm1 r) */
+    const int j = (int)(n & 63);
+    const long long k = (n - j) / 64;
+    if (!(k > -1022 && k < 1023)) return 0;
+    const double Th = NSEM_EXP2[j][0], Tl = NSEM_EXP2[j][1];
+    const nsem_dd pe = nsem_two_prod(Th, b.h);
+    const nsem_dd h = nsem_fast_two_sum(Th, pe.h);
+    const double lo2 = (((h.l + pe.l) + Th * elo) + Tl) + Tl * b.h;
+    const nsem_dd res = nsem_fast_two_sum(h.h, lo2);
+    *hi = res.h;
+    *lo = res.l;
+    /* log: 2^-70 + 2^-96 |log x| absolute (worst-case sum of the terms above
+     * below 2^-72); exp: 2^-70 relative (below 2^-73 for |t| < 700) */
+    *err = ((fabs(y) * (0x1p-70 + 0x1p-96 * fabs(L.h)) + 0x1p-100 * fabs(t.h)) + 0x1p-70) * res.h;
+    *kk = (int)k;
+    return 1;
+}
+
+/* correctly rounded x^y from the fast phase, or 0 when its rounding test
+ * cannot decide: every real within err of hi + lo rounds to the same double
+ * (rounding is monotonic; lo -/+ 2 err absorbs the rounding of the shifted
+ * low parts, which is below 2^-106 hi) */
+NSEM_HD int nsem_pow_fast(double x, double y, double* out) {
+    double hi, lo, err;
+    int k;
+    if (!nsem_pow_fast_core(x, y, &hi, &lo, &err, &k)) return 0;
+    const double a = hi + (lo - 2.0 * err);
+    const double b = hi + (lo + 2.0 * err);
+    if (a != b) return 0;
+    *out = a * nsem_u2d((uint64_t)(k + 1023) << 52);
+    return 1;
+}
+
+/* accurate phase, kept out of line on the device: it runs for about one
+ * call in 2^14 and would otherwise hold registers in every caller */
+#ifdef __CUDACC__
+__host__ __device__ __noinline__ static double nsem_pow_accurate(double x, double y)
+#else
+static double nsem_pow_accurate(double x, double y)
+#endif
+{
+    return nsem_exp_dd(nsem_dd_mul_d(nsem_log_dd(x), y));
+}
+
 /* x^y for the equation of state; x > 0 expected.  Non-positive, infinite or
  * NaN arguments give the IEEE pow result for those cases that occur here. */
 NSEM_HD double nsem_pow(double x, double y) {
@@ -228,7 +348,9 @@ NSEM_HD double nsem_pow(double x, double y) {
         return 0.0 / 0.0;
     }
     if (y == 0.0 || x == 1.0) return 1.0;
-    return nsem_exp_dd(nsem_dd_mul_d(nsem_log_dd(x), y));
+    double r;
+    if (nsem_pow_fast(x, y, &r)) return r;
+    return nsem_pow_accurate(x, y);
 }
 
 #endif

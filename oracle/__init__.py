@@ -57,6 +57,15 @@ def lib():
                                                  ctypes.c_double, ctypes.c_void_p]
         _lib.nsem_oracle_pow_dd.argtypes = [ctypes.c_double, ctypes.c_double]
         _lib.nsem_oracle_pow_dd.restype = ctypes.c_double
+        _lib.nsem_oracle_pow_dd_accurate.argtypes = [ctypes.c_double, ctypes.c_double]
+        _lib.nsem_oracle_pow_dd_accurate.restype = ctypes.c_double
+        D = ctypes.POINTER(ctypes.c_double)
+        _lib.nsem_oracle_pow_fast_core.argtypes = [ctypes.c_double, ctypes.c_double, D, D, D,
+                                                   ctypes.POINTER(ctypes.c_int)]
+        _lib.nsem_oracle_pow_fast_core.restype = ctypes.c_int
+        I64 = ctypes.POINTER(ctypes.c_int64)
+        _lib.nsem_oracle_pow_fast_sweep.argtypes = [ctypes.c_int64, ctypes.c_uint64, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_double, I64, I64]
         _lib.nsem_oracle_set_pow.argtypes = [ctypes.c_int]
         _lib.nsem_oracle_threads.restype = ctypes.c_int
         _lib.nsem_oracle_jvp.argtypes = [ctypes.POINTER(_Mesh), P, P, P, P]
@@ -225,6 +234,29 @@ def set_pow(which):
 
 def pow_dd(x, y):
     return lib().nsem_oracle_pow_dd(float(x), float(y))
+
+
+def pow_dd_accurate(x, y):
+    """The double-double phase of pow_dd alone (no fast phase)."""
+    return lib().nsem_oracle_pow_dd_accurate(float(x), float(y))
+
+
+def pow_fast_core(x, y):
+    """The fast phase's unrounded 2^k (hi + lo) and error bound err (scaled
+    by 2^-k like hi), or None outside its domain."""
+    hi, lo, err, k = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    if not lib().nsem_oracle_pow_fast_core(float(x), float(y), ctypes.byref(hi), ctypes.byref(lo),
+                                           ctypes.byref(err), ctypes.byref(k)):
+        return None
+    return hi.value, lo.value, err.value, k.value
+
+
+def pow_fast_sweep(n, seed, xlo, xhi, y):
+    """(fallbacks, mismatches) of the fast phase over n log-uniform x."""
+    fb, mm = ctypes.c_int64(), ctypes.c_int64()
+    lib().nsem_oracle_pow_fast_sweep(int(n), int(seed), float(xlo), float(xhi), float(y),
+                                     ctypes.byref(fb), ctypes.byref(mm))
+    return fb.value, mm.value
 
 
 def load_dump(path):
