@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define NSEM_ABI_VERSION 2
+#define NSEM_ABI_VERSION 3
 
 typedef enum {
     NSEM_OK = 0,
@@ -131,6 +131,13 @@ nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rho
 nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U,
                             const double* T);
 nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T);
+
+/* The euler app's pressure field p (= p - p_ref, euler.cpp:211-213) on
+ * interior nodes, as the solver holds it when it writes its fields: after a
+ * segregated step the p' of that step (from rho^{n+1} and theta^n,
+ * euler.cpp:210-213); otherwise p' of the current state (euler.cpp:155-160),
+ * with the correctly rounded pow.  Host buffer. */
+nsem_status nsem_get_pressure(nsem_ctx* ctx, double* p_prime);
 
 /* Tendencies L = -Su/cV of (rho, rho u, rho v, rho w, rho theta) for the
  * current state, the divf + src chains of euler.cpp:193-258 evaluated on one

@@ -79,6 +79,7 @@ def load(build_if_missing=True):
         "nsem_get_state": ([P, P, P, P], ctypes.c_int),
         "nsem_set_fields": ([P, P, P, P], ctypes.c_int),
         "nsem_get_fields": ([P, P, P, P], ctypes.c_int),
+        "nsem_get_pressure": ([P, P], ctypes.c_int),
         "nsem_tendency": ([P, ctypes.c_int, vp, P], ctypes.c_int),
         "nsem_step": ([P, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "nsem_diagnostics": ([P, P, P, P], ctypes.c_int),
@@ -292,6 +293,13 @@ class Solver:
         r, u, t = np.empty(n), np.empty((n, 3)), np.empty(n)
         self._check(self._lib.nsem_get_fields(self._ctx, _p(r), _p(u), _p(t)))
         return r, u, t
+
+    def get_pressure(self):
+        """p - p_ref as the euler app holds it (after a segregated step: the p'
+        of that step, from rho^{n+1} and theta^n; otherwise of the state)."""
+        p = np.empty(self.n_int)
+        self._check(self._lib.nsem_get_pressure(self._ctx, _p(p)))
+        return p
 
     def convection_set(self, U, T):
         """Scalar DG convection: the fixed wind U (n_int x 3) and the scalar T."""

@@ -51,6 +51,30 @@ def _stale(obj, src):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+DRIVER = os.path.join(HERE, "driver")
+DRIVER_EXE = os.path.join(OUT, "nsem_euler")
+
+
+def build_driver(verbose=False, force=False):
+    """The host driver nsem_euler (C++17, links libnsem_gpu.so through the C ABI)."""
+    srcs = sorted(os.path.join(DRIVER, f) for f in os.listdir(DRIVER) if f.endswith(".cpp"))
+    deps = srcs + [os.path.join(DRIVER, f) for f in os.listdir(DRIVER) if f.endswith(".h")]
+    deps += [LIB, os.path.join(ROOT, "include", "nsem.h"), __file__]
+    if not force and os.path.exists(DRIVER_EXE):
+        t = os.path.getmtime(DRIVER_EXE)
+        if all(os.path.getmtime(d) <= t for d in deps):
+            return DRIVER_EXE
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + DRIVER]
+    cmd += srcs + ["-L" + OUT, "-lnsem_gpu", "-Wl,-rpath,$ORIGIN", "-o", DRIVER_EXE]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout, r.stderr, file=sys.stderr)
+    return DRIVER_EXE
+
+
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
     cc = nvcc()
@@ -74,6 +98,7 @@ def build(verbose=False, force=False):
     objs = [os.path.join(OUT, n + ".o") for n, _ in UNITS]
     if jobs or not os.path.exists(LIB):
         run([cc] + ARCH + ["-shared", "-o", LIB] + objs)
+    build_driver(verbose, force)
     return LIB
 
 

@@ -38,6 +38,7 @@ struct nsem_ctx {
     /* where the state lives: 0 conserved in buf.u; 1 perturbation in
      * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme) */
     int rep = 0;
+    bool seg_pp_valid = false;   /* sbuf.pp holds the p' of the last segregated step */
     double dt = 0, T0 = 0;
     int64_t n_all = 0;
     std::vector<void*> allocations;
@@ -484,8 +485,26 @@ nsem_status nsem_set_fields(nsem_ctx* ctx, const double* rho, const double* U, c
     int e = nsem_aos_to_soa(ctx->scratch_aos, S.U[0], S.U[1], S.U[2], ctx->dev.n_int, ctx->stream);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
     ctx->rep = 2;
+    ctx->seg_pp_valid = false;
     NSEM_CUDA(cudaStreamSynchronize(ctx->stream));
     return NSEM_OK;
+}
+
+nsem_status nsem_get_pressure(nsem_ctx* ctx, double* p_prime) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (!p_prime) return fail(ctx, NSEM_BAD_ARG, "p_prime is NULL");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ctx->dev.n_int;
+    if (ctx->rep == 2 && ctx->seg_pp_valid) {
+        NSEM_CUDA(cudaMemcpyAsync(p_prime, ctx->sbuf.pp, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        return check_status(ctx);
+    }
+    nsem_status rs = materialise_conserved(ctx);
+    if (rs != NSEM_OK) return rs;
+    const int e = nsem_fp64_prim(&ctx->dev, &ctx->buf, 1, (void*)ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "prim");
+    NSEM_CUDA(cudaMemcpyAsync(p_prime, ctx->buf.prim[4], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
 }
 
 nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
@@ -558,6 +577,7 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
     NSEM_CUDA(cudaSetDevice(ctx->device));
     if (prec == NSEM_MIXED && !ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
     const int form = (scheme == NSEM_REF_SEGREGATED) ? 2 : (prec == NSEM_MIXED ? 1 : 0);
+    ctx->seg_pp_valid = false;
     nsem_status rs = ensure_rep(ctx, form);
     if (rs != NSEM_OK) return rs;
     const int cur = form == 1 ? ctx->mbuf.cur : form == 2 ? ctx->sbuf.cur : 0;
@@ -587,7 +607,10 @@ nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precis
     }
     NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
     if (form == 1) ctx->mbuf.cur ^= (nsteps & 1);
-    if (form == 2) ctx->sbuf.cur ^= (nsteps & 1);
+    if (form == 2) {
+        ctx->sbuf.cur ^= (nsteps & 1);
+        ctx->seg_pp_valid = true;
+    }
     NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, ctx->stream));
     return NSEM_OK;
