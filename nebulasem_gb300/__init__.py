@@ -119,12 +119,23 @@ class Solver:
 
     ``mesh`` is a dict in the reference's layout (the keys of the golden
     fixtures: meta, cC, cV, Jinv, FO, FN, fN, fI, allFaces, faceIdx0,
-    faceIdx1, psi0-2, dpsi0-2, bcU and optionally p_ref, rho_ref).
+    faceIdx1, psi0-2, dpsi0-2, bcU and optionally p_ref, rho_ref).  Fluid
+    constants not given as arguments come from the dict's P0, T0, cp, cv,
+    gravity, viscosity, Pr when present, else 1e5, 300, 1004.5, 717.5,
+    (0, 0, -9.81), 0, 0.9.
     """
 
-    def __init__(self, mesh, dt, P0=1e5, T0=300.0, cp=1004.5, cv=717.5,
-                 gravity=(0.0, 0.0, -9.81), device=0, use_ref_background=True,
-                 viscosity=None, Pr=None):
+    def __init__(self, mesh, dt, P0=None, T0=None, cp=None, cv=None, gravity=None, device=0,
+                 use_ref_background=True, viscosity=None, Pr=None):
+        def const(name, given, default):
+            if given is not None:
+                return given
+            return mesh[name] if name in mesh else default
+        P0 = float(const("P0", P0, 1e5))
+        T0 = float(const("T0", T0, 300.0))
+        cp = float(const("cp", cp, 1004.5))
+        cv = float(const("cv", cv, 717.5))
+        gravity = [float(x) for x in np.asarray(const("gravity", gravity, (0.0, 0.0, -9.81)))]
         lib = load()
         meta = np.asarray(mesh["meta"], dtype=np.int64)
         npx, npy, npz, np_, npf = (int(v) for v in meta[:5])

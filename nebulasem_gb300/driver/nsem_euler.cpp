@@ -6,9 +6,10 @@
  * reference is run,
  *
  *     nsem_euler ./controls [--scheme ref|ssprk3] [--prec fp64|mixed]
- *                           [--print-every K] [--device D] [--dump DIR]
+ *                           [--print-every K] [--device D] [--blocks FILE] [--dump DIR]
  *
- * It reads the controls file, the block description named by `mesh`, and
+ * It reads the controls file, the block description (the mesh app's input:
+ * --blocks, by default the file named by the controls' `mesh` key), and
  * the fields p, U, T, rho at start_step / write_interval; sets up the
  * hydrostatic background and rho from p as euler.cpp:104-147 does; advances
  * the state through libnsem_gpu's C ABI; prints the mass / energy / volume
@@ -55,13 +56,14 @@ struct Options {
     long print_every = 1;
     int device = 0;
     std::string dump;
+    std::string blocks;
 };
 
 [[noreturn]] void usage(const char* msg) {
     if (msg) std::fprintf(stderr, "nsem_euler: %s\n", msg);
     std::fprintf(stderr,
                  "usage: nsem_euler <controls> [--scheme ref|ssprk3] [--prec fp64|mixed]\n"
-                 "                  [--print-every K] [--device D] [--dump DIR]\n");
+                 "                  [--print-every K] [--device D] [--blocks FILE] [--dump DIR]\n");
     std::exit(2);
 }
 
@@ -78,6 +80,7 @@ Options parse_args(int argc, char** argv) {
         else if (a == "--print-every") o.print_every = std::atol(val().c_str());
         else if (a == "--device") o.device = std::atoi(val().c_str());
         else if (a == "--dump") o.dump = val();
+        else if (a == "--blocks") o.blocks = val();
         else if (a == "-h" || a == "--help") usage(nullptr);
         else if (!a.empty() && a[0] == '-') usage(("unknown option " + a).c_str());
         else if (o.controls.empty()) o.controls = a;
@@ -177,8 +180,17 @@ int run(const Options& opt) {
     if (npx < 1 || npy < 1 || npz < 1 || npx > 10 || npy > 10 || npz > 10)
         throw std::runtime_error("npx/npy/npz out of range (0..9)");
 
-    /* mesh */
-    const BlockDesc blk = read_block_description(mesh_name);
+    /* mesh: the block description the mesh app reads (the reference's
+     * test.sh runs `mesh <file> -o <mesh>_0.bin`); by default a file named
+     * after the controls' mesh key */
+    const std::string blocks = opt.blocks.empty() ? mesh_name : opt.blocks;
+    {
+        std::ifstream probe(blocks);
+        if (!probe)
+            throw std::runtime_error("no block description '" + blocks +
+                                     "' (the mesh app's input file; name it with --blocks)");
+    }
+    const BlockDesc blk = read_block_description(blocks);
     /* node coordinates first (boundary conditions fill bc_U below) */
     CaseMesh M = build_box_mesh(blk, npx, npy, npz, {1, 1, 1, 1, 1, 1});
     const long n = (long)M.n_int;

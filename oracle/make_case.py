@@ -15,10 +15,10 @@ CONTROLS = """general
 {{
     solver                       euler
     mesh                         grid
-    P0                           100000
+    P0                           {P0}
     T0                           300
-    cp                           1004.5
-    cv                           717.5
+    cp                           {cp}
+    cv                           {cv}
     state                        TRANSIENT
     start_step                   0
     end_step                     {end_step}
@@ -30,7 +30,7 @@ CONTROLS = """general
     print_time                   0
     viscosity                    {viscosity}
     Pr                           {Pr}
-    gravity   0 0 -9.81
+    gravity   0 0 {gz}
     npx       {npx}
     npy       {npy}
     npz       {npz}
@@ -103,7 +103,8 @@ boundary 3
 
 
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
-               Pr=0.9, solver="euler", wind=None, time_scheme="BDF1"):
+               Pr=0.9, solver="euler", wind=None, time_scheme="BDF1", P0=100000, cp=1004.5,
+               cv=717.5, gz=-9.81):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
@@ -111,7 +112,8 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
     with open(os.path.join(out, "controls"), "w") as f:
         ctl = CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=npy, npz=order,
                               viscosity=viscosity, Pr=Pr,
-                              diffusion="YES" if viscosity else "NO")
+                              diffusion="YES" if viscosity else "NO",
+                              P0=P0, cp=cp, cv=cv, gz=gz)
         ctl = ctl.replace("time_scheme                  BDF1",
                           f"time_scheme                  {time_scheme}")
         if solver != "euler":
@@ -141,6 +143,10 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
 
 # Rising-bubble workloads (2D: one element thick in y, y faces deleted); the
 # scalar convection cases reuse the meshes and the cosine bump as the scalar.
+# The fluid constants of the reference's srtb example (its controls set
+# viscosity 1.5 and gravity -9.80606 and leave P0, cp, cv at the Fluid::
+# defaults of apps/utils/properties.cpp): pass as write_case(**SRTB_FLUID).
+SRTB_FLUID = dict(P0=101325, cp=1004.67, cv=715.5, gz=-9.80606, viscosity=1.5)
 CASES = {
     # 1000 x 1000 m, 10x10 elements, N=4, theta' = 0.25(1+cos(pi r/250))
     "c1_2d": dict(dim=2, n=(10, 1, 10), order=4, length=(1000, 100, 1000),

@@ -62,6 +62,9 @@ SEG_PLAN = {
     "c1_2d_visc": ("c1_2d", 0.005, 30, 1.5, "BDF1"),
     "g3_2_visc": ("g3_2", 0.005, 10, 1.5, "BDF1"),
     "g3_2_visc_ab1": ("g3_2", 0.005, 10, 1.5, "AB1"),
+    # the reference's srtb example as shipped: its viscosity and gravity, the
+    # Fluid:: defaults for P0, cp, cv (examples/atmo/srtb/controls)
+    "srtb": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb"),
 }
 
 # fixture -> (case, dt, steps, wind) for the reference's scalar convection app
@@ -121,9 +124,13 @@ def make_case(name, ref_bin, tmp):
 
 def make_seg_case(name, ref_bin, tmp):
     from nebulasem_gb300.fields import read_field
-    base, dt, nsteps, visc, scheme = SEG_PLAN[name]
+    from oracle.make_case import SRTB_FLUID
+    base, dt, nsteps, visc, scheme = SEG_PLAN[name][:5]
+    fluid = dict(SRTB_FLUID) if len(SEG_PLAN[name]) > 5 else {}
+    fluid.pop("viscosity", None)
     case = os.path.join(tmp, "seg_" + name)
-    write_case(case, dt=dt, steps=nsteps, viscosity=visc, time_scheme=scheme, **CASES[base])
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, time_scheme=scheme, **fluid,
+               **CASES[base])
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
@@ -142,6 +149,14 @@ def make_seg_case(name, ref_bin, tmp):
     out["nsteps"] = np.int64(nsteps)
     out["viscosity"] = np.float64(visc)
     out["Pr"] = np.float64(0.9)
+    if fluid:
+        # constants in the names the oracle and the Python host read
+        out["P0"] = np.float64(fluid["P0"])
+        out["cp"] = np.float64(fluid["cp"])
+        out["cv"] = np.float64(fluid["cv"])
+        out["R"] = np.float64(fluid["cp"] - fluid["cv"])
+        out["gamma"] = np.float64(fluid["cp"] / fluid["cv"])
+        out["gravity"] = np.array([0.0, 0.0, fluid["gz"]])
     path = os.path.join(HERE, f"seg_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"seg_{name}: {n_int} interior nodes, {nsteps} steps -> {path} "

@@ -42,8 +42,11 @@ def test_mesh_equals_python_box_mesh(tmp_path, case, n):
     assert not np.any(d["fld_U"])
 
 
+FLUID = ("P0", "cp", "cv", "R", "gamma", "gravity")
+
+
 @pytest.mark.parametrize("fixture,case", [("seg_c1_2d", "c1_2d"), ("seg_g3_2", "g3_2"),
-                                          ("seg_c1_2d_visc", "c1_2d")])
+                                          ("seg_c1_2d_visc", "c1_2d"), ("seg_srtb", "c1_2d")])
 def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
     """The oracle (C library pow, as the binary) run on the driver's mesh and
     initial fields against the unmodified euler binary's fields after the
@@ -53,9 +56,14 @@ def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
     amplifies in the velocity."""
     g = load_golden(fixture)
     visc = float(g["viscosity"])
+    fluid = {}
+    if "P0" in g:   # the srtb example's constants
+        fluid = dict(P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]),
+                     gz=float(g["gravity"][2]))
     d = dump_case(make_case(tmp_path, case, dt=float(g["dt"]), steps=int(g["nsteps"]),
-                            viscosity=visc))
+                            viscosity=visc, **fluid))
     d["viscosity"] = visc
+    d.update({k: g[k] for k in FLUID if k in g})
     n = int(d["meta"][7])
     m = oracle.OracleMesh(d)
     oracle.set_pow(0)

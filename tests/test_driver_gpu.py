@@ -50,6 +50,35 @@ def test_segregated_run_matches_oracle(tmp_path, visc):
     assert np.all(g == np.array([0.0, 0.0, -9.81]))
 
 
+def test_srtb_example_run(tmp_path):
+    """The reference's srtb example as shipped (viscosity 1.5, gravity
+    -9.80606, the Fluid:: defaults for P0, cp, cv): the driver's run is the
+    oracle's bit for bit and follows the unmodified euler binary's fields."""
+    g = load_golden("seg_srtb")
+    steps = int(g["nsteps"])
+    d = make_case(tmp_path, "c1_2d", dt=float(g["dt"]), steps=steps, viscosity=1.5,
+                  P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]), gz=float(g["gravity"][2]))
+    a = dump_case(d)
+    a.update({k: g[k] for k in ("P0", "cp", "cv", "R", "gamma", "gravity")})
+    a["viscosity"] = 1.5
+    run_driver(d, "--print-every", "25")
+    out = fields(d, 1, ("rho", "U", "T"))
+    m = oracle.OracleMesh(a)
+    oracle.set_pow(1)
+    try:
+        rho, U, T = m.segregated(a["fld_rho"], a["fld_U"], a["fld_T"], float(g["dt"]), steps)
+    finally:
+        oracle.set_pow(0)
+    assert np.array_equal(out["rho"][:, 0], rho)
+    assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
+    assert np.array_equal(out["T"][:, 0], T)
+    n = int(a["meta"][7])
+    kd, kg = node_order(a["cC"], n), node_order(g["cC"], n)
+    assert rel_l2(out["rho"][kd, 0], g["fldN_rho"][kg]) < 1e-13
+    assert rel_l2(out["T"][kd, 0], g["fldN_T"][kg]) < 1e-10
+    assert rel_l2(out["U"][kd], g["fldN_U"].reshape(-1, 3)[kg]) < 2e-9
+
+
 def test_segregated_run_follows_euler_binary(tmp_path):
     """The driver's output files against the unmodified binary's (fixture),
     node by node through the coordinates: round-off of the geometry."""

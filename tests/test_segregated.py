@@ -20,7 +20,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc",
-                                  "seg_g3_2_visc_ab1"])
+                                  "seg_g3_2_visc_ab1", "seg_srtb"])
 def test_segregated_gpu_bitwise_vs_oracle(case):
     import nebulasem_gb300 as ng
     g = load_golden(case)

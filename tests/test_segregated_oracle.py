@@ -11,7 +11,7 @@ from conftest import load_golden
 
 
 @pytest.mark.parametrize("case", ["seg_c1_2d", "seg_g3_2", "seg_c1_2d_visc", "seg_g3_2_visc",
-                                  "seg_g3_2_visc_ab1"])
+                                  "seg_g3_2_visc_ab1", "seg_srtb"])
 def test_segregated_oracle_matches_reference_binary(case):
     g = load_golden(case)
     m = oracle.OracleMesh(g)
