@@ -413,12 +413,10 @@ nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params, n
     if (e) return cuda_fail(ctx, (cudaError_t)e, "volume kernel shared memory");
     if (ctx->dev.nu != 0.0) {
         /* viscous runs: gradient buffers shared by the coupled and the
-         * segregated schemes; the precision form has no viscous terms */
+         * segregated schemes (the precision form keeps its own FP32 ones) */
         if ((s = seg_alloc(ctx)) != NSEM_OK) return s;
         for (int c = 0; c < 12; c++) ctx->buf.G[c] = ctx->sbuf.G[c];
         for (int c = 0; c < 4; c++) ctx->buf.fF[c] = ctx->sbuf.fF[c];
-        ctx->mixed_ready = false;
-        ctx->err = "the precision form has no artificial viscosity (diffusion YES)";
     }
     return NSEM_OK;
 }

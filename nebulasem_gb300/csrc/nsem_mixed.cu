@@ -28,6 +28,13 @@
  * element the metric diagonal and the six neighbours, per z-layer the
  * background.  Discretisation identical to the plain form (same Rusanov
  * speed and jump, same symmetry ghost velocity, same weak form).
+ *
+ * Artificial viscosity (diffusion YES, euler.cpp:189-190, 232, 250): a
+ * gradient kernel per stage forms the strong-form DG gradients of U and
+ * theta of the stage state (gradf<true>, field.h:3327-3360: line derivatives
+ * plus the face terms (cds - own) lifted by J/w_end; zero gradient on the
+ * wall ghosts) into FP32 arrays, and the stage kernel subtracts mu grad U and
+ * (mu / Pr) grad theta, mu = rho nu, from the volume and face fluxes.
  */
 #include <cuda_runtime.h>
 
@@ -58,6 +65,11 @@ struct StageArgs {
     const float* J;            /* [3][n_elem]                             */
     const int32_t* layer;      /* [n_elem]                                */
     const float* Qg;           /* device copy of MixedTabs::Q (coalesced loads) */
+    const float* Dg;           /* derivative tables (gradient kernel)     */
+    const float* Gv[12];       /* viscous runs: grad U (XX..ZX), grad theta */
+    float* Gout[12];           /* gradient kernel output                   */
+    float nu, nu_pr;           /* viscous runs: nu, nu / Pr                */
+    float T0;                  /* background potential temperature        */
     const float* bg;           /* [layers][3][NP]: rho_ref, Theta_ref, p_ref */
     int64_t n_elem;
     float dt, gamma, gR, g[3];
@@ -192,8 +204,13 @@ __device__ __forceinline__ FaceSlot<NX, NY, NZ> face_slot(int t) {
 /* one kernel per stage (0: tendency only): the stage's own loads and update
  * only; registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the
  * stage that also carries the FP64 state (measured best on GB300) */
-template <int NX, int NY, int NZ, int STAGE>
-__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (STAGE == 1 || STAGE == 2) ? 8 : 7)
+/* tensor index of d_r U_c (XX,YY,ZZ,XY,YZ,XZ,YX,ZY,ZX) */
+__device__ __forceinline__ constexpr int tidx(int r, int c) {
+    return r == c ? r : (r == 0 ? (c == 1 ? 3 : 5) : r == 1 ? (c == 2 ? 4 : 6) : (c == 0 ? 8 : 7));
+}
+
+template <int NX, int NY, int NZ, int STAGE, bool VISC>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, VISC ? 6 : (STAGE == 1 || STAGE == 2) ? 8 : 7)
 k_mixed_stage(StageArgs a, MixedTabs tab) {
     using G = Geo<NX, NY, NZ>;
     constexpr int NP = G::NP;
@@ -233,12 +250,33 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
             for (int v = 0; v < 5; v++) u64[v] = __ldg(a.U[v] + n);
         }
     }
+    float gown[12];
+    if constexpr (VISC) {
+        if (t < NP) {
+            const int64_t n = e * NP + t;
+#pragma unroll
+            for (int c = 0; c < 12; c++) gown[c] = __ldg(a.Gv[c] + n);
+        }
+    }
     FaceSlot<NX, NY, NZ> fs;
     int32_t nb = -1;
     float oth[5], bgo[3];
+    float gfs[4] = {0, 0, 0, 0}, gfo[4] = {0, 0, 0, 0};   /* d_c U_dir (c = 0..2), d_dir theta */
     if (t < NFS) {
         fs = face_slot<NX, NY, NZ>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if constexpr (VISC) {
+            const int64_t ns = e * NP + fs.la;
+#pragma unroll
+            for (int c = 0; c < 3; c++) gfs[c] = __ldg(a.Gv[tidx(c, fs.dir)] + ns);
+            gfs[3] = __ldg(a.Gv[9 + fs.dir] + ns);
+            if (nb >= 0) {
+                const int64_t no = (int64_t)nb * NP + fs.lo;
+#pragma unroll
+                for (int c = 0; c < 3; c++) gfo[c] = __ldg(a.Gv[tidx(c, fs.dir)] + no);
+                gfo[3] = __ldg(a.Gv[9 + fs.dir] + no);
+            }
+        }
         if (nb >= 0) {
             const int64_t n = (int64_t)nb * NP + fs.lo;
 #pragma unroll
@@ -265,10 +303,20 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
         const float m[3] = {p.m0, p.m1, p.m2};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            sF4[d * NP + t] = make_float4(m[d], fmaf(m[0], u[d], d == 0 ? p.pp : 0.0f),
-                                          fmaf(m[1], u[d], d == 1 ? p.pp : 0.0f),
-                                          fmaf(m[2], u[d], d == 2 ? p.pp : 0.0f));
-            sF1[d * NP + t] = m[d] * p.th;
+            float4 f = make_float4(m[d], fmaf(m[0], u[d], d == 0 ? p.pp : 0.0f),
+                                   fmaf(m[1], u[d], d == 1 ? p.pp : 0.0f),
+                                   fmaf(m[2], u[d], d == 2 ? p.pp : 0.0f));
+            float f1 = m[d] * p.th;
+            if constexpr (VISC) {
+                /* - mu grad U (momentum r along d: d_r U_d), - (mu / Pr) d_d theta */
+                const float mu = p.rho * a.nu, mt = p.rho * a.nu_pr;
+                f.y = fmaf(-mu, gown[tidx(0, d)], f.y);
+                f.z = fmaf(-mu, gown[tidx(1, d)], f.z);
+                f.w = fmaf(-mu, gown[tidx(2, d)], f.w);
+                f1 = fmaf(-mt, gown[9 + d], f1);
+            }
+            sF4[d * NP + t] = f;
+            sF1[d * NP + t] = f1;
         }
     }
     __syncthreads();
@@ -326,7 +374,18 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
             fm[c] = wL * fmaf(mL[c], uL, pL) + wR * fmaf(mR[c], uR, pR);
             if (c == dir) fm[c] -= lam * (mR[c] - mL[c]);
         }
-        const float ft = (wL * (Lp.rho * uL * Lp.th) + wR * (Rp.rho * uR * Rp.th)) - lam * (Rp.tp - Lp.tp);
+        float ft = (wL * (Lp.rho * uL * Lp.th) + wR * (Rp.rho * uR * Rp.th)) - lam * (Rp.tp - Lp.tp);
+        if constexpr (VISC) {
+            /* average of the two sides' viscous fluxes; the wall ghost has zero
+             * gradient (and weight 1 on a wall, so no viscous wall flux) */
+            const float* gL = self_low ? gfs : gfo;
+            const float* gR = self_low ? gfo : gfs;
+            const float mL_ = Lp.rho * a.nu, mR_ = Rp.rho * a.nu;
+            const float tL_ = Lp.rho * a.nu_pr, tR_ = Rp.rho * a.nu_pr;
+#pragma unroll
+            for (int c = 0; c < 3; c++) fm[c] -= wL * (mL_ * gL[c]) + wR * (mR_ * gR[c]);
+            ft -= wL * (tL_ * gL[3]) + wR * (tR_ * gR[3]);
+        }
         const float fr_o = sg * fr, ft_o = sg * ft;
         fm[0] *= sg; fm[1] *= sg; fm[2] *= sg;
         sFF4[t] = make_float4(fr_o, fm[0], fm[1], fm[2]);
@@ -435,6 +494,173 @@ k_mixed_stage(StageArgs a, MixedTabs tab) {
     }
 }
 
+
+/* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
+ * field.h:3327-3360) for the viscous fluxes: per node
+ *   d_r q = J_r sum_m D_r[a_r][m] q_m  +  (J_r / w_end) (cds(q) - q)  on the
+ *   lower (-) / upper (+) face normal to r through the node,
+ * cds = (own + neighbour) / 2 inside, the ghost value on a wall (SYMMETRY
+ * velocity, NEUMANN theta: cds(theta) - theta = 0 there).  The state is the
+ * stage kernel's (FP32 shadow plus the previous increment for SIN >= 2).
+ * Output Gout[tidx(r, c)] = d_r U_c, Gout[9 + r] = d_r theta. */
+template <int NX, int NY, int NZ, int SIN>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK)
+k_mixed_grad(StageArgs a, MixedTabs tab) {
+    using G = Geo<NX, NY, NZ>;
+    constexpr int NP = G::NP;
+    constexpr int NFS = G::NFS;
+    constexpr bool has_din = SIN >= 2;
+    extern __shared__ float4 gsm4[];
+    float4* sV = gsm4;                                              /* [NP]  U, theta */
+    float4* sD = gsm4 + NP;                                         /* [NFS] cds - own */
+    float* sDg = reinterpret_cast<float*>(gsm4 + NP + NFS);        /* [3][MAXN^2] */
+    float* sJ = sDg + 3 * MAXN * MAXN;                              /* [3] */
+    const int t = threadIdx.x;
+    const int64_t e = blockIdx.x;
+
+    float own[5], bgs[1] = {0};
+    if (t < NP) {
+        const int64_t n = e * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) own[v] = __ldg(a.U32[v] + n);
+        if (has_din) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) own[v] += __ldg(a.Din[v] + n);
+        }
+        const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 3 * NP;
+        bgs[0] = __ldg(bg + t);
+    }
+    FaceSlot<NX, NY, NZ> fs;
+    int32_t nb = -1;
+    float oth[5], bgo[1];
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if (nb >= 0) {
+            const int64_t n = (int64_t)nb * NP + fs.lo;
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(a.U32[v] + n);
+            if (has_din) {
+#pragma unroll
+                for (int v = 0; v < 5; v++) oth[v] += __ldg(a.Din[v] + n);
+            }
+            const float* bg = a.bg + (int64_t)__ldg(a.layer + nb) * 3 * NP;
+            bgo[0] = __ldg(bg + fs.lo);
+        }
+    }
+    for (int q = t; q < 3 * MAXN * MAXN; q += blockDim.x) sDg[q] = __ldg(a.Dg + q);
+    if (t < 3) sJ[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
+
+    /* U = m / rho as make_prim forms it, and theta - T0 from the perturbation:
+     * the background has theta = T0 (Theta_ref = rho_ref T0), so
+     * theta - T0 = (Theta' - T0 rho') / rho -- the same gradient as theta
+     * without FP32 cancellation against T0 */
+    const float T0 = a.T0;
+    auto prim_ut = [T0](const float* s, float rref) {
+        const float inv = rcp_nr(rref + s[0]);
+        return make_float4(s[1] * inv, s[2] * inv, s[3] * inv, fmaf(-T0, s[0], s[4]) * inv);
+    };
+    if (t < NP) sV[t] = prim_ut(own, bgs[0]);
+    __syncthreads();
+
+    if (t < NFS) {
+        const float4 S = sV[fs.la];
+        float4 c;
+        if (nb >= 0) {
+            const float4 O = prim_ut(oth, bgo[0]);
+            c = make_float4(0.5f * S.x + 0.5f * O.x, 0.5f * S.y + 0.5f * O.y,
+                            0.5f * S.z + 0.5f * O.z, 0.5f * S.w + 0.5f * O.w);
+        } else {
+            /* wall ghost: SYMMETRY velocity, NEUMANN theta */
+            const int dir = fs.dir;
+            float r0 = dir == 0 ? 0.0f : S.x;
+            float r1 = dir == 1 ? 0.0f : S.y;
+            float r2 = dir == 2 ? 0.0f : S.z;
+            const float mr = safe_sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+            if (mr > 1e-7f) {
+                const float sc = safe_sqrt(S.x * S.x + S.y * S.y + S.z * S.z) / mr;
+                r0 *= sc; r1 *= sc; r2 *= sc;
+            }
+            c = make_float4(r0, r1, r2, S.w);
+        }
+        sD[t] = make_float4(c.x - S.x, c.y - S.y, c.z - S.z, c.w - S.w);
+    }
+    __syncthreads();
+
+    if (t >= NP) return;
+    const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+    float4 d[3];
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+#pragma unroll
+        for (int m = 0; m < NX; m++) {
+            const float q = sDg[i * MAXN + m];
+            const float4 v = sV[(m * NY + j) * NZ + k];
+            acc.x = fmaf(q, v.x, acc.x); acc.y = fmaf(q, v.y, acc.y);
+            acc.z = fmaf(q, v.z, acc.z); acc.w = fmaf(q, v.w, acc.w);
+        }
+        d[0] = acc;
+    }
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+        if (NY > 1) {
+#pragma unroll
+            for (int m = 0; m < NY; m++) {
+                const float q = sDg[MAXN * MAXN + j * MAXN + m];
+                const float4 v = sV[(i * NY + m) * NZ + k];
+                acc.x = fmaf(q, v.x, acc.x); acc.y = fmaf(q, v.y, acc.y);
+                acc.z = fmaf(q, v.z, acc.z); acc.w = fmaf(q, v.w, acc.w);
+            }
+        }
+        d[1] = acc;
+    }
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+#pragma unroll
+        for (int m = 0; m < NZ; m++) {
+            const float q = sDg[2 * MAXN * MAXN + k * MAXN + m];
+            const float4 v = sV[(i * NY + j) * NZ + m];
+            acc.x = fmaf(q, v.x, acc.x); acc.y = fmaf(q, v.y, acc.y);
+            acc.z = fmaf(q, v.z, acc.z); acc.w = fmaf(q, v.w, acc.w);
+        }
+        d[2] = acc;
+    }
+    const float Jd[3] = {sJ[0], sJ[1], sJ[2]};
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        d[r].x *= Jd[r]; d[r].y *= Jd[r]; d[r].z *= Jd[r]; d[r].w *= Jd[r];
+    }
+    /* face terms: + (J_r / w_end) (cds - own) on the upper face, - on the lower */
+    auto lift = [&](int r, int slot, float coef) {
+        const float4 f = sD[slot];
+        d[r].x = fmaf(coef, f.x, d[r].x); d[r].y = fmaf(coef, f.y, d[r].y);
+        d[r].z = fmaf(coef, f.z, d[r].z); d[r].w = fmaf(coef, f.w, d[r].w);
+    };
+    const float cx = Jd[0] * tab.lift[0], cy = Jd[1] * tab.lift[1], cz = Jd[2] * tab.lift[2];
+    if (i == 0) lift(0, G::OFF_X + j * NZ + k, -cx);
+    if (i == NX - 1) lift(0, G::OFF_X + G::NFX + j * NZ + k, cx);
+    if (NY > 1) {
+        if (j == 0) lift(1, G::OFF_Y + i * NZ + k, -cy);
+        if (j == NY - 1) lift(1, G::OFF_Y + G::NFY + i * NZ + k, cy);
+    }
+    if (k == 0) lift(2, G::OFF_Z + i * NY + j, -cz);
+    if (k == NZ - 1) lift(2, G::OFF_Z + G::NFZ + i * NY + j, cz);
+    const int64_t n = e * NP + t;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        a.Gout[tidx(r, 0)][n] = d[r].x;
+        a.Gout[tidx(r, 1)][n] = d[r].y;
+        a.Gout[tidx(r, 2)][n] = d[r].z;
+        a.Gout[9 + r][n] = d[r].w;
+    }
+}
+
+template <int NX, int NY, int NZ>
+constexpr size_t grad_smem() {
+    using G = Geo<NX, NY, NZ>;
+    return sizeof(float4) * (G::NP + G::NFS) + sizeof(float) * (3 * MAXN * MAXN + 4);
+}
+
 /* full <-> perturbation state (FP64): u' = u - (rho_ref, 0, 0, 0, rho_ref T0) */
 struct Ptr5 {
     double* p[5];
@@ -466,27 +692,56 @@ __global__ void k_convert(Ptr5 src, Ptr5 dst, FPtr5 shadow, const double* rho_re
     }
 }
 
-template <int NX, int NY, int NZ>
-int launch_stage(const StageArgs& a, const MixedTabs& t, cudaStream_t st) {
+template <int NX, int NY, int NZ, bool VISC>
+void launch_stage_v(const StageArgs& a, const MixedTabs& t, cudaStream_t st) {
     using G = Geo<NX, NY, NZ>;
+    const unsigned grid = (unsigned)a.n_elem;
     switch (a.stage) {
-        case 0: k_mixed_stage<NX, NY, NZ, 0><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
-        case 1: k_mixed_stage<NX, NY, NZ, 1><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
-        case 2: k_mixed_stage<NX, NY, NZ, 2><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
-        default: k_mixed_stage<NX, NY, NZ, 3><<<(unsigned)a.n_elem, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        case 0: k_mixed_stage<NX, NY, NZ, 0, VISC><<<grid, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        case 1: k_mixed_stage<NX, NY, NZ, 1, VISC><<<grid, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        case 2: k_mixed_stage<NX, NY, NZ, 2, VISC><<<grid, G::BLOCK, G::SMEM, st>>>(a, t); break;
+        default: k_mixed_stage<NX, NY, NZ, 3, VISC><<<grid, G::BLOCK, G::SMEM, st>>>(a, t); break;
     }
+}
+
+/* one stage; viscous runs first form the gradients of the stage state */
+template <int NX, int NY, int NZ>
+int launch_stage(const StageArgs& a, const MixedTabs& t, cudaStream_t st, bool visc) {
+    using G = Geo<NX, NY, NZ>;
+    if (!visc) {
+        launch_stage_v<NX, NY, NZ, false>(a, t, st);
+        return (int)cudaGetLastError();
+    }
+    const unsigned grid = (unsigned)a.n_elem;
+    const size_t gs = grad_smem<NX, NY, NZ>();
+    if (a.stage <= 1) k_mixed_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, gs, st>>>(a, t);
+    else k_mixed_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a, t);
+    int e = (int)cudaGetLastError();
+    if (e) return e;
+    launch_stage_v<NX, NY, NZ, true>(a, t, st);
     return (int)cudaGetLastError();
 }
 
 template <int NX, int NY, int NZ>
 int prepare_stage() {
     using G = Geo<NX, NY, NZ>;
-    if (G::SMEM <= 48 * 1024) return 0;
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    int e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0>, at, (int)G::SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1>, at, (int)G::SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2>, at, (int)G::SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3>, at, (int)G::SMEM);
+    int e = 0;
+    if (G::SMEM > 48 * 1024) {
+        e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true>, at, (int)G::SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true>, at, (int)G::SMEM);
+    }
+    constexpr size_t gs = grad_smem<NX, NY, NZ>();
+    if (!e && gs > 48 * 1024) {
+        e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 1>, at, (int)gs);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 2>, at, (int)gs);
+    }
     return e;
 }
 
@@ -500,12 +755,12 @@ int prepare(int nx, int ny, int nz) {
 }
 
 int dispatch_stage(int nx, int ny, int nz, const StageArgs& a, const MixedTabs& t,
-                   cudaStream_t st) {
-    if (nx == 5 && ny == 5 && nz == 5) return launch_stage<5, 5, 5>(a, t, st);
-    if (nx == 8 && ny == 8 && nz == 8) return launch_stage<8, 8, 8>(a, t, st);
-    if (nx == 4 && ny == 4 && nz == 4) return launch_stage<4, 4, 4>(a, t, st);
-    if (nx == 5 && ny == 1 && nz == 5) return launch_stage<5, 1, 5>(a, t, st);
-    if (nx == 4 && ny == 1 && nz == 4) return launch_stage<4, 1, 4>(a, t, st);
+                   cudaStream_t st, bool visc) {
+    if (nx == 5 && ny == 5 && nz == 5) return launch_stage<5, 5, 5>(a, t, st, visc);
+    if (nx == 8 && ny == 8 && nz == 8) return launch_stage<8, 8, 8>(a, t, st, visc);
+    if (nx == 4 && ny == 4 && nz == 4) return launch_stage<4, 4, 4>(a, t, st, visc);
+    if (nx == 5 && ny == 1 && nz == 5) return launch_stage<5, 1, 5>(a, t, st, visc);
+    if (nx == 4 && ny == 1 && nz == 4) return launch_stage<4, 1, 4>(a, t, st, visc);
     return (int)cudaErrorNotSupported;
 }
 
@@ -677,8 +932,14 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         return cudaMemcpy(*ptr, vec.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
     };
     const std::vector<float> qtab(&tabs->Q[0][0], &tabs->Q[0][0] + 3 * MAXN * MAXN);
+    /* D_d[a][m] = l_m'(x_a) = dpsi[a * n + m] for the gradient kernel */
+    std::vector<float> dtab(3 * MAXN * MAXN, 0.0f);
+    for (int d = 0; d < 3; d++)
+        for (int aa = 0; aa < npd[d]; aa++)
+            for (int mm = 0; mm < npd[d]; mm++)
+                dtab[d * MAXN * MAXN + aa * MAXN + mm] = (float)m->dpsi[d][aa * npd[d] + mm];
     if (!up(&mb->nbr, nbr) || !up(&mb->J, J) || !up(&mb->layer, layer) || !up(&mb->bg, bg) ||
-        !up(&mb->Qg, qtab)) {
+        !up(&mb->Qg, qtab) || !up(&mb->Dg, dtab)) {
         err = "precision form: device allocation failed";
         return NSEM_NO_MEMORY;
     }
@@ -693,6 +954,17 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             allocs->push_back(mb->U[s][v]);
             allocs->push_back(mb->U32[s][v]);
             allocs->push_back(mb->D[s][v]);
+        }
+    mb->visc = dev.nu != 0.0;
+    mb->nu = (float)dev.nu;
+    mb->nu_pr = (float)(dev.nu * dev.iPr);
+    if (mb->visc)
+        for (int c = 0; c < 12; c++) {
+            if (cudaMalloc((void**)&mb->Gv[c], n_int * sizeof(float)) != cudaSuccess) {
+                err = "precision form: device allocation failed";
+                return NSEM_NO_MEMORY;
+            }
+            allocs->push_back(mb->Gv[c]);
         }
     if (prepare(NX, NY, NZ) != 0) {
         err = "precision form: cannot reserve the kernel's shared memory";
@@ -725,6 +997,14 @@ StageArgs stage_args(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage
     a.J = mb->J;
     a.layer = mb->layer;
     a.Qg = mb->Qg;
+    a.Dg = mb->Dg;
+    for (int c = 0; c < 12; c++) {
+        a.Gv[c] = mb->Gv[c];
+        a.Gout[c] = mb->Gv[c];
+    }
+    a.nu = mb->nu;
+    a.nu_pr = mb->nu_pr;
+    a.T0 = (float)dev->T0;
     a.bg = mb->bg;
     a.n_elem = mb->n_elem;
     a.dt = (float)dt;
@@ -745,7 +1025,8 @@ StageArgs stage_args(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage
 int launch(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int stage, int cur, double dt,
            cudaStream_t st) {
     StageArgs a = stage_args(dev, mb, b, stage, cur, dt);
-    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, *(const MixedTabs*)mb->tabs, st);
+    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, *(const MixedTabs*)mb->tabs, st,
+                          mb->visc);
 }
 
 int grid_for(int64_t n) {

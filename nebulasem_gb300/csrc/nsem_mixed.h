@@ -27,6 +27,10 @@ struct NsemMixedBuf {
     int32_t* layer = nullptr;     /* [n_elem] background layer             */
     float* bg = nullptr;          /* [layers][3][NP] rho_ref, rho_ref T0, p_ref */
     float* Qg = nullptr;          /* device copy of the line-sum weights   */
+    float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a) */
+    float* Gv[12] = {};           /* viscous runs: grad U, grad theta of the stage state (FP32) */
+    bool visc = false;            /* artificial viscosity (diffusion YES) */
+    float nu = 0, nu_pr = 0;      /* nu and nu / Pr */
     void* tabs = nullptr;         /* host copy of the kernel tables        */
     size_t tabs_size = 0;
 };

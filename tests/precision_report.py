@@ -46,13 +46,15 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
 
 
-def run_gpu(name, dt, steps, adjoint_ckpt=0, with_oracle=False):
+def run_gpu(name, dt, steps, adjoint_ckpt=0, with_oracle=False, viscosity=0.0):
     import nebulasem_gb300 as ng
     from nebulasem_gb300.mesh import workload
     m, u0 = workload(name)
     n = int(m["meta"][7])
-    s = ng.Solver(m, dt=dt)
+    s = ng.Solver(m, dt=dt, viscosity=viscosity, Pr=0.9)
     out = dict(workload=name, dt=dt, steps=steps, nodes=n, dof=5 * n, input_sha256=input_digest(m, u0))
+    if viscosity:
+        out["viscosity"] = viscosity
     finals = {}
     for prec, tag in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
         # the second of two identical runs is timed (the first builds the graph)
@@ -122,6 +124,7 @@ def run_gpu(name, dt, steps, adjoint_ckpt=0, with_oracle=False):
             else:
                 err[v] = rel_l2(a, b)
         out["mixed_rel_l2_vs_fp64"] = err
+        out["mixed_momentum_vector_rel_l2"] = rel_l2(np.stack(got[1:4]), np.stack(ref[1:4]))
         th_ref = ref[4] / ref[0] - 300.0
         th_got = got[4] / got[0] - 300.0
         out["mixed_theta_prime_rel_l2"] = rel_l2(th_got, th_ref)
@@ -226,6 +229,8 @@ def main():
                     help="seg: the reference's own segregated update (FP64)")
     ap.add_argument("--with-oracle", action="store_true",
                     help="also run the oracle on this host and compare bit for bit")
+    ap.add_argument("--viscosity", type=float, default=0.0,
+                    help="artificial viscosity nu (diffusion YES, Pr 0.9) for both forms")
     ap.add_argument("--adjoint-ckpt", type=int, default=0,
                     help="also time the FP64 adjoint with checkpoints every k steps")
     a = ap.parse_args()
@@ -236,7 +241,7 @@ def main():
     elif a.oracle:
         r = run_oracle(a.workload, a.dt, a.steps)
     else:
-        r = run_gpu(a.workload, a.dt, a.steps, a.adjoint_ckpt, a.with_oracle)
+        r = run_gpu(a.workload, a.dt, a.steps, a.adjoint_ckpt, a.with_oracle, a.viscosity)
     print(json.dumps(r))
 
 
