@@ -174,6 +174,32 @@ void apply_initialiser(Tokens& t, const std::string& name, Field& f, const doubl
         }
         return;
     }
+    if (name == "gaussian-outside") {
+        /* perturbation inside a sphere, gaussian decay outside it */
+        read_vals(value);
+        read_vals(pert);
+        double center[3];
+        for (double& x : center) x = t.num();
+        const double radius = t.num(), radius2 = t.num();
+        for (long i = 0; i < n; i++) {
+            const double* x = cC + 3 * i;
+            const double d0 = x[0] - center[0], d1 = x[1] - center[1], d2 = x[2] - center[2];
+            double R = std::sqrt(d0 * d0 + (d1 * d1 + (d2 * d2 + 0.0)));
+            R = (R - radius) / radius2;
+            for (int c = 0; c < nc; c++) {
+                double val = value[c];
+                if (R <= 0) {
+                    val += pert[c];
+                } else {
+                    double v = std::exp(-R * R);
+                    if (equal_eps(v, 0.0)) v = 0;
+                    val += pert[c] * v;
+                }
+                f.values[i * nc + c] += val;
+            }
+        }
+        return;
+    }
     if (name == "hydrostatic") {
         read_vals(value);
         const double scale = t.num(), expon = t.num();

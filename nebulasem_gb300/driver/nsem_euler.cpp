@@ -169,6 +169,8 @@ int run(const Options& opt) {
     if (ctl.integer("general", "n_deferred", 0) != 0)
         throw std::runtime_error("n_deferred must be 0");
     if (write_interval < 1) throw std::runtime_error("write_interval must be >= 1");
+    if (ctl.integer("general", "amr_step", 0) != 0)
+        throw std::runtime_error("amr_step is set: adaptive mesh refinement is not supported");
     const std::string app = conv ? "convection" : "euler";
     if (upper(ctl.str(app, "problem_init", "NONE")) != "NONE")
         throw std::runtime_error("problem_init must be NONE");
