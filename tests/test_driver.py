@@ -113,6 +113,7 @@ def _edit(path, old, new):
     ("controls", "npy       0", "npy       4", "npy 0"),
     ("grid", "3{1 1 1}", "3{2 1 1}", "graded spacing"),
     ("grid", "sides   4{1 5 6 2} 4{0 4 7 3}", "sides   4{1 5 6 2}", "no patch"),
+    ("controls", "n_deferred                   0", "n_deferred 0\n    amr_step 1", "amr_step"),
 ])
 def test_refuses_what_the_gpu_path_does_not_model(tmp_path, file, old, new, msg):
     d = make_case(tmp_path, "c1_2d", dt=0.01, steps=10)
@@ -146,3 +147,32 @@ def test_block_with_permuted_vertices(tmp_path):
     d = dump_case(make_case(tmp_path, "c1_2d", dt=0.01, steps=10))
     assert list(d["meta"][:3]) == [5, 1, 5]
     assert int(d["meta"][5]) == 100
+
+
+def test_gaussian_outside_initialiser(tmp_path):
+    """`gaussian-outside value pert centre radius radius2` (field.h:1459-1480):
+    pert inside the sphere, pert exp(-R^2) outside with R = (r - radius) /
+    radius2, as the reference's ctbs example initialises theta'."""
+    d = make_case(tmp_path, "c1_2d", dt=0.01, steps=10)
+    with open(os.path.join(d, "T0.txt")) as f:
+        s = f.read()
+    s = s.replace("internal 1", "internal 2").replace(
+        "cosine 0 0.5    500 50 350   250 1000 250",
+        "gaussian-outside 150  0.5    500 50 300   150 50\n"
+        "    gaussian-outside 150 -0.15   560 50 640     0 50")
+    with open(os.path.join(d, "T0.txt"), "w") as f:
+        f.write(s)
+    a = dump_case(d)
+    n = int(a["meta"][7])
+    x = a["cC"].reshape(-1, 3)[:n]
+
+    def go(value, pert, c, r1, r2):
+        R = np.sqrt(((x - np.asarray(c)) ** 2).sum(axis=1))
+        R = (R - r1) / r2
+        v = np.exp(-R * R)
+        v[np.abs(v) <= 1e-7] = 0.0
+        return value + np.where(R <= 0, pert, pert * v)
+
+    want = 0.0 + go(150, 0.5, (500, 50, 300), 150, 50)
+    want = want + go(150, -0.15, (560, 50, 640), 0, 50)
+    assert np.abs(a["fld_T"] - want).max() <= 1e-12
