@@ -162,58 +162,87 @@ BlockDesc read_block_description(const std::string& path) {
     /* local axes: v0->v1 (i), v0->v3 (j), v0->v4 (k), meshApp.cpp sides */
     BlockDesc b;
     const int axis_vertex[3] = {1, 3, 4};
-    std::array<int, 3> gaxis{};
-    std::array<bool, 3> used{};
     double scale = 0;
     for (int m = 0; m < 8; m++)
         for (int d = 0; d < 3; d++) scale = std::fmax(scale, std::fabs(corner[m][d]));
     const double tol = 1e-9 * (scale > 0 ? scale : 1.0);
-    for (int a = 0; a < 3; a++) {
-        int g = -1;
-        for (int d = 0; d < 3; d++) {
-            const double e = corner[axis_vertex[a]][d] - corner[0][d];
-            if (std::fabs(e) > tol) {
-                if (g >= 0) throw std::runtime_error(path + ": block edges must be parallel to the axes");
-                g = d;
-            }
-        }
-        if (g < 0 || used[g]) throw std::runtime_error(path + ": degenerate block");
-        used[g] = true;
-        gaxis[a] = g;
-    }
-    /* all corners on the box spanned by the three edges (hex vertex order) */
+    std::array<std::array<double, 3>, 3> E{};
+    for (int a = 0; a < 3; a++)
+        for (int d = 0; d < 3; d++) E[a][d] = corner[axis_vertex[a]][d] - corner[0][d];
+    /* all corners on the parallelepiped spanned by the three edges (hex vertex order) */
     static const int bits[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                    {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
     for (int m = 0; m < 8; m++)
         for (int d = 0; d < 3; d++) {
             double want = corner[0][d];
             for (int a = 0; a < 3; a++)
-                if (bits[m][a]) want += corner[axis_vertex[a]][d] - corner[0][d];
+                if (bits[m][a]) want += E[a][d];
             if (std::fabs(corner[m][d] - want) > tol)
-                throw std::runtime_error(path + ": block is not an axis-aligned box");
+                throw std::runtime_error(path + ": block is not a parallelepiped "
+                                         "(only straight, parallel opposite edges are supported)");
         }
-    for (int d = 0; d < 3; d++) {
-        b.lo[d] = corner[0][d];
-        b.hi[d] = corner[0][d];
-        for (int m = 0; m < 8; m++) {
-            b.lo[d] = std::fmin(b.lo[d], corner[m][d]);
-            b.hi[d] = std::fmax(b.hi[d], corner[m][d]);
+    /* axis-aligned: each edge along one coordinate axis, distinct axes */
+    std::array<int, 3> gaxis{};
+    bool aligned = true;
+    {
+        std::array<bool, 3> used{};
+        for (int a = 0; a < 3 && aligned; a++) {
+            int g = -1, nz = 0;
+            for (int d = 0; d < 3; d++)
+                if (std::fabs(E[a][d]) > tol) { g = d; nz++; }
+            if (nz == 0) throw std::runtime_error(path + ": degenerate block");
+            if (nz != 1 || used[g]) aligned = false;
+            else { used[g] = true; gaxis[a] = g; }
         }
     }
-    for (int a = 0; a < 3; a++) b.n[gaxis[a]] = nloc[a];
-
-    /* patches -> box sides (a patch face selects the mesh faces in its plane,
-     * meshApp.cpp:206-230) */
     static const BoxSide sides[6] = {{2, -1}, {2, 1}, {1, -1}, {1, 1}, {0, -1}, {0, 1}};
+    /* the plane of side s: for an aligned block a coordinate; else a point and
+     * the normal of the face spanned by the two other edges */
+    auto on_side = [&](int s, const std::vector<int>& ids) -> bool {
+        const int ax = sides[s].axis;
+        if (aligned) {
+            const double v = sides[s].sign < 0 ? b.lo[ax] : b.hi[ax];
+            for (int id : ids)
+                if (std::fabs(kp[id][ax] - v) > tol) return false;
+            return true;
+        }
+        const auto& e1 = E[(ax + 1) % 3];
+        const auto& e2 = E[(ax + 2) % 3];
+        double nrm[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                         e1[0] * e2[1] - e1[1] * e2[0]};
+        const double mag = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+        double P[3];
+        for (int d = 0; d < 3; d++) P[d] = corner[0][d] + (sides[s].sign > 0 ? E[ax][d] : 0.0);
+        for (int id : ids) {
+            double dist = 0;
+            for (int d = 0; d < 3; d++) dist += (kp[id][d] - P[d]) * nrm[d];
+            if (std::fabs(dist) / mag > tol) return false;
+        }
+        return true;
+    };
+    if (aligned) {
+        for (int d = 0; d < 3; d++) {
+            b.lo[d] = corner[0][d];
+            b.hi[d] = corner[0][d];
+            for (int m = 0; m < 8; m++) {
+                b.lo[d] = std::fmin(b.lo[d], corner[m][d]);
+                b.hi[d] = std::fmax(b.hi[d], corner[m][d]);
+            }
+        }
+        for (int a = 0; a < 3; a++) b.n[gaxis[a]] = nloc[a];
+    } else {
+        b.affine = true;
+        b.origin = corner[0];
+        b.E = E;
+        for (int a = 0; a < 3; a++) b.n[a] = nloc[a];
+    }
+
+    /* patches -> block sides (a patch face selects the mesh faces in its plane,
+     * meshApp.cpp:206-230) */
     for (const auto& pf : patches) {
         int found = -1;
-        for (int s = 0; s < 6; s++) {
-            const int ax = sides[s].axis;
-            const double v = sides[s].sign < 0 ? b.lo[ax] : b.hi[ax];
-            bool on = true;
-            for (int id : pf.second) on = on && std::fabs(kp[id][ax] - v) <= tol;
-            if (on) found = s;
-        }
+        for (int s = 0; s < 6; s++)
+            if (on_side(s, pf.second)) found = s;
         if (found < 0)
             throw std::runtime_error(path + ": patch " + pf.first + " is not on the box boundary");
         if (!b.patch[found].empty() && b.patch[found] != pf.first)
@@ -354,6 +383,24 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     };
     const double area[3] = {hy * hz, hx * hz, hx * hy};
 
+    /* non-axis-aligned block: element edge vectors e_a = E_a / n_a and the
+     * area vectors e_{a+1} x e_{a+2} of the faces normal to axis a, along +e_a */
+    double ev[3][3] = {}, AV[3][3] = {};
+    if (b.affine) {
+        for (int a = 0; a < 3; a++)
+            for (int d = 0; d < 3; d++) ev[a][d] = b.E[a][d] / lim[a];
+        for (int a = 0; a < 3; a++) {
+            const double* e1 = ev[(a + 1) % 3];
+            const double* e2 = ev[(a + 2) % 3];
+            AV[a][0] = e1[1] * e2[2] - e1[2] * e2[1];
+            AV[a][1] = e1[2] * e2[0] - e1[0] * e2[2];
+            AV[a][2] = e1[0] * e2[1] - e1[1] * e2[0];
+            const double dot = AV[a][0] * ev[a][0] + AV[a][1] * ev[a][1] + AV[a][2] * ev[a][2];
+            if (dot < 0)
+                for (int d = 0; d < 3; d++) AV[a][d] = -AV[a][d];
+        }
+    }
+
     struct Group {
         std::vector<int64_t> own, nb, fid;
         int fo;
@@ -372,6 +419,8 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
         g.interior = true;
         g.nv[0] = g.nv[1] = g.nv[2] = 0.0;
         g.nv[axis] = area[axis];
+        if (b.affine)
+            for (int d = 0; d < 3; d++) g.nv[d] = AV[axis][d];
         for (int64_t e = 0; e < ne; e++)
             if (coord(e, axis) < lim[axis] - 1) {
                 g.own.push_back(e);
@@ -395,6 +444,8 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
         g.interior = false;
         g.nv[0] = g.nv[1] = g.nv[2] = 0.0;
         g.nv[axis] = sgn * area[axis];
+        if (b.affine)
+            for (int d = 0; d < 3; d++) g.nv[d] = sgn * AV[axis][d];
         for (int64_t e = 0; e < ne; e++)
             if (coord(e, axis) == (sgn < 0 ? 0 : lim[axis] - 1)) {
                 g.own.push_back(e);
@@ -414,11 +465,49 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     M.cC.assign((size_t)n_all * 3, 0.0);
     M.cV.assign((size_t)n_all, 0.0);
     M.Jinv.assign((size_t)n_all * 9, 0.0);
-    const double V = hx * hy * hz;
+    double V = hx * hy * hz;
     double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     J[XX] = NPX > 1 ? 2.0 / hx : 0.0;
     J[YY] = NPY > 1 ? 2.0 / hy : 0.0;
     J[ZZ] = NPZ > 1 ? 2.0 / hz : 0.0;
+    if (b.affine) {
+        /* V_e = |det(e_0, e_1, e_2)|; Jinv as dg.cpp:412-476 forms it from the
+         * Jacobian dx/dxi (columns e_a / 2 on the reference cube [-1, 1]^3, zero
+         * for a direction with one node): ((J^T J)^-1 J^T)^T with the collapsed
+         * diagonal set to 1 before and 0 after the inversion */
+        V = std::fabs(ev[0][0] * AV[0][0] + ev[0][1] * AV[0][1] + ev[0][2] * AV[0][2]);
+        double Jm[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) Jm[r][c] = npd[c] > 1 ? ev[c][r] / 2 : 0.0;
+        double Mm[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++)
+                Mm[r][c] = Jm[0][r] * Jm[0][c] + Jm[1][r] * Jm[1][c] + Jm[2][r] * Jm[2][c];
+        for (int a = 0; a < 3; a++)
+            if (npd[a] == 1) Mm[a][a] = 1;
+        const double det = Mm[0][0] * (Mm[1][1] * Mm[2][2] - Mm[1][2] * Mm[2][1]) -
+                           Mm[0][1] * (Mm[1][0] * Mm[2][2] - Mm[1][2] * Mm[2][0]) +
+                           Mm[0][2] * (Mm[1][0] * Mm[2][1] - Mm[1][1] * Mm[2][0]);
+        double Mi[3][3];
+        Mi[0][0] = (Mm[1][1] * Mm[2][2] - Mm[1][2] * Mm[2][1]) / det;
+        Mi[0][1] = (Mm[0][2] * Mm[2][1] - Mm[0][1] * Mm[2][2]) / det;
+        Mi[0][2] = (Mm[0][1] * Mm[1][2] - Mm[0][2] * Mm[1][1]) / det;
+        Mi[1][0] = (Mm[1][2] * Mm[2][0] - Mm[1][0] * Mm[2][2]) / det;
+        Mi[1][1] = (Mm[0][0] * Mm[2][2] - Mm[0][2] * Mm[2][0]) / det;
+        Mi[1][2] = (Mm[0][2] * Mm[1][0] - Mm[0][0] * Mm[1][2]) / det;
+        Mi[2][0] = (Mm[1][0] * Mm[2][1] - Mm[1][1] * Mm[2][0]) / det;
+        Mi[2][1] = (Mm[0][1] * Mm[2][0] - Mm[0][0] * Mm[2][1]) / det;
+        Mi[2][2] = (Mm[0][0] * Mm[1][1] - Mm[0][1] * Mm[1][0]) / det;
+        for (int a = 0; a < 3; a++)
+            if (npd[a] == 1) Mi[a][a] = 0;
+        /* P = Mi J^T (3 x 3), Jinv = P^T: Jinv[r][c] = P[c][r] */
+        double P[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++)
+                P[r][c] = Mi[r][0] * Jm[c][0] + Mi[r][1] * Jm[c][1] + Mi[r][2] * Jm[c][2];
+        const int order[9][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {0, 2}, {1, 0}, {2, 1}, {2, 0}};
+        for (int q = 0; q < 9; q++) J[q] = P[order[q][1]][order[q][0]];
+    }
     for (int64_t e = 0; e < ne; e++) {
         const int ix = coord(e, 0), iy = coord(e, 1), iz = coord(e, 2);
         for (int li = 0; li < NPX; li++)
@@ -428,9 +517,15 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
                     const int64_t n = e * NP + t;
                     const double rx = (M.xgl[0][li] + 1) / 2, ry = (M.xgl[1][lj] + 1) / 2,
                                  rz = (M.xgl[2][lk] + 1) / 2;
-                    M.cC[3 * n + 0] = b.lo[0] + (ix * hx + rx * hx);
-                    M.cC[3 * n + 1] = b.lo[1] + (iy * hy + ry * hy);
-                    M.cC[3 * n + 2] = b.lo[2] + (iz * hz + rz * hz);
+                    if (b.affine) {
+                        for (int d = 0; d < 3; d++)
+                            M.cC[3 * n + d] = b.origin[d] + ((ix + rx) * ev[0][d] +
+                                                             ((iy + ry) * ev[1][d] + (iz + rz) * ev[2][d]));
+                    } else {
+                        M.cC[3 * n + 0] = b.lo[0] + (ix * hx + rx * hx);
+                        M.cC[3 * n + 1] = b.lo[1] + (iy * hy + ry * hy);
+                        M.cC[3 * n + 2] = b.lo[2] + (iz * hz + rz * hz);
+                    }
                     M.cV[n] = V * (wg0[li] * wg1[lj] * wg2[lk] / 8);
                     for (int c = 0; c < 9; c++) M.Jinv[9 * n + c] = J[c];
                 }

@@ -4,11 +4,18 @@
  * Input: the block description the reference's mesh app reads
  * (apps/mesh/meshApp.cpp:70-230: key points, hex blocks `8{...} <grading>
  * 3{nx ny nz} ...`, named boundary patches `name 4{a b c d}...`, `default
- * name`).  Supported: one hexahedral block whose edges are parallel to the
- * coordinate axes, uniform spacing (`linear`, or `wall`/`geometric` with all
- * factors 1), no curved edges; a `delete` patch on the two y faces of a block
- * one element thick makes the case two-dimensional (npy 0).  Anything else is
- * rejected with a message: the driver has no CPU path to fall back to.
+ * name`).  Supported: one hexahedral block with straight edges forming a
+ * parallelepiped (axis-aligned, or rotated / sheared as the reference's
+ * srtb-inclined example), uniform spacing (`linear`, or `wall`/`geometric`
+ * with all factors 1); a `delete` patch on the two faces of the block's second
+ * axis, one element thick, makes the case two-dimensional (npy 0).  Anything
+ * else (curved edges, several blocks, grading) is rejected with a message:
+ * the driver has no CPU path to fall back to.
+ *
+ * Metric of a non-axis-aligned block: the reference's pseudo-inverse
+ * (dg.cpp:412-476) Jinv = ((J^T J)^-1 J^T)^T of the constant element Jacobian
+ * J = [e_0/2, e_1/2, e_2/2] (a collapsed direction's column and inverse
+ * diagonal zero), node weights V_e w_i w_j w_k / 8, face area vectors e_b x e_c.
  *
  * Output: the arrays of the reference's Mesh:: / DG:: layout for that box
  * (the nsem_mesh_desc of the C ABI), built with the reference's conventions:
@@ -38,11 +45,19 @@ struct BoxSide {
 };
 
 struct BlockDesc {
-    std::array<double, 3> lo{}, hi{};      /* box extent */
-    std::array<int, 3> n{};                /* elements per global axis */
-    /* patch name of each side, in the order z-, z+, y-, y+, x-, x+ ("" if deleted) */
+    std::array<double, 3> lo{}, hi{};      /* box extent (axis-aligned blocks) */
+    std::array<int, 3> n{};                /* elements per axis: global x, y, z for an
+                                              axis-aligned block, else the block's own
+                                              axes v0->v1, v0->v3, v0->v4 */
+    /* patch name of each side, in the order z-, z+, y-, y+, x-, x+ of those axes
+     * ("" if deleted) */
     std::array<std::string, 6> patch;
     bool two_d = false;                    /* y faces deleted, one element in y */
+    /* a block whose edges are not along the coordinate axes (rotated or
+     * sheared parallelepiped): x = origin + sum_a xi_a E[a], xi_a in [0, 1] */
+    bool affine = false;
+    std::array<double, 3> origin{};
+    std::array<std::array<double, 3>, 3> E{};
 };
 
 /* parse the block description file; throws std::runtime_error */

@@ -8,7 +8,7 @@ import pytest
 
 import oracle
 from conftest import load_golden, rel_l2
-from driver_util import dump_case, make_case, node_order, run_driver
+from driver_util import dump_case, make_case, node_order, rotate_case_z, run_driver
 from nebulasem_gb300.fields import read_field
 
 pytestmark = pytest.mark.gpu
@@ -183,3 +183,27 @@ def test_restart_from_written_fields(tmp_path):
     assert np.array_equal(out["rho"][:, 0], rho)
     assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
     assert np.array_equal(out["T"][:, 0], T)
+
+
+def test_inclined_block_run(tmp_path):
+    """A block rotated by 30 degrees (full, non-diagonal metric): the FP64
+    forms through the driver are the oracle's bit for bit; the precision form,
+    built for axis-aligned elements, is refused with a message."""
+    steps = 20
+    d = make_case(tmp_path, "c1_2d", dt=0.005, steps=steps, viscosity=1.5)
+    rotate_case_z(d, 30.0)
+    a = dump_case(d)
+    a["viscosity"] = 1.5
+    run_driver(d, "--print-every", "10")
+    out = fields(d, 1, ("rho", "U", "T"))
+    m = oracle.OracleMesh(a)
+    oracle.set_pow(1)
+    try:
+        rho, U, T = m.segregated(a["fld_rho"], a["fld_U"], a["fld_T"], 0.005, steps)
+    finally:
+        oracle.set_pow(0)
+    assert np.array_equal(out["rho"][:, 0], rho)
+    assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
+    assert np.array_equal(out["T"][:, 0], T)
+    r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
+    assert r.returncode == 1 and "axis-aligned" in r.stderr, r.stderr
