@@ -155,8 +155,80 @@ inline void sym_vec(const T* p, const double* n, T* out) {
     out[0] = r[0] * s; out[1] = r[1] * s; out[2] = r[2] * s;
 }
 
+/* strong-form DG gradient of ncomp (1 or 3) components per node, as
+ * nsem_oracle.c grad_strong(): face terms fN (x) (cds(p) - p) in the cell's face
+ * order, the volume derivative along the node's three lines, divided by cV;
+ * G[r][c] = d_r p_c (XX..ZX) for vectors, interior nodes only */
+template <typename T>
+void grad_strong_t(const nsem_oracle_mesh* m, int ncomp, const std::vector<T>& p, std::vector<T>& G) {
+    const int NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
+    const int64_t n_all = m->n_all;
+    const int w = ncomp == 1 ? 3 : 9;
+    G.assign((size_t)w * n_all, T(0.0));
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m->n_elem; e++) {
+        const int64_t base = e * NP;
+        for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++)
+            for (int nn = 0; nn < NPF; nn++) {
+                const int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
+                const uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+                const double fi = m->fI[k], fo = 1 - fi;
+                const double* n = m->fN + 3 * k;
+                const bool mine = c1 >= base && c1 < base + NP;
+                const uint32_t own = mine ? c1 : c2;
+                T d[3];
+                for (int c = 0; c < ncomp; c++)
+                    d[c] = (p[(size_t)ncomp * c1 + c] * fi + p[(size_t)ncomp * c2 + c] * fo) -
+                           p[(size_t)ncomp * own + c];
+                T* g = &G[(size_t)w * own];
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < ncomp; c++) {
+                        const int idx = ncomp == 1 ? r : (r == c) ? r : (r == 0 && c == 1) ? XY
+                                      : (r == 1 && c == 2) ? YZ : (r == 0 && c == 2) ? XZ
+                                      : (r == 1 && c == 0) ? YX : (r == 2 && c == 1) ? ZY : ZX;
+                        const T t = n[r] * d[c];
+                        g[idx] = mine ? g[idx] + t : g[idx] - t;
+                    }
+            }
+        for (int ii = 0; ii < NPX; ii++)
+        for (int jj = 0; jj < NPY; jj++)
+        for (int kk = 0; kk < NPZ; kk++) {
+            const int64_t a = base + (int64_t)ii * NPY * NPZ + jj * NPZ + kk;
+            double Jin[9];
+            for (int c = 0; c < 9; c++) Jin[c] = m->Jinv[9 * a + c] * m->cV[a];
+            T* g = &G[(size_t)w * a];
+            for (int pass = 0; pass < 3; pass++) {
+                const int lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
+                for (int q = 0; q < lim; q++) {
+                    int im = ii, jm = jj, km = kk;
+                    if (pass == 0) im = q;
+                    else if (pass == 1) { if (q == jj) continue; jm = q; }
+                    else { if (q == kk) continue; km = q; }
+                    const int64_t b = base + (int64_t)im * NPY * NPZ + jm * NPZ + km;
+                    double dv[3], dj[3];
+                    dv[0] = m->dpsi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[1] = m->psi[0][ii * NPX + im] * m->dpsi[1][jj * NPY + jm] * m->psi[2][kk * NPZ + km];
+                    dv[2] = m->psi[0][ii * NPX + im] * m->psi[1][jj * NPY + jm] * m->dpsi[2][kk * NPZ + km];
+                    dj[0] = Jin[XX] * dv[0] + Jin[XY] * dv[1] + Jin[XZ] * dv[2];
+                    dj[1] = Jin[YX] * dv[0] + Jin[YY] * dv[1] + Jin[YZ] * dv[2];
+                    dj[2] = Jin[ZX] * dv[0] + Jin[ZY] * dv[1] + Jin[ZZ] * dv[2];
+                    for (int r = 0; r < 3; r++)
+                        for (int c = 0; c < ncomp; c++) {
+                            const int idx = ncomp == 1 ? r : (r == c) ? r : (r == 0 && c == 1) ? XY
+                                          : (r == 1 && c == 2) ? YZ : (r == 0 && c == 2) ? XZ
+                                          : (r == 1 && c == 0) ? YX : (r == 2 && c == 1) ? ZY : ZX;
+                            g[idx] = g[idx] + dj[r] * p[(size_t)ncomp * b + c];
+                        }
+                }
+            }
+            for (int c = 0; c < w; c++) g[c] = g[c] / m->cV[a];
+        }
+    }
+}
+
 /* tendency L = -Su/cV on interior nodes, same operator chain as
- * nsem_oracle.c residual() */
+ * nsem_oracle.c residual() (with its artificial viscosity when nu != 0) */
 template <typename T>
 void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>* L) {
     const int NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
@@ -185,6 +257,17 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n_all; i++) p[i] = P0 * pow_(((rho[i] * Th[i]) * R) / P0, gam) - m->p_ref[i];
 
+    /* artificial viscosity: mu = rho nu, gradients of U and theta (zero on ghosts) */
+    const bool visc = m->nu != 0.0;
+    const double iPr = visc ? 1 / m->Pr : 0.0;
+    std::vector<T> mu, GU, GT;
+    if (visc) {
+        mu.resize(n_all);
+        for (int64_t i = 0; i < n_all; i++) mu[i] = rho[i] * m->nu;
+        grad_strong_t(m, 3, U, GU);
+        grad_strong_t(m, 1, Th, GT);
+    }
+
     std::vector<T> dr(n_slot), dm(3 * n_slot), dt_(n_slot);
 #pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < n_slot; k++) {
@@ -211,6 +294,13 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
             outer(Fc1, U1, A);
             outer(Fc2, U2, B);
             for (int c = 0; c < 3; c++) { A[c] = A[c] + p1; B[c] = B[c] + p2; }
+            if (visc) {
+                const bool g1 = c1 < (uint32_t)n_int, g2 = c2 < (uint32_t)n_int;
+                for (int c = 0; c < 9; c++) {
+                    A[c] = A[c] - mu[c1] * (g1 ? GU[9 * (size_t)c1 + c] : T(0.0));
+                    B[c] = B[c] - mu[c2] * (g2 ? GU[9 * (size_t)c2 + c] : T(0.0));
+                }
+            }
             T dq[3];
             for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
             for (int r = 0; r < 3; r++)
@@ -226,7 +316,14 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
         {
             T F[3];
             const T jump = lam * (r2 * T2 - r1 * T1);
-            for (int c = 0; c < 3; c++) F[c] = (U1[c] * r1 * T1 * fi + U2[c] * r2 * T2 * fo) - jump * en[c];
+            for (int c = 0; c < 3; c++) {
+                T a = U1[c] * r1 * T1, b = U2[c] * r2 * T2;
+                if (visc) {
+                    a = a - (mu[c1] * iPr) * (c1 < (uint32_t)n_int ? GT[3 * (size_t)c1 + c] : T(0.0));
+                    b = b - (mu[c2] * iPr) * (c2 < (uint32_t)n_int ? GT[3 * (size_t)c2 + c] : T(0.0));
+                }
+                F[c] = (a * fi + b * fo) - jump * en[c];
+            }
             dt_[k] = vdotd(F, n);
         }
     }
@@ -261,6 +358,10 @@ void tendency(const nsem_oracle_mesh* m, const std::vector<T>* u, std::vector<T>
             outer(Fc, Ub, fm);
             for (int c = 0; c < 3; c++) fm[c] = fm[c] + p[b];
             T ft[3] = {Fc[0] * Th[b], Fc[1] * Th[b], Fc[2] * Th[b]};
+            if (visc) {
+                for (int c = 0; c < 9; c++) fm[c] = fm[c] - mu[b] * GU[9 * b + c];
+                for (int c = 0; c < 3; c++) ft[c] = ft[c] - (mu[b] * iPr) * GT[3 * b + c];
+            }
             for (int pass = 0; pass < 3; pass++) {
                 const int lim = pass == 0 ? NPX : pass == 1 ? NPY : NPZ;
                 for (int q = 0; q < lim; q++) {

@@ -1,8 +1,8 @@
 """The CPU tangent-linear oracle (oracle/nsem_tlm.cpp) against the plain
-oracle: its value part reproduces the oracle bit for bit, several directions in
-one pass equal one pass per direction, and its directional derivatives match
-central differences (eps = 1e-6) of the oracle's SSP-RK3 along 8 seeded
-Gaussian directions."""
+oracle, without and with artificial viscosity: its value part reproduces the
+oracle bit for bit, several directions in one pass equal one pass per
+direction, and its directional derivatives match central differences
+(eps = 1e-6) of the oracle's SSP-RK3 along 8 seeded Gaussian directions."""
 import numpy as np
 import pytest
 
@@ -10,9 +10,10 @@ import oracle
 from conftest import golden_state, load_golden
 
 
-@pytest.fixture(scope="module")
-def case():
-    g = load_golden("g3_2")
+@pytest.fixture(scope="module", params=["g3_2", "g3_2_visc"])
+def case(request):
+    """inviscid, and with the artificial viscosity of diffusion YES"""
+    g = load_golden(request.param)
     return oracle.OracleMesh(g), golden_state(g, "up")
 
 
