@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "nsem_adjoint.h"
+#include "nsem_seg.h"
 #include "nsem_gather.cuh"
 
 namespace {
@@ -365,7 +366,71 @@ struct FaceTanArgs {
     const double* S[5];
     const double* dS[5];
     double* dd[5];           /* per slot: tangent of the lifted face flux */
+    const double* G[12];     /* viscous runs: grad U, grad theta of the state (else null) */
+    const double* dG[12];    /* and their tangents */
 };
+
+__device__ __forceinline__ constexpr int tix(int r, int c) {
+    return r == c ? r : (r == 0 ? (c == 1 ? XY : XZ) : r == 1 ? (c == 2 ? YZ : YX) : (c == 0 ? ZX : ZY));
+}
+
+/* U and theta of the state and their tangents, per node (gradient inputs) */
+struct PrimTanArgs {
+    const double* S[5];
+    const double* dS[5];
+    double* pU[4];
+    double* dpU[4];
+};
+
+__global__ void __launch_bounds__(256) k_tan_prims(const NsemDev m, PrimTanArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_int) return;
+    const double r = a.S[0][i];
+    const double U[3] = {a.S[1][i] / r, a.S[2][i] / r, a.S[3][i] / r};
+    const double T = a.S[4][i] / r;
+    const double dr = a.dS[0][i], inv = 1.0 / r;
+    for (int c = 0; c < 3; c++) {
+        a.pU[c][i] = U[c];
+        a.dpU[c][i] = (a.dS[1 + c][i] - U[c] * dr) * inv;
+    }
+    a.pU[3][i] = T;
+    a.dpU[3][i] = (a.dS[4][i] - T * dr) * inv;
+}
+
+/* tangent of the gradients' face values: d cds(U, theta) per slot, the wall
+ * ghost linearised as the forward ghost (SYMMETRY projection, NEUMANN copy) */
+struct GradFaceTanArgs {
+    const double* pU[4];
+    const double* dpU[4];
+    double* dfF[4];
+};
+
+__global__ void __launch_bounds__(256) k_tan_grad_face(const NsemDev m, GradFaceTanArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double dU1[3] = {a.dpU[0][c1], a.dpU[1][c1], a.dpU[2][c1]};
+    double dU2[3], dT2;
+    if (c2 >= 0) {
+        for (int c = 0; c < 3; c++) dU2[c] = a.dpU[c][c2];
+        dT2 = a.dpU[3][c2];
+    } else {
+        dT2 = a.dpU[3][c1];
+        if (m.bc[k] == 2) {
+            const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+            const double U1[3] = {a.pU[0][c1], a.pU[1][c1], a.pU[2][c1]};
+            double U2[3], rsym[3], magR, magP;
+            bool scaled;
+            sym_fwd(U1, en, U2, rsym, magR, magP, scaled);
+            sym_jvp(U1, en, rsym, magR, magP, scaled, dU1, dU2);
+        } else {
+            for (int c = 0; c < 3; c++) dU2[c] = dU1[c];
+        }
+    }
+    for (int c = 0; c < 3; c++) a.dfF[c][k] = dU1[c] * fi + dU2[c] * fo;
+    a.dfF[3][k] = a.dpU[3][c1] * fi + dT2 * fo;
+}
 
 __global__ void __launch_bounds__(128) k_tan_face(const NsemDev m, FaceTanArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -412,13 +477,23 @@ __global__ void __launch_bounds__(128) k_tan_face(const NsemDev m, FaceTanArgs a
         for (int c = 0; c < 3; c++)
             dd0 += (dFc1[c] * fi + dFc2[c] * fo - (dlam * jump + lam * djump) * en[c]) * n[c];
     }
+    /* viscous flux tangents: - d(mu grad U) = - (dmu G + mu dG), mu = rho nu,
+     * zero gradient on a wall ghost */
+    const bool visc = a.G[0] != nullptr;
+    const bool g2 = c2 >= 0;
+    const double mu1 = P1.r * m.nu, mu2 = P2.r * m.nu, dmu1 = d1.r * m.nu, dmu2 = d2.r * m.nu;
     /* momentum: F[r][c] = (Fc U + p' I)_avg[r][c] - lam (Fc_N - Fc_O)[c] en[r] */
     double ddm[3];
     for (int r = 0; r < 3; r++) {
         double acc = 0;
         for (int c = 0; c < 3; c++) {
-            const double dA = dFc1[r] * P1.U[c] + Fc1[r] * d1.U[c] + (r == c ? d1.p : 0.0);
-            const double dB = dFc2[r] * P2.U[c] + Fc2[r] * d2.U[c] + (r == c ? d2.p : 0.0);
+            double dA = dFc1[r] * P1.U[c] + Fc1[r] * d1.U[c] + (r == c ? d1.p : 0.0);
+            double dB = dFc2[r] * P2.U[c] + Fc2[r] * d2.U[c] + (r == c ? d2.p : 0.0);
+            if (visc) {
+                const int q = tix(r, c);
+                dA -= dmu1 * a.G[q][c1] + mu1 * a.dG[q][c1];
+                if (g2) dB -= dmu2 * a.G[q][c2] + mu2 * a.dG[q][c2];
+            }
             const double ddq = (dFc2[c] - dFc1[c]) * lam + (Fc2[c] - Fc1[c]) * dlam;
             acc += (dA * fi + dB * fo - ddq * en[r]) * n[c];
         }
@@ -430,8 +505,12 @@ __global__ void __launch_bounds__(128) k_tan_face(const NsemDev m, FaceTanArgs a
         const double e1 = P1.r * P1.T, e2 = P2.r * P2.T;
         const double de1 = d1.r * P1.T + P1.r * d1.T, de2 = d2.r * P2.T + P2.r * d2.T;
         for (int c = 0; c < 3; c++) {
-            const double f1 = dFc1[c] * P1.T + Fc1[c] * d1.T;
-            const double f2 = dFc2[c] * P2.T + Fc2[c] * d2.T;
+            double f1 = dFc1[c] * P1.T + Fc1[c] * d1.T;
+            double f2 = dFc2[c] * P2.T + Fc2[c] * d2.T;
+            if (visc) {
+                f1 -= m.iPr * (dmu1 * a.G[9 + c][c1] + mu1 * a.dG[9 + c][c1]);
+                if (g2) f2 -= m.iPr * (dmu2 * a.G[9 + c][c2] + mu2 * a.dG[9 + c][c2]);
+            }
             dd4 += (f1 * fi + f2 * fo - (dlam * (e2 - e1) + lam * (de2 - de1)) * en[c]) * n[c];
         }
     }
@@ -444,6 +523,8 @@ struct VolTanArgs {
     const double* dS[5];
     const double* dd[5];
     double* out[5];          /* J_L(v) dv */
+    const double* G[12];     /* viscous runs (else null) */
+    const double* dG[12];
 };
 
 /* shared layout per node: dfr[3] dfm[9] dft[3] jin[9] */
@@ -477,6 +558,12 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
                 my[3 + idx] = dFc[r] * P.U[c] + Fc[r] * d.U[c] + (r == c ? d.p : 0.0);
             }
         for (int c = 0; c < 3; c++) my[12 + c] = dFc[c] * P.T + Fc[c] * d.T;
+        if (a.G[0]) {
+            const double mu = P.r * m.nu, dmu = d.r * m.nu;
+            for (int c = 0; c < 9; c++) my[3 + c] -= dmu * a.G[c][node] + mu * a.dG[c][node];
+            for (int c = 0; c < 3; c++)
+                my[12 + c] -= m.iPr * (dmu * a.G[9 + c][node] + mu * a.dG[9 + c][node]);
+        }
         for (int c = 0; c < 9; c++) my[15 + c] = m.jin[(int64_t)c * m.n_int + node];
     }
     __syncthreads();
@@ -555,11 +642,30 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
 int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
                  const double* const* dS, double* const* out, NsemAdjBuf* ab, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
-    FaceTanArgs fa;
+    FaceTanArgs fa{};
+    VolTanArgs va{};
+    if (ab->visc) {
+        /* gradients of the state and their tangents (the gradient is linear
+         * in its node and face values) */
+        PrimTanArgs pa;
+        for (int v = 0; v < 5; v++) { pa.S[v] = S[v]; pa.dS[v] = dS[v]; }
+        for (int c = 0; c < 4; c++) { pa.pU[c] = ab->pU[c]; pa.dpU[c] = ab->dpU[c]; }
+        k_tan_prims<<<(unsigned)((m->n_int + 255) / 256), 256, 0, st>>>(*m, pa);
+        int e = nsem_grad_ut(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF, stream);
+        if (e) return e;
+        GradFaceTanArgs ga;
+        for (int c = 0; c < 4; c++) { ga.pU[c] = ab->pU[c]; ga.dpU[c] = ab->dpU[c]; ga.dfF[c] = ab->dfF[c]; }
+        k_tan_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
+        e = nsem_grad_vol(m, t, ab->dpU, ab->dpU[3], ab->dGv, ab->dfF, stream);
+        if (e) return e;
+        for (int c = 0; c < 12; c++) {
+            fa.G[c] = va.G[c] = ab->Gv[c];
+            fa.dG[c] = va.dG[c] = ab->dGv[c];
+        }
+    }
     for (int v = 0; v < 5; v++) { fa.S[v] = S[v]; fa.dS[v] = dS[v]; fa.dd[v] = ab->adjO[v]; }
     const int64_t fb = (m->n_slot + 127) / 128;
     k_tan_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
-    VolTanArgs va;
     for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.dS[v] = dS[v]; va.dd[v] = ab->adjO[v]; va.out[v] = out[v]; }
     const int threads = ((m->np + 31) / 32) * 32;
     const size_t smem = ((size_t)m->np * TAN_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);

@@ -20,6 +20,16 @@ struct NsemAdjBuf {
     double* ckpt = nullptr; /* [n_ckpt][5][n_int] states every k steps     */
     double* seg = nullptr;  /* [k][3][5][n_int] u^n, u1, u2 of a segment   */
     int64_t seg_slots = 0;  /* state slots allocated in seg                 */
+    /* artificial viscosity (nu != 0): per node U, theta of the state and their
+     * tangents / adjoints, gradients (9 + 3) and their tangents / adjoints;
+     * per slot cds(U, theta) and its tangent, face adjoints */
+    bool visc = false;
+    double* pU[4] = {};
+    double* dpU[4] = {};
+    double* Gv[12] = {};
+    double* dGv[12] = {};
+    double* fF[4] = {};
+    double* dfF[4] = {};
     int nsteps = 0, every = 0, n_ckpt = 0;
     bool ready = false;
 };

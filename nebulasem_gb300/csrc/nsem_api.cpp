@@ -633,6 +633,20 @@ static nsem_status adj_alloc(nsem_ctx* ctx) {
         if ((s = dalloc(ctx, &A.g[v], n)) != NSEM_OK) return s;
         if ((s = dalloc(ctx, &A.fin[v], n)) != NSEM_OK) return s;
     }
+    if (ctx->dev.nu != 0.0) {
+        const size_t n = (size_t)ctx->dev.n_int, ns = (size_t)ctx->dev.n_slot;
+        for (int c = 0; c < 4; c++) {
+            if ((s = dalloc(ctx, &A.pU[c], n)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.dpU[c], n)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.fF[c], ns)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.dfF[c], ns)) != NSEM_OK) return s;
+        }
+        for (int c = 0; c < 12; c++) {
+            if ((s = dalloc(ctx, &A.Gv[c], n)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.dGv[c], n)) != NSEM_OK) return s;
+        }
+        A.visc = true;
+    }
     int e = nsem_adj_prepare(&ctx->dev);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "adjoint shared memory");
     A.ready = true;
@@ -694,8 +708,6 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
 
 extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
     if (!ctx) return NSEM_BAD_ARG;
-    if (ctx->dev.nu != 0.0)
-        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
     for (int v = 0; v < 5; v++)
         if (!dv[v] || !Ld[v]) return fail(ctx, NSEM_BAD_ARG, "dv[v] or Ld[v] is NULL");
@@ -717,8 +729,6 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
 extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
                                 double* const du_final[5], double* ms_tlm) {
     if (!ctx) return NSEM_BAD_ARG;
-    if (ctx->dev.nu != 0.0)
-        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
     if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
     for (int v = 0; v < 5; v++)

@@ -645,6 +645,18 @@ int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, 
     return (int)cudaGetLastError();
 }
 
+int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
+                  double* const* G, const double* const* fF, void* stream) {
+    GradArgs ga;
+    for (int c = 0; c < 3; c++) ga.U[c] = U[c];
+    ga.Tf = T;
+    for (int c = 0; c < 12; c++) ga.G[c] = G[c];
+    for (int c = 0; c < 4; c++) ga.fF[c] = const_cast<double*>(fF[c]);
+    const int threads = ((m->np + 31) / 32) * 32;
+    k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), (cudaStream_t)stream>>>(*m, *t, ga);
+    return (int)cudaGetLastError();
+}
+
 int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream) {
     const AdvArgs a = adv_args(b, b->cur, 1.0);
     k_conv_lambda<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);

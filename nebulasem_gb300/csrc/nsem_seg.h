@@ -38,6 +38,10 @@ struct NsemConvBuf {
 int nsem_seg_prepare(const NsemDev* m);
 /* strong-form gradients of U (3 arrays) and the full theta T into G (12 per
  * node) with the per-slot scratch fF (4), for the viscous fluxes */
+/* the volume part of the gradients only, from given per-slot face values fF
+ * (cds of U and theta); linear in (U, T, fF) */
+int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
+                  double* const* G, const double* const* fF, void* stream);
 int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
                  double* const* G, double* const* fF, void* stream);
 /* lambda of the fixed wind (once, after U is set) */

@@ -76,3 +76,31 @@ def test_tlm_trajectory_vs_cpu_and_adjoint_duality():
     lhs, rhs = dot(lamN, duT), dot(lam0, du0)
     assert abs(lhs - rhs) <= 1e-10 * abs(lhs), (lhs, rhs)
     s.close()
+
+
+@pytest.mark.parametrize("case", ["g3_2_visc", "c1_2d_visc"])
+def test_viscous_jvp_and_tlm_vs_cpu_tangent(case):
+    """With the artificial viscosity: the tangent of the viscous fluxes
+    (d(mu grad U) with the gradients' own tangent, the SYMMETRY ghost
+    linearised) against the dual-number oracle, one tendency and a 10-step
+    trajectory."""
+    import nebulasem_gb300 as ng
+    g = load_golden(case)
+    u = golden_state(g, "up")
+    dt = float(g["dt"])
+    s = ng.Solver(g, dt=dt)
+    s.set_state(u)
+    m = oracle.OracleMesh(g)
+    oracle.set_pow(1)
+    rng = np.random.default_rng(13)
+    dv = perturbation(rng, u)
+    _, Ld_cpu = m.jvp(u, dv)
+    Ld = s.jvp(dv)
+    assert rel(Ld, Ld_cpu) <= 1e-11, (case, rel(Ld, Ld_cpu))
+    uT_cpu, duT_cpu = m.tlm_ssprk3(u, dv, dt, 10)
+    oracle.set_pow(0)
+    s.set_state(u)
+    duT, _ = s.tlm(10, dv)
+    assert all(np.array_equal(a, b) for a, b in zip(s.get_state(), uT_cpu))
+    assert rel(duT, duT_cpu) <= 1e-10, (case, rel(duT, duT_cpu))
+    s.close()
