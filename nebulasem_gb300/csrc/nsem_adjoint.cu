@@ -40,6 +40,11 @@ __device__ __forceinline__ double vdot3(const double* a, const double* b) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
+/* tensor index of d_r U_c (XX,YY,ZZ,XY,YZ,XZ,YX,ZY,ZX) */
+__device__ __forceinline__ constexpr int tix(int r, int c) {
+    return r == c ? r : (r == 0 ? (c == 1 ? XY : XZ) : r == 1 ? (c == 2 ? YZ : YX) : (c == 0 ? ZX : ZY));
+}
+
 struct NodePrim {
     double r, U[3], T, p, pp, mu, c;   /* p: full pressure, pp = p - p_ref */
 };
@@ -99,6 +104,7 @@ struct FaceAdjArgs {
     const double* W[5];      /* w = adjoint of L */
     double* adjO[NPA];       /* per slot, owner side primitive adjoints */
     double* adjN[NPA];       /* per slot, neighbour side (0 for ghosts) */
+    double* dbv[4];          /* viscous runs: momentum and theta flux adjoints (else null) */
 };
 
 __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a) {
@@ -127,6 +133,10 @@ __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a
         double x = -a.W[v][c1] / m.cv[c1];
         if (c2 >= 0) x -= -a.W[v][c2] / m.cv[c2];
         db[v] = x;
+    }
+    if (a.dbv[0]) {
+        for (int c = 0; c < 3; c++) a.dbv[c][k] = db[1 + c];
+        a.dbv[3][k] = db[4];
     }
     const double lam = ((P1.mu * fi + P2.mu * fo) + (P1.c * fi + P2.c * fo)) / 2;
     /* primitive adjoints of both sides */
@@ -209,9 +219,19 @@ struct VolAdjArgs {
     const double* adjO[NPA];
     const double* adjN[NPA];
     double* G[5];            /* output: J_L(v)^T w */
+    /* viscous runs (else null): gradients of the state, slot flux adjoints;
+     * out: gradient adjoints / cV and the adjoint of mu per node */
+    const double* Gv[12];
+    const double* dbv[4];
+    double* Gbs[12];
+    double* mub;
 };
 
-__global__ void k_adj_volume(const NsemDev m, const NsemTables tab, VolAdjArgs a) {
+/* registers capped for the largest element: 736 threads (N+1 = 9) inviscid,
+ * 512 (N+1 = 8) with the viscous terms */
+template <bool VISC>
+__global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const NsemTables tab,
+                                                          VolAdjArgs a) {
     extern __shared__ double sm[];
     const int NPX = m.npx, NPY = m.npy, NPZ = m.npz, NP = m.np;
     double* rb = sm;                                 /* [5][NP] rbar of the element */
@@ -272,6 +292,44 @@ __global__ void k_adj_volume(const NsemDev m, const NsemTables tab, VolAdjArgs a
         const double D = Dz[ka * NPZ + km];
         const double dj[3] = {Jin[XZ] * D, Jin[YZ] * D, Jin[ZZ] * D};
         acc(t + (km - ka), dj);
+    }
+    /* viscous fluxes fm -= mu grad U, ft -= (mu / Pr) grad theta (volume) and the
+     * node's side of its face fluxes: adjoints of the node's gradients and of mu */
+    if constexpr (VISC) {
+        const double mu = P.r * m.nu, mt = mu * m.iPr;
+        double Gn[12], Gb[12], mb = 0;
+        for (int c = 0; c < 12; c++) Gn[c] = a.Gv[c][node];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                const int q = tix(r, c);
+                Gb[q] = mu * H[r][c];
+                mb += Gn[q] * H[r][c];
+            }
+        for (int c = 0; c < 3; c++) {
+            Gb[9 + c] = mt * K[c];
+            mb += m.iPr * Gn[9 + c] * K[c];
+        }
+        for (int j = 0; j < 3; j++) {
+            const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+            if (code < 0) break;
+            const int64_t k = code >> 1;
+            const double f = (code & 1) ? 1.0 - m.fi[k] : m.fi[k];
+            const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+            const double dm[3] = {a.dbv[0][k], a.dbv[1][k], a.dbv[2][k]}, dt = a.dbv[3][k];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    const int q = tix(r, c);
+                    Gb[q] -= f * mu * dm[r] * n[c];
+                    mb -= f * dm[r] * n[c] * Gn[q];
+                }
+            for (int c = 0; c < 3; c++) {
+                Gb[9 + c] -= f * mt * dt * n[c];
+                mb -= f * m.iPr * dt * n[c] * Gn[9 + c];
+            }
+        }
+        const double icv = 1.0 / m.cv[node];
+        for (int c = 0; c < 12; c++) a.Gbs[c][node] = Gb[c] * icv;
+        a.mub[node] = mb;
     }
     /* flux adjoints -> primitive adjoints (fr = U rho, fm = (rho U) (x) U + p' I,
      * ft = (rho U) theta; Fbar = -(G, H, K)) */
@@ -369,10 +427,6 @@ struct FaceTanArgs {
     const double* G[12];     /* viscous runs: grad U, grad theta of the state (else null) */
     const double* dG[12];    /* and their tangents */
 };
-
-__device__ __forceinline__ constexpr int tix(int r, int c) {
-    return r == c ? r : (r == 0 ? (c == 1 ? XY : XZ) : r == 1 ? (c == 2 ? YZ : YX) : (c == 0 ? ZX : ZY));
-}
 
 /* U and theta of the state and their tangents, per node (gradient inputs) */
 struct PrimTanArgs {
@@ -593,6 +647,150 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
     for (int v = 0; v < 5; v++) a.out[v][node] = -(r[v] / cv);
 }
 
+/* Transpose of the strong-form gradient (gradf<true>) for the viscous
+ * adjoint.  Forward, per node a: G_a = (1/cV_a) [sum_slots s fN (x) (cds - p_a)
+ * + sum_b (jin_a dpsi(b at a)) (x) p_b], cds = fi p_c1 + fo p_c2 (the wall ghost
+ * p_c2 = SYMMETRY projection / NEUMANN copy of p_c1).  Given Gbs = Gbar / cV:
+ *   face (per slot): v_c1 = fN . Gbs_c1, v_c2 = -fN . Gbs_c2; cdsbar = v_c1 + v_c2;
+ *     pbar_c1 += fi cdsbar - v_c1, pbar_c2 += fo cdsbar - v_c2 (the ghost's
+ *     share folded into c1 through the ghost's transpose);
+ *   volume (per node b): pbar_b += sum over the nodes a on b's lines of
+ *     (jin_a dpsi(b at a))^T Gbs_a. */
+struct GradAdjArgs {
+    const double* S[5];
+    const double* pU[4];      /* U, theta of the state (the ghost's linearisation point) */
+    const double* Gbs[12];
+    double* agO[4];
+    double* agN[4];
+    double* G[5];             /* conserved-state adjoint, added to */
+    const double* mub;
+};
+
+__global__ void __launch_bounds__(256) k_adj_grad_face(const NsemDev m, GradAdjArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_slot) return;
+    const int32_t c1 = m.c1[k], c2 = m.c2[k];
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    double v1[4], v2[4] = {0, 0, 0, 0};
+    for (int c = 0; c < 3; c++) {
+        v1[c] = n[0] * a.Gbs[tix(0, c)][c1] + n[1] * a.Gbs[tix(1, c)][c1] + n[2] * a.Gbs[tix(2, c)][c1];
+        if (c2 >= 0)
+            v2[c] = -(n[0] * a.Gbs[tix(0, c)][c2] + n[1] * a.Gbs[tix(1, c)][c2] +
+                      n[2] * a.Gbs[tix(2, c)][c2]);
+    }
+    v1[3] = n[0] * a.Gbs[9][c1] + n[1] * a.Gbs[10][c1] + n[2] * a.Gbs[11][c1];
+    if (c2 >= 0) v2[3] = -(n[0] * a.Gbs[9][c2] + n[1] * a.Gbs[10][c2] + n[2] * a.Gbs[11][c2]);
+    double cb[4], p1[4], p2[4];
+    for (int c = 0; c < 4; c++) {
+        cb[c] = v1[c] + v2[c];
+        p1[c] = fi * cb[c] - v1[c];
+        p2[c] = fo * cb[c] - v2[c];
+    }
+    if (c2 < 0) {
+        /* ghost: theta copies theta_c1; U is the SYMMETRY projection or a copy */
+        const double gU[3] = {fo * cb[0], fo * cb[1], fo * cb[2]};
+        p1[3] += fo * cb[3];
+        if (m.bc[k] == 2) {
+            const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+            const double U1[3] = {a.pU[0][c1], a.pU[1][c1], a.pU[2][c1]};
+            double U2[3], rsym[3], magR, magP;
+            bool scaled;
+            sym_fwd(U1, en, U2, rsym, magR, magP, scaled);
+            sym_vjp(U1, en, rsym, magR, magP, scaled, gU, p1);
+        } else {
+            for (int c = 0; c < 3; c++) p1[c] += gU[c];
+        }
+        for (int c = 0; c < 4; c++) p2[c] = 0;
+    }
+    for (int c = 0; c < 4; c++) {
+        a.agO[c][k] = p1[c];
+        a.agN[c][k] = p2[c];
+    }
+}
+
+/* shared layout per node: Gbs[12] jin[9] */
+constexpr int GADJ_W = 21;
+
+__global__ void k_adj_grad_vol(const NsemDev m, const NsemTables tab, GradAdjArgs a) {
+    extern __shared__ double sm[];
+    const int NPX = m.npx, NPY = m.npy, NPZ = m.npz, NP = m.np;
+    double* dps = sm + (size_t)NP * GADJ_W;
+    const int t = threadIdx.x;
+    for (int q = t; q < 3 * NSEM_MAX_NPD * NSEM_MAX_NPD; q += blockDim.x)
+        dps[q] = (&tab.dpsi[0][0])[q];
+    const int64_t e = blockIdx.x;
+    const bool active = t < NP;
+    const int64_t node = e * NP + t;
+    if (active) {
+        double* my = sm + (size_t)t * GADJ_W;
+        for (int c = 0; c < 12; c++) my[c] = a.Gbs[c][node];
+        for (int c = 0; c < 9; c++) my[12 + c] = m.jin[(int64_t)c * m.n_int + node];
+    }
+    __syncthreads();
+    if (!active) return;
+    const int ib = t / (NPY * NPZ), jb = (t / NPZ) % NPY, kb = t % NPZ;
+    const double* Dx = dps;
+    const double* Dy = dps + NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Dz = dps + 2 * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    double pb[4] = {0, 0, 0, 0};
+    auto add = [&](int la, const double* dj) {
+        const double* sa = sm + (size_t)la * GADJ_W;
+        for (int c = 0; c < 3; c++)
+            pb[c] += dj[0] * sa[tix(0, c)] + dj[1] * sa[tix(1, c)] + dj[2] * sa[tix(2, c)];
+        pb[3] += dj[0] * sa[9] + dj[1] * sa[10] + dj[2] * sa[11];
+    };
+    /* the nodes a whose gradient used p_b: b's x line (a = b: the full
+     * jin_b . (Dx_bb, Dy_bb, Dz_bb)), its y and z lines without b */
+    for (int ia = 0; ia < NPX; ia++) {
+        const int la = t + (ia - ib) * NPY * NPZ;
+        const double* J = sm + (size_t)la * GADJ_W + 12;
+        double dj[3];
+        if (ia == ib) {
+            const double dv[3] = {Dx[ib * NPX + ib], Dy[jb * NPY + jb], Dz[kb * NPZ + kb]};
+            dj[0] = J[XX] * dv[0] + J[XY] * dv[1] + J[XZ] * dv[2];
+            dj[1] = J[YX] * dv[0] + J[YY] * dv[1] + J[YZ] * dv[2];
+            dj[2] = J[ZX] * dv[0] + J[ZY] * dv[1] + J[ZZ] * dv[2];
+        } else {
+            const double D = Dx[ia * NPX + ib];
+            dj[0] = J[XX] * D; dj[1] = J[YX] * D; dj[2] = J[ZX] * D;
+        }
+        add(la, dj);
+    }
+    for (int q = 0; q + 1 < NPY; q++) {
+        const int ja = q < jb ? q : q + 1;
+        const int la = t + (ja - jb) * NPZ;
+        const double* J = sm + (size_t)la * GADJ_W + 12;
+        const double D = Dy[ja * NPY + jb];
+        const double dj[3] = {J[XY] * D, J[YY] * D, J[ZY] * D};
+        add(la, dj);
+    }
+    for (int q = 0; q + 1 < NPZ; q++) {
+        const int ka = q < kb ? q : q + 1;
+        const int la = t + (ka - kb);
+        const double* J = sm + (size_t)la * GADJ_W + 12;
+        const double D = Dz[ka * NPZ + kb];
+        const double dj[3] = {J[XZ] * D, J[YZ] * D, J[ZZ] * D};
+        add(la, dj);
+    }
+    /* face terms gathered through the lift lists */
+    for (int j = 0; j < 3; j++) {
+        const int32_t code = m.lift[(int64_t)j * m.n_int + node];
+        if (code < 0) break;
+        const int64_t k = code >> 1;
+        const double* const* src = (code & 1) ? a.agN : a.agO;
+        for (int c = 0; c < 4; c++) pb[c] += src[c][k];
+    }
+    /* (rho, U, theta) adjoints -> conserved: U = m / rho, theta = E / rho; mu = rho nu */
+    const double r = a.S[0][node], inv = 1.0 / r;
+    const double U[3] = {a.S[1][node] * inv, a.S[2][node] * inv, a.S[3][node] * inv};
+    const double T = a.S[4][node] / r;
+    const double rbar = m.nu * a.mub[node];
+    a.G[0][node] += rbar - inv * (pb[0] * U[0] + pb[1] * U[1] + pb[2] * U[2]) - inv * pb[3] * T;
+    for (int c = 0; c < 3; c++) a.G[1 + c][node] += pb[c] * inv;
+    a.G[4][node] += pb[3] * inv;
+}
+
 /* lam = c0 * lam + c1 * x + c2 * y (elementwise over 5 arrays) */
 struct Lin3Args {
     double* out[5];
@@ -625,17 +823,42 @@ int grid_for(int64_t n) {
 int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
                  const double* const* W, double* const* G, NsemAdjBuf* ab, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
-    FaceAdjArgs fa;
+    FaceAdjArgs fa{};
+    VolAdjArgs va{};
+    if (ab->visc) {
+        /* U, theta and the gradients of the state */
+        PrimTanArgs pa;
+        for (int v = 0; v < 5; v++) { pa.S[v] = S[v]; pa.dS[v] = S[v]; }
+        for (int c = 0; c < 4; c++) { pa.pU[c] = ab->pU[c]; pa.dpU[c] = ab->dpU[c]; }
+        k_tan_prims<<<(unsigned)((m->n_int + 255) / 256), 256, 0, st>>>(*m, pa);
+        const int e = nsem_grad_ut(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF, stream);
+        if (e) return e;
+        for (int c = 0; c < 4; c++) fa.dbv[c] = ab->dbv[c];
+        for (int c = 0; c < 12; c++) { va.Gv[c] = ab->Gv[c]; va.Gbs[c] = ab->Gbs[c]; }
+        for (int c = 0; c < 4; c++) va.dbv[c] = ab->dbv[c];
+        va.mub = ab->mub;
+    }
     for (int v = 0; v < 5; v++) { fa.S[v] = S[v]; fa.W[v] = W[v]; }
     for (int v = 0; v < NPA; v++) { fa.adjO[v] = ab->adjO[v]; fa.adjN[v] = ab->adjN[v]; }
     const int64_t fb = (m->n_slot + 127) / 128;
     k_adj_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
-    VolAdjArgs va;
     for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.W[v] = W[v]; va.G[v] = G[v]; }
     for (int v = 0; v < NPA; v++) { va.adjO[v] = ab->adjO[v]; va.adjN[v] = ab->adjN[v]; }
     const int threads = ((m->np + 31) / 32) * 32;
     const size_t smem = (5 * (size_t)m->np + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
-    k_adj_volume<<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
+    if (ab->visc) k_adj_volume<true><<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
+    else k_adj_volume<false><<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
+    if (ab->visc) {
+        /* the gradients' transpose, added to the conserved adjoint */
+        GradAdjArgs ga;
+        for (int v = 0; v < 5; v++) { ga.S[v] = S[v]; ga.G[v] = G[v]; }
+        for (int c = 0; c < 4; c++) { ga.pU[c] = ab->pU[c]; ga.agO[c] = ab->agO[c]; ga.agN[c] = ab->agN[c]; }
+        for (int c = 0; c < 12; c++) ga.Gbs[c] = ab->Gbs[c];
+        ga.mub = ab->mub;
+        k_adj_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
+        const size_t gsm = ((size_t)m->np * GADJ_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+        k_adj_grad_vol<<<(unsigned)m->n_elem, threads, gsm, st>>>(*m, *t, ga);
+    }
     return (int)cudaGetLastError();
 }
 
@@ -690,13 +913,21 @@ int nsem_adj_lin3(double* const* out, const double* const* x, double cx, const d
 int nsem_adj_prepare(const NsemDev* m) {
     const size_t smem = (5 * (size_t)m->np + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
     if (smem > 48 * 1024) {
-        const int e = (int)cudaFuncSetAttribute(k_adj_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem);
+        int e = (int)cudaFuncSetAttribute(k_adj_volume<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem);
+        if (!e) e = (int)cudaFuncSetAttribute(k_adj_volume<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem);
         if (e) return e;
     }
     const size_t tsm = ((size_t)m->np * TAN_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
-    if (tsm > 48 * 1024)
-        return (int)cudaFuncSetAttribute(k_tan_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tsm);
+    if (tsm > 48 * 1024) {
+        const int e = (int)cudaFuncSetAttribute(k_tan_volume, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)tsm);
+        if (e) return e;
+    }
+    const size_t gsm = ((size_t)m->np * GADJ_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
+    if (gsm > 48 * 1024)
+        return (int)cudaFuncSetAttribute(k_adj_grad_vol, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)gsm);
     return 0;
 }

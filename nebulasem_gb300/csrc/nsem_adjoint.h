@@ -30,6 +30,11 @@ struct NsemAdjBuf {
     double* dGv[12] = {};
     double* fF[4] = {};
     double* dfF[4] = {};
+    double* dbv[4] = {};    /* per slot: momentum and theta flux adjoints        */
+    double* Gbs[12] = {};   /* per node: gradient adjoints divided by cV         */
+    double* mub = nullptr;  /* per node: adjoint of mu = rho nu                   */
+    double* agO[4] = {};    /* per slot: gradient face-term adjoints, owner side  */
+    double* agN[4] = {};    /* per slot: neighbour side                           */
     int nsteps = 0, every = 0, n_ckpt = 0;
     bool ready = false;
 };

@@ -644,7 +644,14 @@ static nsem_status adj_alloc(nsem_ctx* ctx) {
         for (int c = 0; c < 12; c++) {
             if ((s = dalloc(ctx, &A.Gv[c], n)) != NSEM_OK) return s;
             if ((s = dalloc(ctx, &A.dGv[c], n)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.Gbs[c], n)) != NSEM_OK) return s;
         }
+        for (int c = 0; c < 4; c++) {
+            if ((s = dalloc(ctx, &A.dbv[c], ns)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.agO[c], ns)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.agN[c], ns)) != NSEM_OK) return s;
+        }
+        if ((s = dalloc(ctx, &A.mub, n)) != NSEM_OK) return s;
         A.visc = true;
     }
     int e = nsem_adj_prepare(&ctx->dev);
@@ -686,8 +693,6 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
 
 extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
     if (!ctx) return NSEM_BAD_ARG;
-    if (ctx->dev.nu != 0.0)
-        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
@@ -796,8 +801,6 @@ extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const d
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
     if (!ctx) return NSEM_BAD_ARG;
-    if (ctx->dev.nu != 0.0)
-        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     nsem_status s = ensure_rep(ctx, 0);
@@ -845,8 +848,6 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
 extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                     double* const lam0[5], double* ms_adj) {
     if (!ctx) return NSEM_BAD_ARG;
-    if (ctx->dev.nu != 0.0)
-        return fail(ctx, NSEM_UNSUPPORTED, "adjoint and tangent-linear forms: no artificial viscosity");
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
     NsemAdjBuf& A = ctx->abuf;
     if (!A.ready || !A.ckpt || A.nsteps < 1)

@@ -79,11 +79,11 @@ def test_tlm_trajectory_vs_cpu_and_adjoint_duality():
 
 
 @pytest.mark.parametrize("case", ["g3_2_visc", "c1_2d_visc"])
-def test_viscous_jvp_and_tlm_vs_cpu_tangent(case):
+def test_viscous_jvp_tlm_and_adjoint(case):
     """With the artificial viscosity: the tangent of the viscous fluxes
     (d(mu grad U) with the gradients' own tangent, the SYMMETRY ghost
     linearised) against the dual-number oracle, one tendency and a 10-step
-    trajectory."""
+    trajectory; the adjoint (the gradients' transpose) by duality with it."""
     import nebulasem_gb300 as ng
     g = load_golden(case)
     u = golden_state(g, "up")
@@ -103,4 +103,20 @@ def test_viscous_jvp_and_tlm_vs_cpu_tangent(case):
     duT, _ = s.tlm(10, dv)
     assert all(np.array_equal(a, b) for a, b in zip(s.get_state(), uT_cpu))
     assert rel(duT, duT_cpu) <= 1e-10, (case, rel(duT, duT_cpu))
+    # the adjoint of the viscous terms: duality with the tangent, one tendency
+    # (<w, J dv> = <J^T w, dv>) and the 10-step trajectory (<lam_N, du_N> =
+    # <lam_0, du_0>)
+    s.set_state(u)
+    for trial in range(2):
+        w = [rng.standard_normal(m.n_int) for _ in range(5)]
+        Ld = s.jvp(dv)
+        lhs, rhs = dot(w, Ld), dot(s.vjp(w), dv)
+        scale = sum(np.abs(x * y).sum() for x, y in zip(w, Ld))
+        assert abs(lhs - rhs) <= 1e-11 * scale, (case, trial, lhs, rhs)
+    lamN = [rng.standard_normal(m.n_int) for _ in range(5)]
+    s.set_state(u)
+    s.forward_checkpointed(10, 5)
+    lam0, _ = s.adjoint(lamN)
+    lhs, rhs = dot(lamN, duT), dot(lam0, dv)
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs), (case, lhs, rhs)
     s.close()
