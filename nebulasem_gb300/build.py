@@ -65,7 +65,9 @@ def build_driver(verbose=False, force=False):
         if all(os.path.getmtime(d) <= t for d in deps):
             return DRIVER_EXE
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + DRIVER]
+    # no contraction: the mesh geometry follows the reference operation by operation
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-ffp-contract=off",
+           "-I" + os.path.join(ROOT, "include"), "-I" + DRIVER]
     cmd += srcs + ["-L" + OUT, "-lnsem_gpu", "-Wl,-rpath,$ORIGIN", "-o", DRIVER_EXE]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

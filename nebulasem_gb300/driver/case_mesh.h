@@ -3,29 +3,37 @@
  *
  * Input: the block description the reference's mesh app reads
  * (apps/mesh/meshApp.cpp:70-230: key points, hex blocks `8{...} <grading>
- * 3{nx ny nz} ...`, named boundary patches `name 4{a b c d}...`, `default
- * name`).  Supported: one hexahedral block with straight edges forming a
- * parallelepiped (axis-aligned, or rotated / sheared as the reference's
- * srtb-inclined example), uniform spacing (`linear`, or `wall`/`geometric`
- * with all factors 1); a `delete` patch on the two faces of the block's second
- * axis, one element thick, makes the case two-dimensional (npy 0).  Anything
- * else (curved edges, several blocks, grading) is rejected with a message:
- * the driver has no CPU path to fall back to.
+ * 3{nx ny nz} ... [edges n{...}]`, named boundary patches `name 4{a b c
+ * d}...`, `default name`).  Supported: one hexahedral block, either with
+ * straight edges forming a parallelepiped (axis-aligned, or rotated / sheared
+ * as the reference's srtb-inclined example) or with curved edges (any 8
+ * corners); uniform spacing (`linear`, or `wall`/`geometric` with all factors
+ * 1); a `delete` patch on the two faces of the block's second axis, one
+ * element thick, makes the case two-dimensional (npy 0).  Anything else
+ * (several blocks, grading) is rejected with a message: the driver has no CPU
+ * path to fall back to.
  *
- * Metric of a non-axis-aligned block: the reference's pseudo-inverse
- * (dg.cpp:412-476) Jinv = ((J^T J)^-1 J^T)^T of the constant element Jacobian
- * J = [e_0/2, e_1/2, e_2/2] (a collapsed direction's column and inverse
- * diagonal zero), node weights V_e w_i w_j w_k / 8, face area vectors e_b x e_c.
+ * Geometry, for every block, as the reference's mesh app and LoadMesh form
+ * it, operation by operation so that the arrays agree to the bit: the
+ * block's vertex lattice by transfinite interpolation of its corners, edges
+ * (straight, arcs through the key point, or the bump shapes of
+ * hexMesh.cpp:20-45) and faces; each element straight-edged between its 8
+ * vertices (dg.cpp:167-300), its nodes by transfinite interpolation, the
+ * metric per node from the LGL derivative of the node coordinates and the
+ * pseudo-inverse ((J^T J)^-1 J^T)^T with a collapsed direction's diagonal
+ * zero (dg.cpp:412-476); the node weights from the element volume and the
+ * face weights from the face area vectors as Mesh::calcGeometry forms them
+ * (mesh.cpp:450-520: triangle fans about the vertex centroid, pyramids about
+ * the cell centre).
  *
  * Output: the arrays of the reference's Mesh:: / DG:: layout for that box
  * (the nsem_mesh_desc of the C ABI), built with the reference's conventions:
  * LGL nodes and Lagrange tables as src/field/dg.cpp:32-143, face slots and
- * weights as DG::init_geom (dg.cpp:323-410), node weights cV = V w_i w_j w_k
- * / 8, metric Jinv = diag(2/h).  Node coordinates are the exact affine
- * values; element, face and ghost-cell numbering are canonical (element z
- * fastest, then y, then x; interior faces z, y, x; boundary faces z-, z+,
- * y-, y+, x-, x+), so the discretisation is the reference's up to the order
- * of the face sums and the last bits of the geometry.
+ * weights as DG::init_geom (dg.cpp:323-410).  Element, face and ghost-cell
+ * numbering are canonical (element k fastest, then j, then i; interior faces
+ * normal to k, j, i; boundary faces k-, k+, j-, j+, i-, i+); each node's
+ * face terms are summed in the cell's face order k-, k+, j-, j+, i-, i+ as in
+ * the reference, so its examples run bit-identically.
  */
 #ifndef NSEM_DRIVER_CASE_MESH_H
 #define NSEM_DRIVER_CASE_MESH_H
@@ -45,19 +53,23 @@ struct BoxSide {
 };
 
 struct BlockDesc {
-    std::array<double, 3> lo{}, hi{};      /* box extent (axis-aligned blocks) */
-    std::array<int, 3> n{};                /* elements per axis: global x, y, z for an
-                                              axis-aligned block, else the block's own
-                                              axes v0->v1, v0->v3, v0->v4 */
-    /* patch name of each side, in the order z-, z+, y-, y+, x-, x+ of those axes
+    std::array<int, 3> n{};                /* elements along the block's own axes
+                                              v0->v1, v0->v3, v0->v4 (i, j, k) */
+    /* patch name of each side, in the order k-, k+, j-, j+, i-, i+ of those axes
      * ("" if deleted) */
     std::array<std::string, 6> patch;
-    bool two_d = false;                    /* y faces deleted, one element in y */
-    /* a block whose edges are not along the coordinate axes (rotated or
-     * sheared parallelepiped): x = origin + sum_a xi_a E[a], xi_a in [0, 1] */
-    bool affine = false;
-    std::array<double, 3> origin{};
-    std::array<std::array<double, 3>, 3> E{};
+    bool two_d = false;                    /* j faces deleted, one element in j */
+    /* the 8 corners in hex order and the 12 edges; curved edges from
+     * `edges n{ arc|cosine|gaussian|ridge|schar side key [scale] }` */
+    bool curved = false;
+    bool wall = false;                     /* `wall` spacing: mirrored edge parameters */
+    std::array<std::array<double, 3>, 8> corner{};
+    struct Edge {
+        int type = 0;                      /* 0 straight, 1 arc, 2 cosine, 3 gaussian, 4 ridge, 5 schar */
+        std::array<double, 3> key{};       /* the edge's third key point */
+        double scale = 1.0;
+    };
+    std::array<Edge, 12> edge{};
 };
 
 /* parse the block description file; throws std::runtime_error */

@@ -6,12 +6,13 @@ For each example directory under <ref>/examples/atmo: copy it, shorten the
 run to 20 steps written once, run the reference mesh app and `euler` on it,
 let nsem_euler write its case arrays (--dump, no GPU), run the oracle's
 segregated scheme (C library pow, as the reference) on those arrays, and
-compare the final rho, U, T with the reference's output files node by node
-(nodes matched by coordinates; the reference's geometry from the harness).
-Examples the driver does not model (AMR, curved or multi-block meshes,
-spherical problems, other time schemes) are reported with its message.
+compare the node coordinates and the final rho, U, T with the reference's
+output files node by node (nodes matched by coordinates; the reference's
+geometry from the harness).  Examples the driver does not model (AMR,
+multi-block meshes, spherical problems, other time schemes) are reported with
+its message.
 
-    python oracle/check_examples.py --ref /root/reference srtb ctbs dc lrtb srtb-3d
+    python oracle/check_examples.py --ref /root/reference srtb srtb-inclined srtb-curved ctbs dc lrtb
 """
 import argparse
 import os

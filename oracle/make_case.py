@@ -102,9 +102,37 @@ boundary 3
 """
 
 
+# Curved block edges for the 2D block 8{0 1 5 4 3 2 6 7}: extra key points (in
+# units of the block lengths) and `edges` lines of the mesh app
+# (apps/mesh/meshApp.cpp:159-185).  "arc_y": the reference's srtb-curved
+# example, its x edges bowed out in y through arcs; "hill": a cosine hill
+# 0.15 lz high over 60 % of the bottom edges, as the hills examples build
+# terrain.
+CURVED = {
+    "arc_y": ([(0.5, 2.0, 0.0), (0.5, 4.0, 0.0), (0.5, 4.0, 1.0), (0.5, 2.0, 1.0)],
+              ["arc 0 8", "arc 1 9", "arc 2 10", "arc 3 11"]),
+    "hill": ([(0.5, 0.0, 0.15), (0.5, 1.0, 0.15)],
+             ["cosine 0 8 0.6", "cosine 1 9 0.6"]),
+}
+
+
+def curved_grid(grid, curved, lx, ly, lz):
+    """Insert a CURVED variant's key points and edges into a 2D grid text."""
+    pts, edges = CURVED[curved]
+    lines = grid.split("\n")
+    nkp = int(lines[0])
+    extra = [f"{a * lx!r} {b * ly!r} {c * lz!r}" for a, b, c in pts]
+    lines[0] = str(nkp + len(extra))
+    close = lines.index("}")
+    lines[close:close] = extra
+    blk = next(q for q, l in enumerate(lines) if l.startswith("8{"))
+    lines[blk + 1:blk + 1] = [f"edges {len(edges)}{{"] + ["    " + e for e in edges] + ["}"]
+    return "\n".join(lines)
+
+
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
                Pr=0.9, solver="euler", wind=None, time_scheme="BDF1", P0=100000, cp=1004.5,
-               cv=717.5, gz=-9.81):
+               cv=717.5, gz=-9.81, curved=None):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
@@ -122,8 +150,12 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
             ctl += "\n" + solver + "\n{\n    problem_init NONE\n}\n"
         f.write(ctl)
     grid = GRID_2D if dim == 2 else GRID_3D
+    grid = grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz)
+    if curved:
+        assert dim == 2, "curved variants are for the 2D block"
+        grid = curved_grid(grid, curved, lx, ly, lz)
     with open(os.path.join(out, "grid"), "w") as f:
-        f.write(grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz))
+        f.write(grid)
     cx, cy, cz = center
     rx, ry, rz = radius
     cos_init = f"cosine 0 {amp}    {cx} {cy} {cz}   {rx} {ry} {rz}"

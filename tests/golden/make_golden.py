@@ -65,6 +65,9 @@ SEG_PLAN = {
     # the reference's srtb example as shipped: its viscosity and gravity, the
     # Fluid:: defaults for P0, cp, cv (examples/atmo/srtb/controls)
     "srtb": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb"),
+    # curved blocks: the srtb-curved example's arcs, and a cosine hill
+    "srtb_curved": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb", "arc_y"),
+    "hill": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb", "hill"),
 }
 
 # fixture -> (case, dt, steps, wind) for the reference's scalar convection app
@@ -128,9 +131,10 @@ def make_seg_case(name, ref_bin, tmp):
     base, dt, nsteps, visc, scheme = SEG_PLAN[name][:5]
     fluid = dict(SRTB_FLUID) if len(SEG_PLAN[name]) > 5 else {}
     fluid.pop("viscosity", None)
+    curved = SEG_PLAN[name][6] if len(SEG_PLAN[name]) > 6 else None
     case = os.path.join(tmp, "seg_" + name)
     write_case(case, dt=dt, steps=nsteps, viscosity=visc, time_scheme=scheme, **fluid,
-               **CASES[base])
+               **CASES[base], curved=curved)
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
@@ -149,6 +153,8 @@ def make_seg_case(name, ref_bin, tmp):
     out["nsteps"] = np.int64(nsteps)
     out["viscosity"] = np.float64(visc)
     out["Pr"] = np.float64(0.9)
+    if curved:
+        out["curved"] = np.array(curved)
     if fluid:
         # constants in the names the oracle and the Python host read
         out["P0"] = np.float64(fluid["P0"])

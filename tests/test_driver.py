@@ -17,6 +17,7 @@ from nebulasem_gb300.mesh import box_mesh, bubble_state
 from oracle.make_case import CASES
 
 GEOM_U32 = ["meta", "FO", "FN", "allFaces", "faceIdx0", "faceIdx1", "bcU"]
+GEOM_LAST_BITS = ("cC", "cV", "Jinv", "fN")
 GEOM_F64 = ["cC", "cV", "Jinv", "fN", "fI", "xgl0", "xgl1", "xgl2", "wgl0", "wgl1", "wgl2",
             "psi0", "psi1", "psi2", "dpsi0", "dpsi1", "dpsi2"]
 
@@ -25,13 +26,24 @@ GEOM_F64 = ["cC", "cV", "Jinv", "fN", "fI", "xgl0", "xgl1", "xgl2", "wgl0", "wgl
                                     ("g3_4n3", (4, 4, 2))])
 def test_mesh_equals_python_box_mesh(tmp_path, case, n):
     """The block `wall 3{4 3 2}` of g3_4n3 has 4 elements in y: the mesh app
-    adds one division to an odd wall-graded count (hexMesh.cpp:51-66)."""
+    adds one division to an odd wall-graded count (hexMesh.cpp:51-66).
+
+    Connectivity, face slots and LGL tables are identical; the driver forms
+    the geometry as the reference's mesh app and LoadMesh do (transfinite
+    vertex lattice, calcGeometry volumes and areas, metric from the node
+    coordinates), which differs from the Python box mesh's affine formulas in
+    the last bits only."""
     c = CASES[case]
     d = dump_case(make_case(tmp_path, case, dt=0.01, steps=10))
     m = box_mesh(n, c["order"], c["length"], dim=c["dim"])
     # the Python host marks every wall SYMMETRY for U, as these cases do
     for k in GEOM_U32 + GEOM_F64:
-        assert np.array_equal(np.asarray(d[k]).reshape(-1), np.asarray(m[k]).reshape(-1)), k
+        a, b = np.asarray(d[k]).reshape(-1), np.asarray(m[k]).reshape(-1)
+        if k in GEOM_LAST_BITS:
+            assert a.shape == b.shape, k
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), k
+        else:
+            assert np.array_equal(a, b), k
     u, p_ref, rho_ref, _ = bubble_state(m, c["amp"], c["center"], c["radius"])
     # numpy's vectorised pow / cos may differ from the C library in the last bit
     assert rel_l2(d["p_ref"], p_ref) < 1e-15
@@ -46,20 +58,22 @@ FLUID = ("P0", "cp", "cv", "R", "gamma", "gravity")
 
 
 @pytest.mark.parametrize("fixture,case", [("seg_c1_2d", "c1_2d"), ("seg_g3_2", "g3_2"),
-                                          ("seg_c1_2d_visc", "c1_2d"), ("seg_srtb", "c1_2d")])
+                                          ("seg_c1_2d_visc", "c1_2d"), ("seg_srtb", "c1_2d"),
+                                          ("seg_srtb_curved", "c1_2d"), ("seg_hill", "c1_2d")])
 def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
     """The oracle (C library pow, as the binary) run on the driver's mesh and
     initial fields against the unmodified euler binary's fields after the
-    same steps on the reference's own mesh.  The exact affine geometry
-    differs from the reference's transfinite-interpolation geometry in the
-    last bits (metric ~1e-13 relative), which the hydrostatic balance
-    amplifies in the velocity."""
+    same steps on the reference's own mesh: the driver forms the geometry as
+    the reference's mesh app and LoadMesh do, so node coordinates and the
+    fields after the steps agree bit for bit."""
     g = load_golden(fixture)
     visc = float(g["viscosity"])
     fluid = {}
     if "P0" in g:   # the srtb example's constants
         fluid = dict(P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]),
                      gz=float(g["gravity"][2]))
+    if "curved" in g:   # a block with curved edges
+        fluid["curved"] = str(g["curved"])
     d = dump_case(make_case(tmp_path, case, dt=float(g["dt"]), steps=int(g["nsteps"]),
                             viscosity=visc, **fluid))
     d["viscosity"] = visc
@@ -69,14 +83,11 @@ def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
     oracle.set_pow(0)
     rho, U, T = m.segregated(d["fld_rho"], d["fld_U"], d["fld_T"], float(g["dt"]), int(g["nsteps"]))
     kd, kg = node_order(d["cC"], n), node_order(g["cC"], n)
-    assert np.abs(d["cC"].reshape(-1, 3)[kd] - g["cC"].reshape(-1, 3)[:n][kg]).max() < 1e-9
-    assert rel_l2(rho[kd], g["fldN_rho"][kg]) < 1e-13
-    assert rel_l2(np.asarray(T)[kd], g["fldN_T"][kg]) < 1e-10
-    # velocity as one vector field (the horizontal components are tiny in
-    # these rising-bubble cases): measured 2.2e-10 (2D), 3.3e-10 (2D with
-    # viscosity), 9.9e-11 (3D)
+    assert np.array_equal(d["cC"].reshape(-1, 3)[kd], g["cC"].reshape(-1, 3)[:n][kg])
+    assert np.array_equal(rho[kd], g["fldN_rho"][kg])
+    assert np.array_equal(np.asarray(T)[kd], g["fldN_T"][kg])
     Ud, Ug = np.asarray(U).reshape(-1, 3)[kd], g["fldN_U"].reshape(-1, 3)[kg]
-    assert rel_l2(Ud, Ug) < 2e-9
+    assert np.array_equal(Ud, Ug)
 
 
 def test_initial_fields_in_reference_binary_format(tmp_path):
@@ -213,3 +224,38 @@ def test_inclined_block_is_the_rotated_case(tmp_path):
     assert rel_l2(r1, r0) < 1e-14
     assert rel_l2(T1, T0) < 1e-10
     assert rel_l2(np.asarray(U0).reshape(-1, 3) @ R.T, np.asarray(U1).reshape(-1, 3)) < 1e-8
+
+
+@pytest.mark.parametrize("shape", ["cosine", "gaussian", "ridge", "schar"])
+def test_bump_edges_follow_their_shape(tmp_path, shape):
+    """Terrain from the bump edge shapes of the mesh app (hexMesh.cpp:20-45):
+    the bottom vertices of the element columns lie on h f(m) with m the
+    distance from the key point's foot along the edge over the scale (capped
+    at 1/2 except for schar).  The cosine shape is pinned bit for bit against
+    the euler binary by the seg_hill fixture."""
+    d = make_case(tmp_path, "c1_2d", dt=0.01, steps=10, curved="hill")
+    if shape != "cosine":
+        grid = os.path.join(d, "grid")
+        s = open(grid).read().replace("cosine", shape)
+        open(grid, "w").write(s)
+    dd = dump_case(d)
+    npx, npy, npz = (int(v) for v in dd["meta"][:3])
+    NP = npx * npy * npz
+    cC = dd["cC"].reshape(-1, 3)
+    xs, zs = [], []
+    for ix in range(10):
+        e = ix * 10                     # the element at iz = 0 of column ix
+        for li in (0, npx - 1):
+            t = (li * npy + 0) * npz + 0
+            xs.append(cC[e * NP + t, 0])
+            zs.append(cC[e * NP + t, 2])
+    xs, zs = np.array(xs), np.array(zs)
+    m = np.abs(xs / 1000.0 - 0.5) / 0.6
+    if shape != "schar":
+        m = np.minimum(m, 0.5)
+    f = {"cosine": np.cos(np.pi * m) ** 2, "gaussian": np.exp(-16 * m ** 2),
+         "ridge": 1 - 2 * m, "schar": np.exp(-m ** 2) * np.cos(np.pi * m) ** 2}[shape]
+    assert np.abs(zs - 150.0 * f).max() < 1e-9
+    # a genuinely curved metric: the elements over the slope are not affine
+    J = dd["Jinv"].reshape(-1, 9)[: int(dd["meta"][7])]
+    assert np.abs(J[:, 5]).max() > 1e-5 or np.abs(J[:, 8]).max() > 1e-5

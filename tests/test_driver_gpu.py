@@ -50,14 +50,21 @@ def test_segregated_run_matches_oracle(tmp_path, visc):
     assert np.all(g == np.array([0.0, 0.0, -9.81]))
 
 
-def test_srtb_example_run(tmp_path):
+@pytest.mark.parametrize("fixture", ["seg_srtb", "seg_srtb_curved", "seg_hill"])
+def test_srtb_example_run(tmp_path, fixture):
     """The reference's srtb example as shipped (viscosity 1.5, gravity
-    -9.80606, the Fluid:: defaults for P0, cp, cv): the driver's run is the
-    oracle's bit for bit and follows the unmodified euler binary's fields."""
-    g = load_golden("seg_srtb")
+    -9.80606, the Fluid:: defaults for P0, cp, cv), on its box, on the
+    srtb-curved example's arcs and under a cosine hill: the driver's run is the
+    oracle's bit for bit (correctly rounded pow) and follows the unmodified
+    euler binary's fields; the geometry is the binary's to the bit, and the C
+    library's pow, off by an ulp on some arguments, leaves ~1e-15 in rho and
+    ~1e-10 in the velocity of this flow from rest after 100 steps."""
+    g = load_golden(fixture)
     steps = int(g["nsteps"])
+    curved = {"curved": str(g["curved"])} if "curved" in g else {}
     d = make_case(tmp_path, "c1_2d", dt=float(g["dt"]), steps=steps, viscosity=1.5,
-                  P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]), gz=float(g["gravity"][2]))
+                  P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]), gz=float(g["gravity"][2]),
+                  **curved)
     a = dump_case(d)
     a.update({k: g[k] for k in ("P0", "cp", "cv", "R", "gamma", "gravity")})
     a["viscosity"] = 1.5
@@ -74,14 +81,19 @@ def test_srtb_example_run(tmp_path):
     assert np.array_equal(out["T"][:, 0], T)
     n = int(a["meta"][7])
     kd, kg = node_order(a["cC"], n), node_order(g["cC"], n)
+    assert np.array_equal(a["cC"].reshape(-1, 3)[kd], g["cC"].reshape(-1, 3)[:n][kg])
     assert rel_l2(out["rho"][kd, 0], g["fldN_rho"][kg]) < 1e-13
     assert rel_l2(out["T"][kd, 0], g["fldN_T"][kg]) < 1e-10
     assert rel_l2(out["U"][kd], g["fldN_U"].reshape(-1, 3)[kg]) < 2e-9
+    if "curved" in g:
+        r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
+        assert r.returncode == 1 and "axis-aligned" in r.stderr, r.stderr
 
 
 def test_segregated_run_follows_euler_binary(tmp_path):
     """The driver's output files against the unmodified binary's (fixture),
-    node by node through the coordinates: round-off of the geometry."""
+    node by node through the coordinates: the geometry is the binary's to the
+    bit; the correctly rounded pow against the C library's leaves round-off."""
     g = load_golden("seg_c1_2d")
     d = make_case(tmp_path, "c1_2d", dt=float(g["dt"]), steps=int(g["nsteps"]))
     a = dump_case(d)
@@ -207,3 +219,39 @@ def test_inclined_block_run(tmp_path):
     assert np.array_equal(out["T"][:, 0], T)
     r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
     assert r.returncode == 1 and "axis-aligned" in r.stderr, r.stderr
+
+
+def test_text_output_and_high_order(tmp_path):
+    """write_format TEXT: the driver writes `.txt` fields with 12 significant
+    digits, which read back to the binary run's values within 1e-11; and a
+    3D N=7 case through the driver is the oracle's bit for bit."""
+    d = make_case(tmp_path / "txt", "c1_2d", dt=0.005, steps=20)
+    ctl = os.path.join(d, "controls")
+    with open(ctl) as f:
+        s = f.read()
+    with open(ctl, "w") as f:
+        f.write(s.replace("    mesh                         grid",
+                          "    mesh                         grid\n    write_format TEXT"))
+    run_driver(d, "--print-every", "20")
+    txt = {k: read_field(os.path.join(d, f"{k}1.txt")).values for k in ("rho", "U", "T", "p")}
+    b = make_case(tmp_path / "bin", "c1_2d", dt=0.005, steps=20)
+    run_driver(b, "--print-every", "20")
+    bins = fields(b, 1)
+    for k in ("rho", "p"):
+        assert np.abs(txt[k] - bins[k]).max() <= 1e-11 * np.abs(bins[k]).max(), k
+    assert np.abs(txt["U"] - bins["U"]).max() <= 1e-11 * np.abs(bins["U"]).max() + 1e-300
+    assert np.abs(txt["T"] - bins["T"]).max() <= 1e-11 * np.abs(bins["T"]).max()
+
+    d7 = make_case(tmp_path / "n7", "g3_2n7", dt=0.005, steps=10)
+    a = dump_case(d7)
+    run_driver(d7, "--print-every", "5")
+    out = fields(d7, 1, ("rho", "U", "T"))
+    m = oracle.OracleMesh(a)
+    oracle.set_pow(1)
+    try:
+        rho, U, T = m.segregated(a["fld_rho"], a["fld_U"], a["fld_T"], 0.005, 10)
+    finally:
+        oracle.set_pow(0)
+    assert np.array_equal(out["rho"][:, 0], rho)
+    assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
+    assert np.array_equal(out["T"][:, 0], T)
