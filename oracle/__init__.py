@@ -42,6 +42,8 @@ class _Mesh(ctypes.Structure):
         ("gravity", ctypes.c_double * 3),
         ("P0", ctypes.c_double), ("R", ctypes.c_double), ("gamma", ctypes.c_double),
         ("T0", ctypes.c_double), ("nu", ctypes.c_double), ("Pr", ctypes.c_double),
+        ("n_mortar", ctypes.c_int32), ("mortar", ctypes.c_void_p),
+        ("psi_ref", ctypes.c_void_p * 6), ("psi_cor", ctypes.c_void_p * 6),
     ]
 
 
@@ -142,6 +144,18 @@ class OracleMesh:
         s.T0 = float(g.get("T0", 300.0))
         s.nu = float(g.get("viscosity", 0.0))
         s.Pr = float(g.get("Pr", 0.9))
+        # non-conforming faces of a refined mesh (segregated scheme)
+        mort = np.asarray(g["mortar"], dtype=np.uint32).reshape(-1) if "mortar" in g else None
+        s.n_mortar = 0 if mort is None else len(mort) // 4
+        if s.n_mortar:
+            self._keep["mortar"] = np.ascontiguousarray(mort)
+            s.mortar = _ptr(self._keep["mortar"])
+            for d in range(3):
+                for h in range(2):
+                    for nm, arr in (("psiRef", s.psi_ref), ("psiCor", s.psi_cor)):
+                        key = f"{nm}{d}{h}"
+                        self._keep[key] = f64(key)
+                        arr[d * 2 + h] = _ptr(self._keep[key]).value
         self.cv_heat = cv
         self.struct = s
         self.gh = f64("gh") if "gh" in g else None

@@ -130,9 +130,31 @@ def curved_grid(grid, curved, lx, ly, lz):
     return "\n".join(lines)
 
 
+# adaptive refinement of the initial mesh by the reference's prepare -refine
+# (src/field/field.cpp:625-960): cells whose normalised |theta'| indicator
+# reaches field_max are split once (2D: in the x-z plane, direction = the
+# collapsed axis; 3D: direction 0 0 0), leaving 2:1 non-conforming faces
+REFINE = """
+refinement
+{{
+    direction       {direction}
+    field           T
+    field_min       0.01
+    field_max       {field_max}
+    max_level       1
+    limit           100000
+}}
+
+prepare
+{{
+    fields    4 {{ U T p rho }}
+}}
+"""
+
+
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
                Pr=0.9, solver="euler", wind=None, time_scheme="BDF1", P0=100000, cp=1004.5,
-               cv=717.5, gz=-9.81, curved=None):
+               cv=717.5, gz=-9.81, curved=None, refine=None):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
@@ -148,6 +170,9 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
             ctl = ctl.replace("solver                       euler",
                               f"solver                       {solver}")
             ctl += "\n" + solver + "\n{\n    problem_init NONE\n}\n"
+        if refine:
+            ctl += REFINE.format(direction="0 1 0" if dim == 2 else "0 0 0",
+                                 field_max=refine)
         f.write(ctl)
     grid = GRID_2D if dim == 2 else GRID_3D
     grid = grid.format(lx=lx, ly=ly, lz=lz, nx=nx, ny=ny, nz=nz)

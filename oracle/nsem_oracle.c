@@ -142,7 +142,8 @@ static inline double neumann(const nsem_oracle_mesh* m, const double* f, uint32_
     return f[c1] + 0.0 * vmag(dv);
 }
 
-static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G);
+static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G,
+                        const int8_t* side, const double* fS, const double* fC);
 
 static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t* w,
                      double* p_out) {
@@ -201,8 +202,8 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
     const double iPr = visc ? 1 / m->Pr : 0.0;
     if (visc) {
         for (int64_t i = 0; i < n_all; i++) w->mu[i] = w->rho[i] * m->nu;
-        grad_strong(m, 3, w->U, w->GU);
-        grad_strong(m, 1, w->T, w->GT);
+        grad_strong(m, 3, w->U, w->GU, NULL, NULL, NULL);
+        grad_strong(m, 1, w->T, w->GT, NULL, NULL, NULL);
     }
 
     const double gR = gam * R;
@@ -448,6 +449,109 @@ void nsem_oracle_diagnostics(const nsem_oracle_mesh* m, const double* const u[5]
  * the T equation, strong-form DG gradients (euler.cpp:189-190, 232, 250).
  * ------------------------------------------------------------------------ */
 
+/* Non-conforming (2:1) faces of an adaptively refined mesh
+ * (scatter_non_conforming / gather_non_conforming, field.h:2019-2248).  On a
+ * mortar face the coarse cell's side of every face slot is the interpolation
+ * of the coarse face's node values onto the (finer) mortar nodes with psiRef,
+ * and the face values go back to the coarse face's nodes projected with
+ * psiCor; the fine side is conforming. */
+typedef struct {
+    int64_t fi;          /* the face */
+    int fm;              /* 1: the neighbour (FN) side is coarse, 2: the owner (FO) */
+    int a, b, oa, ob;    /* in-plane axes of the coarse face (a < b) and halves */
+    int fix_axis, fix;   /* its normal axis and node index along it */
+    int64_t cbase;       /* first node of the coarse cell */
+} mortar_geo;
+
+static mortar_geo mortar_get(const nsem_oracle_mesh* m, int q) {
+    mortar_geo g;
+    const uint32_t* r = m->mortar + 4 * (size_t)q;
+    const int npd[3] = {m->npx, m->npy, m->npz};
+    const int fid = (int)r[2];
+    g.fi = r[0];
+    g.fm = (int)r[1];
+    g.oa = (int)(r[3] & 1);
+    g.ob = (int)((r[3] >> 1) & 1);
+    if (fid <= 1) { g.a = 0; g.b = 1; g.fix_axis = 2; }
+    else if (fid <= 3) { g.a = 0; g.b = 2; g.fix_axis = 1; }
+    else { g.a = 1; g.b = 2; g.fix_axis = 0; }
+    g.fix = (fid & 1) ? npd[g.fix_axis] - 1 : 0;
+    const int64_t k0 = g.fi * m->npf;
+    const uint32_t cnode = g.fm == 1 ? m->FN[k0] : m->FO[k0];
+    g.cbase = (int64_t)(cnode / (uint32_t)m->np) * m->np;
+    return g;
+}
+
+static int64_t mortar_node(const nsem_oracle_mesh* m, const mortar_geo* g, int na, int nb) {
+    int idx[3];
+    idx[g->a] = na;
+    idx[g->b] = nb;
+    idx[g->fix_axis] = g->fix;
+    return g->cbase + ((int64_t)idx[0] * m->npy + idx[1]) * m->npz + idx[2];
+}
+
+/* per slot: 0 conforming, 1 the owner (FO) side is a mortar's coarse side,
+ * 2 the neighbour (FN) side is */
+static int8_t* mortar_sides(const nsem_oracle_mesh* m) {
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    int8_t* side = calloc((size_t)n_slot, 1);
+    for (int q = 0; q < m->n_mortar; q++) {
+        const mortar_geo g = mortar_get(m, q);
+        for (int32_t n = 0; n < m->npf; n++) side[g.fi * m->npf + n] = (int8_t)(g.fm == 2 ? 1 : 2);
+    }
+    return side;
+}
+
+/* coarse-side value of the node quantity Q (ncomp per node) at every slot of
+ * every mortar face: sum over the coarse face nodes of Q psiRef_a psiRef_b */
+static void mortar_scatter(const nsem_oracle_mesh* m, int ncomp, const double* Q, double* out) {
+    const int npd[3] = {m->npx, m->npy, m->npz};
+    for (int q = 0; q < m->n_mortar; q++) {
+        const mortar_geo g = mortar_get(m, q);
+        const int Na = npd[g.a], Nb = npd[g.b];
+        const double* Pa = m->psi_ref[g.a * 2 + g.oa];
+        const double* Pb = m->psi_ref[g.b * 2 + g.ob];
+        for (int ia = 0; ia < Na; ia++)
+            for (int ib = 0; ib < Nb; ib++) {
+                double sum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int na = 0; na < Na; na++)
+                    for (int nb = 0; nb < Nb; nb++) {
+                        const double* v = Q + (size_t)ncomp * mortar_node(m, &g, na, nb);
+                        const double fa = Pa[na * Na + ia], fb = Pb[nb * Nb + ib];
+                        for (int c = 0; c < ncomp; c++) sum[c] += v[c] * fa * fb;
+                    }
+                const int64_t k = g.fi * m->npf + (int64_t)ia * Nb + ib;
+                for (int c = 0; c < ncomp; c++) out[(size_t)ncomp * k + c] = sum[c];
+            }
+    }
+}
+
+/* face values F (ncomp per slot) of every mortar face projected onto the
+ * coarse face's nodes: out at slot (na, nb) = sum over the mortar slots of
+ * F psiCor_a psiCor_b */
+static void mortar_gather(const nsem_oracle_mesh* m, int ncomp, const double* F, double* out) {
+    const int npd[3] = {m->npx, m->npy, m->npz};
+    for (int q = 0; q < m->n_mortar; q++) {
+        const mortar_geo g = mortar_get(m, q);
+        const int Na = npd[g.a], Nb = npd[g.b];
+        const double* Pa = m->psi_cor[g.a * 2 + g.oa];
+        const double* Pb = m->psi_cor[g.b * 2 + g.ob];
+        const int64_t k0 = g.fi * m->npf;
+        for (int na = 0; na < Na; na++)
+            for (int nb = 0; nb < Nb; nb++) {
+                double sum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int ia = 0; ia < Na; ia++)
+                    for (int ib = 0; ib < Nb; ib++) {
+                        const double* v = F + (size_t)ncomp * (k0 + (int64_t)ia * Nb + ib);
+                        const double fa = Pa[ia * Na + na], fb = Pb[ib * Nb + nb];
+                        for (int c = 0; c < ncomp; c++) sum[c] += v[c] * fa * fb;
+                    }
+                const int64_t k = k0 + (int64_t)na * Nb + nb;
+                for (int c = 0; c < ncomp; c++) out[(size_t)ncomp * k + c] = sum[c];
+            }
+    }
+}
+
 /* ghosts of a scalar (Neumann) and of the velocity (per slot BC) */
 static void ghosts_scalar(const nsem_oracle_mesh* m, double* f) {
     const int64_t n_slot = (int64_t)m->n_face * m->npf;
@@ -481,7 +585,7 @@ static void ghosts_velocity(const nsem_oracle_mesh* m, double* U) {
  * fluxes d (ncomp per slot) in the cell's face order, then the volume term of
  * the nodal flux F (ncomp x 3 per node: Vector flux for ncomp 1, Tensor for 3) */
 static void seg_divf(const nsem_oracle_mesh* m, int ncomp, const double* F, const double* d,
-                     double* r) {
+                     const int8_t* side, const double* dC, double* r) {
     const int32_t NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
     const int64_t n_all = m->n_all;
     const int w = ncomp == 1 ? 3 : 9;
@@ -494,10 +598,13 @@ static void seg_divf(const nsem_oracle_mesh* m, int ncomp, const double* F, cons
             for (int32_t nn = 0; nn < NPF; nn++) {
                 int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
                 uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                /* a mortar's coarse side takes the projected face value */
                 if (c1 >= base && c1 < base + NP) {
-                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c1 + c] += d[ncomp * k + c];
+                    const double* v = (side && side[k] == 1) ? dC : d;
+                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c1 + c] += v[ncomp * k + c];
                 } else if (c2 < (uint32_t)n_all) {
-                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c2 + c] -= d[ncomp * k + c];
+                    const double* v = (side && side[k] == 2) ? dC : d;
+                    for (int c = 0; c < ncomp; c++) r[ncomp * (size_t)c2 + c] -= v[ncomp * k + c];
                 }
             }
         }
@@ -542,7 +649,8 @@ static void seg_divf(const nsem_oracle_mesh* m, int ncomp, const double* F, cons
  * lines, divided by cV; ncomp 1 (Scalar -> Vector) or 3 (Vector -> Tensor in
  * XX..ZX order, G[r][c] = d_r p_c).  Interior nodes only: the ghosts' gradient
  * is set to zero on every wall (fillBCs, field.h:2731-2769). */
-static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G) {
+static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G,
+                        const int8_t* side, const double* fS, const double* fC) {
     const int32_t NPX = m->npx, NPY = m->npy, NPZ = m->npz, NP = m->np, NPF = m->npf;
     const int64_t n_all = m->n_all;
     const int w = ncomp == 1 ? 3 : 9;
@@ -558,13 +666,20 @@ static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, d
                 if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
                 const double fi = m->fI[k], fo = 1 - fi;
                 const double* n = m->fN + 3 * k;
-                double fF[3];
-                for (int c = 0; c < ncomp; c++)
-                    fF[c] = (p[(size_t)ncomp * c1 + c] * fi) + (p[(size_t)ncomp * c2 + c] * fo);
                 uint32_t own;
                 double sg;
                 if (c1 >= base && c1 < base + NP) { own = c1; sg = 1.0; }
                 else { own = c2; sg = -1.0; }
+                double fF[3];
+                if (side && side[k]) {
+                    /* mortar: cds with the coarse side interpolated, projected
+                     * back onto the coarse side's nodes */
+                    const int coarse = (side[k] == 1) == (sg > 0);
+                    for (int c = 0; c < ncomp; c++) fF[c] = (coarse ? fC : fS)[(size_t)ncomp * k + c];
+                } else {
+                    for (int c = 0; c < ncomp; c++)
+                        fF[c] = (p[(size_t)ncomp * c1 + c] * fi) + (p[(size_t)ncomp * c2 + c] * fo);
+                }
                 double d[3], t[9];
                 for (int c = 0; c < ncomp; c++) d[c] = fF[c] - p[(size_t)ncomp * own + c];
                 if (ncomp == 1) {
@@ -610,6 +725,27 @@ static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, d
     }
 }
 
+/* cds of a node quantity p (ncomp per node) on every mortar slot with the
+ * coarse side interpolated (fS), and fS projected back onto the coarse side
+ * (fC): the face values the strong-form gradient lifts on mortar faces */
+static void mortar_cds(const nsem_oracle_mesh* m, int ncomp, const double* p, const int8_t* side,
+                       double* tmp, double* fS, double* fC) {
+    const int64_t n_slot = (int64_t)m->n_face * m->npf;
+    mortar_scatter(m, ncomp, p, tmp);
+    for (int64_t k = 0; k < n_slot; k++) {
+        if (!side[k]) continue;
+        const uint32_t c1 = m->FO[k], c2 = m->FN[k];
+        if (c1 >= (uint32_t)m->n_all || c2 >= (uint32_t)m->n_all) continue;
+        const double fi = m->fI[k], fo = 1 - fi;
+        for (int c = 0; c < ncomp; c++) {
+            const double a = side[k] == 1 ? tmp[(size_t)ncomp * k + c] : p[(size_t)ncomp * c1 + c];
+            const double b = side[k] == 2 ? tmp[(size_t)ncomp * k + c] : p[(size_t)ncomp * c2 + c];
+            fS[(size_t)ncomp * k + c] = (a * fi) + (b * fo);
+        }
+    }
+    mortar_gather(m, ncomp, fS, fC);
+}
+
 void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U_in, double* T_in,
                             double dt, int nsteps) {
     const int64_t n_int = m->n_int, n_all = m->n_all;
@@ -631,6 +767,20 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
     double* mu = visc ? calloc(na, sizeof(double)) : NULL;
     double* G = visc ? calloc(9 * na, sizeof(double)) : NULL;
     const double iPr = visc ? 1 / m->Pr : 0.0;
+    /* non-conforming faces: coarse-side values per slot (ms*), face flux
+     * vectors on mortar slots (mF), their projection (mP), lifted values (dC) */
+    const int mort = m->n_mortar > 0;
+    int8_t* side = mort ? mortar_sides(m) : NULL;
+    double* nq = mort ? calloc(2 * na, sizeof(double)) : NULL;   /* per node |U|, c; rho theta */
+    double* ms = mort ? calloc(9 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* ms2 = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* mF = mort ? calloc(9 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* mP = mort ? calloc(9 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* dC = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* gS = (mort && visc) ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* gC = (mort && visc) ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    /* the coarse side of a mortar slot: 1 = FO, 2 = FN */
+#define SIDE(k) (mort ? side[k] : 0)
     memcpy(rho, rho_in, (size_t)n_int * sizeof(double));
     memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
     memcpy(T, T_in, (size_t)n_int * sizeof(double));
@@ -650,18 +800,32 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fc[3 * i + c] = rho[i] * U[3 * i + c];
         const double gR = gam * R;
+        if (mort) {
+            for (int64_t i = 0; i < n_all; i++) {
+                nq[2 * i] = vmag(U + 3 * i);
+                nq[2 * i + 1] = sqrt(gR * T[i]);
+            }
+            mortar_scatter(m, 2, nq, ms);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
             if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
             const double fi = m->fI[k], fo = 1 - fi;
-            lam[k] = ((vmag(U + 3 * (size_t)c1) * fi + vmag(U + 3 * (size_t)c2) * fo) +
-                      (sqrt(gR * T[c1]) * fi + sqrt(gR * T[c2]) * fo)) / 2;
+            double u1 = vmag(U + 3 * (size_t)c1), u2 = vmag(U + 3 * (size_t)c2);
+            double s1 = sqrt(gR * T[c1]), s2 = sqrt(gR * T[c2]);
+            if (SIDE(k) == 1) { u1 = ms[2 * k]; s1 = ms[2 * k + 1]; }
+            if (SIDE(k) == 2) { u2 = ms[2 * k]; s2 = ms[2 * k + 1]; }
+            lam[k] = ((u1 * fi + u2 * fo) + (s1 * fi + s2 * fo)) / 2;
         }
         /* rho equation: flux U rho, state rho */
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * rho[i];
+        if (mort) {
+            mortar_scatter(m, 3, Fv, ms);
+            mortar_scatter(m, 1, rho, ms2);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
@@ -670,12 +834,23 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             const double* n = m->fN + 3 * k;
             const double mgn = vmag(n);
             const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
-            double F[3], jump = lam[k] * (rho[c2] - rho[c1]);
-            for (int c = 0; c < 3; c++)
-                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            const double* F1 = Fv + 3 * (size_t)c1;
+            const double* F2 = Fv + 3 * (size_t)c2;
+            double r1 = rho[c1], r2 = rho[c2];
+            if (SIDE(k) == 1) { F1 = ms + 3 * k; r1 = ms2[k]; }
+            if (SIDE(k) == 2) { F2 = ms + 3 * k; r2 = ms2[k]; }
+            double F[3], jump = lam[k] * (r2 - r1);
+            for (int c = 0; c < 3; c++) F[c] = (F1[c] * fi + F2[c] * fo) - en[c] * jump;
             d[k] = vdot(F, n);
+            if (SIDE(k))
+                for (int c = 0; c < 3; c++) mF[3 * k + c] = F[c];
         }
-        seg_divf(m, 1, Fv, d, r);
+        if (mort) {
+            mortar_gather(m, 3, mF, mP);
+            for (int64_t k = 0; k < n_slot; k++)
+                if (side[k]) dC[k] = vdot(mP + 3 * k, m->fN + 3 * k);
+        }
+        seg_divf(m, 1, Fv, d, side, dC, r);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap = c_dt * m->cV[i];
@@ -689,7 +864,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) p[i] -= m->p_ref[i];
         /* U equation: flux Fc (x) U + p' I - mu grad U, state rho U */
-        if (visc) grad_strong(m, 3, U, G);
+        if (visc) {
+            if (mort) mortar_cds(m, 3, U, side, mP, gS, gC);
+            grad_strong(m, 3, U, G, side, gS, gC);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) {
             double* Ft = Fv + 9 * i;
@@ -702,6 +880,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             }
             for (int c = 0; c < 3; c++) q[3 * i + c] = rho[i] * U[3 * i + c];
         }
+        if (mort) {
+            mortar_scatter(m, 9, Fv, ms);
+            mortar_scatter(m, 3, q, ms2);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
@@ -710,13 +892,26 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             const double* n = m->fN + 3 * k;
             const double mgn = vmag(n);
             const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
+            const double* A1 = Fv + 9 * (size_t)c1;
+            const double* A2 = Fv + 9 * (size_t)c2;
+            const double* q1 = q + 3 * (size_t)c1;
+            const double* q2 = q + 3 * (size_t)c2;
+            if (SIDE(k) == 1) { A1 = ms + 9 * k; q1 = ms2 + 3 * k; }
+            if (SIDE(k) == 2) { A2 = ms + 9 * k; q2 = ms2 + 3 * k; }
             double dq[3], O[9], F[9];
-            for (int c = 0; c < 3; c++) dq[c] = (q[3 * (size_t)c2 + c] - q[3 * (size_t)c1 + c]) * lam[k];
+            for (int c = 0; c < 3; c++) dq[c] = (q2[c] - q1[c]) * lam[k];
             outer(en, dq, O);
-            for (int c = 0; c < 9; c++) F[c] = (Fv[9 * (size_t)c1 + c] * fi + Fv[9 * (size_t)c2 + c] * fo) - O[c];
+            for (int c = 0; c < 9; c++) F[c] = (A1[c] * fi + A2[c] * fo) - O[c];
             tdot(F, n, d + 3 * k);
+            if (SIDE(k))
+                for (int c = 0; c < 9; c++) mF[9 * k + c] = F[c];
         }
-        seg_divf(m, 3, Fv, d, r);
+        if (mort) {
+            mortar_gather(m, 9, mF, mP);
+            for (int64_t k = 0; k < n_slot; k++)
+                if (side[k]) tdot(mP + 9 * k, m->fN + 3 * k, dC + 3 * k);
+        }
+        seg_divf(m, 3, Fv, d, side, dC, r);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double s = rho[i] - m->rho_ref[i];
@@ -730,7 +925,10 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
         }
         ghosts_velocity(m, U);
         /* T equation: flux Fc T - (mu / Pr) grad T, state rho T (U no longer enters) */
-        if (visc) grad_strong(m, 1, T, G);
+        if (visc) {
+            if (mort) mortar_cds(m, 1, T, side, mP, gS, gC);
+            grad_strong(m, 1, T, G, side, gS, gC);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) {
@@ -738,6 +936,11 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
                 if (visc)
                     Fv[3 * i + c] = Fv[3 * i + c] - (mu[i] * iPr) * (i < n_int ? G[3 * i + c] : 0.0);
             }
+        if (mort) {
+            for (int64_t i = 0; i < n_all; i++) nq[i] = rho[i] * T[i];
+            mortar_scatter(m, 3, Fv, ms);
+            mortar_scatter(m, 1, nq, ms2);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
@@ -746,12 +949,23 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
             const double* n = m->fN + 3 * k;
             const double mgn = vmag(n);
             const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
-            double F[3], jump = lam[k] * (rho[c2] * T[c2] - rho[c1] * T[c1]);
-            for (int c = 0; c < 3; c++)
-                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            const double* F1 = Fv + 3 * (size_t)c1;
+            const double* F2 = Fv + 3 * (size_t)c2;
+            double s1 = rho[c1] * T[c1], s2 = rho[c2] * T[c2];
+            if (SIDE(k) == 1) { F1 = ms + 3 * k; s1 = ms2[k]; }
+            if (SIDE(k) == 2) { F2 = ms + 3 * k; s2 = ms2[k]; }
+            double F[3], jump = lam[k] * (s2 - s1);
+            for (int c = 0; c < 3; c++) F[c] = (F1[c] * fi + F2[c] * fo) - en[c] * jump;
             d[k] = vdot(F, n);
+            if (SIDE(k))
+                for (int c = 0; c < 3; c++) mF[3 * k + c] = F[c];
         }
-        seg_divf(m, 1, Fv, d, r);
+        if (mort) {
+            mortar_gather(m, 3, mF, mP);
+            for (int64_t k = 0; k < n_slot; k++)
+                if (side[k]) dC[k] = vdot(mP + 3 * k, m->fN + 3 * k);
+        }
+        seg_divf(m, 1, Fv, d, side, dC, r);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap0 = c_dt * m->cV[i];
@@ -762,12 +976,14 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++) T[i] -= T0;
     }
+#undef SIDE
     memcpy(rho_in, rho, (size_t)n_int * sizeof(double));
     memcpy(U_in, U, 3 * (size_t)n_int * sizeof(double));
     memcpy(T_in, T, (size_t)n_int * sizeof(double));
     free(rho); free(rhof); free(U); free(T); free(p); free(lam); free(Fv); free(q); free(d);
     free(r); free(Fc);
     free(mu); free(G);
+    free(side); free(nq); free(ms); free(ms2); free(mF); free(mP); free(dC); free(gS); free(gC);
 }
 
 /* The reference's scalar DG convection (apps/convection/convection.cpp with
@@ -815,7 +1031,7 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
                 F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
             d[k] = vdot(F, n);
         }
-        seg_divf(m, 1, Fv, d, r);
+        seg_divf(m, 1, Fv, d, NULL, NULL, r);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap = c_dt * m->cV[i];

@@ -52,6 +52,15 @@ typedef struct {
     double T0;              /* background potential temperature (segregated scheme) */
     double nu, Pr;          /* artificial viscosity (mu = rho nu) and Prandtl number;
                              * nu = 0: diffusion NO (segregated scheme) */
+    /* non-conforming (2:1) faces of an adaptively refined mesh (segregated
+     * scheme): per face {face id, gFMC (1 coarse side FN, 2 coarse side FO),
+     * the coarse cell's face id, halves (bit 0 first in-plane axis, bit 1
+     * second)}; the 2:1 tables psiRef / psiCor per direction d and half h at
+     * [d * 2 + h] (npd * npd each).  n_mortar = 0: conforming mesh. */
+    int32_t n_mortar;
+    const uint32_t* mortar;
+    const double* psi_ref[6];
+    const double* psi_cor[6];
 } nsem_oracle_mesh;
 
 /* pow used for the equation of state: 0 = C library pow (as the reference),

@@ -256,6 +256,62 @@ void dump_geometry() {
         }
     }
     dump_raw("bcU.u32", bcU.data(), nslot);
+
+    /* non-conforming (2:1) faces left by the adaptive refinement: the face,
+     * which side is the coarse cell (gFMC 1: the neighbour, 2: the owner),
+     * the coarse cell's face id and the halves of its face the mortar covers,
+     * found as scatter_non_conforming does (field.h:2135-2248); and the 2:1
+     * interpolation / projection tables psiRef, psiCor (dg.cpp:493-610) */
+    std::vector<Int> mortar;
+    for (Int fi = 0; fi < gNFacets; fi++) {
+        const Int fm = gFMC[fi];
+        if (fm < 1) continue;
+        const Int cn = (fm == 1) ? gFNC[fi] : gFOC[fi];
+        Cell& c = gCells[cn];
+        Int fid = 0;
+        forEach(c, j) {
+            if (c[j] == fi) { fid = gFaceID[cn][j]; break; }
+        }
+        Vector cco = gFC[fi], ccn(0.0);
+        Int nchildren = 0;
+        forEach(c, j) {
+            if (gFaceID[cn][j] == fid) { ccn += gFC[c[j]]; nchildren++; }
+        }
+        ccn /= Scalar(nchildren);
+        Int oa, ob;
+        if (fid == 0 || fid == 1) {
+            const Int k = (fid == 0) ? 0 : (NPZ - 1);
+            Vector v0 = cC[INDEX4(cn, 0, 0, k)], vx = cC[INDEX4(cn, NPX - 1, 0, k)],
+                   vy = cC[INDEX4(cn, 0, NPY - 1, k)];
+            oa = (dot(ccn - v0, vx - v0) >= dot(cco - v0, vx - v0)) ? 0 : 1;
+            ob = (dot(ccn - v0, vy - v0) >= dot(cco - v0, vy - v0)) ? 0 : 1;
+        } else if (fid == 2 || fid == 3) {
+            const Int j = (fid == 2) ? 0 : (NPY - 1);
+            Vector v0 = cC[INDEX4(cn, 0, j, 0)], vx = cC[INDEX4(cn, NPX - 1, j, 0)],
+                   vz = cC[INDEX4(cn, 0, j, NPZ - 1)];
+            oa = (dot(ccn - v0, vx - v0) >= dot(cco - v0, vx - v0)) ? 0 : 1;
+            ob = (dot(ccn - v0, vz - v0) >= dot(cco - v0, vz - v0)) ? 0 : 1;
+        } else {
+            const Int i = (fid == 4) ? 0 : (NPX - 1);
+            Vector v0 = cC[INDEX4(cn, i, 0, 0)], vy = cC[INDEX4(cn, i, NPY - 1, 0)],
+                   vz = cC[INDEX4(cn, i, 0, NPZ - 1)];
+            oa = (dot(ccn - v0, vy - v0) >= dot(cco - v0, vy - v0)) ? 0 : 1;
+            ob = (dot(ccn - v0, vz - v0) >= dot(cco - v0, vz - v0)) ? 0 : 1;
+        }
+        mortar.push_back(fi);
+        mortar.push_back(fm);
+        mortar.push_back(fid);
+        mortar.push_back(oa | (ob << 1));
+    }
+    dump_raw("mortar.u32", mortar.data(), mortar.size());
+    for (int d = 0; d < 3; d++)
+        for (int h = 0; h < 2; h++) {
+            char nm[32];
+            snprintf(nm, sizeof nm, "psiRef%d%d.f64", d, h);
+            dump_raw(nm, psiRef[d * 2 + h], npd[d] * npd[d]);
+            snprintf(nm, sizeof nm, "psiCor%d%d.f64", d, h);
+            dump_raw(nm, psiCor[d * 2 + h], npd[d] * npd[d]);
+        }
 }
 
 }  // namespace

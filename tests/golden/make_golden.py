@@ -70,6 +70,14 @@ SEG_PLAN = {
     "hill": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb", "hill"),
 }
 
+# fixture -> (case, dt, steps, artificial viscosity, refinement threshold) for
+# the segregated scheme on a mesh refined once by the reference's prepare
+# -refine (2:1 non-conforming faces): 2D with viscosity, 3D with 2x2 mortars
+AMR_PLAN = {
+    "c1_2d_visc": ("c1_2d", 0.005, 20, 1.5, 0.3),
+    "g3_4n3": ("g3_4n3", 0.005, 10, 0.0, 0.2),
+}
+
 # fixture -> (case, dt, steps, wind) for the reference's scalar convection app
 CONV_PLAN = {
     "c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0)),
@@ -169,6 +177,46 @@ def make_seg_case(name, ref_bin, tmp):
           f"({os.path.getsize(path) / 1e6:.2f} MB)")
 
 
+def make_amr_case(name, ref_bin, tmp):
+    """Segregated-scheme fixture on an adaptively refined mesh: the mesh app's
+    grid refined once by the reference's prepare -refine, the harness's dump
+    of that mesh (with its non-conforming faces and 2:1 tables) and initial
+    state, and the unmodified euler binary's fields after the steps."""
+    from nebulasem_gb300.fields import read_field
+    base, dt, nsteps, visc, fmax = AMR_PLAN[name]
+    case = os.path.join(tmp, "amr_" + name)
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, refine=fmax, **CASES[base])
+    run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    run([os.path.join(ref_bin, "prepare"), "./controls", "-refine"], case)
+    os.makedirs(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
+    d = load_dump(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler"), "./controls"], case)
+    n_int = int(d["meta"][7])
+    out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    out["mortar"] = d["mortar"]
+    assert len(out["mortar"]) > 0, "no cell was refined"
+    for dd in range(3):
+        for h in range(2):
+            out[f"psiRef{dd}{h}"] = d[f"psiRef{dd}{h}"]
+            out[f"psiCor{dd}{h}"] = d[f"psiCor{dd}{h}"]
+    out["fld0_rho"] = d["fld_rho"][:n_int]
+    out["fld0_U"] = d["fld_U"][:3 * n_int]
+    out["fld0_T"] = d["fld_T"][:n_int]
+    for f in ("rho", "U", "T"):
+        v = read_field(os.path.join(case, f"{f}1.bin")).values
+        assert v.shape[0] == n_int
+        out[f"fldN_{f}"] = v.reshape(-1)
+    out["dt"] = np.float64(dt)
+    out["nsteps"] = np.int64(nsteps)
+    out["viscosity"] = np.float64(visc)
+    out["Pr"] = np.float64(0.9)
+    path = os.path.join(HERE, f"amr_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"amr_{name}: {n_int} interior nodes, {len(out['mortar']) // 4} mortar faces, "
+          f"{nsteps} steps -> {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
 def make_conv_case(name, ref_bin, tmp):
     """Scalar convection fixture: the unmodified reference `convection` app
     (convection.cpp, problem_init NONE, BDF1) on a uniform wind; geometry and
@@ -209,6 +257,7 @@ def main():
     ap.add_argument("--cases", nargs="*", default=sorted(PLAN))
     ap.add_argument("--seg-cases", nargs="*", default=sorted(SEG_PLAN))
     ap.add_argument("--conv-cases", nargs="*", default=sorted(CONV_PLAN))
+    ap.add_argument("--amr-cases", nargs="*", default=sorted(AMR_PLAN))
     ap.add_argument("-j", type=int, default=8)
     a = ap.parse_args()
     subprocess.run(["make", "-f", "oracle/Makefile.ref", f"REF={a.ref}", f"-j{a.j}"],
@@ -222,6 +271,8 @@ def main():
             make_seg_case(name, ref_bin, tmp)
         for name in a.conv_cases:
             make_conv_case(name, ref_bin, tmp)
+        for name in a.amr_cases:
+            make_amr_case(name, ref_bin, tmp)
     finally:
         shutil.rmtree(tmp)
 
