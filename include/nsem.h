@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define NSEM_ABI_VERSION 3
+#define NSEM_ABI_VERSION 4
 
 typedef enum {
     NSEM_OK = 0,
@@ -89,6 +89,19 @@ typedef struct nsem_mesh_desc {
     const uint32_t* bc_U;       /* [n_face*npf] velocity BC per slot:
                                    0 none, 1 NEUMANN, 2 SYMMETRY; scalars
                                    (rho, T, p) are NEUMANN wherever bc_U != 0 */
+    /* Non-conforming (2:1) faces left by the adaptive refinement
+     * (Mesh::gFMC >= 1; scatter_non_conforming / gather_non_conforming,
+     * field.h:2019-2248).  n_mortar = 0 (and NULL pointers) on a conforming
+     * mesh.  Only NSEM_REF_SEGREGATED steps a mesh with n_mortar > 0.
+     * mortar[4*q .. 4*q+3]: the facet, gFMC (1: the neighbour side FN is the
+     * coarse cell, 2: the owner side FO), the coarse cell's face id
+     * (gFaceID, 0..5), and the halves of that face the facet covers (bit 0
+     * along the face's first in-plane axis x|x|y for ids 0-1|2-3|4-5, bit 1
+     * along the second y|z|z), as scatter_non_conforming finds them. */
+    int32_t n_mortar;
+    const uint32_t* mortar;
+    const double* psi_ref[6];   /* DG::psiRef[d*2+half] [npd*npd] */
+    const double* psi_cor[6];   /* DG::psiCor[d*2+half] [npd*npd] */
 } nsem_mesh_desc;
 
 typedef struct nsem_params {

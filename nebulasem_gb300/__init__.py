@@ -44,6 +44,8 @@ class MeshDesc(ctypes.Structure):
         ("face_idx0", ctypes.c_void_p), ("face_idx1", ctypes.c_void_p),
         ("psi", ctypes.c_void_p * 3), ("dpsi", ctypes.c_void_p * 3),
         ("bc_U", ctypes.c_void_p),
+        ("n_mortar", ctypes.c_int32), ("mortar", ctypes.c_void_p),
+        ("psi_ref", ctypes.c_void_p * 6), ("psi_cor", ctypes.c_void_p * 6),
     ]
 
 
@@ -164,6 +166,17 @@ class Solver:
         for d in range(3):
             md.psi[d] = keep[f"psi{d}"].ctypes.data
             md.dpsi[d] = keep[f"dpsi{d}"].ctypes.data
+        # non-conforming faces of an adaptively refined mesh (the harness's
+        # `mortar` and psiRef/psiCor dumps)
+        if "mortar" in mesh and len(mesh["mortar"]):
+            keep["mortar"] = _u32(mesh["mortar"])
+            md.n_mortar = len(keep["mortar"]) // 4
+            md.mortar = _p(keep["mortar"])
+            for d in range(3):
+                for h in range(2):
+                    for nm, arr in (("psiRef", md.psi_ref), ("psiCor", md.psi_cor)):
+                        keep[f"{nm}{d}{h}"] = _f64(mesh[f"{nm}{d}{h}"])
+                        arr[d * 2 + h] = keep[f"{nm}{d}{h}"].ctypes.data
         pr = Params()
         pr.P0, pr.T0, pr.cp, pr.cv, pr.dt = P0, T0, cp, cv, dt
         for c in range(3):

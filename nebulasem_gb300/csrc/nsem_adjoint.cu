@@ -312,7 +312,7 @@ __global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const
         for (int j = 0; j < 3; j++) {
             const int32_t code = m.lift[(int64_t)j * m.n_int + node];
             if (code < 0) break;
-            const int64_t k = code >> 1;
+            const int64_t k = code >> 2;
             const double f = (code & 1) ? 1.0 - m.fi[k] : m.fi[k];
             const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
             const double dm[3] = {a.dbv[0][k], a.dbv[1][k], a.dbv[2][k]}, dt = a.dbv[3][k];
@@ -362,7 +362,7 @@ __global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const
     for (int j = 0; j < 3; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t k = code >> 2;
         const double* const* src = (code & 1) ? a.adjN : a.adjO;
         rbar += src[0][k]; Ub[0] += src[1][k]; Ub[1] += src[2][k]; Ub[2] += src[3][k];
         Tb += src[4][k]; pb += src[5][k];
@@ -627,7 +627,7 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
     for (int j = 0; j < 3; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t k = code >> 2;
         const double sg = (code & 1) ? -1.0 : 1.0;
         for (int v = 0; v < 5; v++) r[v] += sg * a.dd[v][k];
     }
@@ -777,7 +777,7 @@ __global__ void k_adj_grad_vol(const NsemDev m, const NsemTables tab, GradAdjArg
     for (int j = 0; j < 3; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t k = code >> 2;
         const double* const* src = (code & 1) ? a.agN : a.agO;
         for (int c = 0; c < 4; c++) pb[c] += src[c][k];
     }

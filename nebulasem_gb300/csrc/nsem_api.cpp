@@ -59,6 +59,15 @@ nsem_status fail(nsem_ctx* c, nsem_status s, const std::string& msg) {
     return s;
 }
 
+/* the forms other than the reference's segregated scheme assume conforming
+ * faces (at most 3 face slots per node) */
+nsem_status require_conforming(nsem_ctx* c) {
+    if (c && c->dev.n_ms > 0)
+        return fail(c, NSEM_UNSUPPORTED,
+                    "non-conforming (2:1) faces: only NSEM_REF_SEGREGATED steps this mesh");
+    return NSEM_OK;
+}
+
 nsem_status cuda_fail(nsem_ctx* c, cudaError_t e, const char* where) {
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     return fail(c, NSEM_CUDA_ERROR, m);
@@ -178,9 +187,58 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
     }
     D.n_slot = (int64_t)c1.size();
 
-    /* per-node lift lists in div_flux order (field.h:3097-3113) */
-    std::vector<int32_t> lift(3 * n_int, -1);
-    std::vector<int> cnt(n_int, 0);
+    /* non-conforming faces: per used slot of a mortar face the coarse side
+     * (1: FO, 2: FN) and its mortar slot; mortar slots numbered face by face,
+     * (ia, ib) row-major over the face's in-plane node counts */
+    std::vector<int8_t> mside(n_slot_all, 0);
+    std::vector<int32_t> ms_full(n_slot_all, -1);
+    std::vector<int32_t> msi[NSEM_MS_FIELDS];
+    if (m->n_mortar < 0 || (m->n_mortar > 0 && !m->mortar))
+        return fail(ctx, NSEM_BAD_ARG, "mortar faces: bad count or NULL list");
+    if (m->n_mortar > 0) {
+        for (int t = 0; t < 6; t++)
+            if (!m->psi_ref[t] || !m->psi_cor[t])
+                return fail(ctx, NSEM_BAD_ARG, "mortar faces need psi_ref / psi_cor");
+        const int64_t stride[3] = {(int64_t)m->npy * m->npz, m->npz, 1};
+        for (int32_t q = 0; q < m->n_mortar; q++) {
+            const uint32_t* r = m->mortar + 4 * (size_t)q;
+            const int64_t fi = r[0];
+            const int fm = (int)r[1], fid = (int)r[2];
+            if (fi >= m->n_face || (fm != 1 && fm != 2) || fid > 5 || r[3] > 3)
+                return fail(ctx, NSEM_BAD_ARG, "mortar face entry out of range");
+            int a, b, fix;
+            if (fid <= 1) { a = 0; b = 1; fix = 2; }
+            else if (fid <= 3) { a = 0; b = 2; fix = 1; }
+            else { a = 1; b = 2; fix = 0; }
+            const int Na = npd[a], Nb = npd[b];
+            if ((int64_t)Na * Nb > m->npf) return fail(ctx, NSEM_BAD_ARG, "mortar face larger than npf");
+            const uint32_t cnode = fm == 1 ? m->FN[fi * m->npf] : m->FO[fi * m->npf];
+            if (cnode >= (uint64_t)n_int) return fail(ctx, NSEM_BAD_ARG, "mortar coarse cell is not interior");
+            const int64_t cell = cnode / NP;
+            const int64_t base = cell * NP + ((fid & 1) ? npd[fix] - 1 : 0) * stride[fix];
+            const int32_t first = (int32_t)msi[0].size();
+            for (int ia = 0; ia < Na; ia++)
+                for (int ib = 0; ib < Nb; ib++) {
+                    const int64_t k = fi * m->npf + (int64_t)ia * Nb + ib;
+                    if (compact[k] < 0) return fail(ctx, NSEM_BAD_ARG, "mortar slot unused");
+                    if (m->FN[k] >= (uint64_t)n_int) return fail(ctx, NSEM_BAD_ARG, "mortar face on a boundary");
+                    if (ms_full[k] >= 0) return fail(ctx, NSEM_BAD_ARG, "mortar face listed twice");
+                    ms_full[k] = (int32_t)msi[0].size();
+                    mside[k] = (int8_t)(fm == 2 ? 1 : 2);
+                    const int32_t f[NSEM_MS_FIELDS] = {
+                        (int32_t)compact[k], fm == 2 ? 1 : 2, (int32_t)base,
+                        (int32_t)stride[a], (int32_t)stride[b], Na, Nb,
+                        2 * a + (int)(r[3] & 1), 2 * b + (int)((r[3] >> 1) & 1), ia, ib, first};
+                    for (int c = 0; c < NSEM_MS_FIELDS; c++) msi[c].push_back(f[c]);
+                }
+        }
+    }
+    D.n_ms = (int64_t)msi[0].size();
+
+    /* per-node lift lists in div_flux order (field.h:3097-3113): the used slot
+     * (or, on a mortar's coarse side, the mortar slot) << 2, bit 1 the coarse
+     * side, bit 0 subtract */
+    std::vector<std::vector<int32_t>> lists(n_int);
     for (int64_t e = 0; e < m->n_elem; e++) {
         const int64_t lo = e * NP, hi = lo + NP;
         for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
@@ -196,12 +254,20 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
                 if (node < lo || node >= hi)
                     return fail(ctx, NSEM_BAD_ARG, "face slot does not belong to its cell");
                 if (compact[k] < 0) return fail(ctx, NSEM_BAD_ARG, "lift from an unused slot");
-                if (cnt[node] >= 3) return fail(ctx, NSEM_BAD_ARG, "node on more than 3 faces");
-                lift[(int64_t)cnt[node] * n_int + node] = (int32_t)((compact[k] << 1) | neg);
-                cnt[node]++;
+                const bool coarse = mside[k] == (neg ? 2 : 1);
+                const int64_t idx = coarse ? ms_full[k] : compact[k];
+                if (idx >= (int64_t)1 << 29) return fail(ctx, NSEM_UNSUPPORTED, "more than 2^29 face slots");
+                lists[node].push_back((int32_t)((idx << 2) | (coarse ? 2 : 0) | neg));
             }
         }
     }
+    size_t n_lift = 3;
+    for (const auto& l : lists) n_lift = std::max(n_lift, l.size());
+    if (m->n_mortar == 0 && n_lift > 3) return fail(ctx, NSEM_BAD_ARG, "node on more than 3 faces");
+    D.n_lift = (int32_t)n_lift;
+    std::vector<int32_t> lift(n_lift * n_int, -1);
+    for (int64_t i = 0; i < n_int; i++)
+        for (size_t j = 0; j < lists[i].size(); j++) lift[(int64_t)j * n_int + i] = lists[i][j];
 
     /* node arrays: Jinv*cV (field.h:3445), cV, background */
     std::vector<double> jin(9 * n_int), cv(n_int), pref(n_int), rref(n_int), gh(n_int);
@@ -226,6 +292,24 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
     UP(D.rho_ref, rref);
     UP(D.gh, gh);
     UP(D.lift, lift);
+    if (D.n_ms > 0) {
+        std::vector<int32_t> ms_of(D.n_slot, -1), ms_i;
+        for (int64_t k = 0; k < n_slot_all; k++)
+            if (ms_full[k] >= 0) ms_of[compact[k]] = ms_full[k];
+        for (int c = 0; c < NSEM_MS_FIELDS; c++) ms_i.insert(ms_i.end(), msi[c].begin(), msi[c].end());
+        std::vector<double> pr(6 * NSEM_MAX_NPD * NSEM_MAX_NPD, 0.0), pc(pr.size(), 0.0);
+        for (int t = 0; t < 6; t++) {
+            const int n = npd[t / 2];
+            for (int q = 0; q < n * n; q++) {
+                pr[t * NSEM_MAX_NPD * NSEM_MAX_NPD + q] = m->psi_ref[t][q];
+                pc[t * NSEM_MAX_NPD * NSEM_MAX_NPD + q] = m->psi_cor[t][q];
+            }
+        }
+        UP(D.ms_of, ms_of);
+        UP(D.ms_i, ms_i);
+        UP(D.psir, pr);
+        UP(D.psic, pc);
+    }
     UP(D.c1, c1);
     UP(D.c2, c2);
     UP(D.bc, bc);
@@ -296,6 +380,17 @@ nsem_status seg_alloc(nsem_ctx* ctx) {
             if ((s = dalloc(ctx, &S.G[c], n)) != NSEM_OK) return s;
         for (int c = 0; c < 4; c++)
             if ((s = dalloc(ctx, &S.fF[c], ns)) != NSEM_OK) return s;
+    }
+    if (ctx->dev.n_ms > 0) {
+        const size_t nm = (size_t)ctx->dev.n_ms;
+        for (int c = 0; c < 16; c++)
+            if ((s = dalloc(ctx, &S.mq[c], nm)) != NSEM_OK) return s;
+        for (int c = 0; c < 12; c++)
+            if ((s = dalloc(ctx, &S.mf[c], nm)) != NSEM_OK) return s;
+        for (int c = 0; c < 5; c++)
+            if ((s = dalloc(ctx, &S.dC[c], nm)) != NSEM_OK) return s;
+        for (int c = 0; c < 4; c++)
+            if ((s = dalloc(ctx, &S.gC[c], nm)) != NSEM_OK) return s;
     }
     const int e = nsem_seg_prepare(&ctx->dev);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "segregated-scheme shared memory");
@@ -532,6 +627,7 @@ nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
 
 nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5],
                           double* p_prime) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!L) return fail(ctx, NSEM_BAD_ARG, "L is NULL");
     for (int c = 0; c < 5; c++) if (!L[c]) return fail(ctx, NSEM_BAD_ARG, "L[c] is NULL");
@@ -564,6 +660,7 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
 }
 
 nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec) {
+    if (ctx && ctx->dev.n_ms > 0 && scheme != NSEM_REF_SEGREGATED) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
     if (scheme != NSEM_SSPRK3 && scheme != NSEM_REF_SEGREGATED)
@@ -692,6 +789,7 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
 }
 
 extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
@@ -712,6 +810,7 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
 }
 
 extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
     for (int v = 0; v < 5; v++)
@@ -733,6 +832,7 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
 
 extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
                                 double* const du_final[5], double* ms_tlm) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
     if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
@@ -800,6 +900,7 @@ extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const d
 
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
@@ -847,6 +948,7 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
 
 extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                     double* const lam0[5], double* ms_adj) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
     NsemAdjBuf& A = ctx->abuf;
@@ -920,6 +1022,7 @@ extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final
 /* --------------------------------------------------- scalar convection */
 
 extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const double* T) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!U || !T) return fail(ctx, NSEM_BAD_ARG, "U or T is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
@@ -947,6 +1050,7 @@ extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const
 }
 
 extern "C" nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
     NsemConvBuf& C = ctx->cbuf;
@@ -991,6 +1095,7 @@ extern "C" nsem_status nsem_convection_get(nsem_ctx* ctx, double* T) {
 
 nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double ms[8],
                          int launches[8], char names[8 * 32]) {
+    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!ms || !launches || !names) return fail(ctx, NSEM_BAD_ARG, "output pointer is NULL");
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps < 1");

@@ -256,7 +256,7 @@ __global__ void k_volume(const NsemDev m, const NsemTables tab, VolArgs a) {
     for (int j = 0; j < 3; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t k = code >> 2;
         if (code & 1) {
             r0 -= a.d[0][k]; r1 -= a.d[1][k]; r2 -= a.d[2][k]; r3 -= a.d[3][k]; r4 -= a.d[4][k];
         } else {

@@ -28,6 +28,13 @@ struct NsemTables {
     double dpsi[3][NSEM_MAX_NPD * NSEM_MAX_NPD]; /* dpsi[d][s*npd + i] = l_i'(x_s) */
 };
 
+/* per mortar slot (ms_i rows): its used slot, the coarse side (1: c1, 2: c2),
+ * the coarse face's node (0, 0), node strides and node counts along the face's
+ * two in-plane axes, their 2:1 table ids (axis * 2 + half), the slot's position
+ * on the face, and the face's first mortar slot */
+enum { NSEM_MS_K, NSEM_MS_SIDE, NSEM_MS_BASE, NSEM_MS_SA, NSEM_MS_SB, NSEM_MS_NA, NSEM_MS_NB,
+       NSEM_MS_TA, NSEM_MS_TB, NSEM_MS_IA, NSEM_MS_IB, NSEM_MS_FIRST, NSEM_MS_FIELDS };
+
 struct NsemDev {
     int32_t npx, npy, npz, np;
     int64_t n_elem, n_int, n_slot;
@@ -41,7 +48,14 @@ struct NsemDev {
     double* rho_ref;
     double* p_ref;
     double* gh;
-    int32_t* lift;     /* [3][n_int] */
+    int32_t* lift;     /* [n_lift][n_int]: (index << 2) | (mortar coarse side << 1) | subtract */
+    int32_t n_lift;    /* entries per node: 3 on a conforming mesh */
+    /* non-conforming (2:1) faces, segregated scheme only */
+    int64_t n_ms;      /* mortar slots (0: conforming mesh) */
+    int32_t* ms_of;    /* [n_slot] mortar slot of a used slot, -1 */
+    int32_t* ms_i;     /* [NSEM_MS_FIELDS][n_ms], fields below */
+    double* psir;      /* [6][NSEM_MAX_NPD^2] DG::psiRef, row stride npd */
+    double* psic;      /* [6][NSEM_MAX_NPD^2] DG::psiCor */
     /* slot arrays */
     int32_t* c1;
     int32_t* c2;

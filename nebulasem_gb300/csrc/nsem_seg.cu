@@ -117,9 +117,129 @@ struct SegArgs {
     double* d[5];            /* per slot */
     double* G[12];           /* per node: grad U, grad theta (viscous runs) */
     double* fF[4];           /* per slot: cds(U), cds(theta) (viscous runs) */
+    /* non-conforming faces, per mortar slot */
+    double* mq[16];          /* the coarse side's interpolated quantities */
+    double* mf[12];          /* face flux vectors / tensors */
+    double* dC[5];           /* projected, lifted coarse-side fluxes */
+    double* gC[4];           /* projected cds(U), cds(theta) */
     double c_dt;             /* -1 / dt */
     int visc;
 };
+
+/* Non-conforming (2:1) faces (scatter_non_conforming / gather_non_conforming,
+ * field.h:2019-2248): on a mortar face the coarse cell's side of each face
+ * quantity is interpolated from the coarse face's nodes onto the mortar nodes
+ * (psiRef along the face's two axes), and the face values are projected back
+ * onto the coarse face's nodes (psiCor) before the coarse cell lifts them.
+ * One thread per mortar slot. */
+__device__ __forceinline__ int32_t ms_field(const NsemDev& m, int f, int64_t ms) {
+    return m.ms_i[(int64_t)f * m.n_ms + ms];
+}
+
+/* sum over the coarse face's nodes of Q(node) psiRef_a psiRef_b, in the
+ * reference's order (coarse index along a outer, along b inner) */
+template <int NQ, typename Q>
+__device__ __forceinline__ void mortar_interp(const NsemDev& m, int64_t ms, Q q, double* out) {
+    const int base = ms_field(m, NSEM_MS_BASE, ms), sa = ms_field(m, NSEM_MS_SA, ms),
+              sb = ms_field(m, NSEM_MS_SB, ms), Na = ms_field(m, NSEM_MS_NA, ms),
+              Nb = ms_field(m, NSEM_MS_NB, ms), ia = ms_field(m, NSEM_MS_IA, ms),
+              ib = ms_field(m, NSEM_MS_IB, ms);
+    const double* Pa = m.psir + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Pb = m.psir + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    for (int c = 0; c < NQ; c++) out[c] = 0.0;
+    for (int na = 0; na < Na; na++)
+        for (int nb = 0; nb < Nb; nb++) {
+            double v[NQ];
+            q((int64_t)base + na * sa + nb * sb, v);
+            const double fa = Pa[na * Na + ia], fb = Pb[nb * Nb + ib];
+            for (int c = 0; c < NQ; c++) out[c] += v[c] * fa * fb;
+        }
+}
+
+/* projection of the face's values src (NC arrays over its mortar slots) onto
+ * this slot's coarse node: sum over the face's slots of src psiCor_a psiCor_b */
+template <int NC>
+__device__ __forceinline__ void mortar_project(const NsemDev& m, int64_t ms, double* const* src,
+                                               double* out) {
+    const int Na = ms_field(m, NSEM_MS_NA, ms), Nb = ms_field(m, NSEM_MS_NB, ms),
+              na = ms_field(m, NSEM_MS_IA, ms), nb = ms_field(m, NSEM_MS_IB, ms),
+              first = ms_field(m, NSEM_MS_FIRST, ms);
+    const double* Pa = m.psic + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Pb = m.psic + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    for (int c = 0; c < NC; c++) out[c] = 0.0;
+    for (int ja = 0; ja < Na; ja++)
+        for (int jb = 0; jb < Nb; jb++) {
+            const int64_t s2 = first + ja * Nb + jb;
+            const double fa = Pa[ja * Na + na], fb = Pb[jb * Nb + nb];
+            for (int c = 0; c < NC; c++) out[c] += src[c][s2] * fa * fb;
+        }
+}
+
+/* rho equation and lambda: |U|, c, U rho, rho of the coarse side */
+__global__ void __launch_bounds__(128) k_seg_mortar_rho(const NsemDev m, SegArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    double out[6];
+    mortar_interp<6>(m, ms, [&](int64_t node, double* v) {
+        const double r = a.rho_o[node];
+        v[0] = a.mu[node];
+        v[1] = a.cs[node];
+        for (int c = 0; c < 3; c++) v[2 + c] = a.U[c][node] * r;
+        v[5] = r;
+    }, out);
+    for (int c = 0; c < 6; c++) a.mq[c][ms] = out[c];
+}
+
+/* U and theta equations: the flux tensor Fc (x) U + p' I - mu grad U, the
+ * state rho U, the flux Fc theta - (mu / Pr) grad theta, the state rho theta
+ * of the coarse side */
+__global__ void __launch_bounds__(128) k_seg_mortar_ut(const NsemDev m, SegArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    double out[16];
+    mortar_interp<16>(m, ms, [&](int64_t node, double* v) {
+        const double rn = a.rho_n[node];
+        const double U[3] = {a.U[0][node], a.U[1][node], a.U[2][node]};
+        const double Fc[3] = {a.Fc[0][node], a.Fc[1][node], a.Fc[2][node]};
+        const double Tf = a.Tf[node], p = a.pp[node];
+        const double mu = a.visc ? a.rho_o[node] * m.nu : 0.0;
+        outer(Fc, U, v);
+        for (int c = 0; c < 9; c++) v[c] = v[c] + ((c < 3) ? 1.0 : 0.0) * p;
+        if (a.visc)
+            for (int c = 0; c < 9; c++) v[c] = v[c] - mu * a.G[c][node];
+        for (int c = 0; c < 3; c++) v[9 + c] = rn * U[c];
+        for (int c = 0; c < 3; c++) {
+            v[12 + c] = Fc[c] * Tf;
+            if (a.visc) v[12 + c] = v[12 + c] - (mu * m.iPr) * a.G[9 + c][node];
+        }
+        v[15] = rn * Tf;
+    }, out);
+    for (int c = 0; c < 16; c++) a.mq[c][ms] = out[c];
+}
+
+/* the coarse side's lifted values: the projected flux vectors dotted with the
+ * slot's own weighted normal (div_flux, field.h:3086-3117) */
+template <int EQ>
+__global__ void __launch_bounds__(128) k_seg_mortar_gather(const NsemDev m, SegArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    if (EQ == 0) {
+        double F[3];
+        mortar_project<3>(m, ms, a.mf, F);
+        a.dC[0][ms] = vdot3(F, n);
+    } else {
+        double F[9], FT[3], out[3];
+        mortar_project<9>(m, ms, a.mf, F);
+        mortar_project<3>(m, ms, a.mf + 9, FT);
+        tdot(F, n, out);
+        a.dC[1][ms] = out[0];
+        a.dC[2][ms] = out[1];
+        a.dC[3][ms] = out[2];
+        a.dC[4][ms] = vdot3(FT, n);
+    }
+}
 
 __global__ void __launch_bounds__(256) k_seg_prep(const NsemDev m, SegArgs a) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,15 +274,33 @@ __global__ void __launch_bounds__(256) k_seg_face_rho(const NsemDev m, SegArgs a
         mu2 = sqrt(vdot3(U2, U2));
         cs2 = sqrt(m.gR * (a.Tf[c1] + 0.0));
     }
-    const double lam = ((mu1 * fi + mu2 * fo) + (cs1 * fi + cs2 * fo)) / 2;
+    double X1[3], X2[3];
+    for (int c = 0; c < 3; c++) {
+        X1[c] = U1[c] * r1;
+        X2[c] = U2[c] * r2;
+    }
+    /* a mortar's coarse side: interpolated from the coarse face's nodes */
+    const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+    double mu1v = mu1, cs1v = cs1, r1v = r1;
+    if (ms >= 0) {
+        const bool own = ms_field(m, NSEM_MS_SIDE, ms) == 1;
+        double* mu_ = own ? &mu1v : &mu2;
+        double* cs_ = own ? &cs1v : &cs2;
+        double* r_ = own ? &r1v : &r2;
+        double* X = own ? X1 : X2;
+        *mu_ = a.mq[0][ms];
+        *cs_ = a.mq[1][ms];
+        for (int c = 0; c < 3; c++) X[c] = a.mq[2 + c][ms];
+        *r_ = a.mq[5][ms];
+    }
+    const double lam = ((mu1v * fi + mu2 * fo) + (cs1v * fi + cs2 * fo)) / 2;
     a.lam[k] = lam;
     double F[3];
-    const double jump = lam * (r2 - r1);
-    for (int c = 0; c < 3; c++) {
-        const double x = U1[c] * r1, y = U2[c] * r2;
-        F[c] = (x * fi + y * fo) - en[c] * jump;
-    }
+    const double jump = lam * (r2 - r1v);
+    for (int c = 0; c < 3; c++) F[c] = (X1[c] * fi + X2[c] * fo) - en[c] * jump;
     a.d[0][k] = vdot3(F, n);
+    if (ms >= 0)
+        for (int c = 0; c < 3; c++) a.mf[c][ms] = F[c];
 }
 
 /* weak volume term of one node, sources in the reference's scatter order */
@@ -178,7 +316,47 @@ struct GradArgs {
     const double* Tf;        /* full potential temperature */
     double* G[12];           /* per node: grad U (XX..ZX), grad theta */
     double* fF[4];           /* per slot: cds(U), cds(theta) */
+    double* gC[4];           /* per mortar slot: the projection onto the coarse side */
 };
+
+/* mortar faces: cds(U), cds(theta) with the coarse side interpolated (over
+ * the conforming values of k_seg_grad_face), then projected back */
+__global__ void __launch_bounds__(128) k_seg_mortar_gcds(const NsemDev m, GradArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    double I[4];
+    mortar_interp<4>(m, ms, [&](int64_t node, double* v) {
+        for (int c = 0; c < 3; c++) v[c] = a.U[c][node];
+        v[3] = a.Tf[node];
+    }, I);
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const bool own = ms_field(m, NSEM_MS_SIDE, ms) == 1;
+    const double fi = m.fi[k], fo = 1 - fi;
+    const int64_t fine = own ? m.c2[k] : m.c1[k];
+    for (int c = 0; c < 4; c++) {
+        const double pf = c < 3 ? a.U[c][fine] : a.Tf[fine];
+        const double p1 = own ? I[c] : pf, p2 = own ? pf : I[c];
+        a.fF[c][k] = (p1 * fi) + (p2 * fo);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_seg_mortar_ggather(const NsemDev m, GradArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int Na = ms_field(m, NSEM_MS_NA, ms), Nb = ms_field(m, NSEM_MS_NB, ms),
+              na = ms_field(m, NSEM_MS_IA, ms), nb = ms_field(m, NSEM_MS_IB, ms),
+              first = ms_field(m, NSEM_MS_FIRST, ms);
+    const double* Pa = m.psic + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Pb = m.psic + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    double out[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int ja = 0; ja < Na; ja++)
+        for (int jb = 0; jb < Nb; jb++) {
+            const int64_t k2 = ms_field(m, NSEM_MS_K, first + ja * Nb + jb);
+            const double fa = Pa[ja * Na + na], fb = Pb[jb * Nb + nb];
+            for (int c = 0; c < 4; c++) out[c] += a.fF[c][k2] * fa * fb;
+        }
+    for (int c = 0; c < 4; c++) a.gC[c][ms] = out[c];
+}
 
 /* cds(U), cds(theta) per slot for the gradients */
 __global__ void __launch_bounds__(256) k_seg_grad_face(const NsemDev m, GradArgs a) {
@@ -225,14 +403,19 @@ __global__ void k_seg_grad_vol(const NsemDev m, const NsemTables tab, GradArgs a
     double gU[9], gT[3];
     for (int c = 0; c < 9; c++) gU[c] = 0.0;
     for (int c = 0; c < 3; c++) gT[c] = 0.0;
-    /* face terms, in the cell's face order */
-    for (int j = 0; j < 3; j++) {
+    /* face terms, in the cell's face order; a mortar's coarse side takes the
+     * projected face values */
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t idx = code >> 2;
+        const bool coarse = code & 2;
+        const int64_t k = coarse ? ms_field(m, NSEM_MS_K, idx) : idx;
+        double f4[4];
+        for (int c = 0; c < 4; c++) f4[c] = coarse ? a.gC[c][idx] : a.fF[c][k];
         const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
-        const double dU[3] = {a.fF[0][k] - me[0], a.fF[1][k] - me[1], a.fF[2][k] - me[2]};
-        const double dT = a.fF[3][k] - me[3];
+        const double dU[3] = {f4[0] - me[0], f4[1] - me[1], f4[2] - me[2]};
+        const double dT = f4[3] - me[3];
         double tU[9];
         outer(n, dU, tU);
         if (code & 1) {
@@ -312,12 +495,13 @@ __global__ void k_seg_vol_rho(const NsemDev m, const NsemTables tab, SegArgs a) 
     __syncthreads();
     if (!active) return;
     double r = 0.0;
-    for (int j = 0; j < 3; j++) {
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
-        if (code & 1) r -= a.d[0][k];
-        else r += a.d[0][k];
+        const int64_t idx = code >> 2;
+        const double v = (code & 2) ? a.dC[0][idx] : a.d[0][idx];
+        if (code & 1) r -= v;
+        else r += v;
     }
     volume_gather<W_RHO, 3>(m, sm, dps, t, [&](int lb, const double* dj) {
         r -= vdot3(sm + (size_t)lb * W_RHO, dj);
@@ -359,9 +543,12 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
     /* artificial viscosity mu = rho^n nu; the wall ghosts' gradient is zero */
     const double mu1 = a.visc ? a.rho_o[c1] * m.nu : 0.0;
     const double mu2 = a.visc ? (c2 >= 0 ? a.rho_o[c2] : a.rho_o[c1] + 0.0) * m.nu : 0.0;
+    /* a mortar's coarse side: interpolated from the coarse face's nodes */
+    const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+    const int mside = ms >= 0 ? ms_field(m, NSEM_MS_SIDE, ms) : 0;
     /* U equation: flux Fc (x) U + p' I - mu grad U, state rho U */
     {
-        double A[9], B[9], O[9], F[9], dq[3], out[3];
+        double A[9], B[9], O[9], F[9], dq[3], out[3], q1[3], q2[3];
         outer(Fc1, U1, A);
         outer(Fc2, U2, B);
         for (int c = 0; c < 9; c++) {
@@ -374,27 +561,48 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
                 A[c] = A[c] - mu1 * a.G[c][c1];
                 B[c] = B[c] - mu2 * (c2 >= 0 ? a.G[c][c2] : 0.0);
             }
-        for (int c = 0; c < 3; c++) dq[c] = (r2 * U2[c] - r1 * U1[c]) * lam;
+        for (int c = 0; c < 3; c++) {
+            q1[c] = r1 * U1[c];
+            q2[c] = r2 * U2[c];
+        }
+        if (mside) {
+            double* Am = mside == 1 ? A : B;
+            double* qm = mside == 1 ? q1 : q2;
+            for (int c = 0; c < 9; c++) Am[c] = a.mq[c][ms];
+            for (int c = 0; c < 3; c++) qm[c] = a.mq[9 + c][ms];
+        }
+        for (int c = 0; c < 3; c++) dq[c] = (q2[c] - q1[c]) * lam;
         outer(en, dq, O);
         for (int c = 0; c < 9; c++) F[c] = (A[c] * fi + B[c] * fo) - O[c];
         tdot(F, n, out);
         a.d[1][k] = out[0];
         a.d[2][k] = out[1];
         a.d[3][k] = out[2];
+        if (mside)
+            for (int c = 0; c < 9; c++) a.mf[c][ms] = F[c];
     }
     /* T equation: flux Fc theta - (mu / Pr) grad theta, state rho theta */
     {
-        double F[3];
-        const double jump = lam * (r2 * T2 - r1 * T1);
+        double F[3], x[3], y[3];
+        double s1 = r1 * T1, s2 = r2 * T2;
         for (int c = 0; c < 3; c++) {
-            double x = Fc1[c] * T1, y = Fc2[c] * T2;
+            x[c] = Fc1[c] * T1;
+            y[c] = Fc2[c] * T2;
             if (a.visc) {
-                x = x - (mu1 * m.iPr) * a.G[9 + c][c1];
-                y = y - (mu2 * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
+                x[c] = x[c] - (mu1 * m.iPr) * a.G[9 + c][c1];
+                y[c] = y[c] - (mu2 * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
             }
-            F[c] = (x * fi + y * fo) - en[c] * jump;
         }
+        if (mside) {
+            double* fm = mside == 1 ? x : y;
+            for (int c = 0; c < 3; c++) fm[c] = a.mq[12 + c][ms];
+            (mside == 1 ? s1 : s2) = a.mq[15][ms];
+        }
+        const double jump = lam * (s2 - s1);
+        for (int c = 0; c < 3; c++) F[c] = (x[c] * fi + y[c] * fo) - en[c] * jump;
         a.d[4][k] = vdot3(F, n);
+        if (mside)
+            for (int c = 0; c < 3; c++) a.mf[9 + c][ms] = F[c];
     }
 }
 
@@ -428,14 +636,15 @@ __global__ void k_seg_vol_ut(const NsemDev m, const NsemTables tab, SegArgs a) {
     __syncthreads();
     if (!active) return;
     double r1 = 0.0, r2 = 0.0, r3 = 0.0, r4 = 0.0;
-    for (int j = 0; j < 3; j++) {
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t idx = code >> 2;
+        double* const* src = (code & 2) ? a.dC : a.d;
         if (code & 1) {
-            r1 -= a.d[1][k]; r2 -= a.d[2][k]; r3 -= a.d[3][k]; r4 -= a.d[4][k];
+            r1 -= src[1][idx]; r2 -= src[2][idx]; r3 -= src[3][idx]; r4 -= src[4][idx];
         } else {
-            r1 += a.d[1][k]; r2 += a.d[2][k]; r3 += a.d[3][k]; r4 += a.d[4][k];
+            r1 += src[1][idx]; r2 += src[2][idx]; r3 += src[3][idx]; r4 += src[4][idx];
         }
     }
     volume_gather<W_UT, 12>(m, sm, dps, t, [&](int lb, const double* dj) {
@@ -507,6 +716,10 @@ SegArgs seg_args(const NsemDev* m, NsemSegBuf* b, int cur, double dt) {
     for (int c = 0; c < 5; c++) a.d[c] = b->d[c];
     for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
     for (int c = 0; c < 4; c++) a.fF[c] = b->fF[c];
+    for (int c = 0; c < 16; c++) a.mq[c] = b->mq[c];
+    for (int c = 0; c < 12; c++) a.mf[c] = b->mf[c];
+    for (int c = 0; c < 5; c++) a.dC[c] = b->dC[c];
+    for (int c = 0; c < 4; c++) a.gC[c] = b->gC[c];
     a.c_dt = -1.0 / dt;
     a.visc = m->nu != 0.0;
     return a;
@@ -601,7 +814,7 @@ __global__ void k_conv_vol(const NsemDev m, const NsemTables tab, AdvArgs a) {
     for (int j = 0; j < 3; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
-        const int64_t k = code >> 1;
+        const int64_t k = code >> 2;
         if (code & 1) r -= a.d[k];
         else r += a.d[k];
     }
@@ -638,6 +851,7 @@ int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, 
     ga.Tf = T;
     for (int c = 0; c < 12; c++) ga.G[c] = G[c];
     for (int c = 0; c < 4; c++) ga.fF[c] = fF[c];
+    for (int c = 0; c < 4; c++) ga.gC[c] = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     const int threads = ((m->np + 31) / 32) * 32;
     k_seg_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
@@ -652,6 +866,7 @@ int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U,
     ga.Tf = T;
     for (int c = 0; c < 12; c++) ga.G[c] = G[c];
     for (int c = 0; c < 4; c++) ga.fF[c] = const_cast<double*>(fF[c]);
+    for (int c = 0; c < 4; c++) ga.gC[c] = nullptr;
     const int threads = ((m->np + 31) / 32) * 32;
     k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), (cudaStream_t)stream>>>(*m, *t, ga);
     return (int)cudaGetLastError();
@@ -708,6 +923,8 @@ int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nst
     const unsigned nb = (unsigned)((m->n_int + 255) / 256);
     const unsigned sb = (unsigned)((m->n_slot + 255) / 256);
     const int threads = ((m->np + 31) / 32) * 32;
+    const bool mort = m->n_ms > 0;
+    const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
     int cur = b->cur;
     for (int s = 0; s < nsteps; s++) {
         const SegArgs a = seg_args(m, b, cur, dt);
@@ -718,12 +935,21 @@ int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nst
             ga.Tf = a.Tf;
             for (int c = 0; c < 12; c++) ga.G[c] = a.G[c];
             for (int c = 0; c < 4; c++) ga.fF[c] = a.fF[c];
+            for (int c = 0; c < 4; c++) ga.gC[c] = a.gC[c];
             k_seg_grad_face<<<sb, 256, 0, st>>>(*m, ga);
+            if (mort) {
+                k_seg_mortar_gcds<<<mb, 128, 0, st>>>(*m, ga);
+                k_seg_mortar_ggather<<<mb, 128, 0, st>>>(*m, ga);
+            }
             k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, ga);
         }
+        if (mort) k_seg_mortar_rho<<<mb, 128, 0, st>>>(*m, a);
         k_seg_face_rho<<<sb, 256, 0, st>>>(*m, a);
+        if (mort) k_seg_mortar_gather<0><<<mb, 128, 0, st>>>(*m, a);
         k_seg_vol_rho<<<(unsigned)m->n_elem, threads, smem_rho(m), st>>>(*m, *t, a);
+        if (mort) k_seg_mortar_ut<<<mb, 128, 0, st>>>(*m, a);
         k_seg_face_ut<<<sb, 256, 0, st>>>(*m, a);
+        if (mort) k_seg_mortar_gather<1><<<mb, 128, 0, st>>>(*m, a);
         k_seg_vol_ut<<<(unsigned)m->n_elem, threads, smem_ut(m), st>>>(*m, *t, a);
         const int e = (int)cudaGetLastError();
         if (e) return e;

@@ -23,6 +23,11 @@ struct NsemSegBuf {
     /* artificial viscosity (diffusion YES) */
     double* G[12] = {};           /* per node: grad U (XX..ZX), grad theta  */
     double* fF[4] = {};           /* per slot: cds(U), cds(theta)           */
+    /* non-conforming faces, per mortar slot */
+    double* mq[16] = {};          /* coarse side's interpolated quantities  */
+    double* mf[12] = {};          /* face flux vectors / tensors            */
+    double* dC[5] = {};           /* projected, lifted coarse-side fluxes   */
+    double* gC[4] = {};           /* projected cds(U), cds(theta)           */
 };
 
 /* scalar DG convection (the reference's convection app): T in a fixed wind */
