@@ -175,68 +175,86 @@ __device__ __forceinline__ void mortar_project(const NsemDev& m, int64_t ms, dou
         }
 }
 
+/* One thread per (mortar slot, quantity): each sum is a short dependent
+ * chain over the coarse face's nodes, so the slots' quantities run side by
+ * side. */
+
 /* rho equation and lambda: |U|, c, U rho, rho of the coarse side */
 __global__ void __launch_bounds__(128) k_seg_mortar_rho(const NsemDev m, SegArgs a) {
-    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (ms >= m.n_ms) return;
-    double out[6];
-    mortar_interp<6>(m, ms, [&](int64_t node, double* v) {
-        const double r = a.rho_o[node];
-        v[0] = a.mu[node];
-        v[1] = a.cs[node];
-        for (int c = 0; c < 3; c++) v[2 + c] = a.U[c][node] * r;
-        v[5] = r;
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 6 * m.n_ms) return;
+    const int64_t ms = id / 6;
+    const int c = (int)(id % 6);
+    double out[1];
+    mortar_interp<1>(m, ms, [&](int64_t node, double* v) {
+        if (c == 0) v[0] = a.mu[node];
+        else if (c == 1) v[0] = a.cs[node];
+        else if (c == 5) v[0] = a.rho_o[node];
+        else v[0] = a.U[c - 2][node] * a.rho_o[node];
     }, out);
-    for (int c = 0; c < 6; c++) a.mq[c][ms] = out[c];
+    a.mq[c][ms] = out[0];
 }
 
 /* U and theta equations: the flux tensor Fc (x) U + p' I - mu grad U, the
  * state rho U, the flux Fc theta - (mu / Pr) grad theta, the state rho theta
- * of the coarse side */
+ * of the coarse side (component c of 16) */
 __global__ void __launch_bounds__(128) k_seg_mortar_ut(const NsemDev m, SegArgs a) {
-    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (ms >= m.n_ms) return;
-    double out[16];
-    mortar_interp<16>(m, ms, [&](int64_t node, double* v) {
-        const double rn = a.rho_n[node];
-        const double U[3] = {a.U[0][node], a.U[1][node], a.U[2][node]};
-        const double Fc[3] = {a.Fc[0][node], a.Fc[1][node], a.Fc[2][node]};
-        const double Tf = a.Tf[node], p = a.pp[node];
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 16 * m.n_ms) return;
+    const int64_t ms = id / 16;
+    const int c = (int)(id % 16);
+    /* outer(Fc, U) components XX YY ZZ XY YZ XZ YX ZY ZX */
+    const int ra = c < 9 ? (c < 3 ? c : (c == 3 || c == 5) ? 0 : (c == 4 || c == 6) ? 1 : 2) : 0;
+    const int rb = c < 9 ? (c < 3 ? c : (c == 6 || c == 8) ? 0 : (c == 3 || c == 7) ? 1 : 2) : 0;
+    double out[1];
+    mortar_interp<1>(m, ms, [&](int64_t node, double* v) {
         const double mu = a.visc ? a.rho_o[node] * m.nu : 0.0;
-        outer(Fc, U, v);
-        for (int c = 0; c < 9; c++) v[c] = v[c] + ((c < 3) ? 1.0 : 0.0) * p;
-        if (a.visc)
-            for (int c = 0; c < 9; c++) v[c] = v[c] - mu * a.G[c][node];
-        for (int c = 0; c < 3; c++) v[9 + c] = rn * U[c];
-        for (int c = 0; c < 3; c++) {
-            v[12 + c] = Fc[c] * Tf;
-            if (a.visc) v[12 + c] = v[12 + c] - (mu * m.iPr) * a.G[9 + c][node];
+        if (c < 9) {
+            double x = a.Fc[ra][node] * a.U[rb][node];
+            x = x + ((c < 3) ? 1.0 : 0.0) * a.pp[node];
+            if (a.visc) x = x - mu * a.G[c][node];
+            v[0] = x;
+        } else if (c < 12) {
+            v[0] = a.rho_n[node] * a.U[c - 9][node];
+        } else if (c < 15) {
+            double x = a.Fc[c - 12][node] * a.Tf[node];
+            if (a.visc) x = x - (mu * m.iPr) * a.G[9 + c - 12][node];
+            v[0] = x;
+        } else {
+            v[0] = a.rho_n[node] * a.Tf[node];
         }
-        v[15] = rn * Tf;
     }, out);
-    for (int c = 0; c < 16; c++) a.mq[c][ms] = out[c];
+    a.mq[c][ms] = out[0];
 }
 
 /* the coarse side's lifted values: the projected flux vectors dotted with the
- * slot's own weighted normal (div_flux, field.h:3086-3117) */
+ * slot's own weighted normal (div_flux, field.h:3086-3117); for the U and
+ * theta equations one thread per (mortar slot, output row) */
 template <int EQ>
 __global__ void __launch_bounds__(128) k_seg_mortar_gather(const NsemDev m, SegArgs a) {
-    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (ms >= m.n_ms) return;
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int rows = EQ == 0 ? 1 : 4;
+    if (id >= rows * m.n_ms) return;
+    const int64_t ms = id / rows;
+    const int r = (int)(id % rows);
     const int64_t k = ms_field(m, NSEM_MS_K, ms);
     const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
     if (EQ == 0) {
         double F[3];
         mortar_project<3>(m, ms, a.mf, F);
         a.dC[0][ms] = vdot3(F, n);
+    } else if (r < 3) {
+        /* row r of the tensor-vector product: components (r,x) (r,y) (r,z) */
+        const int cx = r == 0 ? XX : r == 1 ? YX : ZX;
+        const int cy = r == 0 ? XY : r == 1 ? YY : ZY;
+        const int cz = r == 0 ? XZ : r == 1 ? YZ : ZZ;
+        double* src[3] = {a.mf[cx], a.mf[cy], a.mf[cz]};
+        double P[3];
+        mortar_project<3>(m, ms, src, P);
+        a.dC[1 + r][ms] = P[0] * n[0] + P[1] * n[1] + P[2] * n[2];
     } else {
-        double F[9], FT[3], out[3];
-        mortar_project<9>(m, ms, a.mf, F);
+        double FT[3];
         mortar_project<3>(m, ms, a.mf + 9, FT);
-        tdot(F, n, out);
-        a.dC[1][ms] = out[0];
-        a.dC[2][ms] = out[1];
-        a.dC[3][ms] = out[2];
         a.dC[4][ms] = vdot3(FT, n);
     }
 }
@@ -943,13 +961,13 @@ int nsem_seg_steps(const NsemDev* m, const NsemTables* t, NsemSegBuf* b, int nst
             }
             k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, ga);
         }
-        if (mort) k_seg_mortar_rho<<<mb, 128, 0, st>>>(*m, a);
+        if (mort) k_seg_mortar_rho<<<6 * mb, 128, 0, st>>>(*m, a);
         k_seg_face_rho<<<sb, 256, 0, st>>>(*m, a);
         if (mort) k_seg_mortar_gather<0><<<mb, 128, 0, st>>>(*m, a);
         k_seg_vol_rho<<<(unsigned)m->n_elem, threads, smem_rho(m), st>>>(*m, *t, a);
-        if (mort) k_seg_mortar_ut<<<mb, 128, 0, st>>>(*m, a);
+        if (mort) k_seg_mortar_ut<<<16 * mb, 128, 0, st>>>(*m, a);
         k_seg_face_ut<<<sb, 256, 0, st>>>(*m, a);
-        if (mort) k_seg_mortar_gather<1><<<mb, 128, 0, st>>>(*m, a);
+        if (mort) k_seg_mortar_gather<1><<<4 * mb, 128, 0, st>>>(*m, a);
         k_seg_vol_ut<<<(unsigned)m->n_elem, threads, smem_ut(m), st>>>(*m, *t, a);
         const int e = (int)cudaGetLastError();
         if (e) return e;

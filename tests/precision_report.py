@@ -131,16 +131,25 @@ def run_gpu(name, dt, steps, adjoint_ckpt=0, with_oracle=False, viscosity=0.0):
     return out
 
 
-def run_segregated(name, dt, steps, with_oracle=False):
+def run_segregated(name, dt, steps, with_oracle=False, fixture=None):
     """The reference's own update (segregated forward Euler) on the GPU from the
-    workload's fields; throughput and, with the oracle, bitwise comparison."""
+    workload's fields (or a golden fixture's mesh and step-0 fields, e.g. an
+    adaptively refined mesh); throughput and, with the oracle, bitwise
+    comparison."""
     import nebulasem_gb300 as ng
-    from nebulasem_gb300.mesh import workload
-    m, u0 = workload(name)
-    n = int(m["meta"][7])
-    rho = u0[0]
-    U = np.stack([u0[1] / rho, u0[2] / rho, u0[3] / rho], axis=1)
-    T = u0[4] / rho - 300.0
+    if fixture:
+        from conftest import load_golden
+        m = load_golden(fixture)
+        n = int(m["meta"][7])
+        rho, U, T = m["fld0_rho"], m["fld0_U"].reshape(n, 3), m["fld0_T"]
+        name = fixture
+    else:
+        from nebulasem_gb300.mesh import workload
+        m, u0 = workload(name)
+        n = int(m["meta"][7])
+        rho = u0[0]
+        U = np.stack([u0[1] / rho, u0[2] / rho, u0[3] / rho], axis=1)
+        T = u0[4] / rho - 300.0
     s = ng.Solver(m, dt=dt)
     out = dict(workload=name, scheme="REF_SEGREGATED", dt=dt, steps=steps, nodes=n, dof=5 * n)
     for rep in range(2):
@@ -221,7 +230,9 @@ def run_oracle(name, dt, steps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", required=True)
+    ap.add_argument("--workload", default="")
+    ap.add_argument("--fixture", default=None,
+                    help="segregated scheme on a golden fixture's mesh (e.g. amr_g3_4n3)")
     ap.add_argument("--dt", type=float, required=True)
     ap.add_argument("--steps", type=int, required=True)
     ap.add_argument("--oracle", action="store_true")
@@ -235,7 +246,7 @@ def main():
                     help="also time the FP64 adjoint with checkpoints every k steps")
     a = ap.parse_args()
     if a.scheme == "seg":
-        r = run_segregated(a.workload, a.dt, a.steps, a.with_oracle)
+        r = run_segregated(a.workload, a.dt, a.steps, a.with_oracle, a.fixture)
     elif a.scheme == "conv":
         r = run_convection(a.workload, a.dt, a.steps, a.with_oracle)
     elif a.oracle:
