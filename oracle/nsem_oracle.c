@@ -103,6 +103,10 @@ typedef struct {
     double *d_rho, *d_mom, *d_th; /* per-slot lifted fluxes                */
     double *r_rho, *r_mom, *r_th; /* residuals on n_all nodes              */
     double *mu, *GU, *GT;         /* artificial viscosity: rho nu, grad U, grad theta */
+    /* non-conforming faces: coarse-side slot values, node quantities, face
+     * flux vectors, their projection, projected lifted values, gradient cds */
+    int8_t* side;
+    double *mq, *nq, *mF, *mP, *dC, *gS, *gC, *gT;
 } work_t;
 
 static void work_alloc(const nsem_oracle_mesh* m, work_t* w) {
@@ -124,6 +128,8 @@ static void work_alloc(const nsem_oracle_mesh* m, work_t* w) {
         w->GU = calloc(na * 9, sizeof(double));
         w->GT = calloc(na * 3, sizeof(double));
     }
+    w->side = NULL;
+    w->mq = w->nq = w->mF = w->mP = w->dC = w->gS = w->gC = w->gT = NULL;
 }
 
 static void work_free(work_t* w) {
@@ -131,6 +137,8 @@ static void work_free(work_t* w) {
     free(w->d_rho); free(w->d_mom); free(w->d_th);
     free(w->r_rho); free(w->r_mom); free(w->r_th);
     free(w->mu); free(w->GU); free(w->GT);
+    free(w->side); free(w->mq); free(w->nq); free(w->mF); free(w->mP); free(w->dC);
+    free(w->gS); free(w->gC); free(w->gT);
 }
 
 /* NEUMANN (value 0) ghost: interior value + 0*|dv| (field.h:2674-2676). */
@@ -144,6 +152,16 @@ static inline double neumann(const nsem_oracle_mesh* m, const double* f, uint32_
 
 static void grad_strong(const nsem_oracle_mesh* m, int ncomp, const double* p, double* G,
                         const int8_t* side, const double* fS, const double* fC);
+static int8_t* mortar_sides(const nsem_oracle_mesh* m);
+static void mortar_scatter(const nsem_oracle_mesh* m, int ncomp, const double* Q, double* out);
+static void mortar_gather(const nsem_oracle_mesh* m, int ncomp, const double* F, double* out);
+static void mortar_cds(const nsem_oracle_mesh* m, int ncomp, const double* p, const int8_t* side,
+                       double* tmp, double* fS, double* fC);
+
+/* the coupled residual's node quantities a mortar's coarse side interpolates:
+ * |U|, c, U rho (3), rho, the momentum flux tensor (9), the theta flux (3),
+ * rho theta */
+#define NQ_COUPLED 19
 
 static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t* w,
                      double* p_out) {
@@ -200,13 +218,56 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
      * mu = rho nu; strong-form gradients of U and theta, zero on wall ghosts */
     const int visc = m->nu != 0.0;
     const double iPr = visc ? 1 / m->Pr : 0.0;
+    /* non-conforming faces (scatter_non_conforming / gather_non_conforming) */
+    const int mort = m->n_mortar > 0;
+    if (mort && !w->side) {
+        const size_t na = (size_t)n_all + (size_t)NP;
+        w->side = mortar_sides(m);
+        w->mq = calloc((size_t)NQ_COUPLED * n_slot, sizeof(double));
+        w->nq = calloc((size_t)NQ_COUPLED * na, sizeof(double));
+        w->mF = calloc(15 * (size_t)n_slot, sizeof(double));
+        w->mP = calloc(15 * (size_t)n_slot, sizeof(double));
+        w->dC = calloc(5 * (size_t)n_slot, sizeof(double));
+        w->gS = calloc(3 * (size_t)n_slot, sizeof(double));
+        w->gC = calloc(3 * (size_t)n_slot, sizeof(double));
+        w->gT = calloc(9 * (size_t)n_slot, sizeof(double));
+    }
+    const int8_t* side = w->side;
     if (visc) {
         for (int64_t i = 0; i < n_all; i++) w->mu[i] = w->rho[i] * m->nu;
-        grad_strong(m, 3, w->U, w->GU, NULL, NULL, NULL);
-        grad_strong(m, 1, w->T, w->GT, NULL, NULL, NULL);
+        if (mort) mortar_cds(m, 3, w->U, side, w->gT, w->gS, w->gC);
+        grad_strong(m, 3, w->U, w->GU, side, w->gS, w->gC);
+        if (mort) mortar_cds(m, 1, w->T, side, w->gT, w->gS, w->gC);
+        grad_strong(m, 1, w->T, w->GT, side, w->gS, w->gC);
     }
 
     const double gR = gam * R;
+    if (mort) {
+        /* the coarse sides' node quantities, interpolated onto every mortar slot */
+        for (int64_t i = 0; i < n_int; i++) {
+            double* q = w->nq + (size_t)NQ_COUPLED * i;
+            const double* U = w->U + 3 * i;
+            const double r = w->rho[i], T = w->T[i];
+            q[0] = vmag(U);
+            q[1] = sqrt(gR * T);
+            for (int c = 0; c < 3; c++) q[2 + c] = U[c] * r;
+            q[5] = r;
+            double Fc[3] = {U[0] * r, U[1] * r, U[2] * r}, A[9];
+            outer(Fc, U, A);
+            for (int c = 0; c < 9; c++) {
+                A[c] = A[c] + ((c < 3) ? 1.0 : 0.0) * w->p[i];
+                if (visc) A[c] = A[c] - w->mu[i] * w->GU[9 * i + c];
+                q[6 + c] = A[c];
+            }
+            for (int c = 0; c < 3; c++) {
+                double a = (U[c] * r) * T;
+                if (visc) a = a - (w->mu[i] * iPr) * w->GT[3 * i + c];
+                q[15 + c] = a;
+            }
+            q[18] = r * T;
+        }
+        mortar_scatter(m, NQ_COUPLED, w->nq, w->mq);
+    }
     /* face slots: Rusanov fluxes of the three equations dotted with fN */
 #pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < n_slot; k++) {
@@ -217,24 +278,34 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
         const double mgn = vmag(n);
         const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
         const double *U1 = w->U + 3 * (size_t)c1, *U2 = w->U + 3 * (size_t)c2;
-        const double r1 = w->rho[c1], r2 = w->rho[c2];
         const double T1 = w->T[c1], T2 = w->T[c2];
         const double p1 = w->p[c1], p2 = w->p[c2];
-        double lam = ((vmag(U1) * fi + vmag(U2) * fo) +
-                      (sqrt(gR * T1) * fi + sqrt(gR * T2) * fo)) / 2;
+        /* a mortar's coarse side (1: owner, 2: neighbour) takes interpolated values */
+        const int ms = mort ? side[k] : 0;
+        const double* mq = mort ? w->mq + (size_t)NQ_COUPLED * k : NULL;
+        double r1 = w->rho[c1], r2 = w->rho[c2];
+        double u1 = vmag(U1), u2 = vmag(U2), s1 = sqrt(gR * T1), s2 = sqrt(gR * T2);
+        if (ms == 1) { u1 = mq[0]; s1 = mq[1]; r1 = mq[5]; }
+        if (ms == 2) { u2 = mq[0]; s2 = mq[1]; r2 = mq[5]; }
+        double lam = ((u1 * fi + u2 * fo) + (s1 * fi + s2 * fo)) / 2;
         /* rho: flux U*rho, state rho */
         {
             double F[3], jump = lam * (r2 - r1);
             for (int c = 0; c < 3; c++) {
-                double a = U1[c] * r1, b = U2[c] * r2;
+                double a = U1[c] * w->rho[c1], b = U2[c] * w->rho[c2];
+                if (ms == 1) a = mq[2 + c];
+                if (ms == 2) b = mq[2 + c];
                 F[c] = (a * fi + b * fo) - en[c] * jump;
             }
             w->d_rho[k] = vdot(F, n);
+            if (ms)
+                for (int c = 0; c < 3; c++) w->mF[15 * k + c] = F[c];
         }
         /* momentum: flux (rho U) (x) U + p' I, state rho U */
         {
-            double Fc1[3] = {U1[0] * r1, U1[1] * r1, U1[2] * r1};
-            double Fc2[3] = {U2[0] * r2, U2[1] * r2, U2[2] * r2};
+            const double ra = w->rho[c1], rb = w->rho[c2];
+            double Fc1[3] = {U1[0] * ra, U1[1] * ra, U1[2] * ra};
+            double Fc2[3] = {U2[0] * rb, U2[1] * rb, U2[2] * rb};
             double T1t[9], T2t[9], F[9], O[9];
             outer(Fc1, U1, T1t);
             outer(Fc2, U2, T2t);
@@ -250,24 +321,53 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
                     T2t[c] = T2t[c] - w->mu[c2] * (g2 ? w->GU[9 * (size_t)c2 + c] : 0.0);
                 }
             }
+            if (ms) {
+                double* Tm = ms == 1 ? T1t : T2t;
+                double* Fm = ms == 1 ? Fc1 : Fc2;
+                for (int c = 0; c < 9; c++) Tm[c] = mq[6 + c];
+                for (int c = 0; c < 3; c++) Fm[c] = mq[2 + c];
+            }
             double dq[3];
             for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
             outer(en, dq, O);
             for (int c = 0; c < 9; c++) F[c] = (T1t[c] * fi + T2t[c] * fo) - O[c];
             tdot(F, n, w->d_mom + 3 * k);
+            if (ms)
+                for (int c = 0; c < 9; c++) w->mF[15 * k + 3 + c] = F[c];
         }
         /* rho theta: flux (rho U) theta, state rho theta */
         {
-            double F[3], jump = lam * (r2 * T2 - r1 * T1);
+            const double ra = w->rho[c1], rb = w->rho[c2];
+            double q1 = ra * T1, q2 = rb * T2;
+            if (ms == 1) q1 = mq[18];
+            if (ms == 2) q2 = mq[18];
+            double F[3], jump = lam * (q2 - q1);
             for (int c = 0; c < 3; c++) {
-                double a = (U1[c] * r1) * T1, b = (U2[c] * r2) * T2;
+                double a = (U1[c] * ra) * T1, b = (U2[c] * rb) * T2;
                 if (visc) {
                     a = a - (w->mu[c1] * iPr) * (c1 < (uint32_t)n_int ? w->GT[3 * (size_t)c1 + c] : 0.0);
                     b = b - (w->mu[c2] * iPr) * (c2 < (uint32_t)n_int ? w->GT[3 * (size_t)c2 + c] : 0.0);
                 }
+                if (ms == 1) a = mq[15 + c];
+                if (ms == 2) b = mq[15 + c];
                 F[c] = (a * fi + b * fo) - en[c] * jump;
             }
             w->d_th[k] = vdot(F, n);
+            if (ms)
+                for (int c = 0; c < 3; c++) w->mF[15 * k + 12 + c] = F[c];
+        }
+    }
+    if (mort) {
+        /* the coarse sides' lifted values: projected flux vectors dotted with
+         * the slot's own weighted normal */
+        mortar_gather(m, 15, w->mF, w->mP);
+        for (int64_t k = 0; k < n_slot; k++) {
+            if (!side[k]) continue;
+            const double* P = w->mP + 15 * k;
+            const double* n = m->fN + 3 * k;
+            w->dC[5 * k] = vdot(P, n);
+            tdot(P + 3, n, w->dC + 5 * k + 1);
+            w->dC[5 * k + 4] = vdot(P + 12, n);
         }
     }
 
@@ -288,13 +388,27 @@ static void residual(const nsem_oracle_mesh* m, const double* const u[5], work_t
                 int64_t k = (int64_t)m->all_faces[f] * NPF + nn;
                 uint32_t c1 = m->FO[k], c2 = m->FN[k];
                 if (c1 >= base && c1 < base + NP) {
-                    w->r_rho[c1] += w->d_rho[k];
-                    for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c1 + c] += w->d_mom[3 * k + c];
-                    w->r_th[c1] += w->d_th[k];
+                    if (side && side[k] == 1) {
+                        const double* v = w->dC + 5 * k;
+                        w->r_rho[c1] += v[0];
+                        for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c1 + c] += v[1 + c];
+                        w->r_th[c1] += v[4];
+                    } else {
+                        w->r_rho[c1] += w->d_rho[k];
+                        for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c1 + c] += w->d_mom[3 * k + c];
+                        w->r_th[c1] += w->d_th[k];
+                    }
                 } else if (c2 < (uint32_t)n_all) {
-                    w->r_rho[c2] -= w->d_rho[k];
-                    for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c2 + c] -= w->d_mom[3 * k + c];
-                    w->r_th[c2] -= w->d_th[k];
+                    if (side && side[k] == 2) {
+                        const double* v = w->dC + 5 * k;
+                        w->r_rho[c2] -= v[0];
+                        for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c2 + c] -= v[1 + c];
+                        w->r_th[c2] -= v[4];
+                    } else {
+                        w->r_rho[c2] -= w->d_rho[k];
+                        for (int c = 0; c < 3; c++) w->r_mom[3 * (size_t)c2 + c] -= w->d_mom[3 * k + c];
+                        w->r_th[c2] -= w->d_th[k];
+                    }
                 }
             }
         }
@@ -506,6 +620,7 @@ static int8_t* mortar_sides(const nsem_oracle_mesh* m) {
  * every mortar face: sum over the coarse face nodes of Q psiRef_a psiRef_b */
 static void mortar_scatter(const nsem_oracle_mesh* m, int ncomp, const double* Q, double* out) {
     const int npd[3] = {m->npx, m->npy, m->npz};
+    if (ncomp > 32) abort();
     for (int q = 0; q < m->n_mortar; q++) {
         const mortar_geo g = mortar_get(m, q);
         const int Na = npd[g.a], Nb = npd[g.b];
@@ -513,7 +628,7 @@ static void mortar_scatter(const nsem_oracle_mesh* m, int ncomp, const double* Q
         const double* Pb = m->psi_ref[g.b * 2 + g.ob];
         for (int ia = 0; ia < Na; ia++)
             for (int ib = 0; ib < Nb; ib++) {
-                double sum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                double sum[32] = {0};
                 for (int na = 0; na < Na; na++)
                     for (int nb = 0; nb < Nb; nb++) {
                         const double* v = Q + (size_t)ncomp * mortar_node(m, &g, na, nb);
@@ -531,6 +646,7 @@ static void mortar_scatter(const nsem_oracle_mesh* m, int ncomp, const double* Q
  * F psiCor_a psiCor_b */
 static void mortar_gather(const nsem_oracle_mesh* m, int ncomp, const double* F, double* out) {
     const int npd[3] = {m->npx, m->npy, m->npz};
+    if (ncomp > 32) abort();
     for (int q = 0; q < m->n_mortar; q++) {
         const mortar_geo g = mortar_get(m, q);
         const int Na = npd[g.a], Nb = npd[g.b];
@@ -539,7 +655,7 @@ static void mortar_gather(const nsem_oracle_mesh* m, int ncomp, const double* F,
         const int64_t k0 = g.fi * m->npf;
         for (int na = 0; na < Na; na++)
             for (int nb = 0; nb < Nb; nb++) {
-                double sum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                double sum[32] = {0};
                 for (int ia = 0; ia < Na; ia++)
                     for (int ib = 0; ib < Nb; ib++) {
                         const double* v = F + (size_t)ncomp * (k0 + (int64_t)ia * Nb + ib);

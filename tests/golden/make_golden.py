@@ -194,6 +194,18 @@ def make_amr_case(name, ref_bin, tmp):
     run([os.path.join(ref_bin, "euler"), "./controls"], case)
     n_int = int(d["meta"][7])
     out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    # the coupled form on the same mesh: the harness's tendency at its start
+    # state and its SSP-RK3 trajectory over the reference's own operators
+    rk_steps = 5
+    os.makedirs(os.path.join(case, "rk"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls", "rk3", "rk", str(rk_steps),
+         str(rk_steps)], case)
+    r = load_dump(os.path.join(case, "rk"))
+    for v in VARS:
+        out[f"u0_{v}"] = d[f"u0_{v}"]
+        out[f"L0_{v}"] = d[f"L0_{v}"]
+        out[f"rk_{v}"] = r[f"s{rk_steps:05d}_{v}"]
+    out["rk_steps"] = np.int64(rk_steps)
     out["mortar"] = d["mortar"]
     assert len(out["mortar"]) > 0, "no cell was refined"
     for dd in range(3):
