@@ -64,7 +64,8 @@ nsem_status fail(nsem_ctx* c, nsem_status s, const std::string& msg) {
 nsem_status require_conforming(nsem_ctx* c) {
     if (c && c->dev.n_ms > 0)
         return fail(c, NSEM_UNSUPPORTED,
-                    "non-conforming (2:1) faces: only NSEM_REF_SEGREGATED steps this mesh");
+                    "non-conforming (2:1) faces: only the FP64 forms (SSP-RK3 and "
+                    "NSEM_REF_SEGREGATED) step this mesh");
     return NSEM_OK;
 }
 
@@ -383,9 +384,9 @@ nsem_status seg_alloc(nsem_ctx* ctx) {
     }
     if (ctx->dev.n_ms > 0) {
         const size_t nm = (size_t)ctx->dev.n_ms;
-        for (int c = 0; c < 16; c++)
+        for (int c = 0; c < 19; c++)
             if ((s = dalloc(ctx, &S.mq[c], nm)) != NSEM_OK) return s;
-        for (int c = 0; c < 12; c++)
+        for (int c = 0; c < 15; c++)
             if ((s = dalloc(ctx, &S.mf[c], nm)) != NSEM_OK) return s;
         for (int c = 0; c < 5; c++)
             if ((s = dalloc(ctx, &S.dC[c], nm)) != NSEM_OK) return s;
@@ -442,7 +443,8 @@ int fp64_face(nsem_ctx* ctx, int from_state) {
     NsemBuf* b = &ctx->buf;
     if (b->G[0]) {
         const double* U[3] = {b->prim[0], b->prim[1], b->prim[2]};
-        const int e = nsem_grad_ut(&ctx->dev, &ctx->tab, U, b->prim[3], b->G, b->fF, ctx->stream);
+        const int e = nsem_grad_ut_mortar(&ctx->dev, &ctx->tab, U, b->prim[3], b->G, b->fF,
+                                          ctx->dev.n_ms > 0 ? b->gC : nullptr, ctx->stream);
         if (e) return e;
     }
     return nsem_fp64_face(&ctx->dev, b, from_state, ctx->stream);
@@ -512,6 +514,14 @@ nsem_status nsem_create(const nsem_mesh_desc* mesh, const nsem_params* params, n
         if ((s = seg_alloc(ctx)) != NSEM_OK) return s;
         for (int c = 0; c < 12; c++) ctx->buf.G[c] = ctx->sbuf.G[c];
         for (int c = 0; c < 4; c++) ctx->buf.fF[c] = ctx->sbuf.fF[c];
+    }
+    if (ctx->dev.n_ms > 0) {
+        /* non-conforming faces: mortar buffers shared by both FP64 schemes */
+        if ((s = seg_alloc(ctx)) != NSEM_OK) return s;
+        for (int c = 0; c < 19; c++) ctx->buf.mq[c] = ctx->sbuf.mq[c];
+        for (int c = 0; c < 15; c++) ctx->buf.mf[c] = ctx->sbuf.mf[c];
+        for (int c = 0; c < 5; c++) ctx->buf.dC[c] = ctx->sbuf.dC[c];
+        for (int c = 0; c < 4; c++) ctx->buf.gC[c] = ctx->sbuf.gC[c];
     }
     return NSEM_OK;
 }
@@ -627,7 +637,7 @@ nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
 
 nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5],
                           double* p_prime) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && ctx->dev.n_ms > 0 && prec != NSEM_FP64) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!L) return fail(ctx, NSEM_BAD_ARG, "L is NULL");
     for (int c = 0; c < 5; c++) if (!L[c]) return fail(ctx, NSEM_BAD_ARG, "L[c] is NULL");
@@ -660,7 +670,7 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
 }
 
 nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec) {
-    if (ctx && ctx->dev.n_ms > 0 && scheme != NSEM_REF_SEGREGATED) return require_conforming(ctx);
+    if (ctx && ctx->dev.n_ms > 0 && prec != NSEM_FP64) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
     if (scheme != NSEM_SSPRK3 && scheme != NSEM_REF_SEGREGATED)

@@ -26,6 +26,7 @@
 #include "nsem_ddpow.h"
 #include "nsem_gather.cuh"
 #include "nsem_internal.h"
+#include "nsem_mortar.cuh"
 
 namespace {
 
@@ -110,7 +111,72 @@ struct FaceArgs {
     const double* prim[NSEM_NPRIM];
     double* d[5];
     const double* G[12];         /* viscous runs: grad U, grad theta (else null) */
+    /* non-conforming faces, per mortar slot */
+    double* mq[19];              /* the coarse side's interpolated quantities */
+    double* mf[15];              /* face flux vectors (rho 3, momentum 9, theta 3) */
+    double* dC[5];               /* projected, lifted coarse-side fluxes */
 };
+
+/* Non-conforming faces: the coarse side's node quantities of the stage
+ * state interpolated onto each mortar slot, one thread per (slot, quantity):
+ * |U|, c, U rho (3), rho, the momentum flux tensor (rho U) (x) U + p' I
+ * - mu grad U (9), the theta flux (rho U) theta - (mu / Pr) grad theta (3),
+ * rho theta; each exactly as the face kernel forms it at a node. */
+__global__ void __launch_bounds__(128) k_mortar_coupled(const NsemDev m, FaceArgs a) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 19 * m.n_ms) return;
+    const int64_t ms = id / 19;
+    const int c = (int)(id % 19);
+    const int t = c - 6;   /* tensor component of the momentum flux */
+    const int ra = (t >= 0 && t < 9) ? (t < 3 ? t : (t == 3 || t == 5) ? 0 : (t == 4 || t == 6) ? 1 : 2) : 0;
+    const int rb = (t >= 0 && t < 9) ? (t < 3 ? t : (t == 6 || t == 8) ? 0 : (t == 3 || t == 7) ? 1 : 2) : 0;
+    double out[1];
+    mortar_interp<1>(m, ms, [&](int64_t node, double* v) {
+        const double r = a.S0[node];
+        if (c == 0) v[0] = a.prim[5][node];
+        else if (c == 1) v[0] = a.prim[6][node];
+        else if (c < 5) v[0] = a.prim[c - 2][node] * r;
+        else if (c == 5) v[0] = r;
+        else if (c < 15) {
+            double x = (a.prim[ra][node] * r) * a.prim[rb][node];
+            x = x + ((t < 3) ? 1.0 : 0.0) * a.prim[4][node];
+            if (a.G[0]) x = x - (r * m.nu) * a.G[t][node];
+            v[0] = x;
+        } else if (c < 18) {
+            double x = (a.prim[c - 15][node] * r) * a.prim[3][node];
+            if (a.G[0]) x = x - ((r * m.nu) * m.iPr) * a.G[9 + c - 15][node];
+            v[0] = x;
+        } else {
+            v[0] = r * a.prim[3][node];
+        }
+    }, out);
+    a.mq[c][ms] = out[0];
+}
+
+/* the coarse side's lifted values: the projected flux vectors dotted with the
+ * slot's own weighted normal; one thread per (mortar slot, output row) */
+__global__ void __launch_bounds__(128) k_mortar_coupled_gather(const NsemDev m, FaceArgs a) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 5 * m.n_ms) return;
+    const int64_t ms = id / 5;
+    const int r = (int)(id % 5);
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    double P[3];
+    if (r == 0 || r == 4) {
+        double* src[3] = {a.mf[r == 0 ? 0 : 12], a.mf[r == 0 ? 1 : 13], a.mf[r == 0 ? 2 : 14]};
+        mortar_project<3>(m, ms, src, P);
+        a.dC[r][ms] = vdot3(P, n);
+    } else {
+        const int q = r - 1;
+        const int cx = q == 0 ? XX : q == 1 ? YX : ZX;
+        const int cy = q == 0 ? XY : q == 1 ? YY : ZY;
+        const int cz = q == 0 ? XZ : q == 1 ? YZ : ZZ;
+        double* src[3] = {a.mf[3 + cx], a.mf[3 + cy], a.mf[3 + cz]};
+        mortar_project<3>(m, ms, src, P);
+        a.dC[r][ms] = P[0] * n[0] + P[1] * n[1] + P[2] * n[2];
+    }
+}
 
 __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,22 +209,32 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
         mu2 = sqrt(vdot3(U2, U2));
         cs2 = sqrt(m.gR * T2);
     }
-    const double lam = ((mu1 * fi + mu2 * fo) + (cs1 * fi + cs2 * fo)) / 2;
+    /* a mortar's coarse side (1: c1, 2: c2) takes interpolated quantities */
+    const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+    const int side = ms >= 0 ? ms_field(m, NSEM_MS_SIDE, ms) : 0;
+    double mu1v = mu1, cs1v = cs1, r1v = r1, r2v = r2;
+    if (side == 1) { mu1v = a.mq[0][ms]; cs1v = a.mq[1][ms]; r1v = a.mq[5][ms]; }
+    if (side == 2) { mu2 = a.mq[0][ms]; cs2 = a.mq[1][ms]; r2v = a.mq[5][ms]; }
+    const double lam = ((mu1v * fi + mu2 * fo) + (cs1v * fi + cs2 * fo)) / 2;
 
     /* continuity: flux U rho, state rho */
     {
         double F[3];
-        const double jump = lam * (r2 - r1);
+        const double jump = lam * (r2v - r1v);
         for (int c = 0; c < 3; c++) {
-            const double x = U1[c] * r1, y = U2[c] * r2;
+            double x = U1[c] * r1, y = U2[c] * r2;
+            if (side == 1) x = a.mq[2 + c][ms];
+            if (side == 2) y = a.mq[2 + c][ms];
             F[c] = (x * fi + y * fo) - en[c] * jump;
         }
         a.d[0][k] = vdot3(F, n);
+        if (side)
+            for (int c = 0; c < 3; c++) a.mf[c][ms] = F[c];
     }
     /* momentum: flux (rho U)(x)U + p' I, state rho U */
     {
-        const double Fc1[3] = {U1[0] * r1, U1[1] * r1, U1[2] * r1};
-        const double Fc2[3] = {U2[0] * r2, U2[1] * r2, U2[2] * r2};
+        double Fc1[3] = {U1[0] * r1, U1[1] * r1, U1[2] * r1};
+        double Fc2[3] = {U2[0] * r2, U2[1] * r2, U2[2] * r2};
         double A[9], B[9], O[9], F[9], dq[3], out[3];
         outer(Fc1, U1, A);
         outer(Fc2, U2, B);
@@ -176,6 +252,13 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
                 B[c] = B[c] - mu2 * (c2 >= 0 ? a.G[c][c2] : 0.0);
             }
         }
+        if (side == 1) {
+            for (int c = 0; c < 9; c++) A[c] = a.mq[6 + c][ms];
+            for (int c = 0; c < 3; c++) Fc1[c] = a.mq[2 + c][ms];
+        } else if (side == 2) {
+            for (int c = 0; c < 9; c++) B[c] = a.mq[6 + c][ms];
+            for (int c = 0; c < 3; c++) Fc2[c] = a.mq[2 + c][ms];
+        }
         for (int c = 0; c < 3; c++) dq[c] = (Fc2[c] - Fc1[c]) * lam;
         outer(en, dq, O);
         for (int c = 0; c < 9; c++) F[c] = (A[c] * fi + B[c] * fo) - O[c];
@@ -183,11 +266,16 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
         a.d[1][k] = out[0];
         a.d[2][k] = out[1];
         a.d[3][k] = out[2];
+        if (side)
+            for (int c = 0; c < 9; c++) a.mf[3 + c][ms] = F[c];
     }
     /* potential temperature: flux (rho U) theta, state rho theta */
     {
         double F[3];
-        const double jump = lam * (r2 * T2 - r1 * T1);
+        double s1 = r1 * T1, s2 = r2 * T2;
+        if (side == 1) s1 = a.mq[18][ms];
+        if (side == 2) s2 = a.mq[18][ms];
+        const double jump = lam * (s2 - s1);
         for (int c = 0; c < 3; c++) {
             double x = (U1[c] * r1) * T1, y = (U2[c] * r2) * T2;
             if (a.G[0]) {
@@ -195,9 +283,13 @@ __global__ void __launch_bounds__(256) k_face(const NsemDev m, FaceArgs a) {
                 x = x - ((r1 * m.nu) * m.iPr) * a.G[9 + c][c1];
                 y = y - ((r2 * m.nu) * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
             }
+            if (side == 1) x = a.mq[15 + c][ms];
+            if (side == 2) y = a.mq[15 + c][ms];
             F[c] = (x * fi + y * fo) - en[c] * jump;
         }
         a.d[4][k] = vdot3(F, n);
+        if (side)
+            for (int c = 0; c < 3; c++) a.mf[12 + c][ms] = F[c];
     }
 }
 
@@ -210,6 +302,7 @@ struct VolArgs {
     int stage;
     double dt;
     const double* G[12];    /* viscous runs: grad U, grad theta (else null) */
+    const double* dC[5];    /* non-conforming faces: the coarse side's lifted values */
 };
 
 /* shared layout per node: fr[3] fm[9] ft[3] jin[9] = 24 doubles */
@@ -253,14 +346,20 @@ __global__ void k_volume(const NsemDev m, const NsemTables tab, VolArgs a) {
 
     /* surface lift, in the order div_flux visits the element's faces */
     double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0, r4 = 0.0;
-    for (int j = 0; j < 3; j++) {
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
         const int64_t k = code >> 2;
-        if (code & 1) {
-            r0 -= a.d[0][k]; r1 -= a.d[1][k]; r2 -= a.d[2][k]; r3 -= a.d[3][k]; r4 -= a.d[4][k];
+        double v0, v1, v2, v3, v4;
+        if (code & 2) {
+            v0 = a.dC[0][k]; v1 = a.dC[1][k]; v2 = a.dC[2][k]; v3 = a.dC[3][k]; v4 = a.dC[4][k];
         } else {
-            r0 += a.d[0][k]; r1 += a.d[1][k]; r2 += a.d[2][k]; r3 += a.d[3][k]; r4 += a.d[4][k];
+            v0 = a.d[0][k]; v1 = a.d[1][k]; v2 = a.d[2][k]; v3 = a.d[3][k]; v4 = a.d[4][k];
+        }
+        if (code & 1) {
+            r0 -= v0; r1 -= v1; r2 -= v2; r3 -= v3; r4 -= v4;
+        } else {
+            r0 += v0; r1 += v1; r2 += v2; r3 += v3; r4 += v4;
         }
     }
 
@@ -337,8 +436,15 @@ extern "C" int nsem_fp64_face(const NsemDev* m, NsemBuf* b, int from_state, void
     for (int c = 0; c < NSEM_NPRIM; c++) a.prim[c] = b->prim[c];
     for (int c = 0; c < 5; c++) a.d[c] = b->d[c];
     for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
+    for (int c = 0; c < 19; c++) a.mq[c] = b->mq[c];
+    for (int c = 0; c < 15; c++) a.mf[c] = b->mf[c];
+    for (int c = 0; c < 5; c++) a.dC[c] = b->dC[c];
     const int64_t blocks = (m->n_slot + 255) / 256;
-    k_face<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(*m, a);
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+    if (m->n_ms > 0) k_mortar_coupled<<<19 * mb, 128, 0, st>>>(*m, a);
+    k_face<<<(unsigned)blocks, 256, 0, st>>>(*m, a);
+    if (m->n_ms > 0) k_mortar_coupled_gather<<<5 * mb, 128, 0, st>>>(*m, a);
     return launch_err();
 }
 
@@ -371,6 +477,7 @@ extern "C" int nsem_fp64_volume(const NsemDev* m, const NsemTables* t, NsemBuf* 
     }
     for (int c = 0; c < NSEM_NPRIM; c++) a.prim[c] = b->prim[c];
     for (int c = 0; c < 12; c++) a.G[c] = b->G[c];
+    for (int c = 0; c < 5; c++) a.dC[c] = b->dC[c];
     const int threads = ((m->np + 31) / 32) * 32;
     k_volume<<<(unsigned)m->n_elem, threads, vol_smem(m), (cudaStream_t)stream>>>(*m, *t, a);
     return launch_err();

@@ -78,6 +78,11 @@ struct NsemBuf {
     double* L[5];      /* tendency output (nsem_tendency) */
     double* G[12];     /* viscous runs: grad U, grad theta of the stage state */
     double* fF[4];     /* viscous runs: per-slot scratch of the gradients   */
+    /* non-conforming faces, per mortar slot (shared with the segregated scheme) */
+    double* mq[19];    /* the coarse side's interpolated quantities */
+    double* mf[15];    /* face flux vectors / tensors */
+    double* dC[5];     /* projected, lifted coarse-side fluxes */
+    double* gC[4];     /* projected cds(U), cds(theta) */
 };
 
 #ifdef __cplusplus

@@ -42,6 +42,7 @@
 
 #include "nsem_ddpow.h"
 #include "nsem_gather.cuh"
+#include "nsem_mortar.cuh"
 #include "nsem_seg.h"
 
 namespace {
@@ -125,55 +126,6 @@ struct SegArgs {
     double c_dt;             /* -1 / dt */
     int visc;
 };
-
-/* Non-conforming (2:1) faces (scatter_non_conforming / gather_non_conforming,
- * field.h:2019-2248): on a mortar face the coarse cell's side of each face
- * quantity is interpolated from the coarse face's nodes onto the mortar nodes
- * (psiRef along the face's two axes), and the face values are projected back
- * onto the coarse face's nodes (psiCor) before the coarse cell lifts them.
- * One thread per mortar slot. */
-__device__ __forceinline__ int32_t ms_field(const NsemDev& m, int f, int64_t ms) {
-    return m.ms_i[(int64_t)f * m.n_ms + ms];
-}
-
-/* sum over the coarse face's nodes of Q(node) psiRef_a psiRef_b, in the
- * reference's order (coarse index along a outer, along b inner) */
-template <int NQ, typename Q>
-__device__ __forceinline__ void mortar_interp(const NsemDev& m, int64_t ms, Q q, double* out) {
-    const int base = ms_field(m, NSEM_MS_BASE, ms), sa = ms_field(m, NSEM_MS_SA, ms),
-              sb = ms_field(m, NSEM_MS_SB, ms), Na = ms_field(m, NSEM_MS_NA, ms),
-              Nb = ms_field(m, NSEM_MS_NB, ms), ia = ms_field(m, NSEM_MS_IA, ms),
-              ib = ms_field(m, NSEM_MS_IB, ms);
-    const double* Pa = m.psir + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    const double* Pb = m.psir + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    for (int c = 0; c < NQ; c++) out[c] = 0.0;
-    for (int na = 0; na < Na; na++)
-        for (int nb = 0; nb < Nb; nb++) {
-            double v[NQ];
-            q((int64_t)base + na * sa + nb * sb, v);
-            const double fa = Pa[na * Na + ia], fb = Pb[nb * Nb + ib];
-            for (int c = 0; c < NQ; c++) out[c] += v[c] * fa * fb;
-        }
-}
-
-/* projection of the face's values src (NC arrays over its mortar slots) onto
- * this slot's coarse node: sum over the face's slots of src psiCor_a psiCor_b */
-template <int NC>
-__device__ __forceinline__ void mortar_project(const NsemDev& m, int64_t ms, double* const* src,
-                                               double* out) {
-    const int Na = ms_field(m, NSEM_MS_NA, ms), Nb = ms_field(m, NSEM_MS_NB, ms),
-              na = ms_field(m, NSEM_MS_IA, ms), nb = ms_field(m, NSEM_MS_IB, ms),
-              first = ms_field(m, NSEM_MS_FIRST, ms);
-    const double* Pa = m.psic + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    const double* Pb = m.psic + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
-    for (int c = 0; c < NC; c++) out[c] = 0.0;
-    for (int ja = 0; ja < Na; ja++)
-        for (int jb = 0; jb < Nb; jb++) {
-            const int64_t s2 = first + ja * Nb + jb;
-            const double fa = Pa[ja * Na + na], fb = Pb[jb * Nb + nb];
-            for (int c = 0; c < NC; c++) out[c] += src[c][s2] * fa * fb;
-        }
-}
 
 /* One thread per (mortar slot, quantity): each sum is a short dependent
  * chain over the coarse face's nodes, so the slots' quantities run side by
@@ -301,15 +253,17 @@ __global__ void __launch_bounds__(256) k_seg_face_rho(const NsemDev m, SegArgs a
     const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
     double mu1v = mu1, cs1v = cs1, r1v = r1;
     if (ms >= 0) {
-        const bool own = ms_field(m, NSEM_MS_SIDE, ms) == 1;
-        double* mu_ = own ? &mu1v : &mu2;
-        double* cs_ = own ? &cs1v : &cs2;
-        double* r_ = own ? &r1v : &r2;
-        double* X = own ? X1 : X2;
-        *mu_ = a.mq[0][ms];
-        *cs_ = a.mq[1][ms];
-        for (int c = 0; c < 3; c++) X[c] = a.mq[2 + c][ms];
-        *r_ = a.mq[5][ms];
+        if (ms_field(m, NSEM_MS_SIDE, ms) == 1) {
+            mu1v = a.mq[0][ms];
+            cs1v = a.mq[1][ms];
+            for (int c = 0; c < 3; c++) X1[c] = a.mq[2 + c][ms];
+            r1v = a.mq[5][ms];
+        } else {
+            mu2 = a.mq[0][ms];
+            cs2 = a.mq[1][ms];
+            for (int c = 0; c < 3; c++) X2[c] = a.mq[2 + c][ms];
+            r2 = a.mq[5][ms];
+        }
     }
     const double lam = ((mu1v * fi + mu2 * fo) + (cs1v * fi + cs2 * fo)) / 2;
     a.lam[k] = lam;
@@ -583,11 +537,12 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
             q1[c] = r1 * U1[c];
             q2[c] = r2 * U2[c];
         }
-        if (mside) {
-            double* Am = mside == 1 ? A : B;
-            double* qm = mside == 1 ? q1 : q2;
-            for (int c = 0; c < 9; c++) Am[c] = a.mq[c][ms];
-            for (int c = 0; c < 3; c++) qm[c] = a.mq[9 + c][ms];
+        if (mside == 1) {
+            for (int c = 0; c < 9; c++) A[c] = a.mq[c][ms];
+            for (int c = 0; c < 3; c++) q1[c] = a.mq[9 + c][ms];
+        } else if (mside == 2) {
+            for (int c = 0; c < 9; c++) B[c] = a.mq[c][ms];
+            for (int c = 0; c < 3; c++) q2[c] = a.mq[9 + c][ms];
         }
         for (int c = 0; c < 3; c++) dq[c] = (q2[c] - q1[c]) * lam;
         outer(en, dq, O);
@@ -611,10 +566,12 @@ __global__ void __launch_bounds__(256) k_seg_face_ut(const NsemDev m, SegArgs a)
                 y[c] = y[c] - (mu2 * m.iPr) * (c2 >= 0 ? a.G[9 + c][c2] : 0.0);
             }
         }
-        if (mside) {
-            double* fm = mside == 1 ? x : y;
-            for (int c = 0; c < 3; c++) fm[c] = a.mq[12 + c][ms];
-            (mside == 1 ? s1 : s2) = a.mq[15][ms];
+        if (mside == 1) {
+            for (int c = 0; c < 3; c++) x[c] = a.mq[12 + c][ms];
+            s1 = a.mq[15][ms];
+        } else if (mside == 2) {
+            for (int c = 0; c < 3; c++) y[c] = a.mq[12 + c][ms];
+            s2 = a.mq[15][ms];
         }
         const double jump = lam * (s2 - s1);
         for (int c = 0; c < 3; c++) F[c] = (x[c] * fi + y[c] * fo) - en[c] * jump;
@@ -658,11 +615,16 @@ __global__ void k_seg_vol_ut(const NsemDev m, const NsemTables tab, SegArgs a) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
         const int64_t idx = code >> 2;
-        double* const* src = (code & 2) ? a.dC : a.d;
-        if (code & 1) {
-            r1 -= src[1][idx]; r2 -= src[2][idx]; r3 -= src[3][idx]; r4 -= src[4][idx];
+        double v1, v2, v3, v4;
+        if (code & 2) {
+            v1 = a.dC[1][idx]; v2 = a.dC[2][idx]; v3 = a.dC[3][idx]; v4 = a.dC[4][idx];
         } else {
-            r1 += src[1][idx]; r2 += src[2][idx]; r3 += src[3][idx]; r4 += src[4][idx];
+            v1 = a.d[1][idx]; v2 = a.d[2][idx]; v3 = a.d[3][idx]; v4 = a.d[4][idx];
+        }
+        if (code & 1) {
+            r1 -= v1; r2 -= v2; r3 -= v3; r4 -= v4;
+        } else {
+            r1 += v1; r2 += v2; r3 += v3; r4 += v4;
         }
     }
     volume_gather<W_UT, 12>(m, sm, dps, t, [&](int lb, const double* dj) {
@@ -862,19 +824,30 @@ AdvArgs adv_args(NsemConvBuf* b, int cur, double dt) {
 
 }  // namespace
 
-int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
-                 double* const* G, double* const* fF, void* stream) {
+int nsem_grad_ut_mortar(const NsemDev* m, const NsemTables* t, const double* const* U,
+                        const double* T, double* const* G, double* const* fF, double* const* gC,
+                        void* stream) {
     GradArgs ga;
     for (int c = 0; c < 3; c++) ga.U[c] = U[c];
     ga.Tf = T;
     for (int c = 0; c < 12; c++) ga.G[c] = G[c];
     for (int c = 0; c < 4; c++) ga.fF[c] = fF[c];
-    for (int c = 0; c < 4; c++) ga.gC[c] = nullptr;
+    for (int c = 0; c < 4; c++) ga.gC[c] = gC ? gC[c] : nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     const int threads = ((m->np + 31) / 32) * 32;
     k_seg_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
+    if (m->n_ms > 0 && gC) {
+        const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+        k_seg_mortar_gcds<<<mb, 128, 0, st>>>(*m, ga);
+        k_seg_mortar_ggather<<<mb, 128, 0, st>>>(*m, ga);
+    }
     k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), st>>>(*m, *t, ga);
     return (int)cudaGetLastError();
+}
+
+int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
+                 double* const* G, double* const* fF, void* stream) {
+    return nsem_grad_ut_mortar(m, t, U, T, G, fF, nullptr, stream);
 }
 
 int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,

@@ -24,8 +24,8 @@ struct NsemSegBuf {
     double* G[12] = {};           /* per node: grad U (XX..ZX), grad theta  */
     double* fF[4] = {};           /* per slot: cds(U), cds(theta)           */
     /* non-conforming faces, per mortar slot */
-    double* mq[16] = {};          /* coarse side's interpolated quantities  */
-    double* mf[12] = {};          /* face flux vectors / tensors            */
+    double* mq[19] = {};          /* coarse side's interpolated quantities  */
+    double* mf[15] = {};          /* face flux vectors / tensors            */
     double* dC[5] = {};           /* projected, lifted coarse-side fluxes   */
     double* gC[4] = {};           /* projected cds(U), cds(theta)           */
 };
@@ -49,6 +49,11 @@ int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U,
                   double* const* G, const double* const* fF, void* stream);
 int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
                  double* const* G, double* const* fF, void* stream);
+/* the same on a mesh with non-conforming faces: gC (4 arrays per mortar
+ * slot) receives the projected face values */
+int nsem_grad_ut_mortar(const NsemDev* m, const NsemTables* t, const double* const* U,
+                        const double* T, double* const* G, double* const* fF, double* const* gC,
+                        void* stream);
 /* lambda of the fixed wind (once, after U is set) */
 int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream);
 int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps, double dt,

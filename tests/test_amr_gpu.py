@@ -39,6 +39,36 @@ def test_amr_segregated_gpu_bitwise_vs_oracle(case):
     assert rel(r, g["fldN_rho"]) <= 1e-14
     assert rel(t, g["fldN_T"]) <= 1e-10
     with pytest.raises(ng.NsemError) as e:
-        s.step(1)                                   # SSP-RK3 assumes conforming faces
+        s.step(1, prec=ng.MIXED)                    # the precision form is structured-only
     assert "non-conforming" in str(e.value)
+    s.close()
+
+
+VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
+
+
+@pytest.mark.parametrize("case", ["amr_c1_2d_visc", "amr_g3_4n3"])
+def test_amr_coupled_fp64_gpu_bitwise_vs_oracle(case):
+    """The plain FP64 form (tendency and SSP-RK3) on the refined meshes: bit
+    for bit the oracle with the correctly rounded pow; the oracle itself is
+    bit for bit the reference's operators (tests/test_amr_oracle.py)."""
+    import nebulasem_gb300 as ng
+    g = load_golden(case)
+    dt, steps = float(g["dt"]), int(g["rk_steps"])
+    u0 = [g[f"u0_{v}"] for v in VARS]
+    m = oracle.OracleMesh(g)
+    oracle.set_pow(1)
+    try:
+        L_o = m.tendency(u0)
+        u_o = m.ssprk3(u0, dt, steps)
+    finally:
+        oracle.set_pow(0)
+    s = ng.Solver(g, dt=dt)
+    s.set_state(u0)
+    L = s.tendency()
+    for a, b, v in zip(L, L_o, VARS):
+        assert np.array_equal(a, b), v
+    s.step(steps)
+    for a, b, v in zip(s.get_state(), u_o, VARS):
+        assert np.array_equal(a, b), v
     s.close()
