@@ -99,6 +99,8 @@ BlockDesc read_block_description(const std::string& path) {
     bool have_block = false;
     std::array<std::array<double, 3>, 8> corner{};
     std::array<BlockDesc::Edge, 12> edges{};
+    std::array<double, 12> factor{};
+    factor.fill(1.0);
     bool curved = false, wall = false;
     std::array<int, 3> nloc{};
     std::vector<std::pair<std::string, std::vector<int>>> patches;
@@ -123,17 +125,29 @@ BlockDesc read_block_description(const std::string& path) {
                 nloc[d] = (int)n[d];
                 if (nloc[d] < 1) throw std::runtime_error(path + ": division count < 1");
             }
+            factor.fill(1.0);
             if (type == "wall" || type == "geometric") {
-                for (double s : c.list())
-                    if (s != 1.0)
-                        throw std::runtime_error(path + ": graded spacing (factor " + std::to_string(s) +
-                                                 ") is not supported; uniform spacing only");
+                /* grading factors: sz values spread over the 12 edges in
+                 * groups of 12 / sz (meshApp.cpp:120-143) */
+                const std::vector<double> f = c.list();
+                const int sz = (int)f.size();
+                if (sz < 1 || sz > 12) throw std::runtime_error(path + ": bad grading factor list");
+                const int r = 12 / sz;
+                for (int i = 0; i < sz; i++)
+                    for (int j = 0; j < r; j++)
+                        if (i * r + j < 12) factor[i * r + j] = f[i];
+                for (double v : factor)
+                    if (!(v > 0)) throw std::runtime_error(path + ": grading factor must be > 0");
                 /* a wall-graded direction with an odd count above 1 gets one
-                 * more division (src/mesh/hexMesh.cpp:51-66) */
+                 * more division, and the factors of edges d, d+3, d+6, d+9
+                 * are inverted (src/mesh/hexMesh.cpp:51-66, as written there) */
                 if (type == "wall") {
                     wall = true;
                     for (int d = 0; d < 3; d++)
-                        if (nloc[d] % 2 && nloc[d] != 1) nloc[d]++;
+                        if (nloc[d] % 2 && nloc[d] != 1) {
+                            nloc[d]++;
+                            for (int i = d; i < 12; i += 3) factor[i] = 1 / factor[i];
+                        }
                 }
             } else if (type != "linear") {
                 throw std::runtime_error(path + ": block spacing '" + type + "' is not supported");
@@ -193,6 +207,7 @@ BlockDesc read_block_description(const std::string& path) {
     b.edge = edges;
     b.curved = curved;
     b.wall = wall;
+    b.factor = factor;
     for (int a = 0; a < 3; a++) b.n[a] = nloc[a];
     const int axis_vertex[3] = {1, 3, 4};
     for (int a = 0; a < 3; a++) {
@@ -495,14 +510,33 @@ V3 hex_point(const V3* vp, double r, double s, double t) {
     return coons_cell(r, s, t, vp, vd, vf);
 }
 
-/* spacing of a block edge with n divisions at vertex j: uniform, or the
- * mirrored half-spacing of a `wall` edge with factor 1 (hexMesh.cpp:68-96) */
-double edge_param(int j, int n, bool wall) {
-    if (n == 1) return (double)j;
-    if (!wall) return (double)j / n;
-    const int h = n / 2;
-    if (j <= h) return (double)j / h / 2;
-    return 1.0 - (double)(n - j) / h / 2;
+/* the reference's equal(): within 1e-7 absolute or relative (tensor.h:471) */
+bool near_equal(double p, double q) {
+    const double d = std::fabs(p - q);
+    return d <= 1e-7 || d <= 1e-7 * std::fabs(p) || d <= 1e-7 * std::fabs(q);
+}
+
+/* vertex parameters 0..n of a block edge with n divisions and grading factor
+ * s (hexMesh.cpp:68-96): geometric progression with total ratio s, or for a
+ * `wall` edge two mirrored halves each graded by s */
+std::vector<double> edge_params(int n, double s, bool wall) {
+    std::vector<double> sc((size_t)n + 1);
+    s = wall ? std::pow(s, 1. / (n / 2.)) : std::pow(s, 1. / n);
+    if (n == 1) {
+        sc[0] = 0;
+        sc[1] = 1;
+        return sc;
+    }
+    const int nt = wall ? n / 2 : n;
+    const double r = s;
+    for (int j = 0; j <= nt; j++)
+        sc[j] = near_equal(r, 1.0) ? double(j) / nt
+                                   : (1 - std::pow(r, double(j))) / (1 - std::pow(s, double(nt)));
+    if (wall) {
+        for (int j = 0; j <= nt; j++) sc[j] /= 2;
+        for (int j = 0; j <= nt; j++) sc[j + nt] = 1.0 - sc[nt - j];
+    }
+    return sc;
 }
 
 /* area vector of a quadrilateral mesh face as Mesh::calcGeometry forms it
@@ -651,15 +685,20 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     };
     {
         EdgeShape es[12];
-        for (int w = 0; w < 12; w++) es[w] = edge_shape(b, w);
+        std::vector<double> sc[12];
+        const int nd[3] = {nx, ny, nz};
+        for (int w = 0; w < 12; w++) {
+            es[w] = edge_shape(b, w);
+            sc[w] = edge_params(nd[w / 4], b.factor[w], b.wall);
+        }
         const V3* cp = b.corner.data();
         for (int i = 0; i <= nx; i++)
             for (int j = 0; j <= ny; j++)
                 for (int k = 0; k <= nz; k++) {
                     V3 vd[12], vf[6];
-                    for (int w = 0; w < 4; w++) vd[w] = edge_point(es[w], edge_param(i, nx, b.wall));
-                    for (int w = 4; w < 8; w++) vd[w] = edge_point(es[w], edge_param(j, ny, b.wall));
-                    for (int w = 8; w < 12; w++) vd[w] = edge_point(es[w], edge_param(k, nz, b.wall));
+                    for (int w = 0; w < 4; w++) vd[w] = edge_point(es[w], sc[w][i]);
+                    for (int w = 4; w < 8; w++) vd[w] = edge_point(es[w], sc[w][j]);
+                    for (int w = 8; w < 12; w++) vd[w] = edge_point(es[w], sc[w][k]);
                     const double rx = i / double(nx), ry = j / double(ny), rz = k / double(nz);
                     coons_faces(rx, ry, rz, cp, vd, vf);
                     lat[LI(i, j, k)] = coons_cell(rx, ry, rz, cp, vd, vf);

@@ -7,11 +7,11 @@
  * d}...`, `default name`).  Supported: one hexahedral block, either with
  * straight edges forming a parallelepiped (axis-aligned, or rotated / sheared
  * as the reference's srtb-inclined example) or with curved edges (any 8
- * corners); uniform spacing (`linear`, or `wall`/`geometric` with all factors
- * 1); a `delete` patch on the two faces of the block's second axis, one
- * element thick, makes the case two-dimensional (npy 0).  Anything else
- * (several blocks, grading) is rejected with a message: the driver has no CPU
- * path to fall back to.
+ * corners); `linear`, `geometric` or `wall` spacing with grading factors
+ * (hexMesh.cpp:48-100); a `delete` patch on the two faces of the block's
+ * second axis, one element thick, makes the case two-dimensional (npy 0).
+ * Anything else (several blocks, mixed spacing types) is rejected with a
+ * message: the driver has no CPU path to fall back to.
  *
  * Geometry, for every block, as the reference's mesh app and LoadMesh form
  * it, operation by operation so that the arrays agree to the bit: the
@@ -63,6 +63,7 @@ struct BlockDesc {
      * `edges n{ arc|cosine|gaussian|ridge|schar side key [scale] }` */
     bool curved = false;
     bool wall = false;                     /* `wall` spacing: mirrored edge parameters */
+    std::array<double, 12> factor{};       /* grading factor per edge (geometric / wall) */
     std::array<std::array<double, 3>, 8> corner{};
     struct Edge {
         int type = 0;                      /* 0 straight, 1 arc, 2 cosine, 3 gaussian, 4 ridge, 5 schar */

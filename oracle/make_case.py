@@ -154,7 +154,7 @@ prepare
 
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
                Pr=0.9, solver="euler", wind=None, time_scheme="BDF1", P0=100000, cp=1004.5,
-               cv=717.5, gz=-9.81, curved=None, refine=None):
+               cv=717.5, gz=-9.81, curved=None, refine=None, grading=None):
     os.makedirs(out, exist_ok=True)
     lx, ly, lz = length
     nx, ny, nz = n
@@ -179,6 +179,13 @@ def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, vi
     if curved:
         assert dim == 2, "curved variants are for the 2D block"
         grid = curved_grid(grid, curved, lx, ly, lz)
+    if grading:
+        # wall-graded block: grading = (counts, factors), e.g. odd counts that
+        # the mesh app rounds up (hexMesh.cpp:51-66)
+        counts, factors = grading
+        old = "3{%d %d %d} 3{1 1 1}" % (nx, ny, nz)
+        assert old in grid, "grading applies to the wall-spaced block"
+        grid = grid.replace(old, "3{%d %d %d} 3{%r %r %r}" % (*counts, *factors))
     with open(os.path.join(out, "grid"), "w") as f:
         f.write(grid)
     cx, cy, cz = center

@@ -68,6 +68,8 @@ SEG_PLAN = {
     # curved blocks: the srtb-curved example's arcs, and a cosine hill
     "srtb_curved": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb", "arc_y"),
     "hill": ("c1_2d", 0.005, 100, 1.5, "BDF1", "srtb", "hill"),
+    # wall grading with odd counts (one more division, the factor inversion)
+    "graded": ("c1_2d", 0.005, 50, 1.5, "BDF1", "srtb", None, ((9, 1, 9), (0.5, 1.0, 2.0))),
 }
 
 # fixture -> (case, dt, steps, artificial viscosity, refinement threshold) for
@@ -140,9 +142,10 @@ def make_seg_case(name, ref_bin, tmp):
     fluid = dict(SRTB_FLUID) if len(SEG_PLAN[name]) > 5 else {}
     fluid.pop("viscosity", None)
     curved = SEG_PLAN[name][6] if len(SEG_PLAN[name]) > 6 else None
+    grading = SEG_PLAN[name][7] if len(SEG_PLAN[name]) > 7 else None
     case = os.path.join(tmp, "seg_" + name)
     write_case(case, dt=dt, steps=nsteps, viscosity=visc, time_scheme=scheme, **fluid,
-               **CASES[base], curved=curved)
+               **CASES[base], curved=curved, grading=grading)
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls", "setup", "out"], case)
@@ -163,6 +166,8 @@ def make_seg_case(name, ref_bin, tmp):
     out["Pr"] = np.float64(0.9)
     if curved:
         out["curved"] = np.array(curved)
+    if grading:
+        out["grading"] = np.array(grading, dtype=np.float64)
     if fluid:
         # constants in the names the oracle and the Python host read
         out["P0"] = np.float64(fluid["P0"])

@@ -59,7 +59,8 @@ FLUID = ("P0", "cp", "cv", "R", "gamma", "gravity")
 
 @pytest.mark.parametrize("fixture,case", [("seg_c1_2d", "c1_2d"), ("seg_g3_2", "g3_2"),
                                           ("seg_c1_2d_visc", "c1_2d"), ("seg_srtb", "c1_2d"),
-                                          ("seg_srtb_curved", "c1_2d"), ("seg_hill", "c1_2d")])
+                                          ("seg_srtb_curved", "c1_2d"), ("seg_hill", "c1_2d"),
+                                          ("seg_graded", "c1_2d")])
 def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
     """The oracle (C library pow, as the binary) run on the driver's mesh and
     initial fields against the unmodified euler binary's fields after the
@@ -74,6 +75,9 @@ def test_driver_case_follows_euler_binary(tmp_path, fixture, case):
                      gz=float(g["gravity"][2]))
     if "curved" in g:   # a block with curved edges
         fluid["curved"] = str(g["curved"])
+    if "grading" in g:  # wall grading (counts, factors)
+        gr = g["grading"]
+        fluid["grading"] = (tuple(int(v) for v in gr[0]), tuple(float(v) for v in gr[1]))
     d = dump_case(make_case(tmp_path, case, dt=float(g["dt"]), steps=int(g["nsteps"]),
                             viscosity=visc, **fluid))
     d["viscosity"] = visc
@@ -122,7 +126,8 @@ def _edit(path, old, new):
     ("controls", "RUSANOV", "HYBRID", "RUSANOV"),
     ("controls", "time_scheme                  BDF1", "time_scheme BDF2", "BDF2"),
     ("controls", "npy       0", "npy       4", "npy 0"),
-    ("grid", "3{1 1 1}", "3{2 1 1}", "graded spacing"),
+    ("grid", "3{10 1 10} 3{1 1 1}",
+     "3{10 1 10} 3{1 1 1}\n8{0 1 5 4 3 2 6 7} linear 3{2 1 2}", "more than one block"),
     ("grid", "sides   4{1 5 6 2} 4{0 4 7 3}", "sides   4{1 5 6 2}", "no patch"),
     ("controls", "n_deferred                   0", "n_deferred 0\n    amr_step 1", "amr_step"),
 ])

@@ -50,7 +50,7 @@ def test_segregated_run_matches_oracle(tmp_path, visc):
     assert np.all(g == np.array([0.0, 0.0, -9.81]))
 
 
-@pytest.mark.parametrize("fixture", ["seg_srtb", "seg_srtb_curved", "seg_hill"])
+@pytest.mark.parametrize("fixture", ["seg_srtb", "seg_srtb_curved", "seg_hill", "seg_graded"])
 def test_srtb_example_run(tmp_path, fixture):
     """The reference's srtb example as shipped (viscosity 1.5, gravity
     -9.80606, the Fluid:: defaults for P0, cp, cv), on its box, on the
@@ -62,6 +62,9 @@ def test_srtb_example_run(tmp_path, fixture):
     g = load_golden(fixture)
     steps = int(g["nsteps"])
     curved = {"curved": str(g["curved"])} if "curved" in g else {}
+    if "grading" in g:
+        gr = g["grading"]
+        curved["grading"] = (tuple(int(v) for v in gr[0]), tuple(float(v) for v in gr[1]))
     d = make_case(tmp_path, "c1_2d", dt=float(g["dt"]), steps=steps, viscosity=1.5,
                   P0=float(g["P0"]), cp=float(g["cp"]), cv=float(g["cv"]), gz=float(g["gravity"][2]),
                   **curved)
