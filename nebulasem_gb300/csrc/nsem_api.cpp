@@ -64,8 +64,8 @@ nsem_status fail(nsem_ctx* c, nsem_status s, const std::string& msg) {
 nsem_status require_conforming(nsem_ctx* c) {
     if (c && c->dev.n_ms > 0)
         return fail(c, NSEM_UNSUPPORTED,
-                    "non-conforming (2:1) faces: only the FP64 forms (SSP-RK3 and "
-                    "NSEM_REF_SEGREGATED) step this mesh");
+                    "non-conforming (2:1) faces: only the FP64 forms (SSP-RK3, "
+                    "NSEM_REF_SEGREGATED, convection) step this mesh");
     return NSEM_OK;
 }
 
@@ -1032,7 +1032,6 @@ extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final
 /* --------------------------------------------------- scalar convection */
 
 extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const double* T) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!U || !T) return fail(ctx, NSEM_BAD_ARG, "U or T is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
@@ -1046,6 +1045,10 @@ extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const
         if ((s = dalloc(ctx, &C.lam, ns)) != NSEM_OK) return s;
         if ((s = dalloc(ctx, &C.d, ns)) != NSEM_OK) return s;
         if ((s = seg_alloc(ctx)) != NSEM_OK) return s;   /* shared-memory attributes */
+        /* non-conforming faces: the segregated scheme's mortar buffers */
+        for (int c = 0; c < 4; c++) C.mq[c] = ctx->sbuf.mq[c];
+        for (int c = 0; c < 3; c++) C.mf[c] = ctx->sbuf.mf[c];
+        C.dC = ctx->sbuf.dC[0];
         C.ready = true;
     }
     C.cur = 0;
@@ -1060,7 +1063,7 @@ extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const
 }
 
 extern "C" nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
     NsemConvBuf& C = ctx->cbuf;

@@ -724,8 +724,42 @@ struct AdvArgs {
     const double* U[3];
     double* lam;
     double* d;
+    double* mq[4];
+    double* mf[3];
+    double* dC;
     double c_dt;
 };
+
+/* non-conforming faces: the coarse side's |U| (stage 0) or U T, T (stage 1)
+ * interpolated onto each mortar slot, one thread per (slot, quantity) */
+template <int STAGE>
+__global__ void __launch_bounds__(128) k_conv_mortar(const NsemDev m, AdvArgs a) {
+    const int nq = STAGE == 0 ? 1 : 4;
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nq * m.n_ms) return;
+    const int64_t ms = id / nq;
+    const int c = (int)(id % nq);
+    double out[1];
+    mortar_interp<1>(m, ms, [&](int64_t node, double* v) {
+        if (STAGE == 0) {
+            const double U[3] = {a.U[0][node], a.U[1][node], a.U[2][node]};
+            v[0] = sqrt(vdot3(U, U));
+        } else {
+            v[0] = c < 3 ? a.U[c][node] * a.T_o[node] : a.T_o[node];
+        }
+    }, out);
+    a.mq[c][ms] = out[0];
+}
+
+__global__ void __launch_bounds__(128) k_conv_mortar_gather(const NsemDev m, AdvArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    double F[3];
+    mortar_project<3>(m, ms, a.mf, F);
+    a.dC[ms] = vdot3(F, n);
+}
 
 __global__ void __launch_bounds__(256) k_conv_lambda(const NsemDev m, AdvArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -740,7 +774,13 @@ __global__ void __launch_bounds__(256) k_conv_lambda(const NsemDev m, AdvArgs a)
     } else {
         ghost_U(m, k, n, U1, U2);
     }
-    a.lam[k] = (sqrt(vdot3(U1, U1)) * fi + sqrt(vdot3(U2, U2)) * fo) / 2;
+    double u1 = sqrt(vdot3(U1, U1)), u2 = sqrt(vdot3(U2, U2));
+    const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+    if (ms >= 0) {
+        if (ms_field(m, NSEM_MS_SIDE, ms) == 1) u1 = a.mq[0][ms];
+        else u2 = a.mq[0][ms];
+    }
+    a.lam[k] = (u1 * fi + u2 * fo) / 2;
 }
 
 __global__ void __launch_bounds__(256) k_conv_face(const NsemDev m, AdvArgs a) {
@@ -760,13 +800,27 @@ __global__ void __launch_bounds__(256) k_conv_face(const NsemDev m, AdvArgs a) {
         ghost_U(m, k, n, U1, U2);
         T2 = T1 + 0.0;
     }
-    double F[3];
-    const double jump = a.lam[k] * (T2 - T1);
+    double X1[3], X2[3];
     for (int c = 0; c < 3; c++) {
-        const double x = U1[c] * T1, y = U2[c] * T2;
-        F[c] = (x * fi + y * fo) - en[c] * jump;
+        X1[c] = U1[c] * T1;
+        X2[c] = U2[c] * T2;
     }
+    const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+    const int side = ms >= 0 ? ms_field(m, NSEM_MS_SIDE, ms) : 0;
+    double T1v = T1, T2v = T2;
+    if (side == 1) {
+        for (int c = 0; c < 3; c++) X1[c] = a.mq[c][ms];
+        T1v = a.mq[3][ms];
+    } else if (side == 2) {
+        for (int c = 0; c < 3; c++) X2[c] = a.mq[c][ms];
+        T2v = a.mq[3][ms];
+    }
+    double F[3];
+    const double jump = a.lam[k] * (T2v - T1v);
+    for (int c = 0; c < 3; c++) F[c] = (X1[c] * fi + X2[c] * fo) - en[c] * jump;
     a.d[k] = vdot3(F, n);
+    if (side)
+        for (int c = 0; c < 3; c++) a.mf[c][ms] = F[c];
 }
 
 constexpr int W_CONV = 12;   /* fv[3] jin[9] */
@@ -791,12 +845,13 @@ __global__ void k_conv_vol(const NsemDev m, const NsemTables tab, AdvArgs a) {
     __syncthreads();
     if (!active) return;
     double r = 0.0;
-    for (int j = 0; j < 3; j++) {
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
         const int64_t k = code >> 2;
-        if (code & 1) r -= a.d[k];
-        else r += a.d[k];
+        const double v = (code & 2) ? a.dC[k] : a.d[k];
+        if (code & 1) r -= v;
+        else r += v;
     }
     volume_gather<W_CONV, 3>(m, sm, dps, t, [&](int lb, const double* dj) {
         r -= vdot3(sm + (size_t)lb * W_CONV, dj);
@@ -818,6 +873,9 @@ AdvArgs adv_args(NsemConvBuf* b, int cur, double dt) {
     for (int c = 0; c < 3; c++) a.U[c] = b->U[c];
     a.lam = b->lam;
     a.d = b->d;
+    for (int c = 0; c < 4; c++) a.mq[c] = b->mq[c];
+    for (int c = 0; c < 3; c++) a.mf[c] = b->mf[c];
+    a.dC = b->dC;
     a.c_dt = -1.0 / dt;
     return a;
 }
@@ -865,6 +923,8 @@ int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U,
 
 int nsem_conv_lambda(const NsemDev* m, NsemConvBuf* b, void* stream) {
     const AdvArgs a = adv_args(b, b->cur, 1.0);
+    if (m->n_ms > 0)
+        k_conv_mortar<0><<<(unsigned)((m->n_ms + 127) / 128), 128, 0, (cudaStream_t)stream>>>(*m, a);
     k_conv_lambda<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*m, a);
     return (int)cudaGetLastError();
 }
@@ -877,7 +937,10 @@ int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int n
     int cur = b->cur;
     for (int s = 0; s < nsteps; s++) {
         const AdvArgs a = adv_args(b, cur, dt);
+        const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+        if (m->n_ms > 0) k_conv_mortar<1><<<4 * mb, 128, 0, st>>>(*m, a);
         k_conv_face<<<sb, 256, 0, st>>>(*m, a);
+        if (m->n_ms > 0) k_conv_mortar_gather<<<mb, 128, 0, st>>>(*m, a);
         k_conv_vol<<<(unsigned)m->n_elem, threads, smem_conv(m), st>>>(*m, *t, a);
         const int e = (int)cudaGetLastError();
         if (e) return e;

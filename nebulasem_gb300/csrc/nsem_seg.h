@@ -38,6 +38,10 @@ struct NsemConvBuf {
     double* U[3] = {};
     double* lam = nullptr;        /* per slot: cds(|U|) / 2                 */
     double* d = nullptr;          /* per slot: lifted flux                  */
+    /* non-conforming faces, per mortar slot (the segregated scheme's buffers) */
+    double* mq[4] = {};           /* coarse side: |U| (lambda), then U T, T */
+    double* mf[3] = {};           /* face flux vectors                      */
+    double* dC = nullptr;         /* projected, lifted coarse-side flux     */
 };
 
 int nsem_seg_prepare(const NsemDev* m);

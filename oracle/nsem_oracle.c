@@ -1122,18 +1122,40 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
     memcpy(T, T_in, (size_t)n_int * sizeof(double));
     ghosts_velocity(m, U);
     ghosts_scalar(m, T);
+    /* non-conforming faces: coarse side interpolated, fluxes projected back */
+    const int mort = m->n_mortar > 0;
+    int8_t* side = mort ? mortar_sides(m) : NULL;
+    double* nq = mort ? calloc(4 * na, sizeof(double)) : NULL;
+    double* ms = mort ? calloc(4 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* mF = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* mP = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
+    double* dC = mort ? calloc((size_t)n_slot, sizeof(double)) : NULL;
+    if (mort) {
+        for (int64_t i = 0; i < n_int; i++) nq[i] = vmag(U + 3 * i);
+        mortar_scatter(m, 1, nq, ms);
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < n_slot; k++) {
         uint32_t c1 = m->FO[k], c2 = m->FN[k];
         if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
         const double fi = m->fI[k], fo = 1 - fi;
-        lam[k] = (vmag(U + 3 * (size_t)c1) * fi + vmag(U + 3 * (size_t)c2) * fo) / 2;
+        double u1 = vmag(U + 3 * (size_t)c1), u2 = vmag(U + 3 * (size_t)c2);
+        if (mort && side[k] == 1) u1 = ms[k];
+        if (mort && side[k] == 2) u2 = ms[k];
+        lam[k] = (u1 * fi + u2 * fo) / 2;
     }
     const double c_dt = -1.0 / dt;
     for (int step = 0; step < nsteps; step++) {
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * T[i];
+        if (mort) {
+            for (int64_t i = 0; i < n_int; i++) {
+                for (int c = 0; c < 3; c++) nq[4 * i + c] = Fv[3 * i + c];
+                nq[4 * i + 3] = T[i];
+            }
+            mortar_scatter(m, 4, nq, ms);
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n_slot; k++) {
             uint32_t c1 = m->FO[k], c2 = m->FN[k];
@@ -1142,12 +1164,24 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
             const double* n = m->fN + 3 * k;
             const double mgn = vmag(n);
             const double en[3] = {n[0] / mgn, n[1] / mgn, n[2] / mgn};
-            double F[3], jump = lam[k] * (T[c2] - T[c1]);
-            for (int c = 0; c < 3; c++)
-                F[c] = (Fv[3 * (size_t)c1 + c] * fi + Fv[3 * (size_t)c2 + c] * fo) - en[c] * jump;
+            const double* F1 = Fv + 3 * (size_t)c1;
+            const double* F2 = Fv + 3 * (size_t)c2;
+            double T1 = T[c1], T2 = T[c2];
+            const int sd = mort ? side[k] : 0;
+            if (sd == 1) { F1 = ms + 4 * k; T1 = ms[4 * k + 3]; }
+            if (sd == 2) { F2 = ms + 4 * k; T2 = ms[4 * k + 3]; }
+            double F[3], jump = lam[k] * (T2 - T1);
+            for (int c = 0; c < 3; c++) F[c] = (F1[c] * fi + F2[c] * fo) - en[c] * jump;
             d[k] = vdot(F, n);
+            if (sd)
+                for (int c = 0; c < 3; c++) mF[3 * k + c] = F[c];
         }
-        seg_divf(m, 1, Fv, d, NULL, NULL, r);
+        if (mort) {
+            mortar_gather(m, 3, mF, mP);
+            for (int64_t k = 0; k < n_slot; k++)
+                if (side[k]) dC[k] = vdot(mP + 3 * k, m->fN + 3 * k);
+        }
+        seg_divf(m, 1, Fv, d, side, dC, r);
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_int; i++) {
             const double ap = c_dt * m->cV[i];
@@ -1157,4 +1191,5 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
     }
     memcpy(T_in, T, (size_t)n_int * sizeof(double));
     free(U); free(T); free(Fv); free(lam); free(d); free(r);
+    free(side); free(nq); free(ms); free(mF); free(mP); free(dC);
 }

@@ -80,10 +80,13 @@ AMR_PLAN = {
     "g3_4n3": ("g3_4n3", 0.005, 10, 0.0, 0.2),
 }
 
-# fixture -> (case, dt, steps, wind) for the reference's scalar convection app
+# fixture -> (case, dt, steps, wind[, refinement threshold]) for the
+# reference's scalar convection app; with a threshold the mesh is refined once
+# by prepare -refine first (2:1 non-conforming faces)
 CONV_PLAN = {
     "c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0)),
     "g3_2": ("g3_2", 1.0, 30, (6.0, -4.0, 5.0)),
+    "amr_c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0), 0.3),
 }
 
 KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
@@ -240,21 +243,32 @@ def make_conv_case(name, ref_bin, tmp):
     the step-0 fields from the harness (run on a copy of the controls naming
     the euler solver, which the harness binary requires)."""
     from nebulasem_gb300.fields import read_field
-    base, dt, nsteps, wind = CONV_PLAN[name]
+    base, dt, nsteps, wind = CONV_PLAN[name][:4]
+    fmax = CONV_PLAN[name][4] if len(CONV_PLAN[name]) > 4 else None
     case = os.path.join(tmp, "conv_" + name)
-    write_case(case, dt=dt, steps=nsteps, solver="convection", wind=wind, **CASES[base])
+    write_case(case, dt=dt, steps=nsteps, solver="convection", wind=wind, refine=fmax,
+               **CASES[base])
     with open(os.path.join(case, "controls")) as f:
         ctl = f.read()
     with open(os.path.join(case, "controls_setup"), "w") as f:
         f.write(ctl.replace("solver                       convection",
                             "solver                       euler"))
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    if fmax:
+        run([os.path.join(ref_bin, "prepare"), "./controls_setup", "-refine"], case)
     os.makedirs(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "euler_oracle"), "./controls_setup", "setup", "out"], case)
     d = load_dump(os.path.join(case, "out"))
     run([os.path.join(ref_bin, "convection"), "./controls"], case)
     n_int = int(d["meta"][7])
     out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    if fmax:
+        assert len(d["mortar"]) > 0, "no cell was refined"
+        out["mortar"] = d["mortar"]
+        for dd in range(3):
+            for h in range(2):
+                out[f"psiRef{dd}{h}"] = d[f"psiRef{dd}{h}"]
+                out[f"psiCor{dd}{h}"] = d[f"psiCor{dd}{h}"]
     out["fld0_U"] = d["fld_U"][:3 * n_int]
     out["fld0_T"] = d["fld_T"][:n_int]
     v = read_field(os.path.join(case, "T1.bin")).values
