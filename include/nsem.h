@@ -15,7 +15,8 @@
  * The reference has no plugin or FFI layer: its operator API is the set of
  * header templates in src/field/field.h over MeshField arrays and the Mesh::
  * and DG:: globals.  A C++ caller of the reference binds this ABI by passing
- * those globals and arrays directly.
+ * those globals and arrays directly: nsem_mesh_desc below names, field by
+ * field, the global each member takes.
  *
  * Conventions
  *  - node index n = e*NP + i*NPY*NPZ + j*NPZ + k (src/field/dg.h:43-44);
@@ -236,9 +237,14 @@ nsem_status nsem_sync(nsem_ctx* ctx);
  * NSEM_TOO_LARGE; NULL pointers or bad constants return NSEM_BAD_ARG.
  * The first call on a device resolves the array's device address for that
  * device (set-up once per device); make that first call before any stream
- * capture.  Every call shares the one array and fully rewrites the part it
- * uses, so calls that overlap on the GPU (different streams or host threads
- * without ordering) race with each other. */
+ * capture.  The address is kept for the life of the process: after
+ * cudaDeviceReset on that device, or when the caller runs in a context other
+ * than the device's primary context, it no longer names the array, so such
+ * callers must not use this entry point.  Every call shares the one array and
+ * fully rewrites the part it uses, so calls that overlap on the GPU
+ * (different streams or host threads without ordering) race with each other.
+ * A launch error left pending by the caller's own earlier work is returned
+ * (and cleared) as NSEM_CUDA_ERROR. */
 #define NSEM_NOALLOC_MAX_NODES ((int64_t)4096 * 65536)
 nsem_status nsem_conservation_sums_noalloc(const double* rho, const double* rhou,
                                            const double* rhov, const double* rhow,

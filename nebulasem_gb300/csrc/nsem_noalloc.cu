@@ -170,7 +170,11 @@ extern "C" nsem_status nsem_conservation_sums_noalloc(
     in.cv_heat = cv;
     const int nchunks = (int)((n_nodes + NSEM_NOALLOC_CHUNK - 1) / NSEM_NOALLOC_CHUNK);
     cudaStream_t st = (cudaStream_t)stream;
+    /* each launch is checked right after it; cudaGetLastError also returns
+     * (and clears) an error left pending by the caller's earlier launches,
+     * which is then reported as this call's NSEM_CUDA_ERROR */
     k_chunk_sums<<<nchunks, NT, 0, st>>>(in, scratch, nchunks);
+    if (cudaGetLastError() != cudaSuccess) return NSEM_CUDA_ERROR;
     k_final<<<1, NT, 0, st>>>(scratch, nchunks, out3);
     return cudaGetLastError() == cudaSuccess ? NSEM_OK : NSEM_CUDA_ERROR;
 }

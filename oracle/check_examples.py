@@ -12,7 +12,7 @@ geometry from the harness).  Examples the driver does not model (AMR,
 multi-block meshes, spherical problems, other time schemes) are reported with
 its message.
 
-    python oracle/check_examples.py --ref /root/reference srtb srtb-inclined srtb-curved ctbs dc lrtb
+    python oracle/check_examples.py --ref <reference source tree> srtb srtb-inclined srtb-curved ctbs dc lrtb
 """
 import argparse
 import os

@@ -22,7 +22,7 @@ Scalar convection fixtures (conv_<case>.npz): the unmodified reference
 `convection` app on a uniform wind; geometry, step-0 fields and its step-N T.
 
 Run in the build container (the reference is not present on GPU machines):
-  python tests/golden/make_golden.py --ref /root/reference
+  python tests/golden/make_golden.py --ref <reference source tree>
 """
 import argparse
 import os

@@ -1,0 +1,97 @@
+"""The rising-bubble workloads at their full sizes and step counts.
+
+Each 3D rising bubble (2000^3 m box, theta' = 0.5 K cosine of radius 400 m at
+(1000, 1000, 600) m, hydrostatic background theta0 = 300 K, SYMMETRY walls) is
+run from the same initial state in the plain FP64 form -- bit for bit the
+oracle on the golden fixtures and, below, at 32^3 -- and in the precision form
+(FP32 bulk, FP64 background subtraction, RK accumulation and compensated
+sums).  Gates:
+
+  * precision form against the FP64 form: relative L2 per conserved variable
+    <= 1e-5 after the stated step count (the precision form's stated
+    tolerance);
+  * drift of the compensated mass sum (euler.cpp:165-176, 263-274) over the
+    run <= 1e-12 relative in both forms (the scheme conserves mass; what is
+    left is the FP64 rounding of the state);
+  * 32^3, N = 4, 200 steps: the FP64 GPU final state equals the oracle's
+    (C restatement on the host cores, same correctly rounded pow) bit for bit.
+
+Time steps: the 32^3 mesh (h = 62.5 m) diverges at dt = 0.01 s and runs at
+0.0075 s; the 48^3 mesh (h = 41.7 m) at 0.005 s; 16^3 at N = 7 is stable at
+its stated 0.005 s.
+"""
+import numpy as np
+import pytest
+
+from conftest import VARS, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# workload, dt, steps
+CASES = {
+    "bubble3d_32_n4": (0.0075, 200),   # 32^3 elements, N = 4: 4.1 M nodes
+    "bubble3d_16_n7": (0.005, 400),    # 16^3 elements, N = 7: 2.1 M nodes
+    "bubble3d_48_n4": (0.005, 100),    # 48^3 elements, N = 4: 13.8 M nodes
+}
+TOL = 1e-5
+MASS_DRIFT = 1e-12
+
+
+def run_both(name):
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300.mesh import workload
+
+    dt, steps = CASES[name]
+    m, u0 = workload(name)
+    s = ng.Solver(m, dt=dt)
+    out = {}
+    for prec, tag in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
+        s.set_state(u0)
+        d0 = s.diagnostics()
+        s.step(steps, prec=prec)
+        u = s.get_state()
+        d1 = s.diagnostics()
+        out[tag] = u
+        out[tag + "_mass_drift"] = (d1[0] - d0[0]) / d0[0]
+    s.close()
+    return m, u0, out
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_precision_form_vs_fp64_full_size(name):
+    _, _, out = run_both(name)
+    ref, got = out["fp64"], out["mixed"]
+    for a, b, v in zip(got, ref, VARS):
+        assert np.isfinite(a).all(), v
+        err = rel_l2(a, b)
+        assert err <= TOL, f"{name} {v}: {err:.3e}"
+    th_ref = ref[4] / ref[0] - 300.0
+    th_got = got[4] / got[0] - 300.0
+    assert rel_l2(th_got, th_ref) <= TOL
+    for tag in ("fp64", "mixed"):
+        drift = out[tag + "_mass_drift"]
+        assert abs(drift) <= MASS_DRIFT, f"{name} {tag} mass drift {drift:.3e}"
+
+
+def test_fp64_full_size_equals_oracle_bitwise():
+    """32^3, N = 4, 200 steps of dt 0.0075: GPU and oracle (same inputs, same
+    host, correctly rounded pow) end in the same bits."""
+    import nebulasem_gb300 as ng
+    import oracle
+    from nebulasem_gb300.mesh import workload
+
+    dt, steps = CASES["bubble3d_32_n4"]
+    m, u0 = workload("bubble3d_32_n4")
+    s = ng.Solver(m, dt=dt)
+    s.set_state(u0)
+    s.step(steps, prec=ng.FP64)
+    got = s.get_state()
+    s.close()
+    om = oracle.OracleMesh(m)
+    oracle.set_pow(1)
+    try:
+        want = om.ssprk3(u0, dt, steps)
+    finally:
+        oracle.set_pow(0)
+    for a, b, v in zip(got, want, VARS):
+        assert np.array_equal(a, b), f"{v}: {int((a != b).sum())} values differ"

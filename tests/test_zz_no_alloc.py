@@ -48,6 +48,14 @@ def _check_case(mesh, u, gh, p_ref, dt):
     out = torch.zeros(3, dtype=torch.float64, device="cuda")
     fn = _noalloc_fn(ng.load())
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = [ctypes.c_void_p(t.data_ptr()) for t in dev]
+    # warm-up call (resolves the array's address on this device), then the
+    # device's free memory must not move across the checked calls
+    assert fn(*args, ctypes.c_void_p(cV.data_ptr()), ctypes.c_void_p(ghd.data_ptr()),
+              ctypes.c_void_p(prd.data_ptr()), n, 1e5, 1004.5, 717.5,
+              ctypes.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     for call in range(2):
         out.fill_(-1.0)
         st = fn(*[ctypes.c_void_p(t.data_ptr()) for t in dev],
@@ -55,6 +63,8 @@ def _check_case(mesh, u, gh, p_ref, dt):
                 ctypes.c_void_p(prd.data_ptr()), n, 1e5, 1004.5, 717.5,
                 ctypes.c_void_p(out.data_ptr()), stream)
         assert st == 0, f"call {call}: status {st}"
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0, "the call changed the device's free memory"
         got = out.cpu().numpy()
         assert np.allclose(got, want, rtol=RTOL, atol=0), (call, got, want)
     # beyond the fixed capacity: refused before any device work
@@ -74,4 +84,13 @@ def test_noalloc_sums_match_diagnostics_many_chunks():
     from nebulasem_gb300.mesh import workload
 
     m, u = workload("bubble3d_8_n4")
+    _check_case(m, u, m["gh"], m["p_ref"], 0.0075)
+
+
+def test_noalloc_sums_match_diagnostics_over_256_chunks():
+    # 4.1 M nodes = 1000 chunks: the final pass strides over its partial sums
+    # and merges several per thread
+    from nebulasem_gb300.mesh import workload
+
+    m, u = workload("bubble3d_32_n4")
     _check_case(m, u, m["gh"], m["p_ref"], 0.0075)
