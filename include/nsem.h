@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-#define NSEM_ABI_VERSION 4
+#define NSEM_ABI_VERSION 5
 
 typedef enum {
     NSEM_OK = 0,
@@ -197,6 +197,21 @@ nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5], doub
 nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every, double* ms_fwd);
 nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double* const lam0[5],
                          double* ms_adj);
+
+/* The same pair in either form (no reference counterpart).
+ * nsem_forward_checkpointed_prec: as nsem_forward_checkpointed, in the plain
+ * (NSEM_FP64) or the precision form (NSEM_MIXED: checkpoints of the FP64
+ * perturbation state; each segment's recomputation keeps the FP32 stage
+ * states).  nsem_adjoint then differentiates that run in its own form: the
+ * precision form's reverse sweep evaluates the transposed stage in FP32 at
+ * the forward's own FP32 stage states and accumulates the adjoint state in
+ * FP64.  nsem_vjp_prec: g = J_L(u)^T w in the given form (the precision form
+ * at the FP32 shadow of the current state).  The precision form needs an
+ * inviscid context on the meshes it supports (NSEM_UNSUPPORTED otherwise). */
+nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps, int ckpt_every,
+                                           nsem_precision prec, double* ms_fwd);
+nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const double* const w[5],
+                          double* const g[5]);
 
 /* Scalar DG convection: the reference's convection app (apps/convection/
  * convection.cpp with problem_init NONE and time_scheme BDF1), a scalar T

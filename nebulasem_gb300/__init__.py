@@ -90,6 +90,9 @@ def load(build_if_missing=True):
         "nsem_vjp": ([P, vp, vp], ctypes.c_int),
         "nsem_forward_checkpointed": ([P, ctypes.c_int, ctypes.c_int, P], ctypes.c_int),
         "nsem_adjoint": ([P, vp, vp, P], ctypes.c_int),
+        "nsem_forward_checkpointed_prec": ([P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P],
+                                           ctypes.c_int),
+        "nsem_vjp_prec": ([P, ctypes.c_int, vp, vp], ctypes.c_int),
         "nsem_jvp": ([P, vp, vp], ctypes.c_int),
         "nsem_convection_set": ([P, P, P], ctypes.c_int),
         "nsem_convection_step": ([P, ctypes.c_int], ctypes.c_int),
@@ -254,14 +257,14 @@ class Solver:
                 out[nm] = (ms[i], cnt[i])
         return out
 
-    def vjp(self, w):
-        """g = J_L(u)^T w at the current state (plain form)."""
+    def vjp(self, w, prec=FP64):
+        """g = J_L(u)^T w at the current state (plain or precision form)."""
         n = self.n_int
         ws = [_f64(a) for a in w]
         g = [np.empty(n) for _ in range(5)]
         wa = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in ws])
         ga = (ctypes.c_void_p * 5)(*[a.ctypes.data for a in g])
-        self._check(self._lib.nsem_vjp(self._ctx, wa, ga))
+        self._check(self._lib.nsem_vjp_prec(self._ctx, int(prec), wa, ga))
         return g
 
     def jvp(self, dv):
@@ -286,11 +289,12 @@ class Solver:
         self._check(self._lib.nsem_tlm(self._ctx, int(nsteps), da, oa, ctypes.byref(ms)))
         return out, ms.value
 
-    def forward_checkpointed(self, nsteps, ckpt_every):
-        """Advance nsteps FP64 steps keeping checkpoints; returns device ms."""
+    def forward_checkpointed(self, nsteps, ckpt_every, prec=FP64):
+        """Advance nsteps steps in the given form keeping checkpoints;
+        returns device ms.  adjoint() then differentiates this run."""
         ms = ctypes.c_double()
-        self._check(self._lib.nsem_forward_checkpointed(self._ctx, int(nsteps), int(ckpt_every),
-                                                        ctypes.byref(ms)))
+        self._check(self._lib.nsem_forward_checkpointed_prec(
+            self._ctx, int(nsteps), int(ckpt_every), int(prec), ctypes.byref(ms)))
         return ms.value
 
     def adjoint(self, lam_final):

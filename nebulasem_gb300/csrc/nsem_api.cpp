@@ -39,6 +39,7 @@ struct nsem_ctx {
      * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme) */
     int rep = 0;
     bool seg_pp_valid = false;   /* sbuf.pp holds the p' of the last segregated step */
+    int adj_form = -1;           /* form of the last checkpointed forward run (-1: none) */
     double dt = 0, T0 = 0;
     int64_t n_all = 0;
     std::vector<void*> allocations;
@@ -534,6 +535,12 @@ void nsem_destroy(nsem_ctx* ctx) {
     for (void* p : ctx->allocations) cudaFree(p);
     if (ctx->abuf.ckpt) cudaFree(ctx->abuf.ckpt);
     if (ctx->abuf.seg) cudaFree(ctx->abuf.seg);
+    {
+        NsemMixedBuf& M = ctx->mbuf;
+        void* mp[] = {M.ckpt, M.seg, M.lam, M.fin, M.abar[0], M.abar[1], M.abar[2]};
+        for (void* p : mp)
+            if (p) cudaFree(p);
+    }
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -953,6 +960,123 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
     A.nsteps = nsteps;
     A.every = ckpt_every;
     A.n_ckpt = n_ckpt;
+    ctx->adj_form = 0;
+    return NSEM_OK;
+}
+
+/* the precision form's checkpointed forward run */
+static nsem_status mixed_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
+                                              double* ms_fwd) {
+    if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+    if (ctx->mbuf.visc)
+        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
+    nsem_status s = ensure_rep(ctx, 1);
+    if (s != NSEM_OK) return s;
+    ctx->adj_form = -1;
+    cudaEvent_t e0, e1;
+    NSEM_CUDA(cudaEventCreate(&e0));
+    NSEM_CUDA(cudaEventCreate(&e1));
+    NSEM_CUDA(cudaEventRecord(e0, ctx->stream));
+    int e = nsem_mixed_fwd_ckpt(&ctx->dev, &ctx->mbuf, nsteps, ckpt_every, ctx->dt, ctx->stream);
+    if (e) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return e == (int)cudaErrorMemoryAllocation
+                   ? fail(ctx, NSEM_NO_MEMORY, "checkpoint allocation failed")
+                   : cuda_fail(ctx, (cudaError_t)e, "checkpointed forward");
+    }
+    NSEM_CUDA(cudaEventRecord(e1, ctx->stream));
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    s = check_status(ctx);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != NSEM_OK) return s;
+    if (ms_fwd) *ms_fwd = ms;
+    ctx->adj_form = 1;
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps, int ckpt_every,
+                                                      nsem_precision prec, double* ms_fwd) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (prec == NSEM_FP64) return nsem_forward_checkpointed(ctx, nsteps, ckpt_every, ms_fwd);
+    if (prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    if (ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    return mixed_forward_checkpointed(ctx, nsteps, ckpt_every, ms_fwd);
+}
+
+extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const double* const w[5],
+                                     double* const g[5]) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (prec == NSEM_FP64) return nsem_vjp(ctx, w, g);
+    if (prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
+    if (ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
+    for (int v = 0; v < 5; v++)
+        if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
+    if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
+    if (ctx->mbuf.visc)
+        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    nsem_status s = ensure_rep(ctx, 1);
+    if (s != NSEM_OK) return s;
+    int e = nsem_mixed_adj_alloc(&ctx->mbuf);
+    if (e) return fail(ctx, NSEM_NO_MEMORY, "adjoint allocation failed");
+    const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);
+    NsemBuf* b = &ctx->buf;
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(b->L[v], w[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    e = nsem_mixed_vjp(&ctx->dev, &ctx->mbuf, b->L, b->L, ctx->mbuf.abar[0], ctx->mbuf.abar[1],
+                       ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "precision-form vjp");
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(g[v], b->L[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+/* the precision form's reverse sweep of the last checkpointed run */
+static nsem_status mixed_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
+                                 double* const lam0[5], double* ms_adj) {
+    NsemMixedBuf& M = ctx->mbuf;
+    NsemBuf* b = &ctx->buf;
+    const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);
+    for (int v = 0; v < 5; v++) {
+        if (!lam_final[v] || !lam0[v]) return fail(ctx, NSEM_BAD_ARG, "lam array is NULL");
+        NSEM_CUDA(cudaMemcpyAsync(b->L[v], lam_final[v], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    /* the state is read back through ensure_rep after the sweep: the sweep
+     * needs the precision form's buffers, not the conserved copy */
+    nsem_status s = ensure_rep(ctx, 1);
+    if (s != NSEM_OK) return s;
+    int e = nsem_mixed_layout(&M, 0, b->L, M.lam, nullptr, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "adjoint layout");
+    cudaEvent_t e0, e1;
+    NSEM_CUDA(cudaEventCreate(&e0));
+    NSEM_CUDA(cudaEventCreate(&e1));
+    NSEM_CUDA(cudaEventRecord(e0, ctx->stream));
+    e = nsem_mixed_adjoint_run(&ctx->dev, &M, ctx->dt, ctx->stream);
+    if (e) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(ctx, (cudaError_t)e, "precision-form adjoint sweep");
+    }
+    NSEM_CUDA(cudaEventRecord(e1, ctx->stream));
+    e = nsem_mixed_layout(&M, 1, nullptr, M.lam, b->L, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "adjoint layout");
+    for (int v = 0; v < 5; v++)
+        NSEM_CUDA(cudaMemcpyAsync(lam0[v], b->L[v], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    s = check_status(ctx);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != NSEM_OK) return s;
+    if (ms_adj) *ms_adj = ms;
     return NSEM_OK;
 }
 
@@ -961,6 +1085,10 @@ extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final
     if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
+    if (ctx->adj_form == 1) {
+        NSEM_CUDA(cudaSetDevice(ctx->device));
+        return mixed_adjoint(ctx, lam_final, lam0, ms_adj);
+    }
     NsemAdjBuf& A = ctx->abuf;
     if (!A.ready || !A.ckpt || A.nsteps < 1)
         return fail(ctx, NSEM_BAD_ARG, "no checkpointed forward run to differentiate");

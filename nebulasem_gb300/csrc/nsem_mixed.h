@@ -1,6 +1,7 @@
 /*
  * Precision form (FP32 bulk arithmetic, FP64 state, background subtraction,
- * RK accumulation and conservation sums) and auxiliary kernels.
+ * RK accumulation and conservation sums), its discrete adjoint, and
+ * auxiliary kernels.
  */
 #ifndef NSEM_MIXED_H
 #define NSEM_MIXED_H
@@ -13,26 +14,36 @@
 
 #define NSEM_RED_PARTIALS 1024
 
+/* State arrays are element-blocked: [n_elem][5][NP] (see nsem_mixed_dev.cuh). */
 struct NsemMixedBuf {
     bool ready = false;
     int64_t n_elem = 0;
+    int64_t n_int = 0;
     int npd[3] = {0, 0, 0};
     int n_layers = 0;
-    int cur = 0;                  /* which of U[0], U[1] holds u'^n      */
-    double* U[2][5] = {};         /* FP64 perturbation state, ping-pong   */
-    float* U32[2][5] = {};        /* FP32 shadow of U (read by the stages) */
-    float* D[2][5] = {};          /* FP32 stage increments                */
+    int cur = 0;                  /* which of U[0], U[1] holds u'^n        */
+    double* U[2] = {};            /* FP64 perturbation state, ping-pong     */
+    float* S[2] = {};             /* FP32 shadow of U (read by the stages)  */
+    float* D[2] = {};             /* FP32 stage increments                  */
     int32_t* nbr = nullptr;       /* [6][n_elem] neighbour element, -1 wall */
-    float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h       */
-    int32_t* layer = nullptr;     /* [n_elem] background layer             */
-    float* bg = nullptr;          /* [layers][3][NP] rho_ref, rho_ref T0, p_ref */
-    float* Qg = nullptr;          /* device copy of the line-sum weights   */
-    float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a) */
-    float* Gv[12] = {};           /* viscous runs: grad U, grad theta of the stage state (FP32) */
-    bool visc = false;            /* artificial viscosity (diffusion YES) */
-    float nu = 0, nu_pr = 0;      /* nu and nu / Pr */
-    void* tabs = nullptr;         /* host copy of the kernel tables        */
-    size_t tabs_size = 0;
+    float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h        */
+    int32_t* layer = nullptr;     /* [n_elem] background layer              */
+    float* bg = nullptr;          /* [layers][4][NP] rho_ref, Theta_ref, 1/Theta_ref, p_ref */
+    float* Qg = nullptr;          /* line-sum weights Q_d[a][m], row stride MAXN+1 */
+    float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a), same layout */
+    float* G = nullptr;           /* viscous runs: [n_elem][12][NP] gradients of the stage state */
+    bool visc = false;            /* artificial viscosity (diffusion YES)   */
+    float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
+    float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
+    /* discrete adjoint (allocated on first use) */
+    double* ckpt = nullptr;       /* [n_ckpt][5 n_int] FP64 checkpoints of u'      */
+    float* seg = nullptr;         /* [seg_steps][3][5 n_int] per step: shadow, d1, d2 */
+    int64_t seg_steps = 0, ckpt_slots = 0;
+    double* lam = nullptr;        /* [5 n_int] FP64 adjoint state             */
+    double* fin = nullptr;        /* [5 n_int] FP64 final state of the forward */
+    float* abar[3] = {};          /* FP32 stage adjoints: sbar, d2bar, d1bar  */
+    int nsteps = 0, every = 0, n_ckpt = 0;
+    int fin_cur = 0;
 };
 
 /* u' <-> u conversion of the current state (to_pert: buf.u -> U[cur]) */
@@ -45,6 +56,26 @@ int nsem_mixed_steps(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, const Nse
                      int nsteps, double dt, void* stream);
 int nsem_mixed_tendency(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, const NsemTables* t,
                         void* stream);
+
+bool nsem_mixed_supported(int nx, int ny, int nz);
+/* one SSP-RK3 step with explicit buffers (element-blocked): stage base S (the
+ * FP32 shadow of u'^n), increments d1 and d2, FP64 u'^n -> Unew with its
+ * shadow Snew */
+int nsem_mixed_step_bufs(const NsemDev* dev, const NsemMixedBuf* mb, const double* U,
+                         const float* S, float* d1, float* d2, double* Unew, float* Snew,
+                         double dt, void* stream);
+
+/* discrete adjoint of the precision form (nsem_mixed_adj.cu) */
+int nsem_mixed_adj_prepare(const NsemMixedBuf* mb);
+int nsem_mixed_adj_alloc(NsemMixedBuf* mb);
+/* dir 0: node-order SoA soa[5] -> element-blocked blk; dir 1: blk -> soa_out[5] */
+int nsem_mixed_layout(const NsemMixedBuf* mb, int dir, const double* const soa[5], double* blk,
+                      double* const soa_out[5], void* stream);
+int nsem_mixed_vjp(const NsemDev* dev, NsemMixedBuf* mb, const double* const w[5],
+                   double* const g[5], float* scratch_in, float* scratch_out, void* stream);
+int nsem_mixed_fwd_ckpt(const NsemDev* dev, NsemMixedBuf* mb, int nsteps, int every, double dt,
+                        void* stream);
+int nsem_mixed_adjoint_run(const NsemDev* dev, NsemMixedBuf* mb, double dt, void* stream);
 
 /* launch-by-launch interface for measurement (nsem_profile) */
 const char* const* nsem_mixed_kernel_names();

@@ -1,0 +1,714 @@
+/*
+ * Discrete adjoint of the precision form (FP32 bulk, FP64 adjoint state).
+ * No reference counterpart: the reference has no adjoint.  This is the
+ * transpose of the precision form's stage (nsem_mixed.cu), i.e. of the
+ * operator chain of field.h:2928-2943 (Rusanov flux), 3086-3117 (weak lift)
+ * and 3440-3464 (volume term), evaluated at the precision form's own FP32
+ * stage states.
+ *
+ * Tendency of node a (element e, stage state x, FP32):
+ *   L_a = sum_d J_d sum_m Q_d[a_d][m] F_d(x_m)                (volume)
+ *       - sum_{faces f through a} C_f Phi_f(x_a, x_o)           (lift, C_f = J_d / w_end)
+ *       + (0, rho'_a g, 0)                                      (buoyancy)
+ * with Phi_f = s (F_n(x_a) + F_n(x_o)) / 2 - lam (q_o - q_a) (mass, normal
+ * momentum, Theta' components), lam = (|u|_a + |u|_o + c_a + c_o) / 4, or on a
+ * wall Phi = e_n (s p'_a + lam_w m_n,a), lam_w = (|u_ghost| + c_a) / 2.  The
+ * neighbour's element sees -Phi.  Given gbar per node, the transpose is
+ *   xbar_b = sum_d JF_d(x_b)^T Fbar_d(b) + face terms + buoyancy, with
+ *   Fbar_d(b) = J_d sum_a Q_d[a_d][b_d] gbar_a       (transposed line sums),
+ * and on each face node of the element Phibar = C'_f gbar_o - C_f gbar_a
+ * (both elements' lifts of the shared flux): JF_n(x_a)^T (s Phibar / 2) is
+ * merged into Fbar_n, and the terms of lam and of the jump are added directly.
+ *
+ * Reverse of one SSP-RK3 step in increment form (x1 = S, x2 = S + d1,
+ * x3 = S + d2 the FP32 stage states of the forward step, S = fp32(u'^n)):
+ *   R3: gbar = 2/3 lam;   xbar3 = dt J(x3)^T gbar;  A = xbar3;  B = 2/3 lam + xbar3
+ *   R2: gbar = B / 4;     xbar2 = dt J(x2)^T gbar;  A += xbar2; C = B / 4 + xbar2
+ *   R1: gbar = C;         xbar1 = dt J(x1)^T gbar;  lam <- lam + A + xbar1 (FP64)
+ * One fused kernel per reverse stage, one element per CTA, structured like the
+ * forward stage kernel: phase 1 (node) primitives and derivative data, phase 2
+ * (face node) face adjoints, phase 3 (node) transposed line sums, pointwise
+ * transposes and the stage combination.
+ */
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "nsem_mixed.h"
+#include "nsem_mixed_dev.cuh"
+
+using namespace nsem_mx;
+
+namespace {
+
+struct AdjArgs {
+    const float* S;            /* stage base: FP32 shadow of u'^n, [e][5][NP] */
+    const float* Din;          /* d2 (R3), d1 (R2), null (R1, R0)             */
+    const double* lam;         /* FP64 adjoint state (R3 input, R1 in/out)    */
+    double* lam_out;           /* R1                                          */
+    const float* Gin;          /* B (R2), C (R1), w (R0)                      */
+    float* A;                  /* sbar accumulator (R3 writes, R2 updates, R1 reads) */
+    float* Bout;               /* R3: d2bar; R2: d1bar (C); R0: xbar          */
+    const int32_t* nbr;
+    const float* J;
+    const int32_t* layer;
+    const float* Qg;
+    const float* bg;
+    int64_t n_elem;
+    float dt, gamma, gR, g[3];
+    float lift[3];
+    float eos[6];
+};
+
+template <int NX, int NY, int NZ>
+struct AdjSmem {
+    using G = Geo<NX, NY, NZ>;
+    static constexpr int NP = G::NP, NFS = G::NFS;
+    /* floats: gbar G4[NP] (x4) + G1[NP]; own values P[3][NP] (x4) and
+     * Theta'; face results Fa4[NFS] (x4) + Fa1[NFS] (merged into Fbar_n),
+     * Xd4[NFS] (x4) + Xd1[NFS] (added to xbar); Q; metric */
+    static constexpr int OFF_G1 = 4 * NP;
+    static constexpr int OFF_P = (5 * NP + 3) / 4 * 4;
+    static constexpr int OFF_T = OFF_P + 12 * NP;
+    static constexpr int OFF_FA4 = (OFF_T + NP + 3) / 4 * 4;
+    static constexpr int OFF_FA1 = OFF_FA4 + 4 * NFS;
+    static constexpr int OFF_XD4 = (OFF_FA1 + NFS + 3) / 4 * 4;
+    static constexpr int OFF_XD1 = OFF_XD4 + 4 * NFS;
+    static constexpr int OFF_Q = OFF_XD1 + NFS;
+    static constexpr int OFF_META = OFF_Q + QTAB;
+    static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
+};
+
+template <int NX, int NY, int NZ>
+constexpr int adj_min_blocks() {
+    /* order 7 (512 threads): two CTAs with 64 registers, no spills */
+    return min_blocks(Geo<NX, NY, NZ>::BLOCK >= 512 ? 2 : 6, Geo<NX, NY, NZ>::BLOCK,
+                      AdjSmem<NX, NY, NZ>::BYTES);
+}
+
+/* gbar of a node from the stage's input: 2/3 lam (R3), B/4 (R2), C (R1), w (R0) */
+template <int RS>
+__device__ __forceinline__ void load_gbar(const AdjArgs& a, int64_t o, int np, float* gb) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        if constexpr (RS == 3) gb[v] = (2.0f / 3.0f) * d2f_rn(__ldg(a.lam + o + v * np));
+        else if constexpr (RS == 2) gb[v] = 0.25f * __ldg(a.Gin + o + v * np);
+        else gb[v] = __ldg(a.Gin + o + v * np);
+    }
+}
+
+/* xbar += JF_d(x)^T fb for the volume flux along d:
+ *   F_d = (m_d, m_c u_d + p' delta_cd, m_d theta) */
+template <int D>
+__device__ __forceinline__ void jft(const float* u, float th, float pth, float fa, float fb0,
+                                    float fb1, float fb2, float ft, float* xb) {
+    const float ud = u[D];
+    const float bu = fmaf(fb0, u[0], fmaf(fb1, u[1], fb2 * u[2]));
+    const float w = fmaf(ft, th, bu);                 /* b.u + t theta */
+    xb[0] = fmaf(-ud, w, xb[0]);
+    xb[1] = fmaf(fb0, ud, xb[1]);
+    xb[2] = fmaf(fb1, ud, xb[2]);
+    xb[3] = fmaf(fb2, ud, xb[3]);
+    xb[1 + D] += fa + w;
+    const float fbd = D == 0 ? fb0 : D == 1 ? fb1 : fb2;
+    xb[4] = fmaf(fbd, pth, fmaf(ft, ud, xb[4]));
+}
+
+/* phase 2: adjoint of the flux through face node t of direction DIR */
+template <int NX, int NY, int NZ, int DIR>
+__device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const float* xo,
+                                         const float* bgo, const float* go, float cn,
+                                         const float4* sG4, const float* sG1, const float4* sP,
+                                         const float* sT, float cs, const AdjArgs& a, float4& fa4,
+                                         float& fa1, float4& xd4, float& xd1) {
+    constexpr int NP = Geo<NX, NY, NZ>::NP;
+    const float sg = fs.side ? 1.0f : -1.0f;
+    const float4 P0 = sP[fs.la], P1 = sP[NP + fs.la], P2 = sP[2 * NP + fs.la];
+    const float tp_s = sT[fs.la];
+    /* own values: P0 = (rho', m0, m1, m2), P1 = (rho, |u|, c, 1/Theta),
+     * P2 = (u0, u1, u2, dp'/dTheta') */
+    const float rho = P1.x, um = P1.y, c = P1.z, iTh = P1.w;
+    const float inv = rcp_nr(rho);
+    const float4 ga4 = sG4[fs.la];
+    const float ga1 = sG1[fs.la];
+    const float md = DIR == 0 ? P0.y : DIR == 1 ? P0.z : P0.w;
+    const float uvec[3] = {P2.x, P2.y, P2.z};
+    if (nb >= 0) {
+        const Pt q = pointwise(xo, bgo, a.eos, a.gamma, a.gR);
+        const float lam = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(um, q.umag), __fadd_rn(c, q.c)));
+        /* Phibar = C' gbar_o - C gbar_a */
+        const float pb0 = fmaf(cn, go[0], -cs * ga4.x);
+        const float pb1 = fmaf(cn, go[1], -cs * ga4.y);
+        const float pb2 = fmaf(cn, go[2], -cs * ga4.z);
+        const float pb3 = fmaf(cn, go[3], -cs * ga4.w);
+        const float pb4 = fmaf(cn, go[4], -cs * ga1);
+        const float h = 0.5f * sg;
+        fa4 = make_float4(h * pb0, h * pb1, h * pb2, h * pb3);
+        fa1 = h * pb4;
+        const float pbm = DIR == 0 ? pb1 : DIR == 1 ? pb2 : pb3;
+        /* jump terms: d(-lam (q_o - q_a))/dx_a = lam on the masked components,
+         * minus (jump . Phibar) dlam/dx_a */
+        const float jr = xo[0] - P0.x, jm = xo[1 + DIR] - md, jt = xo[4] - tp_s;
+        const float s = fmaf(jr, pb0, fmaf(jm, pbm, jt * pb4));
+        /* dlam/dx_a = (d|u| + dc) / 4: d|u|/drho' = -|u|/rho, d|u|/dm_k = u_k/(rho |u|),
+         * dc/drho' = -c/(2 rho), dc/dTheta' = c/(2 Theta) */
+        const float ku = um > 0.0f ? inv * rcp_nr(um) : 0.0f;
+        const float q4 = -0.25f * s;
+        float x0 = fmaf(q4, -fmaf(0.5f, c, um) * inv, lam * pb0);
+        float xm[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) xm[k] = q4 * (uvec[k] * ku);
+        xm[DIR] = fmaf(lam, pbm, xm[DIR]);
+        const float x4 = fmaf(q4, 0.5f * c * iTh, lam * pb4);
+        xd4 = make_float4(x0, xm[0], xm[1], xm[2]);
+        xd1 = x4;
+    } else {
+        /* wall: Phi_n = s p' + lam_w m_n; Phibar = -C gbar_a (normal momentum) */
+        const float pbm = -cs * (DIR == 0 ? ga4.y : DIR == 1 ? ga4.z : ga4.w);
+        const float r0 = DIR == 0 ? 0.0f : uvec[0];
+        const float r1 = DIR == 1 ? 0.0f : uvec[1];
+        const float r2 = DIR == 2 ? 0.0f : uvec[2];
+        const float mr = safe_sqrt(__fmaf_rn(r0, r0, __fmaf_rn(r1, r1, __fmul_rn(r2, r2))));
+        const bool full = mr > 1e-7f;
+        const float um_g = full ? um : mr;
+        const float lam = __fmul_rn(0.5f, __fadd_rn(um_g, c));
+        /* d|u_ghost|: of |u| (rescaled tangential velocity) or of |r| */
+        const float nrm = full ? um : mr;
+        const float ku = nrm > 0.0f ? inv * rcp_nr(nrm) : 0.0f;
+        const float q2 = 0.5f * md * pbm;
+        const float vr[3] = {full ? uvec[0] : r0, full ? uvec[1] : r1, full ? uvec[2] : r2};
+        float x0 = q2 * -fmaf(0.5f, c, um_g) * inv;
+        float xm[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) xm[k] = q2 * (vr[k] * ku);
+        xm[DIR] = fmaf(lam, pbm, xm[DIR]);
+        const float x4 = fmaf(q2, 0.5f * c * iTh, sg * P2.w * pbm);
+        fa4 = make_float4(0, 0, 0, 0);
+        fa1 = 0.0f;
+        xd4 = make_float4(x0, xm[0], xm[1], xm[2]);
+        xd1 = x4;
+    }
+}
+
+template <int NX, int NY, int NZ, int RS>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (adj_min_blocks<NX, NY, NZ>()))
+k_mixed_adj(AdjArgs a) {
+    using G = Geo<NX, NY, NZ>;
+    using SM = AdjSmem<NX, NY, NZ>;
+    constexpr int NP = G::NP;
+    constexpr int NFS = G::NFS;
+    extern __shared__ float4 asm4[];
+    float* smem = reinterpret_cast<float*>(asm4);
+    float4* sG4 = asm4;
+    float* sG1 = smem + SM::OFF_G1;
+    float4* sP = reinterpret_cast<float4*>(smem + SM::OFF_P);
+    float* sT = smem + SM::OFF_T;
+    float4* sFa4 = reinterpret_cast<float4*>(smem + SM::OFF_FA4);
+    float* sFa1 = smem + SM::OFF_FA1;
+    float4* sXd4 = reinterpret_cast<float4*>(smem + SM::OFF_XD4);
+    float* sXd1 = smem + SM::OFF_XD1;
+    float* sQ = smem + SM::OFF_Q;
+    float* sMeta = smem + SM::OFF_META;
+
+    const int t = threadIdx.x;
+    const int64_t e = blockIdx.x;
+    constexpr bool has_din = RS == 3 || RS == 2;
+
+    float x[5], gb[5], bgs[4] = {0, 0, 0, 0};
+    if (t < NP) {
+        const int64_t o = e * 5 * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) x[v] = __ldg(a.S + o + v * NP);
+        if constexpr (has_din) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) x[v] = __fadd_rn(x[v], __ldg(a.Din + o + v * NP));
+        }
+        load_gbar<RS>(a, o, NP, gb);
+        const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
+    }
+    FaceSlot fs{};
+    int32_t nb = -1;
+    float xo[5], bgo[4], go[5], cn = 0.0f;
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if (nb >= 0) {
+            const int64_t o = (int64_t)nb * 5 * NP + fs.lo;
+#pragma unroll
+            for (int v = 0; v < 5; v++) xo[v] = __ldg(a.S + o + v * NP);
+            if constexpr (has_din) {
+#pragma unroll
+                for (int v = 0; v < 5; v++) xo[v] = __fadd_rn(xo[v], __ldg(a.Din + o + v * NP));
+            }
+            load_gbar<RS>(a, o, NP, go);
+            const float* bg = a.bg + (int64_t)__ldg(a.layer + nb) * 4 * NP + fs.lo;
+#pragma unroll
+            for (int c = 0; c < 4; c++) bgo[c] = __ldg(bg + c * NP);
+            cn = __ldg(a.J + (int64_t)fs.dir * a.n_elem + nb) * a.lift[fs.dir];
+        }
+    }
+    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
+    if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
+
+    /* phase 1: gbar and the node's values for the face and pointwise transposes */
+    float uu[3], th = 0.0f, pth = 0.0f;
+    if (t < NP) {
+        const Pt p = pointwise(x, bgs, a.eos, a.gamma, a.gR);
+        const float Th = __fadd_rn(bgs[1], x[4]);
+        const float iTh = rcp_nr(Th);
+        pth = a.gamma * (bgs[3] + p.pp) * iTh;      /* dp'/dTheta' = gamma p / Theta */
+        uu[0] = p.u[0]; uu[1] = p.u[1]; uu[2] = p.u[2];
+        th = p.th;
+        sG4[t] = make_float4(gb[0], gb[1], gb[2], gb[3]);
+        sG1[t] = gb[4];
+        sP[t] = make_float4(x[0], x[1], x[2], x[3]);
+        sP[NP + t] = make_float4(p.rho, p.umag, p.c, iTh);
+        sP[2 * NP + t] = make_float4(p.u[0], p.u[1], p.u[2], pth);
+        sT[t] = x[4];
+    }
+    __syncthreads();
+
+    /* phase 2: face adjoints */
+    if (t < NFS) {
+        const float cs = sMeta[fs.dir] * a.lift[fs.dir];
+        float4 fa4, xd4;
+        float fa1, xd1;
+        if (fs.dir == 0)
+            face_adj<NX, NY, NZ, 0>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+        else if (G::HAS_Y && fs.dir == 1)
+            face_adj<NX, NY, NZ, 1>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+        else
+            face_adj<NX, NY, NZ, 2>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+        sFa4[t] = fa4;
+        sFa1[t] = fa1;
+        sXd4[t] = xd4;
+        sXd1[t] = xd1;
+    }
+    __syncthreads();
+
+    /* phase 3: transposed line sums, pointwise transposes, face and source terms */
+    if (t >= NP) return;
+    const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+    float xb[5] = {0, 0, 0, 0, 0};
+    {
+        /* x: Fbar_x(b) = J_x sum_a Q_x[a][i] gbar(a, j, k) */
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
+#pragma unroll
+        for (int m = 0; m < NX; m++) {
+            const float q = sQ[m * QS + i];
+            const int b = (m * NY + j) * NZ + k;
+            const float4 f = sG4[b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sG1[b], acc1);
+        }
+        const float Jx = sMeta[0];
+        acc.x *= Jx; acc.y *= Jx; acc.z *= Jx; acc.w *= Jx; acc1 *= Jx;
+        const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
+        if (sx >= 0) {
+            const float4 f = sFa4[sx];
+            acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sx];
+        }
+        jft<0>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+    }
+    if constexpr (G::HAS_Y) {
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
+#pragma unroll
+        for (int m = 0; m < NY; m++) {
+            const float q = sQ[MAXN * QS + m * QS + j];
+            const int b = (i * NY + m) * NZ + k;
+            const float4 f = sG4[b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sG1[b], acc1);
+        }
+        const float Jy = sMeta[1];
+        acc.x *= Jy; acc.y *= Jy; acc.z *= Jy; acc.w *= Jy; acc1 *= Jy;
+        const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
+        if (sy >= 0) {
+            const float4 f = sFa4[sy];
+            acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sy];
+        }
+        jft<1>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+    }
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+        float acc1 = 0.0f;
+#pragma unroll
+        for (int m = 0; m < NZ; m++) {
+            const float q = sQ[2 * MAXN * QS + m * QS + k];
+            const int b = (i * NY + j) * NZ + m;
+            const float4 f = sG4[b];
+            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
+            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
+            acc1 = fmaf(q, sG1[b], acc1);
+        }
+        const float Jz = sMeta[2];
+        acc.x *= Jz; acc.y *= Jz; acc.z *= Jz; acc.w *= Jz; acc1 *= Jz;
+        const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
+        if (sz >= 0) {
+            const float4 f = sFa4[sz];
+            acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sz];
+        }
+        jft<2>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+    }
+    /* direct face terms of the faces through the node */
+    auto direct = [&](int slot) {
+        const float4 f = sXd4[slot];
+        xb[0] += f.x; xb[1] += f.y; xb[2] += f.z; xb[3] += f.w; xb[4] += sXd1[slot];
+    };
+    {
+        const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
+        if (sx >= 0) direct(sx);
+        if constexpr (G::HAS_Y) {
+            const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
+            if (sy >= 0) direct(sy);
+        }
+        const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
+        if (sz >= 0) direct(sz);
+    }
+    /* buoyancy: L_m += rho' g */
+    xb[0] = fmaf(a.g[0], gb[1], fmaf(a.g[1], gb[2], fmaf(a.g[2], gb[3], xb[0])));
+
+    const int64_t o = e * 5 * NP + t;
+    if constexpr (RS == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.Bout[o + v * NP] = xb[v];
+        return;
+    }
+    const float dt = a.dt;
+    if constexpr (RS == 3) {
+        /* A = xbar3; B = 2/3 lam + xbar3 (gb = 2/3 lam) */
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x3 = dt * xb[v];
+            a.A[o + v * NP] = x3;
+            a.Bout[o + v * NP] = gb[v] + x3;
+        }
+    } else if constexpr (RS == 2) {
+        /* A += xbar2; C = B/4 + xbar2 (gb = B/4) */
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x2 = dt * xb[v];
+            a.A[o + v * NP] = __ldg(a.A + o + v * NP) + x2;
+            a.Bout[o + v * NP] = gb[v] + x2;
+        }
+    } else {
+        /* lam <- lam + A + xbar1 (FP64) */
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x1 = dt * xb[v];
+            const double l = __ldg(a.lam + o + v * NP);
+            a.lam_out[o + v * NP] = l + (f2d(__ldg(a.A + o + v * NP)) + f2d(x1));
+        }
+    }
+}
+
+template <int NX, int NY, int NZ>
+int launch_adj(const AdjArgs& a, int rs, cudaStream_t st) {
+    using G = Geo<NX, NY, NZ>;
+    constexpr int SMEM = (int)AdjSmem<NX, NY, NZ>::BYTES;
+    const unsigned grid = (unsigned)a.n_elem;
+    switch (rs) {
+        case 0: k_mixed_adj<NX, NY, NZ, 0><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 1: k_mixed_adj<NX, NY, NZ, 1><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 2: k_mixed_adj<NX, NY, NZ, 2><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        default: k_mixed_adj<NX, NY, NZ, 3><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+    }
+    return (int)cudaGetLastError();
+}
+
+template <int NX, int NY, int NZ>
+int prepare_adj() {
+    constexpr int SMEM = (int)AdjSmem<NX, NY, NZ>::BYTES;
+    if (SMEM <= 48 * 1024) return 0;
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    int e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 0>, at, SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 1>, at, SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 2>, at, SMEM);
+    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 3>, at, SMEM);
+    return e;
+}
+
+#define NSEM_ADJ_DIMS(X)  X(5, 5, 5) X(8, 8, 8) X(4, 4, 4) X(5, 1, 5) X(4, 1, 4)
+
+int dispatch_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
+    const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
+#define NSEM_ADJ(A, B, C) if (nx == A && ny == B && nz == C) return launch_adj<A, B, C>(a, rs, st);
+    NSEM_ADJ_DIMS(NSEM_ADJ)
+#undef NSEM_ADJ
+    return (int)cudaErrorNotSupported;
+}
+
+AdjArgs adj_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
+    AdjArgs a{};
+    a.nbr = mb->nbr;
+    a.J = mb->J;
+    a.layer = mb->layer;
+    a.Qg = mb->Qg;
+    a.bg = mb->bg;
+    a.n_elem = mb->n_elem;
+    a.dt = (float)dt;
+    a.gamma = (float)dev->gamma;
+    a.gR = (float)dev->gR;
+    for (int c = 0; c < 3; c++) {
+        a.g[c] = (float)dev->g[c];
+        a.lift[c] = mb->lift[c];
+    }
+    double ck = 1.0;
+    for (int k = 1; k <= 6; k++) {
+        ck *= (dev->gamma - (k - 1)) / k;
+        a.eos[k - 1] = (float)ck;
+    }
+    return a;
+}
+
+/* node-order SoA (5 arrays) <-> element-blocked, FP64 or FP32 */
+struct CPtr5 {
+    const double* p[5];
+};
+struct DPtr5 {
+    double* p[5];
+};
+
+template <int NP>
+__global__ void k_soa_to_blk(CPtr5 src, double* dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP, o = e * 5 * NP + (i - e * NP);
+#pragma unroll
+        for (int v = 0; v < 5; v++) dst[o + v * NP] = src.p[v][i];
+    }
+}
+
+template <int NP>
+__global__ void k_soa_to_blk32(CPtr5 src, float* dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP, o = e * 5 * NP + (i - e * NP);
+#pragma unroll
+        for (int v = 0; v < 5; v++) dst[o + v * NP] = (float)src.p[v][i];
+    }
+}
+
+template <int NP>
+__global__ void k_blk_to_soa(const double* src, DPtr5 dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP, o = e * 5 * NP + (i - e * NP);
+#pragma unroll
+        for (int v = 0; v < 5; v++) dst.p[v][i] = src[o + v * NP];
+    }
+}
+
+template <int NP>
+__global__ void k_blk32_to_soa(const float* src, DPtr5 dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP, o = e * 5 * NP + (i - e * NP);
+#pragma unroll
+        for (int v = 0; v < 5; v++) dst.p[v][i] = (double)src[o + v * NP];
+    }
+}
+
+__global__ void k_shadow(const double* U, float* S, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        S[i] = d2f_rn(U[i]);
+}
+
+int grid_for(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+int nsem_mixed_adj_prepare(const NsemMixedBuf* mb) {
+    const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
+#define NSEM_PREP(A, B, C) if (nx == A && ny == B && nz == C) return prepare_adj<A, B, C>();
+    NSEM_ADJ_DIMS(NSEM_PREP)
+#undef NSEM_PREP
+    return (int)cudaErrorNotSupported;
+}
+
+int nsem_mixed_layout(const NsemMixedBuf* mb, int dir, const double* const soa[5], double* blk,
+                      double* const soa_out[5], void* stream) {
+    const int NP = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    const int64_t n = mb->n_int;
+    cudaStream_t st = (cudaStream_t)stream;
+#define NSEM_LAY(A, B, C)                                                               \
+    if (NP == A * B * C) {                                                              \
+        if (dir == 0) {                                                                 \
+            CPtr5 s;                                                                    \
+            for (int v = 0; v < 5; v++) s.p[v] = soa[v];                                \
+            k_soa_to_blk<A * B * C><<<grid_for(n), 256, 0, st>>>(s, blk, n);            \
+        } else {                                                                        \
+            DPtr5 d;                                                                    \
+            for (int v = 0; v < 5; v++) d.p[v] = soa_out[v];                            \
+            k_blk_to_soa<A * B * C><<<grid_for(n), 256, 0, st>>>(blk, d, n);            \
+        }                                                                               \
+        return (int)cudaGetLastError();                                                 \
+    }
+    NSEM_ADJ_DIMS(NSEM_LAY)
+#undef NSEM_LAY
+    return (int)cudaErrorNotSupported;
+}
+
+/* g = J_L(u)^T w for the current precision-form state (tendency VJP, FP32
+ * bulk): w in five node-order FP64 arrays, g out likewise */
+int nsem_mixed_vjp(const NsemDev* dev, NsemMixedBuf* mb, const double* const w[5],
+                   double* const g[5], float* scratch_in, float* scratch_out, void* stream) {
+    const int NP = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    const int64_t n = mb->n_int;
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = 0;
+#define NSEM_W(A, B, C)                                                                 \
+    if (NP == A * B * C) {                                                              \
+        CPtr5 s;                                                                        \
+        for (int v = 0; v < 5; v++) s.p[v] = w[v];                                      \
+        k_soa_to_blk32<A * B * C><<<grid_for(n), 256, 0, st>>>(s, scratch_in, n);       \
+        e = (int)cudaGetLastError();                                                    \
+    }
+    NSEM_ADJ_DIMS(NSEM_W)
+#undef NSEM_W
+    if (e) return e;
+    AdjArgs a = adj_args(dev, mb, 0.0);
+    a.S = mb->S[mb->cur];
+    a.Gin = scratch_in;
+    a.Bout = scratch_out;
+    if ((e = dispatch_adj(mb, a, 0, st))) return e;
+#define NSEM_G(A, B, C)                                                                 \
+    if (NP == A * B * C) {                                                              \
+        DPtr5 d;                                                                        \
+        for (int v = 0; v < 5; v++) d.p[v] = g[v];                                      \
+        k_blk32_to_soa<A * B * C><<<grid_for(n), 256, 0, st>>>(scratch_out, d, n);      \
+        return (int)cudaGetLastError();                                                 \
+    }
+    NSEM_ADJ_DIMS(NSEM_G)
+#undef NSEM_G
+    return (int)cudaErrorNotSupported;
+}
+
+/* adjoint arrays (lam, fin, abar), allocated on first use */
+int nsem_mixed_adj_alloc(NsemMixedBuf* mb) {
+    if (mb->lam) return 0;
+    const int64_t n5 = 5 * mb->n_int;
+    cudaError_t ce = cudaMalloc((void**)&mb->lam, (size_t)n5 * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->fin, (size_t)n5 * sizeof(double));
+    for (int q = 0; q < 3 && ce == cudaSuccess; q++)
+        ce = cudaMalloc((void**)&mb->abar[q], (size_t)n5 * sizeof(float));
+    if (ce != cudaSuccess) return (int)ce;
+    return nsem_mixed_adj_prepare(mb);
+}
+
+/* Checkpointed forward run of the precision form from u'^n = U[cur]:
+ * checkpoints of u' (FP64) every `every` steps.  Storage (checkpoints, one
+ * segment of stage states, adjoint arrays) is allocated here, outside any
+ * stream capture. */
+int nsem_mixed_fwd_ckpt(const NsemDev* dev, NsemMixedBuf* mb, int nsteps, int every, double dt,
+                        void* stream) {
+    const int64_t n5 = 5 * mb->n_int;
+    const int n_ckpt = (nsteps + every - 1) / every;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (mb->ckpt_slots < n_ckpt) {
+        if (mb->ckpt) cudaFree(mb->ckpt);
+        mb->ckpt = nullptr;
+        mb->ckpt_slots = 0;
+        cudaError_t ce = cudaMalloc((void**)&mb->ckpt, (size_t)n_ckpt * n5 * sizeof(double));
+        if (ce != cudaSuccess) return (int)ce;
+        mb->ckpt_slots = n_ckpt;
+    }
+    if (mb->seg_steps < every) {
+        if (mb->seg) cudaFree(mb->seg);
+        mb->seg = nullptr;
+        mb->seg_steps = 0;
+        cudaError_t ce = cudaMalloc((void**)&mb->seg, (size_t)every * 3 * n5 * sizeof(float));
+        if (ce != cudaSuccess) return (int)ce;
+        mb->seg_steps = every;
+    }
+    int e = nsem_mixed_adj_alloc(mb);
+    if (e) return e;
+    int cur = mb->cur;
+    for (int s = 0; s < nsteps; s++) {
+        if (s % every == 0) {
+            cudaError_t ce = cudaMemcpyAsync(mb->ckpt + (int64_t)(s / every) * n5, mb->U[cur],
+                                             (size_t)n5 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            if (ce != cudaSuccess) return (int)ce;
+        }
+        if ((e = nsem_mixed_step_bufs(dev, mb, mb->U[cur], mb->S[cur], mb->D[0], mb->D[1],
+                                      mb->U[cur ^ 1], mb->S[cur ^ 1], dt, stream)))
+            return e;
+        cur ^= 1;
+    }
+    mb->cur = cur;
+    mb->nsteps = nsteps;
+    mb->every = every;
+    mb->n_ckpt = n_ckpt;
+    return 0;
+}
+
+/* Reverse sweep: lam (element-blocked FP64, mb->lam) holds dJ/du' at the
+ * final state; on return it holds dJ/du' at the initial state.  Each segment
+ * is recomputed from its checkpoint keeping S, d1, d2 of every step, then
+ * swept backwards.  The forward's final state is restored afterwards. */
+int nsem_mixed_adjoint_run(const NsemDev* dev, NsemMixedBuf* mb, double dt, void* stream) {
+    const int64_t n5 = 5 * mb->n_int;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int cur = mb->cur;
+    /* keep the final state (the recomputation uses the ping-pong buffers) */
+    cudaError_t ce = cudaMemcpyAsync(mb->fin, mb->U[cur], (size_t)n5 * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, st);
+    if (ce != cudaSuccess) return (int)ce;
+    int e = 0;
+    AdjArgs a = adj_args(dev, mb, dt);
+    for (int sg = mb->n_ckpt - 1; sg >= 0; sg--) {
+        const int start = sg * mb->every;
+        const int cnt = (mb->nsteps - start < mb->every) ? mb->nsteps - start : mb->every;
+        /* recompute the segment: step j reads U (FP64) and its shadow seg_S[j],
+         * writes d1, d2 into the segment and the next shadow into seg_S[j+1] */
+        const double* Uin = mb->ckpt + (int64_t)sg * n5;
+        float* S0 = mb->seg;
+        k_shadow<<<grid_for(n5), 256, 0, st>>>(Uin, S0, n5);
+        if ((e = (int)cudaGetLastError())) return e;
+        int pp = 0;
+        for (int j = 0; j < cnt; j++) {
+            float* Sj = mb->seg + (int64_t)j * 3 * n5;
+            float* d1 = Sj + n5;
+            float* d2 = Sj + 2 * n5;
+            /* the last step's next shadow is not needed: write it to the
+             * ping-pong shadow instead of past the segment */
+            float* Snext = (j + 1 < cnt) ? mb->seg + (int64_t)(j + 1) * 3 * n5 : mb->S[pp];
+            double* Unext = mb->U[pp];
+            if ((e = nsem_mixed_step_bufs(dev, mb, Uin, Sj, d1, d2, Unext, Snext, dt, stream)))
+                return e;
+            Uin = Unext;
+            pp ^= 1;
+        }
+        for (int j = cnt - 1; j >= 0; j--) {
+            const float* Sj = mb->seg + (int64_t)j * 3 * n5;
+            const float* d1 = Sj + n5;
+            const float* d2 = Sj + 2 * n5;
+            /* R3 at x3 = S + d2 */
+            a.S = Sj; a.Din = d2; a.lam = mb->lam; a.A = mb->abar[0]; a.Bout = mb->abar[1];
+            if ((e = dispatch_adj(mb, a, 3, st))) return e;
+            /* R2 at x2 = S + d1 */
+            a.S = Sj; a.Din = d1; a.Gin = mb->abar[1]; a.A = mb->abar[0]; a.Bout = mb->abar[2];
+            if ((e = dispatch_adj(mb, a, 2, st))) return e;
+            /* R1 at x1 = S */
+            a.S = Sj; a.Din = nullptr; a.Gin = mb->abar[2]; a.A = mb->abar[0];
+            a.lam = mb->lam; a.lam_out = mb->lam;
+            if ((e = dispatch_adj(mb, a, 1, st))) return e;
+        }
+    }
+    /* restore the final state and its shadow */
+    ce = cudaMemcpyAsync(mb->U[cur], mb->fin, (size_t)n5 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    if (ce != cudaSuccess) return (int)ce;
+    k_shadow<<<grid_for(n5), 256, 0, st>>>(mb->U[cur], mb->S[cur], n5);
+    return (int)cudaGetLastError();
+}
