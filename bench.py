@@ -20,6 +20,17 @@ advanced through one RK stage.
   --impl reference  times only that CPU path (the reference's own code does
                not run on the GPU machine: it has no GPU path, and its
                sources are not present there), on the same metric.
+  l2_vs_fp64, mass_drift, adjoint_over_forward
+               the metric's accuracy and adjoint parts, measured after the
+               timed region: relative L2 per conserved variable of the
+               precision form against the plain FP64 form after 200 steps
+               from the same initial state, the drift of the compensated mass
+               sum over those steps in both forms, and the reverse sweep's
+               device time over the plain forward's for 200 steps with
+               checkpoints every 20 (precision form; the FP64 form's ratio
+               beside it over 20 steps)
+  --stage-profile  prints per-kernel mean device times of a few steps (a short
+               fixed launch sequence for ncu captures) and exits
 
 Inputs (>= 560 MB of state, stage and primitive arrays) exceed the 129 MB L2,
 so no L2 flush is needed between timed steps.
@@ -164,6 +175,116 @@ def cpu_baseline(mesh, u, seconds, dt):
                       f"{sec:.2f} s"}
 
 
+def config(dofs, world):
+    """The workload as both arms name it."""
+    return {"workload": WORKLOAD, "elements": 32 ** 3, "order": 4, "dofs": dofs, "dt": DT,
+            "scheme": "SSP-RK3", "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (no flush needed)"}
+
+
+def accuracy(solver, u0, steps):
+    """Precision form against the plain FP64 form after `steps` steps from u0:
+    relative L2 per conserved variable (and of theta'), and the relative drift
+    of the compensated mass sum in both forms."""
+    import nebulasem_gb300 as ng
+
+    finals, drift = {}, {}
+    for prec, tag in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
+        solver.set_state(u0)
+        m0 = solver.diagnostics()[0]
+        solver.step(steps, prec=prec)
+        finals[tag] = solver.get_state()
+        drift[tag] = (solver.diagnostics()[0] - m0) / m0
+    ref, got = finals["fp64"], finals["mixed"]
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    l2 = {v: rel(a, b) for v, a, b in zip(ng.VARS, got, ref)}
+    l2["theta_prime"] = rel(got[4] / got[0] - 300.0, ref[4] / ref[0] - 300.0)
+    return {"steps": steps, "l2": l2, "mass_drift": drift}
+
+
+def adjoint_ratio(solver, mesh, u0, steps, every, prec):
+    """Device time of the reverse sweep over that of the plain (graph-launched)
+    forward run of the same steps, for J = 1/2 sum theta'^2 over the box
+    x in [800, 1200], z in [800, 1200] m."""
+    import torch
+
+    from nebulasem_gb300 import objective as ob
+
+    n = solver.n_int
+    xyz = np.asarray(mesh["cC"]).reshape(-1, 3)[:n]
+    mask = ob.box_mask(xyz, (800.0, 1200.0, 800.0, 1200.0))
+    stream = torch.cuda.ExternalStream(solver.stream)
+    solver.set_state(u0)
+    solver.step(steps, prec=prec)            # builds the graph
+    solver.set_state(u0)
+    solver.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.step(steps, prec=prec, sync=False)
+    e1.record(stream)
+    solver.sync()
+    ms_fwd = e0.elapsed_time(e1)
+    solver.set_state(u0)
+    ms_ckpt = solver.forward_checkpointed(steps, every, prec=prec)
+    _, ms_adj = solver.adjoint(ob.objective_grad(solver.get_state(), mask))
+    return {"steps": steps, "ckpt_every": every, "forward_ms": ms_fwd,
+            "checkpointed_forward_ms": ms_ckpt, "adjoint_ms": ms_adj,
+            "ratio": ms_adj / ms_fwd}
+
+
+def stage_profile(args):
+    """Per-kernel mean device times of a few steps: 3 graph-launched steps,
+    then `--profile-steps` launch by launch (a short fixed launch sequence for
+    ncu captures: 3 x launches-per-step launches precede the profiled ones).
+    --scheme seg instead runs `--profile-steps` graph-launched steps of the
+    reference's own segregated update (from the workload's fields, or from a
+    golden fixture's mesh and step-0 fields with --fixture) and prints their
+    wall time."""
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300.mesh import workload
+
+    if args.scheme == "seg":
+        if args.fixture:
+            sys.path.insert(0, os.path.join(ROOT, "tests"))
+            from conftest import load_golden
+
+            m = load_golden(args.fixture)
+            n = int(m["meta"][7])
+            rho, U, T = m["fld0_rho"], m["fld0_U"].reshape(n, 3), m["fld0_T"]
+        else:
+            m, u = workload(args.workload)
+            n = int(m["meta"][7])
+            rho = u[0]
+            U = np.stack([u[1] / rho, u[2] / rho, u[3] / rho], axis=1)
+            T = u[4] / rho - 300.0
+        s = ng.Solver(m, dt=args.dt)
+        s.set_fields(rho, U, T)
+        s.step(args.profile_steps, scheme=ng.REF_SEGREGATED)   # builds the graph
+        s.set_fields(rho, U, T)
+        s.sync()
+        t0 = time.perf_counter()
+        s.step(args.profile_steps, scheme=ng.REF_SEGREGATED)
+        s.sync()
+        wall = time.perf_counter() - t0
+        print(json.dumps({"scheme": "segregated", "nodes": n, "steps": args.profile_steps,
+                          "seconds": wall,
+                          "dof_steps_per_s": 5 * n * args.profile_steps / wall}))
+        s.close()
+        return
+    prec = ng.MIXED if args.prec != "fp64" else ng.FP64
+    m, u = workload(args.workload)
+    s = ng.Solver(m, dt=args.dt)
+    s.set_state(u)
+    s.step(3, prec=prec)
+    prof = s.profile(args.profile_steps, prec=prec)
+    print(json.dumps({k: v[0] / v[1] for k, v in prof.items()}))
+    s.close()
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -192,8 +313,8 @@ def run_reference(args):
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (rising thermal bubble initial state, deterministic)",
-        "config": {"workload": WORKLOAD, "elements": 32 ** 3, "order": 4, "dofs": dofs,
-                   "dt": DT, "scheme": "SSP-RK3"},
+        "config": config(dofs, world),
+        "form": "fp64",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{done} of {steps} SSP-RK3 steps of the full workload "
                                    f"({m.n_int} nodes), {sec:.1f} s"},
@@ -219,13 +340,15 @@ def run_ours(args):
     n = solver.n_int
     dofs = 5 * n
     prec_name = args.prec
+    fallback = None
     if prec_name == "auto":
         try:
             solver.set_state(u0)
             solver.tendency(prec=ng.MIXED)
             prec_name = "mixed"
-        except ng.NsemError:
+        except ng.NsemError as e:
             prec_name = "fp64"
+            fallback = f"precision form unavailable on this workload: {e}"
     prec = ng.MIXED if prec_name == "mixed" else ng.FP64
     stream = torch.cuda.ExternalStream(solver.stream)
 
@@ -285,9 +408,24 @@ def run_ours(args):
         solver.step(1, prec=prec, sync=False)
         solver.get_state_raw(rho, mom, rt)
     e2e_s = time.perf_counter() - t0
+    nbytes = int(rho.nbytes + mom.nbytes + rt.nbytes)
+    # the copy legs alone (state staged in and read back, no step)
+    reps = 5
+    solver.sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        solver.set_state_raw(rho, mom, rt)
+    solver.sync()
+    h2d_s = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        solver.get_state_raw(rho, mom, rt)
+    d2h_s = (time.perf_counter() - t0) / reps
     e2e = {"value": world * dofs * 3 * args.steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(rho.nbytes + mom.nbytes + rt.nbytes),
-           "d2h_bytes_per_step": int(rho.nbytes + mom.nbytes + rt.nbytes)}
+           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+           "ms_per_step": 1e3 * e2e_s / args.steps,
+           "set_state_ms": 1e3 * h2d_s, "get_state_ms": 1e3 * d2h_s,
+           "h2d_gbs": nbytes / h2d_s / 1e9, "d2h_gbs": nbytes / d2h_s / 1e9}
 
     # per-kernel device times (launch by launch, CUDA events on the same stream)
     solver.set_state(u0)
@@ -320,6 +458,12 @@ def run_ours(args):
         own = ng.mixed_own_bytes_per_node_stage()
         roof["own_layout_bytes_per_dof_stage"] = sum(own.values()) / 15.0
 
+    acc = adj = adj64 = None
+    if prec_name == "mixed" and not args.no_extra:
+        acc = accuracy(solver, u0, 200)
+        adj = adjoint_ratio(solver, mesh, u0, 200, 20, ng.MIXED)
+        adj64 = adjoint_ratio(solver, mesh, u0, 20, 5, ng.FP64)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(mesh, u0, args.cpu_seconds, DT)
@@ -331,16 +475,21 @@ def run_ours(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if prec_name == "mixed" else "f64",
             "data": "synthetic (rising thermal bubble initial state, deterministic)",
-            "config": {"workload": WORKLOAD, "elements": 32 ** 3, "order": 4, "dofs": dofs,
-                       "dt": DT, "scheme": "SSP-RK3", "form": prec_name,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (no flush needed)"},
+            "config": config(dofs, world), "form": prec_name,
             "e2e": e2e, "gpu_launches": int(round(launches_per_step * args.steps)),
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
         }
         if other:
             line["fp64_value"] = other["fp64_value"]
             line["mixed_over_fp64"] = value / other["fp64_value"]
+        if fallback:
+            line["form_fallback"] = fallback
+        if acc:
+            line["l2_vs_fp64"] = dict(acc["l2"], steps=acc["steps"])
+            line["mass_drift"] = dict(acc["mass_drift"], steps=acc["steps"])
+        if adj:
+            line["adjoint_over_forward"] = adj["ratio"]
+            line["adjoint"] = {"mixed": adj, "fp64": adj64}
         print(json.dumps(line), flush=True)
     solver.close()
     if world > 1:
@@ -359,8 +508,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--backend", default="nccl")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the accuracy and adjoint measurements")
+    ap.add_argument("--stage-profile", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--dt", type=float, default=DT)
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg"])
+    ap.add_argument("--fixture", default=None)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.stage_profile:
+        stage_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

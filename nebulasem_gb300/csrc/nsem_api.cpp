@@ -36,7 +36,10 @@ struct nsem_ctx {
     NsemConvBuf cbuf{};
     bool mixed_ready = false;
     /* where the state lives: 0 conserved in buf.u; 1 perturbation in
-     * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme) */
+     * mbuf.U[cur]; 2 primitive fields in sbuf (segregated scheme); 3 as the
+     * caller passed it to nsem_set_state: rho in buf.u[0], rho theta in
+     * buf.u[4], rho U (AoS) in scratch_aos -- converted on first use, straight
+     * into the form that steps it */
     int rep = 0;
     bool seg_pp_valid = false;   /* sbuf.pp holds the p' of the last segregated step */
     int adj_form = -1;           /* form of the last checkpointed forward run (-1: none) */
@@ -404,6 +407,21 @@ nsem_status seg_alloc(nsem_ctx* ctx) {
 nsem_status ensure_rep(nsem_ctx* ctx, int want) {
     if (ctx->rep == want) return NSEM_OK;
     int e = 0;
+    if (ctx->rep == 3) {
+        if (want == 1 && ctx->mixed_ready) {
+            /* one pass from the caller's layout to the precision form */
+            if ((e = nsem_mixed_host_layout(&ctx->dev, &ctx->mbuf, 1, ctx->buf.u[0],
+                                            ctx->scratch_aos, ctx->buf.u[4], ctx->stream)))
+                return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+            ctx->rep = 1;
+            return NSEM_OK;
+        }
+        if ((e = nsem_aos_to_soa(ctx->scratch_aos, ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3],
+                                 ctx->dev.n_int, ctx->stream)))
+            return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
+        ctx->rep = 0;
+        if (want == 0) return NSEM_OK;
+    }
     if (ctx->rep == 2) {
         /* primitive fields -> conserved state */
         if ((e = nsem_seg_to_cons(&ctx->dev, &ctx->sbuf, ctx->buf.u, ctx->stream)))
@@ -556,10 +574,8 @@ nsem_status nsem_set_state(nsem_ctx* ctx, const double* rho, const double* rhoU,
     NSEM_CUDA(cudaMemcpyAsync(ctx->buf.u[0], rho, n * 8, cudaMemcpyHostToDevice, ctx->stream));
     NSEM_CUDA(cudaMemcpyAsync(ctx->buf.u[4], rhoTheta, n * 8, cudaMemcpyHostToDevice, ctx->stream));
     NSEM_CUDA(cudaMemcpyAsync(ctx->scratch_aos, rhoU, 3 * n * 8, cudaMemcpyHostToDevice, ctx->stream));
-    int e = nsem_aos_to_soa(ctx->scratch_aos, ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3],
-                            ctx->dev.n_int, ctx->stream);
-    if (e) return cuda_fail(ctx, (cudaError_t)e, "aos_to_soa");
-    ctx->rep = 0;
+    /* converted when first used, into the form that uses it */
+    ctx->rep = 3;
     return NSEM_OK;
 }
 
@@ -568,6 +584,17 @@ nsem_status nsem_get_state(nsem_ctx* ctx, double* rho, double* rhoU, double* rho
     if (!rho || !rhoU || !rhoTheta) return fail(ctx, NSEM_BAD_ARG, "state pointer is NULL");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     const size_t n = (size_t)ctx->dev.n_int;
+    if (ctx->rep == 1) {
+        /* precision form: one pass into the caller's layout; the state stays
+         * where it is (a following precision-form step needs no conversion) */
+        int e = nsem_mixed_host_layout(&ctx->dev, &ctx->mbuf, 0, ctx->buf.u[0], ctx->scratch_aos,
+                                       ctx->buf.u[4], ctx->stream);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "state conversion");
+        NSEM_CUDA(cudaMemcpyAsync(rho, ctx->buf.u[0], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        NSEM_CUDA(cudaMemcpyAsync(rhoTheta, ctx->buf.u[4], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        NSEM_CUDA(cudaMemcpyAsync(rhoU, ctx->scratch_aos, 3 * n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        return check_status(ctx);
+    }
     nsem_status rs = materialise_conserved(ctx);
     if (rs != NSEM_OK) return rs;
     int e = nsem_soa_to_aos(ctx->buf.u[1], ctx->buf.u[2], ctx->buf.u[3], ctx->scratch_aos,
@@ -1166,6 +1193,8 @@ extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const
     NsemConvBuf& C = ctx->cbuf;
     const size_t n = (size_t)ctx->dev.n_int, ns = (size_t)ctx->dev.n_slot;
     nsem_status s;
+    /* the staging buffer below may still hold the Euler state as passed */
+    if (ctx->rep == 3 && (s = ensure_rep(ctx, 0)) != NSEM_OK) return s;
     if (!C.ready) {
         double** arrays[] = {&C.T[0], &C.T[1], &C.U[0], &C.U[1], &C.U[2]};
         for (double** a : arrays)

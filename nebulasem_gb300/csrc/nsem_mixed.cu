@@ -47,7 +47,9 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <map>
+#include <string>
 #include <vector>
 
 #include "nsem_mixed.h"
@@ -97,8 +99,45 @@ struct StageSmem {
     static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
 };
 
+/* Tensor-core line sums (order 7, 8 nodes per direction).  The volume term
+ * of direction d is, per conserved variable v and line l through the
+ * element, r_l = Q_d f_l: as a matrix product R^T = F^T Q_d^T with the rows
+ * (v, l) of F^T as M (5 x 64 = 320 rows: 20 tiles of 16), the 8 nodes along
+ * the line as K and the 8 output nodes as N, one mma.sync m16n8k8 per tile
+ * and TF32 pass.  FP32 accuracy from three TF32 products (a_lo b_hi +
+ * a_hi b_lo + a_hi b_hi, Markidis' split; FP32 accumulation).  The fluxes
+ * are kept per direction as F_d[v][a][m][b]: m the node index along d, (a, b)
+ * the other two with b fastest (x: (j, k), y: (i, k), z: (i, j)), so each
+ * fragment load and the in-place result store touch 32 distinct banks or
+ * at most two ways. */
+template <int D>
+__device__ __forceinline__ int tc_idx(int i, int j, int k) {
+    return D == 0 ? j * 64 + i * 8 + k : D == 1 ? i * 64 + j * 8 + k : i * 64 + k * 8 + j;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
 /* registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the stage
  * that also carries the FP64 state (measured best on GB300), 6 when viscous */
+#ifndef NSEM_MIXED_MB12
+#define NSEM_MIXED_MB12 8
+#endif
+#ifndef NSEM_MIXED_MB3
+#define NSEM_MIXED_MB3 7
+#endif
 template <int NX, int NY, int NZ, int STAGE, bool VISC>
 constexpr int stage_min_blocks() {
     /* order 7 (512 threads, 64 KB of shared memory): three CTAs, two for the
@@ -106,12 +145,13 @@ constexpr int stage_min_blocks() {
     if (Geo<NX, NY, NZ>::BLOCK >= 512)
         return min_blocks((VISC || STAGE == 3 || STAGE == 0) ? 2 : 3, Geo<NX, NY, NZ>::BLOCK,
                           StageSmem<NX, NY, NZ>::BYTES);
-    return min_blocks(VISC ? 6 : (STAGE == 1 || STAGE == 2) ? 8 : 7, Geo<NX, NY, NZ>::BLOCK,
+    return min_blocks(VISC ? 6 : (STAGE == 1 || STAGE == 2) ? NSEM_MIXED_MB12 : NSEM_MIXED_MB3,
+                      Geo<NX, NY, NZ>::BLOCK,
                       StageSmem<NX, NY, NZ>::BYTES);
 }
 
 /* phase 2: flux through face node t of direction DIR, seen from the element */
-template <int NX, int NY, int NZ, int DIR, bool VISC>
+template <int NX, int NY, int NZ, int DIR, bool VISC, bool TC>
 __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const float* oth,
                                           const float* bgo, const float* gfo, const float4* sF4,
                                           const float* sF1, const float4* sP, const StageArgs& a,
@@ -122,8 +162,17 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
     const float md_s = DIR == 0 ? P0.y : DIR == 1 ? P0.z : P0.w;
     const float um_s = P1.z, c_s = P1.w;
     if (nb >= 0) {
-        const float4 A4 = sF4[DIR * NP + fs.la];
-        const float A1 = sF1[DIR * NP + fs.la];
+        float4 A4;
+        float A1;
+        if constexpr (TC) {
+            const float* f = reinterpret_cast<const float*>(sF4) + DIR * 5 * NP +
+                             tc_idx<DIR>(fs.la >> 6, (fs.la >> 3) & 7, fs.la & 7);
+            A4 = make_float4(f[0], f[NP], f[2 * NP], f[3 * NP]);
+            A1 = f[4 * NP];
+        } else {
+            A4 = sF4[DIR * NP + fs.la];
+            A1 = sF1[DIR * NP + fs.la];
+        }
         const Pt q = pointwise(oth, bgo, a.eos, a.gamma, a.gR);
         float g12[12] = {};
         if constexpr (VISC) {
@@ -170,9 +219,10 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
 }
 
 /* one kernel per stage (0: tendency only): the stage's own loads and update */
-template <int NX, int NY, int NZ, int STAGE, bool VISC>
+template <int NX, int NY, int NZ, int STAGE, bool VISC, bool TC>
 __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (stage_min_blocks<NX, NY, NZ, STAGE, VISC>()))
 k_mixed_stage(StageArgs a) {
+    static_assert(!TC || (NX == 8 && NY == 8 && NZ == 8), "tensor-core line sums: order 7");
     using G = Geo<NX, NY, NZ>;
     using SM = StageSmem<NX, NY, NZ>;
     constexpr int NP = G::NP;
@@ -263,14 +313,28 @@ k_mixed_stage(StageArgs a) {
         sP[2 * NP + t] = make_float4(p.u[0], p.u[1], p.u[2], p.pp);
         float4 f4;
         float f1;
-        vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-        sF4[t] = f4; sF1[t] = f1;
-        if constexpr (G::HAS_Y) {
+        if constexpr (TC) {
+            const int i = t >> 6, j = (t >> 3) & 7, k = t & 7;
+            auto put = [&](int d, int idx) {
+                float* f = smem + d * 5 * NP + idx;
+                f[0] = f4.x; f[NP] = f4.y; f[2 * NP] = f4.z; f[3 * NP] = f4.w; f[4 * NP] = f1;
+            };
+            vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
+            put(0, tc_idx<0>(i, j, k));
             vol_flux<1, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            sF4[NP + t] = f4; sF1[NP + t] = f1;
+            put(1, tc_idx<1>(i, j, k));
+            vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
+            put(2, tc_idx<2>(i, j, k));
+        } else {
+            vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
+            sF4[t] = f4; sF1[t] = f1;
+            if constexpr (G::HAS_Y) {
+                vol_flux<1, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
+                sF4[NP + t] = f4; sF1[NP + t] = f1;
+            }
+            vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
+            sF4[2 * NP + t] = f4; sF1[2 * NP + t] = f1;
         }
-        vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-        sF4[2 * NP + t] = f4; sF1[2 * NP + t] = f1;
     }
     __syncthreads();
 
@@ -279,20 +343,56 @@ k_mixed_stage(StageArgs a) {
         float4 o4;
         float o1;
         if (fs.dir == 0)
-            face_flux<NX, NY, NZ, 0, VISC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 0, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
         else if (G::HAS_Y && fs.dir == 1)
-            face_flux<NX, NY, NZ, 1, VISC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 1, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
         else
-            face_flux<NX, NY, NZ, 2, VISC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 2, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
         sFF4[t] = o4;
         sFF1[t] = o1;
     }
     __syncthreads();
 
     /* phase 3: weak volume term (line sums with Q), lift, buoyancy, update */
+    if constexpr (TC) {
+        /* tensor-core line sums, results in place of the fluxes */
+        const int lane = t & 31, w = t >> 5, gq = lane >> 2, tg = lane & 3;
+        for (int q = w; q < 60; q += G::BLOCK / 32) {
+            const int d = q / 20, r = q % 20, v = r >> 2, a0 = (r & 3) * 2;
+            float* base = smem + d * 5 * NP + v * NP + a0 * 64;
+            uint32_t ah[4], al[4], bh0, bl0, bh1, bl1;
+            split_tf32(base[tg * 8 + gq], ah[0], al[0]);
+            split_tf32(base[64 + tg * 8 + gq], ah[1], al[1]);
+            split_tf32(base[(tg + 4) * 8 + gq], ah[2], al[2]);
+            split_tf32(base[64 + (tg + 4) * 8 + gq], ah[3], al[3]);
+            const float* qd = sQ + d * MAXN * QS + gq * QS;
+            split_tf32(qd[tg], bh0, bl0);
+            split_tf32(qd[tg + 4], bh1, bl1);
+            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            mma_tf32(c, al, bh0, bh1);
+            mma_tf32(c, ah, bl0, bl1);
+            mma_tf32(c, ah, bh0, bh1);
+            base[(2 * tg) * 8 + gq] = c[0];
+            base[(2 * tg + 1) * 8 + gq] = c[1];
+            base[64 + (2 * tg) * 8 + gq] = c[2];
+            base[64 + (2 * tg + 1) * 8 + gq] = c[3];
+        }
+        __syncthreads();
+    }
     if (t >= NP) return;
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
     float L0, L1, L2, L3, L4;
+    if constexpr (TC) {
+        const float Jx = sMeta[0], Jy = sMeta[1], Jz = sMeta[2];
+        const float* rx = smem + tc_idx<0>(i, j, k);
+        const float* ry = smem + 5 * NP + tc_idx<1>(i, j, k);
+        const float* rz = smem + 10 * NP + tc_idx<2>(i, j, k);
+        float Lt[5];
+#pragma unroll
+        for (int v = 0; v < 5; v++)
+            Lt[v] = fmaf(Jz, rz[v * NP], fmaf(Jy, ry[v * NP], Jx * rx[v * NP]));
+        L0 = Lt[0]; L1 = Lt[1]; L2 = Lt[2]; L3 = Lt[3]; L4 = Lt[4];
+    } else {
     {
         float4 acc = make_float4(0, 0, 0, 0);
         float acc1 = 0.0f;
@@ -339,6 +439,7 @@ k_mixed_stage(StageArgs a) {
         const float Jz = sMeta[2];
         L0 = fmaf(Jz, acc.x, L0); L1 = fmaf(Jz, acc.y, L1); L2 = fmaf(Jz, acc.z, L2);
         L3 = fmaf(Jz, acc.w, L3); L4 = fmaf(Jz, acc1, L4);
+    }
     }
     /* surface lift: -(J_d / w_end) F_out for the face of each axis through
      * the node (at most one per axis) */
@@ -604,25 +705,80 @@ __global__ void k_from_pert(const double* U, Ptr5 full, const double* rho_ref, d
     }
 }
 
-template <int NX, int NY, int NZ, bool VISC>
+/* the host boundary's layout (rho, rho U as AoS xyz, rho theta; node order)
+ * <-> perturbation state, in one pass each way (no conserved SoA copy) */
+template <int NP>
+__global__ void k_host_to_pert(const double* rho, const double* mom, const double* rt, double* U,
+                               float* S, const double* rho_ref, double T0, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP;
+        const int64_t o = e * 5 * NP + (i - e * NP);
+        const double rr = rho_ref[i];
+        const double tr = __dmul_rn(rr, T0);
+        const double v[5] = {__dsub_rn(rho[i], rr), mom[3 * i], mom[3 * i + 1], mom[3 * i + 2],
+                             __dsub_rn(rt[i], tr)};
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            U[o + c * NP] = v[c];
+            S[o + c * NP] = d2f_rn(v[c]);
+        }
+    }
+}
+
+template <int NP>
+__global__ void k_pert_to_host(const double* U, double* rho, double* mom, double* rt,
+                               const double* rho_ref, double T0, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / NP;
+        const int64_t o = e * 5 * NP + (i - e * NP);
+        const double rr = rho_ref[i];
+        const double tr = __dmul_rn(rr, T0);
+        rho[i] = __dadd_rn(U[o], rr);
+        mom[3 * i] = U[o + NP];
+        mom[3 * i + 1] = U[o + 2 * NP];
+        mom[3 * i + 2] = U[o + 3 * NP];
+        rt[i] = __dadd_rn(U[o + 4 * NP], tr);
+    }
+}
+
+template <int NX, int NY, int NZ, bool VISC, bool TC>
 void launch_stage_v(const StageArgs& a, int stage, cudaStream_t st) {
     using G = Geo<NX, NY, NZ>;
     constexpr size_t SMEM = StageSmem<NX, NY, NZ>::BYTES;
     const unsigned grid = (unsigned)a.n_elem;
     switch (stage) {
-        case 0: k_mixed_stage<NX, NY, NZ, 0, VISC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 1: k_mixed_stage<NX, NY, NZ, 1, VISC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 2: k_mixed_stage<NX, NY, NZ, 2, VISC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        default: k_mixed_stage<NX, NY, NZ, 3, VISC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 0: k_mixed_stage<NX, NY, NZ, 0, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 1: k_mixed_stage<NX, NY, NZ, 1, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 2: k_mixed_stage<NX, NY, NZ, 2, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        default: k_mixed_stage<NX, NY, NZ, 3, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
     }
+}
+
+/* the tensor-core line sums exist for order 7 only */
+template <int NX, int NY, int NZ>
+constexpr bool tc_dims() {
+    return NX == 8 && NY == 8 && NZ == 8;
+}
+
+template <int NX, int NY, int NZ, bool VISC>
+void launch_stage_tc(const StageArgs& a, int stage, cudaStream_t st, bool tc) {
+    if constexpr (tc_dims<NX, NY, NZ>()) {
+        if (tc) {
+            launch_stage_v<NX, NY, NZ, VISC, true>(a, stage, st);
+            return;
+        }
+    }
+    launch_stage_v<NX, NY, NZ, VISC, false>(a, stage, st);
 }
 
 /* one stage; viscous runs first form the gradients of the stage state */
 template <int NX, int NY, int NZ>
-int launch_stage(const StageArgs& a, int stage, cudaStream_t st, bool visc) {
+int launch_stage(const StageArgs& a, int stage, cudaStream_t st, bool visc, bool tc) {
     using G = Geo<NX, NY, NZ>;
     if (!visc) {
-        launch_stage_v<NX, NY, NZ, false>(a, stage, st);
+        launch_stage_tc<NX, NY, NZ, false>(a, stage, st, tc);
         return (int)cudaGetLastError();
     }
     const unsigned grid = (unsigned)a.n_elem;
@@ -631,7 +787,7 @@ int launch_stage(const StageArgs& a, int stage, cudaStream_t st, bool visc) {
     else k_mixed_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a);
     int e = (int)cudaGetLastError();
     if (e) return e;
-    launch_stage_v<NX, NY, NZ, true>(a, stage, st);
+    launch_stage_tc<NX, NY, NZ, true>(a, stage, st, tc);
     return (int)cudaGetLastError();
 }
 
@@ -641,14 +797,24 @@ int prepare_stage() {
     constexpr int SMEM = (int)StageSmem<NX, NY, NZ>::BYTES;
     int e = 0;
     if (SMEM > 48 * 1024) {
-        e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true>, at, SMEM);
+        e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true, false>, at, SMEM);
+        if constexpr (tc_dims<NX, NY, NZ>()) {
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true, true>, at, SMEM);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true, true>, at, SMEM);
+        }
     }
     constexpr size_t gs = grad_smem<NX, NY, NZ>();
     if (!e && gs > 48 * 1024) {
@@ -681,9 +847,9 @@ int prepare(int nx, int ny, int nz) {
 }
 
 int dispatch_stage(int nx, int ny, int nz, const StageArgs& a, int stage, cudaStream_t st,
-                   bool visc) {
+                   bool visc, bool tc) {
 #define NSEM_DISP(A, B, C) \
-    if (nx == A && ny == B && nz == C) return launch_stage<A, B, C>(a, stage, st, visc);
+    if (nx == A && ny == B && nz == C) return launch_stage<A, B, C>(a, stage, st, visc, tc);
     NSEM_MIXED_DIMS(NSEM_DISP)
 #undef NSEM_DISP
     return (int)cudaErrorNotSupported;
@@ -885,6 +1051,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         err = "precision form: cannot reserve the kernel's shared memory";
         return NSEM_CUDA_ERROR;
     }
+    /* line sums of order 7 on the tensor cores unless NSEM_MIXED_LINES=fp32 */
+    {
+        const char* lines = std::getenv("NSEM_MIXED_LINES");
+        mb->tc = NX == 8 && NY == 8 && NZ == 8 && !(lines && std::string(lines) == "fp32");
+    }
     mb->n_elem = ne;
     mb->n_int = n_int;
     mb->npd[0] = NX; mb->npd[1] = NY; mb->npd[2] = NZ;
@@ -929,7 +1100,7 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
 }
 
 int launch_args(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
-    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, mb->visc);
+    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, mb->visc, mb->tc);
 }
 
 }  // namespace
@@ -980,6 +1151,28 @@ int nsem_mixed_convert(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int to_
     }
     NSEM_MIXED_DIMS(NSEM_CONV)
 #undef NSEM_CONV
+    return (int)cudaErrorNotSupported;
+}
+
+int nsem_mixed_host_layout(const NsemDev* dev, NsemMixedBuf* mb, int to_pert, double* rho,
+                           double* mom, double* rt, void* stream) {
+    const int NP = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    cudaStream_t st = (cudaStream_t)stream;
+    const int grid = grid_for(dev->n_int);
+    double* U = mb->U[mb->cur];
+    float* S = mb->S[mb->cur];
+#define NSEM_HOSTL(A, B, C)                                                                    \
+    if (NP == A * B * C) {                                                                     \
+        if (to_pert)                                                                           \
+            k_host_to_pert<A * B * C><<<grid, 256, 0, st>>>(rho, mom, rt, U, S, dev->rho_ref,  \
+                                                            dev->T0, dev->n_int);              \
+        else                                                                                   \
+            k_pert_to_host<A * B * C><<<grid, 256, 0, st>>>(U, rho, mom, rt, dev->rho_ref,     \
+                                                            dev->T0, dev->n_int);              \
+        return (int)cudaGetLastError();                                                        \
+    }
+    NSEM_MIXED_DIMS(NSEM_HOSTL)
+#undef NSEM_HOSTL
     return (int)cudaErrorNotSupported;
 }
 

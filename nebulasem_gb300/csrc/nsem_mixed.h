@@ -33,6 +33,7 @@ struct NsemMixedBuf {
     float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a), same layout */
     float* G = nullptr;           /* viscous runs: [n_elem][12][NP] gradients of the stage state */
     bool visc = false;            /* artificial viscosity (diffusion YES)   */
+    bool tc = false;              /* order-7 line sums on the tensor cores  */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */
@@ -49,6 +50,11 @@ struct NsemMixedBuf {
 /* u' <-> u conversion of the current state (to_pert: buf.u -> U[cur]) */
 int nsem_mixed_convert(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int to_pert,
                        void* stream);
+
+/* the host boundary's layout (rho, rho U AoS, rho theta in node order) <->
+ * the current perturbation state U[cur] (to_pert: host layout -> U, S) */
+int nsem_mixed_host_layout(const NsemDev* dev, NsemMixedBuf* mb, int to_pert, double* rho,
+                           double* mom, double* rt, void* stream);
 
 nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMixedBuf* mb,
                              std::vector<void*>* allocs, std::string& err);

@@ -1107,8 +1107,8 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho_in, double* U
  * lambda = cds(|U|)/2 (convection.cpp:106-108); per step the flux Fc T with the
  * Rusanov state T, T^{n+1} = Su/ap with ap = (-1/dt) cV and Su += T^n ap
  * (addTemporal<1> without density), Neumann ghosts of T. */
-void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, double* T_in, double dt,
-                            int nsteps) {
+static void convection_core(const nsem_oracle_mesh* m, const double* U_in, const double* U_all,
+                            const double* scale, int order, double* T_in, double dt, int nsteps) {
     const int64_t n_int = m->n_int, n_all = m->n_all;
     const int64_t n_slot = (int64_t)m->n_face * m->npf;
     const size_t na = (size_t)n_all + (size_t)m->np;
@@ -1118,9 +1118,17 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
     double* lam = calloc((size_t)n_slot, sizeof(double));
     double* d = calloc((size_t)n_slot, sizeof(double));
     double* r = calloc(na, sizeof(double));
-    memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
+    double* r0 = order == 2 ? calloc(na, sizeof(double)) : NULL;  /* previous rhs (AB2) */
+    if (U_all) {
+        /* the app's analytic wind: every cell node, ghosts included, from
+         * the node coordinates (convection.cpp:64-93 loops over the whole
+         * cell field) */
+        memcpy(U, U_all, 3 * (size_t)n_all * sizeof(double));
+    } else {
+        memcpy(U, U_in, 3 * (size_t)n_int * sizeof(double));
+        ghosts_velocity(m, U);
+    }
     memcpy(T, T_in, (size_t)n_int * sizeof(double));
-    ghosts_velocity(m, U);
     ghosts_scalar(m, T);
     /* non-conforming faces: coarse side interpolated, fluxes projected back */
     const int mort = m->n_mortar > 0;
@@ -1130,22 +1138,31 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
     double* mF = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
     double* mP = mort ? calloc(3 * (size_t)n_slot, sizeof(double)) : NULL;
     double* dC = mort ? calloc((size_t)n_slot, sizeof(double)) : NULL;
-    if (mort) {
-        for (int64_t i = 0; i < n_int; i++) nq[i] = vmag(U + 3 * i);
-        mortar_scatter(m, 1, nq, ms);
-    }
-#pragma omp parallel for schedule(static)
-    for (int64_t k = 0; k < n_slot; k++) {
-        uint32_t c1 = m->FO[k], c2 = m->FN[k];
-        if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
-        const double fi = m->fI[k], fo = 1 - fi;
-        double u1 = vmag(U + 3 * (size_t)c1), u2 = vmag(U + 3 * (size_t)c2);
-        if (mort && side[k] == 1) u1 = ms[k];
-        if (mort && side[k] == 2) u2 = ms[k];
-        lam[k] = (u1 * fi + u2 * fo) / 2;
-    }
     const double c_dt = -1.0 / dt;
     for (int step = 0; step < nsteps; step++) {
+        if (U_all || step == 0) {
+            /* the wind of this step (U = U(x) cos(pi t / T) for the app's
+             * analytic winds: the product with the step's factor, in the
+             * app's operation order) and its Rusanov speed cds(|U|)/2 */
+            if (U_all && scale) {
+#pragma omp parallel for schedule(static)
+                for (int64_t i = 0; i < 3 * n_all; i++) U[i] = U_all[i] * scale[step];
+            }
+            if (mort) {
+                for (int64_t i = 0; i < n_int; i++) nq[i] = vmag(U + 3 * i);
+                mortar_scatter(m, 1, nq, ms);
+            }
+#pragma omp parallel for schedule(static)
+            for (int64_t k = 0; k < n_slot; k++) {
+                uint32_t c1 = m->FO[k], c2 = m->FN[k];
+                if (c1 >= (uint32_t)n_all || c2 >= (uint32_t)n_all) continue;
+                const double fi = m->fI[k], fo = 1 - fi;
+                double u1 = vmag(U + 3 * (size_t)c1), u2 = vmag(U + 3 * (size_t)c2);
+                if (mort && side[k] == 1) u1 = ms[k];
+                if (mort && side[k] == 2) u2 = ms[k];
+                lam[k] = (u1 * fi + u2 * fo) / 2;
+            }
+        }
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n_all; i++)
             for (int c = 0; c < 3; c++) Fv[3 * i + c] = U[3 * i + c] * T[i];
@@ -1182,14 +1199,42 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
                 if (side[k]) dC[k] = vdot(mP + 3 * k, m->fN + 3 * k);
         }
         seg_divf(m, 1, Fv, d, side, dC, r);
+        if (order == 2 && step > 0) {
+            /* AB2 (field.h:3796-3798): Su = T ap + (3 R^n - R^{n-1}) / 2, T = Su / ap */
 #pragma omp parallel for schedule(static)
-        for (int64_t i = 0; i < n_int; i++) {
-            const double ap = c_dt * m->cV[i];
-            T[i] = (r[i] + T[i] * ap) / (0.0 + ap);
+            for (int64_t i = 0; i < n_int; i++) {
+                const double ap = c_dt * m->cV[i];
+                const double rn = r[i];
+                T[i] = (T[i] * ap + (3.0 * rn - r0[i]) / 2.0) / ap;
+                r0[i] = rn;
+            }
+        } else {
+            /* BDF1 / AB1 (the first AB2 step): T = (R + T ap) / ap */
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n_int; i++) {
+                const double ap = c_dt * m->cV[i];
+                if (r0) r0[i] = r[i];
+                T[i] = (r[i] + T[i] * ap) / (0.0 + ap);
+            }
         }
         ghosts_scalar(m, T);
     }
     memcpy(T_in, T, (size_t)n_int * sizeof(double));
     free(U); free(T); free(Fv); free(lam); free(d); free(r);
-    free(side); free(nq); free(ms); free(mF); free(mP); free(dC);
+    free(side); free(nq); free(ms); free(mF); free(mP); free(dC); free(r0);
+}
+
+void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, double* T_in, double dt,
+                            int nsteps) {
+    convection_core(m, U_in, NULL, NULL, 1, T_in, dt, nsteps);
+}
+
+/* The convection app with an analytic wind (problem_init LEVEQUE,
+ * convection.cpp:45-93, 103-123): U_all [n_all*3] is the wind's spatial part
+ * on every node (ghosts included) and scale[step] its time factor
+ * cos(pi t / T), multiplied in the app's order; order 1 = BDF1/AB1,
+ * 2 = AB2 (the first step AB1). */
+void nsem_oracle_convection_wind(const nsem_oracle_mesh* m, const double* U_all, const double* scale,
+                                 int order, double* T_in, double dt, int nsteps) {
+    convection_core(m, NULL, U_all, scale, order, T_in, dt, nsteps);
 }

@@ -108,6 +108,8 @@ void nsem_oracle_segregated(const nsem_oracle_mesh* m, double* rho, double* U, d
  * (AoS) for nsteps steps, in place. */
 void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U, double* T, double dt,
                             int nsteps);
+void nsem_oracle_convection_wind(const nsem_oracle_mesh* m, const double* U_all, const double* scale,
+                                 int order, double* T, double dt, int nsteps);
 
 int nsem_oracle_threads(void);
 

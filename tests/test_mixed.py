@@ -94,3 +94,30 @@ def test_mixed_mass_conservation_and_state_switching():
     assert abs(m1[0] - m0[0]) / m0[0] < 1e-10, (m0, m1)
     assert abs(m1[2] - m0[2]) == 0.0
     s.close()
+
+
+def test_mixed_order7_line_sum_paths(monkeypatch):
+    """Order 7: line sums on the tensor cores (three TF32 products per term,
+    the default) and on the FP32 pipes (NSEM_MIXED_LINES=fp32) both stay within
+    1e-5 of the FP64 form and agree with each other to FP32 rounding."""
+    import nebulasem_gb300 as ng
+    g = load_golden("g3_2n7")
+    u = golden_state(g, "up")
+    got = {}
+    for lines in ("fp32", "tensor"):
+        monkeypatch.setenv("NSEM_MIXED_LINES", lines)
+        s = make(g)
+        s.set_state(u)
+        L64 = s.tendency(prec=ng.FP64)
+        got[lines] = s.tendency(prec=ng.MIXED)
+        s.step(5, prec=ng.MIXED)
+        got[lines + "_traj"] = s.get_state()
+        s.close()
+        for a, b, v in zip(got[lines], L64, VARS):
+            if np.linalg.norm(b) < 1e-8 * max(np.linalg.norm(x) for x in L64):
+                continue
+            assert rel_l2(a, b) <= 1e-5, (lines, v, rel_l2(a, b))
+    for a, b, v in zip(got["tensor"], got["fp32"], VARS):
+        assert rel_l2(a, b) <= 1e-6, (v, rel_l2(a, b))
+    for a, b, v in zip(got["tensor_traj"], got["fp32_traj"], VARS):
+        assert rel_l2(a, b) <= 1e-6, (v, rel_l2(a, b))
