@@ -224,6 +224,23 @@ nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const double* T)
 nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps);
 nsem_status nsem_convection_get(nsem_ctx* ctx, double* T);
 
+/* The convection app's analytic winds and its AB2 scheme
+ * (apps/convection/convection.cpp:45-93, 103-123 with problem_init LEVEQUE;
+ * src/field/field.h:3787-3804, 3885-3906 with time_scheme AB2).  Call after
+ * nsem_convection_set, which resets both.
+ * nsem_convection_wind: U_all [n_all*3] AoS is the wind's spatial part on
+ * every node, ghost nodes included (the app fills the whole cell field from
+ * the node coordinates, e.g. (sin^2(pi x) sin(2 pi y), -sin^2(pi y) sin(2 pi x),
+ * 0) for LEVEQUE), or NULL to keep nsem_convection_set's wind and its wall
+ * ghosts; time_scheme 1 = BDF1/AB1, 2 = AB2 (the first step AB1, as the app's
+ * history starts with one stored right-hand side).
+ * nsem_convection_step_scaled: nsteps steps, the wind of step s being the
+ * spatial part times scale[s] in its first two components (the app's
+ * u, v times cos(pi t / T); w as given); scale NULL means 1.  The AB2
+ * history carries over from one call to the next. */
+nsem_status nsem_convection_wind(nsem_ctx* ctx, const double* U_all, int time_scheme);
+nsem_status nsem_convection_step_scaled(nsem_ctx* ctx, int nsteps, const double* scale);
+
 /* Measurement helper: run nsteps SSP-RK3 steps launch by launch (no graph)
  * with CUDA events on the context's stream around every kernel, and report
  * per kernel class the summed device time in ms, the launch count and the

@@ -97,6 +97,8 @@ def load(build_if_missing=True):
         "nsem_convection_set": ([P, P, P], ctypes.c_int),
         "nsem_convection_step": ([P, ctypes.c_int], ctypes.c_int),
         "nsem_convection_get": ([P, P], ctypes.c_int),
+        "nsem_convection_wind": ([P, P, ctypes.c_int], ctypes.c_int),
+        "nsem_convection_step_scaled": ([P, ctypes.c_int, P], ctypes.c_int),
         "nsem_tlm": ([P, ctypes.c_int, vp, vp, P], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
@@ -337,6 +339,19 @@ class Solver:
 
     def convection_step(self, nsteps):
         self._check(self._lib.nsem_convection_step(self._ctx, int(nsteps)))
+
+    def convection_wind(self, U_all=None, time_scheme=1):
+        """Analytic wind (spatial part on all n_all nodes, (n_all, 3)) and the
+        time scheme (1: BDF1/AB1, 2: AB2) of the convection app."""
+        u = None if U_all is None else _f64(np.asarray(U_all).reshape(-1))
+        self._check(self._lib.nsem_convection_wind(self._ctx, _p(u) if u is not None else None,
+                                                   int(time_scheme)))
+
+    def convection_step_scaled(self, nsteps, scale=None):
+        """nsteps steps with the wind's spatial part times scale[s]."""
+        sc = None if scale is None else _f64(scale)
+        self._check(self._lib.nsem_convection_step_scaled(
+            self._ctx, int(nsteps), _p(sc) if sc is not None else None))
 
     def convection_get(self):
         t = np.empty(self.n_int)

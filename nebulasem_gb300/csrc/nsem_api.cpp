@@ -46,6 +46,7 @@ struct nsem_ctx {
     double dt = 0, T0 = 0;
     int64_t n_all = 0;
     std::vector<void*> allocations;
+    std::vector<int64_t> slot_ghost;  /* per used slot: its ghost node (-1: interior face) */
     double* scratch_aos = nullptr;   /* [3*n_int] AoS staging for rhoU */
     double* red = nullptr;           /* reduction partials */
     double* h_red = nullptr;         /* pinned host copy of the reduction result */
@@ -178,6 +179,7 @@ nsem_status build_device_mesh(nsem_ctx* ctx, const nsem_mesh_desc* m, const nsem
         c1.push_back((int32_t)o);
         const bool ghost = n >= (uint64_t)n_int;
         c2.push_back(ghost ? -1 : (int32_t)n);
+        ctx->slot_ghost.push_back(ghost ? (int64_t)n : -1);
         if (ghost && m->bc_U[k] == 0)
             return fail(ctx, NSEM_BAD_ARG, "boundary slot without a boundary condition");
         if (m->bc_U[k] > 2) return fail(ctx, NSEM_UNSUPPORTED, "velocity BC other than NEUMANN/SYMMETRY");
@@ -1209,6 +1211,9 @@ extern "C" nsem_status nsem_convection_set(nsem_ctx* ctx, const double* U, const
         C.ready = true;
     }
     C.cur = 0;
+    C.analytic = false;
+    C.order = 1;
+    C.hist = 0;
     NSEM_CUDA(cudaMemcpyAsync(C.T[0], T, n * 8, cudaMemcpyHostToDevice, ctx->stream));
     NSEM_CUDA(cudaMemcpyAsync(ctx->scratch_aos, U, 3 * n * 8, cudaMemcpyHostToDevice, ctx->stream));
     int e = nsem_aos_to_soa(ctx->scratch_aos, C.U[0], C.U[1], C.U[2], (int64_t)n, ctx->stream);
@@ -1226,6 +1231,7 @@ extern "C" nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps) {
     NsemConvBuf& C = ctx->cbuf;
     if (!C.ready) return fail(ctx, NSEM_BAD_ARG, "nsem_convection_set was not called");
     if (nsteps == 0) return NSEM_OK;
+    if (C.analytic || C.order != 1) return nsem_convection_step_scaled(ctx, nsteps, nullptr);
     NSEM_CUDA(cudaSetDevice(ctx->device));
     auto key = std::make_pair(3 * 2 + C.cur, nsteps);
     auto it = ctx->graphs.find(key);
@@ -1247,6 +1253,55 @@ extern "C" nsem_status nsem_convection_step(nsem_ctx* ctx, int nsteps) {
     }
     NSEM_CUDA(cudaGraphLaunch(it->second, ctx->stream));
     C.cur ^= (nsteps & 1);
+    NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_convection_wind(nsem_ctx* ctx, const double* U_all, int time_scheme) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (time_scheme != 1 && time_scheme != 2)
+        return fail(ctx, NSEM_UNSUPPORTED, "convection time schemes: 1 (BDF1/AB1) or 2 (AB2)");
+    NsemConvBuf& C = ctx->cbuf;
+    if (!C.ready) return fail(ctx, NSEM_BAD_ARG, "nsem_convection_set was not called");
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const int64_t n = ctx->dev.n_int, ns = ctx->dev.n_slot;
+    nsem_status s;
+    if (time_scheme == 2 && !C.R[0]) {
+        if ((s = dalloc(ctx, &C.R[0], (size_t)n)) != NSEM_OK) return s;
+        if ((s = dalloc(ctx, &C.R[1], (size_t)n)) != NSEM_OK) return s;
+    }
+    C.order = time_scheme;
+    C.hist = 0;
+    if (!U_all) return NSEM_OK;
+    if (!C.A[0])
+        for (int c = 0; c < 3; c++) {
+            if ((s = dalloc(ctx, &C.A[c], (size_t)n)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &C.Ag[c], (size_t)ns)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &C.Ug[c], (size_t)ns)) != NSEM_OK) return s;
+        }
+    /* spatial part on interior nodes (SoA) and at each used slot's ghost */
+    std::vector<double> a((size_t)n), g((size_t)ns, 0.0);
+    for (int c = 0; c < 3; c++) {
+        for (int64_t i = 0; i < n; i++) a[i] = U_all[3 * i + c];
+        for (int64_t k = 0; k < ns; k++)
+            g[k] = ctx->slot_ghost[k] >= 0 ? U_all[3 * ctx->slot_ghost[k] + c] : 0.0;
+        NSEM_CUDA(cudaMemcpy(C.A[c], a.data(), (size_t)n * 8, cudaMemcpyHostToDevice));
+        NSEM_CUDA(cudaMemcpy(C.Ag[c], g.data(), (size_t)ns * 8, cudaMemcpyHostToDevice));
+    }
+    C.analytic = true;
+    return NSEM_OK;
+}
+
+extern "C" nsem_status nsem_convection_step_scaled(nsem_ctx* ctx, int nsteps, const double* scale) {
+    if (!ctx) return NSEM_BAD_ARG;
+    if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
+    NsemConvBuf& C = ctx->cbuf;
+    if (!C.ready) return fail(ctx, NSEM_BAD_ARG, "nsem_convection_set was not called");
+    if (nsteps == 0) return NSEM_OK;
+    NSEM_CUDA(cudaSetDevice(ctx->device));
+    const int e = nsem_conv_steps_wind(&ctx->dev, &ctx->tab, &C, nsteps, ctx->dt, scale, ctx->stream);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "convection step");
     NSEM_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->dev.status, sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, ctx->stream));
     return NSEM_OK;

@@ -1051,10 +1051,12 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         err = "precision form: cannot reserve the kernel's shared memory";
         return NSEM_CUDA_ERROR;
     }
-    /* line sums of order 7 on the tensor cores unless NSEM_MIXED_LINES=fp32 */
+    /* order 7: line sums on the FP32 pipes (measured faster than the
+     * tensor-core variant on GB300); NSEM_MIXED_LINES=tensor selects the
+     * tensor-core line sums */
     {
         const char* lines = std::getenv("NSEM_MIXED_LINES");
-        mb->tc = NX == 8 && NY == 8 && NZ == 8 && !(lines && std::string(lines) == "fp32");
+        mb->tc = NX == 8 && NY == 8 && NZ == 8 && lines && std::string(lines) == "tensor";
     }
     mb->n_elem = ne;
     mb->n_int = n_int;

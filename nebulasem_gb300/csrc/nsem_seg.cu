@@ -722,13 +722,28 @@ struct AdvArgs {
     const double* T_o;
     double* T_n;
     const double* U[3];
+    const double* Ug[3];   /* analytic wind at each slot's ghost (or null: bc_U) */
     double* lam;
     double* d;
     double* mq[4];
     double* mf[3];
     double* dC;
+    double* R_n;           /* AB2: this step's right-hand side (or null)        */
+    const double* R_o;     /* AB2: the previous step's                          */
+    int ab2;               /* AB2 update (field.h:3796-3798)                    */
     double c_dt;
 };
+
+/* the step's analytic wind: U = A s for the horizontal components (the app
+ * forms u, v as the spatial part times cos(pi t / T) and sets w = 0,
+ * convection.cpp:86-91), on interior nodes and at each used slot's ghost */
+__global__ void k_conv_wind(const NsemDev m, NsemConvBuf b, double s) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.n_int)
+        for (int c = 0; c < 3; c++) b.U[c][i] = c < 2 ? b.A[c][i] * s : b.A[c][i];
+    if (i < m.n_slot)
+        for (int c = 0; c < 3; c++) b.Ug[c][i] = c < 2 ? b.Ag[c][i] * s : b.Ag[c][i];
+}
 
 /* non-conforming faces: the coarse side's |U| (stage 0) or U T, T (stage 1)
  * interpolated onto each mortar slot, one thread per (slot, quantity) */
@@ -771,6 +786,8 @@ __global__ void __launch_bounds__(256) k_conv_lambda(const NsemDev m, AdvArgs a)
     double U2[3];
     if (c2 >= 0) {
         U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
+    } else if (a.Ug[0]) {
+        U2[0] = a.Ug[0][k]; U2[1] = a.Ug[1][k]; U2[2] = a.Ug[2][k];
     } else {
         ghost_U(m, k, n, U1, U2);
     }
@@ -797,7 +814,11 @@ __global__ void __launch_bounds__(256) k_conv_face(const NsemDev m, AdvArgs a) {
         U2[0] = a.U[0][c2]; U2[1] = a.U[1][c2]; U2[2] = a.U[2][c2];
         T2 = a.T_o[c2];
     } else {
-        ghost_U(m, k, n, U1, U2);
+        if (a.Ug[0]) {
+            U2[0] = a.Ug[0][k]; U2[1] = a.Ug[1][k]; U2[2] = a.Ug[2][k];
+        } else {
+            ghost_U(m, k, n, U1, U2);
+        }
         T2 = T1 + 0.0;
     }
     double X1[3], X2[3];
@@ -857,7 +878,15 @@ __global__ void k_conv_vol(const NsemDev m, const NsemTables tab, AdvArgs a) {
         r -= vdot3(sm + (size_t)lb * W_CONV, dj);
     });
     const double ap = a.c_dt * m.cv[node];
-    const double Tn = (r + T * ap) / (0.0 + ap);
+    double Tn;
+    if (a.ab2) {
+        /* AB2: Su = T ap + (3 R^n - R^{n-1}) / 2, T = Su / ap */
+        Tn = (T * ap + (3.0 * r - a.R_o[node]) / 2.0) / ap;
+    } else {
+        /* BDF1 / AB1 (the same sum in either order): T = (R + T ap) / ap */
+        Tn = (r + T * ap) / (0.0 + ap);
+    }
+    if (a.R_n) a.R_n[node] = r;
     a.T_n[node] = Tn;
     if (!isfinite(Tn)) atomicOr(m.status, NSEM_STATUS_NONFINITE);
 }
@@ -871,6 +900,10 @@ AdvArgs adv_args(NsemConvBuf* b, int cur, double dt) {
     a.T_o = b->T[cur];
     a.T_n = b->T[cur ^ 1];
     for (int c = 0; c < 3; c++) a.U[c] = b->U[c];
+    for (int c = 0; c < 3; c++) a.Ug[c] = b->analytic ? b->Ug[c] : nullptr;
+    a.R_n = nullptr;
+    a.R_o = nullptr;
+    a.ab2 = 0;
     a.lam = b->lam;
     a.d = b->d;
     for (int c = 0; c < 4; c++) a.mq[c] = b->mq[c];
@@ -945,6 +978,39 @@ int nsem_conv_steps(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int n
         const int e = (int)cudaGetLastError();
         if (e) return e;
         cur ^= 1;
+    }
+    return 0;
+}
+
+int nsem_conv_steps_wind(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps,
+                         double dt, const double* scale, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned sb = (unsigned)((m->n_slot + 255) / 256);
+    const int threads = ((m->np + 31) / 32) * 32;
+    const int64_t nw = m->n_int > m->n_slot ? m->n_int : m->n_slot;
+    for (int s = 0; s < nsteps; s++) {
+        if (b->analytic) {
+            k_conv_wind<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(*m, *b, scale ? scale[s] : 1.0);
+            int e = (int)cudaGetLastError();
+            if (!e) e = nsem_conv_lambda(m, b, stream);
+            if (e) return e;
+        }
+        AdvArgs a = adv_args(b, b->cur, dt);
+        if (b->order == 2) {
+            /* the first step of a run is AB1 (one right-hand side stored) */
+            a.R_n = b->R[b->hist & 1];
+            a.R_o = b->R[(b->hist + 1) & 1];
+            a.ab2 = b->hist >= 1;
+        }
+        const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+        if (m->n_ms > 0) k_conv_mortar<1><<<4 * mb, 128, 0, st>>>(*m, a);
+        k_conv_face<<<sb, 256, 0, st>>>(*m, a);
+        if (m->n_ms > 0) k_conv_mortar_gather<<<mb, 128, 0, st>>>(*m, a);
+        k_conv_vol<<<(unsigned)m->n_elem, threads, smem_conv(m), st>>>(*m, *t, a);
+        const int e = (int)cudaGetLastError();
+        if (e) return e;
+        b->cur ^= 1;
+        if (b->order == 2) b->hist++;
     }
     return 0;
 }

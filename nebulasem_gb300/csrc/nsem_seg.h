@@ -42,9 +42,21 @@ struct NsemConvBuf {
     double* mq[4] = {};           /* coarse side: |U| (lambda), then U T, T */
     double* mf[3] = {};           /* face flux vectors                      */
     double* dC = nullptr;         /* projected, lifted coarse-side flux     */
+    /* analytic winds (the app's problem_init LEVEQUE) and the AB2 scheme */
+    bool analytic = false;        /* wind = A(x) scaled per step            */
+    double* A[3] = {};            /* spatial part on interior nodes         */
+    double* Ag[3] = {};           /* spatial part at each used slot's ghost */
+    double* Ug[3] = {};           /* the step's wind at each slot's ghost   */
+    double* R[2] = {};            /* right-hand sides of the last two steps */
+    int order = 1;                /* 1: BDF1 / AB1, 2: AB2                  */
+    int hist = 0;                 /* right-hand sides stored (AB2)          */
 };
 
 int nsem_seg_prepare(const NsemDev* m);
+/* convection steps with the analytic wind scaled by scale[s] (NULL: 1) and
+ * the buffer's time scheme; advances b->cur and the AB2 history */
+int nsem_conv_steps_wind(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, int nsteps,
+                         double dt, const double* scale, void* stream);
 /* strong-form gradients of U (3 arrays) and the full theta T into G (12 per
  * node) with the per-slot scratch fF (4), for the viscous fluxes */
 /* the volume part of the gradients only, from given per-slot face values fF

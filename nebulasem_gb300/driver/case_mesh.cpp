@@ -266,13 +266,19 @@ BlockDesc read_block_description(const std::string& path) {
         if (b.patch[s].empty())
             throw std::runtime_error(path + ": a box side belongs to no patch and no default is set");
         if (b.patch[s] == "delete") {
-            if (sides[s].axis != 1 || b.patch[2] != "delete" || b.patch[3] != "delete" || b.n[1] != 1)
-                throw std::runtime_error(path + ": only the two y faces of a block one element "
-                                         "thick in y can be deleted (2D case)");
-            b.two_d = true;
+            /* the two faces of the j or the k axis of a block one element
+             * thick along it (srtb: y; advection-leveque: z) */
+            const int ax = sides[s].axis;
+            const int lo = ax == 1 ? 2 : 0;
+            if (ax == 0 || b.patch[lo] != "delete" || b.patch[lo + 1] != "delete" || b.n[ax] != 1)
+                throw std::runtime_error(path + ": only the two faces of the block's second or "
+                                         "third axis, one element thick along it, can be "
+                                         "deleted (2D case)");
+            b.del_axis = ax;
         }
     }
-    if (b.two_d) b.patch[2] = b.patch[3] = "";
+    if (b.del_axis == 1) b.patch[2] = b.patch[3] = "";
+    if (b.del_axis == 2) b.patch[0] = b.patch[1] = "";
     return b;
 }
 
@@ -597,10 +603,12 @@ void metric_pinv(const double J[3][3], const int npd[3], double out[9]) {
 
 CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
                         const std::array<uint32_t, 6>& side_bc) {
-    if (b.two_d && NPY != 1) throw std::runtime_error("a 2D case (y faces deleted) needs npy 0");
-    if (!b.two_d && NPY == 1) throw std::runtime_error("npy 0 needs the y faces deleted (2D case)");
+    if (b.del_axis == 1 && NPY != 1) throw std::runtime_error("a 2D case (y faces deleted) needs npy 0");
+    if (b.del_axis == 2 && NPZ != 1) throw std::runtime_error("a 2D case (z faces deleted) needs npz 0");
+    if (b.del_axis != 1 && NPY == 1) throw std::runtime_error("npy 0 needs the y faces deleted (2D case)");
+    if (b.del_axis != 2 && NPZ == 1) throw std::runtime_error("npz 0 needs the z faces deleted (2D case)");
     CaseMesh M;
-    const int nx = b.n[0], ny = b.two_d ? 1 : b.n[1], nz = b.n[2];
+    const int nx = b.n[0], ny = b.del_axis == 1 ? 1 : b.n[1], nz = b.del_axis == 2 ? 1 : b.n[2];
     const int NP = NPX * NPY * NPZ;
     int NPF;
     if (NPX <= NPY && NPX <= NPZ) NPF = NPY * NPZ;
@@ -637,7 +645,7 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     const int inner[3][2] = {{2, 1}, {1, 3}, {0, 5}};
     for (const auto& af : inner) {
         const int axis = af[0], fo = af[1];
-        if (b.two_d && axis == 1) continue;
+        if (axis == b.del_axis) continue;
         Group g;
         g.fo = fo;
         g.interior = true;
@@ -657,7 +665,7 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     std::vector<int64_t> bfaces;
     for (int fo = 0; fo < 6; fo++) {
         const int axis = sides[fo].axis, sgn = sides[fo].sign;
-        if (b.two_d && axis == 1) continue;
+        if (axis == b.del_axis) continue;
         Group g;
         g.fo = fo;
         g.interior = false;
@@ -842,8 +850,9 @@ CaseMesh build_box_mesh(const BlockDesc& b, int NPX, int NPY, int NPZ,
     }
 
     /* cell face lists (interior: z-, z+, y-, y+, x-, x+; ghost: its face) */
-    std::vector<int> order_ids = b.two_d ? std::vector<int>{0, 1, 4, 5}
-                                         : std::vector<int>{0, 1, 2, 3, 4, 5};
+    std::vector<int> order_ids = b.del_axis == 1   ? std::vector<int>{0, 1, 4, 5}
+                                 : b.del_axis == 2 ? std::vector<int>{2, 3, 4, 5}
+                                                   : std::vector<int>{0, 1, 2, 3, 4, 5};
     const int nfe = (int)order_ids.size();
     for (int64_t e = 0; e < ne; e++)
         for (int f : order_ids) M.all_faces.push_back((uint32_t)elem_faces[e * 6 + f]);

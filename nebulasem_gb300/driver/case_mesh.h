@@ -58,7 +58,9 @@ struct BlockDesc {
     /* patch name of each side, in the order k-, k+, j-, j+, i-, i+ of those axes
      * ("" if deleted) */
     std::array<std::string, 6> patch;
-    bool two_d = false;                    /* j faces deleted, one element in j */
+    /* 2D case: the axis (1 = j, 2 = k) whose two faces are deleted, one
+     * element thick along it (the mesh app's `delete` patch); -1 in 3D */
+    int del_axis = -1;
     /* the 8 corners in hex order and the 12 edges; curved edges from
      * `edges n{ arc|cosine|gaussian|ridge|schar side key [scale] }` */
     bool curved = false;

@@ -164,16 +164,22 @@ int run(const Options& opt) {
     if (upper(ctl.str("general", "convection_scheme", "HYBRID")) != "RUSANOV")
         throw std::runtime_error("convection_scheme must be RUSANOV (the DG flux of the GPU path)");
     const std::string ts = upper(ctl.str("general", "time_scheme", "BDF1"));
-    if (opt.scheme == "ref" && ts != "BDF1" && ts != "AB1")
-        throw std::runtime_error("time_scheme " + ts + " is not supported (BDF1 or AB1)");
+    if (opt.scheme == "ref" && ts != "BDF1" && ts != "AB1" && !(conv && ts == "AB2"))
+        throw std::runtime_error("time_scheme " + ts + " is not supported (BDF1 or AB1; AB2 for "
+                                 "the convection app)");
+    const int conv_order = ts == "AB2" ? 2 : 1;
     if (ctl.integer("general", "n_deferred", 0) != 0)
         throw std::runtime_error("n_deferred must be 0");
     if (write_interval < 1) throw std::runtime_error("write_interval must be >= 1");
     if (ctl.integer("general", "amr_step", 0) != 0)
         throw std::runtime_error("amr_step is set: adaptive mesh refinement is not supported");
     const std::string app = conv ? "convection" : "euler";
-    if (upper(ctl.str(app, "problem_init", "NONE")) != "NONE")
-        throw std::runtime_error("problem_init must be NONE");
+    const std::string pinit = upper(ctl.str(app, "problem_init", "NONE"));
+    /* the convection app's analytic winds: LEVEQUE on flat meshes
+     * (convection.cpp:86-91); the LAURITZEN winds need the spherical meshes */
+    const bool leveque = conv && pinit == "LEVEQUE";
+    if (pinit != "NONE" && !leveque)
+        throw std::runtime_error("problem_init must be NONE (or LEVEQUE for the convection app)");
     const bool buoyancy = conv ? false : ctl.flag("euler", "buoyancy", true);
     const bool diffusion = conv ? false : ctl.flag("euler", "diffusion", true);
     const int npx = (int)ctl.integer("general", "npx", 1) + 1;
@@ -352,8 +358,25 @@ int run(const Options& opt) {
     };
 
     double mass0 = 0, energy0 = 0, volume0 = 0;
+    /* LEVEQUE: the wind's spatial part on every node, ghosts included, with
+     * the C library's sin and pow in the app's order; its time factor
+     * cos(PI t / T), t = step dt, T = end_step dt, per step below */
+    constexpr double PI = 3.14159265358979323846264;
+    std::vector<double> scale;
     if (conv) {
         check(ctx, nsem_convection_set(ctx, U.values.data(), T.values.data()), "nsem_convection_set");
+        if (leveque) {
+            std::vector<double> A((size_t)M.n_all * 3);
+            for (int64_t k = 0; k < M.n_all; k++) {
+                const double x = M.cC[3 * k], y = M.cC[3 * k + 1];
+                A[3 * k] = std::pow(std::sin(PI * x), 2.0) * std::sin(2 * PI * y);
+                A[3 * k + 1] = -std::pow(std::sin(PI * y), 2.0) * std::sin(2 * PI * x);
+                A[3 * k + 2] = 0.0;
+            }
+            check(ctx, nsem_convection_wind(ctx, A.data(), conv_order), "nsem_convection_wind");
+        } else if (conv_order != 1) {
+            check(ctx, nsem_convection_wind(ctx, nullptr, conv_order), "nsem_convection_wind");
+        }
     } else {
         check(ctx, nsem_set_fields(ctx, rho0.data(), U.values.data(), T.values.data()), "nsem_set_fields");
         check(ctx, nsem_diagnostics(ctx, &mass0, &energy0, &volume0), "nsem_diagnostics");
@@ -371,8 +394,20 @@ int run(const Options& opt) {
         const long next_write = ((i + write_interval - 1) / write_interval) * write_interval;
         stop = std::min(stop, next_write);
         const int chunk = (int)(stop - i + 1);
-        if (conv) check(ctx, nsem_convection_step(ctx, chunk), "nsem_convection_step");
-        else check(ctx, nsem_step(ctx, chunk, scheme, prec), "nsem_step");
+        if (conv && leveque) {
+            scale.resize(chunk);
+            const double period = (double)end_step * dt;
+            for (int q = 0; q < chunk; q++) {
+                const double time = (double)(i + q) * dt;
+                scale[q] = std::cos(PI * time / period);
+            }
+            check(ctx, nsem_convection_step_scaled(ctx, chunk, scale.data()),
+                  "nsem_convection_step_scaled");
+        } else if (conv) {
+            check(ctx, nsem_convection_step(ctx, chunk), "nsem_convection_step");
+        } else {
+            check(ctx, nsem_step(ctx, chunk, scheme, prec), "nsem_step");
+        }
         steps += chunk;
         i = stop;
         std::printf("Time %f\n", (double)i * dt);

@@ -81,6 +81,10 @@ def lib():
                                                 ctypes.c_double, ctypes.c_int]
         _lib.nsem_oracle_convection.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        _lib.nsem_oracle_convection_wind.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_int,
+                                                     ctypes.c_void_p, ctypes.c_double,
+                                                     ctypes.c_int]
     return _lib
 
 
@@ -231,6 +235,18 @@ class OracleMesh:
         assert u.shape == (self.n_int, 3) and t.shape == (self.n_int,)
         lib().nsem_oracle_convection(ctypes.byref(self.struct), _ptr(u), _ptr(t), float(dt),
                                      int(nsteps))
+        return t
+
+    def convection_wind(self, U_all, scale, order, T, dt, nsteps):
+        """The convection app with an analytic wind: spatial part U_all on all
+        n_all nodes (n_all x 3) times scale[s] at step s (first two
+        components), order 1 (BDF1/AB1) or 2 (AB2)."""
+        u = np.ascontiguousarray(np.asarray(U_all, dtype=np.float64).reshape(-1, 3))
+        sc = np.ascontiguousarray(np.asarray(scale, dtype=np.float64))
+        t = np.array(T, dtype=np.float64, copy=True)
+        assert u.shape == (self.n_all, 3) and t.shape == (self.n_int,) and sc.shape == (nsteps,)
+        lib().nsem_oracle_convection_wind(ctypes.byref(self.struct), _ptr(u), _ptr(sc), int(order),
+                                          _ptr(t), float(dt), int(nsteps))
         return t
 
     def diagnostics(self, u):

@@ -152,6 +152,75 @@ prepare
 """
 
 
+# The reference's advection-leveque example, made small: the unit square in
+# x-y (z faces deleted, npz 0), problem_init LEVEQUE (the wind
+# (sin^2(pi x) sin(2 pi y), -sin^2(pi y) sin(2 pi x), 0) cos(pi t / T),
+# apps/convection/convection.cpp:86-91) and a cosine2 scalar bump
+GRID_XY = """8
+{{
+0 0 0
+1 0 0
+1 1 0
+0 1 0
+0 0 0.1
+1 0 0.1
+1 1 0.1
+0 1 0.1
+}}
+
+8{{0 1 2 3 4 5 6 7}} wall 3{{{nx} {ny} 1}} 3{{1 1 1}}
+
+top     4{{3 2 6 7}}
+bottom  4{{0 1 5 4}}
+delete  4{{0 1 2 3}} 4{{4 5 6 7}}
+sides   4{{1 2 5 6}} 4{{0 4 7 3}}
+"""
+
+
+def write_leveque_case(out, *, n, order, dt, steps, time_scheme="AB2"):
+    """The advection-leveque example's set-up on an n x n block of order `order`
+    for `steps` steps (end_step = steps, so the wind reverses once); a
+    controls_setup beside it names the euler app for the oracle harness."""
+    os.makedirs(out, exist_ok=True)
+    ctl = CONTROLS.format(end_step=steps, dt=dt, npx=order, npy=order, npz=0, viscosity=0.0,
+                          Pr=0.9, diffusion="NO", P0=100000, cp=1004.5, cv=717.5, gz=0)
+    ctl = ctl.replace("time_scheme                  BDF1",
+                      f"time_scheme                  {time_scheme}")
+    setup = ctl
+    ctl = ctl.replace("solver                       euler", "solver                       convection")
+    ctl += "\nconvection\n{\n    t_UR            0.8\n    problem_init    LEVEQUE\n}\n"
+    with open(os.path.join(out, "controls"), "w") as f:
+        f.write(ctl)
+    with open(os.path.join(out, "controls_setup"), "w") as f:
+        f.write(setup)
+    with open(os.path.join(out, "grid"), "w") as f:
+        f.write(GRID_XY.format(nx=n, ny=n))
+    files = {
+        "T0.txt": (1, "cosine2 0 0.5    0.25 0.25 0.05   0.25 0.25 1", "NEUMANN"),
+        "U0.txt": (3, "uniform 0 0 0", "SYMMETRY"),
+        "p0.txt": (1, "uniform 0", "NEUMANN"),
+        "rho0.txt": (1, "uniform 0", "NEUMANN"),
+    }
+    for name, (size, init, bc) in files.items():
+        with open(os.path.join(out, name), "w") as f:
+            f.write(FIELD.format(size=size, init=init, bc=bc))
+
+
+def leveque_wind(cC, steps, dt):
+    """The LEVEQUE wind's spatial part on every node and its time factor per
+    step, with the C library's sin, cos and pow in the app's operation order
+    (u = pow(sin(PI x), 2.0) * sin(2 PI y) * cos(PI t / T), t = i dt for step
+    i = 1..steps, T = end_step dt; w = 0)."""
+    import math
+    PI = 3.14159265358979323846264
+    xyz = cC.reshape(-1, 3)
+    A = [[math.pow(math.sin(PI * x), 2.0) * math.sin(2 * PI * y),
+          -math.pow(math.sin(PI * y), 2.0) * math.sin(2 * PI * x), 0.0] for x, y, _ in xyz]
+    period = steps * dt
+    scale = [math.cos(PI * (i * dt) / period) for i in range(1, steps + 1)]
+    return A, scale
+
+
 def write_case(out, *, dim, n, order, length, dt, steps, amp, center, radius, viscosity=0.0,
                Pr=0.9, solver="euler", wind=None, time_scheme="BDF1", P0=100000, cp=1004.5,
                cv=717.5, gz=-9.81, curved=None, refine=None, grading=None):

@@ -1142,11 +1142,16 @@ static void convection_core(const nsem_oracle_mesh* m, const double* U_in, const
     for (int step = 0; step < nsteps; step++) {
         if (U_all || step == 0) {
             /* the wind of this step (U = U(x) cos(pi t / T) for the app's
-             * analytic winds: the product with the step's factor, in the
-             * app's operation order) and its Rusanov speed cds(|U|)/2 */
+             * analytic winds: the product with the step's factor in the
+             * horizontal components, in the app's operation order; w = 0 as
+             * the app sets it) and its Rusanov speed cds(|U|)/2 */
             if (U_all && scale) {
 #pragma omp parallel for schedule(static)
-                for (int64_t i = 0; i < 3 * n_all; i++) U[i] = U_all[i] * scale[step];
+                for (int64_t i = 0; i < n_all; i++) {
+                    U[3 * i] = U_all[3 * i] * scale[step];
+                    U[3 * i + 1] = U_all[3 * i + 1] * scale[step];
+                    U[3 * i + 2] = U_all[3 * i + 2];
+                }
             }
             if (mort) {
                 for (int64_t i = 0; i < n_int; i++) nq[i] = vmag(U + 3 * i);
@@ -1232,8 +1237,8 @@ void nsem_oracle_convection(const nsem_oracle_mesh* m, const double* U_in, doubl
 /* The convection app with an analytic wind (problem_init LEVEQUE,
  * convection.cpp:45-93, 103-123): U_all [n_all*3] is the wind's spatial part
  * on every node (ghosts included) and scale[step] its time factor
- * cos(pi t / T), multiplied in the app's order; order 1 = BDF1/AB1,
- * 2 = AB2 (the first step AB1). */
+ * cos(pi t / T), multiplied into the first two components in the app's
+ * order; order 1 = BDF1/AB1, 2 = AB2 (the first step AB1). */
 void nsem_oracle_convection_wind(const nsem_oracle_mesh* m, const double* U_all, const double* scale,
                                  int order, double* T_in, double dt, int nsteps) {
     convection_core(m, NULL, U_all, scale, order, T_in, dt, nsteps);

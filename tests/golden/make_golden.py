@@ -89,6 +89,11 @@ CONV_PLAN = {
     "amr_c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0), 0.3),
 }
 
+# the advection-leveque example made small: n x n elements, order, dt, steps
+LEVEQUE_PLAN = {
+    "leveque_ab2": (8, 4, 0.0005, 40),
+}
+
 KEEP_F64 = ["cC", "cV", "Jinv", "fN", "fI", "p_ref", "rho_ref", "gh",
             "xgl0", "xgl1", "xgl2", "wgl0", "wgl1", "wgl2",
             "psi0", "psi1", "psi2", "dpsi0", "dpsi1", "dpsi2"]
@@ -282,6 +287,37 @@ def make_conv_case(name, ref_bin, tmp):
           f"({os.path.getsize(path) / 1e6:.2f} MB)")
 
 
+def make_leveque_case(name, ref_bin, tmp):
+    """The unmodified `convection` app with problem_init LEVEQUE and AB2: the
+    wind's spatial part on every node and its time factors (C library sin,
+    cos, pow, as the app evaluates them), step-0 and step-N scalar."""
+    from nebulasem_gb300.fields import read_field
+    from oracle.make_case import leveque_wind, write_leveque_case
+
+    n, order, dt, nsteps = LEVEQUE_PLAN[name]
+    case = os.path.join(tmp, "conv_" + name)
+    write_leveque_case(case, n=n, order=order, dt=dt, steps=nsteps)
+    run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
+    os.makedirs(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "euler_oracle"), "./controls_setup", "setup", "out"], case)
+    d = load_dump(os.path.join(case, "out"))
+    run([os.path.join(ref_bin, "convection"), "./controls"], case)
+    n_int = int(d["meta"][7])
+    out = {k: d[k] for k in KEEP_F64 + KEEP_U32}
+    A, scale = leveque_wind(d["cC"], nsteps, dt)
+    out["wind_all"] = np.asarray(A, dtype=np.float64).reshape(-1)
+    out["wind_scale"] = np.asarray(scale, dtype=np.float64)
+    out["fld0_T"] = d["fld_T"][:n_int]
+    v = read_field(os.path.join(case, "T1.bin")).values
+    assert v.shape[0] == n_int
+    out["fldN_T"] = v.reshape(-1)
+    out["dt"] = np.float64(dt)
+    out["nsteps"] = np.int64(nsteps)
+    out["time_scheme"] = np.int64(2)
+    np.savez_compressed(os.path.join(HERE, f"conv_{name}.npz"), **out)
+    print("wrote", f"conv_{name}.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", required=True, help="reference NebulaSEM source tree")
@@ -289,6 +325,7 @@ def main():
     ap.add_argument("--seg-cases", nargs="*", default=sorted(SEG_PLAN))
     ap.add_argument("--conv-cases", nargs="*", default=sorted(CONV_PLAN))
     ap.add_argument("--amr-cases", nargs="*", default=sorted(AMR_PLAN))
+    ap.add_argument("--leveque-cases", nargs="*", default=sorted(LEVEQUE_PLAN))
     ap.add_argument("-j", type=int, default=8)
     a = ap.parse_args()
     subprocess.run(["make", "-f", "oracle/Makefile.ref", f"REF={a.ref}", f"-j{a.j}"],
@@ -302,6 +339,8 @@ def main():
             make_seg_case(name, ref_bin, tmp)
         for name in a.conv_cases:
             make_conv_case(name, ref_bin, tmp)
+        for name in a.leveque_cases:
+            make_leveque_case(name, ref_bin, tmp)
         for name in a.amr_cases:
             make_amr_case(name, ref_bin, tmp)
     finally:

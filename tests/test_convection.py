@@ -27,3 +27,24 @@ def test_convection_gpu_bitwise_vs_reference(case):
     m = oracle.OracleMesh(g)
     assert np.array_equal(t, m.convection(U, g["fld0_T"], dt, steps))
     s.close()
+
+
+def test_convection_gpu_leveque_ab2_bitwise_vs_reference():
+    """The analytic LEVEQUE wind and AB2 on the GPU, in two calls (the AB2
+    history carries over): the unmodified app's scalar bit for bit."""
+    import nebulasem_gb300 as ng
+    g = load_golden("conv_leveque_ab2")
+    n = int(g["meta"][7])
+    n_all = int(g["meta"][8])
+    dt, steps = float(g["dt"]), int(g["nsteps"])
+    A = g["wind_all"].reshape(-1, 3)[:n_all]
+    sc = g["wind_scale"]
+    s = ng.Solver(g, dt=dt)
+    s.convection_set(np.zeros((n, 3)), g["fld0_T"])
+    s.convection_wind(A, 2)
+    k = steps // 3
+    s.convection_step_scaled(k, sc[:k])
+    s.convection_step_scaled(steps - k, sc[k:])
+    t = s.convection_get()
+    assert np.array_equal(t, g["fldN_T"])
+    s.close()

@@ -264,3 +264,24 @@ def test_bump_edges_follow_their_shape(tmp_path, shape):
     # a genuinely curved metric: the elements over the slope are not affine
     J = dd["Jinv"].reshape(-1, 9)[: int(dd["meta"][7])]
     assert np.abs(J[:, 5]).max() > 1e-5 or np.abs(J[:, 8]).max() > 1e-5
+
+
+def test_driver_leveque_case_follows_convection_binary(tmp_path):
+    """The advection-leveque set-up (unit square in x-y, z faces deleted,
+    npz 0, problem_init LEVEQUE, AB2) made small: the oracle run on the
+    driver's mesh and initial scalar, with the analytic wind on the driver's
+    node coordinates, ends in the unmodified convection binary's scalar bit
+    for bit (nodes matched by coordinates)."""
+    from oracle.make_case import leveque_wind, write_leveque_case
+    g = load_golden("conv_leveque_ab2")
+    dt, steps = float(g["dt"]), int(g["nsteps"])
+    case = os.path.join(str(tmp_path), "leveque")
+    write_leveque_case(case, n=8, order=4, dt=dt, steps=steps)
+    a = dump_case(case)
+    n, n_all = int(a["meta"][7]), int(a["meta"][8])
+    A, sc = leveque_wind(np.asarray(a["cC"])[:3 * n_all], steps, dt)
+    assert np.array_equal(np.asarray(sc), g["wind_scale"])
+    t = oracle.OracleMesh(a).convection_wind(np.asarray(A), sc, 2, a["fld_T"], dt, steps)
+    kd, kg = node_order(a["cC"], n), node_order(g["cC"], n)
+    assert np.array_equal(a["cC"].reshape(-1, 3)[:n][kd], g["cC"].reshape(-1, 3)[:n][kg])
+    assert np.array_equal(t[kd], g["fldN_T"][kg])

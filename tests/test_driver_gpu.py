@@ -258,3 +258,20 @@ def test_text_output_and_high_order(tmp_path):
     assert np.array_equal(out["rho"][:, 0], rho)
     assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
     assert np.array_equal(out["T"][:, 0], T)
+
+
+def test_convection_leveque_ab2_run_matches_binary(tmp_path):
+    """solver convection with problem_init LEVEQUE and AB2 through the driver
+    on the GPU: the written scalar equals the unmodified convection binary's
+    bit for bit (nodes matched by coordinates)."""
+    from oracle.make_case import write_leveque_case
+    g = load_golden("conv_leveque_ab2")
+    dt, steps = float(g["dt"]), int(g["nsteps"])
+    d = os.path.join(str(tmp_path), "leveque")
+    write_leveque_case(d, n=8, order=4, dt=dt, steps=steps)
+    a = dump_case(d)
+    run_driver(d, "--print-every", "7")
+    T = read_field(os.path.join(d, "T1.bin")).values[:, 0]
+    n = int(a["meta"][7])
+    kd, kg = node_order(a["cC"], n), node_order(g["cC"], n)
+    assert np.array_equal(T[kd], g["fldN_T"][kg])

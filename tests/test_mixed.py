@@ -97,9 +97,9 @@ def test_mixed_mass_conservation_and_state_switching():
 
 
 def test_mixed_order7_line_sum_paths(monkeypatch):
-    """Order 7: line sums on the tensor cores (three TF32 products per term,
-    the default) and on the FP32 pipes (NSEM_MIXED_LINES=fp32) both stay within
-    1e-5 of the FP64 form and agree with each other to FP32 rounding."""
+    """Order 7: line sums on the FP32 pipes (the default) and on the tensor
+    cores (NSEM_MIXED_LINES=tensor: three TF32 products per term) both stay
+    within 1e-5 of the FP64 form and agree with each other to FP32 rounding."""
     import nebulasem_gb300 as ng
     g = load_golden("g3_2n7")
     u = golden_state(g, "up")
