@@ -30,6 +30,7 @@
 #include "nsem_adjoint.h"
 #include "nsem_seg.h"
 #include "nsem_gather.cuh"
+#include "nsem_mortar.cuh"
 
 namespace {
 
@@ -110,6 +111,7 @@ struct FaceAdjArgs {
 __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.n_slot) return;
+    if (m.n_ms && m.ms_of[k] >= 0) return;   /* non-conforming: k_adj_face_mortar */
     const int32_t c1 = m.c1[k], c2 = m.c2[k];
     const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
     const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
@@ -213,6 +215,53 @@ __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a
     a.adjN[4][k] = Tb2; a.adjN[5][k] = pb2;
 }
 
+/* ------------------------------------------------------------------------
+ * Non-conforming (2:1) faces, inviscid.  The forward face flux of a mortar
+ * slot (nsem_fp64.cu, k_face) reads the coarse side through 19 quantities
+ * interpolated from the coarse face's nodes: |U|, c, U rho (3), rho, the
+ * momentum flux tensor (rho U) (x) U + p' I (9, tensor order), the theta flux
+ * (rho U) theta (3), rho theta.  The flux is a function of the two sides'
+ * quantity sets alone, so its tangent and transpose are written on quantity
+ * sets: the fine side's from its node, the coarse side's interpolated
+ * (tangents: interpolated tangents; adjoints: scattered back through the
+ * transposed interpolation, then through the quantities' chain at each
+ * coarse node).  The coarse side lifts the projection of the slot fluxes
+ * (psiCor) dotted with each slot's normal: its transpose gathers over the
+ * facet's slots.
+ * ------------------------------------------------------------------------ */
+__device__ __forceinline__ void tens_rc(int t, int& ra, int& rb) {
+    ra = t < 3 ? t : (t == XY || t == XZ) ? 0 : (t == YZ || t == YX) ? 1 : 2;
+    rb = t < 3 ? t : (t == YX || t == ZX) ? 0 : (t == XY || t == ZY) ? 1 : 2;
+}
+
+/* adjoints qb of the 19 face quantities of a node -> its primitive adjoints */
+__device__ __forceinline__ void face_q_vjp(const NsemDev& m, const NodePrim& P, const double* qb,
+                                           double& rbar, double* Ub, double& Tb, double& pb) {
+    const double Fc[3] = {P.U[0] * P.r, P.U[1] * P.r, P.U[2] * P.r};
+    if (P.mu > 0)
+        for (int c = 0; c < 3; c++) Ub[c] += qb[0] * P.U[c] / P.mu;
+    if (P.c > 0) Tb += qb[1] * m.gR / (2 * P.c);
+    double Fcb[3] = {qb[2], qb[3], qb[4]};
+    rbar += qb[5];
+    for (int t = 0; t < 9; t++) {
+        int ra, rb;
+        tens_rc(t, ra, rb);
+        Fcb[ra] += qb[6 + t] * P.U[rb];
+        Ub[rb] += qb[6 + t] * Fc[ra];
+        if (t < 3) pb += qb[6 + t];
+    }
+    for (int c = 0; c < 3; c++) {
+        Fcb[c] += qb[15 + c] * P.T;
+        Tb += qb[15 + c] * Fc[c];
+    }
+    rbar += qb[18] * P.T;
+    Tb += qb[18] * P.r;
+    for (int c = 0; c < 3; c++) {
+        Ub[c] += Fcb[c] * P.r;
+        rbar += Fcb[c] * P.U[c];
+    }
+}
+
 struct VolAdjArgs {
     const double* S[5];
     const double* W[5];
@@ -225,6 +274,9 @@ struct VolAdjArgs {
     const double* dbv[4];
     double* Gbs[12];
     double* mub;
+    /* non-conforming faces: per node the adjoints of the 19 face quantities
+     * interpolated from it onto mortar slots (else null) */
+    const double* qb[19];
 };
 
 /* registers capped for the largest element: 736 threads (N+1 = 9) inviscid,
@@ -358,14 +410,21 @@ __global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const
     /* gravity source: r_m -= g (rho - rho_ref) cV */
     const double cv = m.cv[node];
     rbar += -(rb[NP + t] * m.g[0] + rb[2 * NP + t] * m.g[1] + rb[3 * NP + t] * m.g[2]) * cv;
-    /* face contributions gathered through the lift lists */
-    for (int j = 0; j < 3; j++) {
+    /* face contributions gathered through the lift lists (a coarse side of a
+     * non-conforming face contributes through its interpolated quantities) */
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
+        if (code & 2) continue;
         const int64_t k = code >> 2;
         const double* const* src = (code & 1) ? a.adjN : a.adjO;
         rbar += src[0][k]; Ub[0] += src[1][k]; Ub[1] += src[2][k]; Ub[2] += src[3][k];
         Tb += src[4][k]; pb += src[5][k];
+    }
+    if (a.qb[0]) {
+        double q[19];
+        for (int c = 0; c < 19; c++) q[c] = a.qb[c][node];
+        face_q_vjp(m, P, q, rbar, Ub, Tb, pb);
     }
     /* EOS: p = P0 (rho theta R / P0)^gamma */
     rbar += pb * m.gamma * P.p / P.r;
@@ -418,6 +477,275 @@ __device__ __forceinline__ void sym_jvp(const double* p, const double* en, const
     const double ds = (magP > 0 ? vdot3(p, dp) / (magP * magR) : 0.0) -
                       magP * vdot3(r, dp) / (magR * magR * magR);
     for (int k = 0; k < 3; k++) dout[k] = Ad[k] * s + r[k] * ds;
+}
+
+/* the 19 face quantities of a node, and their tangents along d (d may be null) */
+__device__ __forceinline__ void face_q(const NodePrim& P, const NodeTan* d, double* q, double* dq) {
+    const double Fc[3] = {P.U[0] * P.r, P.U[1] * P.r, P.U[2] * P.r};
+    q[0] = P.mu;
+    q[1] = P.c;
+    for (int c = 0; c < 3; c++) q[2 + c] = Fc[c];
+    q[5] = P.r;
+    for (int t = 0; t < 9; t++) {
+        int ra, rb;
+        tens_rc(t, ra, rb);
+        q[6 + t] = Fc[ra] * P.U[rb] + (t < 3 ? P.pp : 0.0);
+    }
+    for (int c = 0; c < 3; c++) q[15 + c] = Fc[c] * P.T;
+    q[18] = P.r * P.T;
+    if (!d) return;
+    double dFc[3];
+    for (int c = 0; c < 3; c++) dFc[c] = d->U[c] * P.r + P.U[c] * d->r;
+    dq[0] = d->mu;
+    dq[1] = d->c;
+    for (int c = 0; c < 3; c++) dq[2 + c] = dFc[c];
+    dq[5] = d->r;
+    for (int t = 0; t < 9; t++) {
+        int ra, rb;
+        tens_rc(t, ra, rb);
+        dq[6 + t] = dFc[ra] * P.U[rb] + Fc[ra] * d->U[rb] + (t < 3 ? d->p : 0.0);
+    }
+    for (int c = 0; c < 3; c++) dq[15 + c] = dFc[c] * P.T + Fc[c] * d->T;
+    dq[18] = d->r * P.T + P.r * d->T;
+}
+
+struct MortarArgs {
+    const double* S[5];
+    const double* dS[5];     /* tangent runs (else null) */
+    const double* W[5];      /* adjoint runs: w */
+    double* mq[19];
+    double* dmq[19];
+    double* dmf[15];
+    double* ddC[5];
+    double* dd[5];           /* tangent runs: per slot lifted tangent (fine side) */
+    double* mqb[19];
+    double* qb[19];
+    double* adjO[NPA];
+    double* adjN[NPA];
+};
+
+/* per mortar slot: the coarse side's quantities (and tangents) interpolated */
+__global__ void __launch_bounds__(128) k_mortar_q(const NsemDev m, MortarArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const bool tan = a.dS[0] != nullptr;
+    double out[38];
+    mortar_interp<38>(m, ms, [&](int64_t node, double* v) {
+        const NodePrim P = node_prim(m, a.S, node);
+        if (tan) {
+            const NodeTan d = node_tan(m, P, a.dS, node);
+            face_q(P, &d, v, v + 19);
+        } else {
+            face_q(P, nullptr, v, nullptr);
+            for (int c = 19; c < 38; c++) v[c] = 0.0;
+        }
+    }, out);
+    for (int c = 0; c < 19; c++) {
+        a.mq[c][ms] = out[c];
+        if (tan) a.dmq[c][ms] = out[19 + c];
+    }
+}
+
+/* the two sides' quantity sets of a mortar slot: the fine node's own, the
+ * coarse side's interpolated */
+__device__ __forceinline__ void mortar_sides(const NsemDev& m, const MortarArgs& a, int64_t ms,
+                                             int64_t k, int side, bool tan, double* q1, double* dq1,
+                                             double* q2, double* dq2, NodePrim& Pf) {
+    const int64_t fine = side == 1 ? m.c2[k] : m.c1[k];
+    Pf = node_prim(m, a.S, fine);
+    double* qf = side == 1 ? q2 : q1;
+    double* dqf = side == 1 ? dq2 : dq1;
+    double* qc = side == 1 ? q1 : q2;
+    double* dqc = side == 1 ? dq1 : dq2;
+    if (tan) {
+        const NodeTan d = node_tan(m, Pf, a.dS, fine);
+        face_q(Pf, &d, qf, dqf);
+    } else {
+        face_q(Pf, nullptr, qf, nullptr);
+    }
+    for (int c = 0; c < 19; c++) {
+        qc[c] = a.mq[c][ms];
+        if (tan) dqc[c] = a.dmq[c][ms];
+    }
+}
+
+/* tangent of a mortar slot's flux: the fine side's lifted value and the flux
+ * vectors for the coarse side's projection */
+__global__ void __launch_bounds__(128) k_tan_face_mortar(const NsemDev m, MortarArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const int side = ms_field(m, NSEM_MS_SIDE, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    double q1[19], dq1[19], q2[19], dq2[19];
+    NodePrim Pf;
+    mortar_sides(m, a, ms, k, side, true, q1, dq1, q2, dq2, Pf);
+    const double lam = ((q1[0] * fi + q2[0] * fo) + (q1[1] * fi + q2[1] * fo)) / 2;
+    const double dlam = ((dq1[0] * fi + dq2[0] * fo) + (dq1[1] * fi + dq2[1] * fo)) / 2;
+    double dF[15];
+    for (int c = 0; c < 3; c++)
+        dF[c] = dq1[2 + c] * fi + dq2[2 + c] * fo -
+                en[c] * (dlam * (q2[5] - q1[5]) + lam * (dq2[5] - dq1[5]));
+    double ddq[3];
+    for (int c = 0; c < 3; c++)
+        ddq[c] = (dq2[2 + c] - dq1[2 + c]) * lam + (q2[2 + c] - q1[2 + c]) * dlam;
+    for (int t = 0; t < 9; t++) {
+        int r, c;
+        tens_rc(t, r, c);
+        dF[3 + t] = dq1[6 + t] * fi + dq2[6 + t] * fo - en[r] * ddq[c];
+    }
+    for (int c = 0; c < 3; c++)
+        dF[12 + c] = dq1[15 + c] * fi + dq2[15 + c] * fo -
+                     en[c] * (dlam * (q2[18] - q1[18]) + lam * (dq2[18] - dq1[18]));
+    for (int c = 0; c < 15; c++) a.dmf[c][ms] = dF[c];
+    a.dd[0][k] = vdot3(dF, n);
+    a.dd[1][k] = dF[3 + XX] * n[0] + dF[3 + XY] * n[1] + dF[3 + XZ] * n[2];
+    a.dd[2][k] = dF[3 + YX] * n[0] + dF[3 + YY] * n[1] + dF[3 + YZ] * n[2];
+    a.dd[3][k] = dF[3 + ZX] * n[0] + dF[3 + ZY] * n[1] + dF[3 + ZZ] * n[2];
+    a.dd[4][k] = vdot3(dF + 12, n);
+}
+
+/* the coarse side's lifted tangents: projected flux tangents . the slot's normal */
+__global__ void __launch_bounds__(128) k_tan_mortar_gather(const NsemDev m, MortarArgs a) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 5 * m.n_ms) return;
+    const int64_t ms = id / 5;
+    const int r = (int)(id % 5);
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    double P[3];
+    if (r == 0 || r == 4) {
+        double* src[3] = {a.dmf[r == 0 ? 0 : 12], a.dmf[r == 0 ? 1 : 13], a.dmf[r == 0 ? 2 : 14]};
+        mortar_project<3>(m, ms, src, P);
+    } else {
+        const int q = r - 1;
+        double* src[3] = {a.dmf[3 + (q == 0 ? XX : q == 1 ? YX : ZX)],
+                          a.dmf[3 + (q == 0 ? XY : q == 1 ? YY : ZY)],
+                          a.dmf[3 + (q == 0 ? XZ : q == 1 ? YZ : ZZ)]};
+        mortar_project<3>(m, ms, src, P);
+    }
+    a.ddC[r][ms] = vdot3(P, n);
+}
+
+/* adjoint of a mortar slot's flux: the flux-vector adjoints from the fine
+ * side's lift of this slot and from the coarse side's lifts of the facet's
+ * projections, then the two quantity sets' adjoints: the fine side's to its
+ * primitive adjoints (gathered by the volume kernel), the coarse side's kept
+ * per slot for the transposed interpolation */
+__global__ void __launch_bounds__(128) k_adj_face_mortar(const NsemDev m, MortarArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const int side = ms_field(m, NSEM_MS_SIDE, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
+    const double fi = m.fi[k], fo = 1 - fi;
+    double q1[19], q2[19];
+    NodePrim Pf;
+    mortar_sides(m, a, ms, k, side, false, q1, nullptr, q2, nullptr, Pf);
+    const double lam = ((q1[0] * fi + q2[0] * fo) + (q1[1] * fi + q2[1] * fo)) / 2;
+    /* flux-vector adjoints: rbar = -w / cV; the owner lifts +, the neighbour - */
+    double Fb[15] = {0};
+    {
+        const int64_t fine = side == 1 ? m.c2[k] : m.c1[k];
+        const double sg = side == 1 ? -1.0 : 1.0;
+        double db[5];
+        for (int v = 0; v < 5; v++) db[v] = sg * (-a.W[v][fine] / m.cv[fine]);
+        for (int c = 0; c < 3; c++) {
+            Fb[c] += db[0] * n[c];
+            Fb[12 + c] += db[4] * n[c];
+        }
+        for (int t = 0; t < 9; t++) {
+            int r, c;
+            tens_rc(t, r, c);
+            Fb[3 + t] += db[1 + r] * n[c];
+        }
+    }
+    {
+        /* the coarse side: dC[s'] = (sum_j Pcor(j -> s') F_j) . n_s' over the
+         * facet's slots s' */
+        const int Na = ms_field(m, NSEM_MS_NA, ms), Nb = ms_field(m, NSEM_MS_NB, ms);
+        const int64_t first = ms_field(m, NSEM_MS_FIRST, ms);
+        const int ja = (int)((ms - first) / Nb), jb = (int)((ms - first) % Nb);
+        for (int sa = 0; sa < Na; sa++)
+            for (int sb = 0; sb < Nb; sb++) {
+                const int64_t s2 = first + sa * Nb + sb;
+                const int64_t k2 = ms_field(m, NSEM_MS_K, s2);
+                const int side2 = ms_field(m, NSEM_MS_SIDE, s2);
+                const int64_t coarse = side2 == 1 ? m.c1[k2] : m.c2[k2];
+                const double sg = side2 == 1 ? 1.0 : -1.0;
+                const double* Pa = m.psic + ms_field(m, NSEM_MS_TA, s2) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+                const double* Pb = m.psic + ms_field(m, NSEM_MS_TB, s2) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+                const int na = ms_field(m, NSEM_MS_IA, s2), nb = ms_field(m, NSEM_MS_IB, s2);
+                const double w = Pa[ja * Na + na] * Pb[jb * Nb + nb];
+                const double n2[3] = {m.fn[k2], m.fn[m.n_slot + k2], m.fn[2 * m.n_slot + k2]};
+                double db[5];
+                for (int v = 0; v < 5; v++) db[v] = w * sg * (-a.W[v][coarse] / m.cv[coarse]);
+                for (int c = 0; c < 3; c++) {
+                    Fb[c] += db[0] * n2[c];
+                    Fb[12 + c] += db[4] * n2[c];
+                }
+                for (int t = 0; t < 9; t++) {
+                    int r, c;
+                    tens_rc(t, r, c);
+                    Fb[3 + t] += db[1 + r] * n2[c];
+                }
+            }
+    }
+    /* the quantity sets' adjoints */
+    const double A0 = vdot3(Fb, en), B4 = vdot3(Fb + 12, en);
+    double dqb[3] = {0, 0, 0};
+    for (int t = 0; t < 9; t++) {
+        int r, c;
+        tens_rc(t, r, c);
+        dqb[c] -= Fb[3 + t] * en[r];
+    }
+    double lamb = -A0 * (q2[5] - q1[5]) - B4 * (q2[18] - q1[18]);
+    for (int c = 0; c < 3; c++) lamb += dqb[c] * (q2[2 + c] - q1[2 + c]);
+    double qb1[19], qb2[19];
+    qb1[0] = lamb * fi / 2; qb2[0] = lamb * fo / 2;
+    qb1[1] = lamb * fi / 2; qb2[1] = lamb * fo / 2;
+    for (int c = 0; c < 3; c++) {
+        qb1[2 + c] = Fb[c] * fi - dqb[c] * lam;
+        qb2[2 + c] = Fb[c] * fo + dqb[c] * lam;
+    }
+    qb1[5] = A0 * lam; qb2[5] = -A0 * lam;
+    for (int t = 0; t < 9; t++) { qb1[6 + t] = Fb[3 + t] * fi; qb2[6 + t] = Fb[3 + t] * fo; }
+    for (int c = 0; c < 3; c++) { qb1[15 + c] = Fb[12 + c] * fi; qb2[15 + c] = Fb[12 + c] * fo; }
+    qb1[18] = B4 * lam; qb2[18] = -B4 * lam;
+    const double* qbf = side == 1 ? qb2 : qb1;
+    const double* qbc = side == 1 ? qb1 : qb2;
+    double rbar = 0, Ub[3] = {0, 0, 0}, Tb = 0, pb = 0;
+    face_q_vjp(m, Pf, qbf, rbar, Ub, Tb, pb);
+    double* const* fine_out = side == 1 ? a.adjN : a.adjO;
+    double* const* coarse_out = side == 1 ? a.adjO : a.adjN;
+    fine_out[0][k] = rbar; fine_out[1][k] = Ub[0]; fine_out[2][k] = Ub[1]; fine_out[3][k] = Ub[2];
+    fine_out[4][k] = Tb; fine_out[5][k] = pb;
+    for (int v = 0; v < NPA; v++) coarse_out[v][k] = 0.0;
+    for (int c = 0; c < 19; c++) a.mqb[c][ms] = qbc[c];
+}
+
+/* the transposed interpolation: each mortar slot's coarse-side adjoints back
+ * onto the coarse face's nodes (atomic: a node takes several slots) */
+__global__ void __launch_bounds__(128) k_adj_mortar_scatter(const NsemDev m, MortarArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int base = ms_field(m, NSEM_MS_BASE, ms), sa = ms_field(m, NSEM_MS_SA, ms),
+              sb = ms_field(m, NSEM_MS_SB, ms), Na = ms_field(m, NSEM_MS_NA, ms),
+              Nb = ms_field(m, NSEM_MS_NB, ms), ia = ms_field(m, NSEM_MS_IA, ms),
+              ib = ms_field(m, NSEM_MS_IB, ms);
+    const double* Pa = m.psir + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Pb = m.psir + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    double qb[19];
+    for (int c = 0; c < 19; c++) qb[c] = a.mqb[c][ms];
+    for (int na = 0; na < Na; na++)
+        for (int nb = 0; nb < Nb; nb++) {
+            const int64_t node = (int64_t)base + na * sa + nb * sb;
+            const double w = Pa[na * Na + ia] * Pb[nb * Nb + ib];
+            for (int c = 0; c < 19; c++) atomicAdd(a.qb[c] + node, w * qb[c]);
+        }
 }
 
 struct FaceTanArgs {
@@ -489,6 +817,7 @@ __global__ void __launch_bounds__(256) k_tan_grad_face(const NsemDev m, GradFace
 __global__ void __launch_bounds__(128) k_tan_face(const NsemDev m, FaceTanArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.n_slot) return;
+    if (m.n_ms && m.ms_of[k] >= 0) return;   /* non-conforming: k_tan_face_mortar */
     const int32_t c1 = m.c1[k], c2 = m.c2[k];
     const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
     const double en[3] = {m.en[k], m.en[m.n_slot + k], m.en[2 * m.n_slot + k]};
@@ -576,6 +905,7 @@ struct VolTanArgs {
     const double* S[5];
     const double* dS[5];
     const double* dd[5];
+    const double* ddC[5];    /* non-conforming faces: projected, lifted tangents */
     double* out[5];          /* J_L(v) dv */
     const double* G[12];     /* viscous runs (else null) */
     const double* dG[12];
@@ -623,13 +953,18 @@ __global__ void k_tan_volume(const NsemDev m, const NsemTables tab, VolTanArgs a
     __syncthreads();
     if (!active) return;
     double r[5] = {0, 0, 0, 0, 0};
-    /* surface lift */
-    for (int j = 0; j < 3; j++) {
+    /* surface lift (a coarse side of a non-conforming face lifts the
+     * projected tangent) */
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
         const int64_t k = code >> 2;
         const double sg = (code & 1) ? -1.0 : 1.0;
-        for (int v = 0; v < 5; v++) r[v] += sg * a.dd[v][k];
+        if (code & 2) {
+            for (int v = 0; v < 5; v++) r[v] += sg * a.ddC[v][k];
+        } else {
+            for (int v = 0; v < 5; v++) r[v] += sg * a.dd[v][k];
+        }
     }
     /* volume term: r[a] -= dF_b . (Jin_b dpsi(b -> a)) over the lines through a */
     nsem_volume_gather<TAN_W, 15>(NPX, NPY, NPZ, sm, dps, t, [&](int lb, const double* dj) {
@@ -842,6 +1177,22 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
     for (int v = 0; v < NPA; v++) { fa.adjO[v] = ab->adjO[v]; fa.adjN[v] = ab->adjN[v]; }
     const int64_t fb = (m->n_slot + 127) / 128;
     k_adj_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
+    for (int c = 0; c < 19; c++) va.qb[c] = nullptr;
+    if (m->n_ms > 0) {
+        MortarArgs ma{};
+        for (int v = 0; v < 5; v++) { ma.S[v] = S[v]; ma.W[v] = W[v]; }
+        for (int c = 0; c < 19; c++) { ma.mq[c] = ab->mq[c]; ma.mqb[c] = ab->mqb[c]; ma.qb[c] = ab->qb[c]; }
+        for (int v = 0; v < NPA; v++) { ma.adjO[v] = ab->adjO[v]; ma.adjN[v] = ab->adjN[v]; }
+        for (int c = 0; c < 19; c++) {
+            const cudaError_t ce = cudaMemsetAsync(ab->qb[c], 0, (size_t)m->n_int * sizeof(double), st);
+            if (ce != cudaSuccess) return (int)ce;
+        }
+        const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+        k_mortar_q<<<mb, 128, 0, st>>>(*m, ma);
+        k_adj_face_mortar<<<mb, 128, 0, st>>>(*m, ma);
+        k_adj_mortar_scatter<<<mb, 128, 0, st>>>(*m, ma);
+        for (int c = 0; c < 19; c++) va.qb[c] = ab->qb[c];
+    }
     for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.W[v] = W[v]; va.G[v] = G[v]; }
     for (int v = 0; v < NPA; v++) { va.adjO[v] = ab->adjO[v]; va.adjN[v] = ab->adjN[v]; }
     const int threads = ((m->np + 31) / 32) * 32;
@@ -889,6 +1240,19 @@ int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
     for (int v = 0; v < 5; v++) { fa.S[v] = S[v]; fa.dS[v] = dS[v]; fa.dd[v] = ab->adjO[v]; }
     const int64_t fb = (m->n_slot + 127) / 128;
     k_tan_face<<<(unsigned)fb, 128, 0, st>>>(*m, fa);
+    for (int v = 0; v < 5; v++) va.ddC[v] = nullptr;
+    if (m->n_ms > 0) {
+        MortarArgs ma{};
+        for (int v = 0; v < 5; v++) { ma.S[v] = S[v]; ma.dS[v] = dS[v]; ma.dd[v] = ab->adjO[v]; }
+        for (int c = 0; c < 19; c++) { ma.mq[c] = ab->mq[c]; ma.dmq[c] = ab->dmq[c]; }
+        for (int c = 0; c < 15; c++) ma.dmf[c] = ab->dmf[c];
+        for (int v = 0; v < 5; v++) ma.ddC[v] = ab->ddC[v];
+        const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+        k_mortar_q<<<mb, 128, 0, st>>>(*m, ma);
+        k_tan_face_mortar<<<mb, 128, 0, st>>>(*m, ma);
+        k_tan_mortar_gather<<<(unsigned)((5 * m->n_ms + 127) / 128), 128, 0, st>>>(*m, ma);
+        for (int v = 0; v < 5; v++) va.ddC[v] = ab->ddC[v];
+    }
     for (int v = 0; v < 5; v++) { va.S[v] = S[v]; va.dS[v] = dS[v]; va.dd[v] = ab->adjO[v]; va.out[v] = out[v]; }
     const int threads = ((m->np + 31) / 32) * 32;
     const size_t smem = ((size_t)m->np * TAN_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);

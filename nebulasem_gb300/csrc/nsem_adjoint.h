@@ -35,6 +35,16 @@ struct NsemAdjBuf {
     double* mub = nullptr;  /* per node: adjoint of mu = rho nu                   */
     double* agO[4] = {};    /* per slot: gradient face-term adjoints, owner side  */
     double* agN[4] = {};    /* per slot: neighbour side                           */
+    /* non-conforming (2:1) faces, inviscid runs: per mortar slot the coarse
+     * side's 19 interpolated face quantities and their tangents, the tangent
+     * flux vectors (15) and the projected, lifted tangents (5), the adjoints of
+     * the interpolated quantities; per node the transposed interpolation */
+    double* mq[19] = {};
+    double* dmq[19] = {};
+    double* dmf[15] = {};
+    double* ddC[5] = {};
+    double* mqb[19] = {};
+    double* qb[19] = {};
     int nsteps = 0, every = 0, n_ckpt = 0;
     bool ready = false;
 };

@@ -74,6 +74,16 @@ nsem_status require_conforming(nsem_ctx* c) {
     return NSEM_OK;
 }
 
+/* the FP64 tangent-linear and adjoint forms take non-conforming faces in
+ * inviscid runs */
+nsem_status require_inviscid_on_mortars(nsem_ctx* c) {
+    if (c && c->dev.n_ms > 0 && c->dev.nu != 0.0)
+        return fail(c, NSEM_UNSUPPORTED,
+                    "non-conforming (2:1) faces with the artificial viscosity: the "
+                    "tangent-linear and adjoint forms are built for inviscid runs there");
+    return NSEM_OK;
+}
+
 nsem_status cuda_fail(nsem_ctx* c, cudaError_t e, const char* where) {
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     return fail(c, NSEM_CUDA_ERROR, m);
@@ -767,6 +777,20 @@ static nsem_status adj_alloc(nsem_ctx* ctx) {
         if ((s = dalloc(ctx, &A.adjO[v], ctx->dev.n_slot)) != NSEM_OK) return s;
         if ((s = dalloc(ctx, &A.adjN[v], ctx->dev.n_slot)) != NSEM_OK) return s;
     }
+    if (ctx->dev.n_ms > 0) {
+        /* non-conforming faces: per mortar slot and per node (inviscid) */
+        const size_t nm = (size_t)ctx->dev.n_ms, n = (size_t)ctx->dev.n_int;
+        for (int c = 0; c < 19; c++) {
+            if ((s = dalloc(ctx, &A.mq[c], nm)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.dmq[c], nm)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.mqb[c], nm)) != NSEM_OK) return s;
+            if ((s = dalloc(ctx, &A.qb[c], n)) != NSEM_OK) return s;
+        }
+        for (int c = 0; c < 15; c++)
+            if ((s = dalloc(ctx, &A.dmf[c], nm)) != NSEM_OK) return s;
+        for (int c = 0; c < 5; c++)
+            if ((s = dalloc(ctx, &A.ddC[c], nm)) != NSEM_OK) return s;
+    }
     for (int v = 0; v < 5; v++) {
         const size_t n = (size_t)ctx->dev.n_int;
         if ((s = dalloc(ctx, &A.lam[v], n)) != NSEM_OK) return s;
@@ -835,7 +859,7 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
 }
 
 extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
@@ -856,7 +880,7 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
 }
 
 extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
     for (int v = 0; v < 5; v++)
@@ -878,7 +902,7 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
 
 extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
                                 double* const du_final[5], double* ms_tlm) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
     if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
@@ -946,7 +970,7 @@ extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const d
 
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
@@ -1111,7 +1135,7 @@ static nsem_status mixed_adjoint(nsem_ctx* ctx, const double* const lam_final[5]
 
 extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                     double* const lam0[5], double* ms_adj) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
     if (ctx->adj_form == 1) {

@@ -97,7 +97,21 @@ struct StageSmem {
     static constexpr int OFF_META = OFF_Q + QTAB;
     static_assert(OFF_P % 4 == 0 && OFF_FF4 % 4 == 0, "float4 regions must be 16-byte aligned");
     static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
+    /* persistent kernels: the next element's stage base, increment and
+     * background, staged by asynchronous copies while the current element
+     * computes */
+    static constexpr int OFF_STG = OFF_META + 4;
+    static constexpr size_t BYTES_P = sizeof(float) * (OFF_STG + 14 * NP);
 };
+
+/* 4-byte asynchronous copies global -> shared (no registers held while in
+ * flight) */
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 /* Tensor-core line sums (order 7, 8 nodes per direction).  The volume term
  * of direction d is, per conserved variable v and line l through the
@@ -138,7 +152,7 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
 #ifndef NSEM_MIXED_MB3
 #define NSEM_MIXED_MB3 7
 #endif
-template <int NX, int NY, int NZ, int STAGE, bool VISC>
+template <int NX, int NY, int NZ, int STAGE, bool VISC, bool PERSIST = false>
 constexpr int stage_min_blocks() {
     /* order 7 (512 threads, 64 KB of shared memory): three CTAs, two for the
      * stages that hold more live values (no spills) */
@@ -147,7 +161,7 @@ constexpr int stage_min_blocks() {
                           StageSmem<NX, NY, NZ>::BYTES);
     return min_blocks(VISC ? 6 : (STAGE == 1 || STAGE == 2) ? NSEM_MIXED_MB12 : NSEM_MIXED_MB3,
                       Geo<NX, NY, NZ>::BLOCK,
-                      StageSmem<NX, NY, NZ>::BYTES);
+                      PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
 }
 
 /* phase 2: flux through face node t of direction DIR, seen from the element */
@@ -219,8 +233,13 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
 }
 
 /* one kernel per stage (0: tendency only): the stage's own loads and update */
-template <int NX, int NY, int NZ, int STAGE, bool VISC, bool TC>
-__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (stage_min_blocks<NX, NY, NZ, STAGE, VISC>()))
+/* PERSIST: a grid of resident CTAs walks the elements (e, e + grid, ...);
+ * while one element computes, the next element's own stage base and
+ * increment stream into shared memory, so their load latency is hidden; the
+ * line-sum table is staged once per CTA. */
+template <int NX, int NY, int NZ, int STAGE, bool VISC, bool TC, bool PERSIST>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK,
+                                  (stage_min_blocks<NX, NY, NZ, STAGE, VISC, PERSIST>()))
 k_mixed_stage(StageArgs a) {
     static_assert(!TC || (NX == 8 && NY == 8 && NZ == 8), "tensor-core line sums: order 7");
     using G = Geo<NX, NY, NZ>;
@@ -238,28 +257,71 @@ k_mixed_stage(StageArgs a) {
     float* sMeta = smem + SM::OFF_META;
 
     const int t = threadIdx.x;
-    const int64_t e = blockIdx.x;
     constexpr bool has_din = STAGE >= 2;
+    float* sStg = smem + SM::OFF_STG;                             /* [14][NP] (PERSIST) */
+    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
+    auto prefetch = [&](int64_t en, int32_t lay) {
+        if (t < NP) {
+            const float* s = a.S + en * 5 * NP + t;
+#pragma unroll
+            for (int v = 0; v < 5; v++) cp_async4(sStg + v * NP + t, s + v * NP);
+            if constexpr (has_din) {
+                const float* d = a.Din + en * 5 * NP + t;
+#pragma unroll
+                for (int v = 0; v < 5; v++) cp_async4(sStg + (5 + v) * NP + t, d + v * NP);
+            }
+            const float* bg = a.bg + (int64_t)lay * 4 * NP + t;
+#pragma unroll
+            for (int c = 0; c < 4; c++) cp_async4(sStg + (10 + c) * NP + t, bg + c * NP);
+        }
+        cp_async_commit();
+    };
+    const int64_t e_step = gridDim.x;
+    auto element = [&](const int64_t e) {
+    int32_t lay_next = 0;
+    if constexpr (PERSIST) {
+        cp_async_wait_all();
+        __syncthreads();
+        /* the next element's background layer, needed when its copies start */
+        if (e + e_step < a.n_elem) lay_next = __ldg(a.layer + e + e_step);
+    }
 
     /* issue every global load first: own node, face neighbour, stage-3 FP64 */
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0};
     double u64[5];
     float gown[12];
     if (t < NP) {
-        const float* s = a.S + e * 5 * NP + t;
+        if constexpr (PERSIST) {
 #pragma unroll
-        for (int v = 0; v < 5; v++) own[v] = __ldg(s + v * NP);
-        if constexpr (has_din) {
-            const float* d = a.Din + e * 5 * NP + t;
+            for (int v = 0; v < 5; v++) own[v] = sStg[v * NP + t];
+            if constexpr (has_din) {
 #pragma unroll
-            for (int v = 0; v < 5; v++) {
-                din[v] = __ldg(d + v * NP);
-                own[v] = __fadd_rn(own[v], din[v]);
+                for (int v = 0; v < 5; v++) {
+                    din[v] = sStg[(5 + v) * NP + t];
+                    own[v] = __fadd_rn(own[v], din[v]);
+                }
+            }
+        } else {
+            const float* s = a.S + e * 5 * NP + t;
+#pragma unroll
+            for (int v = 0; v < 5; v++) own[v] = __ldg(s + v * NP);
+            if constexpr (has_din) {
+                const float* d = a.Din + e * 5 * NP + t;
+#pragma unroll
+                for (int v = 0; v < 5; v++) {
+                    din[v] = __ldg(d + v * NP);
+                    own[v] = __fadd_rn(own[v], din[v]);
+                }
             }
         }
-        const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t;
+        if constexpr (PERSIST) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
+            for (int c = 0; c < 4; c++) bgs[c] = sStg[(10 + c) * NP + t];
+        } else {
+            const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t;
+#pragma unroll
+            for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
+        }
         if constexpr (STAGE == 3) {
             const double* u = a.U + e * 5 * NP + t;
 #pragma unroll
@@ -302,7 +364,6 @@ k_mixed_stage(StageArgs a) {
             }
         }
     }
-    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
     if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
 
     /* phase 1: own node primitives and volume fluxes */
@@ -337,6 +398,10 @@ k_mixed_stage(StageArgs a) {
         }
     }
     __syncthreads();
+    if constexpr (PERSIST) {
+        /* the staging area is free: stream in the next element */
+        if (e + e_step < a.n_elem) prefetch(e + e_step, lay_next);
+    }
 
     /* phase 2: Rusanov flux on every face node */
     if (t < NFS) {
@@ -379,7 +444,7 @@ k_mixed_stage(StageArgs a) {
         }
         __syncthreads();
     }
-    if (t >= NP) return;
+    if (t < NP) {
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
     float L0, L1, L2, L3, L4;
     if constexpr (TC) {
@@ -469,7 +534,6 @@ k_mixed_stage(StageArgs a) {
         const int64_t n = e * NP + t;
 #pragma unroll
         for (int v = 0; v < 5; v++) a.L[v][n] = f2d(Lv[v]);
-        return;
     }
     const int64_t o = e * 5 * NP + t;
     const float dt = a.dt;
@@ -479,7 +543,7 @@ k_mixed_stage(StageArgs a) {
     } else if constexpr (STAGE == 2) {
 #pragma unroll
         for (int v = 0; v < 5; v++) a.Dout[o + v * NP] = 0.25f * fmaf(dt, Lv[v], din[v]);
-    } else {
+    } else if constexpr (STAGE == 3) {
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
@@ -491,6 +555,15 @@ k_mixed_stage(StageArgs a) {
             finite = finite && ((__double2hiint(un) & 0x7ff00000) != 0x7ff00000);
         }
         if (!finite) atomicOr(a.status, NSEM_STATUS_NONFINITE);
+    }
+    }  /* t < NP */
+    };  /* element */
+    if constexpr (PERSIST) {
+        prefetch(blockIdx.x, __ldg(a.layer + blockIdx.x));
+        for (int64_t e = blockIdx.x; e < a.n_elem; e += e_step) element(e);
+        cp_async_wait_all();
+    } else {
+        element(blockIdx.x);
     }
 }
 
@@ -743,42 +816,63 @@ __global__ void k_pert_to_host(const double* U, double* rho, double* mom, double
     }
 }
 
-template <int NX, int NY, int NZ, bool VISC, bool TC>
-void launch_stage_v(const StageArgs& a, int stage, cudaStream_t st) {
+/* launch configuration of the stage kernels: tensor-core line sums (order 7),
+ * persistent CTAs and their grid per stage (resident CTAs x SMs) */
+struct LaunchCfg {
+    bool visc, tc, persist;
+    int pgrid[4];
+};
+
+template <int NX, int NY, int NZ, bool VISC, bool TC, bool PERSIST>
+void launch_stage_v(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     using G = Geo<NX, NY, NZ>;
-    constexpr size_t SMEM = StageSmem<NX, NY, NZ>::BYTES;
-    const unsigned grid = (unsigned)a.n_elem;
+    constexpr size_t SMEM = PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES;
+    int64_t g = a.n_elem;
+    if (PERSIST && c.pgrid[stage] > 0 && c.pgrid[stage] < g) g = c.pgrid[stage];
+    const unsigned grid = (unsigned)g;
     switch (stage) {
-        case 0: k_mixed_stage<NX, NY, NZ, 0, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 1: k_mixed_stage<NX, NY, NZ, 1, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 2: k_mixed_stage<NX, NY, NZ, 2, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        default: k_mixed_stage<NX, NY, NZ, 3, VISC, TC><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 0: k_mixed_stage<NX, NY, NZ, 0, VISC, TC, PERSIST><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 1: k_mixed_stage<NX, NY, NZ, 1, VISC, TC, PERSIST><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 2: k_mixed_stage<NX, NY, NZ, 2, VISC, TC, PERSIST><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        default: k_mixed_stage<NX, NY, NZ, 3, VISC, TC, PERSIST><<<grid, G::BLOCK, SMEM, st>>>(a); break;
     }
 }
 
-/* the tensor-core line sums exist for order 7 only */
+/* the tensor-core line sums exist for order 7 only; persistent CTAs for the
+ * inviscid kernels of up to 256 threads (order 7's 64 KB of shared memory
+ * leaves no room for the staging area) */
 template <int NX, int NY, int NZ>
 constexpr bool tc_dims() {
     return NX == 8 && NY == 8 && NZ == 8;
 }
+template <int NX, int NY, int NZ>
+constexpr bool persist_dims() {
+    return Geo<NX, NY, NZ>::BLOCK <= 256;
+}
 
 template <int NX, int NY, int NZ, bool VISC>
-void launch_stage_tc(const StageArgs& a, int stage, cudaStream_t st, bool tc) {
+void launch_stage_tc(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     if constexpr (tc_dims<NX, NY, NZ>()) {
-        if (tc) {
-            launch_stage_v<NX, NY, NZ, VISC, true>(a, stage, st);
+        if (c.tc) {
+            launch_stage_v<NX, NY, NZ, VISC, true, false>(a, stage, st, c);
             return;
         }
     }
-    launch_stage_v<NX, NY, NZ, VISC, false>(a, stage, st);
+    if constexpr (!VISC && persist_dims<NX, NY, NZ>()) {
+        if (c.persist) {
+            launch_stage_v<NX, NY, NZ, false, false, true>(a, stage, st, c);
+            return;
+        }
+    }
+    launch_stage_v<NX, NY, NZ, VISC, false, false>(a, stage, st, c);
 }
 
 /* one stage; viscous runs first form the gradients of the stage state */
 template <int NX, int NY, int NZ>
-int launch_stage(const StageArgs& a, int stage, cudaStream_t st, bool visc, bool tc) {
+int launch_stage(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     using G = Geo<NX, NY, NZ>;
-    if (!visc) {
-        launch_stage_tc<NX, NY, NZ, false>(a, stage, st, tc);
+    if (!c.visc) {
+        launch_stage_tc<NX, NY, NZ, false>(a, stage, st, c);
         return (int)cudaGetLastError();
     }
     const unsigned grid = (unsigned)a.n_elem;
@@ -787,36 +881,62 @@ int launch_stage(const StageArgs& a, int stage, cudaStream_t st, bool visc, bool
     else k_mixed_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a);
     int e = (int)cudaGetLastError();
     if (e) return e;
-    launch_stage_tc<NX, NY, NZ, true>(a, stage, st, tc);
+    launch_stage_tc<NX, NY, NZ, true>(a, stage, st, c);
     return (int)cudaGetLastError();
 }
 
-template <int NX, int NY, int NZ>
-int prepare_stage() {
+template <int NX, int NY, int NZ, bool VISC, bool TC, bool PERSIST>
+int set_smem(int stage) {
+    constexpr int SMEM = (int)(PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
+    if (SMEM <= 48 * 1024) return 0;
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    constexpr int SMEM = (int)StageSmem<NX, NY, NZ>::BYTES;
+    switch (stage) {
+        case 0: return (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, VISC, TC, PERSIST>, at, SMEM);
+        case 1: return (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, VISC, TC, PERSIST>, at, SMEM);
+        case 2: return (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, VISC, TC, PERSIST>, at, SMEM);
+        default: return (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, VISC, TC, PERSIST>, at, SMEM);
+    }
+}
+
+/* resident CTAs of a persistent stage kernel on the whole GPU */
+template <int NX, int NY, int NZ, int STAGE>
+int persist_grid() {
+    int per_sm = 0, dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_mixed_stage<NX, NY, NZ, STAGE, false, false, true>, Geo<NX, NY, NZ>::BLOCK,
+            StageSmem<NX, NY, NZ>::BYTES_P) != cudaSuccess)
+        return 0;
+    return per_sm * sms;
+}
+
+template <int NX, int NY, int NZ>
+int prepare_stage(LaunchCfg* c) {
     int e = 0;
-    if (SMEM > 48 * 1024) {
-        e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true, false>, at, SMEM);
-        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true, false>, at, SMEM);
+    for (int st = 0; st < 4 && !e; st++) {
+        e = set_smem<NX, NY, NZ, false, false, false>(st);
+        if (!e) e = set_smem<NX, NY, NZ, true, false, false>(st);
         if constexpr (tc_dims<NX, NY, NZ>()) {
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, false, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, false, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, false, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, false, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 0, true, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 1, true, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 2, true, true>, at, SMEM);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage<NX, NY, NZ, 3, true, true>, at, SMEM);
+            if (!e) e = set_smem<NX, NY, NZ, false, true, false>(st);
+            if (!e) e = set_smem<NX, NY, NZ, true, true, false>(st);
+        }
+        if constexpr (persist_dims<NX, NY, NZ>()) {
+            if (!e) e = set_smem<NX, NY, NZ, false, false, true>(st);
         }
     }
+    if constexpr (persist_dims<NX, NY, NZ>()) {
+        c->pgrid[0] = persist_grid<NX, NY, NZ, 0>();
+        c->pgrid[1] = persist_grid<NX, NY, NZ, 1>();
+        c->pgrid[2] = persist_grid<NX, NY, NZ, 2>();
+        c->pgrid[3] = persist_grid<NX, NY, NZ, 3>();
+        if (!c->pgrid[0] || !c->pgrid[1] || !c->pgrid[2] || !c->pgrid[3]) c->persist = false;
+    } else {
+        c->persist = false;
+    }
     constexpr size_t gs = grad_smem<NX, NY, NZ>();
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
     if (!e && gs > 48 * 1024) {
         e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 1>, at, (int)gs);
         if (!e) e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 2>, at, (int)gs);
@@ -839,17 +959,17 @@ bool nsem_mixed_supported(int nx, int ny, int nz) {
 
 namespace {
 
-int prepare(int nx, int ny, int nz) {
-#define NSEM_PREP(A, B, C) if (nx == A && ny == B && nz == C) return prepare_stage<A, B, C>();
+int prepare(int nx, int ny, int nz, LaunchCfg* c) {
+#define NSEM_PREP(A, B, C) if (nx == A && ny == B && nz == C) return prepare_stage<A, B, C>(c);
     NSEM_MIXED_DIMS(NSEM_PREP)
 #undef NSEM_PREP
     return (int)cudaErrorNotSupported;
 }
 
 int dispatch_stage(int nx, int ny, int nz, const StageArgs& a, int stage, cudaStream_t st,
-                   bool visc, bool tc) {
+                   const LaunchCfg& c) {
 #define NSEM_DISP(A, B, C) \
-    if (nx == A && ny == B && nz == C) return launch_stage<A, B, C>(a, stage, st, visc, tc);
+    if (nx == A && ny == B && nz == C) return launch_stage<A, B, C>(a, stage, st, c);
     NSEM_MIXED_DIMS(NSEM_DISP)
 #undef NSEM_DISP
     return (int)cudaErrorNotSupported;
@@ -1047,9 +1167,20 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         err = "precision form: device allocation failed";
         return NSEM_NO_MEMORY;
     }
-    if (prepare(NX, NY, NZ) != 0) {
-        err = "precision form: cannot reserve the kernel's shared memory";
-        return NSEM_CUDA_ERROR;
+    /* persistent stage kernels only with NSEM_MIXED_PERSIST=1: measured on
+     * GB300 (32^3, N = 4) they are slower than one CTA per element -- the
+     * register cap of 8 resident CTAs makes the element loop spill, and with
+     * fewer CTAs the prefetch only breaks even */
+    {
+        const char* pers = std::getenv("NSEM_MIXED_PERSIST");
+        LaunchCfg c{};
+        c.persist = pers && std::string(pers) == "1";
+        if (prepare(NX, NY, NZ, &c) != 0) {
+            err = "precision form: cannot reserve the kernel's shared memory";
+            return NSEM_CUDA_ERROR;
+        }
+        mb->persist = c.persist;
+        for (int q = 0; q < 4; q++) mb->pgrid[q] = c.pgrid[q];
     }
     /* order 7: line sums on the FP32 pipes (measured faster than the
      * tensor-core variant on GB300); NSEM_MIXED_LINES=tensor selects the
@@ -1102,7 +1233,12 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
 }
 
 int launch_args(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
-    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, mb->visc, mb->tc);
+    LaunchCfg c{};
+    c.visc = mb->visc;
+    c.tc = mb->tc;
+    c.persist = mb->persist;
+    for (int q = 0; q < 4; q++) c.pgrid[q] = mb->pgrid[q];
+    return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, c);
 }
 
 }  // namespace

@@ -34,6 +34,8 @@ struct NsemMixedBuf {
     float* G = nullptr;           /* viscous runs: [n_elem][12][NP] gradients of the stage state */
     bool visc = false;            /* artificial viscosity (diffusion YES)   */
     bool tc = false;              /* order-7 line sums on the tensor cores  */
+    bool persist = false;         /* persistent stage kernels               */
+    int pgrid[4] = {0, 0, 0, 0};  /* their grids (resident CTAs), per stage */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */
