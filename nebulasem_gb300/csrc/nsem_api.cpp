@@ -1023,6 +1023,8 @@ static nsem_status mixed_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckp
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
     if (ctx->mbuf.visc)
         return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
+    if (ctx->mbuf.gen)
+        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     nsem_status s = ensure_rep(ctx, 1);
     if (s != NSEM_OK) return s;
     ctx->adj_form = -1;
@@ -1075,6 +1077,8 @@ extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const d
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
     if (ctx->mbuf.visc)
         return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
+    if (ctx->mbuf.gen)
+        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     nsem_status s = ensure_rep(ctx, 1);
     if (s != NSEM_OK) return s;

@@ -35,7 +35,9 @@
  * element the metric diagonal and the six neighbours, per z-layer the
  * background.  Discretisation identical to the plain form (same Rusanov
  * speed and jump -- normal momentum component only, field.h:2928-2943 --,
- * same symmetry ghost velocity, same weak form).
+ * same symmetry ghost velocity, same weak form).  Inclined and curved
+ * elements (inviscid runs) take k_mixed_stage_gen: the full metric Jinv cV
+ * per node, contravariant volume fluxes and per-node face normals.
  *
  * Artificial viscosity (diffusion YES, euler.cpp:189-190, 232, 250): a
  * gradient kernel per stage forms the strong-form DG gradients of U and
@@ -75,6 +77,8 @@ struct StageArgs {
     const float* G;            /* viscous runs: [e][12][NP] gradients      */
     float* Gout;               /* gradient kernel output                   */
     const float* bg;           /* [layers][4][NP]                          */
+    const float* Jg;           /* general geometry: [e][10][NP] Jinv cV (9), 1/cV */
+    const float* Fn;           /* general geometry: [e][3][NFS] outward weighted normals */
     int64_t n_elem;
     float dt, gamma, gR, g[3];
     float nu, nu_pr, T0;
@@ -568,6 +572,268 @@ k_mixed_stage(StageArgs a) {
 }
 
 
+/* ------------------------------------------------------------------------
+ * General geometry (inclined, curved elements; inviscid): the metric is a
+ * full 3x3 per node and the faces' normals are per face node.  The volume term
+ * in the weak form of the plain form (field.h:3440-3464): per node the
+ * contravariant fluxes G_d = sum_c F_c (Jinv cV)[c][d] -- mass M.Jcol_d,
+ * momentum m_r (u.Jcol_d) + p' Jcol_d[r], theta (M.Jcol_d) theta -- and
+ *   L_a = (1/cV_a) [sum_d sum_m l_a'(x_m) G_d(m) - sum_faces F_out] + rho' g,
+ * F_out = (F_s + F_o).fN / 2 - lam (|fN| drho', en (dm.fN), |fN| dTheta'),
+ * fN the face node's weighted normal pointing out of the element (the
+ * reference's Rusanov flux, field.h:2928-2943, with the jump of the normal
+ * momentum).  Both elements of a face evaluate it with fN and -fN: the
+ * results are exact negatives, the face conserves exactly.
+ * ------------------------------------------------------------------------ */
+template <int NX, int NY, int NZ>
+struct GenSmem {
+    using G = Geo<NX, NY, NZ>;
+    static constexpr int NP = G::NP, NFS = G::NFS;
+    /* floats: contravariant fluxes G4[3][NP] (x4) + G1[3][NP]; own values
+     * P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS]; line table */
+    static constexpr int OFF_G1 = 12 * NP;
+    static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
+    static constexpr int OFF_FF4 = OFF_P + 16 * NP;
+    static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
+    static constexpr int OFF_Q = OFF_FF1 + NFS;
+    static constexpr size_t BYTES = sizeof(float) * (OFF_Q + QTAB);
+};
+
+/* normal flux F(x).fN of one side */
+__device__ __forceinline__ void normal_flux(const float* m, const float* u, float pp, float th,
+                                            const float* fN, float4& f4, float& f1) {
+    const float mn = __fmaf_rn(m[0], fN[0], __fmaf_rn(m[1], fN[1], __fmul_rn(m[2], fN[2])));
+    const float un = __fmaf_rn(u[0], fN[0], __fmaf_rn(u[1], fN[1], __fmul_rn(u[2], fN[2])));
+    f4.x = mn;
+    f4.y = __fmaf_rn(m[0], un, __fmul_rn(pp, fN[0]));
+    f4.z = __fmaf_rn(m[1], un, __fmul_rn(pp, fN[1]));
+    f4.w = __fmaf_rn(m[2], un, __fmul_rn(pp, fN[2]));
+    f1 = __fmul_rn(mn, th);
+}
+
+template <int NX, int NY, int NZ, int STAGE>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK,
+                                  (min_blocks(NX == 8 ? 2 : 6, Geo<NX, NY, NZ>::BLOCK,
+                                              GenSmem<NX, NY, NZ>::BYTES)))
+k_mixed_stage_gen(StageArgs a) {
+    using G = Geo<NX, NY, NZ>;
+    using SM = GenSmem<NX, NY, NZ>;
+    constexpr int NP = G::NP;
+    constexpr int NFS = G::NFS;
+    extern __shared__ float4 gen4[];
+    float* smem = reinterpret_cast<float*>(gen4);
+    float4* sG4 = gen4;
+    float* sG1 = smem + SM::OFF_G1;
+    float4* sP = reinterpret_cast<float4*>(smem + SM::OFF_P);
+    float4* sFF4 = reinterpret_cast<float4*>(smem + SM::OFF_FF4);
+    float* sFF1 = smem + SM::OFF_FF1;
+    float* sQ = smem + SM::OFF_Q;
+    const int t = threadIdx.x;
+    const int64_t e = blockIdx.x;
+    constexpr bool has_din = STAGE >= 2;
+    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
+
+    float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0}, jin[9], icv = 0.0f;
+    double u64[5];
+    if (t < NP) {
+        const float* sp = a.S + e * 5 * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) own[v] = __ldg(sp + v * NP);
+        if constexpr (has_din) {
+            const float* d = a.Din + e * 5 * NP + t;
+#pragma unroll
+            for (int v = 0; v < 5; v++) {
+                din[v] = __ldg(d + v * NP);
+                own[v] = __fadd_rn(own[v], din[v]);
+            }
+        }
+        const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
+        const float* jg = a.Jg + e * 10 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
+        icv = __ldg(jg + 9 * NP);
+        if constexpr (STAGE == 3) {
+            const double* u = a.U + e * 5 * NP + t;
+#pragma unroll
+            for (int v = 0; v < 5; v++) u64[v] = __ldg(u + v * NP);
+        }
+    }
+    FaceSlot fs{};
+    int32_t nb = -1;
+    float oth[5], bgo[4], fno[3] = {0, 0, 0};
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+#pragma unroll
+        for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);
+        if (nb >= 0) {
+            const float* sp = a.S + (int64_t)nb * 5 * NP + fs.lo;
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(sp + v * NP);
+            if constexpr (has_din) {
+                const float* d = a.Din + (int64_t)nb * 5 * NP + fs.lo;
+#pragma unroll
+                for (int v = 0; v < 5; v++) oth[v] = __fadd_rn(oth[v], __ldg(d + v * NP));
+            }
+            const float* bg = a.bg + (int64_t)__ldg(a.layer + nb) * 4 * NP + fs.lo;
+#pragma unroll
+            for (int c = 0; c < 4; c++) bgo[c] = __ldg(bg + c * NP);
+        }
+    }
+
+    /* phase 1: primitives and contravariant fluxes */
+    if (t < NP) {
+        const Pt p = pointwise(own, bgs, a.eos, a.gamma, a.gR);
+        sP[t] = make_float4(own[0], own[1], own[2], own[3]);
+        sP[NP + t] = make_float4(own[4], p.rho, p.umag, p.c);
+        sP[2 * NP + t] = make_float4(p.u[0], p.u[1], p.u[2], p.pp);
+        sP[3 * NP + t] = make_float4(p.th, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (d == 1 && !G::HAS_Y) continue;
+            const float j0 = jin[tidx(0, d)], j1 = jin[tidx(1, d)], j2 = jin[tidx(2, d)];
+            const float Mt = fmaf(own[1], j0, fmaf(own[2], j1, own[3] * j2));
+            const float ut = fmaf(p.u[0], j0, fmaf(p.u[1], j1, p.u[2] * j2));
+            sG4[d * NP + t] = make_float4(Mt, fmaf(own[1], ut, p.pp * j0), fmaf(own[2], ut, p.pp * j1),
+                                          fmaf(own[3], ut, p.pp * j2));
+            sG1[d * NP + t] = Mt * p.th;
+        }
+    }
+    __syncthreads();
+
+    /* phase 2: Rusanov flux through every face node, dotted with its normal */
+    if (t < NFS) {
+        const float4 P0 = sP[fs.la], P1 = sP[NP + fs.la], P2 = sP[2 * NP + fs.la];
+        const float th_s = sP[3 * NP + fs.la].x;
+        const float ms[3] = {P0.y, P0.z, P0.w}, us[3] = {P2.x, P2.y, P2.z};
+        const float nrm = __fsqrt_rn(__fmaf_rn(fno[0], fno[0], __fmaf_rn(fno[1], fno[1], __fmul_rn(fno[2], fno[2]))));
+        const float inrm = nrm > 0.0f ? 1.0f / nrm : 0.0f;
+        const float en[3] = {__fmul_rn(fno[0], inrm), __fmul_rn(fno[1], inrm), __fmul_rn(fno[2], inrm)};
+        float4 o4;
+        float o1;
+        if (nb >= 0) {
+            const Pt q = pointwise(oth, bgo, a.eos, a.gamma, a.gR);
+            float4 A4, B4;
+            float A1, B1;
+            normal_flux(ms, us, P2.w, th_s, fno, A4, A1);
+            normal_flux(oth + 1, q.u, q.pp, q.th, fno, B4, B1);
+            const float lam = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(P1.z, q.umag), __fadd_rn(P1.w, q.c)));
+            const float dm0 = __fsub_rn(oth[1], ms[0]), dm1 = __fsub_rn(oth[2], ms[1]),
+                        dm2 = __fsub_rn(oth[3], ms[2]);
+            const float dmn = __fmaf_rn(dm0, fno[0], __fmaf_rn(dm1, fno[1], __fmul_rn(dm2, fno[2])));
+            const float jr = __fmul_rn(nrm, __fsub_rn(oth[0], P0.x));
+            const float jt = __fmul_rn(nrm, __fsub_rn(oth[4], P1.x));
+            o4.x = __fmaf_rn(-lam, jr, __fmul_rn(0.5f, __fadd_rn(A4.x, B4.x)));
+            o4.y = __fmaf_rn(-lam, __fmul_rn(en[0], dmn), __fmul_rn(0.5f, __fadd_rn(A4.y, B4.y)));
+            o4.z = __fmaf_rn(-lam, __fmul_rn(en[1], dmn), __fmul_rn(0.5f, __fadd_rn(A4.z, B4.z)));
+            o4.w = __fmaf_rn(-lam, __fmul_rn(en[2], dmn), __fmul_rn(0.5f, __fadd_rn(A4.w, B4.w)));
+            o1 = __fmaf_rn(-lam, jt, __fmul_rn(0.5f, __fadd_rn(A1, B1)));
+        } else {
+            /* wall ghost (SYMMETRY velocity, NEUMANN rho, theta, p): the ghost's
+             * normal flux is p' fN, the jump term lam en (m.fN) */
+            const float un = __fmaf_rn(us[0], en[0], __fmaf_rn(us[1], en[1], __fmul_rn(us[2], en[2])));
+            const float r0 = __fmaf_rn(-un, en[0], us[0]), r1 = __fmaf_rn(-un, en[1], us[1]),
+                        r2 = __fmaf_rn(-un, en[2], us[2]);
+            const float mr = safe_sqrt(__fmaf_rn(r0, r0, __fmaf_rn(r1, r1, __fmul_rn(r2, r2))));
+            const float um_g = mr > 1e-7f ? P1.z : mr;
+            const float lam = __fmul_rn(0.5f, __fadd_rn(um_g, P1.w));
+            const float mn = __fmaf_rn(ms[0], fno[0], __fmaf_rn(ms[1], fno[1], __fmul_rn(ms[2], fno[2])));
+            o4.x = 0.0f;
+            o4.y = __fmaf_rn(lam, __fmul_rn(en[0], mn), __fmul_rn(P2.w, fno[0]));
+            o4.z = __fmaf_rn(lam, __fmul_rn(en[1], mn), __fmul_rn(P2.w, fno[1]));
+            o4.w = __fmaf_rn(lam, __fmul_rn(en[2], mn), __fmul_rn(P2.w, fno[2]));
+            o1 = 0.0f;
+        }
+        sFF4[t] = o4;
+        sFF1[t] = o1;
+    }
+    __syncthreads();
+
+    /* phase 3: line sums l_a'(x_m) G_d(m), lift, 1/cV, buoyancy, update */
+    if (t >= NP) return;
+    const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+    float4 acc = make_float4(0, 0, 0, 0);
+    float acc1 = 0.0f;
+    {
+        const float* q = sQ + i * QS;
+#pragma unroll
+        for (int m = 0; m < NX; m++) {
+            const int b = (m * NY + j) * NZ + k;
+            const float4 f = sG4[b];
+            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
+            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
+            acc1 = fmaf(q[m], sG1[b], acc1);
+        }
+    }
+    if constexpr (G::HAS_Y) {
+        const float* q = sQ + MAXN * QS + j * QS;
+#pragma unroll
+        for (int m = 0; m < NY; m++) {
+            const int b = (i * NY + m) * NZ + k;
+            const float4 f = sG4[NP + b];
+            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
+            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
+            acc1 = fmaf(q[m], sG1[NP + b], acc1);
+        }
+    }
+    {
+        const float* q = sQ + 2 * MAXN * QS + k * QS;
+#pragma unroll
+        for (int m = 0; m < NZ; m++) {
+            const int b = (i * NY + j) * NZ + m;
+            const float4 f = sG4[2 * NP + b];
+            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
+            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
+            acc1 = fmaf(q[m], sG1[2 * NP + b], acc1);
+        }
+    }
+    auto lift = [&](int slot) {
+        const float4 f = sFF4[slot];
+        acc.x -= f.x; acc.y -= f.y; acc.z -= f.z; acc.w -= f.w; acc1 -= sFF1[slot];
+    };
+    {
+        const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
+        if (sx >= 0) lift(sx);
+        if constexpr (G::HAS_Y) {
+            const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
+            if (sy >= 0) lift(sy);
+        }
+        const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
+        if (sz >= 0) lift(sz);
+    }
+    const float rp = own[0];
+    const float Lv[5] = {icv * acc.x, fmaf(rp, a.g[0], icv * acc.y), fmaf(rp, a.g[1], icv * acc.z),
+                         fmaf(rp, a.g[2], icv * acc.w), icv * acc1};
+    if constexpr (STAGE == 0) {
+        const int64_t n = e * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.L[v][n] = f2d(Lv[v]);
+        return;
+    }
+    const int64_t o = e * 5 * NP + t;
+    const float dt = a.dt;
+    if constexpr (STAGE == 1) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.Dout[o + v * NP] = dt * Lv[v];
+    } else if constexpr (STAGE == 2) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.Dout[o + v * NP] = 0.25f * fmaf(dt, Lv[v], din[v]);
+    } else {
+        bool finite = true;
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], din[v]);
+            const double un = u64[v] + f2d(D);
+            a.Unew[o + v * NP] = un;
+            a.Snew[o + v * NP] = d2f_rn(un);
+            finite = finite && ((__double2hiint(un) & 0x7ff00000) != 0x7ff00000);
+        }
+        if (!finite) atomicOr(a.status, NSEM_STATUS_NONFINITE);
+    }
+}
+
 /* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
  * field.h:3327-3360) for the viscous fluxes: per node
  *   d_r q = J_r sum_m D_r[a_r][m] q_m  +  (J_r / w_end) (cds(q) - q)  on the
@@ -819,7 +1085,7 @@ __global__ void k_pert_to_host(const double* U, double* rho, double* mom, double
 /* launch configuration of the stage kernels: tensor-core line sums (order 7),
  * persistent CTAs and their grid per stage (resident CTAs x SMs) */
 struct LaunchCfg {
-    bool visc, tc, persist;
+    bool visc, tc, persist, gen;
     int pgrid[4];
 };
 
@@ -871,6 +1137,18 @@ void launch_stage_tc(const StageArgs& a, int stage, cudaStream_t st, const Launc
 template <int NX, int NY, int NZ>
 int launch_stage(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     using G = Geo<NX, NY, NZ>;
+    if (c.gen) {
+        /* general geometry (inviscid) */
+        constexpr size_t SMEM = GenSmem<NX, NY, NZ>::BYTES;
+        const unsigned grid = (unsigned)a.n_elem;
+        switch (stage) {
+            case 0: k_mixed_stage_gen<NX, NY, NZ, 0><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            case 1: k_mixed_stage_gen<NX, NY, NZ, 1><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            case 2: k_mixed_stage_gen<NX, NY, NZ, 2><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            default: k_mixed_stage_gen<NX, NY, NZ, 3><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        }
+        return (int)cudaGetLastError();
+    }
     if (!c.visc) {
         launch_stage_tc<NX, NY, NZ, false>(a, stage, st, c);
         return (int)cudaGetLastError();
@@ -934,6 +1212,16 @@ int prepare_stage(LaunchCfg* c) {
         if (!c->pgrid[0] || !c->pgrid[1] || !c->pgrid[2] || !c->pgrid[3]) c->persist = false;
     } else {
         c->persist = false;
+    }
+    {
+        constexpr int GS = (int)GenSmem<NX, NY, NZ>::BYTES;
+        const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (!e && GS > 48 * 1024) {
+            e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 0>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 1>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 2>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 3>, at, GS);
+        }
     }
     constexpr size_t gs = grad_smem<NX, NY, NZ>();
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -999,23 +1287,43 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
     const int64_t n_all = (int64_t)m->n_cells * NP;
     const int npd[3] = {NX, NY, NZ};
 
-    /* per-element diagonal metric; reject non-affine or rotated elements */
+    /* per-element diagonal metric of axis-aligned affine elements; any other
+     * element (inclined, curved) selects the general-geometry kernels */
     std::vector<float> J(3 * ne);
-    for (int64_t e = 0; e < ne; e++) {
+    bool gen = false;
+    for (int64_t e = 0; e < ne && !gen; e++) {
         const double* J0 = m->Jinv + 9 * (e * NP);
         const double diag0[3] = {J0[0], J0[1], J0[2]};
-        for (int64_t a = 0; a < NP; a++) {
+        const double scale = std::fabs(diag0[0]) + std::fabs(diag0[1]) + std::fabs(diag0[2]);
+        for (int64_t a = 0; a < NP && !gen; a++) {
             const double* Ja = m->Jinv + 9 * (e * NP + a);
             for (int c = 0; c < 9; c++) {
                 const double ref = (c < 3) ? diag0[c] : 0.0;
-                const double scale = std::fabs(diag0[0]) + std::fabs(diag0[1]) + std::fabs(diag0[2]);
-                if (std::fabs(Ja[c] - ref) > 1e-9 * scale) {
-                    err = "precision form needs axis-aligned affine elements";
-                    return NSEM_UNSUPPORTED;
-                }
+                if (std::fabs(Ja[c] - ref) > 1e-9 * scale) gen = true;
             }
         }
         for (int d = 0; d < 3; d++) J[d * ne + e] = (float)diag0[d];
+    }
+    if (gen && dev.nu != 0.0) {
+        err = "precision form on inclined or curved elements is inviscid";
+        return NSEM_UNSUPPORTED;
+    }
+    /* general geometry: Jinv cV and 1/cV per node, outward weighted normals
+     * per element face slot */
+    const int nfx = NY * NZ, nfy = NX * NZ, nfz = NX * NY;
+    const int off_y = 2 * nfx, off_z = 2 * nfx + (NY > 1 ? 2 * nfy : 0);
+    const int nfs = off_z + 2 * nfz;
+    std::vector<float> Jg, Fn;
+    if (gen) {
+        Jg.assign((size_t)ne * 10 * NP, 0.0f);
+        Fn.assign((size_t)ne * 3 * nfs, 0.0f);
+        for (int64_t e = 0; e < ne; e++)
+            for (int64_t a = 0; a < NP; a++) {
+                const int64_t i = e * NP + a;
+                for (int c = 0; c < 9; c++)
+                    Jg[(e * 10 + c) * NP + a] = (float)(m->Jinv[9 * i + c] * m->cV[i]);
+                Jg[(e * 10 + 9) * NP + a] = (float)(1.0 / m->cV[i]);
+            }
     }
 
     /* neighbours from the face slots: element face lists + FO/FN */
@@ -1035,16 +1343,29 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             const bool own = (o / NP) == (uint64_t)e;
             const int64_t mine = own ? o : n;
             const int64_t other = own ? n : o;
-            const int la = (int)local(mine);
-            const int ia = la / (NY * NZ), ja = (la / NZ) % NY, ka = la % NZ;
-            /* which face of e: the coordinate that is at an end on this face */
-            const double* nv = m->fN + 3 * k;
-            int dir = 0;
-            const double ax = std::fabs(nv[0]), ay = std::fabs(nv[1]), az = std::fabs(nv[2]);
-            if (ay > ax && ay > az) dir = 1;
-            else if (az > ax && az > ay) dir = 2;
-            const int cidx[3] = {ia, ja, ka};
-            const int side = (cidx[dir] == npd[dir] - 1 && npd[dir] > 1) ? 1 : 0;
+            (void)mine;
+            /* which face of e: the local index direction held at one end by
+             * every node of the face */
+            int dir = -1, side = 0;
+            for (int d = 0; d < 3 && dir < 0; d++) {
+                if (npd[d] == 1) continue;
+                for (int sd = 0; sd < 2 && dir < 0; sd++) {
+                    const int want = sd ? npd[d] - 1 : 0;
+                    bool all = true;
+                    for (int q = 0; q < m->npf && all; q++) {
+                        const int64_t kk = fid * m->npf + q;
+                        if (m->FO[kk] >= (uint64_t)n_all || m->FN[kk] >= (uint64_t)n_all) continue;
+                        const int l2 = (int)local(own ? m->FO[kk] : m->FN[kk]);
+                        const int c2[3] = {l2 / (NY * NZ), (l2 / NZ) % NY, l2 % NZ};
+                        all = c2[d] == want;
+                    }
+                    if (all) { dir = d; side = sd; }
+                }
+            }
+            if (dir < 0) {
+                err = "precision form needs faces on the element's local index planes";
+                return NSEM_UNSUPPORTED;
+            }
             const int32_t nb = (other < (int64_t)n_int) ? (int32_t)(other / NP) : -1;
             nbr[(2 * dir + side) * ne + e] = nb;
             /* verify the structured slot mapping on every used slot */
@@ -1057,8 +1378,16 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                 const int l2 = (int)local(mine2);
                 int c2[3] = {l2 / (NY * NZ), (l2 / NZ) % NY, l2 % NZ};
                 if (c2[dir] != (side ? npd[dir] - 1 : 0)) {
-                    err = "precision form needs axis-aligned faces";
+                    err = "precision form needs faces on the element's local index planes";
                     return NSEM_UNSUPPORTED;
+                }
+                if (gen) {
+                    const int t = dir == 0 ? side * nfx + c2[1] * NZ + c2[2]
+                                : dir == 1 ? off_y + side * nfy + c2[0] * NZ + c2[2]
+                                           : off_z + side * nfz + c2[0] * NY + c2[1];
+                    const double sg = own ? 1.0 : -1.0;
+                    for (int c = 0; c < 3; c++)
+                        Fn[(e * 3 + c) * nfs + t] = (float)(sg * m->fN[3 * kk + c]);
                 }
                 if (nb >= 0) {
                     if (other2 / NP != nb) { err = "face with two neighbours"; return NSEM_UNSUPPORTED; }
@@ -1130,7 +1459,10 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         const std::vector<double>& w = wdir[d];
         for (int aa = 0; aa < n; aa++)
             for (int mm = 0; mm < n; mm++) {
-                qtab[d * MAXN * QS + aa * QS + mm] = (float)(m->dpsi[d][mm * n + aa] * w[mm] / w[aa]);
+                /* general geometry: the plain weak-form table l_a'(x_m), the
+                 * weights sit in Jinv cV and 1/cV */
+                qtab[d * MAXN * QS + aa * QS + mm] =
+                    gen ? (float)m->dpsi[d][mm * n + aa] : (float)(m->dpsi[d][mm * n + aa] * w[mm] / w[aa]);
                 /* D_d[a][m] = l_m'(x_a) = dpsi[a * n + m] for the gradient kernel */
                 dtab[d * MAXN * QS + aa * QS + mm] = (float)m->dpsi[d][aa * n + mm];
             }
@@ -1145,10 +1477,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         return cudaMemcpy(*ptr, vec.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
     };
     if (!up(&mb->nbr, nbr) || !up(&mb->J, J) || !up(&mb->layer, layer) || !up(&mb->bg, bg) ||
-        !up(&mb->Qg, qtab) || !up(&mb->Dg, dtab)) {
+        !up(&mb->Qg, qtab) || !up(&mb->Dg, dtab) || (gen && (!up(&mb->Jg, Jg) || !up(&mb->Fn, Fn)))) {
         err = "precision form: device allocation failed";
         return NSEM_NO_MEMORY;
     }
+    mb->gen = gen;
     auto dal = [&](auto** p, size_t bytes) -> bool {
         if (cudaMalloc((void**)p, bytes) != cudaSuccess) return false;
         allocs->push_back((void*)*p);
@@ -1214,6 +1547,8 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
     a.nu_pr = mb->nu_pr;
     a.T0 = (float)dev->T0;
     a.bg = mb->bg;
+    a.Jg = mb->Jg;
+    a.Fn = mb->Fn;
     a.n_elem = mb->n_elem;
     a.dt = (float)dt;
     a.gamma = (float)dev->gamma;
@@ -1237,6 +1572,7 @@ int launch_args(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStrea
     c.visc = mb->visc;
     c.tc = mb->tc;
     c.persist = mb->persist;
+    c.gen = mb->gen;
     for (int q = 0; q < 4; q++) c.pgrid[q] = mb->pgrid[q];
     return dispatch_stage(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, c);
 }

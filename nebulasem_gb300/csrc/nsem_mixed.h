@@ -35,6 +35,9 @@ struct NsemMixedBuf {
     bool visc = false;            /* artificial viscosity (diffusion YES)   */
     bool tc = false;              /* order-7 line sums on the tensor cores  */
     bool persist = false;         /* persistent stage kernels               */
+    bool gen = false;             /* general geometry (inclined, curved)    */
+    float* Jg = nullptr;          /* gen: [n_elem][10][NP] Jinv cV, 1/cV    */
+    float* Fn = nullptr;          /* gen: [n_elem][3][NFS] outward fN       */
     int pgrid[4] = {0, 0, 0, 0};  /* their grids (resident CTAs), per stage */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */

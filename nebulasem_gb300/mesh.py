@@ -23,6 +23,7 @@ import math
 import numpy as np
 
 XX, YY, ZZ, XY, YZ, XZ, YX, ZY, ZX = range(9)
+TIDX = ((XX, XY, XZ), (YX, YY, YZ), (ZX, ZY, ZZ))   # tensor component (row, column)
 
 
 def legendre(p, x):
@@ -97,8 +98,16 @@ def lagrange_tables(xg):
     return psi, dpsi
 
 
-def box_mesh(n, order, length, dim=3):
-    """Uniform box of n = (nx, ny, nz) elements of order N; dim=2 collapses y."""
+def rotation_y(deg):
+    """Rotation matrix about the y axis by deg degrees (x towards -z)."""
+    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
+    return np.array([[c, 0.0, s], [0.0, 1.0, 0.0], [-s, 0.0, c]])
+
+
+def box_mesh(n, order, length, dim=3, tilt=0.0):
+    """Uniform box of n = (nx, ny, nz) elements of order N; dim=2 collapses y.
+    tilt: the box rotated by that many degrees about the y axis through its
+    centre (inclined elements: full metric Jinv = R diag(2/h), normals R fN)."""
     nx, ny, nz = n
     if dim == 2:
         ny = 1
@@ -238,6 +247,16 @@ def box_mesh(n, order, length, dim=3):
     idx1 = (idx0 + 1).astype(np.uint32)
     idx1[:ne] = idx0[:ne] + nfe
 
+    if tilt:
+        R = rotation_y(tilt)
+        c0 = np.asarray(length, dtype=np.float64) / 2
+        cC = (cC - c0) @ R.T + c0
+        Jd = J[[XX, YY, ZZ]]
+        for r in range(3):
+            for c in range(3):
+                Jinv[:n_int, TIDX[r][c]] = R[r, c] * Jd[c]
+        fN = fN @ R.T
+
     meta = np.zeros(16, dtype=np.uint32)
     meta[:11] = [NPX, NPY, NPZ, NP, NPF, ne, n_cells, n_int, n_all, nf, len(all_faces)]
     out = {
@@ -296,13 +315,24 @@ WORKLOADS = {
                            amp=0.5, center=(1000.0, 1000.0, 600.0), radius=(400.0,) * 3),
     "bubble3d_8_n4": dict(n=(8, 8, 8), order=4, length=(2000.0,) * 3, dim=3,
                           amp=0.5, center=(1000.0, 1000.0, 600.0), radius=(400.0,) * 3),
+    # the 32^3 and 16^3 boxes tilted by 30 degrees about y (inclined elements:
+    # the precision form's general-geometry kernels), bubble tilted with them
+    "bubble3d_32_n4_tilt30": dict(n=(32, 32, 32), order=4, length=(2000.0,) * 3, dim=3, tilt=30.0,
+                                  amp=0.5, center=(1000.0, 1000.0, 600.0), radius=(400.0,) * 3),
+    "bubble3d_16_n4_tilt30": dict(n=(16, 16, 16), order=4, length=(2000.0,) * 3, dim=3, tilt=30.0,
+                                  amp=0.5, center=(1000.0, 1000.0, 600.0), radius=(400.0,) * 3),
 }
 
 
 def workload(name):
     """Mesh dict (with background fields) and initial state of a named workload."""
     w = WORKLOADS[name]
-    m = box_mesh(w["n"], w["order"], w["length"], dim=w["dim"])
-    u, p_ref, rho_ref, gh = bubble_state(m, w["amp"], w["center"], w["radius"])
+    tilt = w.get("tilt", 0.0)
+    m = box_mesh(w["n"], w["order"], w["length"], dim=w["dim"], tilt=tilt)
+    center = np.asarray(w["center"], dtype=np.float64)
+    if tilt:
+        c0 = np.asarray(w["length"], dtype=np.float64) / 2
+        center = rotation_y(tilt) @ (center - c0) + c0
+    u, p_ref, rho_ref, gh = bubble_state(m, w["amp"], center, w["radius"])
     m["p_ref"], m["rho_ref"], m["gh"] = p_ref, rho_ref, gh
     return m, u

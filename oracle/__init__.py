@@ -165,6 +165,8 @@ class OracleMesh:
         self.gh = f64("gh") if "gh" in g else None
 
     def _vec(self, arrays):
+        """Contiguous FP64 copies (where needed) and their pointers; callers
+        keep the returned arrays alive until the C call has returned."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrays]
         for a in arrs:
             assert a.shape == (self.n_int,)
@@ -172,11 +174,12 @@ class OracleMesh:
         return arrs, ptrs
 
     def tendency(self, u, return_p=False):
-        _, up = self._vec(u)
+        ua, up = self._vec(u)
         L = [np.empty(self.n_int) for _ in range(5)]
         _, lp = self._vec(L)
         p = np.empty(self.n_all)
         lib().nsem_oracle_tendency(ctypes.byref(self.struct), up, lp, _ptr(p))
+        del ua
         return (L, p) if return_p else L
 
     def ssprk3(self, u, dt, nsteps):
@@ -186,13 +189,14 @@ class OracleMesh:
 
     def jvp(self, u, du):
         """Tendency L(u) and its directional derivative J_L(u) du (dual numbers)."""
-        _, up = self._vec(u)
-        _, dp = self._vec(du)
+        ua, up = self._vec(u)
+        da, dp = self._vec(du)
         L = [np.empty(self.n_int) for _ in range(5)]
         Ld = [np.empty(self.n_int) for _ in range(5)]
         _, lp = self._vec(L)
         _, ldp = self._vec(Ld)
         lib().nsem_oracle_jvp(ctypes.byref(self.struct), up, dp, lp, ldp)
+        del ua, da
         return L, Ld
 
     def tlm_ssprk3(self, u, du, dt, nsteps):
@@ -250,10 +254,11 @@ class OracleMesh:
         return t
 
     def diagnostics(self, u):
-        _, up = self._vec(u)
+        ua, up = self._vec(u)
         out = np.zeros(3)
         lib().nsem_oracle_diagnostics(ctypes.byref(self.struct), up, _ptr(self.gh),
                                       self.cv_heat, _ptr(out))
+        del ua
         return out
 
 

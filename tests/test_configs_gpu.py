@@ -20,6 +20,8 @@ Time steps: the 32^3 mesh (h = 62.5 m) diverges at dt = 0.01 s and runs at
 0.0075 s; the 48^3 mesh (h = 41.7 m) at 0.005 s; 16^3 at N = 7 is stable at
 its stated 0.005 s.
 """
+import json
+
 import numpy as np
 import pytest
 
@@ -61,12 +63,18 @@ def run_both(name):
 def test_precision_form_vs_fp64_full_size(name):
     _, _, out = run_both(name)
     ref, got = out["fp64"], out["mixed"]
+    th_ref = ref[4] / ref[0] - 300.0
+    th_got = got[4] / got[0] - 300.0
+    # the measured figures (shown with pytest -s)
+    l2 = {v: rel_l2(a, b) for a, b, v in zip(got, ref, VARS)}
+    l2["theta'"] = rel_l2(th_got, th_ref)
+    print(json.dumps({"workload": name, "dt": CASES[name][0], "steps": CASES[name][1],
+                      "l2_vs_fp64": l2, "mass_drift": {t: out[t + "_mass_drift"]
+                                                       for t in ("mixed", "fp64")}}))
     for a, b, v in zip(got, ref, VARS):
         assert np.isfinite(a).all(), v
         err = rel_l2(a, b)
         assert err <= TOL, f"{name} {v}: {err:.3e}"
-    th_ref = ref[4] / ref[0] - 300.0
-    th_got = got[4] / got[0] - 300.0
     assert rel_l2(th_got, th_ref) <= TOL
     for tag in ("fp64", "mixed"):
         drift = out[tag + "_mass_drift"]

@@ -89,8 +89,9 @@ def test_srtb_example_run(tmp_path, fixture):
     assert rel_l2(out["T"][kd, 0], g["fldN_T"][kg]) < 1e-10
     assert rel_l2(out["U"][kd], g["fldN_U"].reshape(-1, 3)[kg]) < 2e-9
     if "curved" in g:
+        # the precision form on curved elements is inviscid
         r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
-        assert r.returncode == 1 and "axis-aligned" in r.stderr, r.stderr
+        assert r.returncode == 1 and "inviscid" in r.stderr, r.stderr
 
 
 def test_segregated_run_follows_euler_binary(tmp_path):
@@ -202,8 +203,9 @@ def test_restart_from_written_fields(tmp_path):
 
 def test_inclined_block_run(tmp_path):
     """A block rotated by 30 degrees (full, non-diagonal metric): the FP64
-    forms through the driver are the oracle's bit for bit; the precision form,
-    built for axis-aligned elements, is refused with a message."""
+    forms through the driver are the oracle's bit for bit; the precision form
+    on inclined elements is inviscid and refuses this viscous run with a
+    message."""
     steps = 20
     d = make_case(tmp_path, "c1_2d", dt=0.005, steps=steps, viscosity=1.5)
     rotate_case_z(d, 30.0)
@@ -221,7 +223,7 @@ def test_inclined_block_run(tmp_path):
     assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
     assert np.array_equal(out["T"][:, 0], T)
     r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
-    assert r.returncode == 1 and "axis-aligned" in r.stderr, r.stderr
+    assert r.returncode == 1 and "inviscid" in r.stderr, r.stderr
 
 
 def test_text_output_and_high_order(tmp_path):
