@@ -79,7 +79,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -384,8 +384,9 @@ def run_ours(args):
     # the other form, for the mixed/FP64 speed-up
     other = None
     if prec_name == "mixed":
-        ms64 = timed(ng.FP64, max(1, args.steps // 2), 1)
-        other = {"fp64_value": world * dofs * 3 * max(1, args.steps // 2) / (ms64 * 1e-3)}
+        n64 = max(1, min(args.steps // 2, 100))
+        ms64 = timed(ng.FP64, n64, 1)
+        other = {"fp64_value": world * dofs * 3 * n64 / (ms64 * 1e-3)}
 
     # end to end through the C ABI with pinned host buffers
     rho = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
@@ -501,7 +502,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--prec", default="auto", choices=["auto", "mixed", "fp64"])

@@ -56,7 +56,9 @@ typedef enum {
 
 typedef enum {
     NSEM_FP64 = 0,  /* plain form: FP64 throughout, reference operation order */
-    NSEM_MIXED = 1  /* precision form: FP32 bulk, FP64 background/RK/sums      */
+    NSEM_MIXED = 1  /* precision form: FP32 bulk, FP64 background/RK/sums;
+                       conforming hex meshes with N+1 = 4, 5, 8 (2D: 4, 5) and
+                       SYMMETRY walls; inclined or curved elements inviscid */
 } nsem_precision;
 
 typedef enum {
@@ -206,8 +208,9 @@ nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double
  * precision form's reverse sweep evaluates the transposed stage in FP32 at
  * the forward's own FP32 stage states and accumulates the adjoint state in
  * FP64.  nsem_vjp_prec: g = J_L(u)^T w in the given form (the precision form
- * at the FP32 shadow of the current state).  The precision form needs an
- * inviscid context on the meshes it supports (NSEM_UNSUPPORTED otherwise). */
+ * at the FP32 shadow of the current state).  The precision form's adjoint
+ * needs an inviscid context on axis-aligned affine elements
+ * (NSEM_UNSUPPORTED otherwise). */
 nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                            nsem_precision prec, double* ms_fwd);
 nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const double* const w[5],

@@ -87,14 +87,29 @@ struct StageArgs {
     uint32_t* status;
 };
 
-template <int NX, int NY, int NZ>
+/* tensor-core flux layout (order 7): a variable's fluxes of one direction
+ * F[a][m][b] -- m the node index along the direction, (a, b) the other two
+ * (x: (j, k), y: (i, k), z: (i, j)) -- at a * TC_SA + p(m) * 8 + (b ^ s(m)),
+ * p(m) = m ^ (m >> 2 & 1), s(m) = 4 (m >> 2 & 1).  TC_SA = 72 puts four
+ * consecutive a in distinct groups of 8 banks; p keeps the rows m = 0-3,
+ * 4-7, the even and the odd rows each in four distinct groups; s separates
+ * the rows that share a group.  Every access is then conflict-free: the
+ * node threads' stores and reads in all three directions (a warp holds one i,
+ * four j and eight k), the face threads' reads, the A-fragment loads (rows
+ * m = tg, tg + 4) and the in-place result stores (rows 2 tg, 2 tg + 1). */
+constexpr int TC_SA = 72;
+constexpr int TC_NP = 8 * TC_SA;
+
+template <int NX, int NY, int NZ, bool TC = false>
 struct StageSmem {
     using G = Geo<NX, NY, NZ>;
     static constexpr int NP = G::NP, NFS = G::NFS;
-    /* floats: volume fluxes F4[3][NP] (x4) + F1[3][NP]; own values
-     * P[3][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS]; Q; metric */
+    /* floats: volume fluxes F4[3][NP] (x4) + F1[3][NP] (tensor-core line sums:
+     * F[3][5][TC_NP]); own values P[3][NP] (x4); face fluxes FF4[NFS] (x4) +
+     * FF1[NFS]; Q; metric */
+    static constexpr int FLUX = TC ? 15 * TC_NP : 15 * NP;
     static constexpr int OFF_F1 = 12 * NP;
-    static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
+    static constexpr int OFF_P = (FLUX + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 12 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
     static constexpr int OFF_Q = OFF_FF1 + NFS;
@@ -124,13 +139,15 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
  * the line as K and the 8 output nodes as N, one mma.sync m16n8k8 per tile
  * and TF32 pass.  FP32 accuracy from three TF32 products (a_lo b_hi +
  * a_hi b_lo + a_hi b_hi, Markidis' split; FP32 accumulation).  The fluxes
- * are kept per direction as F_d[v][a][m][b]: m the node index along d, (a, b)
- * the other two with b fastest (x: (j, k), y: (i, k), z: (i, j)), so each
- * fragment load and the in-place result store touch 32 distinct banks or
- * at most two ways. */
+ * are kept per direction as F_d[v][a][m][b] in the swizzled layout tc_pos. */
+__device__ __forceinline__ int tc_pos(int a, int m, int b) {
+    const int hi = (m >> 2) & 1;
+    return a * TC_SA + ((m ^ hi) << 3) + (b ^ (hi << 2));
+}
+
 template <int D>
 __device__ __forceinline__ int tc_idx(int i, int j, int k) {
-    return D == 0 ? j * 64 + i * 8 + k : D == 1 ? i * 64 + j * 8 + k : i * 64 + k * 8 + j;
+    return D == 0 ? tc_pos(j, i, k) : D == 1 ? tc_pos(i, j, k) : tc_pos(i, k, j);
 }
 
 __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
@@ -183,10 +200,10 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
         float4 A4;
         float A1;
         if constexpr (TC) {
-            const float* f = reinterpret_cast<const float*>(sF4) + DIR * 5 * NP +
+            const float* f = reinterpret_cast<const float*>(sF4) + DIR * 5 * TC_NP +
                              tc_idx<DIR>(fs.la >> 6, (fs.la >> 3) & 7, fs.la & 7);
-            A4 = make_float4(f[0], f[NP], f[2 * NP], f[3 * NP]);
-            A1 = f[4 * NP];
+            A4 = make_float4(f[0], f[TC_NP], f[2 * TC_NP], f[3 * TC_NP]);
+            A1 = f[4 * TC_NP];
         } else {
             A4 = sF4[DIR * NP + fs.la];
             A1 = sF1[DIR * NP + fs.la];
@@ -247,7 +264,7 @@ __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK,
 k_mixed_stage(StageArgs a) {
     static_assert(!TC || (NX == 8 && NY == 8 && NZ == 8), "tensor-core line sums: order 7");
     using G = Geo<NX, NY, NZ>;
-    using SM = StageSmem<NX, NY, NZ>;
+    using SM = StageSmem<NX, NY, NZ, TC>;
     constexpr int NP = G::NP;
     constexpr int NFS = G::NFS;
     extern __shared__ float4 smem4[];
@@ -381,8 +398,9 @@ k_mixed_stage(StageArgs a) {
         if constexpr (TC) {
             const int i = t >> 6, j = (t >> 3) & 7, k = t & 7;
             auto put = [&](int d, int idx) {
-                float* f = smem + d * 5 * NP + idx;
-                f[0] = f4.x; f[NP] = f4.y; f[2 * NP] = f4.z; f[3 * NP] = f4.w; f[4 * NP] = f1;
+                float* f = smem + d * 5 * TC_NP + idx;
+                f[0] = f4.x; f[TC_NP] = f4.y; f[2 * TC_NP] = f4.z; f[3 * TC_NP] = f4.w;
+                f[4 * TC_NP] = f1;
             };
             vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
             put(0, tc_idx<0>(i, j, k));
@@ -426,14 +444,18 @@ k_mixed_stage(StageArgs a) {
     if constexpr (TC) {
         /* tensor-core line sums, results in place of the fluxes */
         const int lane = t & 31, w = t >> 5, gq = lane >> 2, tg = lane & 3;
+        /* lane offsets of the A fragment (rows m = tg, tg + 4) and of the C
+         * fragment (rows 2 tg, 2 tg + 1), line b = gq, within a tile */
+        const int oa0 = tc_pos(0, tg, gq), oa2 = tc_pos(0, tg + 4, gq);
+        const int oc0 = tc_pos(0, 2 * tg, gq), oc1 = tc_pos(0, 2 * tg + 1, gq);
         for (int q = w; q < 60; q += G::BLOCK / 32) {
             const int d = q / 20, r = q % 20, v = r >> 2, a0 = (r & 3) * 2;
-            float* base = smem + d * 5 * NP + v * NP + a0 * 64;
+            float* base = smem + d * 5 * TC_NP + v * TC_NP + a0 * TC_SA;
             uint32_t ah[4], al[4], bh0, bl0, bh1, bl1;
-            split_tf32(base[tg * 8 + gq], ah[0], al[0]);
-            split_tf32(base[64 + tg * 8 + gq], ah[1], al[1]);
-            split_tf32(base[(tg + 4) * 8 + gq], ah[2], al[2]);
-            split_tf32(base[64 + (tg + 4) * 8 + gq], ah[3], al[3]);
+            split_tf32(base[oa0], ah[0], al[0]);
+            split_tf32(base[TC_SA + oa0], ah[1], al[1]);
+            split_tf32(base[oa2], ah[2], al[2]);
+            split_tf32(base[TC_SA + oa2], ah[3], al[3]);
             const float* qd = sQ + d * MAXN * QS + gq * QS;
             split_tf32(qd[tg], bh0, bl0);
             split_tf32(qd[tg + 4], bh1, bl1);
@@ -441,10 +463,10 @@ k_mixed_stage(StageArgs a) {
             mma_tf32(c, al, bh0, bh1);
             mma_tf32(c, ah, bl0, bl1);
             mma_tf32(c, ah, bh0, bh1);
-            base[(2 * tg) * 8 + gq] = c[0];
-            base[(2 * tg + 1) * 8 + gq] = c[1];
-            base[64 + (2 * tg) * 8 + gq] = c[2];
-            base[64 + (2 * tg + 1) * 8 + gq] = c[3];
+            base[oc0] = c[0];
+            base[oc1] = c[1];
+            base[TC_SA + oc0] = c[2];
+            base[TC_SA + oc1] = c[3];
         }
         __syncthreads();
     }
@@ -454,12 +476,12 @@ k_mixed_stage(StageArgs a) {
     if constexpr (TC) {
         const float Jx = sMeta[0], Jy = sMeta[1], Jz = sMeta[2];
         const float* rx = smem + tc_idx<0>(i, j, k);
-        const float* ry = smem + 5 * NP + tc_idx<1>(i, j, k);
-        const float* rz = smem + 10 * NP + tc_idx<2>(i, j, k);
+        const float* ry = smem + 5 * TC_NP + tc_idx<1>(i, j, k);
+        const float* rz = smem + 10 * TC_NP + tc_idx<2>(i, j, k);
         float Lt[5];
 #pragma unroll
         for (int v = 0; v < 5; v++)
-            Lt[v] = fmaf(Jz, rz[v * NP], fmaf(Jy, ry[v * NP], Jx * rx[v * NP]));
+            Lt[v] = fmaf(Jz, rz[v * TC_NP], fmaf(Jy, ry[v * TC_NP], Jx * rx[v * TC_NP]));
         L0 = Lt[0]; L1 = Lt[1]; L2 = Lt[2]; L3 = Lt[3]; L4 = Lt[4];
     } else {
     {
@@ -1092,7 +1114,7 @@ struct LaunchCfg {
 template <int NX, int NY, int NZ, bool VISC, bool TC, bool PERSIST>
 void launch_stage_v(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     using G = Geo<NX, NY, NZ>;
-    constexpr size_t SMEM = PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES;
+    constexpr size_t SMEM = PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ, TC>::BYTES;
     int64_t g = a.n_elem;
     if (PERSIST && c.pgrid[stage] > 0 && c.pgrid[stage] < g) g = c.pgrid[stage];
     const unsigned grid = (unsigned)g;
@@ -1165,7 +1187,7 @@ int launch_stage(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg
 
 template <int NX, int NY, int NZ, bool VISC, bool TC, bool PERSIST>
 int set_smem(int stage) {
-    constexpr int SMEM = (int)(PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
+    constexpr int SMEM = (int)(PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ, TC>::BYTES);
     if (SMEM <= 48 * 1024) return 0;
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
     switch (stage) {

@@ -22,8 +22,8 @@
  * precision form (--prec mixed).  --dump writes the mesh arrays and the
  * initial fields as raw little-endian files and exits without using a GPU.
  * Options the GPU path does not model (other boundary conditions, flux or
- * time schemes, curved or multi-block meshes, steady state) are refused with
- * a message; there is no CPU fallback.
+ * time schemes, multi-block meshes, steady state, adaptive refinement) are
+ * refused with a message; there is no CPU fallback.
  */
 #include <sys/stat.h>
 
