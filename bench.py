@@ -29,8 +29,11 @@ advanced through one RK stage.
                device time over the plain forward's for 200 steps with
                checkpoints every 20 (precision form; the FP64 form's ratio
                beside it over 20 steps)
-  --stage-profile  prints per-kernel mean device times of a few steps (a short
-               fixed launch sequence for ncu captures) and exits
+  --stage-profile  prints per-kernel mean device times of a few steps and the
+               step's DOF-stages/s from them (a short fixed launch sequence for
+               ncu captures; --workload, --prec, --viscosity) and exits
+  --adjoint-profile  prints the adjoint/forward device-time ratio on --workload
+               (--adjoint-steps, --adjoint-every, --prec, --viscosity) and exits
 
 Inputs (>= 560 MB of state, stage and primitive arrays) exceed the 129 MB L2,
 so no L2 flush is needed between timed steps.
@@ -236,6 +239,23 @@ def adjoint_ratio(solver, mesh, u0, steps, every, prec):
             "ratio": ms_adj / ms_fwd}
 
 
+def adjoint_profile(args):
+    """Adjoint/forward device-time ratio on a named workload: `--adjoint-steps`
+    steps with checkpoints every `--adjoint-every`, in the form `--prec`, with
+    `--viscosity` (default none)."""
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300.mesh import workload
+
+    prec = ng.MIXED if args.prec == "mixed" else ng.FP64
+    m, u = workload(args.workload)
+    s = ng.Solver(m, dt=args.dt, viscosity=args.viscosity)
+    r = adjoint_ratio(s, m, u, args.adjoint_steps, args.adjoint_every, prec)
+    r.update({"workload": args.workload, "dt": args.dt, "prec": "mixed" if prec else "fp64",
+              "viscosity": args.viscosity or 0.0})
+    print(json.dumps(r))
+    s.close()
+
+
 def stage_profile(args):
     """Per-kernel mean device times of a few steps: 3 graph-launched steps,
     then `--profile-steps` launch by launch (a short fixed launch sequence for
@@ -243,7 +263,7 @@ def stage_profile(args):
     --scheme seg instead runs `--profile-steps` graph-launched steps of the
     reference's own segregated update (from the workload's fields, or from a
     golden fixture's mesh and step-0 fields with --fixture) and prints their
-    wall time."""
+    wall time; --scheme conv the same for the scalar convection path."""
     import nebulasem_gb300 as ng
     from nebulasem_gb300.mesh import workload
 
@@ -261,7 +281,7 @@ def stage_profile(args):
             rho = u[0]
             U = np.stack([u[1] / rho, u[2] / rho, u[3] / rho], axis=1)
             T = u[4] / rho - 300.0
-        s = ng.Solver(m, dt=args.dt)
+        s = ng.Solver(m, dt=args.dt, viscosity=args.viscosity)
         s.set_fields(rho, U, T)
         s.step(args.profile_steps, scheme=ng.REF_SEGREGATED)   # builds the graph
         s.set_fields(rho, U, T)
@@ -275,13 +295,37 @@ def stage_profile(args):
                           "dof_steps_per_s": 5 * n * args.profile_steps / wall}))
         s.close()
         return
+    if args.scheme == "conv":
+        # the convection app's scalar transport: theta' of the workload in the
+        # uniform wind (6, -4, 5) m/s
+        m, u = workload(args.workload)
+        n = int(m["meta"][7])
+        s = ng.Solver(m, dt=args.dt)
+        U = np.tile(np.array([6.0, -4.0, 5.0]), (n, 1))
+        T = u[4] / u[0] - 300.0
+        s.convection_set(U, T)
+        s.convection_step(args.profile_steps)
+        s.convection_set(U, T)
+        s.sync()
+        t0 = time.perf_counter()
+        s.convection_step(args.profile_steps)
+        s.sync()
+        wall = time.perf_counter() - t0
+        print(json.dumps({"scheme": "convection", "nodes": n, "steps": args.profile_steps,
+                          "seconds": wall, "dof_steps_per_s": n * args.profile_steps / wall}))
+        s.close()
+        return
     prec = ng.MIXED if args.prec != "fp64" else ng.FP64
     m, u = workload(args.workload)
-    s = ng.Solver(m, dt=args.dt)
+    s = ng.Solver(m, dt=args.dt, viscosity=args.viscosity)
     s.set_state(u)
     s.step(3, prec=prec)
     prof = s.profile(args.profile_steps, prec=prec)
-    print(json.dumps({k: v[0] / v[1] for k, v in prof.items()}))
+    out = {k: v[0] / v[1] for k, v in prof.items()}
+    # whole-step throughput of the profiled steps (launch by launch)
+    step_ms = sum(v[0] for v in prof.values()) / args.profile_steps
+    out["dof_stages_per_s"] = 15 * s.n_int / (step_ms * 1e-3)
+    print(json.dumps(out))
     s.close()
 
 
@@ -515,10 +559,17 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--dt", type=float, default=DT)
     ap.add_argument("--profile-steps", type=int, default=5)
-    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg"])
+    ap.add_argument("--scheme", default="ssprk3", choices=["ssprk3", "seg", "conv"])
     ap.add_argument("--fixture", default=None)
+    ap.add_argument("--viscosity", type=float, default=None,
+                    help="--stage-profile, --adjoint-profile: artificial viscosity (diffusion YES), default none")
+    ap.add_argument("--adjoint-profile", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-every", type=int, default=20)
     args = ap.parse_args()
-    if args.stage_profile:
+    if args.adjoint_profile:
+        adjoint_profile(args)
+    elif args.stage_profile:
         stage_profile(args)
     elif args.impl == "reference":
         run_reference(args)
