@@ -64,13 +64,14 @@ nsem_status fail(nsem_ctx* c, nsem_status s, const std::string& msg) {
     return s;
 }
 
-/* the forms other than the reference's segregated scheme assume conforming
- * faces (at most 3 face slots per node) */
+/* calls built for conforming faces only: the precision form's adjoint and the
+ * per-launch profile of the FP64 forms */
 nsem_status require_conforming(nsem_ctx* c) {
     if (c && c->dev.n_ms > 0)
         return fail(c, NSEM_UNSUPPORTED,
-                    "non-conforming (2:1) faces: only the FP64 forms (SSP-RK3, "
-                    "NSEM_REF_SEGREGATED, convection) step this mesh");
+                    "non-conforming (2:1) faces: this call is built for conforming meshes "
+                    "(the FP64 forms, the precision form's steps and the FP64 adjoint "
+                    "take them)");
     return NSEM_OK;
 }
 
@@ -683,7 +684,6 @@ nsem_status nsem_get_fields(nsem_ctx* ctx, double* rho, double* U, double* T) {
 
 nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5],
                           double* p_prime) {
-    if (ctx && ctx->dev.n_ms > 0 && prec != NSEM_FP64) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!L) return fail(ctx, NSEM_BAD_ARG, "L is NULL");
     for (int c = 0; c < 5; c++) if (!L[c]) return fail(ctx, NSEM_BAD_ARG, "L[c] is NULL");
@@ -716,7 +716,6 @@ nsem_status nsem_tendency(nsem_ctx* ctx, nsem_precision prec, double* const L[5]
 }
 
 nsem_status nsem_step(nsem_ctx* ctx, int nsteps, nsem_scheme scheme, nsem_precision prec) {
-    if (ctx && ctx->dev.n_ms > 0 && prec != NSEM_FP64) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 0) return fail(ctx, NSEM_BAD_ARG, "nsteps < 0");
     if (scheme != NSEM_SSPRK3 && scheme != NSEM_REF_SEGREGATED)
@@ -1348,7 +1347,7 @@ extern "C" nsem_status nsem_convection_get(nsem_ctx* ctx, double* T) {
 
 nsem_status nsem_profile(nsem_ctx* ctx, int nsteps, nsem_precision prec, double ms[8],
                          int launches[8], char names[8 * 32]) {
-    if (ctx && ctx->dev.n_ms > 0) return require_conforming(ctx);
+    if (ctx && ctx->dev.n_ms > 0 && prec != NSEM_MIXED) return require_conforming(ctx);
     if (!ctx) return NSEM_BAD_ARG;
     if (!ms || !launches || !names) return fail(ctx, NSEM_BAD_ARG, "output pointer is NULL");
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps < 1");

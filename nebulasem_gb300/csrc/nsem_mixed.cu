@@ -48,6 +48,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <map>
@@ -79,6 +80,8 @@ struct StageArgs {
     const float* bg;           /* [layers][4][NP]                          */
     const float* Jg;           /* general geometry: [e][10][NP] Jinv cV (9), 1/cV */
     const float* Fn;           /* general geometry: [e][3][NFS] outward weighted normals */
+    const float* MF;           /* mortar faces: [n_mf][5][nfmax] outward face values */
+    int nfmax;
     int64_t n_elem;
     float dt, gamma, gR, g[3];
     float nu, nu_pr, T0;
@@ -148,6 +151,15 @@ __device__ __forceinline__ int tc_pos(int a, int m, int b) {
 template <int D>
 __device__ __forceinline__ int tc_idx(int i, int j, int k) {
     return D == 0 ? tc_pos(j, i, k) : D == 1 ? tc_pos(i, j, k) : tc_pos(i, k, j);
+}
+
+/* index of face slot t within its face: x (j, k), y (i, k), z (i, j) */
+template <int NX, int NY, int NZ>
+__device__ __forceinline__ int face_local(int t) {
+    using G = Geo<NX, NY, NZ>;
+    if (t < G::OFF_Y) return t % G::NFX;
+    if (t < G::OFF_Z) return (t - G::OFF_Y) % G::NFY;
+    return (t - G::OFF_Z) % G::NFZ;
 }
 
 __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
@@ -361,6 +373,13 @@ k_mixed_stage(StageArgs a) {
     if (t < NFS) {
         fs = face_slot<NX, NY, NZ>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if (nb <= -2) {
+            /* a face on a 2:1 mortar: its outward values come from the
+             * mortar kernels */
+            const float* mf = a.MF + (int64_t)(-2 - nb) * 5 * a.nfmax + face_local<NX, NY, NZ>(t);
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(mf + v * a.nfmax);
+        }
         if (nb >= 0) {
             const float* s = a.S + (int64_t)nb * 5 * NP + fs.lo;
 #pragma unroll
@@ -397,17 +416,17 @@ k_mixed_stage(StageArgs a) {
         float f1;
         if constexpr (TC) {
             const int i = t >> 6, j = (t >> 3) & 7, k = t & 7;
-            auto put = [&](int d, int idx) {
+            auto put = [&](int d, int idx, const float4& v4, float v1) {
                 float* f = smem + d * 5 * TC_NP + idx;
-                f[0] = f4.x; f[TC_NP] = f4.y; f[2 * TC_NP] = f4.z; f[3 * TC_NP] = f4.w;
-                f[4 * TC_NP] = f1;
+                f[0] = v4.x; f[TC_NP] = v4.y; f[2 * TC_NP] = v4.z; f[3 * TC_NP] = v4.w;
+                f[4 * TC_NP] = v1;
             };
             vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            put(0, tc_idx<0>(i, j, k));
+            put(0, tc_idx<0>(i, j, k), f4, f1);
             vol_flux<1, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            put(1, tc_idx<1>(i, j, k));
+            put(1, tc_idx<1>(i, j, k), f4, f1);
             vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            put(2, tc_idx<2>(i, j, k));
+            put(2, tc_idx<2>(i, j, k), f4, f1);
         } else {
             vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
             sF4[t] = f4; sF1[t] = f1;
@@ -429,7 +448,10 @@ k_mixed_stage(StageArgs a) {
     if (t < NFS) {
         float4 o4;
         float o1;
-        if (fs.dir == 0)
+        if (nb <= -2) {
+            o4 = make_float4(oth[0], oth[1], oth[2], oth[3]);
+            o1 = oth[4];
+        } else if (fs.dir == 0)
             face_flux<NX, NY, NZ, 0, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
         else if (G::HAS_Y && fs.dir == 1)
             face_flux<NX, NY, NZ, 1, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
@@ -854,6 +876,196 @@ k_mixed_stage_gen(StageArgs a) {
         }
         if (!finite) atomicOr(a.status, NSEM_STATUS_NONFINITE);
     }
+}
+
+/* ------------------------------------------------------------------------
+ * Non-conforming (2:1) faces in the precision form (inviscid, axis-aligned
+ * elements): the plain form's mortar treatment (field.h:2019-2248) in FP32 on
+ * the perturbation state.  Per stage, before the stage kernel:
+ *   k_mx_mortar_flux  per mortar slot: the fine node's stage state and the
+ *       coarse side's face quantities interpolated from the coarse face's nodes
+ *       with psiRef (|U|, c, rho U, rho', the momentum flux tensor, the theta
+ *       flux, Theta'; rho' and Theta' corrected by the interpolated minus the
+ *       fine node's background, so that their jumps are those of the full
+ *       fields), the Rusanov flux vectors and the fine side's F.n;
+ *   k_mx_mortar_proj  per mortar slot: the sub-face's flux vectors projected
+ *       onto the slot's coarse node with psiCor, dotted with its normal;
+ *   k_mx_mortar_fill  per node of an element face on a mortar: the sum of its
+ *       entries (fine: one, coarse: one per sub-face), scaled by sign / (cV
+ *       J_d / w_end) into the outward value the stage kernel lifts.
+ * ------------------------------------------------------------------------ */
+enum { MX_FINE, MX_FINE_C1, MX_BASE, MX_SA, MX_SB, MX_NA, MX_NB, MX_IA, MX_IB, MX_FIRST, MX_TA,
+       MX_TB, MX_FIELDS };
+constexpr int MX_COARSE = 1 << 30;
+
+struct MortarMxArgs {
+    const int32_t* mi;     /* [MX_FIELDS][n_ms] */
+    const float* mf;       /* [8][n_ms] */
+    const float* psiR;     /* [6][MAXN^2] */
+    const float* psiC;     /* [6][MAXN^2] */
+    float* F;              /* [15][n_ms] */
+    float* d;              /* [5][n_ms] */
+    float* dC;             /* [5][n_ms] */
+    const int32_t* ent;    /* [n_mf][nfmax][4] */
+    const float* coef;     /* [n_mf][nfmax][4] */
+    float* MF;             /* [n_mf][5][nfmax] */
+    int64_t n_ms, n_mf;
+    int nfmax, np;
+};
+
+/* stage state and primitives of one node (element-blocked layout) */
+template <bool HAS_DIN>
+__device__ __forceinline__ Pt mx_node(const StageArgs& a, int np, int64_t node, float* x) {
+    const int64_t e = node / np;
+    const int l = (int)(node - e * np);
+    const float* s = a.S + e * 5 * np + l;
+#pragma unroll
+    for (int v = 0; v < 5; v++) x[v] = __ldg(s + v * np);
+    if constexpr (HAS_DIN) {
+        const float* d = a.Din + e * 5 * np + l;
+#pragma unroll
+        for (int v = 0; v < 5; v++) x[v] = __fadd_rn(x[v], __ldg(d + v * np));
+    }
+    const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * np + l;
+    float b[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) b[c] = __ldg(bg + c * np);
+    return pointwise(x, b, a.eos, a.gamma, a.gR);
+}
+
+template <bool HAS_DIN>
+__global__ void __launch_bounds__(128) k_mx_mortar_flux(StageArgs a, MortarMxArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    /* the fine side: its own node */
+    float xf[5];
+    const Pt pf = mx_node<HAS_DIN>(a, m.np, fld(MX_FINE), xf);
+    /* the coarse side: quantities interpolated over the coarse face's nodes
+     * (coarse index along a outer, along b inner) */
+    float q[19];
+#pragma unroll
+    for (int c = 0; c < 19; c++) q[c] = 0.0f;
+    const int base = fld(MX_BASE), sa = fld(MX_SA), sb = fld(MX_SB), Na = fld(MX_NA),
+              Nb = fld(MX_NB), ia = fld(MX_IA), ib = fld(MX_IB);
+    const float* Pa = m.psiR + fld(MX_TA) * MAXN * MAXN;
+    const float* Pb = m.psiR + fld(MX_TB) * MAXN * MAXN;
+    for (int na = 0; na < Na; na++)
+        for (int nb = 0; nb < Nb; nb++) {
+            float x[5];
+            const Pt p = mx_node<HAS_DIN>(a, m.np, (int64_t)base + na * sa + nb * sb, x);
+            const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+            q[0] = fmaf(w, p.umag, q[0]);
+            q[1] = fmaf(w, p.c, q[1]);
+#pragma unroll
+            for (int c = 0; c < 3; c++) q[2 + c] = fmaf(w, x[1 + c], q[2 + c]);
+            q[5] = fmaf(w, x[0], q[5]);
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    q[6 + tidx(r, c)] = fmaf(w, fmaf(x[1 + r], p.u[c], r == c ? p.pp : 0.0f),
+                                             q[6 + tidx(r, c)]);
+#pragma unroll
+            for (int c = 0; c < 3; c++) q[15 + c] = fmaf(w, x[1 + c] * p.th, q[15 + c]);
+            q[18] = fmaf(w, x[4], q[18]);
+        }
+    const float* g = m.mf + ms;
+    const float n[3] = {__ldg(g), __ldg(g + m.n_ms), __ldg(g + 2 * m.n_ms)};
+    const float en[3] = {__ldg(g + 3 * m.n_ms), __ldg(g + 4 * m.n_ms), __ldg(g + 5 * m.n_ms)};
+    q[5] += __ldg(g + 6 * m.n_ms);
+    q[18] += __ldg(g + 7 * m.n_ms);
+    /* the fine side's face quantities, in the same layout */
+    float f[19];
+    f[0] = pf.umag;
+    f[1] = pf.c;
+#pragma unroll
+    for (int c = 0; c < 3; c++) f[2 + c] = xf[1 + c];
+    f[5] = xf[0];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[6 + tidx(r, c)] = fmaf(xf[1 + r], pf.u[c], r == c ? pf.pp : 0.0f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) f[15 + c] = xf[1 + c] * pf.th;
+    f[18] = xf[4];
+    /* side 1 (FO) and side 2 (FN) of the slot; the normal points 1 -> 2 */
+    const bool fine1 = fld(MX_FINE_C1) != 0;
+    const float* A = fine1 ? f : q;
+    const float* B = fine1 ? q : f;
+    const float lam = 0.25f * ((A[0] + B[0]) + (A[1] + B[1]));
+    float F[15];
+    {
+        const float jr = lam * (B[5] - A[5]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) F[c] = fmaf(-en[c], jr, 0.5f * (A[2 + c] + B[2 + c]));
+        const float jt = lam * (B[18] - A[18]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) F[12 + c] = fmaf(-en[c], jt, 0.5f * (A[15 + c] + B[15 + c]));
+        float dq[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) dq[c] = (B[2 + c] - A[2 + c]) * lam;
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                F[3 + tidx(r, c)] = fmaf(-en[r], dq[c], 0.5f * (A[6 + tidx(r, c)] + B[6 + tidx(r, c)]));
+    }
+#pragma unroll
+    for (int c = 0; c < 15; c++) m.F[c * m.n_ms + ms] = F[c];
+    m.d[ms] = fmaf(F[0], n[0], fmaf(F[1], n[1], F[2] * n[2]));
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+        m.d[(1 + r) * m.n_ms + ms] =
+            fmaf(F[3 + tidx(r, 0)], n[0], fmaf(F[3 + tidx(r, 1)], n[1], F[3 + tidx(r, 2)] * n[2]));
+    m.d[4 * m.n_ms + ms] = fmaf(F[12], n[0], fmaf(F[13], n[1], F[14] * n[2]));
+}
+
+__global__ void __launch_bounds__(128) k_mx_mortar_proj(MortarMxArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    const int Na = fld(MX_NA), Nb = fld(MX_NB), na = fld(MX_IA), nb = fld(MX_IB),
+              first = fld(MX_FIRST);
+    const float* Pa = m.psiC + fld(MX_TA) * MAXN * MAXN;
+    const float* Pb = m.psiC + fld(MX_TB) * MAXN * MAXN;
+    float P[15];
+#pragma unroll
+    for (int c = 0; c < 15; c++) P[c] = 0.0f;
+    for (int ja = 0; ja < Na; ja++)
+        for (int jb = 0; jb < Nb; jb++) {
+            const int64_t s2 = first + ja * Nb + jb;
+            const float w = __ldg(Pa + ja * Na + na) * __ldg(Pb + jb * Nb + nb);
+#pragma unroll
+            for (int c = 0; c < 15; c++) P[c] = fmaf(w, __ldg(m.F + c * m.n_ms + s2), P[c]);
+        }
+    const float* g = m.mf + ms;
+    const float n[3] = {__ldg(g), __ldg(g + m.n_ms), __ldg(g + 2 * m.n_ms)};
+    m.dC[ms] = fmaf(P[0], n[0], fmaf(P[1], n[1], P[2] * n[2]));
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+        m.dC[(1 + r) * m.n_ms + ms] =
+            fmaf(P[3 + tidx(r, 0)], n[0], fmaf(P[3 + tidx(r, 1)], n[1], P[3 + tidx(r, 2)] * n[2]));
+    m.dC[4 * m.n_ms + ms] = fmaf(P[12], n[0], fmaf(P[13], n[1], P[14] * n[2]));
+}
+
+__global__ void __launch_bounds__(128) k_mx_mortar_fill(MortarMxArgs m) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= m.n_mf * m.nfmax) return;
+    const int64_t f = id / m.nfmax;
+    const int r = (int)(id - f * m.nfmax);
+    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int q = 0; q < 4; q++) {
+        const int32_t en = __ldg(m.ent + id * 4 + q);
+        if (en < 0) break;
+        const float c = __ldg(m.coef + id * 4 + q);
+        const float* src = (en & MX_COARSE) ? m.dC : m.d;
+        const int64_t ms = en & (MX_COARSE - 1);
+#pragma unroll
+        for (int v = 0; v < 5; v++) acc[v] = fmaf(c, __ldg(src + v * m.n_ms + ms), acc[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < 5; v++) m.MF[(f * 5 + v) * m.nfmax + r] = acc[v];
 }
 
 /* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
@@ -1330,6 +1542,15 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         err = "precision form on inclined or curved elements is inviscid";
         return NSEM_UNSUPPORTED;
     }
+    /* non-conforming (2:1) faces: the fine sub-faces' ids */
+    std::vector<int8_t> on_mortar(m->n_mortar > 0 ? m->n_face : 0, 0);
+    if (m->n_mortar > 0) {
+        if (gen || dev.nu != 0.0) {
+            err = "precision form on refined meshes: inviscid runs on axis-aligned elements";
+            return NSEM_UNSUPPORTED;
+        }
+        for (int32_t q = 0; q < m->n_mortar; q++) on_mortar[m->mortar[4 * (size_t)q]] = 1;
+    }
     /* general geometry: Jinv cV and 1/cV per node, outward weighted normals
      * per element face slot */
     const int nfx = NY * NZ, nfy = NX * NZ, nfz = NX * NY;
@@ -1354,6 +1575,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
     for (int64_t e = 0; e < ne; e++) {
         for (uint32_t f = m->face_idx0[e]; f < m->face_idx1[e]; f++) {
             const int64_t fid = m->all_faces[f];
+            if (m->n_mortar > 0 && on_mortar[fid]) continue;   /* below */
             /* find the first used slot of this face */
             int64_t k = -1;
             for (int q = 0; q < m->npf; q++) {
@@ -1491,6 +1713,134 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         mb->lift[d] = (float)(1.0 / w[0]);
     }
 
+
+    /* non-conforming faces: per mortar slot (entries in order, (ia, ib)
+     * row-major, the numbering of the plain form) the fine node, the coarse
+     * face and the interpolation indices, normals and background corrections;
+     * per element face on a mortar its node entries */
+    std::vector<int32_t> mxi[MX_FIELDS];
+    std::vector<float> mxf[8];
+    std::vector<int32_t> ment;
+    std::vector<float> mcoef;
+    std::map<int64_t, int32_t> mf_of;
+    const int nfmax = std::max(nfx, std::max(nfy, nfz));
+    if (m->n_mortar > 0) {
+        const int64_t stride[3] = {(int64_t)NY * NZ, NZ, 1};
+        auto loc = [&](int64_t node, int c[3]) {
+            const int l = (int)(node % NP);
+            c[0] = l / (NY * NZ); c[1] = (l / NZ) % NY; c[2] = l % NZ;
+        };
+        auto in_face = [&](int dir, const int c[3]) {
+            return dir == 0 ? c[1] * NZ + c[2] : dir == 1 ? c[0] * NZ + c[2] : c[0] * NY + c[1];
+        };
+        auto mf_index = [&](int64_t e, int face) {
+            const int64_t key = e * 6 + face;
+            auto it = mf_of.find(key);
+            if (it != mf_of.end()) return it->second;
+            const int32_t id = (int32_t)mf_of.size();
+            mf_of.emplace(key, id);
+            nbr[(int64_t)face * ne + e] = -2 - id;
+            ment.resize((size_t)(id + 1) * nfmax * 4, -1);
+            mcoef.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
+            return id;
+        };
+        auto add = [&](int32_t mf, int r, int32_t code, double c) -> bool {
+            for (int q = 0; q < 4; q++) {
+                const size_t at = ((size_t)mf * nfmax + r) * 4 + q;
+                if (ment[at] < 0) { ment[at] = code; mcoef[at] = (float)c; return true; }
+            }
+            return false;
+        };
+        /* 1 / (cV J_d / w_end), with J_d / w_end as the stage kernel forms it */
+        auto scale = [&](int64_t node, int dir) {
+            const float coef = J[(int64_t)dir * ne + node / NP] * mb->lift[dir];
+            return 1.0 / (m->cV[node] * (double)coef);
+        };
+        for (int32_t q = 0; q < m->n_mortar; q++) {
+            const uint32_t* r = m->mortar + 4 * (size_t)q;
+            const int64_t fi = r[0];
+            const int fm = (int)r[1], fid = (int)r[2];
+            int aa, bb, fix;
+            if (fid <= 1) { aa = 0; bb = 1; fix = 2; }
+            else if (fid <= 3) { aa = 0; bb = 2; fix = 1; }
+            else { aa = 1; bb = 2; fix = 0; }
+            const int Na = npd[aa], Nb = npd[bb];
+            const int64_t k0 = fi * m->npf;
+            const int64_t cnode0 = fm == 1 ? m->FN[k0] : m->FO[k0];
+            const int64_t fnode0 = fm == 1 ? m->FO[k0] : m->FN[k0];
+            if (cnode0 >= n_int || fnode0 >= n_int) {
+                err = "precision form: mortar face on a boundary";
+                return NSEM_UNSUPPORTED;
+            }
+            const int64_t cell_c = cnode0 / NP, cell_f = fnode0 / NP;
+            const int64_t base = cell_c * NP + ((fid & 1) ? npd[fix] - 1 : 0) * stride[fix];
+            /* the fine element's face: the index plane every fine node lies on */
+            int dir_f = -1, side_f = 0;
+            for (int d = 0; d < 3 && dir_f < 0; d++) {
+                if (npd[d] == 1) continue;
+                for (int sd = 0; sd < 2 && dir_f < 0; sd++) {
+                    bool all = true;
+                    for (int w = 0; w < Na * Nb && all; w++) {
+                        const int64_t node = fm == 1 ? m->FO[k0 + w] : m->FN[k0 + w];
+                        int c[3];
+                        loc(node, c);
+                        all = node / NP == cell_f && c[d] == (sd ? npd[d] - 1 : 0);
+                    }
+                    if (all) { dir_f = d; side_f = sd; }
+                }
+            }
+            if (dir_f < 0) {
+                err = "precision form: mortar face off the fine element's index planes";
+                return NSEM_UNSUPPORTED;
+            }
+            const int32_t mf_f = mf_index(cell_f, 2 * dir_f + side_f);
+            const int32_t mf_c = mf_index(cell_c, 2 * fix + (fid & 1));
+            const int32_t first = (int32_t)mxi[0].size();
+            const int ta = 2 * aa + (int)(r[3] & 1), tb = 2 * bb + (int)((r[3] >> 1) & 1);
+            const double* Pa = m->psi_ref[ta];
+            const double* Pb = m->psi_ref[tb];
+            for (int ia = 0; ia < Na; ia++)
+                for (int ib = 0; ib < Nb; ib++) {
+                    const int64_t k = k0 + (int64_t)ia * Nb + ib;
+                    const int64_t fnode = fm == 1 ? m->FO[k] : m->FN[k];
+                    const int64_t cnode = fm == 1 ? m->FN[k] : m->FO[k];
+                    if (fnode / NP != cell_f || cnode / NP != cell_c || m->fI[k] != 0.5) {
+                        err = "precision form: unexpected mortar slot layout";
+                        return NSEM_UNSUPPORTED;
+                    }
+                    const int32_t ms = (int32_t)mxi[0].size();
+                    const int32_t fld[MX_FIELDS] = {(int32_t)fnode, fm == 1 ? 1 : 0, (int32_t)base,
+                                                    (int32_t)stride[aa], (int32_t)stride[bb], Na, Nb,
+                                                    ia, ib, first, ta, tb};
+                    for (int c = 0; c < MX_FIELDS; c++) mxi[c].push_back(fld[c]);
+                    const double* v = m->fN + 3 * k;
+                    const double mg = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                    for (int c = 0; c < 3; c++) {
+                        mxf[c].push_back((float)v[c]);
+                        mxf[3 + c].push_back((float)(v[c] / mg));
+                    }
+                    /* interpolated minus own background (rho_ref, Theta_ref) */
+                    double ir = 0.0;
+                    for (int na = 0; na < Na; na++)
+                        for (int nb = 0; nb < Nb; nb++)
+                            ir += rref_h[base + na * stride[aa] + nb * stride[bb]] * Pa[na * Na + ia] *
+                                  Pb[nb * Nb + ib];
+                    mxf[6].push_back((float)(ir - rref_h[fnode]));
+                    mxf[7].push_back((float)((ir - rref_h[fnode]) * dev.T0));
+                    int c[3];
+                    loc(fnode, c);
+                    bool ok = add(mf_f, in_face(dir_f, c), ms, (fm == 1 ? 1.0 : -1.0) * scale(fnode, dir_f));
+                    loc(cnode, c);
+                    ok = ok && add(mf_c, in_face(fix, c), ms | MX_COARSE,
+                                   (fm == 2 ? 1.0 : -1.0) * scale(cnode, fix));
+                    if (!ok) {
+                        err = "precision form: more than four mortar entries on a face node";
+                        return NSEM_UNSUPPORTED;
+                    }
+                }
+        }
+    }
+
     auto up = [&](auto** ptr, const auto& vec) -> bool {
         using T = typename std::remove_reference<decltype(vec[0])>::type;
         size_t bytes = vec.size() * sizeof(T);
@@ -1504,6 +1854,30 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         return NSEM_NO_MEMORY;
     }
     mb->gen = gen;
+    mb->n_ms = (int64_t)mxi[0].size();
+    mb->n_mf = (int64_t)mf_of.size();
+    mb->nfmax = nfmax;
+    if (mb->n_ms > 0) {
+        std::vector<int32_t> mi;
+        for (int c = 0; c < MX_FIELDS; c++) mi.insert(mi.end(), mxi[c].begin(), mxi[c].end());
+        std::vector<float> mf, psi(2 * 6 * MAXN * MAXN, 0.0f);
+        for (int c = 0; c < 8; c++) mf.insert(mf.end(), mxf[c].begin(), mxf[c].end());
+        for (int t = 0; t < 6; t++) {
+            const int n = npd[t / 2];
+            for (int q = 0; q < n * n; q++) {
+                psi[t * MAXN * MAXN + q] = (float)m->psi_ref[t][q];
+                psi[(6 + t) * MAXN * MAXN + q] = (float)m->psi_cor[t][q];
+            }
+        }
+        const std::vector<float> scratch15(15 * mb->n_ms, 0.0f), scratch5(5 * mb->n_ms, 0.0f),
+            mfv(5 * mb->n_mf * nfmax, 0.0f);
+        if (!up(&mb->mx_i, mi) || !up(&mb->mx_f, mf) || !up(&mb->mx_psi, psi) ||
+            !up(&mb->mx_F, scratch15) || !up(&mb->mx_d, scratch5) || !up(&mb->mx_dC, scratch5) ||
+            !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv)) {
+            err = "precision form: device allocation failed";
+            return NSEM_NO_MEMORY;
+        }
+    }
     auto dal = [&](auto** p, size_t bytes) -> bool {
         if (cudaMalloc((void**)p, bytes) != cudaSuccess) return false;
         allocs->push_back((void*)*p);
@@ -1571,6 +1945,8 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
     a.bg = mb->bg;
     a.Jg = mb->Jg;
     a.Fn = mb->Fn;
+    a.MF = mb->MF;
+    a.nfmax = mb->nfmax;
     a.n_elem = mb->n_elem;
     a.dt = (float)dt;
     a.gamma = (float)dev->gamma;
@@ -1589,7 +1965,37 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
     return a;
 }
 
+int launch_mortars(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+    MortarMxArgs m{};
+    m.mi = mb->mx_i;
+    m.mf = mb->mx_f;
+    m.psiR = mb->mx_psi;
+    m.psiC = mb->mx_psi + 6 * MAXN * MAXN;
+    m.F = mb->mx_F;
+    m.d = mb->mx_d;
+    m.dC = mb->mx_dC;
+    m.ent = mb->mf_ent;
+    m.coef = mb->mf_coef;
+    m.MF = mb->MF;
+    m.n_ms = mb->n_ms;
+    m.n_mf = mb->n_mf;
+    m.nfmax = mb->nfmax;
+    m.np = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    const unsigned gs = (unsigned)((mb->n_ms + 127) / 128);
+    if (stage >= 2)
+        k_mx_mortar_flux<true><<<gs, 128, 0, st>>>(a, m);
+    else
+        k_mx_mortar_flux<false><<<gs, 128, 0, st>>>(a, m);
+    k_mx_mortar_proj<<<gs, 128, 0, st>>>(m);
+    k_mx_mortar_fill<<<(unsigned)((mb->n_mf * mb->nfmax + 127) / 128), 128, 0, st>>>(m);
+    return (int)cudaGetLastError();
+}
+
 int launch_args(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+    if (mb->n_ms > 0) {
+        const int e = launch_mortars(mb, a, stage, st);
+        if (e) return e;
+    }
     LaunchCfg c{};
     c.visc = mb->visc;
     c.tc = mb->tc;

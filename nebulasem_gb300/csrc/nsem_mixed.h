@@ -39,6 +39,23 @@ struct NsemMixedBuf {
     float* Jg = nullptr;          /* gen: [n_elem][10][NP] Jinv cV, 1/cV    */
     float* Fn = nullptr;          /* gen: [n_elem][3][NFS] outward fN       */
     int pgrid[4] = {0, 0, 0, 0};  /* their grids (resident CTAs), per stage */
+    /* non-conforming (2:1) faces (inviscid runs on axis-aligned elements):
+     * per mortar slot the fine node, the coarse face and the interpolation
+     * indices; the flux vectors, the fine side's F.n and the coarse side's
+     * projected F.n; per element face on a mortar the outward face values
+     * that the stage kernels lift (nbr = -2 - index) */
+    int64_t n_ms = 0;             /* mortar slots                           */
+    int32_t* mx_i = nullptr;      /* [MX_FIELDS][n_ms]                      */
+    float* mx_f = nullptr;        /* [8][n_ms]: fN (3), unit normal (3), interpolated minus own rho_ref, Theta_ref */
+    float* mx_psi = nullptr;      /* [2][6][MAXN^2] psiRef, psiCor (FP32)   */
+    float* mx_F = nullptr;        /* [15][n_ms] face flux vectors           */
+    float* mx_d = nullptr;        /* [5][n_ms] fine side F.n                */
+    float* mx_dC = nullptr;       /* [5][n_ms] coarse side projected F.n    */
+    int64_t n_mf = 0;             /* element faces on mortars               */
+    int nfmax = 0;                /* nodes per face (largest direction)     */
+    int32_t* mf_ent = nullptr;    /* [n_mf][nfmax][4] mortar slot (| 1<<30: coarse value), -1 */
+    float* mf_coef = nullptr;     /* [n_mf][nfmax][4] sign / (cV J_d / w_end) */
+    float* MF = nullptr;          /* [n_mf][5][nfmax] outward face values   */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */

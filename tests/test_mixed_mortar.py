@@ -1,0 +1,111 @@
+"""Precision form on adaptively refined meshes (2:1 mortar faces; the
+reference refines with its `prepare -refine`), inviscid runs.
+
+Per stage, mortar kernels interpolate the coarse side's face quantities onto
+each mortar slot with psiRef (the fine side reads its own node), form the
+Rusanov flux vectors there, project them back onto the coarse face's nodes
+with psiCor, and hand both sides' outward values to the stage kernel -- the
+plain form's mortar treatment (field.h:2019-2248) in FP32 on the perturbation
+state.  Checked against the plain FP64 form (itself bit for bit the oracle and
+the reference's operators on these meshes, tests/test_amr_gpu.py) on the
+refined fixtures (2D N = 4, 64 mortar faces; 3D N = 3, 48 faces of 2 x 2
+mortars):
+
+  * tendency at a perturbed developed state: relative L2 per variable <= 1e-5;
+  * 40 SSP-RK3 steps from the fixture's state: relative L2 per conserved
+    variable and in theta' <= 1e-5, mass drift <= 1e-12 relative;
+  * with the artificial viscosity, and for the precision form's adjoint, the
+    refined mesh is refused (UNSUPPORTED).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import VARS, load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+CASES = ["amr_g3_4n3", "amr_c1_2d_visc"]
+
+
+def solver(case):
+    import nebulasem_gb300 as ng
+    g = load_golden(case)
+    s = ng.Solver(g, dt=float(g["dt"]), viscosity=0.0)
+    u0 = [g[f"u0_{v}"] for v in VARS]
+    return s, u0, g
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mortar_tendency_vs_fp64(case):
+    import nebulasem_gb300 as ng
+    s, u0, g = solver(case)
+    s.set_state(u0)
+    s.step(5, prec=ng.FP64)
+    u = s.get_state()
+    rng = np.random.default_rng(3)
+    n = len(u[0])
+    for v, sc in enumerate((1e-3, 1e-1, 1e-1, 1e-1, 1e-1)):
+        u[v] = u[v] + sc * rng.standard_normal(n)
+    s.set_state(u)
+    L64 = s.tendency(prec=ng.FP64)
+    L32 = s.tendency(prec=ng.MIXED)
+    top = max(np.linalg.norm(x) for x in L64)
+    for a, b, v in zip(L32, L64, VARS):
+        if np.linalg.norm(b) < 1e-8 * top:
+            continue
+        assert rel_l2(a, b) <= TOL, f"{case} {v}: {rel_l2(a, b):.3e}"
+    s.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mortar_trajectory_vs_fp64(case):
+    import nebulasem_gb300 as ng
+    s, u0, g = solver(case)
+    steps = 40
+    out = {}
+    for prec, name in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
+        s.set_state(u0)
+        d0 = s.diagnostics()
+        s.step(steps, prec=prec)
+        out[name] = s.get_state()
+        d1 = s.diagnostics()
+        out[name + "_drift"] = (d1[0] - d0[0]) / d0[0]
+    s.close()
+    ref, got = out["fp64"], out["mixed"]
+    l2 = {v: rel_l2(a, b) for a, b, v in zip(got, ref, VARS)}
+    l2["theta'"] = rel_l2(got[4] / got[0] - 300.0, ref[4] / ref[0] - 300.0)
+    # the measured figures (shown with pytest -s)
+    print(json.dumps({"case": case, "steps": steps, "l2_vs_fp64": l2,
+                      "mass_drift": {t: out[t + "_drift"] for t in ("mixed", "fp64")}}))
+    scale = max(np.linalg.norm(x) for x in ref[1:4])
+    assert scale > 0
+    for a, b, v in zip(got, ref, VARS):
+        assert np.isfinite(a).all(), v
+        if np.linalg.norm(b) < 1e-10 * scale:
+            assert np.linalg.norm(a - b) <= 1e-10 * scale, v
+            continue
+        assert l2[v] <= TOL, f"{case} {v}: {l2[v]:.3e}"
+    assert l2["theta'"] <= TOL
+    for t in ("mixed", "fp64"):
+        assert abs(out[t + "_drift"]) <= 1e-12, (t, out[t + "_drift"])
+
+
+def test_mortar_refusals():
+    import nebulasem_gb300 as ng
+    g = load_golden("amr_c1_2d_visc")
+    n = int(g["meta"][7])
+    s = ng.Solver(g, dt=float(g["dt"]))          # the fixture's viscosity 1.5
+    s.set_state([g[f"u0_{v}"] for v in VARS])
+    with pytest.raises(ng.NsemError) as e:
+        s.tendency(prec=ng.MIXED)
+    assert e.value.status == 5 and "inviscid" in str(e.value)
+    s.close()
+    s, u0, g = solver("amr_g3_4n3")
+    s.set_state(u0)
+    with pytest.raises(ng.NsemError) as e:
+        s.vjp([np.zeros(len(u0[0]))] * 5, prec=ng.MIXED)
+    assert e.value.status == 5 and "non-conforming" in str(e.value)
+    s.close()
