@@ -58,8 +58,8 @@ typedef enum {
     NSEM_FP64 = 0,  /* plain form: FP64 throughout, reference operation order */
     NSEM_MIXED = 1  /* precision form: FP32 bulk, FP64 background/RK/sums;
                        hex meshes with N+1 = 4, 5, 8 (2D: 4, 5) and SYMMETRY
-                       walls; inclined or curved elements and 2:1 mortar
-                       faces in inviscid runs */
+                       walls, any metric, 2:1 mortar faces on axis-aligned
+                       elements */
 } nsem_precision;
 
 typedef enum {

@@ -80,7 +80,8 @@ struct StageArgs {
     const float* bg;           /* [layers][4][NP]                          */
     const float* Jg;           /* general geometry: [e][10][NP] Jinv cV (9), 1/cV */
     const float* Fn;           /* general geometry: [e][3][NFS] outward weighted normals */
-    const float* MF;           /* mortar faces: [n_mf][5][nfmax] outward face values */
+    const float* MF;           /* mortar faces: [n_mf][9][nfmax] outward face values (0-4),
+                                  viscous runs' gradient face terms (5-8) */
     int nfmax;
     int64_t n_elem;
     float dt, gamma, gR, g[3];
@@ -376,7 +377,7 @@ k_mixed_stage(StageArgs a) {
         if (nb <= -2) {
             /* a face on a 2:1 mortar: its outward values come from the
              * mortar kernels */
-            const float* mf = a.MF + (int64_t)(-2 - nb) * 5 * a.nfmax + face_local<NX, NY, NZ>(t);
+            const float* mf = a.MF + (int64_t)(-2 - nb) * 9 * a.nfmax + face_local<NX, NY, NZ>(t);
 #pragma unroll
             for (int v = 0; v < 5; v++) oth[v] = __ldg(mf + v * a.nfmax);
         }
@@ -629,18 +630,20 @@ k_mixed_stage(StageArgs a) {
  * momentum).  Both elements of a face evaluate it with fN and -fN: the
  * results are exact negatives, the face conserves exactly.
  * ------------------------------------------------------------------------ */
-template <int NX, int NY, int NZ>
+template <int NX, int NY, int NZ, bool VISC = false>
 struct GenSmem {
     using G = Geo<NX, NY, NZ>;
     static constexpr int NP = G::NP, NFS = G::NFS;
     /* floats: contravariant fluxes G4[3][NP] (x4) + G1[3][NP]; own values
-     * P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS]; line table */
+     * P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS]; line table;
+     * viscous runs: the nodes' gradients GV[12][NP] */
     static constexpr int OFF_G1 = 12 * NP;
     static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 16 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
     static constexpr int OFF_Q = OFF_FF1 + NFS;
-    static constexpr size_t BYTES = sizeof(float) * (OFF_Q + QTAB);
+    static constexpr int OFF_GV = OFF_Q + QTAB;
+    static constexpr size_t BYTES = sizeof(float) * (OFF_GV + (VISC ? 12 * NP : 0));
 };
 
 /* normal flux F(x).fN of one side */
@@ -655,13 +658,13 @@ __device__ __forceinline__ void normal_flux(const float* m, const float* u, floa
     f1 = __fmul_rn(mn, th);
 }
 
-template <int NX, int NY, int NZ, int STAGE>
+template <int NX, int NY, int NZ, int STAGE, bool VISC>
 __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK,
-                                  (min_blocks(NX == 8 ? 2 : 6, Geo<NX, NY, NZ>::BLOCK,
-                                              GenSmem<NX, NY, NZ>::BYTES)))
+                                  (min_blocks(NX == 8 ? 2 : (VISC ? 4 : 6), Geo<NX, NY, NZ>::BLOCK,
+                                              GenSmem<NX, NY, NZ, VISC>::BYTES)))
 k_mixed_stage_gen(StageArgs a) {
     using G = Geo<NX, NY, NZ>;
-    using SM = GenSmem<NX, NY, NZ>;
+    using SM = GenSmem<NX, NY, NZ, VISC>;
     constexpr int NP = G::NP;
     constexpr int NFS = G::NFS;
     extern __shared__ float4 gen4[];
@@ -672,12 +675,14 @@ k_mixed_stage_gen(StageArgs a) {
     float4* sFF4 = reinterpret_cast<float4*>(smem + SM::OFF_FF4);
     float* sFF1 = smem + SM::OFF_FF1;
     float* sQ = smem + SM::OFF_Q;
+    float* sGV = smem + SM::OFF_GV;     /* viscous runs: [12][NP] */
     const int t = threadIdx.x;
     const int64_t e = blockIdx.x;
     constexpr bool has_din = STAGE >= 2;
     for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
 
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0}, jin[9], icv = 0.0f;
+    float gown[12];
     double u64[5];
     if (t < NP) {
         const float* sp = a.S + e * 5 * NP + t;
@@ -703,6 +708,14 @@ k_mixed_stage_gen(StageArgs a) {
 #pragma unroll
             for (int v = 0; v < 5; v++) u64[v] = __ldg(u + v * NP);
         }
+        if constexpr (VISC) {
+            const float* gr = a.G + e * 12 * NP + t;
+#pragma unroll
+            for (int c = 0; c < 12; c++) {
+                gown[c] = __ldg(gr + c * NP);
+                sGV[c * NP + t] = gown[c];
+            }
+        }
     }
     FaceSlot fs{};
     int32_t nb = -1;
@@ -726,6 +739,23 @@ k_mixed_stage_gen(StageArgs a) {
             for (int c = 0; c < 4; c++) bgo[c] = __ldg(bg + c * NP);
         }
     }
+    /* viscous runs: the neighbour's gradients along the face node's normal,
+     * sum_c d_r U_c n_c (r = 0..2) and sum_c d_c theta n_c */
+    float gno[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if constexpr (VISC) {
+        if (t < NFS && nb >= 0) {
+            const float* gr = a.G + (int64_t)nb * 12 * NP + fs.lo;
+            float g[12];
+#pragma unroll
+            for (int c = 0; c < 12; c++) g[c] = __ldg(gr + c * NP);
+            /* the same association as the own side's (exact antisymmetry) */
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+                gno[r] = __fmaf_rn(g[tidx(r, 0)], fno[0],
+                                   __fmaf_rn(g[tidx(r, 1)], fno[1], __fmul_rn(g[tidx(r, 2)], fno[2])));
+            gno[3] = __fmaf_rn(g[9], fno[0], __fmaf_rn(g[10], fno[1], __fmul_rn(g[11], fno[2])));
+        }
+    }
 
     /* phase 1: primitives and contravariant fluxes */
     if (t < NP) {
@@ -740,9 +770,20 @@ k_mixed_stage_gen(StageArgs a) {
             const float j0 = jin[tidx(0, d)], j1 = jin[tidx(1, d)], j2 = jin[tidx(2, d)];
             const float Mt = fmaf(own[1], j0, fmaf(own[2], j1, own[3] * j2));
             const float ut = fmaf(p.u[0], j0, fmaf(p.u[1], j1, p.u[2] * j2));
-            sG4[d * NP + t] = make_float4(Mt, fmaf(own[1], ut, p.pp * j0), fmaf(own[2], ut, p.pp * j1),
-                                          fmaf(own[3], ut, p.pp * j2));
-            sG1[d * NP + t] = Mt * p.th;
+            float4 g4 = make_float4(Mt, fmaf(own[1], ut, p.pp * j0), fmaf(own[2], ut, p.pp * j1),
+                                    fmaf(own[3], ut, p.pp * j2));
+            float g1 = Mt * p.th;
+            if constexpr (VISC) {
+                /* - mu d_r U_c (momentum r, direction c) and - (mu / Pr) d_c theta
+                 * along the metric column, mu = rho nu */
+                const float mu = p.rho * a.nu, mt = p.rho * a.nu_pr;
+                g4.y = fmaf(-mu, fmaf(gown[tidx(0, 0)], j0, fmaf(gown[tidx(0, 1)], j1, gown[tidx(0, 2)] * j2)), g4.y);
+                g4.z = fmaf(-mu, fmaf(gown[tidx(1, 0)], j0, fmaf(gown[tidx(1, 1)], j1, gown[tidx(1, 2)] * j2)), g4.z);
+                g4.w = fmaf(-mu, fmaf(gown[tidx(2, 0)], j0, fmaf(gown[tidx(2, 1)], j1, gown[tidx(2, 2)] * j2)), g4.w);
+                g1 = fmaf(-mt, fmaf(gown[9], j0, fmaf(gown[10], j1, gown[11] * j2)), g1);
+            }
+            sG4[d * NP + t] = g4;
+            sG1[d * NP + t] = g1;
         }
     }
     __syncthreads();
@@ -769,6 +810,27 @@ k_mixed_stage_gen(StageArgs a) {
             const float dmn = __fmaf_rn(dm0, fno[0], __fmaf_rn(dm1, fno[1], __fmul_rn(dm2, fno[2])));
             const float jr = __fmul_rn(nrm, __fsub_rn(oth[0], P0.x));
             const float jt = __fmul_rn(nrm, __fsub_rn(oth[4], P1.x));
+            if constexpr (VISC) {
+                /* both sides' viscous normal fluxes, - mu (grad U) n and
+                 * - (mu / Pr) (grad theta) . n, each side's from its own node */
+                const float* gs = sGV + fs.la;
+                float sn[4];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+                    sn[r] = __fmaf_rn(gs[tidx(r, 0) * NP], fno[0],
+                                      __fmaf_rn(gs[tidx(r, 1) * NP], fno[1], __fmul_rn(gs[tidx(r, 2) * NP], fno[2])));
+                sn[3] = __fmaf_rn(gs[9 * NP], fno[0], __fmaf_rn(gs[10 * NP], fno[1], __fmul_rn(gs[11 * NP], fno[2])));
+                const float mus = __fmul_rn(P1.y, a.nu), muo = __fmul_rn(q.rho, a.nu);
+                const float mts = __fmul_rn(P1.y, a.nu_pr), mto = __fmul_rn(q.rho, a.nu_pr);
+                A4.y = __fmaf_rn(-mus, sn[0], A4.y);
+                A4.z = __fmaf_rn(-mus, sn[1], A4.z);
+                A4.w = __fmaf_rn(-mus, sn[2], A4.w);
+                A1 = __fmaf_rn(-mts, sn[3], A1);
+                B4.y = __fmaf_rn(-muo, gno[0], B4.y);
+                B4.z = __fmaf_rn(-muo, gno[1], B4.z);
+                B4.w = __fmaf_rn(-muo, gno[2], B4.w);
+                B1 = __fmaf_rn(-mto, gno[3], B1);
+            }
             o4.x = __fmaf_rn(-lam, jr, __fmul_rn(0.5f, __fadd_rn(A4.x, B4.x)));
             o4.y = __fmaf_rn(-lam, __fmul_rn(en[0], dmn), __fmul_rn(0.5f, __fadd_rn(A4.y, B4.y)));
             o4.z = __fmaf_rn(-lam, __fmul_rn(en[1], dmn), __fmul_rn(0.5f, __fadd_rn(A4.z, B4.z)));
@@ -908,7 +970,11 @@ struct MortarMxArgs {
     float* dC;             /* [5][n_ms] */
     const int32_t* ent;    /* [n_mf][nfmax][4] */
     const float* coef;     /* [n_mf][nfmax][4] */
-    float* MF;             /* [n_mf][5][nfmax] */
+    float* MF;             /* [n_mf][9][nfmax]: outward values (0-4), gradient terms (5-8) */
+    float* gF;             /* viscous: [4][n_ms] */
+    float* gC;             /* viscous: [4][n_ms] */
+    const int32_t* node;   /* viscous: [n_mf][nfmax] */
+    const float* gs;       /* viscous: [n_mf][nfmax][4] */
     int64_t n_ms, n_mf;
     int nfmax, np;
 };
@@ -933,7 +999,15 @@ __device__ __forceinline__ Pt mx_node(const StageArgs& a, int np, int64_t node, 
     return pointwise(x, b, a.eos, a.gamma, a.gR);
 }
 
-template <bool HAS_DIN>
+/* the node's gradients (viscous runs) */
+__device__ __forceinline__ void mx_grad(const StageArgs& a, int np, int64_t node, float* g) {
+    const int64_t e = node / np;
+    const float* gr = a.G + e * 12 * np + (node - e * np);
+#pragma unroll
+    for (int c = 0; c < 12; c++) g[c] = __ldg(gr + c * np);
+}
+
+template <bool HAS_DIN, bool VISC>
 __global__ void __launch_bounds__(128) k_mx_mortar_flux(StageArgs a, MortarMxArgs m) {
     const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ms >= m.n_ms) return;
@@ -953,8 +1027,15 @@ __global__ void __launch_bounds__(128) k_mx_mortar_flux(StageArgs a, MortarMxArg
     for (int na = 0; na < Na; na++)
         for (int nb = 0; nb < Nb; nb++) {
             float x[5];
-            const Pt p = mx_node<HAS_DIN>(a, m.np, (int64_t)base + na * sa + nb * sb, x);
+            const int64_t cn = (int64_t)base + na * sa + nb * sb;
+            const Pt p = mx_node<HAS_DIN>(a, m.np, cn, x);
             const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+            float g[12], mu = 0.0f, mt = 0.0f;
+            if constexpr (VISC) {
+                mx_grad(a, m.np, cn, g);
+                mu = p.rho * a.nu;
+                mt = p.rho * a.nu_pr;
+            }
             q[0] = fmaf(w, p.umag, q[0]);
             q[1] = fmaf(w, p.c, q[1]);
 #pragma unroll
@@ -963,11 +1044,17 @@ __global__ void __launch_bounds__(128) k_mx_mortar_flux(StageArgs a, MortarMxArg
 #pragma unroll
             for (int r = 0; r < 3; r++)
 #pragma unroll
-                for (int c = 0; c < 3; c++)
-                    q[6 + tidx(r, c)] = fmaf(w, fmaf(x[1 + r], p.u[c], r == c ? p.pp : 0.0f),
-                                             q[6 + tidx(r, c)]);
+                for (int c = 0; c < 3; c++) {
+                    float fl = fmaf(x[1 + r], p.u[c], r == c ? p.pp : 0.0f);
+                    if constexpr (VISC) fl = fmaf(-mu, g[tidx(r, c)], fl);
+                    q[6 + tidx(r, c)] = fmaf(w, fl, q[6 + tidx(r, c)]);
+                }
 #pragma unroll
-            for (int c = 0; c < 3; c++) q[15 + c] = fmaf(w, x[1 + c] * p.th, q[15 + c]);
+            for (int c = 0; c < 3; c++) {
+                float fl = x[1 + c] * p.th;
+                if constexpr (VISC) fl = fmaf(-mt, g[9 + c], fl);
+                q[15 + c] = fmaf(w, fl, q[15 + c]);
+            }
             q[18] = fmaf(w, x[4], q[18]);
         }
     const float* g = m.mf + ms;
@@ -989,6 +1076,15 @@ __global__ void __launch_bounds__(128) k_mx_mortar_flux(StageArgs a, MortarMxArg
 #pragma unroll
     for (int c = 0; c < 3; c++) f[15 + c] = xf[1 + c] * pf.th;
     f[18] = xf[4];
+    if constexpr (VISC) {
+        float g[12];
+        mx_grad(a, m.np, fld(MX_FINE), g);
+        const float mu = pf.rho * a.nu, mt = pf.rho * a.nu_pr;
+#pragma unroll
+        for (int c = 0; c < 9; c++) f[6 + c] = fmaf(-mu, g[c], f[6 + c]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[15 + c] = fmaf(-mt, g[9 + c], f[15 + c]);
+    }
     /* side 1 (FO) and side 2 (FN) of the slot; the normal points 1 -> 2 */
     const bool fine1 = fld(MX_FINE_C1) != 0;
     const float* A = fine1 ? f : q;
@@ -1065,7 +1161,106 @@ __global__ void __launch_bounds__(128) k_mx_mortar_fill(MortarMxArgs m) {
         for (int v = 0; v < 5; v++) acc[v] = fmaf(c, __ldg(src + v * m.n_ms + ms), acc[v]);
     }
 #pragma unroll
-    for (int v = 0; v < 5; v++) m.MF[(f * 5 + v) * m.nfmax + r] = acc[v];
+    for (int v = 0; v < 5; v++) m.MF[(f * 9 + v) * m.nfmax + r] = acc[v];
+}
+
+/* Viscous runs: the gradients' face values on mortars (the plain form's
+ * k_seg_mortar_gcds / k_seg_mortar_ggather in FP32).  Per mortar slot
+ * cds = (fine + interpolated coarse) / 2 of U and theta - T0; per slot its
+ * sub-face's values projected onto the slot's coarse node; per node of an
+ * element face on a mortar sum_entries gs (value - own), which the gradient
+ * kernel lifts like a conforming face's cds - own. */
+__device__ __forceinline__ float4 mx_ut(const StageArgs& a, const float* x, int np, int64_t node) {
+    const int64_t e = node / np;
+    const float rref = __ldg(a.bg + (int64_t)__ldg(a.layer + e) * 4 * np + (node - e * np));
+    const float inv = rcp_nr(__fadd_rn(rref, x[0]));
+    return make_float4(__fmul_rn(x[1], inv), __fmul_rn(x[2], inv), __fmul_rn(x[3], inv),
+                       __fmul_rn(__fmaf_rn(-a.T0, x[0], x[4]), inv));
+}
+
+template <bool HAS_DIN>
+__device__ __forceinline__ float4 mx_node_ut(const StageArgs& a, int np, int64_t node) {
+    const int64_t e = node / np;
+    const int l = (int)(node - e * np);
+    float x[5];
+    const float* s = a.S + e * 5 * np + l;
+#pragma unroll
+    for (int v = 0; v < 5; v++) x[v] = __ldg(s + v * np);
+    if constexpr (HAS_DIN) {
+        const float* d = a.Din + e * 5 * np + l;
+#pragma unroll
+        for (int v = 0; v < 5; v++) x[v] = __fadd_rn(x[v], __ldg(d + v * np));
+    }
+    return mx_ut(a, x, np, node);
+}
+
+template <bool HAS_DIN>
+__global__ void __launch_bounds__(128) k_mx_mortar_gcds(StageArgs a, MortarMxArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    const int base = fld(MX_BASE), sa = fld(MX_SA), sb = fld(MX_SB), Na = fld(MX_NA),
+              Nb = fld(MX_NB), ia = fld(MX_IA), ib = fld(MX_IB);
+    const float* Pa = m.psiR + fld(MX_TA) * MAXN * MAXN;
+    const float* Pb = m.psiR + fld(MX_TB) * MAXN * MAXN;
+    float4 I = make_float4(0, 0, 0, 0);
+    for (int na = 0; na < Na; na++)
+        for (int nb = 0; nb < Nb; nb++) {
+            const float4 v = mx_node_ut<HAS_DIN>(a, m.np, (int64_t)base + na * sa + nb * sb);
+            const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+            I.x = fmaf(w, v.x, I.x); I.y = fmaf(w, v.y, I.y);
+            I.z = fmaf(w, v.z, I.z); I.w = fmaf(w, v.w, I.w);
+        }
+    const float4 f = mx_node_ut<HAS_DIN>(a, m.np, fld(MX_FINE));
+    m.gF[ms] = 0.5f * f.x + 0.5f * I.x;
+    m.gF[m.n_ms + ms] = 0.5f * f.y + 0.5f * I.y;
+    m.gF[2 * m.n_ms + ms] = 0.5f * f.z + 0.5f * I.z;
+    m.gF[3 * m.n_ms + ms] = 0.5f * f.w + 0.5f * I.w;
+}
+
+__global__ void __launch_bounds__(128) k_mx_mortar_ggather(MortarMxArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    const int Na = fld(MX_NA), Nb = fld(MX_NB), na = fld(MX_IA), nb = fld(MX_IB),
+              first = fld(MX_FIRST);
+    const float* Pa = m.psiC + fld(MX_TA) * MAXN * MAXN;
+    const float* Pb = m.psiC + fld(MX_TB) * MAXN * MAXN;
+    float o[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int ja = 0; ja < Na; ja++)
+        for (int jb = 0; jb < Nb; jb++) {
+            const int64_t s2 = first + ja * Nb + jb;
+            const float w = __ldg(Pa + ja * Na + na) * __ldg(Pb + jb * Nb + nb);
+#pragma unroll
+            for (int c = 0; c < 4; c++) o[c] = fmaf(w, __ldg(m.gF + c * m.n_ms + s2), o[c]);
+        }
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.gC[c * m.n_ms + ms] = o[c];
+}
+
+template <bool HAS_DIN>
+__global__ void __launch_bounds__(128) k_mx_mortar_gfill(StageArgs a, MortarMxArgs m) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= m.n_mf * m.nfmax) return;
+    const int64_t f = id / m.nfmax;
+    const int r = (int)(id - f * m.nfmax);
+    const int32_t node = __ldg(m.node + id);
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (node >= 0) {
+        const float4 o = mx_node_ut<HAS_DIN>(a, m.np, node);
+        const float own[4] = {o.x, o.y, o.z, o.w};
+        for (int q = 0; q < 4; q++) {
+            const int32_t en = __ldg(m.ent + id * 4 + q);
+            if (en < 0) break;
+            const float w = __ldg(m.gs + id * 4 + q);
+            const float* src = (en & MX_COARSE) ? m.gC : m.gF;
+            const int64_t ms = en & (MX_COARSE - 1);
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[c] = fmaf(w, __ldg(src + c * m.n_ms + ms) - own[c], acc[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.MF[(f * 9 + 5 + c) * m.nfmax + r] = acc[c];
 }
 
 /* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
@@ -1143,7 +1338,12 @@ k_mixed_grad(StageArgs a) {
     if (t < NP) sV[t] = prim_ut(own, bgs0);
     __syncthreads();
 
-    if (t < NFS) {
+    if (t < NFS && nb <= -2) {
+        /* a face on a 2:1 mortar: the projected values from the mortar kernels */
+        const float* gf = a.MF + ((int64_t)(-2 - nb) * 9 + 5) * a.nfmax + face_local<NX, NY, NZ>(t);
+        sD[t] = make_float4(__ldg(gf), __ldg(gf + a.nfmax), __ldg(gf + 2 * a.nfmax),
+                            __ldg(gf + 3 * a.nfmax));
+    } else if (t < NFS) {
         const float4 S = sV[fs.la];
         float4 c;
         if (nb >= 0) {
@@ -1232,6 +1432,171 @@ k_mixed_grad(StageArgs a) {
         out[tidx(r, 1) * NP] = d[r].y;
         out[tidx(r, 2) * NP] = d[r].z;
         out[(9 + r) * NP] = d[r].w;
+    }
+}
+
+/* General geometry (inclined, curved elements): the same gradients with the
+ * node's full metric and the face nodes' normals (k_seg_grad_vol's strong
+ * form, field.h:3327-3360):
+ *   d_r q = (1/cV) [ sum_d (Jinv cV)[r][d] sum_m D_d[a_d][m] q_m
+ *                    + sum_faces fN_out[r] (cds(q) - q) ],
+ * the SYMMETRY ghost velocity along the face node's unit normal on walls. */
+template <int NX, int NY, int NZ, int SIN>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK)
+k_mixed_grad_gen(StageArgs a) {
+    using G = Geo<NX, NY, NZ>;
+    constexpr int NP = G::NP;
+    constexpr int NFS = G::NFS;
+    constexpr bool has_din = SIN >= 2;
+    extern __shared__ float4 ggsm4[];
+    float4* sV = ggsm4;                                             /* [NP]  U, theta - T0 */
+    float4* sD = ggsm4 + NP;                                        /* [NFS] cds - own */
+    float* sDg = reinterpret_cast<float*>(ggsm4 + NP + NFS);       /* line tables */
+    const int t = threadIdx.x;
+    const int64_t e = blockIdx.x;
+
+    float own[5], bgs0 = 0.0f, jin[9], icv = 0.0f;
+    if (t < NP) {
+        const float* s = a.S + e * 5 * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) own[v] = __ldg(s + v * NP);
+        if (has_din) {
+            const float* d = a.Din + e * 5 * NP + t;
+#pragma unroll
+            for (int v = 0; v < 5; v++) own[v] = __fadd_rn(own[v], __ldg(d + v * NP));
+        }
+        bgs0 = __ldg(a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t);
+        const float* jg = a.Jg + e * 10 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
+        icv = __ldg(jg + 9 * NP);
+    }
+    FaceSlot fs{};
+    int32_t nb = -1;
+    float oth[5], bgo0 = 0.0f, fno[3] = {0, 0, 0};
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+#pragma unroll
+        for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);
+        if (nb >= 0) {
+            const float* s = a.S + (int64_t)nb * 5 * NP + fs.lo;
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(s + v * NP);
+            if (has_din) {
+                const float* d = a.Din + (int64_t)nb * 5 * NP + fs.lo;
+#pragma unroll
+                for (int v = 0; v < 5; v++) oth[v] = __fadd_rn(oth[v], __ldg(d + v * NP));
+            }
+            bgo0 = __ldg(a.bg + (int64_t)__ldg(a.layer + nb) * 4 * NP + fs.lo);
+        }
+    }
+    for (int q = t; q < QTAB; q += G::BLOCK) sDg[q] = __ldg(a.Dg + q);
+
+    const float T0 = a.T0;
+    auto prim_ut = [T0](const float* s, float rref) {
+        const float inv = rcp_nr(__fadd_rn(rref, s[0]));
+        return make_float4(__fmul_rn(s[1], inv), __fmul_rn(s[2], inv), __fmul_rn(s[3], inv),
+                           __fmul_rn(__fmaf_rn(-T0, s[0], s[4]), inv));
+    };
+    if (t < NP) sV[t] = prim_ut(own, bgs0);
+    __syncthreads();
+
+    if (t < NFS) {
+        const float4 S = sV[fs.la];
+        float4 c;
+        if (nb >= 0) {
+            const float4 O = prim_ut(oth, bgo0);
+            c = make_float4(0.5f * S.x + 0.5f * O.x, 0.5f * S.y + 0.5f * O.y,
+                            0.5f * S.z + 0.5f * O.z, 0.5f * S.w + 0.5f * O.w);
+        } else {
+            /* wall ghost: SYMMETRY velocity (tangential part rescaled to |U|),
+             * NEUMANN theta */
+            const float nrm = safe_sqrt(fno[0] * fno[0] + fno[1] * fno[1] + fno[2] * fno[2]);
+            const float inrm = nrm > 0.0f ? 1.0f / nrm : 0.0f;
+            const float en[3] = {fno[0] * inrm, fno[1] * inrm, fno[2] * inrm};
+            const float un = S.x * en[0] + S.y * en[1] + S.z * en[2];
+            float r0 = S.x - un * en[0], r1 = S.y - un * en[1], r2 = S.z - un * en[2];
+            const float mr = safe_sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+            if (mr > 1e-7f) {
+                const float sc = safe_sqrt(S.x * S.x + S.y * S.y + S.z * S.z) / mr;
+                r0 *= sc; r1 *= sc; r2 *= sc;
+            }
+            c = make_float4(r0, r1, r2, S.w);
+        }
+        sD[t] = make_float4(c.x - S.x, c.y - S.y, c.z - S.z, c.w - S.w);
+    }
+    __syncthreads();
+
+    if (t >= NP) return;
+    const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+    /* derivatives along the reference directions */
+    float4 d[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) d[r] = make_float4(0, 0, 0, 0);
+    {
+        const float* q = sDg + i * QS;
+#pragma unroll
+        for (int m = 0; m < NX; m++) {
+            const float4 v = sV[(m * NY + j) * NZ + k];
+            d[0].x = fmaf(q[m], v.x, d[0].x); d[0].y = fmaf(q[m], v.y, d[0].y);
+            d[0].z = fmaf(q[m], v.z, d[0].z); d[0].w = fmaf(q[m], v.w, d[0].w);
+        }
+    }
+    if constexpr (G::HAS_Y) {
+        const float* q = sDg + MAXN * QS + j * QS;
+#pragma unroll
+        for (int m = 0; m < NY; m++) {
+            const float4 v = sV[(i * NY + m) * NZ + k];
+            d[1].x = fmaf(q[m], v.x, d[1].x); d[1].y = fmaf(q[m], v.y, d[1].y);
+            d[1].z = fmaf(q[m], v.z, d[1].z); d[1].w = fmaf(q[m], v.w, d[1].w);
+        }
+    }
+    {
+        const float* q = sDg + 2 * MAXN * QS + k * QS;
+#pragma unroll
+        for (int m = 0; m < NZ; m++) {
+            const float4 v = sV[(i * NY + j) * NZ + m];
+            d[2].x = fmaf(q[m], v.x, d[2].x); d[2].y = fmaf(q[m], v.y, d[2].y);
+            d[2].z = fmaf(q[m], v.z, d[2].z); d[2].w = fmaf(q[m], v.w, d[2].w);
+        }
+    }
+    /* physical components: sum_d (Jinv cV)[r][d] d_d, then the face terms */
+    float4 g[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const float j0 = jin[tidx(r, 0)], j1 = jin[tidx(r, 1)], j2 = jin[tidx(r, 2)];
+        g[r] = make_float4(fmaf(j0, d[0].x, fmaf(j1, d[1].x, j2 * d[2].x)),
+                           fmaf(j0, d[0].y, fmaf(j1, d[1].y, j2 * d[2].y)),
+                           fmaf(j0, d[0].z, fmaf(j1, d[1].z, j2 * d[2].z)),
+                           fmaf(j0, d[0].w, fmaf(j1, d[1].w, j2 * d[2].w)));
+    }
+    auto lift = [&](int slot) {
+        const float4 f = sD[slot];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const float n = __ldg(a.Fn + (e * 3 + r) * NFS + slot);
+            g[r].x = fmaf(n, f.x, g[r].x); g[r].y = fmaf(n, f.y, g[r].y);
+            g[r].z = fmaf(n, f.z, g[r].z); g[r].w = fmaf(n, f.w, g[r].w);
+        }
+    };
+    {
+        const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
+        if (sx >= 0) lift(sx);
+        if constexpr (G::HAS_Y) {
+            const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
+            if (sy >= 0) lift(sy);
+        }
+        const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
+        if (sz >= 0) lift(sz);
+    }
+    float* out = a.Gout + e * 12 * NP + t;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        out[tidx(r, 0) * NP] = icv * g[r].x;
+        out[tidx(r, 1) * NP] = icv * g[r].y;
+        out[tidx(r, 2) * NP] = icv * g[r].z;
+        out[(9 + r) * NP] = icv * g[r].w;
     }
 }
 
@@ -1372,14 +1737,24 @@ template <int NX, int NY, int NZ>
 int launch_stage(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
     using G = Geo<NX, NY, NZ>;
     if (c.gen) {
-        /* general geometry (inviscid) */
-        constexpr size_t SMEM = GenSmem<NX, NY, NZ>::BYTES;
+        /* general geometry */
         const unsigned grid = (unsigned)a.n_elem;
+        if (c.visc) {
+            constexpr size_t SMEM = GenSmem<NX, NY, NZ, true>::BYTES;
+            switch (stage) {
+                case 0: k_mixed_stage_gen<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 1: k_mixed_stage_gen<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 2: k_mixed_stage_gen<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                default: k_mixed_stage_gen<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            }
+            return (int)cudaGetLastError();
+        }
+        constexpr size_t SMEM = GenSmem<NX, NY, NZ>::BYTES;
         switch (stage) {
-            case 0: k_mixed_stage_gen<NX, NY, NZ, 0><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-            case 1: k_mixed_stage_gen<NX, NY, NZ, 1><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-            case 2: k_mixed_stage_gen<NX, NY, NZ, 2><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-            default: k_mixed_stage_gen<NX, NY, NZ, 3><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            case 0: k_mixed_stage_gen<NX, NY, NZ, 0, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            case 1: k_mixed_stage_gen<NX, NY, NZ, 1, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            case 2: k_mixed_stage_gen<NX, NY, NZ, 2, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            default: k_mixed_stage_gen<NX, NY, NZ, 3, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
         }
         return (int)cudaGetLastError();
     }
@@ -1387,13 +1762,23 @@ int launch_stage(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg
         launch_stage_tc<NX, NY, NZ, false>(a, stage, st, c);
         return (int)cudaGetLastError();
     }
+    launch_stage_tc<NX, NY, NZ, true>(a, stage, st, c);
+    return (int)cudaGetLastError();
+}
+
+/* viscous runs: the gradients of the stage state, before the stage */
+template <int NX, int NY, int NZ>
+int launch_grad(const StageArgs& a, int stage, cudaStream_t st, const LaunchCfg& c) {
+    using G = Geo<NX, NY, NZ>;
     const unsigned grid = (unsigned)a.n_elem;
     constexpr size_t gs = grad_smem<NX, NY, NZ>();
-    if (stage <= 1) k_mixed_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, gs, st>>>(a);
-    else k_mixed_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a);
-    int e = (int)cudaGetLastError();
-    if (e) return e;
-    launch_stage_tc<NX, NY, NZ, true>(a, stage, st, c);
+    if (c.gen) {
+        if (stage <= 1) k_mixed_grad_gen<NX, NY, NZ, 1><<<grid, G::BLOCK, gs, st>>>(a);
+        else k_mixed_grad_gen<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a);
+    } else {
+        if (stage <= 1) k_mixed_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, gs, st>>>(a);
+        else k_mixed_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, gs, st>>>(a);
+    }
     return (int)cudaGetLastError();
 }
 
@@ -1449,12 +1834,19 @@ int prepare_stage(LaunchCfg* c) {
     }
     {
         constexpr int GS = (int)GenSmem<NX, NY, NZ>::BYTES;
+        constexpr int GSV = (int)GenSmem<NX, NY, NZ, true>::BYTES;
         const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
         if (!e && GS > 48 * 1024) {
-            e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 0>, at, GS);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 1>, at, GS);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 2>, at, GS);
-            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 3>, at, GS);
+            e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 0, false>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 1, false>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 2, false>, at, GS);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 3, false>, at, GS);
+        }
+        if (!e && GSV > 48 * 1024) {
+            e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 0, true>, at, GSV);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 1, true>, at, GSV);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 2, true>, at, GSV);
+            if (!e) e = (int)cudaFuncSetAttribute(k_mixed_stage_gen<NX, NY, NZ, 3, true>, at, GSV);
         }
     }
     constexpr size_t gs = grad_smem<NX, NY, NZ>();
@@ -1462,6 +1854,8 @@ int prepare_stage(LaunchCfg* c) {
     if (!e && gs > 48 * 1024) {
         e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 1>, at, (int)gs);
         if (!e) e = (int)cudaFuncSetAttribute(k_mixed_grad<NX, NY, NZ, 2>, at, (int)gs);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_grad_gen<NX, NY, NZ, 1>, at, (int)gs);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_grad_gen<NX, NY, NZ, 2>, at, (int)gs);
     }
     return e;
 }
@@ -1494,6 +1888,15 @@ int dispatch_stage(int nx, int ny, int nz, const StageArgs& a, int stage, cudaSt
     if (nx == A && ny == B && nz == C) return launch_stage<A, B, C>(a, stage, st, c);
     NSEM_MIXED_DIMS(NSEM_DISP)
 #undef NSEM_DISP
+    return (int)cudaErrorNotSupported;
+}
+
+int dispatch_grad(int nx, int ny, int nz, const StageArgs& a, int stage, cudaStream_t st,
+                  const LaunchCfg& c) {
+#define NSEM_DISPG(A, B, C) \
+    if (nx == A && ny == B && nz == C) return launch_grad<A, B, C>(a, stage, st, c);
+    NSEM_MIXED_DIMS(NSEM_DISPG)
+#undef NSEM_DISPG
     return (int)cudaErrorNotSupported;
 }
 
@@ -1538,15 +1941,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         }
         for (int d = 0; d < 3; d++) J[d * ne + e] = (float)diag0[d];
     }
-    if (gen && dev.nu != 0.0) {
-        err = "precision form on inclined or curved elements is inviscid";
-        return NSEM_UNSUPPORTED;
-    }
     /* non-conforming (2:1) faces: the fine sub-faces' ids */
     std::vector<int8_t> on_mortar(m->n_mortar > 0 ? m->n_face : 0, 0);
     if (m->n_mortar > 0) {
-        if (gen || dev.nu != 0.0) {
-            err = "precision form on refined meshes: inviscid runs on axis-aligned elements";
+        if (gen) {
+            err = "precision form on refined meshes: axis-aligned elements";
             return NSEM_UNSUPPORTED;
         }
         for (int32_t q = 0; q < m->n_mortar; q++) on_mortar[m->mortar[4 * (size_t)q]] = 1;
@@ -1720,8 +2119,8 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
      * per element face on a mortar its node entries */
     std::vector<int32_t> mxi[MX_FIELDS];
     std::vector<float> mxf[8];
-    std::vector<int32_t> ment;
-    std::vector<float> mcoef;
+    std::vector<int32_t> ment, mnode;
+    std::vector<float> mcoef, mgs;
     std::map<int64_t, int32_t> mf_of;
     const int nfmax = std::max(nfx, std::max(nfy, nfz));
     if (m->n_mortar > 0) {
@@ -1742,12 +2141,20 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             nbr[(int64_t)face * ne + e] = -2 - id;
             ment.resize((size_t)(id + 1) * nfmax * 4, -1);
             mcoef.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
+            mgs.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
+            mnode.resize((size_t)(id + 1) * nfmax, -1);
             return id;
         };
-        auto add = [&](int32_t mf, int r, int32_t code, double c) -> bool {
+        /* an entry of a face node: the mortar slot, the flux coefficient and
+         * the gradient weight */
+        auto add = [&](int32_t mf, int r, int64_t node, int32_t code, double c, double g) -> bool {
+            mnode[(size_t)mf * nfmax + r] = (int32_t)node;
             for (int q = 0; q < 4; q++) {
                 const size_t at = ((size_t)mf * nfmax + r) * 4 + q;
-                if (ment[at] < 0) { ment[at] = code; mcoef[at] = (float)c; return true; }
+                if (ment[at] < 0) {
+                    ment[at] = code; mcoef[at] = (float)c; mgs[at] = (float)g;
+                    return true;
+                }
             }
             return false;
         };
@@ -1829,10 +2236,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                     mxf[7].push_back((float)((ir - rref_h[fnode]) * dev.T0));
                     int c[3];
                     loc(fnode, c);
-                    bool ok = add(mf_f, in_face(dir_f, c), ms, (fm == 1 ? 1.0 : -1.0) * scale(fnode, dir_f));
+                    const double sf = scale(fnode, dir_f), sc = scale(cnode, fix);
+                    bool ok = add(mf_f, in_face(dir_f, c), fnode, ms, (fm == 1 ? 1.0 : -1.0) * sf, mg * sf);
                     loc(cnode, c);
-                    ok = ok && add(mf_c, in_face(fix, c), ms | MX_COARSE,
-                                   (fm == 2 ? 1.0 : -1.0) * scale(cnode, fix));
+                    ok = ok && add(mf_c, in_face(fix, c), cnode, ms | MX_COARSE,
+                                   (fm == 2 ? 1.0 : -1.0) * sc, mg * sc);
                     if (!ok) {
                         err = "precision form: more than four mortar entries on a face node";
                         return NSEM_UNSUPPORTED;
@@ -1870,10 +2278,12 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             }
         }
         const std::vector<float> scratch15(15 * mb->n_ms, 0.0f), scratch5(5 * mb->n_ms, 0.0f),
-            mfv(5 * mb->n_mf * nfmax, 0.0f);
+            scratch4(4 * mb->n_ms, 0.0f), mfv(9 * mb->n_mf * nfmax, 0.0f);
         if (!up(&mb->mx_i, mi) || !up(&mb->mx_f, mf) || !up(&mb->mx_psi, psi) ||
             !up(&mb->mx_F, scratch15) || !up(&mb->mx_d, scratch5) || !up(&mb->mx_dC, scratch5) ||
-            !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv)) {
+            !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv) ||
+            !up(&mb->mx_gF, scratch4) || !up(&mb->mx_gC, scratch4) || !up(&mb->mf_node, mnode) ||
+            !up(&mb->mf_gs, mgs)) {
             err = "precision form: device allocation failed";
             return NSEM_NO_MEMORY;
         }
@@ -1965,7 +2375,7 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
     return a;
 }
 
-int launch_mortars(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+MortarMxArgs mortar_args(const NsemMixedBuf* mb) {
     MortarMxArgs m{};
     m.mi = mb->mx_i;
     m.mf = mb->mx_f;
@@ -1981,22 +2391,59 @@ int launch_mortars(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaSt
     m.n_mf = mb->n_mf;
     m.nfmax = mb->nfmax;
     m.np = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    m.gF = mb->mx_gF;
+    m.gC = mb->mx_gC;
+    m.node = mb->mf_node;
+    m.gs = mb->mf_gs;
+    return m;
+}
+
+/* the mortar kernels of the stage's fluxes */
+int launch_mortars(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+    const MortarMxArgs m = mortar_args(mb);
     const unsigned gs = (unsigned)((mb->n_ms + 127) / 128);
-    if (stage >= 2)
-        k_mx_mortar_flux<true><<<gs, 128, 0, st>>>(a, m);
-    else
-        k_mx_mortar_flux<false><<<gs, 128, 0, st>>>(a, m);
+    if (mb->visc) {
+        if (stage >= 2) k_mx_mortar_flux<true, true><<<gs, 128, 0, st>>>(a, m);
+        else k_mx_mortar_flux<false, true><<<gs, 128, 0, st>>>(a, m);
+    } else {
+        if (stage >= 2) k_mx_mortar_flux<true, false><<<gs, 128, 0, st>>>(a, m);
+        else k_mx_mortar_flux<false, false><<<gs, 128, 0, st>>>(a, m);
+    }
     k_mx_mortar_proj<<<gs, 128, 0, st>>>(m);
     k_mx_mortar_fill<<<(unsigned)((mb->n_mf * mb->nfmax + 127) / 128), 128, 0, st>>>(m);
     return (int)cudaGetLastError();
 }
 
+/* the mortar kernels of the gradients' face values (viscous runs) */
+int launch_mortar_grads(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+    const MortarMxArgs m = mortar_args(mb);
+    const unsigned gs = (unsigned)((mb->n_ms + 127) / 128);
+    const unsigned gf = (unsigned)((mb->n_mf * mb->nfmax + 127) / 128);
+    if (stage >= 2) k_mx_mortar_gcds<true><<<gs, 128, 0, st>>>(a, m);
+    else k_mx_mortar_gcds<false><<<gs, 128, 0, st>>>(a, m);
+    k_mx_mortar_ggather<<<gs, 128, 0, st>>>(m);
+    if (stage >= 2) k_mx_mortar_gfill<true><<<gf, 128, 0, st>>>(a, m);
+    else k_mx_mortar_gfill<false><<<gf, 128, 0, st>>>(a, m);
+    return (int)cudaGetLastError();
+}
+
 int launch_args(const NsemMixedBuf* mb, const StageArgs& a, int stage, cudaStream_t st) {
+    LaunchCfg c{};
+    c.visc = mb->visc;
+    c.gen = mb->gen;
+    if (mb->visc) {
+        /* the stage state's gradients first (their mortar face values before them) */
+        if (mb->n_ms > 0) {
+            const int e = launch_mortar_grads(mb, a, stage, st);
+            if (e) return e;
+        }
+        const int e = dispatch_grad(mb->npd[0], mb->npd[1], mb->npd[2], a, stage, st, c);
+        if (e) return e;
+    }
     if (mb->n_ms > 0) {
         const int e = launch_mortars(mb, a, stage, st);
         if (e) return e;
     }
-    LaunchCfg c{};
     c.visc = mb->visc;
     c.tc = mb->tc;
     c.persist = mb->persist;

@@ -55,7 +55,13 @@ struct NsemMixedBuf {
     int nfmax = 0;                /* nodes per face (largest direction)     */
     int32_t* mf_ent = nullptr;    /* [n_mf][nfmax][4] mortar slot (| 1<<30: coarse value), -1 */
     float* mf_coef = nullptr;     /* [n_mf][nfmax][4] sign / (cV J_d / w_end) */
-    float* MF = nullptr;          /* [n_mf][5][nfmax] outward face values   */
+    float* MF = nullptr;          /* [n_mf][9][nfmax] outward face values (0-4) and,
+                                     viscous runs, gradient face terms (5-8) */
+    /* viscous runs: the gradients' face values on mortars */
+    float* mx_gF = nullptr;       /* [4][n_ms] cds(U), cds(theta - T0) per slot */
+    float* mx_gC = nullptr;       /* [4][n_ms] their projection onto the coarse node */
+    int32_t* mf_node = nullptr;   /* [n_mf][nfmax] the element face's node  */
+    float* mf_gs = nullptr;       /* [n_mf][nfmax][4] |fN| / (cV J_d / w_end) */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */

@@ -2,8 +2,8 @@
 non-conforming faces) on the GPU through the C ABI, against the oracle's
 mortar restatement (itself bit-identical to the unmodified euler binary,
 tests/test_amr_oracle.py).  With the correctly rounded pow in the oracle the
-GPU result is bit for bit; the precision form refuses the viscous refined
-mesh (it steps refined meshes in inviscid runs, tests/test_mixed_mortar.py)."""
+GPU result is bit for bit (the precision form on these meshes:
+tests/test_mixed_mortar.py)."""
 import numpy as np
 import pytest
 
@@ -38,11 +38,6 @@ def test_amr_segregated_gpu_bitwise_vs_oracle(case):
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     assert rel(r, g["fldN_rho"]) <= 1e-14
     assert rel(t, g["fldN_T"]) <= 1e-10
-    if float(g["viscosity"]) != 0.0:
-        # the precision form steps refined meshes in inviscid runs only
-        with pytest.raises(ng.NsemError) as e:
-            s.step(1, prec=ng.MIXED)
-        assert "inviscid" in str(e.value)
     s.close()
 
 

@@ -58,7 +58,9 @@ def test_srtb_example_run(tmp_path, fixture):
     oracle's bit for bit (correctly rounded pow) and follows the unmodified
     euler binary's fields; the geometry is the binary's to the bit, and the C
     library's pow, off by an ulp on some arguments, leaves ~1e-15 in rho and
-    ~1e-10 in the velocity of this flow from rest after 100 steps."""
+    ~1e-10 in the velocity of this flow from rest after 100 steps.  On the
+    curved blocks the precision form's SSP-RK3 run stays within 1e-5 of the
+    FP64 form's."""
     g = load_golden(fixture)
     steps = int(g["nsteps"])
     curved = {"curved": str(g["curved"])} if "curved" in g else {}
@@ -89,9 +91,18 @@ def test_srtb_example_run(tmp_path, fixture):
     assert rel_l2(out["T"][kd, 0], g["fldN_T"][kg]) < 1e-10
     assert rel_l2(out["U"][kd], g["fldN_U"].reshape(-1, 3)[kg]) < 2e-9
     if "curved" in g:
-        # the precision form on curved elements is inviscid
-        r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
-        assert r.returncode == 1 and "inviscid" in r.stderr, r.stderr
+        ssprk3_precision_vs_fp64(d)
+
+
+def ssprk3_precision_vs_fp64(d):
+    """SSP-RK3 through the driver on the case: the precision form's fields
+    against the FP64 form's, relative L2 <= 1e-5 (rho, U, theta')."""
+    run_driver(d, "--scheme", "ssprk3", "--print-every", "50")
+    ref = fields(d, 1, ("rho", "U", "T"))
+    run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", "--print-every", "50")
+    got = fields(d, 1, ("rho", "U", "T"))
+    for f in ("rho", "U", "T"):
+        assert rel_l2(got[f], ref[f]) <= 1e-5, (f, rel_l2(got[f], ref[f]))
 
 
 def test_segregated_run_follows_euler_binary(tmp_path):
@@ -204,8 +215,7 @@ def test_restart_from_written_fields(tmp_path):
 def test_inclined_block_run(tmp_path):
     """A block rotated by 30 degrees (full, non-diagonal metric): the FP64
     forms through the driver are the oracle's bit for bit; the precision form
-    on inclined elements is inviscid and refuses this viscous run with a
-    message."""
+    (general-geometry kernels, viscous) within 1e-5 of the FP64 form."""
     steps = 20
     d = make_case(tmp_path, "c1_2d", dt=0.005, steps=steps, viscosity=1.5)
     rotate_case_z(d, 30.0)
@@ -222,8 +232,7 @@ def test_inclined_block_run(tmp_path):
     assert np.array_equal(out["rho"][:, 0], rho)
     assert np.array_equal(out["U"].reshape(-1), np.asarray(U).reshape(-1))
     assert np.array_equal(out["T"][:, 0], T)
-    r = run_driver(d, "--scheme", "ssprk3", "--prec", "mixed", check=False)
-    assert r.returncode == 1 and "inviscid" in r.stderr, r.stderr
+    ssprk3_precision_vs_fp64(d)
 
 
 def test_text_output_and_high_order(tmp_path):

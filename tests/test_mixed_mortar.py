@@ -1,12 +1,16 @@
 """Precision form on adaptively refined meshes (2:1 mortar faces; the
-reference refines with its `prepare -refine`), inviscid runs.
+reference refines with its `prepare -refine`), with and without the
+artificial viscosity of diffusion YES.
 
 Per stage, mortar kernels interpolate the coarse side's face quantities onto
 each mortar slot with psiRef (the fine side reads its own node), form the
 Rusanov flux vectors there, project them back onto the coarse face's nodes
 with psiCor, and hand both sides' outward values to the stage kernel -- the
 plain form's mortar treatment (field.h:2019-2248) in FP32 on the perturbation
-state.  Checked against the plain FP64 form (itself bit for bit the oracle and
+state; viscous runs give the gradients' face values the same treatment (the
+coarse side's U and theta interpolated into the face averages, which are
+projected back onto the coarse nodes) and carry -mu grad U, -(mu/Pr) grad theta
+in the interpolated flux tensors.  Checked against the plain FP64 form (itself bit for bit the oracle and
 the reference's operators on these meshes, tests/test_amr_gpu.py) on the
 refined fixtures (2D N = 4, 64 mortar faces; 3D N = 3, 48 faces of 2 x 2
 mortars):
@@ -14,8 +18,8 @@ mortars):
   * tendency at a perturbed developed state: relative L2 per variable <= 1e-5;
   * 40 SSP-RK3 steps from the fixture's state: relative L2 per conserved
     variable and in theta' <= 1e-5, mass drift <= 1e-12 relative;
-  * with the artificial viscosity, and for the precision form's adjoint, the
-    refined mesh is refused (UNSUPPORTED).
+  * each mesh inviscid and with viscosity 1.5 (the 2D fixture's value);
+  * the precision form's adjoint refuses the refined mesh (UNSUPPORTED).
 """
 import json
 
@@ -28,20 +32,22 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-5
 CASES = ["amr_g3_4n3", "amr_c1_2d_visc"]
+VISC = [0.0, 1.5]
 
 
-def solver(case):
+def solver(case, visc=0.0):
     import nebulasem_gb300 as ng
     g = load_golden(case)
-    s = ng.Solver(g, dt=float(g["dt"]), viscosity=0.0)
+    s = ng.Solver(g, dt=float(g["dt"]), viscosity=visc)
     u0 = [g[f"u0_{v}"] for v in VARS]
     return s, u0, g
 
 
+@pytest.mark.parametrize("visc", VISC)
 @pytest.mark.parametrize("case", CASES)
-def test_mortar_tendency_vs_fp64(case):
+def test_mortar_tendency_vs_fp64(case, visc):
     import nebulasem_gb300 as ng
-    s, u0, g = solver(case)
+    s, u0, g = solver(case, visc)
     s.set_state(u0)
     s.step(5, prec=ng.FP64)
     u = s.get_state()
@@ -56,14 +62,15 @@ def test_mortar_tendency_vs_fp64(case):
     for a, b, v in zip(L32, L64, VARS):
         if np.linalg.norm(b) < 1e-8 * top:
             continue
-        assert rel_l2(a, b) <= TOL, f"{case} {v}: {rel_l2(a, b):.3e}"
+        assert rel_l2(a, b) <= TOL, f"{case} nu={visc} {v}: {rel_l2(a, b):.3e}"
     s.close()
 
 
+@pytest.mark.parametrize("visc", VISC)
 @pytest.mark.parametrize("case", CASES)
-def test_mortar_trajectory_vs_fp64(case):
+def test_mortar_trajectory_vs_fp64(case, visc):
     import nebulasem_gb300 as ng
-    s, u0, g = solver(case)
+    s, u0, g = solver(case, visc)
     steps = 40
     out = {}
     for prec, name in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
@@ -78,7 +85,7 @@ def test_mortar_trajectory_vs_fp64(case):
     l2 = {v: rel_l2(a, b) for a, b, v in zip(got, ref, VARS)}
     l2["theta'"] = rel_l2(got[4] / got[0] - 300.0, ref[4] / ref[0] - 300.0)
     # the measured figures (shown with pytest -s)
-    print(json.dumps({"case": case, "steps": steps, "l2_vs_fp64": l2,
+    print(json.dumps({"case": case, "viscosity": visc, "steps": steps, "l2_vs_fp64": l2,
                       "mass_drift": {t: out[t + "_drift"] for t in ("mixed", "fp64")}}))
     scale = max(np.linalg.norm(x) for x in ref[1:4])
     assert scale > 0
@@ -87,22 +94,14 @@ def test_mortar_trajectory_vs_fp64(case):
         if np.linalg.norm(b) < 1e-10 * scale:
             assert np.linalg.norm(a - b) <= 1e-10 * scale, v
             continue
-        assert l2[v] <= TOL, f"{case} {v}: {l2[v]:.3e}"
+        assert l2[v] <= TOL, f"{case} nu={visc} {v}: {l2[v]:.3e}"
     assert l2["theta'"] <= TOL
     for t in ("mixed", "fp64"):
         assert abs(out[t + "_drift"]) <= 1e-12, (t, out[t + "_drift"])
 
 
-def test_mortar_refusals():
+def test_mortar_adjoint_refused():
     import nebulasem_gb300 as ng
-    g = load_golden("amr_c1_2d_visc")
-    n = int(g["meta"][7])
-    s = ng.Solver(g, dt=float(g["dt"]))          # the fixture's viscosity 1.5
-    s.set_state([g[f"u0_{v}"] for v in VARS])
-    with pytest.raises(ng.NsemError) as e:
-        s.tendency(prec=ng.MIXED)
-    assert e.value.status == 5 and "inviscid" in str(e.value)
-    s.close()
     s, u0, g = solver("amr_g3_4n3")
     s.set_state(u0)
     with pytest.raises(ng.NsemError) as e:
