@@ -87,6 +87,7 @@ CONV_PLAN = {
     "c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0)),
     "g3_2": ("g3_2", 1.0, 30, (6.0, -4.0, 5.0)),
     "amr_c1_2d": ("c1_2d", 0.5, 40, (5.0, 0.0, 3.0), 0.3),
+    "amr_g3_4n3": ("g3_4n3", 1.0, 30, (6.0, -4.0, 5.0), 0.2),
 }
 
 # the advection-leveque example made small: n x n elements, order, dt, steps

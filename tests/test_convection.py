@@ -11,7 +11,7 @@ from conftest import load_golden
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case", ["conv_c1_2d", "conv_g3_2", "conv_amr_c1_2d"])
+@pytest.mark.parametrize("case", ["conv_c1_2d", "conv_g3_2", "conv_amr_c1_2d", "conv_amr_g3_4n3"])
 def test_convection_gpu_bitwise_vs_reference(case):
     import nebulasem_gb300 as ng
     g = load_golden(case)

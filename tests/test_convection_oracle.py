@@ -9,7 +9,7 @@ import oracle
 from conftest import load_golden
 
 
-@pytest.mark.parametrize("case", ["conv_c1_2d", "conv_g3_2", "conv_amr_c1_2d"])
+@pytest.mark.parametrize("case", ["conv_c1_2d", "conv_g3_2", "conv_amr_c1_2d", "conv_amr_g3_4n3"])
 def test_convection_oracle_matches_reference_binary(case):
     g = load_golden(case)
     m = oracle.OracleMesh(g)
