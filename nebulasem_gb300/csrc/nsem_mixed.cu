@@ -51,6 +51,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <string>
 #include <vector>
@@ -91,6 +92,11 @@ struct StageArgs {
     uint32_t* status;
 };
 
+/* rows per element face of the mortar face buffer: the 5 outward values,
+ * then the gradient face terms: 4 (cds - own, axis-aligned elements) or
+ * 12 (fN_out[r] (cds - own)_c, general geometry) */
+constexpr int MF_ROWS = 9, MF_ROWS_GEN = 17;
+
 /* tensor-core flux layout (order 7): a variable's fluxes of one direction
  * F[a][m][b] -- m the node index along the direction, (a, b) the other two
  * (x: (j, k), y: (i, k), z: (i, j)) -- at a * TC_SA + p(m) * 8 + (b ^ s(m)),
@@ -103,6 +109,7 @@ struct StageArgs {
  * m = tg, tg + 4) and the in-place result stores (rows 2 tg, 2 tg + 1). */
 constexpr int TC_SA = 72;
 constexpr int TC_NP = 8 * TC_SA;
+constexpr int TC_QTAB = 3 * 2 * 64;   /* B fragments per direction: high, low; [k][n] */
 
 template <int NX, int NY, int NZ, bool TC = false>
 struct StageSmem {
@@ -119,7 +126,10 @@ struct StageSmem {
     static constexpr int OFF_Q = OFF_FF1 + NFS;
     static constexpr int OFF_META = OFF_Q + QTAB;
     static_assert(OFF_P % 4 == 0 && OFF_FF4 % 4 == 0, "float4 regions must be 16-byte aligned");
-    static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
+    /* tensor-core line sums: the B fragments of Q_d^T pre-split into TF32
+     * high and low parts, [3][2][8][8] words after the metric */
+    static constexpr int OFF_QTC = OFF_META + 4;
+    static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4 + (TC ? TC_QTAB : 0));
     /* persistent kernels: the next element's stage base, increment and
      * background, staged by asynchronous copies while the current element
      * computes */
@@ -294,6 +304,10 @@ k_mixed_stage(StageArgs a) {
     constexpr bool has_din = STAGE >= 2;
     float* sStg = smem + SM::OFF_STG;                             /* [14][NP] (PERSIST) */
     for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
+    if constexpr (TC) {
+        float* sQtc = smem + SM::OFF_QTC;
+        for (int q = t; q < TC_QTAB; q += G::BLOCK) sQtc[q] = __ldg(a.Qg + QTAB + q);
+    }
     auto prefetch = [&](int64_t en, int32_t lay) {
         if (t < NP) {
             const float* s = a.S + en * 5 * NP + t;
@@ -377,7 +391,7 @@ k_mixed_stage(StageArgs a) {
         if (nb <= -2) {
             /* a face on a 2:1 mortar: its outward values come from the
              * mortar kernels */
-            const float* mf = a.MF + (int64_t)(-2 - nb) * 9 * a.nfmax + face_local<NX, NY, NZ>(t);
+            const float* mf = a.MF + (int64_t)(-2 - nb) * MF_ROWS * a.nfmax + face_local<NX, NY, NZ>(t);
 #pragma unroll
             for (int v = 0; v < 5; v++) oth[v] = __ldg(mf + v * a.nfmax);
         }
@@ -479,9 +493,13 @@ k_mixed_stage(StageArgs a) {
             split_tf32(base[TC_SA + oa0], ah[1], al[1]);
             split_tf32(base[oa2], ah[2], al[2]);
             split_tf32(base[TC_SA + oa2], ah[3], al[3]);
-            const float* qd = sQ + d * MAXN * QS + gq * QS;
-            split_tf32(qd[tg], bh0, bl0);
-            split_tf32(qd[tg + 4], bh1, bl1);
+            /* B = Q_d^T, pre-split on the host exactly as split_tf32 would:
+             * rows k = tg, tg + 4 of the high and the low part, column n = gq */
+            const float* qb = smem + SM::OFF_QTC + d * 128 + tg * 8 + gq;
+            bh0 = __float_as_uint(qb[0]);
+            bh1 = __float_as_uint(qb[32]);
+            bl0 = __float_as_uint(qb[64]);
+            bl1 = __float_as_uint(qb[96]);
             float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             mma_tf32(c, al, bh0, bh1);
             mma_tf32(c, ah, bl0, bl1);
@@ -725,6 +743,12 @@ k_mixed_stage_gen(StageArgs a) {
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
 #pragma unroll
         for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);
+        if (nb <= -2) {
+            /* a face on a 2:1 mortar: its outward values from the mortar kernels */
+            const float* mf = a.MF + (int64_t)(-2 - nb) * MF_ROWS_GEN * a.nfmax + face_local<NX, NY, NZ>(t);
+#pragma unroll
+            for (int v = 0; v < 5; v++) oth[v] = __ldg(mf + v * a.nfmax);
+        }
         if (nb >= 0) {
             const float* sp = a.S + (int64_t)nb * 5 * NP + fs.lo;
 #pragma unroll
@@ -798,7 +822,10 @@ k_mixed_stage_gen(StageArgs a) {
         const float en[3] = {__fmul_rn(fno[0], inrm), __fmul_rn(fno[1], inrm), __fmul_rn(fno[2], inrm)};
         float4 o4;
         float o1;
-        if (nb >= 0) {
+        if (nb <= -2) {
+            o4 = make_float4(oth[0], oth[1], oth[2], oth[3]);
+            o1 = oth[4];
+        } else if (nb >= 0) {
             const Pt q = pointwise(oth, bgo, a.eos, a.gamma, a.gR);
             float4 A4, B4;
             float A1, B1;
@@ -971,6 +998,7 @@ struct MortarMxArgs {
     const int32_t* ent;    /* [n_mf][nfmax][4] */
     const float* coef;     /* [n_mf][nfmax][4] */
     float* MF;             /* [n_mf][9][nfmax]: outward values (0-4), gradient terms (5-8) */
+    int rows;              /* MF_ROWS or MF_ROWS_GEN */
     float* gF;             /* viscous: [4][n_ms] */
     float* gC;             /* viscous: [4][n_ms] */
     const int32_t* node;   /* viscous: [n_mf][nfmax] */
@@ -1161,7 +1189,7 @@ __global__ void __launch_bounds__(128) k_mx_mortar_fill(MortarMxArgs m) {
         for (int v = 0; v < 5; v++) acc[v] = fmaf(c, __ldg(src + v * m.n_ms + ms), acc[v]);
     }
 #pragma unroll
-    for (int v = 0; v < 5; v++) m.MF[(f * 9 + v) * m.nfmax + r] = acc[v];
+    for (int v = 0; v < 5; v++) m.MF[(f * m.rows + v) * m.nfmax + r] = acc[v];
 }
 
 /* Viscous runs: the gradients' face values on mortars (the plain form's
@@ -1238,14 +1266,17 @@ __global__ void __launch_bounds__(128) k_mx_mortar_ggather(MortarMxArgs m) {
     for (int c = 0; c < 4; c++) m.gC[c * m.n_ms + ms] = o[c];
 }
 
-template <bool HAS_DIN>
+template <bool HAS_DIN, bool GEN>
 __global__ void __launch_bounds__(128) k_mx_mortar_gfill(StageArgs a, MortarMxArgs m) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= m.n_mf * m.nfmax) return;
     const int64_t f = id / m.nfmax;
     const int r = (int)(id - f * m.nfmax);
     const int32_t node = __ldg(m.node + id);
-    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    constexpr int NA = GEN ? 12 : 4;
+    float acc[NA];
+#pragma unroll
+    for (int c = 0; c < NA; c++) acc[c] = 0.0f;
     if (node >= 0) {
         const float4 o = mx_node_ut<HAS_DIN>(a, m.np, node);
         const float own[4] = {o.x, o.y, o.z, o.w};
@@ -1255,12 +1286,25 @@ __global__ void __launch_bounds__(128) k_mx_mortar_gfill(StageArgs a, MortarMxAr
             const float w = __ldg(m.gs + id * 4 + q);
             const float* src = (en & MX_COARSE) ? m.gC : m.gF;
             const int64_t ms = en & (MX_COARSE - 1);
+            float dv[4];
 #pragma unroll
-            for (int c = 0; c < 4; c++) acc[c] = fmaf(w, __ldg(src + c * m.n_ms + ms) - own[c], acc[c]);
+            for (int c = 0; c < 4; c++) dv[c] = __ldg(src + c * m.n_ms + ms) - own[c];
+            if constexpr (GEN) {
+                /* w the outward sign; the slot's weighted normal per row */
+#pragma unroll
+                for (int rr = 0; rr < 3; rr++) {
+                    const float n = w * __ldg(m.mf + rr * m.n_ms + ms);
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[rr * 4 + c] = fmaf(n, dv[c], acc[rr * 4 + c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[c] = fmaf(w, dv[c], acc[c]);
+            }
         }
     }
 #pragma unroll
-    for (int c = 0; c < 4; c++) m.MF[(f * 9 + 5 + c) * m.nfmax + r] = acc[c];
+    for (int c = 0; c < NA; c++) m.MF[(f * m.rows + 5 + c) * m.nfmax + r] = acc[c];
 }
 
 /* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
@@ -1340,7 +1384,7 @@ k_mixed_grad(StageArgs a) {
 
     if (t < NFS && nb <= -2) {
         /* a face on a 2:1 mortar: the projected values from the mortar kernels */
-        const float* gf = a.MF + ((int64_t)(-2 - nb) * 9 + 5) * a.nfmax + face_local<NX, NY, NZ>(t);
+        const float* gf = a.MF + ((int64_t)(-2 - nb) * MF_ROWS + 5) * a.nfmax + face_local<NX, NY, NZ>(t);
         sD[t] = make_float4(__ldg(gf), __ldg(gf + a.nfmax), __ldg(gf + 2 * a.nfmax),
                             __ldg(gf + 3 * a.nfmax));
     } else if (t < NFS) {
@@ -1502,7 +1546,7 @@ k_mixed_grad_gen(StageArgs a) {
     if (t < NP) sV[t] = prim_ut(own, bgs0);
     __syncthreads();
 
-    if (t < NFS) {
+    if (t < NFS && nb > -2) {
         const float4 S = sV[fs.la];
         float4 c;
         if (nb >= 0) {
@@ -1572,6 +1616,21 @@ k_mixed_grad_gen(StageArgs a) {
                            fmaf(j0, d[0].w, fmaf(j1, d[1].w, j2 * d[2].w)));
     }
     auto lift = [&](int slot) {
+        const FaceSlot f2 = face_slot<NX, NY, NZ>(slot);
+        const int32_t nbf = __ldg(a.nbr + (int64_t)f2.face * a.n_elem + e);
+        if (nbf <= -2) {
+            /* a face on a 2:1 mortar: fN_out[r] (cds - own) summed by the mortar kernels */
+            const float* gf = a.MF + ((int64_t)(-2 - nbf) * MF_ROWS_GEN + 5) * a.nfmax +
+                              face_local<NX, NY, NZ>(slot);
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                g[r].x += __ldg(gf + (4 * r) * a.nfmax);
+                g[r].y += __ldg(gf + (4 * r + 1) * a.nfmax);
+                g[r].z += __ldg(gf + (4 * r + 2) * a.nfmax);
+                g[r].w += __ldg(gf + (4 * r + 3) * a.nfmax);
+            }
+            return;
+        }
         const float4 f = sD[slot];
 #pragma unroll
         for (int r = 0; r < 3; r++) {
@@ -1944,10 +2003,6 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
     /* non-conforming (2:1) faces: the fine sub-faces' ids */
     std::vector<int8_t> on_mortar(m->n_mortar > 0 ? m->n_face : 0, 0);
     if (m->n_mortar > 0) {
-        if (gen) {
-            err = "precision form on refined meshes: axis-aligned elements";
-            return NSEM_UNSUPPORTED;
-        }
         for (int32_t q = 0; q < m->n_mortar; q++) on_mortar[m->mortar[4 * (size_t)q]] = 1;
     }
     /* general geometry: Jinv cV and 1/cV per node, outward weighted normals
@@ -2111,6 +2166,29 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             }
         mb->lift[d] = (float)(1.0 / w[0]);
     }
+    /* order 7: the tensor-core line sums' B fragments, Q_d^T split into TF32
+     * high and low parts as cvt.rna.tf32 does (round to nearest, ties away
+     * from zero, in the magnitude: + 2^12 and the low 13 bits cleared) */
+    if (NX == 8 && NY == 8 && NZ == 8 && !gen) {
+        auto rna = [](float x) {
+            uint32_t b;
+            std::memcpy(&b, &x, 4);
+            b = (b + 0x1000u) & 0xffffe000u;
+            float r;
+            std::memcpy(&r, &b, 4);
+            return r;
+        };
+        std::vector<float> tcb(TC_QTAB, 0.0f);
+        for (int d = 0; d < 3; d++)
+            for (int k = 0; k < 8; k++)
+                for (int n = 0; n < 8; n++) {
+                    const float q = qtab[d * MAXN * QS + n * QS + k];   /* B[k][n] = Q[n][k] */
+                    const float hi = rna(q);
+                    tcb[d * 128 + k * 8 + n] = hi;
+                    tcb[d * 128 + 64 + k * 8 + n] = rna(q - hi);
+                }
+        qtab.insert(qtab.end(), tcb.begin(), tcb.end());
+    }
 
 
     /* non-conforming faces: per mortar slot (entries in order, (ia, ib)
@@ -2236,11 +2314,16 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                     mxf[7].push_back((float)((ir - rref_h[fnode]) * dev.T0));
                     int c[3];
                     loc(fnode, c);
-                    const double sf = scale(fnode, dir_f), sc = scale(cnode, fix);
-                    bool ok = add(mf_f, in_face(dir_f, c), fnode, ms, (fm == 1 ? 1.0 : -1.0) * sf, mg * sf);
+                    /* general geometry: the stage kernel lifts F.n itself (1/cV
+                     * in its update) and the gradient kernel the normal-weighted
+                     * terms, so both weights are the outward sign only */
+                    const double sf = gen ? 1.0 : scale(fnode, dir_f), sc = gen ? 1.0 : scale(cnode, fix);
+                    const double gf = gen ? (fm == 1 ? 1.0 : -1.0) : mg * sf;
+                    const double gc = gen ? (fm == 2 ? 1.0 : -1.0) : mg * sc;
+                    bool ok = add(mf_f, in_face(dir_f, c), fnode, ms, (fm == 1 ? 1.0 : -1.0) * sf, gf);
                     loc(cnode, c);
                     ok = ok && add(mf_c, in_face(fix, c), cnode, ms | MX_COARSE,
-                                   (fm == 2 ? 1.0 : -1.0) * sc, mg * sc);
+                                   (fm == 2 ? 1.0 : -1.0) * sc, gc);
                     if (!ok) {
                         err = "precision form: more than four mortar entries on a face node";
                         return NSEM_UNSUPPORTED;
@@ -2278,7 +2361,8 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             }
         }
         const std::vector<float> scratch15(15 * mb->n_ms, 0.0f), scratch5(5 * mb->n_ms, 0.0f),
-            scratch4(4 * mb->n_ms, 0.0f), mfv(9 * mb->n_mf * nfmax, 0.0f);
+            scratch4(4 * mb->n_ms, 0.0f),
+            mfv((size_t)(gen ? MF_ROWS_GEN : MF_ROWS) * mb->n_mf * nfmax, 0.0f);
         if (!up(&mb->mx_i, mi) || !up(&mb->mx_f, mf) || !up(&mb->mx_psi, psi) ||
             !up(&mb->mx_F, scratch15) || !up(&mb->mx_d, scratch5) || !up(&mb->mx_dC, scratch5) ||
             !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv) ||
@@ -2395,6 +2479,7 @@ MortarMxArgs mortar_args(const NsemMixedBuf* mb) {
     m.gC = mb->mx_gC;
     m.node = mb->mf_node;
     m.gs = mb->mf_gs;
+    m.rows = mb->gen ? MF_ROWS_GEN : MF_ROWS;
     return m;
 }
 
@@ -2422,8 +2507,13 @@ int launch_mortar_grads(const NsemMixedBuf* mb, const StageArgs& a, int stage, c
     if (stage >= 2) k_mx_mortar_gcds<true><<<gs, 128, 0, st>>>(a, m);
     else k_mx_mortar_gcds<false><<<gs, 128, 0, st>>>(a, m);
     k_mx_mortar_ggather<<<gs, 128, 0, st>>>(m);
-    if (stage >= 2) k_mx_mortar_gfill<true><<<gf, 128, 0, st>>>(a, m);
-    else k_mx_mortar_gfill<false><<<gf, 128, 0, st>>>(a, m);
+    if (mb->gen) {
+        if (stage >= 2) k_mx_mortar_gfill<true, true><<<gf, 128, 0, st>>>(a, m);
+        else k_mx_mortar_gfill<false, true><<<gf, 128, 0, st>>>(a, m);
+    } else {
+        if (stage >= 2) k_mx_mortar_gfill<true, false><<<gf, 128, 0, st>>>(a, m);
+        else k_mx_mortar_gfill<false, false><<<gf, 128, 0, st>>>(a, m);
+    }
     return (int)cudaGetLastError();
 }
 

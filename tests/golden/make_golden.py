@@ -78,6 +78,8 @@ SEG_PLAN = {
 AMR_PLAN = {
     "c1_2d_visc": ("c1_2d", 0.005, 20, 1.5, 0.3),
     "g3_4n3": ("g3_4n3", 0.005, 10, 0.0, 0.2),
+    # the block under the cosine hill, refined (curved and non-conforming)
+    "hill_2d_visc": ("c1_2d", 0.005, 20, 1.5, 0.3, "hill"),
 }
 
 # fixture -> (case, dt, steps, wind[, refinement threshold]) for the
@@ -197,9 +199,11 @@ def make_amr_case(name, ref_bin, tmp):
     of that mesh (with its non-conforming faces and 2:1 tables) and initial
     state, and the unmodified euler binary's fields after the steps."""
     from nebulasem_gb300.fields import read_field
-    base, dt, nsteps, visc, fmax = AMR_PLAN[name]
+    base, dt, nsteps, visc, fmax = AMR_PLAN[name][:5]
+    curved = AMR_PLAN[name][5] if len(AMR_PLAN[name]) > 5 else None
     case = os.path.join(tmp, "amr_" + name)
-    write_case(case, dt=dt, steps=nsteps, viscosity=visc, refine=fmax, **CASES[base])
+    write_case(case, dt=dt, steps=nsteps, viscosity=visc, refine=fmax, curved=curved,
+               **CASES[base])
     run([os.path.join(ref_bin, "mesh"), "grid", "-o", "grid_0.bin"], case)
     run([os.path.join(ref_bin, "prepare"), "./controls", "-refine"], case)
     os.makedirs(os.path.join(case, "out"))

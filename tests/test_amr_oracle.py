@@ -16,7 +16,7 @@ import oracle
 from conftest import load_golden
 
 
-@pytest.mark.parametrize("case", ["amr_c1_2d_visc", "amr_g3_4n3"])
+@pytest.mark.parametrize("case", ["amr_c1_2d_visc", "amr_g3_4n3", "amr_hill_2d_visc"])
 def test_amr_oracle_bitwise_vs_euler_binary(case):
     g = load_golden(case)
     n = int(g["meta"][7])
@@ -53,7 +53,7 @@ def test_amr_mesh_shape():
 VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
 
 
-@pytest.mark.parametrize("case", ["amr_c1_2d_visc", "amr_g3_4n3"])
+@pytest.mark.parametrize("case", ["amr_c1_2d_visc", "amr_g3_4n3", "amr_hill_2d_visc"])
 def test_amr_coupled_oracle_bitwise_vs_reference_operators(case):
     """The coupled form on the refined mesh: the oracle's tendency equals the
     reference's own operators (the harness) at the start state, and 5 SSP-RK3

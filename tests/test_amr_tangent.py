@@ -25,7 +25,7 @@ from conftest import load_golden
 pytestmark = pytest.mark.gpu
 
 VARS = ("rho", "rhou", "rhov", "rhow", "rhotheta")
-CASES = ["amr_g3_4n3", "amr_c1_2d_visc"]
+CASES = ["amr_g3_4n3", "amr_c1_2d_visc", "amr_hill_2d_visc"]
 
 
 def dot(a, b):

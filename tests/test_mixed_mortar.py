@@ -31,7 +31,7 @@ from conftest import VARS, load_golden, rel_l2
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-5
-CASES = ["amr_g3_4n3", "amr_c1_2d_visc"]
+CASES = ["amr_g3_4n3", "amr_c1_2d_visc", "amr_hill_2d_visc"]
 VISC = [0.0, 1.5]
 
 
