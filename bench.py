@@ -316,7 +316,15 @@ def stage_profile(args):
         s.close()
         return
     prec = ng.MIXED if args.prec != "fp64" else ng.FP64
-    m, u = workload(args.workload)
+    if args.fixture:
+        # a golden fixture's mesh (e.g. a refined one) and its state u0
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from conftest import VARS, load_golden
+
+        m = load_golden(args.fixture)
+        u = [m[f"u0_{v}"] for v in VARS]
+    else:
+        m, u = workload(args.workload)
     s = ng.Solver(m, dt=args.dt, viscosity=args.viscosity)
     s.set_state(u)
     s.step(3, prec=prec)
