@@ -79,8 +79,7 @@ struct StageArgs {
     const float* G;            /* viscous runs: [e][12][NP] gradients      */
     float* Gout;               /* gradient kernel output                   */
     const float* bg;           /* [layers][4][NP]                          */
-    const float* Jg;           /* general geometry: [e][10][NP] Jinv cV (9), 1/cV
-                                  (curved elements; affine ones: J [e][GEN_EL]) */
+    const float* Jg;           /* general geometry: [e][10][NP] Jinv cV (9), 1/cV */
     const float* Fn;           /* general geometry: [e][3][NFS] outward weighted normals */
     const float* MF;           /* mortar faces: [n_mf][9][nfmax] outward face values (0-4),
                                   viscous runs' gradient face terms (5-8) */
@@ -97,8 +96,6 @@ struct StageArgs {
  * then the gradient face terms: 4 (cds - own, axis-aligned elements) or
  * 12 (fN_out[r] (cds - own)_c, general geometry) */
 constexpr int MF_ROWS = 9, MF_ROWS_GEN = 17;
-/* general geometry: per element [vol, Jinv (9), unused] (vol 0: curved) */
-constexpr int GEN_EL = 11;
 
 /* tensor-core flux layout (order 7): a variable's fluxes of one direction
  * F[a][m][b] -- m the node index along the direction, (a, b) the other two
@@ -720,20 +717,10 @@ k_mixed_stage_gen(StageArgs a) {
         const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t;
 #pragma unroll
         for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
-        /* affine elements (vol > 0): Jinv per element, cV = vol W[node];
-         * curved ones: Jinv cV and 1/cV per node */
-        const float vol = __ldg(a.J + e * GEN_EL);
-        if (vol > 0.0f) {
-            const float cv = vol * __ldg(a.Qg + QTAB + t);
+        const float* jg = a.Jg + e * 10 * NP + t;
 #pragma unroll
-            for (int c = 0; c < 9; c++) jin[c] = __ldg(a.J + e * GEN_EL + 1 + c) * cv;
-            icv = 1.0f / cv;
-        } else {
-            const float* jg = a.Jg + e * 10 * NP + t;
-#pragma unroll
-            for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
-            icv = __ldg(jg + 9 * NP);
-        }
+        for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
+        icv = __ldg(jg + 9 * NP);
         if constexpr (STAGE == 3) {
             const double* u = a.U + e * 5 * NP + t;
 #pragma unroll
@@ -1523,20 +1510,10 @@ k_mixed_grad_gen(StageArgs a) {
             for (int v = 0; v < 5; v++) own[v] = __fadd_rn(own[v], __ldg(d + v * NP));
         }
         bgs0 = __ldg(a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t);
-        /* affine elements (vol > 0): Jinv per element, cV = vol W[node];
-         * curved ones: Jinv cV and 1/cV per node */
-        const float vol = __ldg(a.J + e * GEN_EL);
-        if (vol > 0.0f) {
-            const float cv = vol * __ldg(a.Qg + QTAB + t);
+        const float* jg = a.Jg + e * 10 * NP + t;
 #pragma unroll
-            for (int c = 0; c < 9; c++) jin[c] = __ldg(a.J + e * GEN_EL + 1 + c) * cv;
-            icv = 1.0f / cv;
-        } else {
-            const float* jg = a.Jg + e * 10 * NP + t;
-#pragma unroll
-            for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
-            icv = __ldg(jg + 9 * NP);
-        }
+        for (int c = 0; c < 9; c++) jin[c] = __ldg(jg + c * NP);
+        icv = __ldg(jg + 9 * NP);
     }
     FaceSlot fs{};
     int32_t nb = -1;
@@ -2189,37 +2166,6 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             }
         mb->lift[d] = (float)(1.0 / w[0]);
     }
-    /* general geometry: the node weight products W = w_i w_j w_k / 8 after the
-     * line tables, and per element [vol, Jinv] where the element is affine
-     * (Jinv the same at every node, cV = vol W), else vol = 0 */
-    std::vector<float> jel;
-    if (gen) {
-        std::vector<double> W(NP);
-        for (int64_t a = 0; a < NP; a++) {
-            const int i = (int)(a / (NY * NZ)), j = (int)((a / NZ) % NY), k = (int)(a % NZ);
-            W[a] = wdir[0][i] * wdir[1][j] * wdir[2][k] / 8.0;
-        }
-        jel.assign((size_t)ne * GEN_EL, 0.0f);
-        int64_t n_aff = 0;
-        for (int64_t e = 0; e < ne; e++) {
-            const double* J0 = m->Jinv + 9 * (e * NP);
-            const double vol = m->cV[e * NP] / W[0];
-            double sc = 0.0;
-            for (int c = 0; c < 9; c++) sc = std::max(sc, std::fabs(J0[c]));
-            bool aff = vol > 0.0;
-            for (int64_t a = 0; a < NP && aff; a++) {
-                const double* Ja = m->Jinv + 9 * (e * NP + a);
-                for (int c = 0; c < 9 && aff; c++) aff = std::fabs(Ja[c] - J0[c]) <= 1e-9 * sc;
-                aff = aff && std::fabs(m->cV[e * NP + a] - vol * W[a]) <= 1e-9 * vol * W[a];
-            }
-            if (!aff) continue;
-            n_aff++;
-            jel[(size_t)e * GEN_EL] = (float)vol;
-            for (int c = 0; c < 9; c++) jel[(size_t)e * GEN_EL + 1 + c] = (float)J0[c];
-        }
-        for (int64_t a = 0; a < NP; a++) qtab.push_back((float)W[a]);
-        mb->n_affine = n_aff;
-    }
     /* order 7: the tensor-core line sums' B fragments, Q_d^T split into TF32
      * high and low parts as cvt.rna.tf32 does (round to nearest, ties away
      * from zero, in the magnitude: + 2^12 and the low 13 bits cleared) */
@@ -2393,7 +2339,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
         allocs->push_back((void*)*ptr);
         return cudaMemcpy(*ptr, vec.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
     };
-    if (!up(&mb->nbr, nbr) || !up(&mb->J, gen ? jel : J) || !up(&mb->layer, layer) || !up(&mb->bg, bg) ||
+    if (!up(&mb->nbr, nbr) || !up(&mb->J, J) || !up(&mb->layer, layer) || !up(&mb->bg, bg) ||
         !up(&mb->Qg, qtab) || !up(&mb->Dg, dtab) || (gen && (!up(&mb->Jg, Jg) || !up(&mb->Fn, Fn)))) {
         err = "precision form: device allocation failed";
         return NSEM_NO_MEMORY;

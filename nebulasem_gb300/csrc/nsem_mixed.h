@@ -26,9 +26,7 @@ struct NsemMixedBuf {
     float* S[2] = {};             /* FP32 shadow of U (read by the stages)  */
     float* D[2] = {};             /* FP32 stage increments                  */
     int32_t* nbr = nullptr;       /* [6][n_elem] neighbour element, -1 wall */
-    float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h; general
-                                     geometry: [n_elem][11] vol, Jinv (affine elements) */
-    int64_t n_affine = 0;         /* general geometry: affine elements      */
+    float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h        */
     int32_t* layer = nullptr;     /* [n_elem] background layer              */
     float* bg = nullptr;          /* [layers][4][NP] rho_ref, Theta_ref, 1/Theta_ref, p_ref */
     float* Qg = nullptr;          /* line-sum weights Q_d[a][m], row stride MAXN+1 */
