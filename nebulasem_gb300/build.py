@@ -28,6 +28,8 @@ UNITS = [
     ("nsem_fp64.cu", EXACT),
     ("nsem_aux.cu", EXACT),
     ("nsem_mixed.cu", []),
+    ("nsem_mixed_stage.cu", []),
+    ("nsem_mixed_gen.cu", []),
     ("nsem_mixed_adj.cu", []),
     ("nsem_noalloc.cu", EXACT),
     ("nsem_seg.cu", EXACT),

@@ -434,12 +434,11 @@ int prepare_adj() {
     return e;
 }
 
-#define NSEM_ADJ_DIMS(X)  X(5, 5, 5) X(8, 8, 8) X(4, 4, 4) X(5, 1, 5) X(4, 1, 4)
 
 int dispatch_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
     const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
 #define NSEM_ADJ(A, B, C) if (nx == A && ny == B && nz == C) return launch_adj<A, B, C>(a, rs, st);
-    NSEM_ADJ_DIMS(NSEM_ADJ)
+    NSEM_MIXED_DIMS(NSEM_ADJ)
 #undef NSEM_ADJ
     return (int)cudaErrorNotSupported;
 }
@@ -532,7 +531,7 @@ int grid_for(int64_t n) {
 int nsem_mixed_adj_prepare(const NsemMixedBuf* mb) {
     const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
 #define NSEM_PREP(A, B, C) if (nx == A && ny == B && nz == C) return prepare_adj<A, B, C>();
-    NSEM_ADJ_DIMS(NSEM_PREP)
+    NSEM_MIXED_DIMS(NSEM_PREP)
 #undef NSEM_PREP
     return (int)cudaErrorNotSupported;
 }
@@ -555,7 +554,7 @@ int nsem_mixed_layout(const NsemMixedBuf* mb, int dir, const double* const soa[5
         }                                                                               \
         return (int)cudaGetLastError();                                                 \
     }
-    NSEM_ADJ_DIMS(NSEM_LAY)
+    NSEM_MIXED_DIMS(NSEM_LAY)
 #undef NSEM_LAY
     return (int)cudaErrorNotSupported;
 }
@@ -575,7 +574,7 @@ int nsem_mixed_vjp(const NsemDev* dev, NsemMixedBuf* mb, const double* const w[5
         k_soa_to_blk32<A * B * C><<<grid_for(n), 256, 0, st>>>(s, scratch_in, n);       \
         e = (int)cudaGetLastError();                                                    \
     }
-    NSEM_ADJ_DIMS(NSEM_W)
+    NSEM_MIXED_DIMS(NSEM_W)
 #undef NSEM_W
     if (e) return e;
     AdjArgs a = adj_args(dev, mb, 0.0);
@@ -590,7 +589,7 @@ int nsem_mixed_vjp(const NsemDev* dev, NsemMixedBuf* mb, const double* const w[5
         k_blk32_to_soa<A * B * C><<<grid_for(n), 256, 0, st>>>(scratch_out, d, n);      \
         return (int)cudaGetLastError();                                                 \
     }
-    NSEM_ADJ_DIMS(NSEM_G)
+    NSEM_MIXED_DIMS(NSEM_G)
 #undef NSEM_G
     return (int)cudaErrorNotSupported;
 }

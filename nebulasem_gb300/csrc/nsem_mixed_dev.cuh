@@ -20,6 +20,10 @@
 
 #include "nsem_internal.h"
 
+/* the node counts per direction the precision form is built for (the
+ * kernels' dispatch in every translation unit of the form) */
+#define NSEM_MIXED_DIMS(X) X(5, 5, 5) X(8, 8, 8) X(4, 4, 4) X(5, 1, 5) X(4, 1, 4)
+
 namespace nsem_mx {
 
 constexpr int MAXN = NSEM_MAX_NPD;
