@@ -58,8 +58,8 @@ typedef enum {
     NSEM_FP64 = 0,  /* plain form: FP64 throughout, reference operation order */
     NSEM_MIXED = 1  /* precision form: FP32 bulk, FP64 background/RK/sums;
                        hex meshes with N+1 = 4, 5, 8 (2D: 4, 5) and SYMMETRY
-                       walls, any metric, 2:1 mortar faces on axis-aligned
-                       elements */
+                       walls, any metric (axis-aligned, inclined, curved),
+                       2:1 mortar faces on straight or curved elements */
 } nsem_precision;
 
 typedef enum {
