@@ -720,6 +720,8 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                 dtab[d * MAXN * QS + aa * QS + mm] = (float)m->dpsi[d][aa * n + mm];
             }
         mb->lift[d] = (float)(1.0 / w[0]);
+        for (int aa = 0; aa < n && aa < 8; aa++)
+            for (int mm = 0; mm < n && mm < 8; mm++) mb->qc[d][aa][mm] = qtab[d * MAXN * QS + aa * QS + mm];
     }
     /* order 7: the tensor-core line sums' B fragments, Q_d^T split into TF32
      * high and low parts as cvt.rna.tf32 does (round to nearest, ties away
@@ -1004,6 +1006,7 @@ StageArgs base_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
         a.g[c] = (float)dev->g[c];
         a.lift[c] = mb->lift[c];
     }
+    std::memcpy(a.qc, mb->qc, sizeof(a.qc));
     /* binomial coefficients C(gamma, k) of (1 + d)^gamma - 1 */
     double ck = 1.0;
     for (int k = 1; k <= 6; k++) {

@@ -28,6 +28,7 @@ struct NsemMixedBuf {
     int32_t* nbr = nullptr;       /* [6][n_elem] neighbour element, -1 wall */
     float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h        */
     int32_t* layer = nullptr;     /* [n_elem] background layer              */
+    float qc[3][8][8] = {};       /* host copy of the line-sum weights      */
     float* bg = nullptr;          /* [layers][4][NP] rho_ref, Theta_ref, 1/Theta_ref, p_ref */
     float* Qg = nullptr;          /* line-sum weights Q_d[a][m], row stride MAXN+1 */
     float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a), same layout */

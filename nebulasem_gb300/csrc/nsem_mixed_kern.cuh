@@ -43,6 +43,9 @@ struct StageArgs {
     float lift[3];             /* 1 / w_end per direction                  */
     float eos[6];              /* binomial coefficients C(gamma, k), k = 1..6 */
     uint32_t* status;
+    /* line-sum weights Q_d[a][m] as kernel parameters: read with
+     * compile-time indices they are constant-bank operands of the FMAs */
+    float qc[3][8][8];
 };
 
 /* rows per element face of the mortar face buffer: the 5 outward values,

@@ -17,16 +17,14 @@ template <int NX, int NY, int NZ, bool TC = false>
 struct StageSmem {
     using G = Geo<NX, NY, NZ>;
     static constexpr int NP = G::NP, NFS = G::NFS;
-    /* floats: volume fluxes F4[3][NP] (x4) + F1[3][NP] (tensor-core line sums:
-     * F[3][5][TC_NP]); own values P[3][NP] (x4); face fluxes FF4[NFS] (x4) +
-     * FF1[NFS]; Q; metric */
+    /* floats: volume fluxes, line-major per direction [3][n][5][NL] (tensor-core
+     * line sums: F[3][5][TC_NP]); own values P[3][NP] (x4); face fluxes
+     * FF4[NFS] (x4) + FF1[NFS]; metric */
     static constexpr int FLUX = TC ? 15 * TC_NP : 15 * NP;
-    static constexpr int OFF_F1 = 12 * NP;
     static constexpr int OFF_P = (FLUX + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 12 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
-    static constexpr int OFF_Q = OFF_FF1 + NFS;
-    static constexpr int OFF_META = OFF_Q + QTAB;
+    static constexpr int OFF_META = OFF_FF1 + NFS;
     static_assert(OFF_P % 4 == 0 && OFF_FF4 % 4 == 0, "float4 regions must be 16-byte aligned");
     /* tensor-core line sums: the B fragments of Q_d^T pre-split into TF32
      * high and low parts, [3][2][8][8] words after the metric */
@@ -82,6 +80,48 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+/* FP32 line sums as an in-place line transform.  The fluxes of direction D
+ * are kept line-major: variable v at node m along line l (x: l = j NZ + k,
+ * y: l = i NZ + k, z: l = i NY + j) at D 5 NP + m ROW + v NL + l, with NL
+ * lines and ROW = 5 NL.  After the face phase, thread r < ROW takes the
+ * line and variable (v, l) = (r / NL, r % NL) of each direction: it reads
+ * the n values m ROW + r (a warp reads consecutive words), forms
+ * R_a = sum_m Q_D[a][m] F_m with the weights as constant-bank operands, and
+ * writes R_a over F_a.  A node then reads its three R's.  Each flux value
+ * is read once from shared memory instead of once per node of its line. */
+template <int NX, int NY, int NZ, int D>
+struct LineLay {
+    static constexpr int NP = NX * NY * NZ;
+    static constexpr int n = D == 0 ? NX : D == 1 ? NY : NZ;
+    static constexpr int NL = NP / n;
+    static constexpr int ROW = 5 * NL;
+    /* position of variable 0 at node (i, j, k) */
+    __device__ static __forceinline__ int at(int i, int j, int k) {
+        return D * 5 * NP + (D == 0 ? i : D == 1 ? j : k) * ROW +
+               (D == 0 ? j * NZ + k : D == 1 ? i * NZ + k : i * NY + j);
+    }
+};
+
+template <int NX, int NY, int NZ, int D>
+__device__ __forceinline__ void line_transform(float* F, const StageArgs& a, int t) {
+    using LL = LineLay<NX, NY, NZ, D>;
+    constexpr int BLOCK = Geo<NX, NY, NZ>::BLOCK;
+    float* f = F + D * 5 * LL::NP;
+#pragma unroll 1
+    for (int r = t; r < LL::ROW; r += BLOCK) {
+        float in[LL::n];
+#pragma unroll
+        for (int m = 0; m < LL::n; m++) in[m] = f[m * LL::ROW + r];
+#pragma unroll
+        for (int q = 0; q < LL::n; q++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int m = 0; m < LL::n; m++) acc = fmaf(a.qc[D][q][m], in[m], acc);
+            f[q * LL::ROW + r] = acc;
+        }
+    }
+}
+
 /* registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the stage
  * that also carries the FP64 state (measured best on GB300), 6 when viscous */
 #ifndef NSEM_MIXED_MB12
@@ -105,8 +145,8 @@ constexpr int stage_min_blocks() {
 /* phase 2: flux through face node t of direction DIR, seen from the element */
 template <int NX, int NY, int NZ, int DIR, bool VISC, bool TC>
 __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const float* oth,
-                                          const float* bgo, const float* gfo, const float4* sF4,
-                                          const float* sF1, const float4* sP, const StageArgs& a,
+                                          const float* bgo, const float* gfo, const float* sF,
+                                          const float4* sP, const StageArgs& a,
                                           float4& o4, float& o1) {
     constexpr int NP = Geo<NX, NY, NZ>::NP;
     const float sg = fs.side ? 1.0f : -1.0f;   /* outward normal = sg e_DIR */
@@ -117,13 +157,15 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
         float4 A4;
         float A1;
         if constexpr (TC) {
-            const float* f = reinterpret_cast<const float*>(sF4) + DIR * 5 * TC_NP +
+            const float* f = sF + DIR * 5 * TC_NP +
                              tc_idx<DIR>(fs.la >> 6, (fs.la >> 3) & 7, fs.la & 7);
             A4 = make_float4(f[0], f[TC_NP], f[2 * TC_NP], f[3 * TC_NP]);
             A1 = f[4 * TC_NP];
         } else {
-            A4 = sF4[DIR * NP + fs.la];
-            A1 = sF1[DIR * NP + fs.la];
+            using LL = LineLay<NX, NY, NZ, DIR>;
+            const float* f = sF + LL::at(fs.la / (NY * NZ), (fs.la / NZ) % NY, fs.la % NZ);
+            A4 = make_float4(f[0], f[LL::NL], f[2 * LL::NL], f[3 * LL::NL]);
+            A1 = f[4 * LL::NL];
         }
         const Pt q = pointwise(oth, bgo, a.eos, a.gamma, a.gR);
         float g12[12] = {};
@@ -186,18 +228,14 @@ k_mixed_stage(StageArgs a) {
     constexpr int NFS = G::NFS;
     extern __shared__ float4 smem4[];
     float* smem = reinterpret_cast<float*>(smem4);
-    float4* sF4 = smem4;                                          /* [3][NP] */
-    float* sF1 = smem + SM::OFF_F1;                               /* [3][NP] */
     float4* sP = reinterpret_cast<float4*>(smem + SM::OFF_P);     /* [3][NP] */
     float4* sFF4 = reinterpret_cast<float4*>(smem + SM::OFF_FF4); /* [NFS] */
     float* sFF1 = smem + SM::OFF_FF1;                             /* [NFS] */
-    float* sQ = smem + SM::OFF_Q;
     float* sMeta = smem + SM::OFF_META;
 
     const int t = threadIdx.x;
     constexpr bool has_din = STAGE >= 2;
     float* sStg = smem + SM::OFF_STG;                             /* [14][NP] (PERSIST) */
-    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
     if constexpr (TC) {
         float* sQtc = smem + SM::OFF_QTC;
         for (int q = t; q < TC_QTAB; q += G::BLOCK) sQtc[q] = __ldg(a.Qg + QTAB + q);
@@ -337,14 +375,18 @@ k_mixed_stage(StageArgs a) {
             vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
             put(2, tc_idx<2>(i, j, k), f4, f1);
         } else {
+            const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+            auto put = [&](float* f, int nl, const float4& v4, float v1) {
+                f[0] = v4.x; f[nl] = v4.y; f[2 * nl] = v4.z; f[3 * nl] = v4.w; f[4 * nl] = v1;
+            };
             vol_flux<0, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            sF4[t] = f4; sF1[t] = f1;
+            put(smem + LineLay<NX, NY, NZ, 0>::at(i, j, k), LineLay<NX, NY, NZ, 0>::NL, f4, f1);
             if constexpr (G::HAS_Y) {
                 vol_flux<1, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-                sF4[NP + t] = f4; sF1[NP + t] = f1;
+                put(smem + LineLay<NX, NY, NZ, 1>::at(i, j, k), LineLay<NX, NY, NZ, 1>::NL, f4, f1);
             }
             vol_flux<2, VISC>(own, p, gown, a.nu, a.nu_pr, f4, f1);
-            sF4[2 * NP + t] = f4; sF1[2 * NP + t] = f1;
+            put(smem + LineLay<NX, NY, NZ, 2>::at(i, j, k), LineLay<NX, NY, NZ, 2>::NL, f4, f1);
         }
     }
     __syncthreads();
@@ -361,11 +403,11 @@ k_mixed_stage(StageArgs a) {
             o4 = make_float4(oth[0], oth[1], oth[2], oth[3]);
             o1 = oth[4];
         } else if (fs.dir == 0)
-            face_flux<NX, NY, NZ, 0, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 0, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
         else if (G::HAS_Y && fs.dir == 1)
-            face_flux<NX, NY, NZ, 1, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 1, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
         else
-            face_flux<NX, NY, NZ, 2, VISC, TC>(fs, nb, oth, bgo, gfo, sF4, sF1, sP, a, o4, o1);
+            face_flux<NX, NY, NZ, 2, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
         sFF4[t] = o4;
         sFF1[t] = o1;
     }
@@ -404,6 +446,11 @@ k_mixed_stage(StageArgs a) {
             base[TC_SA + oc1] = c[3];
         }
         __syncthreads();
+    } else {
+        line_transform<NX, NY, NZ, 0>(smem, a, t);
+        if constexpr (G::HAS_Y) line_transform<NX, NY, NZ, 1>(smem, a, t);
+        line_transform<NX, NY, NZ, 2>(smem, a, t);
+        __syncthreads();
     }
     if (t < NP) {
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
@@ -419,53 +466,24 @@ k_mixed_stage(StageArgs a) {
             Lt[v] = fmaf(Jz, rz[v * TC_NP], fmaf(Jy, ry[v * TC_NP], Jx * rx[v * TC_NP]));
         L0 = Lt[0]; L1 = Lt[1]; L2 = Lt[2]; L3 = Lt[3]; L4 = Lt[4];
     } else {
-    {
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-        const float* q = sQ + i * QS;
+        /* the three directions' line sums at this node, scaled by J_d */
+        const float* rx = smem + LineLay<NX, NY, NZ, 0>::at(i, j, k);
+        const float* rz = smem + LineLay<NX, NY, NZ, 2>::at(i, j, k);
+        constexpr int NLX = LineLay<NX, NY, NZ, 0>::NL, NLZ = LineLay<NX, NY, NZ, 2>::NL;
+        const float Jx = sMeta[0], Jz = sMeta[2];
+        float Lt[5];
 #pragma unroll
-        for (int m = 0; m < NX; m++) {
-            const int b = (m * NY + j) * NZ + k;
-            const float4 f = sF4[b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sF1[b], acc1);
-        }
-        const float Jx = sMeta[0];
-        L0 = Jx * acc.x; L1 = Jx * acc.y; L2 = Jx * acc.z; L3 = Jx * acc.w; L4 = Jx * acc1;
-    }
-    if constexpr (G::HAS_Y) {
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-        const float* q = sQ + MAXN * QS + j * QS;
+        for (int v = 0; v < 5; v++) Lt[v] = Jx * rx[v * NLX];
+        if constexpr (G::HAS_Y) {
+            const float* ry = smem + LineLay<NX, NY, NZ, 1>::at(i, j, k);
+            constexpr int NLY = LineLay<NX, NY, NZ, 1>::NL;
+            const float Jy = sMeta[1];
 #pragma unroll
-        for (int m = 0; m < NY; m++) {
-            const int b = (i * NY + m) * NZ + k;
-            const float4 f = sF4[NP + b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sF1[NP + b], acc1);
+            for (int v = 0; v < 5; v++) Lt[v] = fmaf(Jy, ry[v * NLY], Lt[v]);
         }
-        const float Jy = sMeta[1];
-        L0 = fmaf(Jy, acc.x, L0); L1 = fmaf(Jy, acc.y, L1); L2 = fmaf(Jy, acc.z, L2);
-        L3 = fmaf(Jy, acc.w, L3); L4 = fmaf(Jy, acc1, L4);
-    }
-    {
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-        const float* q = sQ + 2 * MAXN * QS + k * QS;
 #pragma unroll
-        for (int m = 0; m < NZ; m++) {
-            const int b = (i * NY + j) * NZ + m;
-            const float4 f = sF4[2 * NP + b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sF1[2 * NP + b], acc1);
-        }
-        const float Jz = sMeta[2];
-        L0 = fmaf(Jz, acc.x, L0); L1 = fmaf(Jz, acc.y, L1); L2 = fmaf(Jz, acc.z, L2);
-        L3 = fmaf(Jz, acc.w, L3); L4 = fmaf(Jz, acc1, L4);
-    }
+        for (int v = 0; v < 5; v++) Lt[v] = fmaf(Jz, rz[v * NLZ], Lt[v]);
+        L0 = Lt[0]; L1 = Lt[1]; L2 = Lt[2]; L3 = Lt[3]; L4 = Lt[4];
     }
     /* surface lift: -(J_d / w_end) F_out for the face of each axis through
      * the node (at most one per axis) */
