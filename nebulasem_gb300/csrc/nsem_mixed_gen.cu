@@ -29,15 +29,13 @@ template <int NX, int NY, int NZ, bool VISC = false>
 struct GenSmem {
     using G = Geo<NX, NY, NZ>;
     static constexpr int NP = G::NP, NFS = G::NFS;
-    /* floats: contravariant fluxes G4[3][NP] (x4) + G1[3][NP]; own values
-     * P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS]; line table;
+    /* floats: contravariant fluxes, line-major per direction [3][n][5][NL];
+     * own values P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS];
      * viscous runs: the nodes' gradients GV[12][NP] */
-    static constexpr int OFF_G1 = 12 * NP;
     static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 16 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
-    static constexpr int OFF_Q = OFF_FF1 + NFS;
-    static constexpr int OFF_GV = OFF_Q + QTAB;
+    static constexpr int OFF_GV = OFF_FF1 + NFS;
     static constexpr size_t BYTES = sizeof(float) * (OFF_GV + (VISC ? 12 * NP : 0));
 };
 
@@ -53,9 +51,15 @@ __device__ __forceinline__ void normal_flux(const float* m, const float* u, floa
     f1 = __fmul_rn(mn, th);
 }
 
+/* resident CTAs per SM the registers are sized for (order 4 and below,
+ * inviscid): stages 1-2, which carry no FP64 state */
+#ifndef NSEM_GEN_MB12
+#define NSEM_GEN_MB12 7
+#endif
+
 template <int NX, int NY, int NZ, int STAGE, bool VISC>
 __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK,
-                                  (min_blocks(NX == 8 ? 2 : (VISC ? 4 : 6), Geo<NX, NY, NZ>::BLOCK,
+                                  (min_blocks(NX == 8 ? 2 : (VISC ? 4 : (STAGE == 1 || STAGE == 2) ? NSEM_GEN_MB12 : 6), Geo<NX, NY, NZ>::BLOCK,
                                               GenSmem<NX, NY, NZ, VISC>::BYTES)))
 k_mixed_stage_gen(StageArgs a) {
     using G = Geo<NX, NY, NZ>;
@@ -64,17 +68,13 @@ k_mixed_stage_gen(StageArgs a) {
     constexpr int NFS = G::NFS;
     extern __shared__ float4 gen4[];
     float* smem = reinterpret_cast<float*>(gen4);
-    float4* sG4 = gen4;
-    float* sG1 = smem + SM::OFF_G1;
     float4* sP = reinterpret_cast<float4*>(smem + SM::OFF_P);
     float4* sFF4 = reinterpret_cast<float4*>(smem + SM::OFF_FF4);
     float* sFF1 = smem + SM::OFF_FF1;
-    float* sQ = smem + SM::OFF_Q;
     float* sGV = smem + SM::OFF_GV;     /* viscous runs: [12][NP] */
     const int t = threadIdx.x;
     const int64_t e = blockIdx.x;
     constexpr bool has_din = STAGE >= 2;
-    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
 
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0}, jin[9], icv = 0.0f;
     float gown[12];
@@ -165,6 +165,10 @@ k_mixed_stage_gen(StageArgs a) {
         sP[NP + t] = make_float4(own[4], p.rho, p.umag, p.c);
         sP[2 * NP + t] = make_float4(p.u[0], p.u[1], p.u[2], p.pp);
         sP[3 * NP + t] = make_float4(p.th, 0.0f, 0.0f, 0.0f);
+        const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+        const int lpos[3] = {LineLay<NX, NY, NZ, 0>::at(i, j, k), LineLay<NX, NY, NZ, 1>::at(i, j, k),
+                             LineLay<NX, NY, NZ, 2>::at(i, j, k)};
+        const int lnl[3] = {LineLay<NX, NY, NZ, 0>::NL, LineLay<NX, NY, NZ, 1>::NL, LineLay<NX, NY, NZ, 2>::NL};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             if (d == 1 && !G::HAS_Y) continue;
@@ -183,8 +187,9 @@ k_mixed_stage_gen(StageArgs a) {
                 g4.w = fmaf(-mu, fmaf(gown[tidx(2, 0)], j0, fmaf(gown[tidx(2, 1)], j1, gown[tidx(2, 2)] * j2)), g4.w);
                 g1 = fmaf(-mt, fmaf(gown[9], j0, fmaf(gown[10], j1, gown[11] * j2)), g1);
             }
-            sG4[d * NP + t] = g4;
-            sG1[d * NP + t] = g1;
+            float* f = smem + lpos[d];
+            const int nl = lnl[d];
+            f[0] = g4.x; f[nl] = g4.y; f[2 * nl] = g4.z; f[3 * nl] = g4.w; f[4 * nl] = g1;
         }
     }
     __syncthreads();
@@ -261,43 +266,30 @@ k_mixed_stage_gen(StageArgs a) {
     }
     __syncthreads();
 
-    /* phase 3: line sums l_a'(x_m) G_d(m), lift, 1/cV, buoyancy, update */
+    /* phase 3: line sums l_a'(x_m) G_d(m) (in-place line transform), lift,
+     * 1/cV, buoyancy, update */
+    line_transform<NX, NY, NZ, 0>(smem, a, t);
+    if constexpr (G::HAS_Y) line_transform<NX, NY, NZ, 1>(smem, a, t);
+    line_transform<NX, NY, NZ, 2>(smem, a, t);
+    __syncthreads();
     if (t >= NP) return;
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
-    float4 acc = make_float4(0, 0, 0, 0);
-    float acc1 = 0.0f;
+    float4 acc;
+    float acc1;
     {
-        const float* q = sQ + i * QS;
-#pragma unroll
-        for (int m = 0; m < NX; m++) {
-            const int b = (m * NY + j) * NZ + k;
-            const float4 f = sG4[b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sG1[b], acc1);
+        const float* rx = smem + LineLay<NX, NY, NZ, 0>::at(i, j, k);
+        const float* rz = smem + LineLay<NX, NY, NZ, 2>::at(i, j, k);
+        constexpr int NLX = LineLay<NX, NY, NZ, 0>::NL, NLZ = LineLay<NX, NY, NZ, 2>::NL;
+        acc = make_float4(rx[0], rx[NLX], rx[2 * NLX], rx[3 * NLX]);
+        acc1 = rx[4 * NLX];
+        if constexpr (G::HAS_Y) {
+            const float* ry = smem + LineLay<NX, NY, NZ, 1>::at(i, j, k);
+            constexpr int NLY = LineLay<NX, NY, NZ, 1>::NL;
+            acc.x += ry[0]; acc.y += ry[NLY]; acc.z += ry[2 * NLY]; acc.w += ry[3 * NLY];
+            acc1 += ry[4 * NLY];
         }
-    }
-    if constexpr (G::HAS_Y) {
-        const float* q = sQ + MAXN * QS + j * QS;
-#pragma unroll
-        for (int m = 0; m < NY; m++) {
-            const int b = (i * NY + m) * NZ + k;
-            const float4 f = sG4[NP + b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sG1[NP + b], acc1);
-        }
-    }
-    {
-        const float* q = sQ + 2 * MAXN * QS + k * QS;
-#pragma unroll
-        for (int m = 0; m < NZ; m++) {
-            const int b = (i * NY + j) * NZ + m;
-            const float4 f = sG4[2 * NP + b];
-            acc.x = fmaf(q[m], f.x, acc.x); acc.y = fmaf(q[m], f.y, acc.y);
-            acc.z = fmaf(q[m], f.z, acc.z); acc.w = fmaf(q[m], f.w, acc.w);
-            acc1 = fmaf(q[m], sG1[2 * NP + b], acc1);
-        }
+        acc.x += rz[0]; acc.y += rz[NLZ]; acc.z += rz[2 * NLZ]; acc.w += rz[3 * NLZ];
+        acc1 += rz[4 * NLZ];
     }
     auto lift = [&](int slot) {
         const float4 f = sFF4[slot];

@@ -80,48 +80,6 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-/* FP32 line sums as an in-place line transform.  The fluxes of direction D
- * are kept line-major: variable v at node m along line l (x: l = j NZ + k,
- * y: l = i NZ + k, z: l = i NY + j) at D 5 NP + m ROW + v NL + l, with NL
- * lines and ROW = 5 NL.  After the face phase, thread r < ROW takes the
- * line and variable (v, l) = (r / NL, r % NL) of each direction: it reads
- * the n values m ROW + r (a warp reads consecutive words), forms
- * R_a = sum_m Q_D[a][m] F_m with the weights as constant-bank operands, and
- * writes R_a over F_a.  A node then reads its three R's.  Each flux value
- * is read once from shared memory instead of once per node of its line. */
-template <int NX, int NY, int NZ, int D>
-struct LineLay {
-    static constexpr int NP = NX * NY * NZ;
-    static constexpr int n = D == 0 ? NX : D == 1 ? NY : NZ;
-    static constexpr int NL = NP / n;
-    static constexpr int ROW = 5 * NL;
-    /* position of variable 0 at node (i, j, k) */
-    __device__ static __forceinline__ int at(int i, int j, int k) {
-        return D * 5 * NP + (D == 0 ? i : D == 1 ? j : k) * ROW +
-               (D == 0 ? j * NZ + k : D == 1 ? i * NZ + k : i * NY + j);
-    }
-};
-
-template <int NX, int NY, int NZ, int D>
-__device__ __forceinline__ void line_transform(float* F, const StageArgs& a, int t) {
-    using LL = LineLay<NX, NY, NZ, D>;
-    constexpr int BLOCK = Geo<NX, NY, NZ>::BLOCK;
-    float* f = F + D * 5 * LL::NP;
-#pragma unroll 1
-    for (int r = t; r < LL::ROW; r += BLOCK) {
-        float in[LL::n];
-#pragma unroll
-        for (int m = 0; m < LL::n; m++) in[m] = f[m * LL::ROW + r];
-#pragma unroll
-        for (int q = 0; q < LL::n; q++) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int m = 0; m < LL::n; m++) acc = fmaf(a.qc[D][q][m], in[m], acc);
-            f[q * LL::ROW + r] = acc;
-        }
-    }
-}
-
 /* registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the stage
  * that also carries the FP64 state (measured best on GB300), 6 when viscous */
 #ifndef NSEM_MIXED_MB12
