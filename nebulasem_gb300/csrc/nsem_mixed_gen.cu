@@ -32,7 +32,7 @@ struct GenSmem {
     /* floats: contravariant fluxes, line-major per direction [3][n][5][NL];
      * own values P[4][NP] (x4); face fluxes FF4[NFS] (x4) + FF1[NFS];
      * viscous runs: the nodes' gradients GV[12][NP] */
-    static constexpr int OFF_P = (15 * NP + 3) / 4 * 4;
+    static constexpr int OFF_P = (line_floats<NX, NY, NZ>() + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 16 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
     static constexpr int OFF_GV = OFF_FF1 + NFS;

@@ -20,7 +20,7 @@ struct StageSmem {
     /* floats: volume fluxes, line-major per direction [3][n][5][NL] (tensor-core
      * line sums: F[3][5][TC_NP]); own values P[3][NP] (x4); face fluxes
      * FF4[NFS] (x4) + FF1[NFS]; metric */
-    static constexpr int FLUX = TC ? 15 * TC_NP : 15 * NP;
+    static constexpr int FLUX = TC ? 15 * TC_NP : line_floats<NX, NY, NZ>();
     static constexpr int OFF_P = (FLUX + 3) / 4 * 4;
     static constexpr int OFF_FF4 = OFF_P + 12 * NP;
     static constexpr int OFF_FF1 = OFF_FF4 + 4 * NFS;
