@@ -32,6 +32,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <vector>
 
 #include "nsem_mixed.h"
@@ -58,24 +59,25 @@ struct AdjArgs {
     float dt, gamma, gR, g[3];
     float lift[3];
     float eos[6];
+    float qc[3][8][8];         /* line-sum weights Q_d[a][m] (constant-bank operands) */
 };
 
 template <int NX, int NY, int NZ>
 struct AdjSmem {
     using G = Geo<NX, NY, NZ>;
     static constexpr int NP = G::NP, NFS = G::NFS;
-    /* floats: gbar G4[NP] (x4) + G1[NP]; own values P[3][NP] (x4) and
-     * Theta'; face results Fa4[NFS] (x4) + Fa1[NFS] (merged into Fbar_n),
-     * Xd4[NFS] (x4) + Xd1[NFS] (added to xbar); Q; metric */
-    static constexpr int OFF_G1 = 4 * NP;
-    static constexpr int OFF_P = (5 * NP + 3) / 4 * 4;
+    /* floats: gbar GB[5][NP]; the transposed line sums, line-major per
+     * direction; own values P[3][NP] (x4) and Theta'; face results Fa4[NFS]
+     * (x4) + Fa1[NFS] (merged into Fbar_n), Xd4[NFS] (x4) + Xd1[NFS] (added
+     * to xbar); metric */
+    static constexpr int OFF_R = (5 * NP + 3) / 4 * 4;
+    static constexpr int OFF_P = (OFF_R + line_floats<NX, NY, NZ>() + 3) / 4 * 4;
     static constexpr int OFF_T = OFF_P + 12 * NP;
     static constexpr int OFF_FA4 = (OFF_T + NP + 3) / 4 * 4;
     static constexpr int OFF_FA1 = OFF_FA4 + 4 * NFS;
     static constexpr int OFF_XD4 = (OFF_FA1 + NFS + 3) / 4 * 4;
     static constexpr int OFF_XD1 = OFF_XD4 + 4 * NFS;
-    static constexpr int OFF_Q = OFF_XD1 + NFS;
-    static constexpr int OFF_META = OFF_Q + QTAB;
+    static constexpr int OFF_META = OFF_XD1 + NFS;
     static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
 };
 
@@ -84,6 +86,35 @@ constexpr int adj_min_blocks() {
     /* order 7 (512 threads): two CTAs with 64 registers, no spills */
     return min_blocks(Geo<NX, NY, NZ>::BLOCK >= 512 ? 2 : 6, Geo<NX, NY, NZ>::BLOCK,
                       AdjSmem<NX, NY, NZ>::BYTES);
+}
+
+/* Transposed line sums as a line transform: for direction D, line l and
+ * variable v (thread r = v NL + l), R(b) = sum_m Q_D[m][b] gbar(m) over the
+ * line's nodes, written line-major (the forward's layout) for the node
+ * threads to read.  gbar is read from its node-ordered rows. */
+template <int NX, int NY, int NZ, int D>
+__device__ __forceinline__ void line_transform_t(const float* gbn, float* R, const AdjArgs& a, int t) {
+    using LL = LineLay<NX, NY, NZ, D>;
+    constexpr int NP = LL::NP, NL = LL::NL, n = LL::n;
+    constexpr int BLOCK = Geo<NX, NY, NZ>::BLOCK;
+    float* f = R + LL::BASE;
+#pragma unroll 1
+    for (int r = t; r < 5 * NL; r += BLOCK) {
+        const int v = r / NL, l = r - v * NL;
+        /* node of position m on line l: x (m, l), y (l / NZ, m, l % NZ), z (l, m) */
+        const int n0 = D == 0 ? l : D == 1 ? (l / NZ) * NY * NZ + (l % NZ) : l * NZ;
+        constexpr int ms = D == 0 ? NY * NZ : D == 1 ? NZ : 1;
+        float x[n];
+#pragma unroll
+        for (int m = 0; m < n; m++) x[m] = gbn[v * NP + n0 + m * ms];
+#pragma unroll
+        for (int b = 0; b < n; b++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int m = 0; m < n; m++) acc = fmaf(a.qc[D][m][b], x[m], acc);
+            f[b * LL::ROW + r] = acc;
+        }
+    }
 }
 
 /* gbar of a node from the stage's input: 2/3 lam (R3), B/4 (R2), C (R1), w (R0) */
@@ -118,7 +149,7 @@ __device__ __forceinline__ void jft(const float* u, float th, float pth, float f
 template <int NX, int NY, int NZ, int DIR>
 __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const float* xo,
                                          const float* bgo, const float* go, float cn,
-                                         const float4* sG4, const float* sG1, const float4* sP,
+                                         const float* sGb, const float4* sP,
                                          const float* sT, float cs, const AdjArgs& a, float4& fa4,
                                          float& fa1, float4& xd4, float& xd1) {
     constexpr int NP = Geo<NX, NY, NZ>::NP;
@@ -129,8 +160,8 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
      * P2 = (u0, u1, u2, dp'/dTheta') */
     const float rho = P1.x, um = P1.y, c = P1.z, iTh = P1.w;
     const float inv = rcp_nr(rho);
-    const float4 ga4 = sG4[fs.la];
-    const float ga1 = sG1[fs.la];
+    const float4 ga4 = make_float4(sGb[fs.la], sGb[NP + fs.la], sGb[2 * NP + fs.la], sGb[3 * NP + fs.la]);
+    const float ga1 = sGb[4 * NP + fs.la];
     const float md = DIR == 0 ? P0.y : DIR == 1 ? P0.z : P0.w;
     const float uvec[3] = {P2.x, P2.y, P2.z};
     if (nb >= 0) {
@@ -199,15 +230,14 @@ k_mixed_adj(AdjArgs a) {
     constexpr int NFS = G::NFS;
     extern __shared__ float4 asm4[];
     float* smem = reinterpret_cast<float*>(asm4);
-    float4* sG4 = asm4;
-    float* sG1 = smem + SM::OFF_G1;
+    float* sGb = smem;                                          /* [5][NP] */
+    float* sR = smem + SM::OFF_R;
     float4* sP = reinterpret_cast<float4*>(smem + SM::OFF_P);
     float* sT = smem + SM::OFF_T;
     float4* sFa4 = reinterpret_cast<float4*>(smem + SM::OFF_FA4);
     float* sFa1 = smem + SM::OFF_FA1;
     float4* sXd4 = reinterpret_cast<float4*>(smem + SM::OFF_XD4);
     float* sXd1 = smem + SM::OFF_XD1;
-    float* sQ = smem + SM::OFF_Q;
     float* sMeta = smem + SM::OFF_META;
 
     const int t = threadIdx.x;
@@ -249,7 +279,6 @@ k_mixed_adj(AdjArgs a) {
             cn = __ldg(a.J + (int64_t)fs.dir * a.n_elem + nb) * a.lift[fs.dir];
         }
     }
-    for (int q = t; q < QTAB; q += G::BLOCK) sQ[q] = __ldg(a.Qg + q);
     if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
 
     /* phase 1: gbar and the node's values for the face and pointwise transposes */
@@ -261,8 +290,8 @@ k_mixed_adj(AdjArgs a) {
         pth = a.gamma * (bgs[3] + p.pp) * iTh;      /* dp'/dTheta' = gamma p / Theta */
         uu[0] = p.u[0]; uu[1] = p.u[1]; uu[2] = p.u[2];
         th = p.th;
-        sG4[t] = make_float4(gb[0], gb[1], gb[2], gb[3]);
-        sG1[t] = gb[4];
+#pragma unroll
+        for (int v = 0; v < 5; v++) sGb[v * NP + t] = gb[v];
         sP[t] = make_float4(x[0], x[1], x[2], x[3]);
         sP[NP + t] = make_float4(p.rho, p.umag, p.c, iTh);
         sP[2 * NP + t] = make_float4(p.u[0], p.u[1], p.u[2], pth);
@@ -276,16 +305,20 @@ k_mixed_adj(AdjArgs a) {
         float4 fa4, xd4;
         float fa1, xd1;
         if (fs.dir == 0)
-            face_adj<NX, NY, NZ, 0>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+            face_adj<NX, NY, NZ, 0>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
         else if (G::HAS_Y && fs.dir == 1)
-            face_adj<NX, NY, NZ, 1>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+            face_adj<NX, NY, NZ, 1>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
         else
-            face_adj<NX, NY, NZ, 2>(fs, nb, xo, bgo, go, cn, sG4, sG1, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+            face_adj<NX, NY, NZ, 2>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
         sFa4[t] = fa4;
         sFa1[t] = fa1;
         sXd4[t] = xd4;
         sXd1[t] = xd1;
     }
+    /* the transposed line sums of the three directions */
+    line_transform_t<NX, NY, NZ, 0>(sGb, sR, a, t);
+    if constexpr (G::HAS_Y) line_transform_t<NX, NY, NZ, 1>(sGb, sR, a, t);
+    line_transform_t<NX, NY, NZ, 2>(sGb, sR, a, t);
     __syncthreads();
 
     /* phase 3: transposed line sums, pointwise transposes, face and source terms */
@@ -294,17 +327,10 @@ k_mixed_adj(AdjArgs a) {
     float xb[5] = {0, 0, 0, 0, 0};
     {
         /* x: Fbar_x(b) = J_x sum_a Q_x[a][i] gbar(a, j, k) */
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-#pragma unroll
-        for (int m = 0; m < NX; m++) {
-            const float q = sQ[m * QS + i];
-            const int b = (m * NY + j) * NZ + k;
-            const float4 f = sG4[b];
-            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
-            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
-            acc1 = fmaf(q, sG1[b], acc1);
-        }
+        const float* rr = sR + LineLay<NX, NY, NZ, 0>::at(i, j, k);
+        constexpr int NL = LineLay<NX, NY, NZ, 0>::NL;
+        float4 acc = make_float4(rr[0], rr[NL], rr[2 * NL], rr[3 * NL]);
+        float acc1 = rr[4 * NL];
         const float Jx = sMeta[0];
         acc.x *= Jx; acc.y *= Jx; acc.z *= Jx; acc.w *= Jx; acc1 *= Jx;
         const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
@@ -315,17 +341,10 @@ k_mixed_adj(AdjArgs a) {
         jft<0>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
     }
     if constexpr (G::HAS_Y) {
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-#pragma unroll
-        for (int m = 0; m < NY; m++) {
-            const float q = sQ[MAXN * QS + m * QS + j];
-            const int b = (i * NY + m) * NZ + k;
-            const float4 f = sG4[b];
-            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
-            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
-            acc1 = fmaf(q, sG1[b], acc1);
-        }
+        const float* rr = sR + LineLay<NX, NY, NZ, 1>::at(i, j, k);
+        constexpr int NL = LineLay<NX, NY, NZ, 1>::NL;
+        float4 acc = make_float4(rr[0], rr[NL], rr[2 * NL], rr[3 * NL]);
+        float acc1 = rr[4 * NL];
         const float Jy = sMeta[1];
         acc.x *= Jy; acc.y *= Jy; acc.z *= Jy; acc.w *= Jy; acc1 *= Jy;
         const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
@@ -336,17 +355,10 @@ k_mixed_adj(AdjArgs a) {
         jft<1>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
     }
     {
-        float4 acc = make_float4(0, 0, 0, 0);
-        float acc1 = 0.0f;
-#pragma unroll
-        for (int m = 0; m < NZ; m++) {
-            const float q = sQ[2 * MAXN * QS + m * QS + k];
-            const int b = (i * NY + j) * NZ + m;
-            const float4 f = sG4[b];
-            acc.x = fmaf(q, f.x, acc.x); acc.y = fmaf(q, f.y, acc.y);
-            acc.z = fmaf(q, f.z, acc.z); acc.w = fmaf(q, f.w, acc.w);
-            acc1 = fmaf(q, sG1[b], acc1);
-        }
+        const float* rr = sR + LineLay<NX, NY, NZ, 2>::at(i, j, k);
+        constexpr int NL = LineLay<NX, NY, NZ, 2>::NL;
+        float4 acc = make_float4(rr[0], rr[NL], rr[2 * NL], rr[3 * NL]);
+        float acc1 = rr[4 * NL];
         const float Jz = sMeta[2];
         acc.x *= Jz; acc.y *= Jz; acc.z *= Jz; acc.w *= Jz; acc1 *= Jz;
         const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
@@ -458,6 +470,7 @@ AdjArgs adj_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
         a.g[c] = (float)dev->g[c];
         a.lift[c] = mb->lift[c];
     }
+    std::memcpy(a.qc, mb->qc, sizeof(a.qc));
     double ck = 1.0;
     for (int k = 1; k <= 6; k++) {
         ck *= (dev->gamma - (k - 1)) / k;

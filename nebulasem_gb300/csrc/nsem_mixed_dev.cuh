@@ -190,6 +190,55 @@ __device__ __forceinline__ FaceSlot face_slot(int t) {
     return f;
 }
 
+/* FP32 line sums as an in-place line transform (the stage kernels, and
+ * transposed in the adjoint).  The fluxes of direction D are kept line-major:
+ * variable v at node m along line l (x: l = j NZ + k, y: l = i NZ + k,
+ * z: l = i NY + j) at BASE_D + m ROW + v NL + l, with NL lines and
+ * ROW = 5 NL + padding.  After the face phase, thread r < 5 NL takes the
+ * line and variable (v, l) = (r / NL, r % NL) of each direction: it reads
+ * the n values m ROW + r (a warp reads consecutive words), forms
+ * R_a = sum_m Q_D[a][m] F_m with the weights (the weak-form table of the
+ * kernel's geometry) as constant-bank operands, and writes R_a over F_a.  A
+ * node then reads its three R's.  Each flux value is read once from shared
+ * memory instead of once per node of its line.
+ *
+ * Row padding (floats) per direction: puts the node threads' accesses
+ * (stores in phase 1, reads of the results) and the face threads' reads in
+ * distinct banks as far as possible -- chosen by counting the wavefronts of
+ * every such warp access for each padding up to 31. */
+template <int NX, int NY, int NZ>
+constexpr int line_pad(int D) {
+    return (NX == 5 && NY == 5) ? (D == 0 ? 28 : D == 1 ? 30 : 16)
+         : (NX == 8 && NY == 8) ? (D == 0 ? 0 : D == 1 ? 8 : 4)
+         : (NX == 4 && NY == 4) ? (D == 0 ? 0 : 8)
+         : (NX == 5 && NY == 1) ? (D == 1 ? 0 : 1)
+         : 0;
+}
+
+template <int NX, int NY, int NZ, int D>
+struct LineLay {
+    static constexpr int NP = NX * NY * NZ;
+    static constexpr int n = D == 0 ? NX : D == 1 ? NY : NZ;
+    static constexpr int NL = NP / n;
+    static constexpr int ROW = 5 * NL + line_pad<NX, NY, NZ>(D);
+    static constexpr int SIZE = n * ROW;
+    static constexpr int BASE = D == 0 ? 0 : LineLay<NX, NY, NZ, D - 1>::BASE + LineLay<NX, NY, NZ, D - 1>::SIZE;
+    /* position of variable 0 at node (i, j, k) */
+    __device__ static __forceinline__ int at(int i, int j, int k) {
+        return BASE + (D == 0 ? i : D == 1 ? j : k) * ROW +
+               (D == 0 ? j * NZ + k : D == 1 ? i * NZ + k : i * NY + j);
+    }
+};
+template <int NX, int NY, int NZ>
+struct LineLay<NX, NY, NZ, -1> {
+    static constexpr int BASE = 0, SIZE = 0;
+};
+/* floats of the three directions' flux rows */
+template <int NX, int NY, int NZ>
+constexpr int line_floats() {
+    return LineLay<NX, NY, NZ, 2>::BASE + LineLay<NX, NY, NZ, 2>::SIZE;
+}
+
 /* slot of the face of direction D through local node (i, j, k), or -1 */
 template <int NX, int NY, int NZ, int D>
 __device__ __forceinline__ int face_of_node(int i, int j, int k) {
