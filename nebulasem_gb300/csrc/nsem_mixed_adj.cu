@@ -145,14 +145,17 @@ __device__ __forceinline__ void jft(const float* u, float th, float pth, float f
     xb[4] = fmaf(fbd, pth, fmaf(ft, ud, xb[4]));
 }
 
-/* phase 2: adjoint of the flux through face node t of direction DIR */
-template <int NX, int NY, int NZ, int DIR>
+/* phase 2: adjoint of the flux through face node t (the face's axis a
+ * run-time value: selects, no divergent branches between axes) */
+template <int NX, int NY, int NZ>
 __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const float* xo,
                                          const float* bgo, const float* go, float cn,
                                          const float* sGb, const float4* sP,
                                          const float* sT, float cs, const AdjArgs& a, float4& fa4,
                                          float& fa1, float4& xd4, float& xd1) {
     constexpr int NP = Geo<NX, NY, NZ>::NP;
+    const int DIR = fs.dir;
+    const bool d0 = DIR == 0, d1 = DIR == 1;
     const float sg = fs.side ? 1.0f : -1.0f;
     const float4 P0 = sP[fs.la], P1 = sP[NP + fs.la], P2 = sP[2 * NP + fs.la];
     const float tp_s = sT[fs.la];
@@ -162,7 +165,7 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
     const float inv = rcp_nr(rho);
     const float4 ga4 = make_float4(sGb[fs.la], sGb[NP + fs.la], sGb[2 * NP + fs.la], sGb[3 * NP + fs.la]);
     const float ga1 = sGb[4 * NP + fs.la];
-    const float md = DIR == 0 ? P0.y : DIR == 1 ? P0.z : P0.w;
+    const float md = d0 ? P0.y : d1 ? P0.z : P0.w;
     const float uvec[3] = {P2.x, P2.y, P2.z};
     if (nb >= 0) {
         const Pt q = pointwise(xo, bgo, a.eos, a.gamma, a.gR);
@@ -176,10 +179,11 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
         const float h = 0.5f * sg;
         fa4 = make_float4(h * pb0, h * pb1, h * pb2, h * pb3);
         fa1 = h * pb4;
-        const float pbm = DIR == 0 ? pb1 : DIR == 1 ? pb2 : pb3;
+        const float pbm = d0 ? pb1 : d1 ? pb2 : pb3;
         /* jump terms: d(-lam (q_o - q_a))/dx_a = lam on the masked components,
          * minus (jump . Phibar) dlam/dx_a */
-        const float jr = xo[0] - P0.x, jm = xo[1 + DIR] - md, jt = xo[4] - tp_s;
+        const float xmo = d0 ? xo[1] : d1 ? xo[2] : xo[3];
+        const float jr = xo[0] - P0.x, jm = xmo - md, jt = xo[4] - tp_s;
         const float s = fmaf(jr, pb0, fmaf(jm, pbm, jt * pb4));
         /* dlam/dx_a = (d|u| + dc) / 4: d|u|/drho' = -|u|/rho, d|u|/dm_k = u_k/(rho |u|),
          * dc/drho' = -c/(2 rho), dc/dTheta' = c/(2 Theta) */
@@ -189,15 +193,16 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
         float xm[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) xm[k] = q4 * (uvec[k] * ku);
-        xm[DIR] = fmaf(lam, pbm, xm[DIR]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) xm[k] = k == DIR ? fmaf(lam, pbm, xm[k]) : xm[k];
         const float x4 = fmaf(q4, 0.5f * c * iTh, lam * pb4);
         xd4 = make_float4(x0, xm[0], xm[1], xm[2]);
         xd1 = x4;
     } else {
         /* wall: Phi_n = s p' + lam_w m_n; Phibar = -C gbar_a (normal momentum) */
-        const float pbm = -cs * (DIR == 0 ? ga4.y : DIR == 1 ? ga4.z : ga4.w);
-        const float r0 = DIR == 0 ? 0.0f : uvec[0];
-        const float r1 = DIR == 1 ? 0.0f : uvec[1];
+        const float pbm = -cs * (d0 ? ga4.y : d1 ? ga4.z : ga4.w);
+        const float r0 = d0 ? 0.0f : uvec[0];
+        const float r1 = d1 ? 0.0f : uvec[1];
         const float r2 = DIR == 2 ? 0.0f : uvec[2];
         const float mr = safe_sqrt(__fmaf_rn(r0, r0, __fmaf_rn(r1, r1, __fmul_rn(r2, r2))));
         const bool full = mr > 1e-7f;
@@ -212,7 +217,8 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
         float xm[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) xm[k] = q2 * (vr[k] * ku);
-        xm[DIR] = fmaf(lam, pbm, xm[DIR]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) xm[k] = k == DIR ? fmaf(lam, pbm, xm[k]) : xm[k];
         const float x4 = fmaf(q2, 0.5f * c * iTh, sg * P2.w * pbm);
         fa4 = make_float4(0, 0, 0, 0);
         fa1 = 0.0f;
@@ -304,12 +310,7 @@ k_mixed_adj(AdjArgs a) {
         const float cs = sMeta[fs.dir] * a.lift[fs.dir];
         float4 fa4, xd4;
         float fa1, xd1;
-        if (fs.dir == 0)
-            face_adj<NX, NY, NZ, 0>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
-        else if (G::HAS_Y && fs.dir == 1)
-            face_adj<NX, NY, NZ, 1>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
-        else
-            face_adj<NX, NY, NZ, 2>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
+        face_adj<NX, NY, NZ>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
         sFa4[t] = fa4;
         sFa1[t] = fa1;
         sXd4[t] = xd4;

@@ -100,42 +100,60 @@ constexpr int stage_min_blocks() {
                       PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
 }
 
-/* phase 2: flux through face node t of direction DIR, seen from the element */
-template <int NX, int NY, int NZ, int DIR, bool VISC, bool TC>
+/* phase 2: flux through face node t, seen from the element.  The face's
+ * axis is a run-time value (selects, no branches), so a warp whose face
+ * nodes lie on faces of two axes runs one instruction stream; the operations
+ * and their operands are those of the plain per-axis form, so the two
+ * elements of a face still produce exact negatives. */
+template <int NX, int NY, int NZ, bool VISC, bool TC>
 __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const float* oth,
                                           const float* bgo, const float* gfo, const float* sF,
                                           const float4* sP, const StageArgs& a,
                                           float4& o4, float& o1) {
     constexpr int NP = Geo<NX, NY, NZ>::NP;
-    const float sg = fs.side ? 1.0f : -1.0f;   /* outward normal = sg e_DIR */
+    const int dir = fs.dir;
+    const bool d0 = dir == 0, d1 = dir == 1, d2 = dir == 2;
+    const float sg = fs.side ? 1.0f : -1.0f;   /* outward normal = sg e_dir */
     const float4 P0 = sP[fs.la], P1 = sP[NP + fs.la];
-    const float md_s = DIR == 0 ? P0.y : DIR == 1 ? P0.z : P0.w;
+    const float md_s = d0 ? P0.y : d1 ? P0.z : P0.w;
     const float um_s = P1.z, c_s = P1.w;
     if (nb >= 0) {
         float4 A4;
         float A1;
+        const int i = fs.la / (NY * NZ), j = (fs.la / NZ) % NY, k = fs.la % NZ;
         if constexpr (TC) {
-            const float* f = sF + DIR * 5 * TC_NP +
-                             tc_idx<DIR>(fs.la >> 6, (fs.la >> 3) & 7, fs.la & 7);
+            const float* f = sF + dir * 5 * TC_NP +
+                             (d0 ? tc_idx<0>(i, j, k) : d1 ? tc_idx<1>(i, j, k) : tc_idx<2>(i, j, k));
             A4 = make_float4(f[0], f[TC_NP], f[2 * TC_NP], f[3 * TC_NP]);
             A1 = f[4 * TC_NP];
         } else {
-            using LL = LineLay<NX, NY, NZ, DIR>;
-            const float* f = sF + LL::at(fs.la / (NY * NZ), (fs.la / NZ) % NY, fs.la % NZ);
-            A4 = make_float4(f[0], f[LL::NL], f[2 * LL::NL], f[3 * LL::NL]);
-            A1 = f[4 * LL::NL];
+            using L0 = LineLay<NX, NY, NZ, 0>;
+            using L1 = LineLay<NX, NY, NZ, 1>;
+            using L2 = LineLay<NX, NY, NZ, 2>;
+            const float* f = sF + (d0 ? L0::at(i, j, k) : d1 ? L1::at(i, j, k) : L2::at(i, j, k));
+            const int nl = d0 ? L0::NL : d1 ? L1::NL : L2::NL;
+            A4 = make_float4(f[0], f[nl], f[2 * nl], f[3 * nl]);
+            A1 = f[4 * nl];
         }
         const Pt q = pointwise(oth, bgo, a.eos, a.gamma, a.gR);
-        float g12[12] = {};
-        if constexpr (VISC) {
-            g12[tidx(0, DIR)] = gfo[0];
-            g12[tidx(1, DIR)] = gfo[1];
-            g12[tidx(2, DIR)] = gfo[2];
-            g12[9 + DIR] = gfo[3];
-        }
+        /* the neighbour's volume flux along the axis (vol_flux of its node) */
+        const float ud = d0 ? q.u[0] : d1 ? q.u[1] : q.u[2];
+        const float mdo = d0 ? oth[1] : d1 ? oth[2] : oth[3];
         float4 B4;
         float B1;
-        vol_flux<DIR, VISC>(oth, q, g12, a.nu, a.nu_pr, B4, B1);
+        B4.x = mdo;
+        B4.y = __fmaf_rn(oth[1], ud, d0 ? q.pp : 0.0f);
+        B4.z = __fmaf_rn(oth[2], ud, d1 ? q.pp : 0.0f);
+        B4.w = __fmaf_rn(oth[3], ud, d2 ? q.pp : 0.0f);
+        B1 = __fmul_rn(mdo, q.th);
+        if constexpr (VISC) {
+            /* gfo: the neighbour's d_c U_dir (c = 0..2) and d_dir theta */
+            const float mu = __fmul_rn(q.rho, a.nu), mt = __fmul_rn(q.rho, a.nu_pr);
+            B4.y = __fmaf_rn(-mu, gfo[0], B4.y);
+            B4.z = __fmaf_rn(-mu, gfo[1], B4.z);
+            B4.w = __fmaf_rn(-mu, gfo[2], B4.w);
+            B1 = __fmaf_rn(-mt, gfo[3], B1);
+        }
         const float lam = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(um_s, q.umag), __fadd_rn(c_s, q.c)));
         const float av0 = __fmul_rn(0.5f, __fadd_rn(A4.x, B4.x));
         const float av1 = __fmul_rn(0.5f, __fadd_rn(A4.y, B4.y));
@@ -143,12 +161,13 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
         const float av3 = __fmul_rn(0.5f, __fadd_rn(A4.w, B4.w));
         const float av4 = __fmul_rn(0.5f, __fadd_rn(A1, B1));
         const float jr = __fsub_rn(oth[0], P0.x);
-        const float jm = __fsub_rn(oth[1 + DIR], md_s);
+        const float jm = __fsub_rn(mdo, md_s);
         const float jt = __fsub_rn(oth[4], P1.x);
+        const float s1 = sg * av1, s2 = sg * av2, s3 = sg * av3;
         o4.x = __fmaf_rn(-lam, jr, sg * av0);
-        o4.y = DIR == 0 ? __fmaf_rn(-lam, jm, sg * av1) : sg * av1;
-        o4.z = DIR == 1 ? __fmaf_rn(-lam, jm, sg * av2) : sg * av2;
-        o4.w = DIR == 2 ? __fmaf_rn(-lam, jm, sg * av3) : sg * av3;
+        o4.y = d0 ? __fmaf_rn(-lam, jm, s1) : s1;
+        o4.z = d1 ? __fmaf_rn(-lam, jm, s2) : s2;
+        o4.w = d2 ? __fmaf_rn(-lam, jm, s3) : s3;
         o1 = __fmaf_rn(-lam, jt, sg * av4);
     } else {
         /* wall ghost: rho, theta, p NEUMANN; SYMMETRY velocity (tangential
@@ -158,14 +177,14 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
          * s p' + lam m_n, lam = (|U_ghost| + c) / 2.  No viscous wall flux
          * (zero ghost gradient). */
         const float4 P2 = sP[2 * NP + fs.la];
-        const float r0 = DIR == 0 ? 0.0f : P2.x;
-        const float r1 = DIR == 1 ? 0.0f : P2.y;
-        const float r2 = DIR == 2 ? 0.0f : P2.z;
+        const float r0 = d0 ? 0.0f : P2.x;
+        const float r1 = d1 ? 0.0f : P2.y;
+        const float r2 = d2 ? 0.0f : P2.z;
         const float mr = safe_sqrt(__fmaf_rn(r0, r0, __fmaf_rn(r1, r1, __fmul_rn(r2, r2))));
         const float um_g = mr > 1e-7f ? um_s : mr;
         const float lam = __fmul_rn(0.5f, __fadd_rn(um_g, c_s));
         const float fn = __fmaf_rn(lam, md_s, sg * P2.w);
-        o4 = make_float4(0.0f, DIR == 0 ? fn : 0.0f, DIR == 1 ? fn : 0.0f, DIR == 2 ? fn : 0.0f);
+        o4 = make_float4(0.0f, d0 ? fn : 0.0f, d1 ? fn : 0.0f, d2 ? fn : 0.0f);
         o1 = 0.0f;
     }
 }
@@ -360,12 +379,9 @@ k_mixed_stage(StageArgs a) {
         if (nb <= -2) {
             o4 = make_float4(oth[0], oth[1], oth[2], oth[3]);
             o1 = oth[4];
-        } else if (fs.dir == 0)
-            face_flux<NX, NY, NZ, 0, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
-        else if (G::HAS_Y && fs.dir == 1)
-            face_flux<NX, NY, NZ, 1, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
-        else
-            face_flux<NX, NY, NZ, 2, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
+        } else {
+            face_flux<NX, NY, NZ, VISC, TC>(fs, nb, oth, bgo, gfo, smem, sP, a, o4, o1);
+        }
         sFF4[t] = o4;
         sFF1[t] = o1;
     }
