@@ -97,8 +97,10 @@ typedef struct nsem_mesh_desc {
      * (Mesh::gFMC >= 1; scatter_non_conforming / gather_non_conforming,
      * field.h:2019-2248).  n_mortar = 0 (and NULL pointers) on a conforming
      * mesh.  The FP64 forms (NSEM_REF_SEGREGATED; NSEM_SSPRK3 and
-     * nsem_tendency with NSEM_FP64) and nsem_convection_* step a mesh with
-     * n_mortar > 0; the others return NSEM_UNSUPPORTED.
+     * nsem_tendency with NSEM_FP64), nsem_convection_*, the precision form's
+     * steps (NSEM_MIXED) and the FP64 tangent-linear and adjoint calls take a
+     * mesh with n_mortar > 0, with or without the artificial viscosity; the
+     * precision form's adjoint returns NSEM_UNSUPPORTED there.
      * mortar[4*q .. 4*q+3]: the facet, gFMC (1: the neighbour side FN is the
      * coarse cell, 2: the owner side FO), the coarse cell's face id
      * (gFaceID, 0..5), and the halves of that face the facet covers (bit 0

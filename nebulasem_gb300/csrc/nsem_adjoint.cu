@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a
 }
 
 /* ------------------------------------------------------------------------
- * Non-conforming (2:1) faces, inviscid.  The forward face flux of a mortar
+ * Non-conforming (2:1) faces.  The forward face flux of a mortar
  * slot (nsem_fp64.cu, k_face) reads the coarse side through 19 quantities
  * interpolated from the coarse face's nodes: |U|, c, U rho (3), rho, the
  * momentum flux tensor (rho U) (x) U + p' I (9, tensor order), the theta flux
@@ -227,7 +227,12 @@ __global__ void __launch_bounds__(128) k_adj_face(const NsemDev m, FaceAdjArgs a
  * transposed interpolation, then through the quantities' chain at each
  * coarse node).  The coarse side lifts the projection of the slot fluxes
  * (psiCor) dotted with each slot's normal: its transpose gathers over the
- * facet's slots.
+ * facet's slots.  With the artificial viscosity the momentum and theta flux
+ * quantities carry - mu grad U and - (mu / Pr) grad theta of their node, so
+ * the quantity sets' adjoints also give the nodes' gradient and mu adjoints;
+ * the gradients' own mortar face terms (the coarse side interpolated into
+ * cds, the projection onto the coarse side) are transposed by
+ * k_adj_grad_mortar_a / _b.
  * ------------------------------------------------------------------------ */
 __device__ __forceinline__ void tens_rc(int t, int& ra, int& rb) {
     ra = t < 3 ? t : (t == XY || t == XZ) ? 0 : (t == YZ || t == YX) ? 1 : 2;
@@ -275,8 +280,10 @@ struct VolAdjArgs {
     double* Gbs[12];
     double* mub;
     /* non-conforming faces: per node the adjoints of the 19 face quantities
-     * interpolated from it onto mortar slots (else null) */
+     * interpolated from it onto mortar slots (else null); viscous runs: per
+     * mortar slot the fine side's viscous quantity adjoints */
     const double* qb[19];
+    const double* mqv[12];
 };
 
 /* registers capped for the largest element: 736 threads (N+1 = 9) inviscid,
@@ -361,10 +368,26 @@ __global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const
             Gb[9 + c] = mt * K[c];
             mb += m.iPr * Gn[9 + c] * K[c];
         }
-        for (int j = 0; j < 3; j++) {
+        for (int j = 0; j < m.n_lift; j++) {
             const int32_t code = m.lift[(int64_t)j * m.n_int + node];
             if (code < 0) break;
+            if (code & 2) continue;                 /* a mortar's coarse side: through qb */
             const int64_t k = code >> 2;
+            const int32_t ms = m.n_ms ? m.ms_of[k] : -1;
+            if (ms >= 0) {
+                /* the fine side of a mortar slot */
+                for (int q = 0; q < 9; q++) {
+                    const double b = a.mqv[q][ms];
+                    Gb[q] -= mu * b;
+                    mb -= b * Gn[q];
+                }
+                for (int c = 0; c < 3; c++) {
+                    const double b = a.mqv[9 + c][ms];
+                    Gb[9 + c] -= mt * b;
+                    mb -= m.iPr * b * Gn[9 + c];
+                }
+                continue;
+            }
             const double f = (code & 1) ? 1.0 - m.fi[k] : m.fi[k];
             const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
             const double dm[3] = {a.dbv[0][k], a.dbv[1][k], a.dbv[2][k]}, dt = a.dbv[3][k];
@@ -377,6 +400,20 @@ __global__ void __maxnreg__(VISC ? 128 : 88) k_adj_volume(const NsemDev m, const
             for (int c = 0; c < 3; c++) {
                 Gb[9 + c] -= f * mt * dt * n[c];
                 mb -= f * m.iPr * dt * n[c] * Gn[9 + c];
+            }
+        }
+        if (a.qb[0]) {
+            /* a coarse side of mortar slots: the viscous parts of the node's
+             * interpolated quantities */
+            for (int q = 0; q < 9; q++) {
+                const double b = a.qb[6 + q][node];
+                Gb[q] -= mu * b;
+                mb -= b * Gn[q];
+            }
+            for (int c = 0; c < 3; c++) {
+                const double b = a.qb[15 + c][node];
+                Gb[9 + c] -= mt * b;
+                mb -= m.iPr * b * Gn[9 + c];
             }
         }
         const double icv = 1.0 / m.cv[node];
@@ -479,8 +516,13 @@ __device__ __forceinline__ void sym_jvp(const double* p, const double* en, const
     for (int k = 0; k < 3; k++) dout[k] = Ad[k] * s + r[k] * ds;
 }
 
-/* the 19 face quantities of a node, and their tangents along d (d may be null) */
-__device__ __forceinline__ void face_q(const NodePrim& P, const NodeTan* d, double* q, double* dq) {
+/* the 19 face quantities of a node, and their tangents along d (d may be
+ * null); viscous runs (Gn: the node's 12 gradients, dGn their tangents) take
+ * the momentum and theta fluxes with - mu grad U and - (mu / Pr) grad theta,
+ * mu = rho nu, as the forward's mortar quantities (nsem_fp64.cu) */
+__device__ __forceinline__ void face_q(const NodePrim& P, const NodeTan* d, double* q, double* dq,
+                                       const double* Gn = nullptr, const double* dGn = nullptr,
+                                       double nu = 0.0, double iPr = 0.0) {
     const double Fc[3] = {P.U[0] * P.r, P.U[1] * P.r, P.U[2] * P.r};
     q[0] = P.mu;
     q[1] = P.c;
@@ -493,6 +535,11 @@ __device__ __forceinline__ void face_q(const NodePrim& P, const NodeTan* d, doub
     }
     for (int c = 0; c < 3; c++) q[15 + c] = Fc[c] * P.T;
     q[18] = P.r * P.T;
+    const double mu = P.r * nu, mt = mu * iPr;
+    if (Gn) {
+        for (int t = 0; t < 9; t++) q[6 + t] -= mu * Gn[t];
+        for (int c = 0; c < 3; c++) q[15 + c] -= mt * Gn[9 + c];
+    }
     if (!d) return;
     double dFc[3];
     for (int c = 0; c < 3; c++) dFc[c] = d->U[c] * P.r + P.U[c] * d->r;
@@ -507,6 +554,11 @@ __device__ __forceinline__ void face_q(const NodePrim& P, const NodeTan* d, doub
     }
     for (int c = 0; c < 3; c++) dq[15 + c] = dFc[c] * P.T + Fc[c] * d->T;
     dq[18] = d->r * P.T + P.r * d->T;
+    if (Gn) {
+        const double dmu = nu * d->r, dmt = dmu * iPr;
+        for (int t = 0; t < 9; t++) dq[6 + t] -= dmu * Gn[t] + mu * dGn[t];
+        for (int c = 0; c < 3; c++) dq[15 + c] -= dmt * Gn[9 + c] + mt * dGn[9 + c];
+    }
 }
 
 struct MortarArgs {
@@ -522,7 +574,19 @@ struct MortarArgs {
     double* qb[19];
     double* adjO[NPA];
     double* adjN[NPA];
+    /* viscous runs (else null): the state's gradients and their tangents per
+     * node; out: the fine side's viscous quantity adjoints per mortar slot */
+    const double* G[12];
+    const double* dG[12];
+    double* mqv[12];
 };
+
+/* the 12 gradients (and tangents) of a node for face_q, or null */
+__device__ __forceinline__ const double* node_grads(const double* const* G, int64_t i, double* buf) {
+    if (!G[0]) return nullptr;
+    for (int c = 0; c < 12; c++) buf[c] = G[c][i];
+    return buf;
+}
 
 /* per mortar slot: the coarse side's quantities (and tangents) interpolated */
 __global__ void __launch_bounds__(128) k_mortar_q(const NsemDev m, MortarArgs a) {
@@ -532,11 +596,13 @@ __global__ void __launch_bounds__(128) k_mortar_q(const NsemDev m, MortarArgs a)
     double out[38];
     mortar_interp<38>(m, ms, [&](int64_t node, double* v) {
         const NodePrim P = node_prim(m, a.S, node);
+        double gb[12], dgb[12];
+        const double* Gn = node_grads(a.G, node, gb);
         if (tan) {
             const NodeTan d = node_tan(m, P, a.dS, node);
-            face_q(P, &d, v, v + 19);
+            face_q(P, &d, v, v + 19, Gn, Gn ? node_grads(a.dG, node, dgb) : nullptr, m.nu, m.iPr);
         } else {
-            face_q(P, nullptr, v, nullptr);
+            face_q(P, nullptr, v, nullptr, Gn, nullptr, m.nu, m.iPr);
             for (int c = 19; c < 38; c++) v[c] = 0.0;
         }
     }, out);
@@ -557,11 +623,13 @@ __device__ __forceinline__ void mortar_sides(const NsemDev& m, const MortarArgs&
     double* dqf = side == 1 ? dq2 : dq1;
     double* qc = side == 1 ? q1 : q2;
     double* dqc = side == 1 ? dq1 : dq2;
+    double gb[12], dgb[12];
+    const double* Gn = node_grads(a.G, fine, gb);
     if (tan) {
         const NodeTan d = node_tan(m, Pf, a.dS, fine);
-        face_q(Pf, &d, qf, dqf);
+        face_q(Pf, &d, qf, dqf, Gn, Gn ? node_grads(a.dG, fine, dgb) : nullptr, m.nu, m.iPr);
     } else {
-        face_q(Pf, nullptr, qf, nullptr);
+        face_q(Pf, nullptr, qf, nullptr, Gn, nullptr, m.nu, m.iPr);
     }
     for (int c = 0; c < 19; c++) {
         qc[c] = a.mq[c][ms];
@@ -725,6 +793,12 @@ __global__ void __launch_bounds__(128) k_adj_face_mortar(const NsemDev m, Mortar
     fine_out[4][k] = Tb; fine_out[5][k] = pb;
     for (int v = 0; v < NPA; v++) coarse_out[v][k] = 0.0;
     for (int c = 0; c < 19; c++) a.mqb[c][ms] = qbc[c];
+    if (a.mqv[0]) {
+        /* the fine node's - mu grad U, - (mu / Pr) grad theta parts: taken
+         * by the volume kernel into the node's gradient and mu adjoints */
+        for (int t = 0; t < 9; t++) a.mqv[t][ms] = qbf[6 + t];
+        for (int c = 0; c < 3; c++) a.mqv[9 + c][ms] = qbf[15 + c];
+    }
 }
 
 /* the transposed interpolation: each mortar slot's coarse-side adjoints back
@@ -999,11 +1073,22 @@ struct GradAdjArgs {
     double* agN[4];
     double* G[5];             /* conserved-state adjoint, added to */
     const double* mub;
+    /* non-conforming faces (else null): per node the (U, theta) adjoints of
+     * the mortar slots' gradient face terms; per mortar slot the adjoints of
+     * the fine side's face value and of the coarse side's projected value */
+    double* pbM[4];
+    double* fFb[4];
+    double* gCb[4];
 };
 
 __global__ void __launch_bounds__(256) k_adj_grad_face(const NsemDev m, GradAdjArgs a) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.n_slot) return;
+    if (m.n_ms && m.ms_of[k] >= 0) {
+        /* a mortar slot: k_adj_grad_mortar_* */
+        for (int c = 0; c < 4; c++) a.agO[c][k] = a.agN[c][k] = 0.0;
+        return;
+    }
     const int32_t c1 = m.c1[k], c2 = m.c2[k];
     const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
     const double fi = m.fi[k], fo = 1 - fi;
@@ -1042,6 +1127,83 @@ __global__ void __launch_bounds__(256) k_adj_grad_face(const NsemDev m, GradAdjA
         a.agO[c][k] = p1[c];
         a.agN[c][k] = p2[c];
     }
+}
+
+/* Gradient face terms on mortar slots (forward: k_seg_mortar_gcds,
+ * k_seg_mortar_ggather, k_seg_grad_vol).  Forward, per mortar slot ms with
+ * fine node f and coarse node c (the slot's c1 / c2 by its side), the
+ * gradients take s_f n (x) (fF[ms] - p_f) at f and s_c n (x) (gC[ms] - p_c)
+ * at c (s = +1 on the owner side, -1 on the neighbour side), with
+ * fF = cds of p_f and the coarse side interpolated onto the slot, gC the
+ * facet's fF projected onto c's position.  Adjoint, first pass (per slot):
+ * v = s n . Gbar/cV at f and at c, taken off the nodes' (U, theta) adjoints
+ * and kept as the adjoints of fF (fine) and gC (coarse). */
+__global__ void __launch_bounds__(128) k_adj_grad_mortar_a(const NsemDev m, GradAdjArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const int side = ms_field(m, NSEM_MS_SIDE, ms);
+    const double n[3] = {m.fn[k], m.fn[m.n_slot + k], m.fn[2 * m.n_slot + k]};
+    /* side 1: the coarse node is the owner c1; side 2: the neighbour c2 */
+    const int64_t fine = side == 1 ? m.c2[k] : m.c1[k];
+    const int64_t coarse = side == 1 ? m.c1[k] : m.c2[k];
+    const double sf = side == 1 ? -1.0 : 1.0, sc = -sf;
+    double vf[4], vc[4];
+    for (int c = 0; c < 3; c++) {
+        vf[c] = sf * (n[0] * a.Gbs[tix(0, c)][fine] + n[1] * a.Gbs[tix(1, c)][fine] +
+                      n[2] * a.Gbs[tix(2, c)][fine]);
+        vc[c] = sc * (n[0] * a.Gbs[tix(0, c)][coarse] + n[1] * a.Gbs[tix(1, c)][coarse] +
+                      n[2] * a.Gbs[tix(2, c)][coarse]);
+    }
+    vf[3] = sf * (n[0] * a.Gbs[9][fine] + n[1] * a.Gbs[10][fine] + n[2] * a.Gbs[11][fine]);
+    vc[3] = sc * (n[0] * a.Gbs[9][coarse] + n[1] * a.Gbs[10][coarse] + n[2] * a.Gbs[11][coarse]);
+    for (int c = 0; c < 4; c++) {
+        atomicAdd(a.pbM[c] + fine, -vf[c]);
+        atomicAdd(a.pbM[c] + coarse, -vc[c]);
+        a.fFb[c][ms] = vf[c];
+        a.gCb[c][ms] = vc[c];
+    }
+}
+
+/* second pass (per slot): the adjoint of fF[ms] -- its own part plus the
+ * transposed projection of the facet's gC adjoints -- split by the cds
+ * weights onto the fine node and onto the interpolated coarse value, which
+ * the transposed interpolation returns to the coarse face's nodes */
+__global__ void __launch_bounds__(128) k_adj_grad_mortar_b(const NsemDev m, GradAdjArgs a) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    const int64_t k = ms_field(m, NSEM_MS_K, ms);
+    const int side = ms_field(m, NSEM_MS_SIDE, ms);
+    const int Na = ms_field(m, NSEM_MS_NA, ms), Nb = ms_field(m, NSEM_MS_NB, ms);
+    const int64_t first = ms_field(m, NSEM_MS_FIRST, ms);
+    const int ja = (int)((ms - first) / Nb), jb = (int)((ms - first) % Nb);
+    double fb[4];
+    for (int c = 0; c < 4; c++) fb[c] = a.fFb[c][ms];
+    for (int sa = 0; sa < Na; sa++)
+        for (int sb = 0; sb < Nb; sb++) {
+            const int64_t s2 = first + sa * Nb + sb;
+            const double* Pa = m.psic + ms_field(m, NSEM_MS_TA, s2) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+            const double* Pb = m.psic + ms_field(m, NSEM_MS_TB, s2) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+            const int na = ms_field(m, NSEM_MS_IA, s2), nb = ms_field(m, NSEM_MS_IB, s2);
+            const double w = Pa[ja * Na + na] * Pb[jb * Nb + nb];
+            for (int c = 0; c < 4; c++) fb[c] += w * a.gCb[c][s2];
+        }
+    /* fF = p1 fi + p2 fo, the coarse (interpolated) value on side `side` */
+    const double fi = m.fi[k], fo = 1 - fi;
+    const double wf = side == 1 ? fo : fi, wc = side == 1 ? fi : fo;
+    const int64_t fine = side == 1 ? m.c2[k] : m.c1[k];
+    for (int c = 0; c < 4; c++) atomicAdd(a.pbM[c] + fine, wf * fb[c]);
+    const int base = ms_field(m, NSEM_MS_BASE, ms), sa = ms_field(m, NSEM_MS_SA, ms),
+              sb = ms_field(m, NSEM_MS_SB, ms), ia = ms_field(m, NSEM_MS_IA, ms),
+              ib = ms_field(m, NSEM_MS_IB, ms);
+    const double* Ra = m.psir + ms_field(m, NSEM_MS_TA, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    const double* Rb = m.psir + ms_field(m, NSEM_MS_TB, ms) * NSEM_MAX_NPD * NSEM_MAX_NPD;
+    for (int na = 0; na < Na; na++)
+        for (int nb = 0; nb < Nb; nb++) {
+            const int64_t node = (int64_t)base + na * sa + nb * sb;
+            const double w = wc * Ra[na * Na + ia] * Rb[nb * Nb + ib];
+            for (int c = 0; c < 4; c++) atomicAdd(a.pbM[c] + node, w * fb[c]);
+        }
 }
 
 /* shared layout per node: Gbs[12] jin[9] */
@@ -1108,14 +1270,17 @@ __global__ void k_adj_grad_vol(const NsemDev m, const NsemTables tab, GradAdjArg
         const double dj[3] = {J[XZ] * D, J[YZ] * D, J[ZZ] * D};
         add(la, dj);
     }
-    /* face terms gathered through the lift lists */
-    for (int j = 0; j < 3; j++) {
+    /* face terms gathered through the lift lists (mortar slots: pbM) */
+    for (int j = 0; j < m.n_lift; j++) {
         const int32_t code = m.lift[(int64_t)j * m.n_int + node];
         if (code < 0) break;
+        if (code & 2) continue;
         const int64_t k = code >> 2;
         const double* const* src = (code & 1) ? a.agN : a.agO;
         for (int c = 0; c < 4; c++) pb[c] += src[c][k];
     }
+    if (a.pbM[0])
+        for (int c = 0; c < 4; c++) pb[c] += a.pbM[c][node];
     /* (rho, U, theta) adjoints -> conserved: U = m / rho, theta = E / rho; mu = rho nu */
     const double r = a.S[0][node], inv = 1.0 / r;
     const double U[3] = {a.S[1][node] * inv, a.S[2][node] * inv, a.S[3][node] * inv};
@@ -1166,7 +1331,8 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
         for (int v = 0; v < 5; v++) { pa.S[v] = S[v]; pa.dS[v] = S[v]; }
         for (int c = 0; c < 4; c++) { pa.pU[c] = ab->pU[c]; pa.dpU[c] = ab->dpU[c]; }
         k_tan_prims<<<(unsigned)((m->n_int + 255) / 256), 256, 0, st>>>(*m, pa);
-        const int e = nsem_grad_ut(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF, stream);
+        const int e = nsem_grad_ut_mortar(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF,
+                                          m->n_ms > 0 ? ab->gC : nullptr, stream);
         if (e) return e;
         for (int c = 0; c < 4; c++) fa.dbv[c] = ab->dbv[c];
         for (int c = 0; c < 12; c++) { va.Gv[c] = ab->Gv[c]; va.Gbs[c] = ab->Gbs[c]; }
@@ -1181,6 +1347,8 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
     if (m->n_ms > 0) {
         MortarArgs ma{};
         for (int v = 0; v < 5; v++) { ma.S[v] = S[v]; ma.W[v] = W[v]; }
+        if (ab->visc)
+            for (int c = 0; c < 12; c++) { ma.G[c] = ab->Gv[c]; ma.mqv[c] = ab->mqv[c]; va.mqv[c] = ab->mqv[c]; }
         for (int c = 0; c < 19; c++) { ma.mq[c] = ab->mq[c]; ma.mqb[c] = ab->mqb[c]; ma.qb[c] = ab->qb[c]; }
         for (int v = 0; v < NPA; v++) { ma.adjO[v] = ab->adjO[v]; ma.adjN[v] = ab->adjN[v]; }
         for (int c = 0; c < 19; c++) {
@@ -1201,12 +1369,22 @@ int nsem_adj_vjp(const NsemDev* m, const NsemTables* t, const double* const* S,
     else k_adj_volume<false><<<(unsigned)m->n_elem, threads, smem, st>>>(*m, *t, va);
     if (ab->visc) {
         /* the gradients' transpose, added to the conserved adjoint */
-        GradAdjArgs ga;
+        GradAdjArgs ga{};
         for (int v = 0; v < 5; v++) { ga.S[v] = S[v]; ga.G[v] = G[v]; }
         for (int c = 0; c < 4; c++) { ga.pU[c] = ab->pU[c]; ga.agO[c] = ab->agO[c]; ga.agN[c] = ab->agN[c]; }
         for (int c = 0; c < 12; c++) ga.Gbs[c] = ab->Gbs[c];
         ga.mub = ab->mub;
         k_adj_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
+        if (m->n_ms > 0) {
+            for (int c = 0; c < 4; c++) {
+                ga.pbM[c] = ab->pbM[c]; ga.fFb[c] = ab->fFb[c]; ga.gCb[c] = ab->gCb[c];
+                const cudaError_t ce = cudaMemsetAsync(ab->pbM[c], 0, (size_t)m->n_int * sizeof(double), st);
+                if (ce != cudaSuccess) return (int)ce;
+            }
+            const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+            k_adj_grad_mortar_a<<<mb, 128, 0, st>>>(*m, ga);
+            k_adj_grad_mortar_b<<<mb, 128, 0, st>>>(*m, ga);
+        }
         const size_t gsm = ((size_t)m->np * GADJ_W + 3 * NSEM_MAX_NPD * NSEM_MAX_NPD) * sizeof(double);
         k_adj_grad_vol<<<(unsigned)m->n_elem, threads, gsm, st>>>(*m, *t, ga);
     }
@@ -1225,12 +1403,17 @@ int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
         for (int v = 0; v < 5; v++) { pa.S[v] = S[v]; pa.dS[v] = dS[v]; }
         for (int c = 0; c < 4; c++) { pa.pU[c] = ab->pU[c]; pa.dpU[c] = ab->dpU[c]; }
         k_tan_prims<<<(unsigned)((m->n_int + 255) / 256), 256, 0, st>>>(*m, pa);
-        int e = nsem_grad_ut(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF, stream);
+        const bool mort = m->n_ms > 0;
+        int e = nsem_grad_ut_mortar(m, t, ab->pU, ab->pU[3], ab->Gv, ab->fF, mort ? ab->gC : nullptr, stream);
         if (e) return e;
         GradFaceTanArgs ga;
         for (int c = 0; c < 4; c++) { ga.pU[c] = ab->pU[c]; ga.dpU[c] = ab->dpU[c]; ga.dfF[c] = ab->dfF[c]; }
         k_tan_grad_face<<<(unsigned)((m->n_slot + 255) / 256), 256, 0, st>>>(*m, ga);
-        e = nsem_grad_vol(m, t, ab->dpU, ab->dpU[3], ab->dGv, ab->dfF, stream);
+        /* mortar slots: the face values' tangents are the (linear) mortar
+         * face values of the tangents */
+        if (mort && (e = nsem_grad_mortar_faces(m, ab->dpU, ab->dpU[3], ab->dfF, ab->dgC, stream)))
+            return e;
+        e = nsem_grad_vol(m, t, ab->dpU, ab->dpU[3], ab->dGv, ab->dfF, mort ? ab->dgC : nullptr, stream);
         if (e) return e;
         for (int c = 0; c < 12; c++) {
             fa.G[c] = va.G[c] = ab->Gv[c];
@@ -1244,6 +1427,8 @@ int nsem_adj_jvp(const NsemDev* m, const NsemTables* t, const double* const* S,
     if (m->n_ms > 0) {
         MortarArgs ma{};
         for (int v = 0; v < 5; v++) { ma.S[v] = S[v]; ma.dS[v] = dS[v]; ma.dd[v] = ab->adjO[v]; }
+        if (ab->visc)
+            for (int c = 0; c < 12; c++) { ma.G[c] = ab->Gv[c]; ma.dG[c] = ab->dGv[c]; }
         for (int c = 0; c < 19; c++) { ma.mq[c] = ab->mq[c]; ma.dmq[c] = ab->dmq[c]; }
         for (int c = 0; c < 15; c++) ma.dmf[c] = ab->dmf[c];
         for (int v = 0; v < 5; v++) ma.ddC[v] = ab->ddC[v];

@@ -35,7 +35,7 @@ struct NsemAdjBuf {
     double* mub = nullptr;  /* per node: adjoint of mu = rho nu                   */
     double* agO[4] = {};    /* per slot: gradient face-term adjoints, owner side  */
     double* agN[4] = {};    /* per slot: neighbour side                           */
-    /* non-conforming (2:1) faces, inviscid runs: per mortar slot the coarse
+    /* non-conforming (2:1) faces: per mortar slot the coarse
      * side's 19 interpolated face quantities and their tangents, the tangent
      * flux vectors (15) and the projected, lifted tangents (5), the adjoints of
      * the interpolated quantities; per node the transposed interpolation */
@@ -45,6 +45,18 @@ struct NsemAdjBuf {
     double* ddC[5] = {};
     double* mqb[19] = {};
     double* qb[19] = {};
+    /* non-conforming faces with the artificial viscosity: the gradients'
+     * projected coarse-side face values and their tangents (4 per mortar
+     * slot), the fine side's viscous quantity adjoints (12 per mortar slot),
+     * the gradient face values' adjoints from the fine side and the coarse
+     * side (4 each per mortar slot), and per node the mortars' (U, theta)
+     * adjoints of the gradient face terms */
+    double* gC[4] = {};
+    double* dgC[4] = {};
+    double* mqv[12] = {};
+    double* fFb[4] = {};
+    double* gCb[4] = {};
+    double* pbM[4] = {};
     int nsteps = 0, every = 0, n_ckpt = 0;
     bool ready = false;
 };

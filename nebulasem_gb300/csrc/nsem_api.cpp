@@ -75,16 +75,6 @@ nsem_status require_conforming(nsem_ctx* c) {
     return NSEM_OK;
 }
 
-/* the FP64 tangent-linear and adjoint forms take non-conforming faces in
- * inviscid runs */
-nsem_status require_inviscid_on_mortars(nsem_ctx* c) {
-    if (c && c->dev.n_ms > 0 && c->dev.nu != 0.0)
-        return fail(c, NSEM_UNSUPPORTED,
-                    "non-conforming (2:1) faces with the artificial viscosity: the "
-                    "tangent-linear and adjoint forms are built for inviscid runs there");
-    return NSEM_OK;
-}
-
 nsem_status cuda_fail(nsem_ctx* c, cudaError_t e, const char* where) {
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     return fail(c, NSEM_CUDA_ERROR, m);
@@ -777,7 +767,7 @@ static nsem_status adj_alloc(nsem_ctx* ctx) {
         if ((s = dalloc(ctx, &A.adjN[v], ctx->dev.n_slot)) != NSEM_OK) return s;
     }
     if (ctx->dev.n_ms > 0) {
-        /* non-conforming faces: per mortar slot and per node (inviscid) */
+        /* non-conforming faces: per mortar slot and per node */
         const size_t nm = (size_t)ctx->dev.n_ms, n = (size_t)ctx->dev.n_int;
         for (int c = 0; c < 19; c++) {
             if ((s = dalloc(ctx, &A.mq[c], nm)) != NSEM_OK) return s;
@@ -818,6 +808,18 @@ static nsem_status adj_alloc(nsem_ctx* ctx) {
             if ((s = dalloc(ctx, &A.agN[c], ns)) != NSEM_OK) return s;
         }
         if ((s = dalloc(ctx, &A.mub, n)) != NSEM_OK) return s;
+        if (ctx->dev.n_ms > 0) {
+            const size_t nm = (size_t)ctx->dev.n_ms;
+            for (int c = 0; c < 4; c++) {
+                if ((s = dalloc(ctx, &A.gC[c], nm)) != NSEM_OK) return s;
+                if ((s = dalloc(ctx, &A.dgC[c], nm)) != NSEM_OK) return s;
+                if ((s = dalloc(ctx, &A.fFb[c], nm)) != NSEM_OK) return s;
+                if ((s = dalloc(ctx, &A.gCb[c], nm)) != NSEM_OK) return s;
+                if ((s = dalloc(ctx, &A.pbM[c], n)) != NSEM_OK) return s;
+            }
+            for (int c = 0; c < 12; c++)
+                if ((s = dalloc(ctx, &A.mqv[c], nm)) != NSEM_OK) return s;
+        }
         A.visc = true;
     }
     int e = nsem_adj_prepare(&ctx->dev);
@@ -858,7 +860,6 @@ static nsem_status fp64_step(nsem_ctx* ctx, double* const* keep1, double* const*
 }
 
 extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double* const g[5]) {
-    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
@@ -879,7 +880,6 @@ extern "C" nsem_status nsem_vjp(nsem_ctx* ctx, const double* const w[5], double*
 }
 
 extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double* const Ld[5]) {
-    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!dv || !Ld) return fail(ctx, NSEM_BAD_ARG, "dv or Ld is NULL");
     for (int v = 0; v < 5; v++)
@@ -901,7 +901,6 @@ extern "C" nsem_status nsem_jvp(nsem_ctx* ctx, const double* const dv[5], double
 
 extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const du0[5],
                                 double* const du_final[5], double* ms_tlm) {
-    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps must be >= 1");
     if (!du0 || !du_final) return fail(ctx, NSEM_BAD_ARG, "du0 or du_final is NULL");
@@ -969,7 +968,6 @@ extern "C" nsem_status nsem_tlm(nsem_ctx* ctx, int nsteps, const double* const d
 
 extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                                  double* ms_fwd) {
-    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
@@ -1138,7 +1136,6 @@ static nsem_status mixed_adjoint(nsem_ctx* ctx, const double* const lam_final[5]
 
 extern "C" nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                     double* const lam0[5], double* ms_adj) {
-    if (ctx && require_inviscid_on_mortars(ctx) != NSEM_OK) return NSEM_UNSUPPORTED;
     if (!ctx) return NSEM_BAD_ARG;
     if (!lam_final || !lam0) return fail(ctx, NSEM_BAD_ARG, "lam_final or lam0 is NULL");
     if (ctx->adj_form == 1) {

@@ -941,14 +941,28 @@ int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, 
     return nsem_grad_ut_mortar(m, t, U, T, G, fF, nullptr, stream);
 }
 
+int nsem_grad_mortar_faces(const NsemDev* m, const double* const* U, const double* T,
+                           double* const* fF, double* const* gC, void* stream) {
+    if (m->n_ms == 0) return 0;
+    GradArgs ga{};
+    for (int c = 0; c < 3; c++) ga.U[c] = U[c];
+    ga.Tf = T;
+    for (int c = 0; c < 4; c++) { ga.fF[c] = fF[c]; ga.gC[c] = gC[c]; }
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned mb = (unsigned)((m->n_ms + 127) / 128);
+    k_seg_mortar_gcds<<<mb, 128, 0, st>>>(*m, ga);
+    k_seg_mortar_ggather<<<mb, 128, 0, st>>>(*m, ga);
+    return (int)cudaGetLastError();
+}
+
 int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
-                  double* const* G, const double* const* fF, void* stream) {
+                  double* const* G, const double* const* fF, const double* const* gC, void* stream) {
     GradArgs ga;
     for (int c = 0; c < 3; c++) ga.U[c] = U[c];
     ga.Tf = T;
     for (int c = 0; c < 12; c++) ga.G[c] = G[c];
     for (int c = 0; c < 4; c++) ga.fF[c] = const_cast<double*>(fF[c]);
-    for (int c = 0; c < 4; c++) ga.gC[c] = nullptr;
+    for (int c = 0; c < 4; c++) ga.gC[c] = gC ? const_cast<double*>(gC[c]) : nullptr;
     const int threads = ((m->np + 31) / 32) * 32;
     k_seg_grad_vol<<<(unsigned)m->n_elem, threads, smem_grad(m), (cudaStream_t)stream>>>(*m, *t, ga);
     return (int)cudaGetLastError();

@@ -60,9 +60,16 @@ int nsem_conv_steps_wind(const NsemDev* m, const NsemTables* t, NsemConvBuf* b, 
 /* strong-form gradients of U (3 arrays) and the full theta T into G (12 per
  * node) with the per-slot scratch fF (4), for the viscous fluxes */
 /* the volume part of the gradients only, from given per-slot face values fF
- * (cds of U and theta); linear in (U, T, fF) */
+ * (cds of U and theta) and, on a mesh with non-conforming faces, the
+ * projected coarse-side values gC (4 arrays per mortar slot; else null);
+ * linear in (U, T, fF, gC) */
 int nsem_grad_vol(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
-                  double* const* G, const double* const* fF, void* stream);
+                  double* const* G, const double* const* fF, const double* const* gC, void* stream);
+/* the mortar slots' face values of the gradients alone: cds(U, theta) with
+ * the coarse side interpolated into fF, and its projection onto the coarse
+ * side into gC; linear in (U, T) */
+int nsem_grad_mortar_faces(const NsemDev* m, const double* const* U, const double* T,
+                           double* const* fF, double* const* gC, void* stream);
 int nsem_grad_ut(const NsemDev* m, const NsemTables* t, const double* const* U, const double* T,
                  double* const* G, double* const* fF, void* stream);
 /* the same on a mesh with non-conforming faces: gC (4 arrays per mortar
