@@ -100,6 +100,127 @@ constexpr int stage_min_blocks() {
                       PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
 }
 
+/* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
+ * field.h:3327-3360) for the viscous fluxes: per node
+ *   d_r q = J_r sum_m D_r[a_r][m] q_m  +  (J_r / w_end) (cds(q) - q)  on the
+ *   lower (-) / upper (+) face normal to r through the node,
+ * cds = (own + neighbour) / 2 inside, the ghost value on a wall (SYMMETRY
+ * velocity, NEUMANN theta: cds(theta) - theta = 0 there).  The state is the
+ * stage kernel's (FP32 shadow plus the previous increment for SIN >= 2).
+ * Output [e][12][NP]: tidx(r, c) = d_r U_c, 9 + r = d_r theta.
+ * Written with explicit rounding throughout (no contraction left to the
+ * compiler), so any kernel using these helpers forms the same bits. */
+
+/* U = m / rho as the stage kernel forms it, and theta - T0 from the
+ * perturbation: the background has theta = T0 (Theta_ref = rho_ref T0), so
+ * theta - T0 = (Theta' - T0 rho') / rho -- the same gradient as theta without
+ * FP32 cancellation against T0 */
+__device__ __forceinline__ float4 prim_ut(const float* s, float rref, float T0) {
+    const float inv = rcp_nr(__fadd_rn(rref, s[0]));
+    return make_float4(__fmul_rn(s[1], inv), __fmul_rn(s[2], inv), __fmul_rn(s[3], inv),
+                       __fmul_rn(__fmaf_rn(-T0, s[0], s[4]), inv));
+}
+
+/* the face term cds - own of face node slot t: O the neighbour's values, or
+ * (o == nullptr) the wall ghost of the face's axis */
+__device__ __forceinline__ float4 cds_minus_own(const float4 S, const float4* O, int dir) {
+    float4 c;
+    if (O) {
+        c = make_float4(__fadd_rn(__fmul_rn(0.5f, S.x), __fmul_rn(0.5f, O->x)),
+                        __fadd_rn(__fmul_rn(0.5f, S.y), __fmul_rn(0.5f, O->y)),
+                        __fadd_rn(__fmul_rn(0.5f, S.z), __fmul_rn(0.5f, O->z)),
+                        __fadd_rn(__fmul_rn(0.5f, S.w), __fmul_rn(0.5f, O->w)));
+    } else {
+        /* wall ghost: SYMMETRY velocity, NEUMANN theta */
+        float r0 = dir == 0 ? 0.0f : S.x;
+        float r1 = dir == 1 ? 0.0f : S.y;
+        float r2 = dir == 2 ? 0.0f : S.z;
+        const float mr = safe_sqrt(__fmaf_rn(r0, r0, __fmaf_rn(r1, r1, __fmul_rn(r2, r2))));
+        if (mr > 1e-7f) {
+            const float sc =
+                __fdiv_rn(safe_sqrt(__fmaf_rn(S.x, S.x, __fmaf_rn(S.y, S.y, __fmul_rn(S.z, S.z)))), mr);
+            r0 = __fmul_rn(r0, sc); r1 = __fmul_rn(r1, sc); r2 = __fmul_rn(r2, sc);
+        }
+        c = make_float4(r0, r1, r2, S.w);
+    }
+    return make_float4(__fsub_rn(c.x, S.x), __fsub_rn(c.y, S.y), __fsub_rn(c.z, S.z),
+                       __fsub_rn(c.w, S.w));
+}
+
+/* the gradients of node (i, j, k) from the element's values sV [NP], the
+ * face terms sD [NFS] and the derivative tables sDg; out in the 12-entry
+ * layout */
+template <int NX, int NY, int NZ>
+__device__ __forceinline__ void grad_node(int i, int j, int k, const float4* sV, const float4* sD,
+                                          const float* sDg, const float* Jd, const float* lift,
+                                          float* out) {
+    using G = Geo<NX, NY, NZ>;
+    float4 d[3];
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+        const float* q = sDg + i * QS;
+#pragma unroll
+        for (int m = 0; m < NX; m++) {
+            const float4 v = sV[(m * NY + j) * NZ + k];
+            acc.x = __fmaf_rn(q[m], v.x, acc.x); acc.y = __fmaf_rn(q[m], v.y, acc.y);
+            acc.z = __fmaf_rn(q[m], v.z, acc.z); acc.w = __fmaf_rn(q[m], v.w, acc.w);
+        }
+        d[0] = acc;
+    }
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+        if (NY > 1) {
+            const float* q = sDg + MAXN * QS + j * QS;
+#pragma unroll
+            for (int m = 0; m < NY; m++) {
+                const float4 v = sV[(i * NY + m) * NZ + k];
+                acc.x = __fmaf_rn(q[m], v.x, acc.x); acc.y = __fmaf_rn(q[m], v.y, acc.y);
+                acc.z = __fmaf_rn(q[m], v.z, acc.z); acc.w = __fmaf_rn(q[m], v.w, acc.w);
+            }
+        }
+        d[1] = acc;
+    }
+    {
+        float4 acc = make_float4(0, 0, 0, 0);
+        const float* q = sDg + 2 * MAXN * QS + k * QS;
+#pragma unroll
+        for (int m = 0; m < NZ; m++) {
+            const float4 v = sV[(i * NY + j) * NZ + m];
+            acc.x = __fmaf_rn(q[m], v.x, acc.x); acc.y = __fmaf_rn(q[m], v.y, acc.y);
+            acc.z = __fmaf_rn(q[m], v.z, acc.z); acc.w = __fmaf_rn(q[m], v.w, acc.w);
+        }
+        d[2] = acc;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        d[r].x = __fmul_rn(d[r].x, Jd[r]); d[r].y = __fmul_rn(d[r].y, Jd[r]);
+        d[r].z = __fmul_rn(d[r].z, Jd[r]); d[r].w = __fmul_rn(d[r].w, Jd[r]);
+    }
+    /* face terms: + (J_r / w_end) (cds - own) on the upper face, - on the lower */
+    auto lf = [&](int r, int slot, float coef) {
+        const float4 f = sD[slot];
+        d[r].x = __fmaf_rn(coef, f.x, d[r].x); d[r].y = __fmaf_rn(coef, f.y, d[r].y);
+        d[r].z = __fmaf_rn(coef, f.z, d[r].z); d[r].w = __fmaf_rn(coef, f.w, d[r].w);
+    };
+    const float cx = __fmul_rn(Jd[0], lift[0]), cy = __fmul_rn(Jd[1], lift[1]),
+                cz = __fmul_rn(Jd[2], lift[2]);
+    if (i == 0) lf(0, G::OFF_X + j * NZ + k, -cx);
+    if (i == NX - 1) lf(0, G::OFF_X + G::NFX + j * NZ + k, cx);
+    if (NY > 1) {
+        if (j == 0) lf(1, G::OFF_Y + i * NZ + k, -cy);
+        if (j == NY - 1) lf(1, G::OFF_Y + G::NFY + i * NZ + k, cy);
+    }
+    if (k == 0) lf(2, G::OFF_Z + i * NY + j, -cz);
+    if (k == NZ - 1) lf(2, G::OFF_Z + G::NFZ + i * NY + j, cz);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        out[tidx(r, 0)] = d[r].x;
+        out[tidx(r, 1)] = d[r].y;
+        out[tidx(r, 2)] = d[r].z;
+        out[9 + r] = d[r].w;
+    }
+}
+
 /* phase 2: flux through face node t, seen from the element.  The face's
  * axis is a run-time value (selects, no branches), so a warp whose face
  * nodes lie on faces of two axes runs one instruction stream; the operations
@@ -522,15 +643,6 @@ k_mixed_stage(StageArgs a) {
 
 
 
-/* Strong-form DG gradients of U and theta of a stage state (gradf<true>,
- * field.h:3327-3360) for the viscous fluxes: per node
- *   d_r q = J_r sum_m D_r[a_r][m] q_m  +  (J_r / w_end) (cds(q) - q)  on the
- *   lower (-) / upper (+) face normal to r through the node,
- * cds = (own + neighbour) / 2 inside, the ghost value on a wall (SYMMETRY
- * velocity, NEUMANN theta: cds(theta) - theta = 0 there).  The state is the
- * stage kernel's (FP32 shadow plus the previous increment for SIN >= 2).
- * Output [e][12][NP]: tidx(r, c) = d_r U_c, 9 + r = d_r theta. */
-
 template <int NX, int NY, int NZ, int SIN>
 __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK)
 k_mixed_grad(StageArgs a) {
@@ -579,17 +691,7 @@ k_mixed_grad(StageArgs a) {
     for (int q = t; q < QTAB; q += G::BLOCK) sDg[q] = __ldg(a.Dg + q);
     if (t < 3) sJ[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
 
-    /* U = m / rho as the stage kernel forms it, and theta - T0 from the
-     * perturbation: the background has theta = T0 (Theta_ref = rho_ref T0),
-     * so theta - T0 = (Theta' - T0 rho') / rho -- the same gradient as theta
-     * without FP32 cancellation against T0 */
-    const float T0 = a.T0;
-    auto prim_ut = [T0](const float* s, float rref) {
-        const float inv = rcp_nr(__fadd_rn(rref, s[0]));
-        return make_float4(__fmul_rn(s[1], inv), __fmul_rn(s[2], inv), __fmul_rn(s[3], inv),
-                           __fmul_rn(__fmaf_rn(-T0, s[0], s[4]), inv));
-    };
-    if (t < NP) sV[t] = prim_ut(own, bgs0);
+    if (t < NP) sV[t] = prim_ut(own, bgs0, a.T0);
     __syncthreads();
 
     if (t < NFS && nb <= -2) {
@@ -598,95 +700,18 @@ k_mixed_grad(StageArgs a) {
         sD[t] = make_float4(__ldg(gf), __ldg(gf + a.nfmax), __ldg(gf + 2 * a.nfmax),
                             __ldg(gf + 3 * a.nfmax));
     } else if (t < NFS) {
-        const float4 S = sV[fs.la];
-        float4 c;
-        if (nb >= 0) {
-            const float4 O = prim_ut(oth, bgo0);
-            c = make_float4(0.5f * S.x + 0.5f * O.x, 0.5f * S.y + 0.5f * O.y,
-                            0.5f * S.z + 0.5f * O.z, 0.5f * S.w + 0.5f * O.w);
-        } else {
-            /* wall ghost: SYMMETRY velocity, NEUMANN theta */
-            const int dir = fs.dir;
-            float r0 = dir == 0 ? 0.0f : S.x;
-            float r1 = dir == 1 ? 0.0f : S.y;
-            float r2 = dir == 2 ? 0.0f : S.z;
-            const float mr = safe_sqrt(r0 * r0 + r1 * r1 + r2 * r2);
-            if (mr > 1e-7f) {
-                const float sc = safe_sqrt(S.x * S.x + S.y * S.y + S.z * S.z) / mr;
-                r0 *= sc; r1 *= sc; r2 *= sc;
-            }
-            c = make_float4(r0, r1, r2, S.w);
-        }
-        sD[t] = make_float4(c.x - S.x, c.y - S.y, c.z - S.z, c.w - S.w);
+        const float4 O = nb >= 0 ? prim_ut(oth, bgo0, a.T0) : make_float4(0, 0, 0, 0);
+        sD[t] = cds_minus_own(sV[fs.la], nb >= 0 ? &O : nullptr, fs.dir);
     }
     __syncthreads();
 
     if (t >= NP) return;
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
-    float4 d[3];
-    {
-        float4 acc = make_float4(0, 0, 0, 0);
-        const float* q = sDg + i * QS;
-#pragma unroll
-        for (int m = 0; m < NX; m++) {
-            const float4 v = sV[(m * NY + j) * NZ + k];
-            acc.x = fmaf(q[m], v.x, acc.x); acc.y = fmaf(q[m], v.y, acc.y);
-            acc.z = fmaf(q[m], v.z, acc.z); acc.w = fmaf(q[m], v.w, acc.w);
-        }
-        d[0] = acc;
-    }
-    {
-        float4 acc = make_float4(0, 0, 0, 0);
-        if (NY > 1) {
-            const float* q = sDg + MAXN * QS + j * QS;
-#pragma unroll
-            for (int m = 0; m < NY; m++) {
-                const float4 v = sV[(i * NY + m) * NZ + k];
-                acc.x = fmaf(q[m], v.x, acc.x); acc.y = fmaf(q[m], v.y, acc.y);
-                acc.z = fmaf(q[m], v.z, acc.z); acc.w = fmaf(q[m], v.w, acc.w);
-            }
-        }
-        d[1] = acc;
-    }
-    {
-        float4 acc = make_float4(0, 0, 0, 0);
-        const float* q = sDg + 2 * MAXN * QS + k * QS;
-#pragma unroll
-        for (int m = 0; m < NZ; m++) {
-            const float4 v = sV[(i * NY + j) * NZ + m];
-            acc.x = fmaf(q[m], v.x, acc.x); acc.y = fmaf(q[m], v.y, acc.y);
-            acc.z = fmaf(q[m], v.z, acc.z); acc.w = fmaf(q[m], v.w, acc.w);
-        }
-        d[2] = acc;
-    }
-    const float Jd[3] = {sJ[0], sJ[1], sJ[2]};
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-        d[r].x *= Jd[r]; d[r].y *= Jd[r]; d[r].z *= Jd[r]; d[r].w *= Jd[r];
-    }
-    /* face terms: + (J_r / w_end) (cds - own) on the upper face, - on the lower */
-    auto lift = [&](int r, int slot, float coef) {
-        const float4 f = sD[slot];
-        d[r].x = fmaf(coef, f.x, d[r].x); d[r].y = fmaf(coef, f.y, d[r].y);
-        d[r].z = fmaf(coef, f.z, d[r].z); d[r].w = fmaf(coef, f.w, d[r].w);
-    };
-    const float cx = Jd[0] * a.lift[0], cy = Jd[1] * a.lift[1], cz = Jd[2] * a.lift[2];
-    if (i == 0) lift(0, G::OFF_X + j * NZ + k, -cx);
-    if (i == NX - 1) lift(0, G::OFF_X + G::NFX + j * NZ + k, cx);
-    if (NY > 1) {
-        if (j == 0) lift(1, G::OFF_Y + i * NZ + k, -cy);
-        if (j == NY - 1) lift(1, G::OFF_Y + G::NFY + i * NZ + k, cy);
-    }
-    if (k == 0) lift(2, G::OFF_Z + i * NY + j, -cz);
-    if (k == NZ - 1) lift(2, G::OFF_Z + G::NFZ + i * NY + j, cz);
+    float g12[12];
+    grad_node<NX, NY, NZ>(i, j, k, sV, sD, sDg, sJ, a.lift, g12);
     float* out = a.Gout + e * 12 * NP + t;
 #pragma unroll
-    for (int r = 0; r < 3; r++) {
-        out[tidx(r, 0) * NP] = d[r].x;
-        out[tidx(r, 1) * NP] = d[r].y;
-        out[tidx(r, 2) * NP] = d[r].z;
-        out[(9 + r) * NP] = d[r].w;
-    }
+    for (int c = 0; c < 12; c++) out[c * NP] = g12[c];
 }
 
 template <int NX, int NY, int NZ, bool VISC, bool TC, bool PERSIST>
