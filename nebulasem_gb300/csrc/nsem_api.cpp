@@ -558,7 +558,7 @@ void nsem_destroy(nsem_ctx* ctx) {
     if (ctx->abuf.seg) cudaFree(ctx->abuf.seg);
     {
         NsemMixedBuf& M = ctx->mbuf;
-        void* mp[] = {M.ckpt, M.seg, M.lam, M.fin, M.abar[0], M.abar[1], M.abar[2]};
+        void* mp[] = {M.ckpt, M.seg, M.lam, M.fin, M.abar[0], M.abar[1], M.abar[2], M.GB, M.XB};
         for (void* p : mp)
             if (p) cudaFree(p);
     }
@@ -1018,8 +1018,6 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
 static nsem_status mixed_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                               double* ms_fwd) {
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    if (ctx->mbuf.visc)
-        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
     if (ctx->mbuf.gen)
         return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     nsem_status s = ensure_rep(ctx, 1);
@@ -1072,8 +1070,6 @@ extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const d
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    if (ctx->mbuf.visc)
-        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for inviscid runs");
     if (ctx->mbuf.gen)
         return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     NSEM_CUDA(cudaSetDevice(ctx->device));

@@ -721,7 +721,10 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             }
         mb->lift[d] = (float)(1.0 / w[0]);
         for (int aa = 0; aa < n && aa < 8; aa++)
-            for (int mm = 0; mm < n && mm < 8; mm++) mb->qc[d][aa][mm] = qtab[d * MAXN * QS + aa * QS + mm];
+            for (int mm = 0; mm < n && mm < 8; mm++) {
+                mb->qc[d][aa][mm] = qtab[d * MAXN * QS + aa * QS + mm];
+                mb->dc[d][aa][mm] = dtab[d * MAXN * QS + aa * QS + mm];
+            }
     }
     /* order 7: the tensor-core line sums' B fragments, Q_d^T split into TF32
      * high and low parts as cvt.rna.tf32 does (round to nearest, ties away
@@ -1125,6 +1128,17 @@ int nsem_mixed_step_bufs(const NsemDev* dev, const NsemMixedBuf* mb, const doubl
     a.Unew = Unew;
     a.Snew = Snew;
     return launch_args(mb, a, 3, st);
+}
+
+int nsem_mixed_grad_at(const NsemDev* dev, const NsemMixedBuf* mb, const float* S,
+                       const float* Din, void* stream) {
+    StageArgs a = base_args(dev, mb, 0.0);
+    a.S = S;
+    a.Din = Din;
+    LaunchCfg c{};
+    c.visc = true;
+    c.gen = mb->gen;
+    return dispatch_grad(mb->npd[0], mb->npd[1], mb->npd[2], a, Din ? 2 : 1, (cudaStream_t)stream, c);
 }
 
 int nsem_mixed_convert(const NsemDev* dev, NsemMixedBuf* mb, NsemBuf* b, int to_pert,

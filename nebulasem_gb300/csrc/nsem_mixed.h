@@ -29,6 +29,7 @@ struct NsemMixedBuf {
     float* J = nullptr;           /* [3][n_elem] metric diagonal 2/h        */
     int32_t* layer = nullptr;     /* [n_elem] background layer              */
     float qc[3][8][8] = {};       /* host copy of the line-sum weights      */
+    float dc[3][8][8] = {};       /* host copy of the derivative tables D_d[a][m] */
     float* bg = nullptr;          /* [layers][4][NP] rho_ref, Theta_ref, 1/Theta_ref, p_ref */
     float* Qg = nullptr;          /* line-sum weights Q_d[a][m], row stride MAXN+1 */
     float* Dg = nullptr;          /* derivative tables D_d[a][m] = l_m'(x_a), same layout */
@@ -72,6 +73,8 @@ struct NsemMixedBuf {
     double* lam = nullptr;        /* [5 n_int] FP64 adjoint state             */
     double* fin = nullptr;        /* [5 n_int] FP64 final state of the forward */
     float* abar[3] = {};          /* FP32 stage adjoints: sbar, d2bar, d1bar  */
+    float* GB = nullptr;          /* viscous adjoint: gradient adjoints [e][12][NP] */
+    float* XB = nullptr;          /* viscous adjoint: first-pass state adjoint [e][5][NP] */
     int nsteps = 0, every = 0, n_ckpt = 0;
     int fin_cur = 0;
 };
@@ -99,6 +102,9 @@ bool nsem_mixed_supported(int nx, int ny, int nz);
 int nsem_mixed_step_bufs(const NsemDev* dev, const NsemMixedBuf* mb, const double* U,
                          const float* S, float* d1, float* d2, double* Unew, float* Snew,
                          double dt, void* stream);
+/* viscous runs: the gradients of the stage state S (+ Din) into mb->G */
+int nsem_mixed_grad_at(const NsemDev* dev, const NsemMixedBuf* mb, const float* S,
+                       const float* Din, void* stream);
 
 /* discrete adjoint of the precision form (nsem_mixed_adj.cu) */
 int nsem_mixed_adj_prepare(const NsemMixedBuf* mb);

@@ -60,6 +60,15 @@ struct AdjArgs {
     float lift[3];
     float eos[6];
     float qc[3][8][8];         /* line-sum weights Q_d[a][m] (constant-bank operands) */
+    /* viscous runs: the stage state's gradients [e][12][NP] (forward), the
+     * gradient adjoints [e][12][NP] and the first pass's state adjoint
+     * [e][5][NP] (between the two passes), mu / rho, mu / (rho Pr), T0 and the
+     * derivative tables D_d[a][m] = l_m'(x_a) */
+    const float* Gv;
+    float* GB;
+    float* XB;
+    float nu, nu_pr, T0;
+    float dc[3][8][8];
 };
 
 template <int NX, int NY, int NZ>
@@ -227,7 +236,22 @@ __device__ __forceinline__ void face_adj(const FaceSlot& fs, int32_t nb, const f
     }
 }
 
-template <int NX, int NY, int NZ, int RS>
+/* viscous runs, first pass: the volume flux of direction D carries
+ * - mu d_r U_D (momentum r) and - (mu / Pr) d_D theta, mu = rho nu, so its
+ * adjoint Fbar_D also gives the node's gradient adjoints and, through mu,
+ * a density adjoint */
+template <int D>
+__device__ __forceinline__ void visc_t(const float4& fb, float fb1, const float* gv, float mu,
+                                       float mt, float* gbv, float& sm, float& st) {
+    gbv[tidx(0, D)] = -mu * fb.y;
+    gbv[tidx(1, D)] = -mu * fb.z;
+    gbv[tidx(2, D)] = -mu * fb.w;
+    gbv[9 + D] = -mt * fb1;
+    sm = fmaf(fb.y, gv[tidx(0, D)], fmaf(fb.z, gv[tidx(1, D)], fmaf(fb.w, gv[tidx(2, D)], sm)));
+    st = fmaf(fb1, gv[9 + D], st);
+}
+
+template <int NX, int NY, int NZ, int RS, bool VISC>
 __global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK, (adj_min_blocks<NX, NY, NZ>()))
 k_mixed_adj(AdjArgs a) {
     using G = Geo<NX, NY, NZ>;
@@ -264,6 +288,14 @@ k_mixed_adj(AdjArgs a) {
 #pragma unroll
         for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
     }
+    float gv[12];
+    if constexpr (VISC) {
+        if (t < NP) {
+            const float* gr = a.Gv + e * 12 * NP + t;
+#pragma unroll
+            for (int c = 0; c < 12; c++) gv[c] = __ldg(gr + c * NP);
+        }
+    }
     FaceSlot fs{};
     int32_t nb = -1;
     float xo[5], bgo[4], go[5], cn = 0.0f;
@@ -288,9 +320,10 @@ k_mixed_adj(AdjArgs a) {
     if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
 
     /* phase 1: gbar and the node's values for the face and pointwise transposes */
-    float uu[3], th = 0.0f, pth = 0.0f;
+    float uu[3], th = 0.0f, pth = 0.0f, rho = 0.0f;
     if (t < NP) {
         const Pt p = pointwise(x, bgs, a.eos, a.gamma, a.gR);
+        rho = p.rho;
         const float Th = __fadd_rn(bgs[1], x[4]);
         const float iTh = rcp_nr(Th);
         pth = a.gamma * (bgs[3] + p.pp) * iTh;      /* dp'/dTheta' = gamma p / Theta */
@@ -326,6 +359,10 @@ k_mixed_adj(AdjArgs a) {
     if (t >= NP) return;
     const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
     float xb[5] = {0, 0, 0, 0, 0};
+    /* viscous runs: gradient adjoints and the mu sums of the flux adjoints */
+    float gbv[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float smv = 0.0f, stv = 0.0f;
+    const float mu = rho * a.nu, mt = rho * a.nu_pr;
     {
         /* x: Fbar_x(b) = J_x sum_a Q_x[a][i] gbar(a, j, k) */
         const float* rr = sR + LineLay<NX, NY, NZ, 0>::at(i, j, k);
@@ -340,6 +377,7 @@ k_mixed_adj(AdjArgs a) {
             acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sx];
         }
         jft<0>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+        if constexpr (VISC) visc_t<0>(acc, acc1, gv, mu, mt, gbv, smv, stv);
     }
     if constexpr (G::HAS_Y) {
         const float* rr = sR + LineLay<NX, NY, NZ, 1>::at(i, j, k);
@@ -354,6 +392,7 @@ k_mixed_adj(AdjArgs a) {
             acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sy];
         }
         jft<1>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+        if constexpr (VISC) visc_t<1>(acc, acc1, gv, mu, mt, gbv, smv, stv);
     }
     {
         const float* rr = sR + LineLay<NX, NY, NZ, 2>::at(i, j, k);
@@ -368,6 +407,7 @@ k_mixed_adj(AdjArgs a) {
             acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; acc1 += sFa1[sz];
         }
         jft<2>(uu, th, pth, acc.x, acc.y, acc.z, acc.w, acc1, xb);
+        if constexpr (VISC) visc_t<2>(acc, acc1, gv, mu, mt, gbv, smv, stv);
     }
     /* direct face terms of the faces through the node */
     auto direct = [&](int slot) {
@@ -388,6 +428,18 @@ k_mixed_adj(AdjArgs a) {
     xb[0] = fmaf(a.g[0], gb[1], fmaf(a.g[1], gb[2], fmaf(a.g[2], gb[3], xb[0])));
 
     const int64_t o = e * 5 * NP + t;
+    if constexpr (VISC) {
+        /* mu = (rho_ref + rho') nu: the density adjoint of the viscous
+         * fluxes; the first pass ends here, the gradients' transpose and the
+         * stage combination follow in k_mixed_adj_grad */
+        xb[0] = fmaf(-a.nu, smv, fmaf(-a.nu_pr, stv, xb[0]));
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.XB[o + v * NP] = xb[v];
+        float* gbo = a.GB + e * 12 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 12; c++) gbo[c * NP] = gbv[c];
+        return;
+    }
     if constexpr (RS == 0) {
 #pragma unroll
         for (int v = 0; v < 5; v++) a.Bout[o + v * NP] = xb[v];
@@ -421,16 +473,263 @@ k_mixed_adj(AdjArgs a) {
     }
 }
 
+/* Viscous runs, second pass: the transpose of the gradients of U and
+ * theta - T0 (k_mixed_grad) applied to the first pass's gradient adjoints,
+ * then the stage combination.  Forward, per node a and axis r:
+ *   G_r(a) = J_r sum_m D_r[a_r][m] V_m + sum_faces s (J_r / w_end) (cds - V_a),
+ * V = (U, theta - T0) = prim_ut(x), cds = (V_a + V_o) / 2 inside, the wall
+ * ghost's value on a wall.  Transpose: the line sums with D_r^T (a line
+ * transform, the weights constant operands), and per face node the face
+ * term's adjoint sDbar = s (J_r / w_end) Gbar_r(a): -sDbar / 2 to the node and
+ * +sDbar / 2 to the neighbour's node -- which this element takes from the
+ * neighbour's side of the same face (its gradient adjoints at its face node,
+ * its J_r), so no element writes another's adjoint.  On a wall the ghost's
+ * transpose (the SYMMETRY rescaling) replaces the neighbour's half. */
+template <int NX, int NY, int NZ>
+struct AdjGradSmem {
+    using G = Geo<NX, NY, NZ>;
+    static constexpr int NP = G::NP, NFS = G::NFS;
+    /* floats: gradient-adjoint rows, line-major per axis (4 of the 5 slots);
+     * V [NP] (x4); face contributions [NFS] (x4); metric */
+    static constexpr int OFF_V = (line_floats<NX, NY, NZ>() + 3) / 4 * 4;
+    static constexpr int OFF_F = OFF_V + 4 * NP;
+    static constexpr int OFF_META = OFF_F + 4 * NFS;
+    static constexpr size_t BYTES = sizeof(float) * (OFF_META + 4);
+};
+
+/* the transposed line sums of the gradient rows of axis D (4 quantities) */
+template <int NX, int NY, int NZ, int D>
+__device__ __forceinline__ void grad_transform_t(float* R, const AdjArgs& a, int t) {
+    using LL = LineLay<NX, NY, NZ, D>;
+    constexpr int BLOCK = Geo<NX, NY, NZ>::BLOCK;
+    float* f = R + LL::BASE;
+#pragma unroll 1
+    for (int r = t; r < 4 * LL::NL; r += BLOCK) {
+        float in[LL::n];
+#pragma unroll
+        for (int m = 0; m < LL::n; m++) in[m] = f[m * LL::ROW + r];
+#pragma unroll
+        for (int b = 0; b < LL::n; b++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int m = 0; m < LL::n; m++) acc = fmaf(a.dc[D][m][b], in[m], acc);
+            f[b * LL::ROW + r] = acc;
+        }
+    }
+}
+
+template <int NX, int NY, int NZ, int RS>
+__global__ void __launch_bounds__(Geo<NX, NY, NZ>::BLOCK)
+k_mixed_adj_grad(AdjArgs a) {
+    using G = Geo<NX, NY, NZ>;
+    using SM = AdjGradSmem<NX, NY, NZ>;
+    constexpr int NP = G::NP;
+    constexpr int NFS = G::NFS;
+    extern __shared__ float4 agm4[];
+    float* smem = reinterpret_cast<float*>(agm4);
+    float* sR = smem;
+    float4* sV = reinterpret_cast<float4*>(smem + SM::OFF_V);
+    float4* sF = reinterpret_cast<float4*>(smem + SM::OFF_F);
+    float* sMeta = smem + SM::OFF_META;
+    const int t = threadIdx.x;
+    const int64_t e = blockIdx.x;
+    constexpr bool has_din = RS == 3 || RS == 2;
+
+    float x[5], rref = 0.0f, gbv[12], xbp[5], gb[5];
+    if (t < NP) {
+        const int64_t o = e * 5 * NP + t;
+#pragma unroll
+        for (int v = 0; v < 5; v++) x[v] = __ldg(a.S + o + v * NP);
+        if constexpr (has_din) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) x[v] = __fadd_rn(x[v], __ldg(a.Din + o + v * NP));
+        }
+        rref = __ldg(a.bg + (int64_t)__ldg(a.layer + e) * 4 * NP + t);
+        const float* gr = a.GB + e * 12 * NP + t;
+#pragma unroll
+        for (int c = 0; c < 12; c++) gbv[c] = gr[c * NP];
+#pragma unroll
+        for (int v = 0; v < 5; v++) xbp[v] = a.XB[o + v * NP];
+        load_gbar<RS>(a, o, NP, gb);
+    }
+    FaceSlot fs{};
+    int32_t nb = -1;
+    float4 gbn = make_float4(0, 0, 0, 0);
+    float Jn = 0.0f;
+    if (t < NFS) {
+        fs = face_slot<NX, NY, NZ>(t);
+        nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        if (nb >= 0) {
+            /* the neighbour's gradient adjoints along this face's axis at its node */
+            const float* gr = a.GB + (int64_t)nb * 12 * NP + fs.lo;
+            const int d = fs.dir;
+            gbn = make_float4(gr[tidx(d, 0) * NP], gr[tidx(d, 1) * NP], gr[tidx(d, 2) * NP],
+                              gr[(9 + d) * NP]);
+            Jn = __ldg(a.J + (int64_t)d * a.n_elem + nb);
+        }
+    }
+    if (t < 3) sMeta[t] = __ldg(a.J + (int64_t)t * a.n_elem + e);
+
+    /* phase 1: V of the node, the gradient adjoints into their rows */
+    float inv = 0.0f;
+    if (t < NP) {
+        inv = rcp_nr(__fadd_rn(rref, x[0]));
+        sV[t] = make_float4(__fmul_rn(x[1], inv), __fmul_rn(x[2], inv), __fmul_rn(x[3], inv),
+                            __fmul_rn(__fmaf_rn(-a.T0, x[0], x[4]), inv));
+        const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+        auto put = [&](float* f, int nl, int r) {
+            f[0] = gbv[tidx(r, 0)]; f[nl] = gbv[tidx(r, 1)]; f[2 * nl] = gbv[tidx(r, 2)];
+            f[3 * nl] = gbv[9 + r];
+        };
+        put(sR + LineLay<NX, NY, NZ, 0>::at(i, j, k), LineLay<NX, NY, NZ, 0>::NL, 0);
+        if constexpr (G::HAS_Y) put(sR + LineLay<NX, NY, NZ, 1>::at(i, j, k), LineLay<NX, NY, NZ, 1>::NL, 1);
+        put(sR + LineLay<NX, NY, NZ, 2>::at(i, j, k), LineLay<NX, NY, NZ, 2>::NL, 2);
+    }
+    __syncthreads();
+
+    /* phase 2: per face node the face terms' adjoints for the node */
+    if (t < NFS) {
+        const int r = fs.dir;
+        const int la = fs.la;
+        const int i = la / (NY * NZ), j = (la / NZ) % NY, k = la % NZ;
+        using L0 = LineLay<NX, NY, NZ, 0>;
+        using L1 = LineLay<NX, NY, NZ, 1>;
+        using L2 = LineLay<NX, NY, NZ, 2>;
+        const float* f = sR + (r == 0 ? L0::at(i, j, k) : r == 1 ? L1::at(i, j, k) : L2::at(i, j, k));
+        const int nl = r == 0 ? L0::NL : r == 1 ? L1::NL : L2::NL;
+        const float sg = fs.side ? 1.0f : -1.0f;
+        const float co = sg * sMeta[r] * a.lift[r];
+        const float4 sd = make_float4(co * f[0], co * f[nl], co * f[2 * nl], co * f[3 * nl]);
+        float4 out;
+        if (nb >= 0) {
+            /* own: cds - V_a -> -1/2; the neighbour's face term has V_a in its
+             * cds with weight 1/2 and its own sign (the opposite side) */
+            const float cn = -sg * Jn * a.lift[r];
+            out = make_float4(0.5f * fmaf(cn, gbn.x, -sd.x), 0.5f * fmaf(cn, gbn.y, -sd.y),
+                              0.5f * fmaf(cn, gbn.z, -sd.z), 0.5f * fmaf(cn, gbn.w, -sd.w));
+        } else {
+            /* wall: sD = ghost(V) - V; the ghost's theta is V's (no term), its
+             * velocity the SYMMETRY projection rescaled to |U| (as the forward) */
+            const float4 V = sV[la];
+            const float p[3] = {V.x, V.y, V.z};
+            float rv[3] = {r == 0 ? 0.0f : V.x, r == 1 ? 0.0f : V.y, r == 2 ? 0.0f : V.z};
+            const float gs[3] = {sd.x, sd.y, sd.z};
+            const float Ag[3] = {r == 0 ? 0.0f : gs[0], r == 1 ? 0.0f : gs[1], r == 2 ? 0.0f : gs[2]};
+            const float mr = safe_sqrt(__fmaf_rn(rv[0], rv[0], __fmaf_rn(rv[1], rv[1], __fmul_rn(rv[2], rv[2]))));
+            float ub[3];
+            if (mr > 1e-7f) {
+                const float mp = safe_sqrt(__fmaf_rn(p[0], p[0], __fmaf_rn(p[1], p[1], __fmul_rn(p[2], p[2]))));
+                const float sc = mp / mr;
+                const float rg = rv[0] * gs[0] + rv[1] * gs[1] + rv[2] * gs[2];
+                const float c1 = mp > 0.0f ? rg / (mp * mr) : 0.0f;
+                const float c2 = rg * mp / (mr * mr * mr);
+#pragma unroll
+                for (int c = 0; c < 3; c++) ub[c] = sc * Ag[c] + c1 * p[c] - c2 * rv[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; c++) ub[c] = Ag[c];
+            }
+            out = make_float4(ub[0] - sd.x, ub[1] - sd.y, ub[2] - sd.z, 0.0f);
+        }
+        sF[t] = out;
+    }
+    __syncthreads();
+
+    /* phase 3: transposed line sums */
+    grad_transform_t<NX, NY, NZ, 0>(sR, a, t);
+    if constexpr (G::HAS_Y) grad_transform_t<NX, NY, NZ, 1>(sR, a, t);
+    grad_transform_t<NX, NY, NZ, 2>(sR, a, t);
+    __syncthreads();
+    if (t >= NP) return;
+    const int i = t / (NY * NZ), j = (t / NZ) % NY, k = t % NZ;
+    float vb[4] = {0, 0, 0, 0};
+    auto lines = [&](const float* f, int nl, float J) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) vb[c] = fmaf(J, f[c * nl], vb[c]);
+    };
+    lines(sR + LineLay<NX, NY, NZ, 0>::at(i, j, k), LineLay<NX, NY, NZ, 0>::NL, sMeta[0]);
+    if constexpr (G::HAS_Y) lines(sR + LineLay<NX, NY, NZ, 1>::at(i, j, k), LineLay<NX, NY, NZ, 1>::NL, sMeta[1]);
+    lines(sR + LineLay<NX, NY, NZ, 2>::at(i, j, k), LineLay<NX, NY, NZ, 2>::NL, sMeta[2]);
+    auto face = [&](int slot) {
+        const float4 f = sF[slot];
+        vb[0] += f.x; vb[1] += f.y; vb[2] += f.z; vb[3] += f.w;
+    };
+    {
+        const int sx = face_of_node<NX, NY, NZ, 0>(i, j, k);
+        if (sx >= 0) face(sx);
+        if constexpr (G::HAS_Y) {
+            const int sy = face_of_node<NX, NY, NZ, 1>(i, j, k);
+            if (sy >= 0) face(sy);
+        }
+        const int sz = face_of_node<NX, NY, NZ, 2>(i, j, k);
+        if (sz >= 0) face(sz);
+    }
+    /* V = (m / rho, (Theta' - T0 rho') / rho), rho = rho_ref + rho' */
+    const float4 V = sV[t];
+    float xb[5];
+    xb[0] = xbp[0] - inv * (vb[0] * V.x + vb[1] * V.y + vb[2] * V.z + vb[3] * (a.T0 + V.w));
+    xb[1] = xbp[1] + vb[0] * inv;
+    xb[2] = xbp[2] + vb[1] * inv;
+    xb[3] = xbp[3] + vb[2] * inv;
+    xb[4] = xbp[4] + vb[3] * inv;
+
+    const int64_t o = e * 5 * NP + t;
+    if constexpr (RS == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) a.Bout[o + v * NP] = xb[v];
+        return;
+    }
+    const float dt = a.dt;
+    if constexpr (RS == 3) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x3 = dt * xb[v];
+            a.A[o + v * NP] = x3;
+            a.Bout[o + v * NP] = gb[v] + x3;
+        }
+    } else if constexpr (RS == 2) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x2 = dt * xb[v];
+            a.A[o + v * NP] = __ldg(a.A + o + v * NP) + x2;
+            a.Bout[o + v * NP] = gb[v] + x2;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float x1 = dt * xb[v];
+            const double l = __ldg(a.lam + o + v * NP);
+            a.lam_out[o + v * NP] = l + (f2d(__ldg(a.A + o + v * NP)) + f2d(x1));
+        }
+    }
+}
+
 template <int NX, int NY, int NZ>
 int launch_adj(const AdjArgs& a, int rs, cudaStream_t st) {
     using G = Geo<NX, NY, NZ>;
     constexpr int SMEM = (int)AdjSmem<NX, NY, NZ>::BYTES;
     const unsigned grid = (unsigned)a.n_elem;
+    if (a.GB) {
+        /* viscous: the flux transposes, then the gradients' transpose and the
+         * stage combination */
+        constexpr int GS = (int)AdjGradSmem<NX, NY, NZ>::BYTES;
+        switch (rs) {
+            case 0: k_mixed_adj<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a);
+                    k_mixed_adj_grad<NX, NY, NZ, 0><<<grid, G::BLOCK, GS, st>>>(a); break;
+            case 1: k_mixed_adj<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a);
+                    k_mixed_adj_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, GS, st>>>(a); break;
+            case 2: k_mixed_adj<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a);
+                    k_mixed_adj_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, GS, st>>>(a); break;
+            default: k_mixed_adj<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a);
+                     k_mixed_adj_grad<NX, NY, NZ, 3><<<grid, G::BLOCK, GS, st>>>(a); break;
+        }
+        return (int)cudaGetLastError();
+    }
     switch (rs) {
-        case 0: k_mixed_adj<NX, NY, NZ, 0><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 1: k_mixed_adj<NX, NY, NZ, 1><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        case 2: k_mixed_adj<NX, NY, NZ, 2><<<grid, G::BLOCK, SMEM, st>>>(a); break;
-        default: k_mixed_adj<NX, NY, NZ, 3><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 0: k_mixed_adj<NX, NY, NZ, 0, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 1: k_mixed_adj<NX, NY, NZ, 1, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        case 2: k_mixed_adj<NX, NY, NZ, 2, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+        default: k_mixed_adj<NX, NY, NZ, 3, false><<<grid, G::BLOCK, SMEM, st>>>(a); break;
     }
     return (int)cudaGetLastError();
 }
@@ -438,12 +737,25 @@ int launch_adj(const AdjArgs& a, int rs, cudaStream_t st) {
 template <int NX, int NY, int NZ>
 int prepare_adj() {
     constexpr int SMEM = (int)AdjSmem<NX, NY, NZ>::BYTES;
-    if (SMEM <= 48 * 1024) return 0;
+    constexpr int GS = (int)AdjGradSmem<NX, NY, NZ>::BYTES;
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    int e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 0>, at, SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 1>, at, SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 2>, at, SMEM);
-    if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 3>, at, SMEM);
+    int e = 0;
+    if (SMEM > 48 * 1024) {
+        e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 0, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 1, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 2, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 3, false>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 0, true>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 1, true>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 2, true>, at, SMEM);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj<NX, NY, NZ, 3, true>, at, SMEM);
+    }
+    if (!e && GS > 48 * 1024) {
+        e = (int)cudaFuncSetAttribute(k_mixed_adj_grad<NX, NY, NZ, 0>, at, GS);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj_grad<NX, NY, NZ, 1>, at, GS);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj_grad<NX, NY, NZ, 2>, at, GS);
+        if (!e) e = (int)cudaFuncSetAttribute(k_mixed_adj_grad<NX, NY, NZ, 3>, at, GS);
+    }
     return e;
 }
 
@@ -464,6 +776,15 @@ AdjArgs adj_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
     a.Qg = mb->Qg;
     a.bg = mb->bg;
     a.n_elem = mb->n_elem;
+    if (mb->visc) {
+        a.Gv = mb->G;
+        a.GB = mb->GB;
+        a.XB = mb->XB;
+    }
+    a.nu = mb->nu;
+    a.nu_pr = mb->nu_pr;
+    a.T0 = (float)dev->T0;
+    std::memcpy(a.dc, mb->dc, sizeof(a.dc));
     a.dt = (float)dt;
     a.gamma = (float)dev->gamma;
     a.gR = (float)dev->gR;
@@ -595,6 +916,7 @@ int nsem_mixed_vjp(const NsemDev* dev, NsemMixedBuf* mb, const double* const w[5
     a.S = mb->S[mb->cur];
     a.Gin = scratch_in;
     a.Bout = scratch_out;
+    if (mb->visc && (e = nsem_mixed_grad_at(dev, mb, a.S, nullptr, stream))) return e;
     if ((e = dispatch_adj(mb, a, 0, st))) return e;
 #define NSEM_G(A, B, C)                                                                 \
     if (NP == A * B * C) {                                                              \
@@ -616,6 +938,10 @@ int nsem_mixed_adj_alloc(NsemMixedBuf* mb) {
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->fin, (size_t)n5 * sizeof(double));
     for (int q = 0; q < 3 && ce == cudaSuccess; q++)
         ce = cudaMalloc((void**)&mb->abar[q], (size_t)n5 * sizeof(float));
+    if (ce == cudaSuccess && mb->visc) {
+        ce = cudaMalloc((void**)&mb->GB, (size_t)12 * mb->n_int * sizeof(float));
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->XB, (size_t)n5 * sizeof(float));
+    }
     if (ce != cudaSuccess) return (int)ce;
     return nsem_mixed_adj_prepare(mb);
 }
@@ -707,15 +1033,18 @@ int nsem_mixed_adjoint_run(const NsemDev* dev, NsemMixedBuf* mb, double dt, void
             const float* Sj = mb->seg + (int64_t)j * 3 * n5;
             const float* d1 = Sj + n5;
             const float* d2 = Sj + 2 * n5;
-            /* R3 at x3 = S + d2 */
+            /* R3 at x3 = S + d2 (viscous runs: the stage state's gradients first) */
             a.S = Sj; a.Din = d2; a.lam = mb->lam; a.A = mb->abar[0]; a.Bout = mb->abar[1];
+            if (mb->visc && (e = nsem_mixed_grad_at(dev, mb, Sj, d2, stream))) return e;
             if ((e = dispatch_adj(mb, a, 3, st))) return e;
             /* R2 at x2 = S + d1 */
             a.S = Sj; a.Din = d1; a.Gin = mb->abar[1]; a.A = mb->abar[0]; a.Bout = mb->abar[2];
+            if (mb->visc && (e = nsem_mixed_grad_at(dev, mb, Sj, d1, stream))) return e;
             if ((e = dispatch_adj(mb, a, 2, st))) return e;
             /* R1 at x1 = S */
             a.S = Sj; a.Din = nullptr; a.Gin = mb->abar[2]; a.A = mb->abar[0];
             a.lam = mb->lam; a.lam_out = mb->lam;
+            if (mb->visc && (e = nsem_mixed_grad_at(dev, mb, Sj, nullptr, stream))) return e;
             if ((e = dispatch_adj(mb, a, 1, st))) return e;
         }
     }

@@ -3,13 +3,15 @@
   * transpose test: <w, J(u) du> from the CPU FP64 tangent-linear oracle
     against <J32(u)^T w, du> from the precision form's vector-Jacobian
     product (FP32 at the FP32 shadow of u): agreement to 1e-5 of
-    sum |w . J du|;
+    sum |w . J du|, inviscid and with the artificial viscosity (the viscous
+    fluxes' transposes and the gradients' transpose);
   * gradient of J = 1/2 sum_box theta'^2 at the final time with respect to the
     initial state, precision-form forward and reverse sweep against the plain
     FP64 adjoint (itself checked against the tangent-linear model and finite
-    differences): relative L2 <= 1e-5 of dJ/dtheta'_0, on a golden fixture and
-    on the 48^3, N = 4 bubble (100 steps of dt 0.005 s, checkpoints every 10
-    steps); the rising-bubble box x in [800, 1200], z in [800, 1200] m.
+    differences): relative L2 <= 1e-5 of dJ/dtheta'_0, on golden fixtures
+    (inviscid and viscous) and on the 48^3, N = 4 bubble (100 steps of dt
+    0.005 s, checkpoints every 10 steps); the rising-bubble box x in
+    [800, 1200], z in [800, 1200] m.
 """
 import numpy as np
 import pytest
@@ -26,7 +28,7 @@ def dot(a, b):
     return float(sum(np.dot(x, y) for x, y in zip(a, b)))
 
 
-@pytest.mark.parametrize("case", ["g3_2", "g3_4n3", "c1_2d", "g3_2n7"])
+@pytest.mark.parametrize("case", ["g3_2", "g3_4n3", "c1_2d", "g3_2n7", "g3_2_visc", "c1_2d_visc"])
 def test_mixed_vjp_transpose(case):
     import nebulasem_gb300 as ng
     g = load_golden(case)
@@ -38,7 +40,7 @@ def test_mixed_vjp_transpose(case):
     n = m.n_int
     for trial in range(2):
         du = [rng.standard_normal(n) * sc for sc in (1e-3, 1e-1, 1e-1, 1e-1, 1e-1)]
-        if case == "c1_2d":
+        if case.startswith("c1_2d"):
             du[2][:] = 0.0
         w = [rng.standard_normal(n) for _ in range(5)]
         _, Ld = m.jvp(u, du)
@@ -76,11 +78,12 @@ def _gradients(mesh, u_init, dt, steps, every, box):
     return out
 
 
-def test_mixed_adjoint_gradient_fixture():
-    g = load_golden("g3_2")
+@pytest.mark.parametrize("case", ["g3_2", "g3_2_visc"])
+def test_mixed_adjoint_gradient_fixture(case):
+    g = load_golden(case)
     out = _gradients(g, golden_state(g, "u0"), 0.01, 20, 5, (800.0, 1200.0, 400.0, 1000.0))
     assert out["fp64_J"] > 0
-    assert rel_l2(out["mixed"], out["fp64"]) <= TOL, rel_l2(out["mixed"], out["fp64"])
+    assert rel_l2(out["mixed"], out["fp64"]) <= TOL, (case, rel_l2(out["mixed"], out["fp64"]))
 
 
 def test_mixed_adjoint_gradient_48cubed():
