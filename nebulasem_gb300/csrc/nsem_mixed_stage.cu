@@ -81,7 +81,9 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
 }
 
 /* registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the stage
- * that also carries the FP64 state (measured best on GB300), 6 when viscous */
+ * that also carries the FP64 state (measured best on GB300); viscous runs 6,
+ * and 5 in stage 3 (its gradients and FP64 state spill at 6: 335 against
+ * 365 us at 32^3) */
 #ifndef NSEM_MIXED_MB12
 #define NSEM_MIXED_MB12 8
 #endif
@@ -95,7 +97,7 @@ constexpr int stage_min_blocks() {
     if (Geo<NX, NY, NZ>::BLOCK >= 512)
         return min_blocks((VISC || STAGE == 3 || STAGE == 0) ? 2 : 3, Geo<NX, NY, NZ>::BLOCK,
                           StageSmem<NX, NY, NZ>::BYTES);
-    return min_blocks(VISC ? 6 : (STAGE == 1 || STAGE == 2) ? NSEM_MIXED_MB12 : NSEM_MIXED_MB3,
+    return min_blocks(VISC ? (STAGE == 3 ? 5 : 6) : (STAGE == 1 || STAGE == 2) ? NSEM_MIXED_MB12 : NSEM_MIXED_MB3,
                       Geo<NX, NY, NZ>::BLOCK,
                       PERSIST ? StageSmem<NX, NY, NZ>::BYTES_P : StageSmem<NX, NY, NZ>::BYTES);
 }
