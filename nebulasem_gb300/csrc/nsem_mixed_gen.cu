@@ -116,7 +116,7 @@ k_mixed_stage_gen(StageArgs a) {
     int32_t nb = -1;
     float oth[5], bgo[4], fno[3] = {0, 0, 0};
     if (t < NFS) {
-        fs = face_slot<NX, NY, NZ>(t);
+        fs = face_slot<NX, NY, NZ, STAGE == 1 || STAGE == 2>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
 #pragma unroll
         for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);

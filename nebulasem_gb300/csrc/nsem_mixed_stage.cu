@@ -243,17 +243,22 @@ __device__ __forceinline__ void face_flux(const FaceSlot& fs, int32_t nb, const 
     if (nb >= 0) {
         float4 A4;
         float A1;
-        const int i = fs.la / (NY * NZ), j = (fs.la / NZ) % NY, k = fs.la % NZ;
         if constexpr (TC) {
+            const int i = fs.la / (NY * NZ), j = (fs.la / NZ) % NY, k = fs.la % NZ;
             const float* f = sF + dir * 5 * TC_NP +
                              (d0 ? tc_idx<0>(i, j, k) : d1 ? tc_idx<1>(i, j, k) : tc_idx<2>(i, j, k));
             A4 = make_float4(f[0], f[TC_NP], f[2 * TC_NP], f[3 * TC_NP]);
             A1 = f[4 * TC_NP];
         } else {
+            /* the node's flux row along the face's axis: the face plane's
+             * row (first or last) at the node's in-plane index */
             using L0 = LineLay<NX, NY, NZ, 0>;
             using L1 = LineLay<NX, NY, NZ, 1>;
             using L2 = LineLay<NX, NY, NZ, 2>;
-            const float* f = sF + (d0 ? L0::at(i, j, k) : d1 ? L1::at(i, j, k) : L2::at(i, j, k));
+            const int row = d0 ? L0::BASE + (fs.side ? NX - 1 : 0) * L0::ROW
+                          : d1 ? L1::BASE + (fs.side ? NY - 1 : 0) * L1::ROW
+                               : L2::BASE + (fs.side ? NZ - 1 : 0) * L2::ROW;
+            const float* f = sF + row + fs.r;
             const int nl = d0 ? L0::NL : d1 ? L1::NL : L2::NL;
             A4 = make_float4(f[0], f[nl], f[2 * nl], f[3 * nl]);
             A1 = f[4 * nl];
@@ -418,7 +423,7 @@ k_mixed_stage(StageArgs a) {
     float oth[5], bgo[4];
     float gfo[4] = {0, 0, 0, 0};
     if (t < NFS) {
-        fs = face_slot<NX, NY, NZ>(t);
+        fs = face_slot<NX, NY, NZ, STAGE == 1 || STAGE == 2>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
         if (nb <= -2) {
             /* a face on a 2:1 mortar: its outward values come from the
