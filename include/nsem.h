@@ -212,8 +212,8 @@ nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double
  * the forward's own FP32 stage states and accumulates the adjoint state in
  * FP64.  nsem_vjp_prec: g = J_L(u)^T w in the given form (the precision form
  * at the FP32 shadow of the current state).  The precision form's adjoint
- * needs axis-aligned affine elements and conforming faces (with or without
- * the artificial viscosity; NSEM_UNSUPPORTED otherwise). */
+ * needs conforming faces (any element metric, with or without the artificial
+ * viscosity; NSEM_UNSUPPORTED on meshes with 2:1 mortar faces). */
 nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                            nsem_precision prec, double* ms_fwd);
 nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const double* const w[5],

@@ -1018,8 +1018,6 @@ extern "C" nsem_status nsem_forward_checkpointed(nsem_ctx* ctx, int nsteps, int 
 static nsem_status mixed_forward_checkpointed(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                               double* ms_fwd) {
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    if (ctx->mbuf.gen)
-        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     nsem_status s = ensure_rep(ctx, 1);
     if (s != NSEM_OK) return s;
     ctx->adj_form = -1;
@@ -1070,8 +1068,6 @@ extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const d
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
     if (!ctx->mixed_ready) return fail(ctx, NSEM_UNSUPPORTED, ctx->err);
-    if (ctx->mbuf.gen)
-        return fail(ctx, NSEM_UNSUPPORTED, "the precision-form adjoint is built for axis-aligned elements");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     nsem_status s = ensure_rep(ctx, 1);
     if (s != NSEM_OK) return s;

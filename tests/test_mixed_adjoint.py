@@ -11,7 +11,10 @@
     differences): relative L2 <= 1e-5 of dJ/dtheta'_0, on golden fixtures
     (inviscid and viscous) and on the 48^3, N = 4 bubble (100 steps of dt
     0.005 s, checkpoints every 10 steps); the rising-bubble box x in
-    [800, 1200], z in [800, 1200] m.
+    [800, 1200], z in [800, 1200] m;
+  * inclined and curved elements: the transpose test on the curved 2D
+    fixtures (hill, srtb-curved) and the gradient on the 16^3 bubble box
+    tilted by 30 degrees, inviscid and viscous.
 """
 import numpy as np
 import pytest
@@ -93,3 +96,49 @@ def test_mixed_adjoint_gradient_48cubed():
     assert out["fp64_J"] > 1.0
     err = rel_l2(out["mixed"], out["fp64"])
     assert err <= TOL, err
+
+
+GENERAL = [("seg_hill", 0.0), ("seg_hill", 1.5), ("seg_srtb_curved", 0.0), ("seg_srtb_curved", 1.5)]
+
+
+@pytest.mark.parametrize("case,nu", GENERAL)
+def test_mixed_vjp_transpose_general_geometry(case, nu):
+    """Curved elements (the cosine hill, the srtb-curved arcs: per-node metric
+    and face normals), inviscid and viscous, at a state 5 steps into the run."""
+    import nebulasem_gb300 as ng
+    g = dict(load_golden(case))
+    g["viscosity"] = nu
+    s = ng.Solver(g, dt=float(g["dt"]))
+    s.set_fields(g["fld0_rho"], g["fld0_U"], g["fld0_T"])
+    s.step(5)
+    u = s.get_state()
+    m = oracle.OracleMesh(g)
+    rng = np.random.default_rng(7)
+    n = m.n_int
+    for trial in range(2):
+        du = [rng.standard_normal(n) * sc for sc in (1e-3, 1e-1, 1e-1, 1e-1, 1e-1)]
+        du[2][:] = 0.0
+        w = [rng.standard_normal(n) for _ in range(5)]
+        _, Ld = m.jvp(u, du)
+        lhs = dot(w, Ld)
+        s.set_state(u)
+        gv = s.vjp(w, prec=ng.MIXED)
+        rhs = dot(gv, du)
+        scale = sum(np.abs(x * y).sum() for x, y in zip(w, Ld))
+        assert abs(lhs - rhs) <= TOL * scale, (case, nu, trial, lhs, rhs, scale)
+    s.close()
+
+
+@pytest.mark.parametrize("nu", [0.0, 1.5])
+def test_mixed_adjoint_gradient_tilted_16cubed(nu):
+    """The 16^3, N = 4 bubble in the box tilted by 30 degrees (every element
+    inclined), 20 steps, checkpoints every 5: the precision form's gradient
+    against the FP64 adjoint's."""
+    from nebulasem_gb300.mesh import workload
+    m, u = workload("bubble3d_16_n4_tilt30")
+    m = dict(m)
+    m["viscosity"] = nu
+    out = _gradients(m, u, 0.005 if nu else 0.01, 20, 5, (800.0, 1200.0, 800.0, 1200.0))
+    assert out["fp64_J"] > 0
+    err = rel_l2(out["mixed"], out["fp64"])
+    assert err <= TOL, (nu, err)

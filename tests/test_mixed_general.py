@@ -19,7 +19,7 @@ variable <= 1e-5 at a perturbed developed state; state after 50 SSP-RK3 steps
 <= 1e-5 per conserved variable and in theta'; mass drift <= 1e-12 relative;
 the hydrostatic rest state on the hill stays exactly at rest.  Each mesh
 inviscid and with viscosity 1.5 (the srtb examples' value).  The precision
-form's adjoint on such elements refuses (UNSUPPORTED).
+form's adjoint on such elements: tests/test_mixed_adjoint.py.
 """
 import json
 
@@ -173,14 +173,3 @@ def test_general_geometry_rest_state_is_exact():
         assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max())
     s.close()
 
-
-def test_general_geometry_adjoint_refused():
-    import nebulasem_gb300 as ng
-    g = load_golden("seg_hill")
-    n = int(g["meta"][7])
-    s = ng.Solver(g, dt=float(g["dt"]), viscosity=0.0)
-    s.set_fields(g["fld0_rho"], g["fld0_U"], g["fld0_T"])
-    with pytest.raises(ng.NsemError) as e:
-        s.vjp([np.zeros(n)] * 5, prec=ng.MIXED)
-    assert e.value.status == 5 and "axis-aligned" in str(e.value)
-    s.close()
