@@ -31,6 +31,7 @@ UNITS = [
     ("nsem_mixed_stage.cu", []),
     ("nsem_mixed_gen.cu", []),
     ("nsem_mixed_adj.cu", []),
+    ("nsem_mixed_adj_gen.cu", []),
     ("nsem_noalloc.cu", EXACT),
     ("nsem_seg.cu", EXACT),
     ("nsem_adjoint.cu", []),
