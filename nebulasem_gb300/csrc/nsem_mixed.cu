@@ -78,10 +78,6 @@ namespace {
  *       entries (fine: one, coarse: one per sub-face), scaled by sign / (cV
  *       J_d / w_end) into the outward value the stage kernel lifts.
  * ------------------------------------------------------------------------ */
-enum { MX_FINE, MX_FINE_C1, MX_BASE, MX_SA, MX_SB, MX_NA, MX_NB, MX_IA, MX_IB, MX_FIRST, MX_TA,
-       MX_TB, MX_FIELDS };
-constexpr int MX_COARSE = 1 << 30;
-
 struct MortarMxArgs {
     const int32_t* mi;     /* [MX_FIELDS][n_ms] */
     const float* mf;       /* [8][n_ms] */
@@ -758,7 +754,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
     std::vector<int32_t> mxi[MX_FIELDS];
     std::vector<float> mxf[8];
     std::vector<int32_t> ment, mnode;
-    std::vector<float> mcoef, mgs;
+    std::vector<float> mcoef, mgs, macoef;
     std::map<int64_t, int32_t> mf_of;
     const int nfmax = std::max(nfx, std::max(nfy, nfz));
     if (m->n_mortar > 0) {
@@ -779,18 +775,29 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             nbr[(int64_t)face * ne + e] = -2 - id;
             ment.resize((size_t)(id + 1) * nfmax * 4, -1);
             mcoef.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
+            macoef.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
             mgs.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
             mnode.resize((size_t)(id + 1) * nfmax, -1);
             return id;
         };
-        /* an entry of a face node: the mortar slot, the flux coefficient and
-         * the gradient weight */
-        auto add = [&](int32_t mf, int r, int64_t node, int32_t code, double c, double g) -> bool {
+        /* the lift coefficient of a face node of direction dir in the stage
+         * kernel: J_d / w_end (axis-aligned elements, formed as the kernel
+         * forms it) or 1 / cV (general geometry) */
+        auto liftc = [&](int64_t node, int dir) {
+            if (gen) return 1.0 / m->cV[node];
+            return (double)(J[(int64_t)dir * ne + node / NP] * mb->lift[dir]);
+        };
+        /* an entry of a face node: the mortar slot, the flux coefficient, the
+         * gradient weight and the adjoint weight (minus the lift coefficient
+         * times the flux coefficient) */
+        auto add = [&](int32_t mf, int r, int64_t node, int32_t code, double c, double g,
+                       int dir) -> bool {
             mnode[(size_t)mf * nfmax + r] = (int32_t)node;
             for (int q = 0; q < 4; q++) {
                 const size_t at = ((size_t)mf * nfmax + r) * 4 + q;
                 if (ment[at] < 0) {
                     ment[at] = code; mcoef[at] = (float)c; mgs[at] = (float)g;
+                    macoef[at] = (float)(-liftc(node, dir) * c);
                     return true;
                 }
             }
@@ -849,7 +856,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                     const int64_t k = k0 + (int64_t)ia * Nb + ib;
                     const int64_t fnode = fm == 1 ? m->FO[k] : m->FN[k];
                     const int64_t cnode = fm == 1 ? m->FN[k] : m->FO[k];
-                    if (fnode / NP != cell_f || cnode / NP != cell_c || m->fI[k] != 0.5) {
+                    /* the slot's coarse node is node (ia, ib) of the coarse
+                     * face: the projection lands there and the adjoint's
+                     * interpolation transpose starts from it */
+                    if (fnode / NP != cell_f || cnode / NP != cell_c || m->fI[k] != 0.5 ||
+                        cnode != base + ia * stride[aa] + ib * stride[bb]) {
                         err = "precision form: unexpected mortar slot layout";
                         return NSEM_UNSUPPORTED;
                     }
@@ -880,10 +891,11 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
                     const double sf = gen ? 1.0 : scale(fnode, dir_f), sc = gen ? 1.0 : scale(cnode, fix);
                     const double gf = gen ? (fm == 1 ? 1.0 : -1.0) : mg * sf;
                     const double gc = gen ? (fm == 2 ? 1.0 : -1.0) : mg * sc;
-                    bool ok = add(mf_f, in_face(dir_f, c), fnode, ms, (fm == 1 ? 1.0 : -1.0) * sf, gf);
+                    bool ok = add(mf_f, in_face(dir_f, c), fnode, ms, (fm == 1 ? 1.0 : -1.0) * sf, gf,
+                                  dir_f);
                     loc(cnode, c);
                     ok = ok && add(mf_c, in_face(fix, c), cnode, ms | MX_COARSE,
-                                   (fm == 2 ? 1.0 : -1.0) * sc, gc);
+                                   (fm == 2 ? 1.0 : -1.0) * sc, gc, fix);
                     if (!ok) {
                         err = "precision form: more than four mortar entries on a face node";
                         return NSEM_UNSUPPORTED;
@@ -927,7 +939,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             !up(&mb->mx_F, scratch15) || !up(&mb->mx_d, scratch5) || !up(&mb->mx_dC, scratch5) ||
             !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv) ||
             !up(&mb->mx_gF, scratch4) || !up(&mb->mx_gC, scratch4) || !up(&mb->mf_node, mnode) ||
-            !up(&mb->mf_gs, mgs)) {
+            !up(&mb->mf_gs, mgs) || !up(&mb->mf_acoef, macoef)) {
             err = "precision form: device allocation failed";
             return NSEM_NO_MEMORY;
         }

@@ -64,6 +64,8 @@ struct NsemMixedBuf {
     float* mx_gC = nullptr;       /* [4][n_ms] their projection onto the coarse node */
     int32_t* mf_node = nullptr;   /* [n_mf][nfmax] the element face's node  */
     float* mf_gs = nullptr;       /* [n_mf][nfmax][4] |fN| / (cV J_d / w_end) */
+    float* mf_acoef = nullptr;    /* [n_mf][nfmax][4] the entry's weight in the adjoint: minus
+                                     the lift coefficient of the face node times mf_coef */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */
@@ -75,6 +77,13 @@ struct NsemMixedBuf {
     float* abar[3] = {};          /* FP32 stage adjoints: sbar, d2bar, d1bar  */
     float* GB = nullptr;          /* viscous adjoint: gradient adjoints [e][12][NP] */
     float* XB = nullptr;          /* viscous adjoint: first-pass state adjoint [e][5][NP] */
+    /* adjoint on mortar faces: the fine side's and the projected coarse
+     * side's F.n adjoints, the coarse side's interpolated-quantity adjoints
+     * and the fine node's state adjoint, per slot */
+    float* mxa_db = nullptr;      /* [5][n_ms]  */
+    float* mxa_dCb = nullptr;     /* [5][n_ms]  */
+    float* mxa_qb = nullptr;      /* [19][n_ms] */
+    float* mxa_xf = nullptr;      /* [5][n_ms]  */
     int nsteps = 0, every = 0, n_ckpt = 0;
     int fin_cur = 0;
 };

@@ -213,7 +213,10 @@ k_mixed_adj(AdjArgs a) {
 
     /* phase 2: face adjoints */
     if (t < NFS) {
-        const float cs = sMeta[fs.dir] * a.lift[fs.dir];
+        /* a face on a 2:1 mortar (nb <= -2) lifts the mortar's outward value,
+         * not a flux of its own: a zero coefficient zeroes its face terms
+         * (the mortar transposes add the node's state adjoint afterwards) */
+        const float cs = nb <= -2 ? 0.0f : sMeta[fs.dir] * a.lift[fs.dir];
         float4 fa4, xd4;
         float fa1, xd1;
         face_adj<NX, NY, NZ>(fs, nb, xo, bgo, go, cn, sGb, sP, sT, cs, a, fa4, fa1, xd4, xd1);
@@ -587,15 +590,342 @@ int prepare_adj() {
     return e;
 }
 
+/* ------------------------------------------------------------------------
+ * Transposes of the mortar kernels (inviscid runs).  On a face on a 2:1
+ * mortar the stage kernel lifts MF = sum over the face node's entries of
+ * coef d, with d = F.n at the fine node's slot and dC its projection onto a
+ * coarse node (psiCor); F, the Rusanov flux of the slot, is formed from the
+ * fine node's 19 face quantities and the coarse face's, interpolated with
+ * psiRef (|u|, c, m, rho', the momentum flux tensor, the theta flux, Theta').
+ * Per reverse stage, after the transposed stage kernel (whose face terms
+ * are zero on mortar faces):
+ *   k_mxa_fill_t  per mortar face node: MFbar = -C gbar (C the node's lift
+ *                 coefficient), handed to its entries' dbar and dCbar (each
+ *                 slot has one fine and one coarse entry);
+ *   k_mxa_flux_t  per slot: Fbar = n dbar + the psiCor-weighted n dCbar of
+ *                 the sub-face's slots; the Rusanov transpose gives both
+ *                 sides' face-quantity adjoints; the fine side's go through
+ *                 the fine node's quantity Jacobian into its state adjoint,
+ *                 the coarse side's are kept per slot;
+ *   k_mxa_gather  per mortar face node: the fine node takes its slot's state
+ *                 adjoint; a coarse node sums, per sub-face, the psiRef-
+ *                 weighted coarse-side adjoints of the slots interpolating
+ *                 from it and applies its own quantity Jacobian; the result
+ *                 enters the stage combination like the kernel's xbar
+ *                 (atomic adds: an edge node lies on two faces).
+ * ------------------------------------------------------------------------ */
+struct MxaArgs {
+    const int32_t* mi;     /* [MX_FIELDS][n_ms] */
+    const float* mf;       /* [8][n_ms] */
+    const float* psiR;     /* [6][MAXN^2] */
+    const float* psiC;     /* [6][MAXN^2] */
+    const int32_t* ent;    /* [n_mf][nfmax][4] */
+    const float* acoef;    /* [n_mf][nfmax][4] */
+    const int32_t* node;   /* [n_mf][nfmax] */
+    float* db;             /* [5][n_ms] */
+    float* dCb;            /* [5][n_ms] */
+    float* qb;             /* [19][n_ms] */
+    float* xf;             /* [5][n_ms] */
+    int64_t n_ms, n_mf;
+    int nfmax, np;
+};
+
+/* stage state, background and primitives of one node */
+template <bool HAS_DIN>
+__device__ __forceinline__ Pt mxa_node(const AdjArgs& a, int np, int64_t node, float* x, float* b) {
+    const int64_t e = node / np;
+    const int l = (int)(node - e * np);
+    const int64_t o = e * 5 * np + l;
+#pragma unroll
+    for (int v = 0; v < 5; v++) x[v] = __ldg(a.S + o + v * np);
+    if constexpr (HAS_DIN) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) x[v] = __fadd_rn(x[v], __ldg(a.Din + o + v * np));
+    }
+    const float* bg = a.bg + (int64_t)__ldg(a.layer + e) * 4 * np + l;
+#pragma unroll
+    for (int c = 0; c < 4; c++) b[c] = __ldg(bg + c * np);
+    return pointwise(x, b, a.eos, a.gamma, a.gR);
+}
+
+/* the 19 face quantities of a node, in the mortar flux kernel's layout */
+__device__ __forceinline__ void face_q19(const float* x, const Pt& p, float* f) {
+    f[0] = p.umag;
+    f[1] = p.c;
+#pragma unroll
+    for (int c = 0; c < 3; c++) f[2 + c] = x[1 + c];
+    f[5] = x[0];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[6 + tidx(r, c)] = fmaf(x[1 + r], p.u[c], r == c ? p.pp : 0.0f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) f[15 + c] = x[1 + c] * p.th;
+    f[18] = x[4];
+}
+
+/* xb += (d q19 / dx)^T qb: |u| and c (d|u|/drho' = -|u|/rho, d|u|/dm_k =
+ * u_k / (rho |u|), dc/drho' = -c / (2 rho), dc/dTheta' = c / (2 Theta)),
+ * rho' and Theta' directly, and per direction c the flux vector
+ * (m_c, m_r u_c + p' delta_rc, m_c theta) through the flux Jacobian */
+__device__ __forceinline__ void face_q19_t(const float* x, const float* b, const Pt& p,
+                                           const float* qb, const AdjArgs& a, float* xb) {
+    const float Th = __fadd_rn(b[1], x[4]);
+    const float iTh = rcp_nr(Th);
+    const float ku = p.umag > 0.0f ? p.inv * rcp_nr(p.umag) : 0.0f;
+    xb[0] += fmaf(qb[0], -p.umag * p.inv, fmaf(qb[1], -0.5f * p.c * p.inv, qb[5]));
+#pragma unroll
+    for (int k = 0; k < 3; k++) xb[1 + k] = fmaf(qb[0], p.u[k] * ku, xb[1 + k]);
+    xb[4] += fmaf(qb[1], 0.5f * p.c * iTh, qb[18]);
+    const float pth = a.gamma * (b[3] + p.pp) * iTh;
+    jft<0>(p.u, p.th, pth, qb[2], qb[6 + tidx(0, 0)], qb[6 + tidx(1, 0)], qb[6 + tidx(2, 0)], qb[15], xb);
+    jft<1>(p.u, p.th, pth, qb[3], qb[6 + tidx(0, 1)], qb[6 + tidx(1, 1)], qb[6 + tidx(2, 1)], qb[16], xb);
+    jft<2>(p.u, p.th, pth, qb[4], qb[6 + tidx(0, 2)], qb[6 + tidx(1, 2)], qb[6 + tidx(2, 2)], qb[17], xb);
+}
+
+template <int RS>
+__global__ void __launch_bounds__(128) k_mxa_fill_t(AdjArgs a, MxaArgs m) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= m.n_mf * m.nfmax) return;
+    const int32_t node = __ldg(m.node + id);
+    if (node < 0) return;
+    const int64_t e = node / m.np;
+    float gb[5];
+    load_gbar<RS>(a, e * 5 * m.np + (node - e * m.np), m.np, gb);
+    for (int q = 0; q < 4; q++) {
+        const int32_t en = __ldg(m.ent + id * 4 + q);
+        if (en < 0) break;
+        const float c = __ldg(m.acoef + id * 4 + q);
+        float* dst = (en & MX_COARSE) ? m.dCb : m.db;
+        const int64_t ms = en & (MX_COARSE - 1);
+#pragma unroll
+        for (int v = 0; v < 5; v++) dst[v * m.n_ms + ms] = c * gb[v];
+    }
+}
+
+template <bool HAS_DIN>
+__global__ void __launch_bounds__(128) k_mxa_flux_t(AdjArgs a, MxaArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    /* the forward's face quantities: the fine node's, and the coarse face's
+     * interpolated onto the slot */
+    float xf[5], bf[4], f[19], q[19];
+    const Pt pf = mxa_node<HAS_DIN>(a, m.np, fld(MX_FINE), xf, bf);
+    face_q19(xf, pf, f);
+#pragma unroll
+    for (int c = 0; c < 19; c++) q[c] = 0.0f;
+    const int base = fld(MX_BASE), sa = fld(MX_SA), sb = fld(MX_SB), Na = fld(MX_NA),
+              Nb = fld(MX_NB), ia = fld(MX_IA), ib = fld(MX_IB), first = fld(MX_FIRST),
+              ta = fld(MX_TA), tb = fld(MX_TB);
+    {
+        const float* Pa = m.psiR + ta * MAXN * MAXN;
+        const float* Pb = m.psiR + tb * MAXN * MAXN;
+        for (int na = 0; na < Na; na++)
+            for (int nb = 0; nb < Nb; nb++) {
+                float x[5], b[4], qn[19];
+                const Pt p = mxa_node<HAS_DIN>(a, m.np, (int64_t)base + na * sa + nb * sb, x, b);
+                face_q19(x, p, qn);
+                const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+#pragma unroll
+                for (int c = 0; c < 19; c++) q[c] = fmaf(w, qn[c], q[c]);
+            }
+    }
+    const float* g = m.mf + ms;
+    q[5] += __ldg(g + 6 * m.n_ms);
+    q[18] += __ldg(g + 7 * m.n_ms);
+    const float en[3] = {__ldg(g + 3 * m.n_ms), __ldg(g + 4 * m.n_ms), __ldg(g + 5 * m.n_ms)};
+    /* Fbar: the fine side's d = F.n and the projections of the sub-face's
+     * slots onto their coarse nodes, P(slot k) = sum_j psiCor(j -> k) F_j */
+    float nd[5][3];
+    {
+        const float n[3] = {__ldg(g), __ldg(g + m.n_ms), __ldg(g + 2 * m.n_ms)};
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float d = __ldg(m.db + v * m.n_ms + ms);
+#pragma unroll
+            for (int c = 0; c < 3; c++) nd[v][c] = d * n[c];
+        }
+        const float* Pa = m.psiC + ta * MAXN * MAXN;
+        const float* Pb = m.psiC + tb * MAXN * MAXN;
+        for (int ka = 0; ka < Na; ka++)
+            for (int kb = 0; kb < Nb; kb++) {
+                const int64_t k = first + ka * Nb + kb;
+                const float w = __ldg(Pa + ia * Na + ka) * __ldg(Pb + ib * Nb + kb);
+                const float* gk = m.mf + k;
+                const float nk[3] = {w * __ldg(gk), w * __ldg(gk + m.n_ms), w * __ldg(gk + 2 * m.n_ms)};
+#pragma unroll
+                for (int v = 0; v < 5; v++) {
+                    const float d = __ldg(m.dCb + v * m.n_ms + k);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) nd[v][c] = fmaf(d, nk[c], nd[v][c]);
+                }
+            }
+    }
+    /* Rusanov transpose: F_mass = (A_m + B_m)/2 - en lam (B_rho' - A_rho'),
+     * F_mom[r][c] = (A + B)/2 - en_r lam (B_m - A_m)_c, F_theta likewise with
+     * Theta', lam = ((|u|_A + |u|_B) + (c_A + c_B)) / 4; side 1 is the fine
+     * side when MX_FINE_C1 is set */
+    const bool fine1 = fld(MX_FINE_C1) != 0;
+    float A[19], B[19];
+#pragma unroll
+    for (int c = 0; c < 19; c++) {
+        A[c] = fine1 ? f[c] : q[c];
+        B[c] = fine1 ? q[c] : f[c];
+    }
+    const float lam = 0.25f * ((A[0] + B[0]) + (A[1] + B[1]));
+    float Ab[19], Bb[19];
+#pragma unroll
+    for (int c = 0; c < 19; c++) { Ab[c] = 0.0f; Bb[c] = 0.0f; }
+    float lb = 0.0f;
+    {
+        const float jrb = -(en[0] * nd[0][0] + en[1] * nd[0][1] + en[2] * nd[0][2]);
+        const float jtb = -(en[0] * nd[4][0] + en[1] * nd[4][1] + en[2] * nd[4][2]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            Ab[2 + c] = 0.5f * nd[0][c];
+            Ab[15 + c] = 0.5f * nd[4][c];
+        }
+        lb = fmaf(jrb, B[5] - A[5], jtb * (B[18] - A[18]));
+        Ab[5] = -lam * jrb;
+        Bb[5] = lam * jrb;
+        Ab[18] = -lam * jtb;
+        Bb[18] = lam * jtb;
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) Ab[6 + tidx(r, c)] = 0.5f * nd[1 + r][c];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float dqb = -(en[0] * nd[1][c] + en[1] * nd[2][c] + en[2] * nd[3][c]);
+            lb = fmaf(dqb, B[2 + c] - A[2 + c], lb);
+            Bb[2 + c] = fmaf(lam, dqb, Ab[2 + c]);
+            Ab[2 + c] = fmaf(-lam, dqb, Ab[2 + c]);
+        }
+#pragma unroll
+        for (int c = 6; c < 18; c++) Bb[c] = Ab[c];
+        Ab[0] = Ab[1] = Bb[0] = Bb[1] = 0.25f * lb;
+    }
+    /* the fine side through its node's Jacobian; the coarse side kept */
+    float fb[19];
+#pragma unroll
+    for (int c = 0; c < 19; c++) {
+        fb[c] = fine1 ? Ab[c] : Bb[c];
+        m.qb[c * m.n_ms + ms] = fine1 ? Bb[c] : Ab[c];
+    }
+    float xb[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    face_q19_t(xf, bf, pf, fb, a, xb);
+#pragma unroll
+    for (int v = 0; v < 5; v++) m.xf[v * m.n_ms + ms] = xb[v];
+}
+
+template <int RS>
+__global__ void __launch_bounds__(128) k_mxa_gather(AdjArgs a, MxaArgs m) {
+    constexpr bool HAS_DIN = RS == 3 || RS == 2;
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= m.n_mf * m.nfmax) return;
+    const int32_t node = __ldg(m.node + id);
+    if (node < 0) return;
+    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float qs[19];
+#pragma unroll
+    for (int c = 0; c < 19; c++) qs[c] = 0.0f;
+    bool coarse = false;
+    for (int q = 0; q < 4; q++) {
+        const int32_t en = __ldg(m.ent + id * 4 + q);
+        if (en < 0) break;
+        const int64_t ms = en & (MX_COARSE - 1);
+        if (!(en & MX_COARSE)) {
+#pragma unroll
+            for (int v = 0; v < 5; v++) acc[v] += __ldg(m.xf + v * m.n_ms + ms);
+            continue;
+        }
+        /* the coarse node is node (IA, IB) of the coarse face; the
+         * sub-face's slots interpolate from it with psiRef */
+        coarse = true;
+        auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+        const int Na = fld(MX_NA), Nb = fld(MX_NB), na = fld(MX_IA), nb = fld(MX_IB),
+                  first = fld(MX_FIRST);
+        const float* Pa = m.psiR + fld(MX_TA) * MAXN * MAXN;
+        const float* Pb = m.psiR + fld(MX_TB) * MAXN * MAXN;
+        for (int ia = 0; ia < Na; ia++)
+            for (int ib = 0; ib < Nb; ib++) {
+                const int64_t k = first + ia * Nb + ib;
+                const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+#pragma unroll
+                for (int c = 0; c < 19; c++) qs[c] = fmaf(w, __ldg(m.qb + c * m.n_ms + k), qs[c]);
+            }
+    }
+    if (coarse) {
+        float x[5], b[4];
+        const Pt p = mxa_node<HAS_DIN>(a, m.np, node, x, b);
+        face_q19_t(x, b, p, qs, a, acc);
+    }
+    /* the stage combination of the kernel's xbar: R3, R2 add dt xbar to A
+     * and to the stage output, R1 to lam (FP64), R0 returns xbar */
+    const int64_t e = node / m.np;
+    const int64_t o = e * 5 * m.np + (node - e * m.np);
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        if constexpr (RS == 0) {
+            atomicAdd(a.Bout + o + v * m.np, acc[v]);
+        } else if constexpr (RS == 1) {
+            atomicAdd(a.lam_out + o + v * m.np, (double)(a.dt * acc[v]));
+        } else {
+            const float xv = a.dt * acc[v];
+            atomicAdd(a.A + o + v * m.np, xv);
+            atomicAdd(a.Bout + o + v * m.np, xv);
+        }
+    }
+}
+
+int launch_mortar_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
+    MxaArgs m{};
+    m.mi = mb->mx_i;
+    m.mf = mb->mx_f;
+    m.psiR = mb->mx_psi;
+    m.psiC = mb->mx_psi + 6 * MAXN * MAXN;
+    m.ent = mb->mf_ent;
+    m.acoef = mb->mf_acoef;
+    m.node = mb->mf_node;
+    m.db = mb->mxa_db;
+    m.dCb = mb->mxa_dCb;
+    m.qb = mb->mxa_qb;
+    m.xf = mb->mxa_xf;
+    m.n_ms = mb->n_ms;
+    m.n_mf = mb->n_mf;
+    m.nfmax = mb->nfmax;
+    m.np = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    const unsigned gn = (unsigned)((m.n_mf * m.nfmax + 127) / 128);
+    const unsigned gs = (unsigned)((m.n_ms + 127) / 128);
+    if (rs == 3) k_mxa_fill_t<3><<<gn, 128, 0, st>>>(a, m);
+    else if (rs == 2) k_mxa_fill_t<2><<<gn, 128, 0, st>>>(a, m);
+    else if (rs == 1) k_mxa_fill_t<1><<<gn, 128, 0, st>>>(a, m);
+    else k_mxa_fill_t<0><<<gn, 128, 0, st>>>(a, m);
+    if (rs == 3 || rs == 2) k_mxa_flux_t<true><<<gs, 128, 0, st>>>(a, m);
+    else k_mxa_flux_t<false><<<gs, 128, 0, st>>>(a, m);
+    if (rs == 3) k_mxa_gather<3><<<gn, 128, 0, st>>>(a, m);
+    else if (rs == 2) k_mxa_gather<2><<<gn, 128, 0, st>>>(a, m);
+    else if (rs == 1) k_mxa_gather<1><<<gn, 128, 0, st>>>(a, m);
+    else k_mxa_gather<0><<<gn, 128, 0, st>>>(a, m);
+    return (int)cudaGetLastError();
+}
 
 int dispatch_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
     const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
-    if (mb->gen) return launch_adj_general(nx, ny, nz, a, rs, st);
+    /* mortar transposes are built for inviscid runs */
+    if (mb->visc && mb->n_ms > 0) return (int)cudaErrorNotSupported;
+    int e = (int)cudaErrorNotSupported;
+    if (mb->gen) {
+        e = launch_adj_general(nx, ny, nz, a, rs, st);
+    } else {
 #define NSEM_ADJ(A, B, C) \
-    if (nx == A && ny == B && nz == C) return launch_adj<A, B, C>(a, rs, st);
-    NSEM_MIXED_DIMS(NSEM_ADJ)
+        if (nx == A && ny == B && nz == C) e = launch_adj<A, B, C>(a, rs, st);
+        NSEM_MIXED_DIMS(NSEM_ADJ)
 #undef NSEM_ADJ
-    return (int)cudaErrorNotSupported;
+    }
+    if (e == 0 && mb->n_ms > 0) e = launch_mortar_adj(mb, a, rs, st);
+    return e;
 }
 
 AdjArgs adj_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
@@ -777,6 +1107,12 @@ int nsem_mixed_adj_alloc(NsemMixedBuf* mb) {
     if (ce == cudaSuccess && mb->visc) {
         ce = cudaMalloc((void**)&mb->GB, (size_t)12 * mb->n_int * sizeof(float));
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->XB, (size_t)n5 * sizeof(float));
+    }
+    if (ce == cudaSuccess && mb->n_ms > 0) {
+        ce = cudaMalloc((void**)&mb->mxa_db, (size_t)5 * mb->n_ms * sizeof(float));
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_dCb, (size_t)5 * mb->n_ms * sizeof(float));
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_qb, (size_t)19 * mb->n_ms * sizeof(float));
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_xf, (size_t)5 * mb->n_ms * sizeof(float));
     }
     if (ce != cudaSuccess) return (int)ce;
     return nsem_mixed_adj_prepare(mb);

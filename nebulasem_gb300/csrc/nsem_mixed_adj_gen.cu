@@ -96,8 +96,11 @@ k_mixed_adj_gen(AdjArgs a) {
     if (t < NFS) {
         fs = face_slot<NX, NY, NZ>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        /* a face on a 2:1 mortar (nb <= -2) lifts the mortar's outward value,
+         * not a flux of its own: a zero normal zeroes its face terms (the
+         * mortar transposes add the node's state adjoint afterwards) */
 #pragma unroll
-        for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);
+        for (int c = 0; c < 3; c++) fno[c] = nb <= -2 ? 0.0f : __ldg(a.Fn + (e * 3 + c) * NFS + t);
         if (nb >= 0) {
             const int64_t o = (int64_t)nb * 5 * NP + fs.lo;
 #pragma unroll

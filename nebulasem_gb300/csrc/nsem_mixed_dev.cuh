@@ -27,6 +27,15 @@
 namespace nsem_mx {
 
 constexpr int MAXN = NSEM_MAX_NPD;
+
+/* fields of a mortar slot ([MX_FIELDS][n_ms]): the fine node, whether the
+ * fine element is side 1, the coarse face's first node and strides, its node
+ * counts, the slot's interpolation indices (ia, ib), the sub-face's first
+ * slot and its psiRef / psiCor tables.  A face node's entry names a slot,
+ * with MX_COARSE set for the coarse side's projected value. */
+enum { MX_FINE, MX_FINE_C1, MX_BASE, MX_SA, MX_SB, MX_NA, MX_NB, MX_IA, MX_IB, MX_FIRST, MX_TA,
+       MX_TB, MX_FIELDS };
+constexpr int MX_COARSE = 1 << 30;
 constexpr int QS = MAXN + 1;            /* row stride of the line tables (bank-conflict free) */
 constexpr int QTAB = 3 * MAXN * QS;     /* floats per line table */
 

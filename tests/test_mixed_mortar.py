@@ -19,7 +19,14 @@ mortars):
   * 40 SSP-RK3 steps from the fixture's state: relative L2 per conserved
     variable and in theta' <= 1e-5, mass drift <= 1e-12 relative;
   * each mesh inviscid and with viscosity 1.5 (the 2D fixture's value);
-  * the precision form's adjoint refuses the refined mesh (UNSUPPORTED).
+  * the precision form's adjoint (inviscid): the transposed stage with the
+    transposes of the mortar kernels, <w, J du> from the plain FP64 tangent
+    (tests/test_amr_tangent.py checks it against central differences and its
+    own adjoint) against <J32^T w, du> to 1e-5 of sum |w . J du|; the gradient
+    of 1/2 sum_box theta'^2 after 20 steps (checkpoints every 5) from the
+    precision-form forward and reverse sweep against the FP64 adjoint's,
+    relative L2 <= 1e-5; with the viscosity it refuses the refined mesh
+    (UNSUPPORTED).
 """
 import json
 
@@ -100,11 +107,74 @@ def test_mortar_trajectory_vs_fp64(case, visc):
         assert abs(out[t + "_drift"]) <= 1e-12, (t, out[t + "_drift"])
 
 
-def test_mortar_adjoint_refused():
+def dot(a, b):
+    return float(sum(np.dot(x, y) for x, y in zip(a, b)))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mortar_vjp_transpose(case):
     import nebulasem_gb300 as ng
-    s, u0, g = solver("amr_g3_4n3")
+    s, u0, g = solver(case)
+    s.set_state(u0)
+    s.step(5, prec=ng.FP64)
+    u = s.get_state()
+    two_d = int(g["meta"][1]) == 1
+    rng = np.random.default_rng(9)
+    n = len(u[0])
+    for trial in range(2):
+        du = [rng.standard_normal(n) * sc for sc in (1e-3, 1e-1, 1e-1, 1e-1, 1e-1)]
+        if two_d:
+            du[2][:] = 0.0
+        w = [rng.standard_normal(n) for _ in range(5)]
+        s.set_state(u)
+        Ld = s.jvp(du)
+        gv = s.vjp(w, prec=ng.MIXED)
+        lhs, rhs = dot(w, Ld), dot(gv, du)
+        scale = sum(np.abs(x * y).sum() for x, y in zip(w, Ld))
+        assert abs(lhs - rhs) <= TOL * scale, (case, trial, lhs, rhs, scale)
+    s.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mortar_adjoint_gradient(case):
+    import nebulasem_gb300 as ng
+    from nebulasem_gb300 import objective as ob
+    s, u_fix, g = solver(case)
+    n = len(u_fix[0])
+    xyz = np.asarray(g["cC"]).reshape(-1, 3)[:n]
+    p_ref = np.asarray(g["p_ref"])[:n]
+    th0 = u_fix[4] / u_fix[0] - 300.0
+    u0 = ob.state_from_theta(th0, p_ref)
+    lo, hi = xyz.min(axis=0), xyz.max(axis=0)
+    mid, half = (lo + hi) / 2, (hi - lo) / 4
+    box = (mid[0] - half[0], mid[0] + half[0], mid[2] - half[2], mid[2] + half[2])
+    mask = ob.box_mask(xyz, box)
+    assert mask.any()
+    out = {}
+    for prec, tag in ((ng.FP64, "fp64"), (ng.MIXED, "mixed")):
+        s.set_state(u0)
+        s.forward_checkpointed(20, 5, prec=prec)
+        uN = s.get_state()
+        lam0, _ = s.adjoint(ob.objective_grad(uN, mask))
+        out[tag] = lam0
+        out[tag + "_th"] = ob.theta_grad(lam0, u0, th0)
+        out[tag + "_J"] = ob.objective(uN, mask)
+    s.close()
+    assert out["fp64_J"] > 0
+    err_th = rel_l2(out["mixed_th"], out["fp64_th"])
+    err_all = rel_l2(np.concatenate(out["mixed"]), np.concatenate(out["fp64"]))
+    print(case, "dJ/dtheta'", err_th, "dJ/du", err_all)
+    assert err_th <= TOL, (case, err_th)
+    assert err_all <= TOL, (case, err_all)
+
+
+def test_mortar_adjoint_viscous_refused():
+    import nebulasem_gb300 as ng
+    s, u0, g = solver("amr_g3_4n3", 1.5)
     s.set_state(u0)
     with pytest.raises(ng.NsemError) as e:
         s.vjp([np.zeros(len(u0[0]))] * 5, prec=ng.MIXED)
     assert e.value.status == 5 and "non-conforming" in str(e.value)
+    with pytest.raises(ng.NsemError):
+        s.forward_checkpointed(4, 2, prec=ng.MIXED)
     s.close()
