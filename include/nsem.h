@@ -99,9 +99,8 @@ typedef struct nsem_mesh_desc {
      * mesh.  The FP64 forms (NSEM_REF_SEGREGATED; NSEM_SSPRK3 and
      * nsem_tendency with NSEM_FP64), nsem_convection_*, the precision form's
      * steps (NSEM_MIXED) and the FP64 tangent-linear and adjoint calls take a
-     * mesh with n_mortar > 0, with or without the artificial viscosity; the
-     * precision form's adjoint takes it without the viscosity (returns
-     * NSEM_UNSUPPORTED with it).
+     * mesh with n_mortar > 0, with or without the artificial viscosity, and
+     * so does the precision form's adjoint.
      * mortar[4*q .. 4*q+3]: the facet, gFMC (1: the neighbour side FN is the
      * coarse cell, 2: the owner side FO), the coarse cell's face id
      * (gFaceID, 0..5), and the halves of that face the facet covers (bit 0
@@ -213,9 +212,8 @@ nsem_status nsem_adjoint(nsem_ctx* ctx, const double* const lam_final[5], double
  * the forward's own FP32 stage states and accumulates the adjoint state in
  * FP64.  nsem_vjp_prec: g = J_L(u)^T w in the given form (the precision form
  * at the FP32 shadow of the current state).  The precision form's adjoint
- * takes any element metric with or without the artificial viscosity; on
- * meshes with 2:1 mortar faces it takes inviscid runs (NSEM_UNSUPPORTED
- * with the viscosity there). */
+ * takes any element metric and 2:1 mortar faces, with or without the
+ * artificial viscosity. */
 nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps, int ckpt_every,
                                            nsem_precision prec, double* ms_fwd);
 nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const double* const w[5],

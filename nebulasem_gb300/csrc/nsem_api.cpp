@@ -75,15 +75,6 @@ nsem_status require_conforming(nsem_ctx* c) {
     return NSEM_OK;
 }
 
-/* the precision form's adjoint takes 2:1 mortar faces in inviscid runs */
-nsem_status require_prec_adjoint_mesh(nsem_ctx* c) {
-    if (c && c->dev.n_ms > 0 && c->dev.nu != 0.0)
-        return fail(c, NSEM_UNSUPPORTED,
-                    "non-conforming (2:1) faces with the artificial viscosity: the precision "
-                    "form's adjoint takes them in inviscid runs (the FP64 adjoint takes both)");
-    return NSEM_OK;
-}
-
 nsem_status cuda_fail(nsem_ctx* c, cudaError_t e, const char* where) {
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     return fail(c, NSEM_CUDA_ERROR, m);
@@ -568,7 +559,8 @@ void nsem_destroy(nsem_ctx* ctx) {
     {
         NsemMixedBuf& M = ctx->mbuf;
         void* mp[] = {M.ckpt, M.seg, M.lam, M.fin, M.abar[0], M.abar[1], M.abar[2], M.GB, M.XB,
-                      M.mxa_db, M.mxa_dCb, M.mxa_qb, M.mxa_xf};
+                      M.mxa_db, M.mxa_dCb, M.mxa_qb, M.mxa_xf, M.mxa_gf, M.mxa_gFb, M.mxa_gCb,
+                      M.mxa_vh, M.mxa_vown};
         for (void* p : mp)
             if (p) cudaFree(p);
     }
@@ -1062,7 +1054,6 @@ extern "C" nsem_status nsem_forward_checkpointed_prec(nsem_ctx* ctx, int nsteps,
     if (!ctx) return NSEM_BAD_ARG;
     if (prec == NSEM_FP64) return nsem_forward_checkpointed(ctx, nsteps, ckpt_every, ms_fwd);
     if (prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
-    if (nsem_status rs = require_prec_adjoint_mesh(ctx)) return rs;
     if (nsteps < 1 || ckpt_every < 1) return fail(ctx, NSEM_BAD_ARG, "nsteps and ckpt_every must be >= 1");
     NSEM_CUDA(cudaSetDevice(ctx->device));
     return mixed_forward_checkpointed(ctx, nsteps, ckpt_every, ms_fwd);
@@ -1073,7 +1064,6 @@ extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const d
     if (!ctx) return NSEM_BAD_ARG;
     if (prec == NSEM_FP64) return nsem_vjp(ctx, w, g);
     if (prec != NSEM_MIXED) return fail(ctx, NSEM_BAD_ARG, "unknown precision");
-    if (nsem_status rs = require_prec_adjoint_mesh(ctx)) return rs;
     if (!w || !g) return fail(ctx, NSEM_BAD_ARG, "w or g is NULL");
     for (int v = 0; v < 5; v++)
         if (!w[v] || !g[v]) return fail(ctx, NSEM_BAD_ARG, "w[v] or g[v] is NULL");
@@ -1098,7 +1088,6 @@ extern "C" nsem_status nsem_vjp_prec(nsem_ctx* ctx, nsem_precision prec, const d
 /* the precision form's reverse sweep of the last checkpointed run */
 static nsem_status mixed_adjoint(nsem_ctx* ctx, const double* const lam_final[5],
                                  double* const lam0[5], double* ms_adj) {
-    if (nsem_status rs = require_prec_adjoint_mesh(ctx)) return rs;
     NsemMixedBuf& M = ctx->mbuf;
     NsemBuf* b = &ctx->buf;
     const size_t bytes = (size_t)ctx->dev.n_int * sizeof(double);

@@ -753,7 +753,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
      * per element face on a mortar its node entries */
     std::vector<int32_t> mxi[MX_FIELDS];
     std::vector<float> mxf[8];
-    std::vector<int32_t> ment, mnode;
+    std::vector<int32_t> ment, mnode, mface;
     std::vector<float> mcoef, mgs, macoef;
     std::map<int64_t, int32_t> mf_of;
     const int nfmax = std::max(nfx, std::max(nfy, nfz));
@@ -772,6 +772,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             if (it != mf_of.end()) return it->second;
             const int32_t id = (int32_t)mf_of.size();
             mf_of.emplace(key, id);
+            mface.push_back(face);
             nbr[(int64_t)face * ne + e] = -2 - id;
             ment.resize((size_t)(id + 1) * nfmax * 4, -1);
             mcoef.resize((size_t)(id + 1) * nfmax * 4, 0.0f);
@@ -939,7 +940,7 @@ nsem_status nsem_mixed_setup(const NsemDev& dev, const nsem_mesh_desc* m, NsemMi
             !up(&mb->mx_F, scratch15) || !up(&mb->mx_d, scratch5) || !up(&mb->mx_dC, scratch5) ||
             !up(&mb->mf_ent, ment) || !up(&mb->mf_coef, mcoef) || !up(&mb->MF, mfv) ||
             !up(&mb->mx_gF, scratch4) || !up(&mb->mx_gC, scratch4) || !up(&mb->mf_node, mnode) ||
-            !up(&mb->mf_gs, mgs) || !up(&mb->mf_acoef, macoef)) {
+            !up(&mb->mf_gs, mgs) || !up(&mb->mf_acoef, macoef) || !up(&mb->mf_face, mface)) {
             err = "precision form: device allocation failed";
             return NSEM_NO_MEMORY;
         }
@@ -1150,6 +1151,11 @@ int nsem_mixed_grad_at(const NsemDev* dev, const NsemMixedBuf* mb, const float* 
     LaunchCfg c{};
     c.visc = true;
     c.gen = mb->gen;
+    /* the gradients' face values on mortars first */
+    if (mb->n_ms > 0) {
+        const int e = launch_mortar_grads(mb, a, Din ? 2 : 1, (cudaStream_t)stream);
+        if (e) return e;
+    }
     return dispatch_grad(mb->npd[0], mb->npd[1], mb->npd[2], a, Din ? 2 : 1, (cudaStream_t)stream, c);
 }
 

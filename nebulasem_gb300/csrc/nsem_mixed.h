@@ -66,6 +66,7 @@ struct NsemMixedBuf {
     float* mf_gs = nullptr;       /* [n_mf][nfmax][4] |fN| / (cV J_d / w_end) */
     float* mf_acoef = nullptr;    /* [n_mf][nfmax][4] the entry's weight in the adjoint: minus
                                      the lift coefficient of the face node times mf_coef */
+    int32_t* mf_face = nullptr;   /* [n_mf] the element face (2 dir + side) */
     float nu = 0, nu_pr = 0;      /* nu and nu / Pr                         */
     float lift[3] = {0, 0, 0};    /* 1 / w_end per direction                */
     /* discrete adjoint (allocated on first use) */
@@ -84,6 +85,15 @@ struct NsemMixedBuf {
     float* mxa_dCb = nullptr;     /* [5][n_ms]  */
     float* mxa_qb = nullptr;      /* [19][n_ms] */
     float* mxa_xf = nullptr;      /* [5][n_ms]  */
+    /* viscous runs: the fine node's gradient adjoints per slot, the
+     * gradients' face values' adjoints (fine and coarse entries), their
+     * half-weighted totals per slot, and per mortar face node the adjoint of
+     * its own V through the face terms */
+    float* mxa_gf = nullptr;      /* [12][n_ms] */
+    float* mxa_gFb = nullptr;     /* [4][n_ms]  */
+    float* mxa_gCb = nullptr;     /* [4][n_ms]  */
+    float* mxa_vh = nullptr;      /* [4][n_ms]  */
+    float* mxa_vown = nullptr;    /* [4][n_mf nfmax] */
     int nsteps = 0, every = 0, n_ckpt = 0;
     int fin_cur = 0;
 };

@@ -429,7 +429,9 @@ k_mixed_adj_grad(AdjArgs a) {
         const float* f = sR + (r == 0 ? L0::at(i, j, k) : r == 1 ? L1::at(i, j, k) : L2::at(i, j, k));
         const int nl = r == 0 ? L0::NL : r == 1 ? L1::NL : L2::NL;
         const float sg = fs.side ? 1.0f : -1.0f;
-        const float co = sg * sMeta[r] * a.lift[r];
+        /* a face on a 2:1 mortar: a zero coefficient zeroes the face terms
+         * here; the mortar gradient transposes take them */
+        const float co = nb <= -2 ? 0.0f : sg * sMeta[r] * a.lift[r];
         const float4 sd = make_float4(co * f[0], co * f[nl], co * f[2 * nl], co * f[3 * nl]);
         float4 out;
         if (nb >= 0) {
@@ -536,23 +538,29 @@ k_mixed_adj_grad(AdjArgs a) {
 }
 
 template <int NX, int NY, int NZ>
-int launch_adj(const AdjArgs& a, int rs, cudaStream_t st) {
+int launch_adj(const AdjArgs& a, int rs, cudaStream_t st, int passes) {
     using G = Geo<NX, NY, NZ>;
     constexpr int SMEM = (int)AdjSmem<NX, NY, NZ>::BYTES;
     const unsigned grid = (unsigned)a.n_elem;
     if (a.GB) {
-        /* viscous: the flux transposes, then the gradients' transpose and the
-         * stage combination */
+        /* viscous: pass 1 the flux transposes, pass 2 the gradients'
+         * transpose and the stage combination */
         constexpr int GS = (int)AdjGradSmem<NX, NY, NZ>::BYTES;
-        switch (rs) {
-            case 0: k_mixed_adj<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad<NX, NY, NZ, 0><<<grid, G::BLOCK, GS, st>>>(a); break;
-            case 1: k_mixed_adj<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, GS, st>>>(a); break;
-            case 2: k_mixed_adj<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, GS, st>>>(a); break;
-            default: k_mixed_adj<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                     k_mixed_adj_grad<NX, NY, NZ, 3><<<grid, G::BLOCK, GS, st>>>(a); break;
+        if (passes & 1) {
+            switch (rs) {
+                case 0: k_mixed_adj<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 1: k_mixed_adj<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 2: k_mixed_adj<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                default: k_mixed_adj<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            }
+        }
+        if (passes & 2) {
+            switch (rs) {
+                case 0: k_mixed_adj_grad<NX, NY, NZ, 0><<<grid, G::BLOCK, GS, st>>>(a); break;
+                case 1: k_mixed_adj_grad<NX, NY, NZ, 1><<<grid, G::BLOCK, GS, st>>>(a); break;
+                case 2: k_mixed_adj_grad<NX, NY, NZ, 2><<<grid, G::BLOCK, GS, st>>>(a); break;
+                default: k_mixed_adj_grad<NX, NY, NZ, 3><<<grid, G::BLOCK, GS, st>>>(a); break;
+            }
         }
         return (int)cudaGetLastError();
     }
@@ -591,14 +599,15 @@ int prepare_adj() {
 }
 
 /* ------------------------------------------------------------------------
- * Transposes of the mortar kernels (inviscid runs).  On a face on a 2:1
- * mortar the stage kernel lifts MF = sum over the face node's entries of
- * coef d, with d = F.n at the fine node's slot and dC its projection onto a
- * coarse node (psiCor); F, the Rusanov flux of the slot, is formed from the
- * fine node's 19 face quantities and the coarse face's, interpolated with
- * psiRef (|u|, c, m, rho', the momentum flux tensor, the theta flux, Theta').
- * Per reverse stage, after the transposed stage kernel (whose face terms
- * are zero on mortar faces):
+ * Transposes of the mortar kernels.  On a face on a 2:1 mortar the stage
+ * kernel lifts MF = sum over the face node's entries of coef d, with
+ * d = F.n at the fine node's slot and dC its projection onto a coarse node
+ * (psiCor); F, the Rusanov flux of the slot, is formed from the fine node's
+ * 19 face quantities and the coarse face's, interpolated with psiRef (|u|,
+ * c, m, rho', the momentum flux tensor, the theta flux, Theta'; viscous runs
+ * carry -mu grad U and -(mu/Pr) grad theta in the flux tensors).  Per
+ * reverse stage, after the transposed stage kernel (whose face terms are
+ * zero on mortar faces; in viscous runs after its first pass):
  *   k_mxa_fill_t  per mortar face node: MFbar = -C gbar (C the node's lift
  *                 coefficient), handed to its entries' dbar and dCbar (each
  *                 slot has one fine and one coarse entry);
@@ -612,7 +621,8 @@ int prepare_adj() {
  *                 weighted coarse-side adjoints of the slots interpolating
  *                 from it and applies its own quantity Jacobian; the result
  *                 enters the stage combination like the kernel's xbar
- *                 (atomic adds: an edge node lies on two faces).
+ *                 (atomic adds: an edge node lies on two faces), or in
+ *                 viscous runs the first pass's state and gradient adjoints.
  * ------------------------------------------------------------------------ */
 struct MxaArgs {
     const int32_t* mi;     /* [MX_FIELDS][n_ms] */
@@ -621,11 +631,18 @@ struct MxaArgs {
     const float* psiC;     /* [6][MAXN^2] */
     const int32_t* ent;    /* [n_mf][nfmax][4] */
     const float* acoef;    /* [n_mf][nfmax][4] */
+    const float* gs;       /* [n_mf][nfmax][4] gradient weights */
     const int32_t* node;   /* [n_mf][nfmax] */
+    const int32_t* face;   /* [n_mf] */
     float* db;             /* [5][n_ms] */
     float* dCb;            /* [5][n_ms] */
     float* qb;             /* [19][n_ms] */
     float* xf;             /* [5][n_ms] */
+    float* gf;             /* viscous: [12][n_ms] */
+    float* gFb;            /* viscous: [4][n_ms] */
+    float* gCb;            /* viscous: [4][n_ms] */
+    float* vh;             /* viscous: [4][n_ms] */
+    float* vown;           /* viscous: [4][n_mf nfmax] */
     int64_t n_ms, n_mf;
     int nfmax, np;
 };
@@ -648,8 +665,19 @@ __device__ __forceinline__ Pt mxa_node(const AdjArgs& a, int np, int64_t node, f
     return pointwise(x, b, a.eos, a.gamma, a.gR);
 }
 
-/* the 19 face quantities of a node, in the mortar flux kernel's layout */
-__device__ __forceinline__ void face_q19(const float* x, const Pt& p, float* f) {
+/* the node's gradients (viscous runs) */
+__device__ __forceinline__ void mxa_grad(const AdjArgs& a, int np, int64_t node, float* g) {
+    const int64_t e = node / np;
+    const float* gr = a.Gv + e * 12 * np + (node - e * np);
+#pragma unroll
+    for (int c = 0; c < 12; c++) g[c] = __ldg(gr + c * np);
+}
+
+/* the 19 face quantities of a node, in the mortar flux kernel's layout;
+ * viscous runs carry -mu grad U and -(mu/Pr) grad theta, mu = rho nu */
+template <bool VISC>
+__device__ __forceinline__ void face_q19(const float* x, const Pt& p, const float* g, const AdjArgs& a,
+                                         float* f) {
     f[0] = p.umag;
     f[1] = p.c;
 #pragma unroll
@@ -662,14 +690,24 @@ __device__ __forceinline__ void face_q19(const float* x, const Pt& p, float* f) 
 #pragma unroll
     for (int c = 0; c < 3; c++) f[15 + c] = x[1 + c] * p.th;
     f[18] = x[4];
+    if constexpr (VISC) {
+        const float mu = p.rho * a.nu, mt = p.rho * a.nu_pr;
+#pragma unroll
+        for (int c = 0; c < 9; c++) f[6 + c] = fmaf(-mu, g[c], f[6 + c]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[15 + c] = fmaf(-mt, g[9 + c], f[15 + c]);
+    }
 }
 
 /* xb += (d q19 / dx)^T qb: |u| and c (d|u|/drho' = -|u|/rho, d|u|/dm_k =
  * u_k / (rho |u|), dc/drho' = -c / (2 rho), dc/dTheta' = c / (2 Theta)),
  * rho' and Theta' directly, and per direction c the flux vector
- * (m_c, m_r u_c + p' delta_rc, m_c theta) through the flux Jacobian */
+ * (m_c, m_r u_c + p' delta_rc, m_c theta) through the flux Jacobian;
+ * viscous runs: the density adjoint of mu and the gradient adjoints gb */
+template <bool VISC>
 __device__ __forceinline__ void face_q19_t(const float* x, const float* b, const Pt& p,
-                                           const float* qb, const AdjArgs& a, float* xb) {
+                                           const float* g, const float* qb, const AdjArgs& a,
+                                           float* xb, float* gb) {
     const float Th = __fadd_rn(b[1], x[4]);
     const float iTh = rcp_nr(Th);
     const float ku = p.umag > 0.0f ? p.inv * rcp_nr(p.umag) : 0.0f;
@@ -681,6 +719,41 @@ __device__ __forceinline__ void face_q19_t(const float* x, const float* b, const
     jft<0>(p.u, p.th, pth, qb[2], qb[6 + tidx(0, 0)], qb[6 + tidx(1, 0)], qb[6 + tidx(2, 0)], qb[15], xb);
     jft<1>(p.u, p.th, pth, qb[3], qb[6 + tidx(0, 1)], qb[6 + tidx(1, 1)], qb[6 + tidx(2, 1)], qb[16], xb);
     jft<2>(p.u, p.th, pth, qb[4], qb[6 + tidx(0, 2)], qb[6 + tidx(1, 2)], qb[6 + tidx(2, 2)], qb[17], xb);
+    if constexpr (VISC) {
+        const float mu = p.rho * a.nu, mt = p.rho * a.nu_pr;
+        float sm = 0.0f, st = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 9; c++) {
+            sm = fmaf(g[c], qb[6 + c], sm);
+            gb[c] = -mu * qb[6 + c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            st = fmaf(g[9 + c], qb[15 + c], st);
+            gb[9 + c] = -mt * qb[15 + c];
+        }
+        xb[0] = fmaf(-a.nu, sm, fmaf(-a.nu_pr, st, xb[0]));
+    }
+}
+
+/* a mortar term of the state adjoint into the stage combination (after the
+ * transposed stage kernel): R3, R2 add dt xbar to A and to the stage output,
+ * R1 to lam (FP64), R0 returns xbar; atomic adds, an edge node lies on two
+ * element faces */
+template <int RS>
+__device__ __forceinline__ void add_to_stage(const AdjArgs& a, int64_t o, int np, const float* xb) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        if constexpr (RS == 0) {
+            atomicAdd(a.Bout + o + v * np, xb[v]);
+        } else if constexpr (RS == 1) {
+            atomicAdd(a.lam_out + o + v * np, (double)(a.dt * xb[v]));
+        } else {
+            const float xv = a.dt * xb[v];
+            atomicAdd(a.A + o + v * np, xv);
+            atomicAdd(a.Bout + o + v * np, xv);
+        }
+    }
 }
 
 template <int RS>
@@ -703,16 +776,18 @@ __global__ void __launch_bounds__(128) k_mxa_fill_t(AdjArgs a, MxaArgs m) {
     }
 }
 
-template <bool HAS_DIN>
+template <bool HAS_DIN, bool VISC>
 __global__ void __launch_bounds__(128) k_mxa_flux_t(AdjArgs a, MxaArgs m) {
     const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ms >= m.n_ms) return;
     auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
     /* the forward's face quantities: the fine node's, and the coarse face's
      * interpolated onto the slot */
-    float xf[5], bf[4], f[19], q[19];
-    const Pt pf = mxa_node<HAS_DIN>(a, m.np, fld(MX_FINE), xf, bf);
-    face_q19(xf, pf, f);
+    float xf[5], bf[4], gfn[12], f[19], q[19];
+    const int64_t fnode = fld(MX_FINE);
+    const Pt pf = mxa_node<HAS_DIN>(a, m.np, fnode, xf, bf);
+    if constexpr (VISC) mxa_grad(a, m.np, fnode, gfn);
+    face_q19<VISC>(xf, pf, gfn, a, f);
 #pragma unroll
     for (int c = 0; c < 19; c++) q[c] = 0.0f;
     const int base = fld(MX_BASE), sa = fld(MX_SA), sb = fld(MX_SB), Na = fld(MX_NA),
@@ -723,9 +798,11 @@ __global__ void __launch_bounds__(128) k_mxa_flux_t(AdjArgs a, MxaArgs m) {
         const float* Pb = m.psiR + tb * MAXN * MAXN;
         for (int na = 0; na < Na; na++)
             for (int nb = 0; nb < Nb; nb++) {
-                float x[5], b[4], qn[19];
-                const Pt p = mxa_node<HAS_DIN>(a, m.np, (int64_t)base + na * sa + nb * sb, x, b);
-                face_q19(x, p, qn);
+                float x[5], b[4], g[12], qn[19];
+                const int64_t cn = (int64_t)base + na * sa + nb * sb;
+                const Pt p = mxa_node<HAS_DIN>(a, m.np, cn, x, b);
+                if constexpr (VISC) mxa_grad(a, m.np, cn, g);
+                face_q19<VISC>(x, p, g, a, qn);
                 const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
 #pragma unroll
                 for (int c = 0; c < 19; c++) q[c] = fmaf(w, qn[c], q[c]);
@@ -813,20 +890,32 @@ __global__ void __launch_bounds__(128) k_mxa_flux_t(AdjArgs a, MxaArgs m) {
         fb[c] = fine1 ? Ab[c] : Bb[c];
         m.qb[c * m.n_ms + ms] = fine1 ? Bb[c] : Ab[c];
     }
-    float xb[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    face_q19_t(xf, bf, pf, fb, a, xb);
+    float xb[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, gb[12];
+    face_q19_t<VISC>(xf, bf, pf, gfn, fb, a, xb, gb);
 #pragma unroll
     for (int v = 0; v < 5; v++) m.xf[v * m.n_ms + ms] = xb[v];
+    if constexpr (VISC) {
+#pragma unroll
+        for (int c = 0; c < 12; c++) m.gf[c * m.n_ms + ms] = gb[c];
+    }
 }
 
-template <int RS>
+/* per mortar face node: the fine node takes its slot's adjoints; a coarse
+ * node (node (IA, IB) of the coarse face) sums, per sub-face, the psiRef-
+ * weighted coarse-side adjoints of the slots interpolating from it and
+ * applies its own quantity Jacobian.  Inviscid runs add the result to the
+ * stage combination; viscous runs add it to the first pass's state adjoint
+ * and gradient adjoints, before the gradients' transpose. */
+template <int RS, bool VISC>
 __global__ void __launch_bounds__(128) k_mxa_gather(AdjArgs a, MxaArgs m) {
     constexpr bool HAS_DIN = RS == 3 || RS == 2;
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= m.n_mf * m.nfmax) return;
     const int32_t node = __ldg(m.node + id);
     if (node < 0) return;
-    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, gacc[12];
+#pragma unroll
+    for (int c = 0; c < 12; c++) gacc[c] = 0.0f;
     float qs[19];
 #pragma unroll
     for (int c = 0; c < 19; c++) qs[c] = 0.0f;
@@ -838,10 +927,12 @@ __global__ void __launch_bounds__(128) k_mxa_gather(AdjArgs a, MxaArgs m) {
         if (!(en & MX_COARSE)) {
 #pragma unroll
             for (int v = 0; v < 5; v++) acc[v] += __ldg(m.xf + v * m.n_ms + ms);
+            if constexpr (VISC) {
+#pragma unroll
+                for (int c = 0; c < 12; c++) gacc[c] += __ldg(m.gf + c * m.n_ms + ms);
+            }
             continue;
         }
-        /* the coarse node is node (IA, IB) of the coarse face; the
-         * sub-face's slots interpolate from it with psiRef */
         coarse = true;
         auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
         const int Na = fld(MX_NA), Nb = fld(MX_NB), na = fld(MX_IA), nb = fld(MX_IB),
@@ -857,29 +948,172 @@ __global__ void __launch_bounds__(128) k_mxa_gather(AdjArgs a, MxaArgs m) {
             }
     }
     if (coarse) {
-        float x[5], b[4];
+        float x[5], b[4], g[12], gb[12];
         const Pt p = mxa_node<HAS_DIN>(a, m.np, node, x, b);
-        face_q19_t(x, b, p, qs, a, acc);
-    }
-    /* the stage combination of the kernel's xbar: R3, R2 add dt xbar to A
-     * and to the stage output, R1 to lam (FP64), R0 returns xbar */
-    const int64_t e = node / m.np;
-    const int64_t o = e * 5 * m.np + (node - e * m.np);
+        if constexpr (VISC) mxa_grad(a, m.np, node, g);
+        face_q19_t<VISC>(x, b, p, g, qs, a, acc, gb);
+        if constexpr (VISC) {
 #pragma unroll
-    for (int v = 0; v < 5; v++) {
-        if constexpr (RS == 0) {
-            atomicAdd(a.Bout + o + v * m.np, acc[v]);
-        } else if constexpr (RS == 1) {
-            atomicAdd(a.lam_out + o + v * m.np, (double)(a.dt * acc[v]));
-        } else {
-            const float xv = a.dt * acc[v];
-            atomicAdd(a.A + o + v * m.np, xv);
-            atomicAdd(a.Bout + o + v * m.np, xv);
+            for (int c = 0; c < 12; c++) gacc[c] += gb[c];
         }
+    }
+    const int64_t e = node / m.np;
+    const int l = (int)(node - e * m.np);
+    if constexpr (VISC) {
+        const int64_t o = e * 5 * m.np + l;
+#pragma unroll
+        for (int v = 0; v < 5; v++) atomicAdd(a.XB + o + v * m.np, acc[v]);
+        float* gr = a.GB + e * 12 * m.np + l;
+#pragma unroll
+        for (int c = 0; c < 12; c++) atomicAdd(gr + c * m.np, gacc[c]);
+    } else {
+        add_to_stage<RS>(a, e * 5 * m.np + l, m.np, acc);
     }
 }
 
-int launch_mortar_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
+/* Viscous runs: the transposes of the gradients' mortar face values (after
+ * the gradients' transpose, whose face terms are zero on mortar faces).  The
+ * forward lifts on a mortar face node MF = sum_entries s (cds - V_own), s the
+ * entry's weight (axis-aligned: gs; general geometry: the outward sign times
+ * the slot's weighted normal per row), cds = (V_fine + psiRef-interpolated
+ * V_coarse) / 2 at a slot, projected onto the coarse nodes with psiCor.
+ *   k_mxa_gfill_t  per mortar face node: MFbar from the node's gradient
+ *                  adjoints (the lift coefficient of the face, or 1/cV),
+ *                  handed to the entries' cds adjoints, minus their sum to
+ *                  the node's own V;
+ *   k_mxa_ggather_t per slot: its cds adjoint plus the psiCor-weighted coarse
+ *                  entries of the sub-face, halved;
+ *   k_mxa_gcds_t   per mortar face node: own, fine-slot and psiRef-weighted
+ *                  coarse-slot V adjoints, through V = (m / rho, (Theta' -
+ *                  T0 rho') / rho) into the stage combination. */
+template <bool GEN>
+__global__ void __launch_bounds__(128) k_mxa_gfill_t(AdjArgs a, MxaArgs m) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nid = m.n_mf * m.nfmax;
+    if (id >= nid) return;
+    const int32_t node = __ldg(m.node + id);
+    if (node < 0) return;
+    const int64_t e = node / m.np;
+    const int l = (int)(node - e * m.np);
+    const float* gr = a.GB + e * 12 * m.np + l;
+    constexpr int ND = GEN ? 12 : 4;
+    float D[ND];
+    if constexpr (GEN) {
+        const float icv = __ldg(a.Jg + (e * 10 + 9) * m.np + l);
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            D[4 * r] = icv * gr[tidx(r, 0) * m.np];
+            D[4 * r + 1] = icv * gr[tidx(r, 1) * m.np];
+            D[4 * r + 2] = icv * gr[tidx(r, 2) * m.np];
+            D[4 * r + 3] = icv * gr[(9 + r) * m.np];
+        }
+    } else {
+        const int face = __ldg(m.face + id / m.nfmax), r = face >> 1;
+        const float co = ((face & 1) ? 1.0f : -1.0f) * __ldg(a.J + (int64_t)r * a.n_elem + e) * a.lift[r];
+        D[0] = co * gr[tidx(r, 0) * m.np];
+        D[1] = co * gr[tidx(r, 1) * m.np];
+        D[2] = co * gr[tidx(r, 2) * m.np];
+        D[3] = co * gr[(9 + r) * m.np];
+    }
+    float own[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int q = 0; q < 4; q++) {
+        const int32_t en = __ldg(m.ent + id * 4 + q);
+        if (en < 0) break;
+        const float w = __ldg(m.gs + id * 4 + q);
+        const int64_t ms = en & (MX_COARSE - 1);
+        float sv[4];
+        if constexpr (GEN) {
+            const float n0 = w * __ldg(m.mf + ms), n1 = w * __ldg(m.mf + m.n_ms + ms),
+                        n2 = w * __ldg(m.mf + 2 * m.n_ms + ms);
+#pragma unroll
+            for (int c = 0; c < 4; c++) sv[c] = fmaf(n0, D[c], fmaf(n1, D[4 + c], n2 * D[8 + c]));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; c++) sv[c] = w * D[c];
+        }
+        float* dst = (en & MX_COARSE) ? m.gCb : m.gFb;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            dst[c * m.n_ms + ms] = sv[c];
+            own[c] -= sv[c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.vown[c * nid + id] = own[c];
+}
+
+__global__ void __launch_bounds__(128) k_mxa_ggather_t(MxaArgs m) {
+    const int64_t ms = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ms >= m.n_ms) return;
+    auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+    const int Na = fld(MX_NA), Nb = fld(MX_NB), ia = fld(MX_IA), ib = fld(MX_IB),
+              first = fld(MX_FIRST);
+    const float* Pa = m.psiC + fld(MX_TA) * MAXN * MAXN;
+    const float* Pb = m.psiC + fld(MX_TB) * MAXN * MAXN;
+    float g[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) g[c] = __ldg(m.gFb + c * m.n_ms + ms);
+    for (int ka = 0; ka < Na; ka++)
+        for (int kb = 0; kb < Nb; kb++) {
+            const int64_t k = first + ka * Nb + kb;
+            const float w = __ldg(Pa + ia * Na + ka) * __ldg(Pb + ib * Nb + kb);
+#pragma unroll
+            for (int c = 0; c < 4; c++) g[c] = fmaf(w, __ldg(m.gCb + c * m.n_ms + k), g[c]);
+        }
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.vh[c * m.n_ms + ms] = 0.5f * g[c];
+}
+
+template <int RS>
+__global__ void __launch_bounds__(128) k_mxa_gcds_t(AdjArgs a, MxaArgs m) {
+    constexpr bool HAS_DIN = RS == 3 || RS == 2;
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nid = m.n_mf * m.nfmax;
+    if (id >= nid) return;
+    const int32_t node = __ldg(m.node + id);
+    if (node < 0) return;
+    float vb[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) vb[c] = __ldg(m.vown + c * nid + id);
+    for (int q = 0; q < 4; q++) {
+        const int32_t en = __ldg(m.ent + id * 4 + q);
+        if (en < 0) break;
+        const int64_t ms = en & (MX_COARSE - 1);
+        if (!(en & MX_COARSE)) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) vb[c] += __ldg(m.vh + c * m.n_ms + ms);
+            continue;
+        }
+        auto fld = [&](int f) { return __ldg(m.mi + (int64_t)f * m.n_ms + ms); };
+        const int Na = fld(MX_NA), Nb = fld(MX_NB), na = fld(MX_IA), nb = fld(MX_IB),
+                  first = fld(MX_FIRST);
+        const float* Pa = m.psiR + fld(MX_TA) * MAXN * MAXN;
+        const float* Pb = m.psiR + fld(MX_TB) * MAXN * MAXN;
+        for (int ia = 0; ia < Na; ia++)
+            for (int ib = 0; ib < Nb; ib++) {
+                const int64_t k = first + ia * Nb + ib;
+                const float w = __ldg(Pa + na * Na + ia) * __ldg(Pb + nb * Nb + ib);
+#pragma unroll
+                for (int c = 0; c < 4; c++) vb[c] = fmaf(w, __ldg(m.vh + c * m.n_ms + k), vb[c]);
+            }
+    }
+    /* V = (m / rho, (Theta' - T0 rho') / rho), rho = rho_ref + rho' */
+    float x[5], b[4];
+    mxa_node<HAS_DIN>(a, m.np, node, x, b);
+    const float inv = rcp_nr(__fadd_rn(b[0], x[0]));
+    const float V[4] = {__fmul_rn(x[1], inv), __fmul_rn(x[2], inv), __fmul_rn(x[3], inv),
+                        __fmul_rn(__fmaf_rn(-a.T0, x[0], x[4]), inv)};
+    float xb[5];
+    xb[0] = -inv * (vb[0] * V[0] + vb[1] * V[1] + vb[2] * V[2] + vb[3] * (a.T0 + V[3]));
+    xb[1] = vb[0] * inv;
+    xb[2] = vb[1] * inv;
+    xb[3] = vb[2] * inv;
+    xb[4] = vb[3] * inv;
+    const int64_t e = node / m.np;
+    add_to_stage<RS>(a, e * 5 * m.np + (node - e * m.np), m.np, xb);
+}
+
+MxaArgs mxa_args(const NsemMixedBuf* mb) {
     MxaArgs m{};
     m.mi = mb->mx_i;
     m.mf = mb->mx_f;
@@ -887,45 +1121,98 @@ int launch_mortar_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStre
     m.psiC = mb->mx_psi + 6 * MAXN * MAXN;
     m.ent = mb->mf_ent;
     m.acoef = mb->mf_acoef;
+    m.gs = mb->mf_gs;
     m.node = mb->mf_node;
+    m.face = mb->mf_face;
     m.db = mb->mxa_db;
     m.dCb = mb->mxa_dCb;
     m.qb = mb->mxa_qb;
     m.xf = mb->mxa_xf;
+    m.gf = mb->mxa_gf;
+    m.gFb = mb->mxa_gFb;
+    m.gCb = mb->mxa_gCb;
+    m.vh = mb->mxa_vh;
+    m.vown = mb->mxa_vown;
     m.n_ms = mb->n_ms;
     m.n_mf = mb->n_mf;
     m.nfmax = mb->nfmax;
     m.np = mb->npd[0] * mb->npd[1] * mb->npd[2];
+    return m;
+}
+
+template <int RS>
+void launch_mxa_flux(const MxaArgs& m, const AdjArgs& a, bool visc, cudaStream_t st) {
+    constexpr bool HD = RS == 3 || RS == 2;
     const unsigned gn = (unsigned)((m.n_mf * m.nfmax + 127) / 128);
     const unsigned gs = (unsigned)((m.n_ms + 127) / 128);
-    if (rs == 3) k_mxa_fill_t<3><<<gn, 128, 0, st>>>(a, m);
-    else if (rs == 2) k_mxa_fill_t<2><<<gn, 128, 0, st>>>(a, m);
-    else if (rs == 1) k_mxa_fill_t<1><<<gn, 128, 0, st>>>(a, m);
-    else k_mxa_fill_t<0><<<gn, 128, 0, st>>>(a, m);
-    if (rs == 3 || rs == 2) k_mxa_flux_t<true><<<gs, 128, 0, st>>>(a, m);
-    else k_mxa_flux_t<false><<<gs, 128, 0, st>>>(a, m);
-    if (rs == 3) k_mxa_gather<3><<<gn, 128, 0, st>>>(a, m);
-    else if (rs == 2) k_mxa_gather<2><<<gn, 128, 0, st>>>(a, m);
-    else if (rs == 1) k_mxa_gather<1><<<gn, 128, 0, st>>>(a, m);
-    else k_mxa_gather<0><<<gn, 128, 0, st>>>(a, m);
+    k_mxa_fill_t<RS><<<gn, 128, 0, st>>>(a, m);
+    if (visc) {
+        k_mxa_flux_t<HD, true><<<gs, 128, 0, st>>>(a, m);
+        k_mxa_gather<RS, true><<<gn, 128, 0, st>>>(a, m);
+    } else {
+        k_mxa_flux_t<HD, false><<<gs, 128, 0, st>>>(a, m);
+        k_mxa_gather<RS, false><<<gn, 128, 0, st>>>(a, m);
+    }
+}
+
+template <int RS>
+void launch_mxa_grad(const MxaArgs& m, const AdjArgs& a, bool gen, cudaStream_t st) {
+    const unsigned gn = (unsigned)((m.n_mf * m.nfmax + 127) / 128);
+    const unsigned gs = (unsigned)((m.n_ms + 127) / 128);
+    if (gen) k_mxa_gfill_t<true><<<gn, 128, 0, st>>>(a, m);
+    else k_mxa_gfill_t<false><<<gn, 128, 0, st>>>(a, m);
+    k_mxa_ggather_t<<<gs, 128, 0, st>>>(m);
+    k_mxa_gcds_t<RS><<<gn, 128, 0, st>>>(a, m);
+}
+
+/* part 1: the mortar flux transposes; part 2 (viscous runs): the
+ * transposes of the gradients' mortar face values */
+int launch_mortar_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st, int part) {
+    const MxaArgs m = mxa_args(mb);
+    if (part == 1) {
+        switch (rs) {
+            case 3: launch_mxa_flux<3>(m, a, mb->visc, st); break;
+            case 2: launch_mxa_flux<2>(m, a, mb->visc, st); break;
+            case 1: launch_mxa_flux<1>(m, a, mb->visc, st); break;
+            default: launch_mxa_flux<0>(m, a, mb->visc, st); break;
+        }
+    } else {
+        switch (rs) {
+            case 3: launch_mxa_grad<3>(m, a, mb->gen, st); break;
+            case 2: launch_mxa_grad<2>(m, a, mb->gen, st); break;
+            case 1: launch_mxa_grad<1>(m, a, mb->gen, st); break;
+            default: launch_mxa_grad<0>(m, a, mb->gen, st); break;
+        }
+    }
     return (int)cudaGetLastError();
 }
 
-int dispatch_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
+/* the transposed stage kernels: passes as launch_adj_general */
+int launch_stage_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st, int passes) {
     const int nx = mb->npd[0], ny = mb->npd[1], nz = mb->npd[2];
-    /* mortar transposes are built for inviscid runs */
-    if (mb->visc && mb->n_ms > 0) return (int)cudaErrorNotSupported;
-    int e = (int)cudaErrorNotSupported;
-    if (mb->gen) {
-        e = launch_adj_general(nx, ny, nz, a, rs, st);
-    } else {
+    if (mb->gen) return launch_adj_general(nx, ny, nz, a, rs, st, passes);
 #define NSEM_ADJ(A, B, C) \
-        if (nx == A && ny == B && nz == C) e = launch_adj<A, B, C>(a, rs, st);
-        NSEM_MIXED_DIMS(NSEM_ADJ)
+    if (nx == A && ny == B && nz == C) return launch_adj<A, B, C>(a, rs, st, passes);
+    NSEM_MIXED_DIMS(NSEM_ADJ)
 #undef NSEM_ADJ
+    return (int)cudaErrorNotSupported;
+}
+
+int dispatch_adj(const NsemMixedBuf* mb, const AdjArgs& a, int rs, cudaStream_t st) {
+    if (mb->n_ms == 0) return launch_stage_adj(mb, a, rs, st, 3);
+    int e;
+    if (!mb->visc) {
+        /* the stage kernel, then the mortar transposes into its combination */
+        if ((e = launch_stage_adj(mb, a, rs, st, 3))) return e;
+        return launch_mortar_adj(mb, a, rs, st, 1);
     }
-    if (e == 0 && mb->n_ms > 0) e = launch_mortar_adj(mb, a, rs, st);
-    return e;
+    /* viscous: the flux transposes (stage kernel, then mortar), the
+     * gradients' transpose with the combination, then the mortar terms of
+     * the gradients */
+    if ((e = launch_stage_adj(mb, a, rs, st, 1))) return e;
+    if ((e = launch_mortar_adj(mb, a, rs, st, 1))) return e;
+    if ((e = launch_stage_adj(mb, a, rs, st, 2))) return e;
+    return launch_mortar_adj(mb, a, rs, st, 2);
 }
 
 AdjArgs adj_args(const NsemDev* dev, const NsemMixedBuf* mb, double dt) {
@@ -1113,6 +1400,14 @@ int nsem_mixed_adj_alloc(NsemMixedBuf* mb) {
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_dCb, (size_t)5 * mb->n_ms * sizeof(float));
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_qb, (size_t)19 * mb->n_ms * sizeof(float));
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_xf, (size_t)5 * mb->n_ms * sizeof(float));
+        if (ce == cudaSuccess && mb->visc) {
+            const size_t nid = (size_t)mb->n_mf * mb->nfmax;
+            ce = cudaMalloc((void**)&mb->mxa_gf, (size_t)12 * mb->n_ms * sizeof(float));
+            if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_gFb, (size_t)4 * mb->n_ms * sizeof(float));
+            if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_gCb, (size_t)4 * mb->n_ms * sizeof(float));
+            if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_vh, (size_t)4 * mb->n_ms * sizeof(float));
+            if (ce == cudaSuccess) ce = cudaMalloc((void**)&mb->mxa_vown, 4 * nid * sizeof(float));
+        }
     }
     if (ce != cudaSuccess) return (int)ce;
     return nsem_mixed_adj_prepare(mb);

@@ -192,8 +192,10 @@ __device__ __forceinline__ void grad_transform_t(float* R, const AdjArgs& a, int
 }
 
 /* general-geometry kernels (nsem_mixed_adj_gen.cu), dispatched on the node
- * counts per direction */
-int launch_adj_general(int nx, int ny, int nz, const AdjArgs& a, int rs, cudaStream_t st);
+ * counts per direction; passes (viscous runs): bit 0 the flux transposes,
+ * bit 1 the gradients' transpose with the stage combination */
+int launch_adj_general(int nx, int ny, int nz, const AdjArgs& a, int rs, cudaStream_t st,
+                       int passes);
 int prepare_adj_general(int nx, int ny, int nz);
 
 }  // namespace nsem_mxa

@@ -360,8 +360,10 @@ k_mixed_adj_grad_gen(AdjArgs a) {
     if (t < NFS) {
         fs = face_slot<NX, NY, NZ>(t);
         nb = __ldg(a.nbr + (int64_t)fs.face * a.n_elem + e);
+        /* a face on a 2:1 mortar: a zero normal zeroes the face terms here;
+         * the mortar gradient transposes take them */
 #pragma unroll
-        for (int c = 0; c < 3; c++) fno[c] = __ldg(a.Fn + (e * 3 + c) * NFS + t);
+        for (int c = 0; c < 3; c++) fno[c] = nb <= -2 ? 0.0f : __ldg(a.Fn + (e * 3 + c) * NFS + t);
         /* sum_r fN[r] Gbar_r / cV at the own node and, with -fN, at the
          * neighbour's */
         auto dotn = [&](const float* gr, float ic, float sgn) {
@@ -515,21 +517,29 @@ k_mixed_adj_grad_gen(AdjArgs a) {
 }
 
 template <int NX, int NY, int NZ>
-int launch_adj_gen(const AdjArgs& a, int rs, cudaStream_t st) {
+int launch_adj_gen(const AdjArgs& a, int rs, cudaStream_t st, int passes) {
     using G = Geo<NX, NY, NZ>;
     constexpr int SMEM = (int)AdjGenSmem<NX, NY, NZ>::BYTES;
     constexpr int GS = (int)AdjGradSmem<NX, NY, NZ>::BYTES;
     const unsigned grid = (unsigned)a.n_elem;
     if (a.GB) {
-        switch (rs) {
-            case 0: k_mixed_adj_gen<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad_gen<NX, NY, NZ, 0><<<grid, G::BLOCK, GS, st>>>(a); break;
-            case 1: k_mixed_adj_gen<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad_gen<NX, NY, NZ, 1><<<grid, G::BLOCK, GS, st>>>(a); break;
-            case 2: k_mixed_adj_gen<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                    k_mixed_adj_grad_gen<NX, NY, NZ, 2><<<grid, G::BLOCK, GS, st>>>(a); break;
-            default: k_mixed_adj_gen<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a);
-                     k_mixed_adj_grad_gen<NX, NY, NZ, 3><<<grid, G::BLOCK, GS, st>>>(a); break;
+        /* viscous: pass 1 the flux transposes, pass 2 the gradients'
+         * transpose and the stage combination */
+        if (passes & 1) {
+            switch (rs) {
+                case 0: k_mixed_adj_gen<NX, NY, NZ, 0, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 1: k_mixed_adj_gen<NX, NY, NZ, 1, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                case 2: k_mixed_adj_gen<NX, NY, NZ, 2, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+                default: k_mixed_adj_gen<NX, NY, NZ, 3, true><<<grid, G::BLOCK, SMEM, st>>>(a); break;
+            }
+        }
+        if (passes & 2) {
+            switch (rs) {
+                case 0: k_mixed_adj_grad_gen<NX, NY, NZ, 0><<<grid, G::BLOCK, GS, st>>>(a); break;
+                case 1: k_mixed_adj_grad_gen<NX, NY, NZ, 1><<<grid, G::BLOCK, GS, st>>>(a); break;
+                case 2: k_mixed_adj_grad_gen<NX, NY, NZ, 2><<<grid, G::BLOCK, GS, st>>>(a); break;
+                default: k_mixed_adj_grad_gen<NX, NY, NZ, 3><<<grid, G::BLOCK, GS, st>>>(a); break;
+            }
         }
         return (int)cudaGetLastError();
     }
@@ -571,8 +581,8 @@ int prepare_adj_gen() {
 
 namespace nsem_mxa {
 
-int launch_adj_general(int nx, int ny, int nz, const AdjArgs& a, int rs, cudaStream_t st) {
-#define NSEM_ADJG(A, B, C) if (nx == A && ny == B && nz == C) return launch_adj_gen<A, B, C>(a, rs, st);
+int launch_adj_general(int nx, int ny, int nz, const AdjArgs& a, int rs, cudaStream_t st, int passes) {
+#define NSEM_ADJG(A, B, C) if (nx == A && ny == B && nz == C) return launch_adj_gen<A, B, C>(a, rs, st, passes);
     NSEM_MIXED_DIMS(NSEM_ADJG)
 #undef NSEM_ADJG
     return (int)cudaErrorNotSupported;

@@ -19,14 +19,14 @@ mortars):
   * 40 SSP-RK3 steps from the fixture's state: relative L2 per conserved
     variable and in theta' <= 1e-5, mass drift <= 1e-12 relative;
   * each mesh inviscid and with viscosity 1.5 (the 2D fixture's value);
-  * the precision form's adjoint (inviscid): the transposed stage with the
-    transposes of the mortar kernels, <w, J du> from the plain FP64 tangent
-    (tests/test_amr_tangent.py checks it against central differences and its
-    own adjoint) against <J32^T w, du> to 1e-5 of sum |w . J du|; the gradient
-    of 1/2 sum_box theta'^2 after 20 steps (checkpoints every 5) from the
+  * the precision form's adjoint, inviscid and viscous: the transposed stage
+    with the transposes of the mortar kernels (and of the gradients' mortar
+    face values), <w, J du> from the plain FP64 tangent (tests/test_amr_tangent.py
+    checks it against central differences and its own adjoint) against
+    <J32^T w, du> to 1e-5 of sum |w . J du|; the gradient of
+    1/2 sum_box theta'^2 after 20 steps (checkpoints every 5) from the
     precision-form forward and reverse sweep against the FP64 adjoint's,
-    relative L2 <= 1e-5; with the viscosity it refuses the refined mesh
-    (UNSUPPORTED).
+    relative L2 <= 1e-5.
 """
 import json
 
@@ -111,10 +111,11 @@ def dot(a, b):
     return float(sum(np.dot(x, y) for x, y in zip(a, b)))
 
 
+@pytest.mark.parametrize("visc", VISC)
 @pytest.mark.parametrize("case", CASES)
-def test_mortar_vjp_transpose(case):
+def test_mortar_vjp_transpose(case, visc):
     import nebulasem_gb300 as ng
-    s, u0, g = solver(case)
+    s, u0, g = solver(case, visc)
     s.set_state(u0)
     s.step(5, prec=ng.FP64)
     u = s.get_state()
@@ -131,15 +132,16 @@ def test_mortar_vjp_transpose(case):
         gv = s.vjp(w, prec=ng.MIXED)
         lhs, rhs = dot(w, Ld), dot(gv, du)
         scale = sum(np.abs(x * y).sum() for x, y in zip(w, Ld))
-        assert abs(lhs - rhs) <= TOL * scale, (case, trial, lhs, rhs, scale)
+        assert abs(lhs - rhs) <= TOL * scale, (case, visc, trial, lhs, rhs, scale)
     s.close()
 
 
+@pytest.mark.parametrize("visc", VISC)
 @pytest.mark.parametrize("case", CASES)
-def test_mortar_adjoint_gradient(case):
+def test_mortar_adjoint_gradient(case, visc):
     import nebulasem_gb300 as ng
     from nebulasem_gb300 import objective as ob
-    s, u_fix, g = solver(case)
+    s, u_fix, g = solver(case, visc)
     n = len(u_fix[0])
     xyz = np.asarray(g["cC"]).reshape(-1, 3)[:n]
     p_ref = np.asarray(g["p_ref"])[:n]
@@ -163,18 +165,6 @@ def test_mortar_adjoint_gradient(case):
     assert out["fp64_J"] > 0
     err_th = rel_l2(out["mixed_th"], out["fp64_th"])
     err_all = rel_l2(np.concatenate(out["mixed"]), np.concatenate(out["fp64"]))
-    print(case, "dJ/dtheta'", err_th, "dJ/du", err_all)
-    assert err_th <= TOL, (case, err_th)
-    assert err_all <= TOL, (case, err_all)
-
-
-def test_mortar_adjoint_viscous_refused():
-    import nebulasem_gb300 as ng
-    s, u0, g = solver("amr_g3_4n3", 1.5)
-    s.set_state(u0)
-    with pytest.raises(ng.NsemError) as e:
-        s.vjp([np.zeros(len(u0[0]))] * 5, prec=ng.MIXED)
-    assert e.value.status == 5 and "non-conforming" in str(e.value)
-    with pytest.raises(ng.NsemError):
-        s.forward_checkpointed(4, 2, prec=ng.MIXED)
-    s.close()
+    print(case, visc, "dJ/dtheta'", err_th, "dJ/du", err_all)
+    assert err_th <= TOL, (case, visc, err_th)
+    assert err_all <= TOL, (case, visc, err_all)
