@@ -80,22 +80,23 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-/* registers sized for 8 resident CTAs per SM in stages 1-2 and 7 in the stage
- * that also carries the FP64 state (measured best on GB300); viscous runs 6,
- * and 5 in stage 3 (its gradients and FP64 state spill at 6: 335 against
- * 365 us at 32^3) */
+/* registers sized for 8 resident CTAs per SM in stages 1-2 and 9 in stage 3,
+ * which loads the FP64 state only at the update (measured best on GB300:
+ * 152 us at 32^3, against 172 us with the state held in registers at 7 CTAs
+ * and 163 us at 8); viscous runs 6, and 5 in stage 3 (its gradients spill at
+ * 6) */
 #ifndef NSEM_MIXED_MB12
 #define NSEM_MIXED_MB12 8
 #endif
 #ifndef NSEM_MIXED_MB3
-#define NSEM_MIXED_MB3 7
+#define NSEM_MIXED_MB3 9
 #endif
 template <int NX, int NY, int NZ, int STAGE, bool VISC, bool PERSIST = false>
 constexpr int stage_min_blocks() {
     /* order 7 (512 threads, 64 KB of shared memory): three CTAs, two for the
      * stages that hold more live values (no spills) */
     if (Geo<NX, NY, NZ>::BLOCK >= 512)
-        return min_blocks((VISC || STAGE == 3 || STAGE == 0) ? 2 : 3, Geo<NX, NY, NZ>::BLOCK,
+        return min_blocks((VISC || STAGE == 0) ? 2 : 3, Geo<NX, NY, NZ>::BLOCK,
                           StageSmem<NX, NY, NZ>::BYTES);
     return min_blocks(VISC ? (STAGE == 3 ? 5 : 6) : (STAGE == 1 || STAGE == 2) ? NSEM_MIXED_MB12 : NSEM_MIXED_MB3,
                       Geo<NX, NY, NZ>::BLOCK,
@@ -373,7 +374,6 @@ k_mixed_stage(StageArgs a) {
 
     /* issue every global load first: own node, face neighbour, stage-3 FP64 */
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0};
-    double u64[5];
     float gown[12];
     if (t < NP) {
         if constexpr (PERSIST) {
@@ -408,9 +408,12 @@ k_mixed_stage(StageArgs a) {
             for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
         }
         if constexpr (STAGE == 3) {
+            /* u'^n is needed only at the update: fetched into L2 here, loaded
+             * there (with the increment reloaded from L1/L2), so that neither
+             * holds registers through the element and nine CTAs fit per SM */
             const double* u = a.U + e * 5 * NP + t;
 #pragma unroll
-            for (int v = 0; v < 5; v++) u64[v] = __ldg(u + v * NP);
+            for (int v = 0; v < 5; v++) asm volatile("prefetch.global.L2 [%0];" ::"l"(u + v * NP));
         }
         if constexpr (VISC) {
             const float* gr = a.G + e * 12 * NP + t;
@@ -628,8 +631,8 @@ k_mixed_stage(StageArgs a) {
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], din[v]);
-            const double un = u64[v] + f2d(D);
+            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], __ldg(a.Din + o + v * NP));
+            const double un = __ldg(a.U + o + v * NP) + f2d(D);
             a.Unew[o + v * NP] = un;
             a.Snew[o + v * NP] = d2f_rn(un);
             /* exponent field all ones = inf or nan (integer test, no FP64 op) */
