@@ -374,6 +374,7 @@ k_mixed_stage(StageArgs a) {
 
     /* issue every global load first: own node, face neighbour, stage-3 FP64 */
     float own[5], din[5] = {0, 0, 0, 0, 0}, bgs[4] = {0, 0, 0, 0};
+    double u64[5];
     float gown[12];
     if (t < NP) {
         if constexpr (PERSIST) {
@@ -408,12 +409,18 @@ k_mixed_stage(StageArgs a) {
             for (int c = 0; c < 4; c++) bgs[c] = __ldg(bg + c * NP);
         }
         if constexpr (STAGE == 3) {
-            /* u'^n is needed only at the update: fetched into L2 here, loaded
-             * there (with the increment reloaded from L1/L2), so that neither
-             * holds registers through the element and nine CTAs fit per SM */
+            /* u'^n is needed only at the update: inviscid runs fetch it into L2
+             * here and load it there (with the increment reloaded from L1/L2),
+             * so that neither holds registers through the element and nine
+             * CTAs fit per SM; viscous runs (five CTAs either way) hold it */
             const double* u = a.U + e * 5 * NP + t;
+            if constexpr (VISC) {
 #pragma unroll
-            for (int v = 0; v < 5; v++) asm volatile("prefetch.global.L2 [%0];" ::"l"(u + v * NP));
+                for (int v = 0; v < 5; v++) u64[v] = __ldg(u + v * NP);
+            } else {
+#pragma unroll
+                for (int v = 0; v < 5; v++) asm volatile("prefetch.global.L2 [%0];" ::"l"(u + v * NP));
+            }
         }
         if constexpr (VISC) {
             const float* gr = a.G + e * 12 * NP + t;
@@ -631,8 +638,8 @@ k_mixed_stage(StageArgs a) {
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], __ldg(a.Din + o + v * NP));
-            const double un = __ldg(a.U + o + v * NP) + f2d(D);
+            const float D = (2.0f / 3.0f) * fmaf(dt, Lv[v], VISC ? din[v] : __ldg(a.Din + o + v * NP));
+            const double un = (VISC ? u64[v] : __ldg(a.U + o + v * NP)) + f2d(D);
             a.Unew[o + v * NP] = un;
             a.Snew[o + v * NP] = d2f_rn(un);
             /* exponent field all ones = inf or nan (integer test, no FP64 op) */
